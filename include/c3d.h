@@ -1,0 +1,151 @@
+/*
+ * c3d.h -- C-ABI of the GB300 (sm_103a) time step for compact3d's
+ * incompressible turbulent channel flow.
+ *
+ * The Fortran driver of compact3d (PROGRAM MAIN, compact3d.f:11-189) keeps
+ * its time loop, PARAM.H / COMMON1.FI parameters and wall-model switches.
+ * It replaces the body of GETUP (compact3d.f:879-960) and the per-step
+ * diagnostics DIVCHECK / CFL / CHKMF / WALLSS with calls into this library
+ * through ISO_C_BINDING.  Every argument is a plain pointer, integer or
+ * double; there are no C++ or PyTorch types in any signature.
+ *
+ * Array layouts on the host side are exactly the Fortran ones of the driver
+ * (column-major, first index fastest, M1=N1, M2=N2, M3=N3):
+ *   U(0:M1,0:M2,0:M3,3), HH(0:M1,0:M2,0:M3,3), SGSVIS(0:M1,0:M2,0:M3),
+ *   P(M1,M2,M3), TAUW(0:M1,0:M3,2), TAUB(0:M1,0:M3,2).
+ * On the device the state is kept resident between steps in the library's
+ * own plane-major layout; c3d_upload / c3d_download convert.
+ *
+ * Return convention: 0 on success, a negative C3D_E* code on failure.  The
+ * library never calls exit() or abort(); c3d_error_string() describes a code
+ * and c3d_last_error() gives the message of the most recent failure on the
+ * calling thread.  A channel handle is used from one host thread at a time.
+ */
+#ifndef C3D_H
+#define C3D_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ------------------------------------------------------ */
+#define C3D_OK            0
+#define C3D_EINVAL      (-1)   /* bad extents, null pointer, unsupported size */
+#define C3D_ECUDA       (-2)   /* a CUDA runtime call failed                    */
+#define C3D_ENOMEM      (-3)   /* device or pinned-host allocation failed       */
+#define C3D_ENOTCONV    (-4)   /* a device iteration cap was hit (wall model)   */
+#define C3D_ENONFINITE  (-5)   /* NaN/Inf found by the diagnostics              */
+#define C3D_ESTATE      (-6)   /* call made in the wrong state                  */
+#define C3D_ENODEV      (-7)   /* no usable CUDA device                         */
+
+/* ---- precision forms -------------------------------------------------- */
+#define C3D_FP64   0   /* every operation in FP64                              */
+#define C3D_MIXED  1   /* FP32 line solves / RHS / FFT; FP64 state, reductions,
+                          low-wavenumber Poisson modes and bulk-flow constraint */
+
+/*
+ * Grid and model description.  It carries the values the reference keeps in
+ * COMMON blocks after SETUP/MESH (compact3d.f:192-443):
+ *   /DIM/   N1,N2,N3                       -> n1,n2,n3 (points; cells = n-1)
+ *   /SIZE/  ALX,ALY,ALZ,VOL                -> alx,aly,alz,vol
+ *   /MESH1/ DX1,DX3 (= N1M/ALX, N3M/ALZ)   -> dx1,dx3
+ *   /MESH2/ Y(0:N2)                        -> y     (n2+1 values)
+ *   /MESH3/ DY(0:N2),H,HM,HC,HP(1:N2)      -> dy    (n2+1 values, DY(0)=DY(N2)=0)
+ *                                             h,hm,hc,hp (n2 values, index J-1)
+ *   /MESH4/ DYM,DYC,DYP(1:N2)              -> dym,dyc,dyp (n2 values, index J-1)
+ *   /PARA/  RE                             -> re
+ *   /FINOUT/ FILES (SGS model)             -> files  (0 none, 1 SGSDY, 2 SGSCS)
+ *   /WALLMODEL/ WMODEL                     -> wmodel (0 none, 1 WALLMODEL_INSTANT)
+ * The library takes the driver's metric arrays as given; it recomputes only
+ * the Poisson metrics of INIWAVE / METRICPOISSON (compact3d.f:9182-9263),
+ * which depend on nothing else.
+ */
+typedef struct c3d_grid {
+    int n1, n2, n3;
+    double alx, aly, alz, vol;
+    double dx1, dx3;
+    double re;
+    const double *y;
+    const double *dy;
+    const double *h, *hm, *hc, *hp;
+    const double *dym, *dyc, *dyp;
+    int files;
+    int wmodel;
+    int precision;      /* C3D_FP64 or C3D_MIXED */
+} c3d_grid;
+
+/* Diagnostics of one step (DIVCHECK, CFL, CHKMF, WALLSS; compact3d.f:9049-9169,
+ * 9463-9503, 11077-11143).  Reductions are accumulated in FP64 in every form. */
+typedef struct c3d_diag {
+    double divmax;      /* DIVCHECK: max |div u|                              */
+    double cflm;        /* CFL: max local CFL number / DT                    */
+    double flow1;       /* CHKMF: flow rate through plane i=1 (per unit z)   */
+    double flow3;       /* CHKMF: flow rate through plane k=1                */
+    double wsm[3];      /* WALLSS: plane-mean wall shear / RE / ALY          */
+    int    nonfinite;   /* 1 if any NaN/Inf was met in the reductions        */
+} c3d_diag;
+
+typedef struct c3d_channel c3d_channel;   /* one channel, device-resident   */
+typedef struct c3d_batch   c3d_batch;     /* many channels, one launch      */
+
+/* ---- library ---------------------------------------------------------- */
+const char *c3d_error_string(int code);
+const char *c3d_last_error(void);
+int c3d_version(void);
+/* Selects the CUDA device used by channels created afterwards on this thread. */
+int c3d_set_device(int device);
+
+/* ---- one channel -------------------------------------------------------
+ * c3d_create    replaces SETUP's INIWAVE/METRICPOISSON and allocates the
+ *               device state (compact3d.f:192-299, 9182-9263).
+ * c3d_upload    copies U, P, HH (and SGSVIS, may be NULL) from Fortran arrays
+ *               to the device; PRESG/PRESG3 are passed to c3d_step.
+ * c3d_download  copies them back (any pointer may be NULL to skip it).
+ * c3d_step      one call of GETUP(U,P,HH,SS,NTIME,PRESG,PRESG3,SGSVIS)
+ *               (compact3d.f:879-960): BCOND, RHS1-3 with AB2, GETUH1-3
+ *               (Crank-Nicolson ADI), RHSDP, GETDP (FFT Poisson), UPCALC.
+ *               dt is COMMON /TSTEP/ DT; presg/presg3 are in-out.
+ * c3d_diagnose  DIVCHECK + CFL + CHKMF + WALLSS on the current device state.
+ * c3d_getup     drop-in for a driver that keeps the fields on the host:
+ *               upload, step, download in one call.
+ */
+int c3d_create(const c3d_grid *grid, c3d_channel **out);
+int c3d_destroy(c3d_channel *ch);
+int c3d_upload(c3d_channel *ch, const double *u, const double *p,
+               const double *hh, const double *sgsvis);
+int c3d_download(c3d_channel *ch, double *u, double *p, double *hh,
+                 double *sgsvis);
+int c3d_upload_wall(c3d_channel *ch, const double *tauw, const double *taub);
+int c3d_download_wall(c3d_channel *ch, double *tauw, double *taub);
+int c3d_step(c3d_channel *ch, int ntime, double dt,
+             double *presg, double *presg3);
+int c3d_diagnose(c3d_channel *ch, c3d_diag *out);
+int c3d_getup(c3d_channel *ch, double *u, double *p, double *hh,
+              double *sgsvis, int ntime, double dt,
+              double *presg, double *presg3);
+/* Pressure projection of the current velocity (RHSDP + GETDP + UPCALC with
+ * U taken as the intermediate velocity and DT = 1, no bulk-flow forcing).
+ * Used to make a synthetic initial condition discretely divergence-free. */
+int c3d_project(c3d_channel *ch);
+/* Blocks until all work queued on the channel's stream has finished. */
+int c3d_sync(c3d_channel *ch);
+/* Device time of the last c3d_step in milliseconds (CUDA events on the
+ * channel's stream), and the number of kernels that step launched. */
+int c3d_last_step_stats(c3d_channel *ch, double *ms, int *kernel_launches);
+
+/* ---- batched ensemble --------------------------------------------------
+ * Many independent channels (any mix of grid sizes, RE and precision) that
+ * advance together.  c3d_batch_step launches every channel's step work on one
+ * stream; after the first call the whole step is replayed as one CUDA graph.
+ */
+int c3d_batch_create(int nchan, const c3d_grid *grids, c3d_batch **out);
+int c3d_batch_destroy(c3d_batch *b);
+int c3d_batch_channel(c3d_batch *b, int index, c3d_channel **ch);
+int c3d_batch_step(c3d_batch *b, int ntime, const double *dt,
+                   double *presg, double *presg3);
+int c3d_batch_sync(c3d_batch *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* C3D_H */

@@ -1,0 +1,188 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes wrapper of the FP64 CPU oracle (c3d_oracle.cpp).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use this
+module, as the checker; the product path never imports it.  Parity of the oracle is
+unpinned (the reference ships no golden vectors and cannot be built here); it is checked
+against known answers in tests/test_oracle.py.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "build")
+LIB = os.path.join(BUILD, "libc3d_oracle.so")
+SRC = os.path.join(HERE, "c3d_oracle.cpp")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with g++ (-O3 -fopenmp -ffp-contract=off)."""
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        cmd = ["g++", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17",
+               "-o", LIB + ".tmp", SRC]
+        subprocess.check_call(cmd)
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        vp, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [vp]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_set_threads.argtypes = [ip]
+        L.orc_max_threads.restype = ip
+        L.orc_getup.restype = ip
+        L.orc_getup.argtypes = [vp, dp, dp, dp, dp, ip, ctypes.c_double, dp, dp]
+        L.orc_project.argtypes = [vp, dp]
+        L.orc_bcond.argtypes = [vp, dp]
+        L.orc_getdp.argtypes = [vp, dp, dp]
+        L.orc_rhsdp.argtypes = [vp, dp, ctypes.c_double, dp]
+        L.orc_divcheck.restype = ctypes.c_double
+        L.orc_divcheck.argtypes = [vp, dp]
+        L.orc_cfl.restype = ctypes.c_double
+        L.orc_cfl.argtypes = [vp, dp]
+        L.orc_chkmf.argtypes = [vp, dp, dp, dp]
+        L.orc_wallss.argtypes = [vp, dp, dp]
+        L.orc_set_wall.argtypes = [vp, dp, dp, ip]
+        for f in ("orc_ctdma11", "orc_ctdma_recip"):
+            getattr(L, f).argtypes = [ip, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp, dp]
+        L.orc_tdmap.argtypes = [ip, dp, dp, dp, dp, dp]
+        L.orc_fft.argtypes = [ip, dp, ip]
+        L.orc_dft2d.argtypes = [ip, ip, dp, ip]
+        L.orc_poisson_metrics.argtypes = [vp, dp, dp, dp, dp, dp]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and (a.flags.f_contiguous or a.ndim == 1), "Fortran float64 array"
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Oracle:
+    """One channel in the CPU oracle; arrays are Fortran-layout numpy float64."""
+
+    def __init__(self, grid, threads: int | None = None):
+        self.grid = grid
+        self._gs = grid.struct()
+        self.h = lib().orc_create(ctypes.byref(self._gs))
+        if not self.h:
+            raise ValueError("oracle rejected the grid")
+        if threads:
+            lib().orc_set_threads(threads)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def getup(self, U, P, HH, ntime, dt, presg, presg3, sgsvis=None):
+        a = (ctypes.c_double * 1)(presg)
+        b = (ctypes.c_double * 1)(presg3)
+        rc = lib().orc_getup(self.h, _p(U), _p(P), _p(HH), _p(sgsvis), ntime, dt, a, b)
+        if rc != 0:
+            raise RuntimeError(f"orc_getup failed: {rc}")
+        return a[0], b[0]
+
+    def project(self, U):
+        lib().orc_project(self.h, _p(U))
+
+    def bcond(self, U):
+        lib().orc_bcond(self.h, _p(U))
+
+    def getdp(self, RDP):
+        DP = np.zeros_like(RDP, order="F")
+        lib().orc_getdp(self.h, _p(RDP), _p(DP))
+        return DP
+
+    def rhsdp(self, UH, dt):
+        RDP = self.grid.zeros_p()
+        lib().orc_rhsdp(self.h, _p(UH), dt, _p(RDP))
+        return RDP
+
+    def divcheck(self, U):
+        return lib().orc_divcheck(self.h, _p(U))
+
+    def cfl(self, U):
+        return lib().orc_cfl(self.h, _p(U))
+
+    def chkmf(self, U):
+        f1 = (ctypes.c_double * 1)()
+        f3 = (ctypes.c_double * 1)()
+        lib().orc_chkmf(self.h, _p(U), f1, f3)
+        return f1[0], f3[0]
+
+    def wallss(self, U):
+        w = (ctypes.c_double * 3)()
+        lib().orc_wallss(self.h, _p(U), w)
+        return np.array(w[:])
+
+    def diagnose(self, U):
+        f1, f3 = self.chkmf(U)
+        return dict(divmax=self.divcheck(U), cflm=self.cfl(U), flow1=f1, flow3=f3,
+                    wsm=self.wallss(U))
+
+    def poisson_metrics(self):
+        g = self.grid
+        ak1 = np.zeros(g.n1m)
+        ak3 = np.zeros(g.n3m // 2 + 1)
+        pm, pc, pp = (np.zeros(g.n2m) for _ in range(3))
+        lib().orc_poisson_metrics(self.h, _p(ak1), _p(ak3), _p(pm), _p(pc), _p(pp))
+        return ak1, ak3, pm, pc, pp
+
+
+def ctdma11(d, a, b, c):
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    x = np.zeros_like(d)
+    lib().orc_ctdma11(len(d), a, b, c, _p(d), _p(x))
+    return x
+
+
+def ctdma_recip(d, a, b, c):
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    x = np.zeros_like(d)
+    lib().orc_ctdma_recip(len(d), a, b, c, _p(d), _p(x))
+    return x
+
+
+def tdmap(a, b, c, r):
+    a, b, c, r = (np.ascontiguousarray(v, dtype=np.float64) for v in (a, b, c, r))
+    x = np.zeros_like(r)
+    lib().orc_tdmap(len(r), _p(a), _p(b), _p(c), _p(r), _p(x))
+    return x
+
+
+def fft(z, sign=-1):
+    z = np.ascontiguousarray(z, dtype=np.complex128).copy()
+    lib().orc_fft(len(z), z.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), sign)
+    return z
+
+
+def dft2d(z, sign=-1):
+    """z: Fortran-order complex array (n1, n3)."""
+    z = np.asfortranarray(z, dtype=np.complex128).copy(order="F")
+    n1, n3 = z.shape
+    lib().orc_dft2d(n1, n3, z.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), sign)
+    return z
+
+
+def set_threads(n: int):
+    lib().orc_set_threads(n)
+
+
+def max_threads() -> int:
+    return lib().orc_max_threads()

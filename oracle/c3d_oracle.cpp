@@ -1,0 +1,1469 @@
+// c3d_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// FP64 CPU restatement of compact3d's channel-flow time step (RuifengHu/compact3d,
+// file compact3d.f; citations are compact3d.f:line).  It is the parity checker for
+// the CUDA library and the timed CPU baseline of bench.py.  Nothing in the product
+// path links or calls it.
+//
+// Parity status: UNPINNED.  The reference ships no tests, fixtures or golden vectors,
+// and it cannot be built in this environment (it is Fortran 77 with FFTW and no
+// Fortran compiler or FFTW is installed).  This restatement is therefore checked
+// against known answers (modified wavenumbers of the compact operators, dense solves,
+// numpy.fft, Poisson round trips, divergence after projection, laminar steady state).
+//
+// Conventions kept from the reference:
+//   * loop order, operation order and parenthesisation of every arithmetic expression
+//     follow the Fortran source (compile with -ffp-contract=off so no FMA is formed);
+//   * FP64 everywhere (the reference is assumed built with 8-byte default REAL);
+//   * arrays use the Fortran layouts U(0:M1,0:M2,0:M3,3), P(M1,M2,M3) with M1=N1,
+//     M2=N2, M3=N3, column-major;
+//   * OpenMP parallel loops where the reference has !$omp directives;
+//   * global sums are taken per outer index and then added in index order, so results
+//     do not depend on the thread count (the reference's OpenMP reductions do).
+//   * FFTW (a third-party dependency the reference calls through dfftw_plan_dft_2d /
+//     dfftw_execute_dft, compact3d.f:9315-9333, version not pinned anywhere) is
+//     replaced by a mixed-radix complex FFT written from the DFT definition with
+//     FFTW's conventions: forward exponent -1, backward +1, unnormalised.
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <cstdlib>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include "../include/c3d.h"
+
+namespace {
+
+typedef std::complex<double> cplx;
+
+struct Orc {
+    int N1, N2, N3, N1M, N2M, N3M, N1MH, N3MH;
+    double ALX, ALY, ALZ, VOL, DX1, DX3, DX1Q, DX3Q, RE;
+    int FILES, WMODEL;
+    int IFWALL;
+    // 1-based Fortran vectors (index 0 allowed where the reference declares 0:)
+    std::vector<double> Y, DY, H, HM, HC, HP, DYM, DYC, DYP;
+    std::vector<int> IPA, IMA, KPA, KMA, JPA, JMU, JMV;
+    std::vector<double> FJPA, FJMU, FJMV;
+    std::vector<double> AK1, AK3, PMJ, PCJ, PPJ;
+    std::vector<double> UBC;          // UBC(0:M1,0:M3,3,2)
+    std::vector<double> TAUW, TAUB;   // (0:M1,0:M3,2)
+    // work arrays of GETUP / UHCALC / DPCALC
+    std::vector<double> UH, HH2, RUH1, RUH2, RUH3, DP, RDP;
+    std::vector<double> FRDP, FDP;    // (M1,M2,M3MD)
+    std::vector<cplx> COEF;           // (M1M,M3M,M2)
+
+    long su1, su2, su3;               // strides of (0:M1,0:M2,0:M3)
+    long sp1, sp2;                    // strides of (M1,M2,M3)
+
+    inline long iu(int i, int j, int k) const { return i + su1 * j + su2 * (long)k; }
+    inline long iuc(int i, int j, int k, int c) const { return iu(i, j, k) + su3 * (long)(c - 1); }
+    inline long ip(int i, int j, int k) const { return (i - 1) + sp1 * (j - 1) + sp2 * (long)(k - 1); }
+    inline long itw(int i, int k, int w) const { return i + (long)(N1 + 1) * k + (long)(N1 + 1) * (N3 + 1) * (w - 1); }
+    inline long iubc(int i, int k, int c, int w) const {
+        return i + (long)(N1 + 1) * k + (long)(N1 + 1) * (N3 + 1) * ((c - 1) + 3 * (w - 1));
+    }
+};
+
+// ----------------------------------------------------------------------------------
+// Line solvers (compact3d.f:8630-9046, 9444-9459).  Arrays are 1-based.
+// ----------------------------------------------------------------------------------
+
+// CTDMA11 / CTDMA33: cyclic tridiagonal, bordered LU with divisions (compact3d.f:8952-9046).
+void ctdma_bordered(int n, const double *A, const double *B, const double *C,
+                    const double *D, double *X) {
+    thread_local std::vector<double> s;
+    s.resize(5 * (size_t)(n + 1));
+    double *Z = s.data(), *BETA = Z + (n + 1), *P = BETA + (n + 1), *GAMA = P + (n + 1),
+           *Q = GAMA + (n + 1);
+    BETA[1] = B[1];
+    GAMA[1] = C[1] / BETA[1];
+    for (int i = 2; i <= n - 1; i++) {
+        BETA[i] = B[i] - A[i] * GAMA[i - 1];
+        GAMA[i] = C[i] / BETA[i];
+    }
+    P[1] = C[n];
+    Q[1] = A[1] / BETA[1];
+    for (int i = 2; i <= n - 2; i++) {
+        P[i] = -P[i - 1] * GAMA[i - 1];
+        Q[i] = -A[i] * Q[i - 1] / BETA[i];
+    }
+    P[n - 1] = A[n] - P[n - 2] * GAMA[n - 2];
+    Q[n - 1] = (C[n - 1] - A[n - 1] * Q[n - 2]) / BETA[n - 1];
+    P[n] = B[n];
+    for (int i = 1; i <= n - 1; i++) P[n] = P[n] - P[i] * Q[i];
+    Z[1] = D[1] / BETA[1];
+    for (int i = 2; i <= n - 1; i++) Z[i] = (D[i] - A[i] * Z[i - 1]) / BETA[i];
+    Z[n] = D[n];
+    for (int i = 1; i <= n - 1; i++) Z[n] = Z[n] - P[i] * Z[i];
+    Z[n] = Z[n] / P[n];
+    X[n] = Z[n];
+    X[n - 1] = Z[n - 1] - Q[n - 1] * X[n];
+    for (int i = n - 2; i >= 1; i--) X[i] = Z[i] - GAMA[i] * X[i + 1] - Q[i] * X[n];
+}
+
+// CTDMA1J / CTDMA3I per line: cyclic bordered LU with reciprocals (compact3d.f:8662-8809).
+// D and X may alias (the reference passes the same array).
+void ctdma_recip(int NS, int NF, const double *A, const double *B, const double *C,
+                 const double *D, double *X) {
+    thread_local std::vector<double> s;
+    s.resize(3 * (size_t)(NF + 2));
+    double *GAM = s.data(), *P = GAM + (NF + 2), *Q = P + (NF + 2);
+    int I = NS;
+    double BET1 = 1.0 / B[I];
+    GAM[I] = C[I] * BET1;
+    X[I] = D[I] * BET1;
+    P[I] = C[NF];
+    Q[I] = A[I] * BET1;
+    for (I = NS + 1; I <= NF - 1; I++) {
+        BET1 = 1.0 / (B[I] - A[I] * GAM[I - 1]);
+        GAM[I] = C[I] * BET1;
+        P[I] = -P[I - 1] * GAM[I - 1];
+        Q[I] = -A[I] * BET1 * Q[I - 1];
+        X[I] = (D[I] - A[I] * X[I - 1]) * BET1;
+    }
+    BET1 = 1.0 / (B[NF - 1] - A[NF - 1] * GAM[NF - 2]);
+    P[NF - 1] = A[NF] - P[NF - 2] * GAM[NF - 2];
+    Q[NF - 1] = (C[NF - 1] - A[NF - 1] * Q[NF - 2]) * BET1;
+    X[NF] = D[NF];
+    P[NF] = B[NF];
+    for (I = NS; I <= NF - 1; I++) {
+        X[NF] = X[NF] - P[I] * X[I];
+        P[NF] = P[NF] - P[I] * Q[I];
+    }
+    X[NF] = X[NF] / P[NF];
+    GAM[NF - 1] = 0.0;
+    for (I = NF - 1; I >= NS; I--) X[I] = X[I] - GAM[I] * X[I + 1] - Q[I] * X[NF];
+}
+
+// TDMAI per line (compact3d.f:8630-8659): Thomas, reciprocal form.  D and X may alias.
+void tdmai_line(int NS, int NF, const double *A, const double *B, const double *C,
+                const double *D, double *X) {
+    thread_local std::vector<double> s;
+    s.resize((size_t)NF + 2);
+    double *GAM = s.data();
+    int J = NS;
+    double BET = 1.0 / B[J];
+    GAM[J] = C[J] * BET;
+    X[J] = D[J] * BET;
+    for (J = NS + 1; J <= NF; J++) {
+        BET = 1.0 / (B[J] - A[J] * GAM[J - 1]);
+        GAM[J] = C[J] * BET;
+        X[J] = (D[J] - A[J] * X[J - 1]) * BET;
+    }
+    for (J = NF - 1; J >= NS; J--) X[J] = X[J] - X[J + 1] * GAM[J];
+}
+
+// TDMAP (compact3d.f:9444-9459): Thomas with divisions.  R and X may alias.
+void tdmap(const double *A, const double *B, const double *C, const double *R, int N, double *X) {
+    thread_local std::vector<double> s;
+    s.resize((size_t)N + 2);
+    double *GAM = s.data();
+    double BET = B[1];
+    X[1] = R[1] / BET;
+    for (int J = 2; J <= N; J++) {
+        GAM[J] = C[J - 1] / BET;
+        BET = B[J] - A[J] * GAM[J];
+        X[J] = (R[J] - A[J] * X[J - 1]) / BET;
+    }
+    for (int J = N - 1; J >= 1; J--) X[J] = X[J] - GAM[J + 1] * X[J + 1];
+}
+
+// Convenience wrappers for the constant-coefficient calls of CTDMA11/CTDMA33.
+struct ConstLine {
+    std::vector<double> A, B, C;
+    void set(int n, double a, double b, double c) {
+        A.assign(n + 1, a);
+        B.assign(n + 1, b);
+        C.assign(n + 1, c);
+    }
+};
+
+// ----------------------------------------------------------------------------------
+// FFT: mixed-radix complex DFT, FFTW conventions (forward exponent -1, unnormalised).
+// ----------------------------------------------------------------------------------
+void fft_rec(int n, int sign, const cplx *in, long istride, cplx *out, cplx *scratch) {
+    if (n == 1) {
+        out[0] = in[0];
+        return;
+    }
+    int p = 0;
+    for (int q : {4, 2, 3, 5, 7})
+        if (n % q == 0) {
+            p = q;
+            break;
+        }
+    if (p == 0) {  // naive DFT for any other prime factor
+        for (int k = 0; k < n; k++) {
+            cplx acc(0.0, 0.0);
+            for (int j = 0; j < n; j++) {
+                double ang = sign * 2.0 * M_PI * (double)((long)j * k % n) / n;
+                acc += in[j * istride] * cplx(std::cos(ang), std::sin(ang));
+            }
+            out[k] = acc;
+        }
+        return;
+    }
+    int m = n / p;
+    // decimation in time: sub-sequences in[r + p*j], j=0..m-1
+    for (int r = 0; r < p; r++) fft_rec(m, sign, in + r * istride, istride * p, scratch + r * m, out);
+    for (int k = 0; k < m; k++) {
+        cplx t[8];
+        for (int r = 0; r < p; r++) {
+            double ang = sign * 2.0 * M_PI * (double)(r * k) / n;
+            t[r] = scratch[r * m + k] * cplx(std::cos(ang), std::sin(ang));
+        }
+        for (int s = 0; s < p; s++) {
+            cplx acc(0.0, 0.0);
+            for (int r = 0; r < p; r++) {
+                double ang = sign * 2.0 * M_PI * (double)((r * s) % p) / p;
+                acc += t[r] * cplx(std::cos(ang), std::sin(ang));
+            }
+            out[k + s * m] = acc;
+        }
+    }
+}
+
+void fft1d(int n, int sign, cplx *data, long stride) {
+    thread_local std::vector<cplx> a, b, c;
+    a.resize(n);
+    b.resize(n);
+    c.resize(n);
+    for (int i = 0; i < n; i++) a[i] = data[i * stride];
+    fft_rec(n, sign, a.data(), 1, b.data(), c.data());
+    for (int i = 0; i < n; i++) data[i * stride] = b[i];
+}
+
+// 2-D DFT of a Fortran array COEF(n1,n3) (n1 fastest), as dfftw_plan_dft_2d(n1,n3).
+void dft2d(int n1, int n3, cplx *a, int sign) {
+    for (int k = 0; k < n3; k++) fft1d(n1, sign, a + (long)k * n1, 1);
+    for (int i = 0; i < n1; i++) fft1d(n3, sign, a + i, n1);
+}
+
+// ----------------------------------------------------------------------------------
+// Setup: INDICES (compact3d.f:446-494), INIWAVE (9182-9228), METRICPOISSON (9239-9263)
+// ----------------------------------------------------------------------------------
+void setup_indices(Orc &g) {
+    int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    g.IPA.assign(g.N1 + 1, 0);
+    g.IMA.assign(g.N1 + 1, 0);
+    g.KPA.assign(g.N3 + 1, 0);
+    g.KMA.assign(g.N3 + 1, 0);
+    g.JPA.assign(g.N2 + 1, 0);
+    g.JMU.assign(g.N2 + 1, 0);
+    g.JMV.assign(g.N2 + 1, 0);
+    g.FJPA.assign(g.N2 + 1, 0.0);
+    g.FJMU.assign(g.N2 + 1, 0.0);
+    g.FJMV.assign(g.N2 + 1, 0.0);
+    for (int ic = 1; ic <= N1M; ic++) {
+        g.IPA[ic] = ic + 1;
+        g.IMA[ic] = ic - 1;
+    }
+    g.IPA[N1M] = 1;
+    g.IMA[1] = N1M;
+    for (int kc = 1; kc <= N3M; kc++) {
+        g.KPA[kc] = kc + 1;
+        g.KMA[kc] = kc - 1;
+    }
+    g.KPA[N3M] = 1;
+    g.KMA[1] = N3M;
+    for (int jc = 1; jc <= N2M; jc++) {
+        g.JPA[jc] = jc + 1;
+        g.JMU[jc] = jc - 1;
+        g.JMV[jc] = jc - 1;
+    }
+    g.JPA[N2M] = N2M;
+    g.JMU[1] = 1;
+    g.JMV[2] = 2;
+    for (int jc = 1; jc <= N2M; jc++) {
+        g.FJPA[jc] = g.JPA[jc] - jc;
+        g.FJMU[jc] = jc - g.JMU[jc];
+        g.FJMV[jc] = jc - g.JMV[jc];
+    }
+}
+
+void setup_wave(Orc &g) {
+    int N1M = g.N1M, N3M = g.N3M;
+    g.N3MH = N3M / 2 + 1;
+    g.N1MH = N1M / 2 + 1;
+    double PI = std::acos(-1.0);
+    std::vector<double> ANI(g.N1 + 1), ANK(g.N3 + 1);
+    g.AK1.assign(g.N1 + 1, 0.0);
+    g.AK3.assign(g.N3MH + 1, 0.0);
+    for (int I = 1; I <= N1M; I++) {
+        int II = I;
+        if (I > N1M / 2 + 1) II = I - N1M;
+        ANI[I] = (II - 1) * 2.0 * PI;
+    }
+    for (int II = 1; II <= N1M; II++) {
+        double cs = std::cos(ANI[II] / N1M);
+        double den = (11.0 + cs);
+        g.AK1[II] = 288.0 * g.DX1Q * (1.0 - cs) / (den * den);
+    }
+    for (int K = 1; K <= g.N3MH; K++) ANK[K] = (K - 1) * 2.0 * PI;
+    for (int KK = 1; KK <= g.N3MH; KK++) {
+        double cs = std::cos(ANK[KK] / N3M);
+        double den = (11.0 + cs);
+        g.AK3[KK] = 288.0 * g.DX3Q * (1.0 - cs) / (den * den);
+    }
+    // METRICPOISSON
+    int N2M = g.N2M;
+    g.PMJ.assign(g.N2 + 1, 0.0);
+    g.PCJ.assign(g.N2 + 1, 0.0);
+    g.PPJ.assign(g.N2 + 1, 0.0);
+    const double *DY = g.DY.data(), *H = g.H.data();
+    for (int JC = 1; JC <= N2M; JC++) {
+        int JP = JC + 1;
+        double FJUM = g.FJMU[JC], FJUP = g.FJPA[JC];
+        g.PMJ[JC] = FJUM * FJUP * (1.0 / DY[JC] / H[JC]) + (1. - FJUP) * (1.0 / DY[N2M] / H[N2M]);
+        g.PCJ[JC] = FJUM * FJUP * (-1.0 / DY[JC] / H[JC] - 1.0 / DY[JC] / H[JP]) +
+                    (1. - FJUP) * (-1.0 / DY[N2M] / H[N2M]) + (1. - FJUM) * (-1.0 / DY[1] / H[2]);
+        g.PPJ[JC] = FJUM * FJUP * (1.0 / DY[JC] / H[JP]) + (1. - FJUM) * (1.0 / DY[1] / H[2]);
+    }
+}
+
+// ----------------------------------------------------------------------------------
+// BCOND (compact3d.f:963-1001)
+// ----------------------------------------------------------------------------------
+void bcond(Orc &g, double *U, double *SGSVIS) {
+    int N1M = g.N1M, N3M = g.N3M, N2 = g.N2, N2M = g.N2M;
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int I = 1; I <= N1M; I++) {
+            g.UBC[g.iubc(I, K, 1, 1)] = 0.0;
+            g.UBC[g.iubc(I, K, 2, 1)] = 0.0;
+            g.UBC[g.iubc(I, K, 3, 1)] = 0.0;
+            U[g.iuc(I, 0, K, 1)] = g.UBC[g.iubc(I, K, 1, 1)];
+            U[g.iuc(I, 0, K, 2)] = g.UBC[g.iubc(I, K, 2, 1)];
+            U[g.iuc(I, 0, K, 3)] = g.UBC[g.iubc(I, K, 3, 1)];
+            g.UBC[g.iubc(I, K, 1, 2)] = U[g.iuc(I, N2M, K, 1)] * (2.0 - g.ALY);
+            g.UBC[g.iubc(I, K, 2, 2)] = 0.0;
+            g.UBC[g.iubc(I, K, 3, 2)] = U[g.iuc(I, N2M, K, 3)] * (2.0 - g.ALY);
+            U[g.iuc(I, N2, K, 1)] = g.UBC[g.iubc(I, K, 1, 2)];
+            U[g.iuc(I, N2, K, 2)] = g.UBC[g.iubc(I, K, 2, 2)];
+            U[g.iuc(I, N2, K, 3)] = g.UBC[g.iubc(I, K, 3, 2)];
+            // The reference tests an undeclared local FILES here (always zero-valued in
+            // practice), so SGSVIS's wall planes are left to the SGS routines.
+            (void)SGSVIS;
+        }
+}
+
+// ----------------------------------------------------------------------------------
+// RHS1 (compact3d.f:6063-6782), DNS terms.  The SGS-flux terms (6436-6763) add exact
+// zeros when SGSVIS == 0, which is the case for FILES == 0 (GETUP zeroes SGSVIS).
+// ----------------------------------------------------------------------------------
+void rhs1(Orc &g, const double *U, const double *P, double *HH, const double *HH2,
+          double *RUH1, double PRESG) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
+    const double RE = g.RE, DX1 = g.DX1, DX3 = g.DX3, DX1Q = g.DX1Q, DX3Q = g.DX3Q;
+    const double *DY = g.DY.data(), *H = g.H.data(), *HP = g.HP.data(), *HC = g.HC.data(),
+                 *HM = g.HM.data();
+    auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+
+    // 10: viscous term (1/RE) d2u/dy2
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 1; J <= N2M; J++) {
+            int JP = J + 1, JM = J - 1;
+            for (int I = 1; I <= N1M; I++) {
+                double VISCOS = (1. / RE) * (HP[J] * u(I, JP, K, 1) - HC[J] * u(I, J, K, 1) +
+                                             HM[J] * u(I, JM, K, 1));
+                RUH1[g.iu(I, J, K)] = VISCOS;
+            }
+        }
+    ConstLine L10x, L10z, L22x, L6x, L6z, L22z;
+    L10x.set(N1M, 1.0, 10.0, 1.0);
+    L10z.set(N3M, 1.0, 10.0, 1.0);
+    L22x.set(N1M, 1.0, 22.0, 1.0);
+    L22z.set(N3M, 1.0, 22.0, 1.0);
+    L6x.set(N1M, 1.0, 6.0, 1.0);
+    L6z.set(N3M, 1.0, 6.0, 1.0);
+
+    // 20: (1/RE) d2u/dx2
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        std::vector<double> D1(N1M + 1), X1(N1M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int I = 2; I <= N1M - 1; I++)
+                D1[I] = 12. * DX1Q * (u(I - 1, J, K, 1) - 2. * u(I, J, K, 1) + u(I + 1, J, K, 1));
+            D1[1] = 12. * DX1Q * (u(N1M, J, K, 1) - 2. * u(1, J, K, 1) + u(2, J, K, 1));
+            D1[N1M] = 12. * DX1Q * (u(N1M - 1, J, K, 1) - 2. * u(N1M, J, K, 1) + u(1, J, K, 1));
+            ctdma_bordered(N1M, L10x.A.data(), L10x.B.data(), L10x.C.data(), D1.data(), X1.data());
+            for (int I = 1; I <= N1M; I++) RUH1[g.iu(I, J, K)] = RUH1[g.iu(I, J, K)] + (1. / RE) * X1[I];
+        }
+    }
+    // 30: (1/RE) d2u/dz2
+#pragma omp parallel for
+    for (int I = 1; I <= N1M; I++) {
+        std::vector<double> D3(N3M + 1), X3(N3M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int K = 2; K <= N3M - 1; K++)
+                D3[K] = 12. * DX3Q * (u(I, J, K - 1, 1) - 2. * u(I, J, K, 1) + u(I, J, K + 1, 1));
+            D3[1] = 12. * DX3Q * (u(I, J, N3M, 1) - 2. * u(I, J, 1, 1) + u(I, J, 2, 1));
+            D3[N3M] = 12. * DX3Q * (u(I, J, N3M - 1, 1) - 2. * u(I, J, N3M, 1) + u(I, J, 1, 1));
+            ctdma_bordered(N3M, L10z.A.data(), L10z.B.data(), L10z.C.data(), D3.data(), X3.data());
+            for (int K = 1; K <= N3M; K++) RUH1[g.iu(I, J, K)] = RUH1[g.iu(I, J, K)] + (1. / RE) * X3[K];
+        }
+    }
+    // 40: pressure gradient
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        std::vector<double> D1(N1M + 1), X1(N1M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int I = 2; I <= N1M; I++)
+                D1[I] = 24. * DX1 * (-P[g.ip(I - 1, J, K)] + P[g.ip(I, J, K)]);
+            D1[1] = 24. * DX1 * (-P[g.ip(N1M, J, K)] + P[g.ip(1, J, K)]);
+            ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D1.data(), X1.data());
+            for (int I = 1; I <= N1M; I++) RUH1[g.iu(I, J, K)] = RUH1[g.iu(I, J, K)] - X1[I] - PRESG;
+        }
+    }
+    // d(UV)/dy
+    {
+        std::vector<double> VV1((size_t)(N1M + 1) * (N2M + 2));
+        auto vv1 = [&](int i, int j) -> double & { return VV1[i + (size_t)(N1M + 1) * j]; };
+        for (int K = 1; K <= N3M; K++) {
+#pragma omp parallel for
+            for (int J = 1; J <= N2M; J++) {
+                std::vector<double> D1(N1M + 1), X1(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D1[I] = 4.0 * (u(I - 1, J, K, 2) + u(I, J, K, 2));
+                D1[1] = 4.0 * (u(N1M, J, K, 2) + u(1, J, K, 2));
+                ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+                for (int I = 1; I <= N1M; I++) vv1(I, J) = X1[I];
+            }
+#pragma omp parallel for
+            for (int J = 1; J <= N2M; J++) {
+                int JP = J + 1, JM = J - 1;
+                double FJUM = g.FJMU[J], FJUP = g.FJPA[J];
+                for (int I = 1; I <= N1M; I++) {
+                    double U2 = FJUP * 1.0 / H[JP] * (DY[J] / 2. * u(I, JP, K, 1) + DY[JP] / 2. * u(I, J, K, 1)) +
+                                (1. - FJUP) * u(I, N2, K, 1);
+                    double U1 = FJUM * 1.0 / H[J] * (DY[JM] / 2. * u(I, J, K, 1) + DY[J] / 2. * u(I, JM, K, 1)) +
+                                (1. - FJUM) * u(I, 0, K, 1);
+                    double V2 = (J == N2M) ? 0.0 : vv1(I, JP);
+                    double V1 = (J == 1) ? 0.0 : vv1(I, J);
+                    long id = g.iuc(I, J, K, 1);
+                    HH[id] = HH[id] + 1. / DY[J] * (V2 * U2 - V1 * U1);
+                }
+            }
+        }
+    }
+    // 50: d(UU)/dx
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        std::vector<double> D1(N1M + 1), X1(N1M + 1), UU1(N1M + 1), D11(N1M + 1), X11(N1M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int I = 1; I <= N1M - 1; I++) D1[I] = 4.0 * (u(I, J, K, 1) + u(I + 1, J, K, 1));
+            D1[N1M] = 4.0 * (u(N1M, J, K, 1) + u(1, J, K, 1));
+            ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+            for (int I = 1; I <= N1M; I++) UU1[I] = X1[I];
+            for (int I = 2; I <= N1M; I++) D11[I] = 24. * DX1 * (UU1[I] * UU1[I] - UU1[I - 1] * UU1[I - 1]);
+            D11[1] = 24. * DX1 * (UU1[1] * UU1[1] - UU1[N1M] * UU1[N1M]);
+            ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+            for (int I = 1; I <= N1M; I++) {
+                long id = g.iuc(I, J, K, 1);
+                HH[id] = HH[id] + X11[I];
+            }
+        }
+    }
+    // 60: d(UW)/dz
+    {
+        std::vector<double> UU3((size_t)(N1M + 1) * (N3M + 1)), WW1((size_t)(N1M + 1) * (N3M + 1));
+        auto uu3 = [&](int i, int k) -> double & { return UU3[i + (size_t)(N1M + 1) * k]; };
+        auto ww1 = [&](int i, int k) -> double & { return WW1[i + (size_t)(N1M + 1) * k]; };
+        for (int J = 1; J <= N2M; J++) {
+#pragma omp parallel for
+            for (int I = 1; I <= N1M; I++) {
+                std::vector<double> D3(N3M + 1), X3(N3M + 1);
+                for (int K = 2; K <= N3M; K++) D3[K] = 4. * (u(I, J, K - 1, 1) + u(I, J, K, 1));
+                D3[1] = 4. * (u(I, J, N3M, 1) + u(I, J, 1, 1));
+                ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+                for (int K = 1; K <= N3M; K++) uu3(I, K) = X3[K];
+            }
+#pragma omp parallel for
+            for (int K = 1; K <= N3M; K++) {
+                std::vector<double> D1(N1M + 1), X1(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D1[I] = 4. * (u(I - 1, J, K, 3) + u(I, J, K, 3));
+                D1[1] = 4. * (u(N1M, J, K, 3) + u(1, J, K, 3));
+                ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+                for (int I = 1; I <= N1M; I++) ww1(I, K) = X1[I];
+            }
+#pragma omp parallel for
+            for (int I = 1; I <= N1M; I++) {
+                std::vector<double> D33(N3M + 1), X33(N3M + 1);
+                for (int K = 1; K <= N3M - 1; K++)
+                    D33[K] = 24. * DX3 * (-uu3(I, K) * ww1(I, K) + uu3(I, K + 1) * ww1(I, K + 1));
+                D33[N3M] = 24. * DX3 * (-uu3(I, N3M) * ww1(I, N3M) + uu3(I, 1) * ww1(I, 1));
+                ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+                for (int K = 1; K <= N3M; K++) {
+                    long id = g.iuc(I, J, K, 1);
+                    HH[id] = HH[id] + X33[K];
+                }
+            }
+        }
+    }
+    // 71/73: AB2 and wall-stress boundary term
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 1; J <= N2M; J++) {
+            double FJUM = g.FJMU[J], FJUP = g.FJPA[J];
+            for (int I = 1; I <= N1M; I++) {
+                double BC_DOWN = -g.TAUW[g.itw(I, K, 1)] / DY[1] * g.IFWALL;
+                double BC_UP = -g.TAUW[g.itw(I, K, 2)] / DY[N2M] * g.IFWALL * (g.ALY - 1.);
+                double BC = (1. - FJUM) * BC_DOWN + (1. - FJUP) * BC_UP;
+                long id = g.iu(I, J, K);
+                RUH1[id] = RUH1[id] - 3. / 2. * HH[g.iuc(I, J, K, 1)] + 1. / 2. * HH2[g.iuc(I, J, K, 1)] + BC;
+            }
+        }
+}
+
+// RHS2 (compact3d.f:6784-7396), DNS terms.
+void rhs2(Orc &g, const double *U, const double *P, double *HH, const double *HH2, double *RUH2) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double RE = g.RE, DX1 = g.DX1, DX3 = g.DX3, DX1Q = g.DX1Q, DX3Q = g.DX3Q;
+    const double *DY = g.DY.data(), *H = g.H.data(), *DYP = g.DYP.data(), *DYC = g.DYC.data(),
+                 *DYM = g.DYM.data();
+    auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+    ConstLine L10x, L10z, L22x, L6x, L6z, L22z;
+    L10x.set(N1M, 1.0, 10.0, 1.0);
+    L10z.set(N3M, 1.0, 10.0, 1.0);
+    L22x.set(N1M, 1.0, 22.0, 1.0);
+    L22z.set(N3M, 1.0, 22.0, 1.0);
+    L6x.set(N1M, 1.0, 6.0, 1.0);
+    L6z.set(N3M, 1.0, 6.0, 1.0);
+    // 10
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 2; J <= N2M; J++) {
+            int JP = J + 1, JM = J - 1;
+            for (int I = 1; I <= N1M; I++) {
+                double VISCOS = (1. / RE) * (DYP[J] * u(I, JP, K, 2) - DYC[J] * u(I, J, K, 2) + DYM[J] * u(I, JM, K, 2));
+                double PRESSG2 = (P[g.ip(I, J, K)] - P[g.ip(I, JM, K)]) / H[J];
+                RUH2[g.iu(I, J, K)] = -PRESSG2 + VISCOS;
+                double V2 = 0.5 * (u(I, JP, K, 2) + u(I, J, K, 2));
+                double V1 = 0.5 * (u(I, J, K, 2) + u(I, JM, K, 2));
+                long id = g.iuc(I, J, K, 2);
+                HH[id] = HH[id] + 1. / H[J] * (V2 * V2 - V1 * V1);
+            }
+        }
+    // 20
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        std::vector<double> D1(N1M + 1), X1(N1M + 1);
+        for (int J = 2; J <= N2M; J++) {
+            for (int I = 2; I <= N1M - 1; I++)
+                D1[I] = 12. * DX1Q * (u(I - 1, J, K, 2) - 2. * u(I, J, K, 2) + u(I + 1, J, K, 2));
+            D1[1] = 12. * DX1Q * (u(N1M, J, K, 2) - 2. * u(1, J, K, 2) + u(2, J, K, 2));
+            D1[N1M] = 12. * DX1Q * (u(N1M - 1, J, K, 2) - 2. * u(N1M, J, K, 2) + u(1, J, K, 2));
+            ctdma_bordered(N1M, L10x.A.data(), L10x.B.data(), L10x.C.data(), D1.data(), X1.data());
+            for (int I = 1; I <= N1M; I++) RUH2[g.iu(I, J, K)] = RUH2[g.iu(I, J, K)] + (1. / RE) * X1[I];
+        }
+    }
+    // 30
+#pragma omp parallel for
+    for (int I = 1; I <= N1M; I++) {
+        std::vector<double> D3(N3M + 1), X3(N3M + 1);
+        for (int J = 2; J <= N2M; J++) {
+            for (int K = 2; K <= N3M - 1; K++)
+                D3[K] = 12. * DX3Q * (u(I, J, K - 1, 2) - 2. * u(I, J, K, 2) + u(I, J, K + 1, 2));
+            D3[1] = 12. * DX3Q * (u(I, J, N3M, 2) - 2. * u(I, J, 1, 2) + u(I, J, 2, 2));
+            D3[N3M] = 12. * DX3Q * (u(I, J, N3M - 1, 2) - 2. * u(I, J, N3M, 2) + u(I, J, 1, 2));
+            ctdma_bordered(N3M, L10z.A.data(), L10z.B.data(), L10z.C.data(), D3.data(), X3.data());
+            for (int K = 1; K <= N3M; K++) RUH2[g.iu(I, J, K)] = RUH2[g.iu(I, J, K)] + (1. / RE) * X3[K];
+        }
+    }
+    // 50: d(UV)/dx
+    for (int K = 1; K <= N3M; K++) {
+        std::vector<double> VV1((size_t)(N1M + 2) * (N2M + 1)), UU2((size_t)(N1M + 2) * (N2M + 1));
+        auto vv1 = [&](int i, int j) -> double & { return VV1[i + (size_t)(N1M + 2) * j]; };
+        auto uu2 = [&](int i, int j) -> double & { return UU2[i + (size_t)(N1M + 2) * j]; };
+#pragma omp parallel for
+        for (int J = 2; J <= N2M; J++) {
+            std::vector<double> D1(N1M + 1), X1(N1M + 1);
+            for (int I = 2; I <= N1M; I++) D1[I] = 4. * (u(I - 1, J, K, 2) + u(I, J, K, 2));
+            D1[1] = 4. * (u(N1M, J, K, 2) + u(1, J, K, 2));
+            ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+            for (int I = 1; I <= N1M; I++) vv1(I, J) = X1[I];
+        }
+#pragma omp parallel for
+        for (int I = 1; I <= N1M; I++)
+            for (int J = 2; J <= N2M; J++)
+                uu2(I, J) = 1. / H[J] * (DY[J] / 2. * u(I, J - 1, K, 1) + DY[J - 1] / 2. * u(I, J, K, 1));
+#pragma omp parallel for
+        for (int J = 2; J <= N2M; J++) {
+            std::vector<double> D11(N1M + 1), X11(N1M + 1);
+            for (int I = 1; I <= N1M - 1; I++)
+                D11[I] = 24. * DX1 * (-uu2(I, J) * vv1(I, J) + uu2(I + 1, J) * vv1(I + 1, J));
+            D11[N1M] = 24. * DX1 * (-uu2(N1M, J) * vv1(N1M, J) + uu2(1, J) * vv1(1, J));
+            ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+            for (int I = 1; I <= N1M; I++) {
+                long id = g.iuc(I, J, K, 2);
+                HH[id] = HH[id] + X11[I];
+            }
+        }
+    }
+    // 60: d(VW)/dz
+    for (int I = 1; I <= N1M; I++) {
+        std::vector<double> VV3((size_t)(N2M + 1) * (N3M + 2)), WW2((size_t)(N2M + 1) * (N3M + 2));
+        auto vv3 = [&](int j, int k) -> double & { return VV3[j + (size_t)(N2M + 1) * k]; };
+        auto ww2 = [&](int j, int k) -> double & { return WW2[j + (size_t)(N2M + 1) * k]; };
+#pragma omp parallel for
+        for (int J = 2; J <= N2M; J++) {
+            std::vector<double> D3(N3M + 1), X3(N3M + 1);
+            for (int K = 2; K <= N3M; K++) D3[K] = 4. * (u(I, J, K - 1, 2) + u(I, J, K, 2));
+            D3[1] = 4. * (u(I, J, N3M, 2) + u(I, J, 1, 2));
+            ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+            for (int K = 1; K <= N3M; K++) vv3(J, K) = X3[K];
+        }
+#pragma omp parallel for
+        for (int K = 1; K <= N3M; K++)
+            for (int J = 2; J <= N2M; J++)
+                ww2(J, K) = 1. / H[J] * (DY[J] / 2. * u(I, J - 1, K, 3) + DY[J - 1] / 2. * u(I, J, K, 3));
+#pragma omp parallel for
+        for (int J = 2; J <= N2M; J++) {
+            std::vector<double> D33(N3M + 1), X33(N3M + 1);
+            for (int K = 1; K <= N3M - 1; K++)
+                D33[K] = 24. * DX3 * (-vv3(J, K) * ww2(J, K) + vv3(J, K + 1) * ww2(J, K + 1));
+            D33[N3M] = 24. * DX3 * (-vv3(J, N3M) * ww2(J, N3M) + vv3(J, 1) * ww2(J, 1));
+            ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+            for (int K = 1; K <= N3M; K++) {
+                long id = g.iuc(I, J, K, 2);
+                HH[id] = HH[id] + X33[K];
+            }
+        }
+    }
+    // 61-65: AB2
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 2; J <= N2M; J++)
+            for (int I = 1; I <= N1M; I++) {
+                long id = g.iu(I, J, K);
+                RUH2[id] = RUH2[id] - 3. / 2. * HH[g.iuc(I, J, K, 2)] + 1. / 2. * HH2[g.iuc(I, J, K, 2)];
+            }
+}
+
+// RHS3 (compact3d.f:7399-8114), DNS terms.
+void rhs3(Orc &g, const double *U, const double *P, double *HH, const double *HH2, double *RUH3,
+          double PRESG3) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
+    const double RE = g.RE, DX1 = g.DX1, DX3 = g.DX3, DX1Q = g.DX1Q, DX3Q = g.DX3Q;
+    const double *DY = g.DY.data(), *H = g.H.data(), *HP = g.HP.data(), *HC = g.HC.data(),
+                 *HM = g.HM.data();
+    auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+    ConstLine L10x, L10z, L22x, L6x, L6z, L22z;
+    L10x.set(N1M, 1.0, 10.0, 1.0);
+    L10z.set(N3M, 1.0, 10.0, 1.0);
+    L22x.set(N1M, 1.0, 22.0, 1.0);
+    L22z.set(N3M, 1.0, 22.0, 1.0);
+    L6x.set(N1M, 1.0, 6.0, 1.0);
+    L6z.set(N3M, 1.0, 6.0, 1.0);
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 1; J <= N2M; J++) {
+            int JP = J + 1, JM = J - 1;
+            for (int I = 1; I <= N1M; I++) {
+                double VISCOS = (1. / RE) * (HP[J] * u(I, JP, K, 3) - HC[J] * u(I, J, K, 3) + HM[J] * u(I, JM, K, 3));
+                RUH3[g.iu(I, J, K)] = VISCOS;
+            }
+        }
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        std::vector<double> D1(N1M + 1), X1(N1M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int I = 2; I <= N1M - 1; I++)
+                D1[I] = 12. * DX1Q * (u(I - 1, J, K, 3) - 2. * u(I, J, K, 3) + u(I + 1, J, K, 3));
+            D1[1] = 12. * DX1Q * (u(N1M, J, K, 3) - 2. * u(1, J, K, 3) + u(2, J, K, 3));
+            D1[N1M] = 12. * DX1Q * (u(N1M - 1, J, K, 3) - 2. * u(N1M, J, K, 3) + u(1, J, K, 3));
+            ctdma_bordered(N1M, L10x.A.data(), L10x.B.data(), L10x.C.data(), D1.data(), X1.data());
+            for (int I = 1; I <= N1M; I++) RUH3[g.iu(I, J, K)] = RUH3[g.iu(I, J, K)] + (1. / RE) * X1[I];
+        }
+    }
+#pragma omp parallel for
+    for (int I = 1; I <= N1M; I++) {
+        std::vector<double> D3(N3M + 1), X3(N3M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int K = 2; K <= N3M - 1; K++)
+                D3[K] = 12. * DX3Q * (u(I, J, K - 1, 3) - 2. * u(I, J, K, 3) + u(I, J, K + 1, 3));
+            D3[1] = 12. * DX3Q * (u(I, J, N3M, 3) - 2. * u(I, J, 1, 3) + u(I, J, 2, 3));
+            D3[N3M] = 12. * DX3Q * (u(I, J, N3M - 1, 3) - 2. * u(I, J, N3M, 3) + u(I, J, 1, 3));
+            ctdma_bordered(N3M, L10z.A.data(), L10z.B.data(), L10z.C.data(), D3.data(), X3.data());
+            for (int K = 1; K <= N3M; K++) RUH3[g.iu(I, J, K)] = RUH3[g.iu(I, J, K)] + (1. / RE) * X3[K];
+        }
+    }
+#pragma omp parallel for
+    for (int I = 1; I <= N1M; I++) {
+        std::vector<double> D3(N3M + 1), X3(N3M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int K = 2; K <= N3M; K++) D3[K] = 24. * DX3 * (-P[g.ip(I, J, K - 1)] + P[g.ip(I, J, K)]);
+            D3[1] = 24. * DX3 * (-P[g.ip(I, J, N3M)] + P[g.ip(I, J, 1)]);
+            ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D3.data(), X3.data());
+            for (int K = 1; K <= N3M; K++) RUH3[g.iu(I, J, K)] = RUH3[g.iu(I, J, K)] - X3[K] - PRESG3;
+        }
+    }
+    // d(WV)/dy
+    for (int I = 1; I <= N1M; I++) {
+        std::vector<double> VV3((size_t)(N2M + 2) * (N3M + 1));
+        auto vv3 = [&](int j, int k) -> double & { return VV3[j + (size_t)(N2M + 2) * k]; };
+#pragma omp parallel for
+        for (int J = 1; J <= N2M; J++) {
+            std::vector<double> D3(N3M + 1), X3(N3M + 1);
+            for (int K = 2; K <= N3M; K++) D3[K] = 4.0 * (u(I, J, K - 1, 2) + u(I, J, K, 2));
+            D3[1] = 4.0 * (u(I, J, N3M, 2) + u(I, J, 1, 2));
+            ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+            for (int K = 1; K <= N3M; K++) vv3(J, K) = X3[K];
+        }
+#pragma omp parallel for
+        for (int K = 1; K <= N3M; K++)
+            for (int J = 1; J <= N2M; J++) {
+                int JP = J + 1, JM = J - 1;
+                double FJUM = g.FJMU[J], FJUP = g.FJPA[J];
+                double W2 = FJUP * 1.0 / H[JP] * (DY[JP] / 2. * u(I, J, K, 3) + DY[J] / 2. * u(I, JP, K, 3)) +
+                            (1. - FJUP) * u(I, N2, K, 3);
+                double W1 = FJUM * 1.0 / H[J] * (DY[J] / 2. * u(I, JM, K, 3) + DY[JM] / 2. * u(I, J, K, 3)) +
+                            (1. - FJUM) * u(I, 0, K, 3);
+                double V2 = (J == N2M) ? 0.0 : vv3(JP, K);
+                double V1 = (J == 1) ? 0.0 : vv3(J, K);
+                long id = g.iuc(I, J, K, 3);
+                HH[id] = HH[id] + 1. / DY[J] * (V2 * W2 - V1 * W1);
+            }
+    }
+    // 50: d(WW)/dz
+#pragma omp parallel for
+    for (int I = 1; I <= N1M; I++) {
+        std::vector<double> D3(N3M + 1), X3(N3M + 1), WW3(N3M + 1), D33(N3M + 1), X33(N3M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int K = 1; K <= N3M - 1; K++) D3[K] = 4. * (u(I, J, K, 3) + u(I, J, K + 1, 3));
+            D3[N3M] = 4. * (u(I, J, N3M, 3) + u(I, J, 1, 3));
+            ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+            for (int K = 1; K <= N3M; K++) WW3[K] = X3[K];
+            for (int K = 2; K <= N3M; K++) D33[K] = 24. * DX3 * (WW3[K] * WW3[K] - WW3[K - 1] * WW3[K - 1]);
+            D33[1] = 24. * DX3 * (WW3[1] * WW3[1] - WW3[N3M] * WW3[N3M]);
+            ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+            for (int K = 1; K <= N3M; K++) {
+                long id = g.iuc(I, J, K, 3);
+                HH[id] = HH[id] + X33[K];
+            }
+        }
+    }
+    // 60: d(UW)/dx
+    {
+        std::vector<double> UU3((size_t)(N1M + 2) * (N3M + 1)), WW1((size_t)(N1M + 2) * (N3M + 1));
+        auto uu3 = [&](int i, int k) -> double & { return UU3[i + (size_t)(N1M + 2) * k]; };
+        auto ww1 = [&](int i, int k) -> double & { return WW1[i + (size_t)(N1M + 2) * k]; };
+        for (int J = 1; J <= N2M; J++) {
+#pragma omp parallel for
+            for (int I = 1; I <= N1M; I++) {
+                std::vector<double> D3(N3M + 1), X3(N3M + 1);
+                for (int K = 2; K <= N3M; K++) D3[K] = 4. * (u(I, J, K - 1, 1) + u(I, J, K, 1));
+                D3[1] = 4. * (u(I, J, N3M, 1) + u(I, J, 1, 1));
+                ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+                for (int K = 1; K <= N3M; K++) uu3(I, K) = X3[K];
+            }
+#pragma omp parallel for
+            for (int K = 1; K <= N3M; K++) {
+                std::vector<double> D1(N1M + 1), X1(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D1[I] = 4. * (u(I - 1, J, K, 3) + u(I, J, K, 3));
+                D1[1] = 4. * (u(N1M, J, K, 3) + u(1, J, K, 3));
+                ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+                for (int I = 1; I <= N1M; I++) ww1(I, K) = X1[I];
+            }
+#pragma omp parallel for
+            for (int K = 1; K <= N3M; K++) {
+                std::vector<double> D11(N1M + 1), X11(N1M + 1);
+                for (int I = 1; I <= N1M - 1; I++)
+                    D11[I] = 24. * DX1 * (-uu3(I, K) * ww1(I, K) + uu3(I + 1, K) * ww1(I + 1, K));
+                D11[N1M] = 24. * DX1 * (-uu3(N1M, K) * ww1(N1M, K) + uu3(1, K) * ww1(1, K));
+                ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+                for (int I = 1; I <= N1M; I++) {
+                    long id = g.iuc(I, J, K, 3);
+                    HH[id] = HH[id] + X11[I];
+                }
+            }
+        }
+    }
+    // 71-73: AB2 and wall-stress boundary term
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 1; J <= N2M; J++) {
+            double FJUM = g.FJMU[J], FJUP = g.FJPA[J];
+            for (int I = 1; I <= N1M; I++) {
+                double BC_DOWN = -g.TAUB[g.itw(I, K, 1)] / DY[1] * g.IFWALL;
+                double BC_UP = -g.TAUB[g.itw(I, K, 2)] / DY[N2M] * g.IFWALL * (g.ALY - 1.);
+                double BC = (1. - FJUM) * BC_DOWN + (1. - FJUP) * BC_UP;
+                long id = g.iu(I, J, K);
+                RUH3[id] = RUH3[id] - 3. / 2. * HH[g.iuc(I, J, K, 3)] + 1. / 2. * HH2[g.iuc(I, J, K, 3)] + BC;
+            }
+        }
+}
+
+// ----------------------------------------------------------------------------------
+// GETUH1/2/3 (compact3d.f:8218-8627): Crank-Nicolson delta form, approximate
+// factorisation y -> x -> z (u, v) and y -> z -> x (w), then UH = U + delta.
+// ----------------------------------------------------------------------------------
+void getuh(Orc &g, const double *U, double *UH, const double *RUH, int comp, double DT) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double RE = g.RE, DX1Q = g.DX1Q, DX3Q = g.DX3Q;
+    const int JS = (comp == 2) ? 2 : 1;
+    // y: TDMAI over J for every (I,K)
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        std::vector<double> A(N2M + 2), B(N2M + 2), C(N2M + 2), R(N2M + 2);
+        for (int I = 1; I <= N1M; I++) {
+            for (int J = JS; J <= N2M; J++) {
+                double FJUM = (comp == 2) ? g.FJMV[J] : g.FJMU[J];
+                double FJUP = g.FJPA[J];
+                if (comp == 2) {
+                    C[J] = FJUP * (-0.5 * g.DYP[J] * (1. / RE)) * DT;
+                    B[J] = 1.0 + (+0.5 * g.DYC[J] * (1. / RE)) * DT;
+                    A[J] = FJUM * (-0.5 * g.DYM[J] * (1. / RE)) * DT;
+                    R[J] = DT * RUH[g.iu(I, J, K)];
+                } else {
+                    C[J] = FJUP * (-0.5 * g.HP[J] * (1. / RE)) * DT;
+                    B[J] = 1.0 + (0.5 * g.HC[J] * (1. / RE)) * DT;
+                    A[J] = FJUM * (-0.5 * g.HM[J] * (1. / RE)) * DT;
+                    R[J] = RUH[g.iu(I, J, K)] * DT;
+                }
+            }
+            tdmai_line(JS, N2M, A.data(), B.data(), C.data(), R.data(), R.data());
+            for (int J = JS; J <= N2M; J++) UH[g.iuc(I, J, K, comp)] = R[J];
+        }
+    }
+    const double api = 1.0 - DT / 2.0 * (1. / RE) * 12.0 * DX1Q * (1.0);
+    const double aci = 10.0 - DT / 2.0 * (1. / RE) * 12.0 * DX1Q * (-2.0);
+    const double apk = 1.0 - DT / 2.0 * (1. / RE) * 12.0 * DX3Q * (1.0);
+    const double ack = 10.0 - DT / 2.0 * (1. / RE) * 12.0 * DX3Q * (-2.0);
+    auto xsweep = [&]() {
+#pragma omp parallel for
+        for (int K = 1; K <= N3M; K++) {
+            std::vector<double> A(N1M + 2, api), B(N1M + 2, aci), C(N1M + 2, api), R(N1M + 2);
+            for (int J = JS; J <= N2M; J++) {
+                for (int I = 1; I <= N1M; I++) {
+                    int im = (I == 1) ? N1M : I - 1, ipp = (I == N1M) ? 1 : I + 1;
+                    R[I] = UH[g.iuc(im, J, K, comp)] + 10.0 * UH[g.iuc(I, J, K, comp)] + UH[g.iuc(ipp, J, K, comp)];
+                }
+                ctdma_recip(1, N1M, A.data(), B.data(), C.data(), R.data(), R.data());
+                for (int I = 1; I <= N1M; I++) UH[g.iuc(I, J, K, comp)] = R[I];
+            }
+        }
+    };
+    auto zsweep = [&]() {
+#pragma omp parallel for
+        for (int J = JS; J <= N2M; J++) {
+            std::vector<double> A(N3M + 2, apk), B(N3M + 2, ack), C(N3M + 2, apk), R(N3M + 2), X(N3M + 2);
+            for (int I = 1; I <= N1M; I++) {
+                for (int K = 1; K <= N3M; K++) {
+                    int km = (K == 1) ? N3M : K - 1, kp = (K == N3M) ? 1 : K + 1;
+                    R[K] = UH[g.iuc(I, J, km, comp)] + 10.0 * UH[g.iuc(I, J, K, comp)] + UH[g.iuc(I, J, kp, comp)];
+                }
+                ctdma_recip(1, N3M, A.data(), B.data(), C.data(), R.data(), X.data());
+                for (int K = 1; K <= N3M; K++) UH[g.iuc(I, J, K, comp)] = X[K];
+            }
+        }
+    };
+    if (comp == 3) {
+        zsweep();
+        xsweep();
+    } else {
+        xsweep();
+        zsweep();
+    }
+    (void)U;
+}
+
+// RHSDP (compact3d.f:8117-8214)
+void rhsdp(Orc &g, double *RDP, const double *UH, double DT) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double DX1 = g.DX1, DX3 = g.DX3;
+    const double *DY = g.DY.data();
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 1; J <= N2M; J++) {
+            int JP = J + 1;
+            double FJUM = g.FJMU[J], FJUP = g.FJPA[J];
+            for (int I = 1; I <= N1M; I++) {
+                double DIVUH = (FJUP * UH[g.iuc(I, JP, K, 2)] - FJUM * UH[g.iuc(I, J, K, 2)]) / DY[J];
+                double CBC = (1. - FJUM) * g.UBC[g.iubc(I, K, 2, 1)] / DY[J] -
+                             (1. - FJUP) * g.UBC[g.iubc(I, K, 2, 2)] / DY[J];
+                RDP[g.ip(I, J, K)] = (DIVUH - CBC) / DT;
+            }
+        }
+    ConstLine L22x, L22z;
+    L22x.set(N1M, 1.0, 22.0, 1.0);
+    L22z.set(N3M, 1.0, 22.0, 1.0);
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        std::vector<double> D1(N1M + 1), X1(N1M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int I = 1; I <= N1M - 1; I++)
+                D1[I] = 24. * DX1 * (UH[g.iuc(I + 1, J, K, 1)] - UH[g.iuc(I, J, K, 1)]);
+            D1[N1M] = 24. * DX1 * (UH[g.iuc(1, J, K, 1)] - UH[g.iuc(N1M, J, K, 1)]);
+            ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D1.data(), X1.data());
+            for (int I = 1; I <= N1M; I++) RDP[g.ip(I, J, K)] = RDP[g.ip(I, J, K)] + X1[I] / DT;
+        }
+    }
+#pragma omp parallel for
+    for (int I = 1; I <= N1M; I++) {
+        std::vector<double> D3(N3M + 1), X3(N3M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int K = 1; K <= N3M - 1; K++)
+                D3[K] = 24. * DX3 * (UH[g.iuc(I, J, K + 1, 3)] - UH[g.iuc(I, J, K, 3)]);
+            D3[N3M] = 24. * DX3 * (UH[g.iuc(I, J, 1, 3)] - UH[g.iuc(I, J, N3M, 3)]);
+            ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D3.data(), X3.data());
+            for (int K = 1; K <= N3M; K++) RDP[g.ip(I, J, K)] = RDP[g.ip(I, J, K)] + X3[K] / DT;
+        }
+    }
+}
+
+// GETDP (compact3d.f:9271-9441)
+void getdp(Orc &g, double *DP, const double *RDP) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N1MH = g.N1MH, N3MH = g.N3MH;
+    const long M3MD = N3M + 2;
+    auto coef = [&](int i, int k, int j) -> cplx & {
+        return g.COEF[(i - 1) + (size_t)N1M * ((k - 1) + (size_t)N3M * (j - 1))];
+    };
+    auto frdp = [&](int i, int j, int kk) -> double & {
+        return g.FRDP[(i - 1) + (size_t)g.N1 * ((j - 1) + (size_t)g.N2 * (kk - 1))];
+    };
+    auto fdp = [&](int i, int j, int kk) -> double & {
+        return g.FDP[(i - 1) + (size_t)g.N1 * ((j - 1) + (size_t)g.N2 * (kk - 1))];
+    };
+    (void)M3MD;
+#pragma omp parallel for
+    for (int J = 1; J <= N2M; J++) {
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) coef(I, K, J) = cplx(RDP[g.ip(I, J, K)], 0.0);
+        dft2d(N1M, N3M, &coef(1, 1, J), -1);
+        for (int K = 1; K <= N3MH; K++) {
+            int KR = 2 * K - 1, KI = 2 * K;
+            for (int I = 1; I <= N1M; I++) {
+                frdp(I, J, KR) = coef(I, K, J).real();
+                frdp(I, J, KI) = coef(I, K, J).imag();
+            }
+        }
+    }
+    // real parts
+#pragma omp parallel for
+    for (int K = 1; K <= N3MH; K++) {
+        int KR = 2 * K - 1;
+        std::vector<double> CMJ(N2M + 1), CCJ(N2M + 1), CPJ(N2M + 1), CFJ(N2M + 1);
+        for (int I = 1; I <= N1M; I++) {
+            for (int J = 1; J <= N2M; J++) {
+                CMJ[J] = g.PMJ[J];
+                CCJ[J] = g.PCJ[J] - g.AK3[K] - g.AK1[I];
+                CPJ[J] = g.PPJ[J];
+                CFJ[J] = frdp(I, J, KR);
+                if (I == 1 && K == 1) {
+                    CMJ[1] = 0.0;
+                    CCJ[1] = 1.0;
+                    CPJ[1] = 0.0;
+                    CFJ[1] = 0.0;
+                }
+            }
+            tdmap(CMJ.data(), CCJ.data(), CPJ.data(), CFJ.data(), N2M, CFJ.data());
+            for (int J = 1; J <= N2M; J++) fdp(I, J, KR) = CFJ[J];
+        }
+    }
+    // imaginary parts
+#pragma omp parallel for
+    for (int K = 1; K <= N3MH; K++) {
+        int KI = 2 * K;
+        std::vector<double> CMJ(N2M + 1), CCJ(N2M + 1), CPJ(N2M + 1), CFJ(N2M + 1);
+        for (int I = 1; I <= N1M; I++) {
+            for (int J = 1; J <= N2M; J++) {
+                CMJ[J] = g.PMJ[J];
+                CCJ[J] = g.PCJ[J] - g.AK3[K] - g.AK1[I];
+                CPJ[J] = g.PPJ[J];
+                CFJ[J] = frdp(I, J, KI);
+                if ((I == 1 && K == 1) || (I == 1 && K == N3MH) || (I == N1MH && K == 1) ||
+                    (I == N1MH && K == N3MH)) {
+                    CMJ[J] = 0.0;
+                    CCJ[J] = 1.0;
+                    CPJ[J] = 0.0;
+                    CFJ[J] = 0.0;
+                }
+            }
+            tdmap(CMJ.data(), CCJ.data(), CPJ.data(), CFJ.data(), N2M, CFJ.data());
+            for (int J = 1; J <= N2M; J++) fdp(I, J, KI) = CFJ[J];
+        }
+    }
+    // inverse
+#pragma omp parallel for
+    for (int J = 1; J <= N2M; J++) {
+        for (int K = 1; K <= N3MH; K++) {
+            int KR = 2 * K - 1, KI = 2 * K;
+            for (int I = 1; I <= N1M; I++) coef(I, K, J) = cplx(fdp(I, J, KR), fdp(I, J, KI));
+        }
+        for (int K = N3MH + 1; K <= N3M; K++) {
+            int KK = N3M - K + 2;
+            for (int I = 1; I <= N1M; I++) {
+                int II = N1M - I + 2;
+                if (I == 1) II = 1;
+                coef(I, K, J) = std::conj(coef(II, KK, J));
+            }
+        }
+        dft2d(N1M, N3M, &coef(1, 1, J), +1);
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) DP[g.ip(I, J, K)] = coef(I, K, J).real() / (double)(N1M * N3M);
+    }
+}
+
+// UPCALC (compact3d.f:1052-1238)
+void upcalc(Orc &g, double *U, double *P, const double *UH, const double *DP, double DT,
+            double *PRESG, double *PRESG3, bool bulk_forcing) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
+    const double DX1 = g.DX1, DX3 = g.DX3;
+    const double *DY = g.DY.data(), *H = g.H.data();
+    std::vector<double> pf(N3M + 1), pd(N3M + 1);
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        double f = 0.0, d = 0.0;
+        for (int J = 1; J <= N2M; J++)
+            for (int I = 1; I <= N1M; I++) {
+                int IM = g.IMA[I];
+                f = f + U[g.iuc(I, J, K, 1)] * DY[J] / DX3 / DX1;
+                d = d + UH[g.iuc(I, J, K, 1)] * DY[J] / DX3 / DX1 -
+                    DT * (DP[g.ip(I, J, K)] - DP[g.ip(IM, J, K)]) * DY[J] / DX3;
+            }
+        pf[K] = f;
+        pd[K] = d;
+    }
+    double FLOW1 = 0.0, DMPRESG = 0.0;
+    for (int K = 1; K <= N3M; K++) {
+        FLOW1 += pf[K];
+        DMPRESG += pd[K];
+    }
+    DMPRESG = (DMPRESG - FLOW1) / g.VOL / DT;
+    if (!bulk_forcing) DMPRESG = 0.0;
+    ConstLine L22x, L22z;
+    L22x.set(N1M, 1.0, 22.0, 1.0);
+    L22z.set(N3M, 1.0, 22.0, 1.0);
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        std::vector<double> D1(N1M + 1), X1(N1M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int I = 2; I <= N1M; I++) D1[I] = 24. * DX1 * (-DP[g.ip(I - 1, J, K)] + DP[g.ip(I, J, K)]);
+            D1[1] = 24. * DX1 * (-DP[g.ip(N1M, J, K)] + DP[g.ip(1, J, K)]);
+            ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D1.data(), X1.data());
+            for (int I = 1; I <= N1M; I++) U[g.iuc(I, J, K, 1)] = UH[g.iuc(I, J, K, 1)] - DT * X1[I] - DT * DMPRESG;
+        }
+    }
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int I = 1; I <= N1M; I++) {
+            U[g.iuc(I, 0, K, 1)] = g.UBC[g.iubc(I, K, 1, 1)];
+            U[g.iuc(I, N2, K, 1)] = g.UBC[g.iubc(I, K, 1, 2)];
+        }
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 2; J <= N2M; J++)
+            for (int I = 1; I <= N1M; I++)
+                U[g.iuc(I, J, K, 2)] = UH[g.iuc(I, J, K, 2)] - DT * (DP[g.ip(I, J, K)] - DP[g.ip(I, J - 1, K)]) / H[J];
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int I = 1; I <= N1M; I++) {
+            U[g.iuc(I, 1, K, 2)] = g.UBC[g.iubc(I, K, 2, 1)];
+            U[g.iuc(I, N2, K, 2)] = g.UBC[g.iubc(I, K, 2, 2)];
+        }
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        int KM = g.KMA[K];
+        double f = 0.0, d = 0.0;
+        for (int J = 1; J <= N2M; J++)
+            for (int I = 1; I <= N1M; I++) {
+                f = f + U[g.iuc(I, J, K, 3)] * DY[J] / DX1 / DX3;
+                d = d + UH[g.iuc(I, J, K, 3)] * DY[J] / DX3 / DX1 -
+                    DT * (DP[g.ip(I, J, K)] - DP[g.ip(I, J, KM)]) * DY[J] / DX1;
+            }
+        pf[K] = f;
+        pd[K] = d;
+    }
+    double FLOW3 = 0.0, DMPRESG3 = 0.0;
+    for (int K = 1; K <= N3M; K++) {
+        FLOW3 += pf[K];
+        DMPRESG3 += pd[K];
+    }
+    DMPRESG3 = (DMPRESG3 - FLOW3) / g.VOL / DT;
+    if (!bulk_forcing) DMPRESG3 = 0.0;
+#pragma omp parallel for
+    for (int I = 1; I <= N1M; I++) {
+        std::vector<double> D3(N3M + 1), X3(N3M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int K = 2; K <= N3M; K++) D3[K] = 24. * DX3 * (-DP[g.ip(I, J, K - 1)] + DP[g.ip(I, J, K)]);
+            D3[1] = 24. * DX3 * (-DP[g.ip(I, J, N3M)] + DP[g.ip(I, J, 1)]);
+            ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D3.data(), X3.data());
+            for (int K = 1; K <= N3M; K++) U[g.iuc(I, J, K, 3)] = UH[g.iuc(I, J, K, 3)] - DT * X3[K] - DT * DMPRESG3;
+        }
+    }
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int I = 1; I <= N1M; I++) {
+            U[g.iuc(I, 0, K, 3)] = g.UBC[g.iubc(I, K, 3, 1)];
+            U[g.iuc(I, N2, K, 3)] = g.UBC[g.iubc(I, K, 3, 2)];
+        }
+    if (P) {
+#pragma omp parallel for
+        for (int K = 1; K <= N3M; K++)
+            for (int J = 1; J <= N2M; J++)
+                for (int I = 1; I <= N1M; I++) P[g.ip(I, J, K)] = P[g.ip(I, J, K)] + DP[g.ip(I, J, K)];
+    }
+    if (PRESG) *PRESG = *PRESG + DMPRESG;
+    if (PRESG3) *PRESG3 = *PRESG3 + DMPRESG3;
+}
+
+}  // namespace
+
+// ==================================================================================
+// extern "C" interface used by the tests (ctypes) and by bench.py's CPU baseline.
+// ==================================================================================
+extern "C" {
+
+struct orc_handle;
+
+void *orc_create(const c3d_grid *gr) {
+    if (!gr || gr->n1 < 5 || gr->n2 < 4 || gr->n3 < 5) return nullptr;
+    Orc *g = new Orc();
+    g->N1 = gr->n1;
+    g->N2 = gr->n2;
+    g->N3 = gr->n3;
+    g->N1M = g->N1 - 1;
+    g->N2M = g->N2 - 1;
+    g->N3M = g->N3 - 1;
+    g->ALX = gr->alx;
+    g->ALY = gr->aly;
+    g->ALZ = gr->alz;
+    g->VOL = gr->vol;
+    g->DX1 = gr->dx1;
+    g->DX3 = gr->dx3;
+    g->DX1Q = g->DX1 * g->DX1;
+    g->DX3Q = g->DX3 * g->DX3;
+    g->RE = gr->re;
+    g->FILES = gr->files;
+    g->WMODEL = gr->wmodel;
+    g->IFWALL = 0;
+    int N2 = g->N2;
+    g->Y.assign(gr->y, gr->y + N2 + 1);
+    g->DY.assign(gr->dy, gr->dy + N2 + 1);
+    auto one = [&](std::vector<double> &v, const double *src) {
+        v.assign(N2 + 1, 0.0);
+        for (int j = 1; j <= N2; j++) v[j] = src[j - 1];
+    };
+    one(g->H, gr->h);
+    one(g->HM, gr->hm);
+    one(g->HC, gr->hc);
+    one(g->HP, gr->hp);
+    one(g->DYM, gr->dym);
+    one(g->DYC, gr->dyc);
+    one(g->DYP, gr->dyp);
+    setup_indices(*g);
+    setup_wave(*g);
+    g->su1 = g->N1 + 1;
+    g->su2 = (long)(g->N1 + 1) * (g->N2 + 1);
+    g->su3 = g->su2 * (g->N3 + 1);
+    g->sp1 = g->N1;
+    g->sp2 = (long)g->N1 * g->N2;
+    size_t nu = (size_t)g->su3 * 3, ns = (size_t)g->su3, np = (size_t)g->sp2 * g->N3;
+    g->UBC.assign((size_t)(g->N1 + 1) * (g->N3 + 1) * 6, 0.0);
+    g->TAUW.assign((size_t)(g->N1 + 1) * (g->N3 + 1) * 2, 0.0);
+    g->TAUB.assign((size_t)(g->N1 + 1) * (g->N3 + 1) * 2, 0.0);
+    g->UH.assign(nu, 0.0);
+    g->HH2.assign(nu, 0.0);
+    g->RUH1.assign(ns, 0.0);
+    g->RUH2.assign(ns, 0.0);
+    g->RUH3.assign(ns, 0.0);
+    g->DP.assign(np, 0.0);
+    g->RDP.assign(np, 0.0);
+    g->FRDP.assign((size_t)g->N1 * g->N2 * (g->N3M + 2), 0.0);
+    g->FDP.assign((size_t)g->N1 * g->N2 * (g->N3M + 2), 0.0);
+    g->COEF.assign((size_t)g->N1M * g->N3M * g->N2M, cplx(0, 0));
+    return g;
+}
+
+void orc_destroy(void *h) { delete (Orc *)h; }
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void orc_set_wall(void *h, const double *tauw, const double *taub, int ifwall) {
+    Orc &g = *(Orc *)h;
+    if (tauw) std::memcpy(g.TAUW.data(), tauw, g.TAUW.size() * sizeof(double));
+    if (taub) std::memcpy(g.TAUB.data(), taub, g.TAUB.size() * sizeof(double));
+    g.IFWALL = ifwall;
+}
+
+// GETUP (compact3d.f:879-960) for FILES == 0.  U, P, HH, SGSVIS are Fortran arrays.
+int orc_getup(void *h, double *U, double *P, double *HH, double *SGSVIS, int NTIME, double DT,
+              double *PRESG, double *PRESG3) {
+    Orc &g = *(Orc *)h;
+    (void)NTIME;
+    if (g.FILES != 0) return C3D_EINVAL;
+    const int N1 = g.N1, N2 = g.N2, N3 = g.N3;
+    double *UH = g.UH.data(), *HH2 = g.HH2.data();
+    for (int NV = 1; NV <= 3; NV++) {
+#pragma omp parallel for
+        for (int K = 1; K <= N3; K++)
+            for (int J = 1; J <= N2; J++)
+                for (int I = 1; I <= N1; I++) UH[g.iuc(I, J, K, NV)] = 0.0;
+    }
+#pragma omp parallel for
+    for (int K = 1; K <= N3; K++)
+        for (int J = 1; J <= N2; J++)
+            for (int I = 1; I <= N1; I++) g.DP[g.ip(I, J, K)] = 0.0;
+    if (SGSVIS) {
+#pragma omp parallel for
+        for (int K = 1; K <= N3; K++)
+            for (int J = 0; J <= N2; J++)
+                for (int I = 1; I <= N1; I++) SGSVIS[g.iu(I, J, K)] = 0.0;
+    }
+    for (int NV = 1; NV <= 3; NV++) {
+#pragma omp parallel for
+        for (int K = 1; K <= N3; K++)
+            for (int J = 1; J <= N2; J++)
+                for (int I = 1; I <= N1; I++) {
+                    long id = g.iuc(I, J, K, NV);
+                    HH2[id] = HH[id];
+                    HH[id] = 0.0;
+                }
+    }
+    bcond(g, U, SGSVIS);
+    // UHCALC
+    rhs1(g, U, P, HH, HH2, g.RUH1.data(), *PRESG);
+    rhs2(g, U, P, HH, HH2, g.RUH2.data());
+    rhs3(g, U, P, HH, HH2, g.RUH3.data(), *PRESG3);
+    getuh(g, U, UH, g.RUH1.data(), 1, DT);
+    getuh(g, U, UH, g.RUH2.data(), 2, DT);
+    getuh(g, U, UH, g.RUH3.data(), 3, DT);
+    // end of GETUH3: UH = U + UH
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 1; J <= N2M; J++)
+            for (int I = 1; I <= N1M; I++) {
+                UH[g.iuc(I, J, K, 1)] = U[g.iuc(I, J, K, 1)] + UH[g.iuc(I, J, K, 1)];
+                UH[g.iuc(I, J, K, 3)] = U[g.iuc(I, J, K, 3)] + UH[g.iuc(I, J, K, 3)];
+            }
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 2; J <= N2M; J++)
+            for (int I = 1; I <= N1M; I++) UH[g.iuc(I, J, K, 2)] = U[g.iuc(I, J, K, 2)] + UH[g.iuc(I, J, K, 2)];
+    // DPCALC
+    rhsdp(g, g.RDP.data(), UH, DT);
+    getdp(g, g.DP.data(), g.RDP.data());
+    // UPCALC
+    upcalc(g, U, P, UH, g.DP.data(), DT, PRESG, PRESG3, true);
+    return 0;
+}
+
+// Pressure projection of U (RHSDP + GETDP + UPCALC with UH = U, DT = 1, no bulk forcing);
+// used to make a synthetic initial condition discretely divergence-free.
+int orc_project(void *h, double *U) {
+    Orc &g = *(Orc *)h;
+    bcond(g, U, nullptr);
+    std::vector<double> UH(U, U + g.su3 * 3);
+    rhsdp(g, g.RDP.data(), UH.data(), 1.0);
+    getdp(g, g.DP.data(), g.RDP.data());
+    upcalc(g, U, nullptr, UH.data(), g.DP.data(), 1.0, nullptr, nullptr, false);
+    return 0;
+}
+
+// Individual stages, for unit tests.
+int orc_bcond(void *h, double *U) {
+    bcond(*(Orc *)h, U, nullptr);
+    return 0;
+}
+int orc_getdp(void *h, const double *RDP, double *DP) {
+    getdp(*(Orc *)h, DP, RDP);
+    return 0;
+}
+int orc_rhsdp(void *h, const double *UH, double DT, double *RDP) {
+    rhsdp(*(Orc *)h, RDP, UH, DT);
+    return 0;
+}
+
+// DIVCHECK (compact3d.f:9049-9131)
+double orc_divcheck(void *h, const double *U) {
+    Orc &g = *(Orc *)h;
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double DX1 = g.DX1, DX3 = g.DX3;
+    std::vector<double> DIV((size_t)N1M * N2M * N3M);
+    auto div = [&](int i, int j, int k) -> double & {
+        return DIV[(i - 1) + (size_t)N1M * ((j - 1) + (size_t)N2M * (k - 1))];
+    };
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 1; J <= N2M; J++)
+            for (int I = 1; I <= N1M; I++)
+                div(I, J, K) = (U[g.iuc(I, J + 1, K, 2)] - U[g.iuc(I, J, K, 2)]) / g.DY[J];
+    ConstLine L22x, L22z;
+    L22x.set(N1M, 1.0, 22.0, 1.0);
+    L22z.set(N3M, 1.0, 22.0, 1.0);
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        std::vector<double> D1(N1M + 1), X1(N1M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int I = 1; I <= N1M - 1; I++) D1[I] = 24. * DX1 * (U[g.iuc(I + 1, J, K, 1)] - U[g.iuc(I, J, K, 1)]);
+            D1[N1M] = 24. * DX1 * (U[g.iuc(1, J, K, 1)] - U[g.iuc(N1M, J, K, 1)]);
+            ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D1.data(), X1.data());
+            for (int I = 1; I <= N1M; I++) div(I, J, K) = div(I, J, K) + X1[I];
+        }
+    }
+    std::vector<double> mx(N1M + 1, 0.0);
+#pragma omp parallel for
+    for (int I = 1; I <= N1M; I++) {
+        std::vector<double> D3(N3M + 1), X3(N3M + 1);
+        double m = 0.0;
+        for (int J = 1; J <= N2M; J++) {
+            for (int K = 1; K <= N3M - 1; K++) D3[K] = 24. * DX3 * (U[g.iuc(I, J, K + 1, 3)] - U[g.iuc(I, J, K, 3)]);
+            D3[N3M] = 24. * DX3 * (U[g.iuc(I, J, 1, 3)] - U[g.iuc(I, J, N3M, 3)]);
+            ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D3.data(), X3.data());
+            for (int K = 1; K <= N3M; K++) {
+                div(I, J, K) = div(I, J, K) + X3[K];
+                m = std::max(std::fabs(div(I, J, K)), m);
+            }
+        }
+        mx[I] = m;
+    }
+    double DIVMAX = 0.0;
+    for (int I = 1; I <= N1M; I++) DIVMAX = std::max(mx[I], DIVMAX);
+    return DIVMAX;
+}
+
+// CFL (compact3d.f:9138-9169)
+double orc_cfl(void *h, const double *U) {
+    Orc &g = *(Orc *)h;
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    std::vector<double> mk(N3M + 1, 0.0);
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        int KP = g.KPA[K];
+        double m = 0.0;
+        for (int J = 1; J <= N2M; J++) {
+            int JP = J + 1;
+            for (int I = 1; I <= N1M; I++) {
+                int IP = g.IPA[I];
+                double CFLL = std::fabs(U[g.iuc(I, J, K, 1)] + U[g.iuc(IP, J, K, 1)]) * 0.5 * g.DX1 +
+                              std::fabs(U[g.iuc(I, J, K, 2)] + U[g.iuc(I, JP, K, 2)]) * 0.5 / g.DY[J] +
+                              std::fabs(U[g.iuc(I, J, K, 3)] + U[g.iuc(I, J, KP, 3)]) * 0.5 * g.DX3;
+                m = std::max(m, CFLL);
+            }
+        }
+        mk[K] = m;
+    }
+    double CFLM = 0.0;
+    for (int K = 1; K <= N3M; K++) CFLM = std::max(CFLM, mk[K]);
+    return CFLM;
+}
+
+// CHKMF (compact3d.f:9463-9503)
+void orc_chkmf(void *h, const double *U, double *flow1, double *flow3) {
+    Orc &g = *(Orc *)h;
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    double F1 = 0.0, F3 = 0.0;
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 1; J <= N2M; J++)
+            for (int I = 1; I <= N1M; I++) F1 = F1 + U[g.iuc(1, J, K, 1)] * g.DY[J] / g.DX3 / g.DX1;
+    F1 = F1 / g.ALX / g.ALZ;
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 1; J <= N2M; J++)
+            for (int I = 1; I <= N1M; I++) F3 = F3 + U[g.iuc(I, J, 1, 3)] * g.DY[J] / g.DX1 / g.DX3;
+    F3 = F3 / g.ALX / g.ALZ;
+    *flow1 = F1;
+    *flow3 = F3;
+}
+
+// WALLSS (compact3d.f:11077-11143)
+void orc_wallss(void *h, const double *U, double *wsm) {
+    Orc &g = *(Orc *)h;
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
+    double W1 = 0.0, W2 = 0.0, W3 = 0.0;
+    const double *DY = g.DY.data();
+    double NXZ = 1.0 / (double)(N1M * N3M);
+    for (int K = 1; K <= N3M; K++) {
+        int KP = g.KPA[K];
+        for (int I = 1; I <= N1M; I++) {
+            int IP = g.IPA[I];
+            auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+            double UHC = 0.5 * (u(I, 1, K, 1) + u(IP, 1, K, 1));
+            double UHW = 0.5 * (u(I, 0, K, 1) + u(IP, 0, K, 1));
+            double VHC = u(I, 2, K, 2);
+            double VHW = u(I, 1, K, 2);
+            double WHC = 0.5 * (u(I, 1, K, 3) + u(I, 1, KP, 3));
+            double WHW = 0.5 * (u(I, 0, K, 3) + u(I, 0, KP, 3));
+            double WSB1 = (UHC - UHW) / (DY[1] * 0.5);
+            double WSB2 = (VHC - VHW) / DY[1];
+            double WSB3 = (WHC - WHW) / (DY[1] * 0.5);
+            UHC = 0.5 * (u(I, N2M, K, 1) + u(IP, N2M, K, 1));
+            UHW = 0.5 * (u(I, N2, K, 1) + u(IP, N2, K, 1));
+            double WST1 = (UHC - UHW) / (DY[N2M] * 0.5);
+            W1 = W1 + WSB1 + WST1 * (g.ALY - 1.0);
+            W2 = W2 + WSB2 + WST1 * (g.ALY - 1.0);
+            W3 = W3 + WSB3 + WST1 * (g.ALY - 1.0);
+        }
+    }
+    wsm[0] = W1 * NXZ / g.RE / g.ALY;
+    wsm[1] = W2 * NXZ / g.RE / g.ALY;
+    wsm[2] = W3 * NXZ / g.RE / g.ALY;
+}
+
+// ---- unit-level entry points ----
+// CTDMA11 on one line with constant coefficients (a,b,c); d,x 0-based length n.
+void orc_ctdma11(int n, double a, double b, double c, const double *d, double *x) {
+    std::vector<double> A(n + 1, a), B(n + 1, b), C(n + 1, c), D(n + 1), X(n + 1);
+    for (int i = 0; i < n; i++) D[i + 1] = d[i];
+    ctdma_bordered(n, A.data(), B.data(), C.data(), D.data(), X.data());
+    for (int i = 0; i < n; i++) x[i] = X[i + 1];
+}
+// CTDMA1J/CTDMA3I on one line (reciprocal form).
+void orc_ctdma_recip(int n, double a, double b, double c, const double *d, double *x) {
+    std::vector<double> A(n + 2, a), B(n + 2, b), C(n + 2, c), D(n + 2), X(n + 2);
+    for (int i = 0; i < n; i++) D[i + 1] = d[i];
+    ctdma_recip(1, n, A.data(), B.data(), C.data(), D.data(), X.data());
+    for (int i = 0; i < n; i++) x[i] = X[i + 1];
+}
+// TDMAP on one line; arrays 0-based length n.
+void orc_tdmap(int n, const double *a, const double *b, const double *c, const double *r, double *x) {
+    std::vector<double> A(n + 1), B(n + 1), C(n + 1), R(n + 1), X(n + 1);
+    for (int i = 0; i < n; i++) {
+        A[i + 1] = a[i];
+        B[i + 1] = b[i];
+        C[i + 1] = c[i];
+        R[i + 1] = r[i];
+    }
+    tdmap(A.data(), B.data(), C.data(), R.data(), n, X.data());
+    for (int i = 0; i < n; i++) x[i] = X[i + 1];
+}
+// Complex FFT of n interleaved (re,im) values in place.
+void orc_fft(int n, double *data, int sign) {
+    fft1d(n, sign, (cplx *)data, 1);
+}
+// 2-D DFT of a Fortran complex array (n1 fastest), interleaved doubles.
+void orc_dft2d(int n1, int n3, double *data, int sign) {
+    dft2d(n1, n3, (cplx *)data, sign);
+}
+// Poisson metrics, for tests of the library's own copy.
+void orc_poisson_metrics(void *h, double *ak1, double *ak3, double *pmj, double *pcj, double *ppj) {
+    Orc &g = *(Orc *)h;
+    for (int i = 1; i <= g.N1M; i++) ak1[i - 1] = g.AK1[i];
+    for (int k = 1; k <= g.N3MH; k++) ak3[k - 1] = g.AK3[k];
+    for (int j = 1; j <= g.N2M; j++) {
+        pmj[j - 1] = g.PMJ[j];
+        pcj[j - 1] = g.PCJ[j];
+        ppj[j - 1] = g.PPJ[j];
+    }
+}
+
+}  // extern "C"
