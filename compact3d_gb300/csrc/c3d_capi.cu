@@ -1,0 +1,601 @@
+// c3d_capi.cu -- the C-ABI of include/c3d.h: channel lifecycle, host<->device transfers,
+// the GETUP drop-in step, diagnostics and the batched ensemble.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+#include <string>
+#include <vector>
+#include "../../include/c3d.h"
+#include "c3d_internal.h"
+
+using namespace c3d;
+
+namespace c3d {
+static thread_local std::string g_last_error;
+static thread_local int g_device = -1;
+void set_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace c3d
+
+#define CK(call)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));             \
+            return e_ == cudaErrorMemoryAllocation ? C3D_ENOMEM : C3D_ECUDA;            \
+        }                                                                               \
+    } while (0)
+
+extern "C" {
+
+const char *c3d_error_string(int code) {
+    switch (code) {
+        case C3D_OK: return "ok";
+        case C3D_EINVAL: return "invalid argument (extent, pointer or unsupported size)";
+        case C3D_ECUDA: return "CUDA runtime error";
+        case C3D_ENOMEM: return "out of device or pinned host memory";
+        case C3D_ENOTCONV: return "device iteration cap reached";
+        case C3D_ENONFINITE: return "non-finite value in the fields";
+        case C3D_ESTATE: return "call made in the wrong state";
+        case C3D_ENODEV: return "no usable CUDA device";
+        default: return "unknown error";
+    }
+}
+
+const char *c3d_last_error(void) { return c3d::g_last_error.c_str(); }
+
+int c3d_version(void) { return 10000; }
+
+int c3d_set_device(int device) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        set_error("no CUDA device");
+        return C3D_ENODEV;
+    }
+    if (device < 0 || device >= n) {
+        set_error("device index out of range");
+        return C3D_EINVAL;
+    }
+    CK(cudaSetDevice(device));
+    c3d::g_device = device;
+    return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+bool fft_len_ok(int n) {
+    if (n < 2) return false;
+    while (n % 2 == 0) n /= 2;
+    while (n % 3 == 0) n /= 3;
+    return n == 1;
+}
+
+FftPlan make_plan(int n) {
+    FftPlan p;
+    memset(&p, 0, sizeof(p));
+    p.n = n;
+    int m = n;
+    while (m % 4 == 0) { p.rad[p.nst++] = 4; m /= 4; }
+    while (m % 2 == 0) { p.rad[p.nst++] = 2; m /= 2; }
+    while (m % 3 == 0) { p.rad[p.nst++] = 3; m /= 3; }
+    return p;
+}
+
+// Supported x extents: N1M = P*C with C = ceil(N1M/32) in {1,2,3,4,6,8,12}.
+bool n1_ok(int n1m) {
+    int c = (n1m + 31) / 32;
+    if (!(c == 1 || c == 2 || c == 3 || c == 4 || c == 6 || c == 8 || c == 12)) return false;
+    return n1m % c == 0 && n1m % 2 == 0 && n1m >= 16;
+}
+
+template <typename T>
+int dalloc(T **p, size_t n) {
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        return C3D_ENOMEM;
+    }
+    return 0;
+}
+
+void free_channel(c3d_channel *ch) {
+    if (!ch) return;
+    void *ptrs[] = {ch->u, ch->v, ch->w, ch->p, ch->dp, ch->scal, ch->part, ch->metric, ch->ycn,
+                    ch->prb, ch->pgam, ch->pmj, ch->tw64, ch->tw32, ch->hh[0][0], ch->hh[0][1],
+                    ch->hh[0][2], ch->hh[1][0], ch->hh[1][1], ch->hh[1][2], ch->r[0], ch->r[1],
+                    ch->r[2], ch->exy, ch->exz, ch->eyz, ch->ww1, ch->wsq, ch->rdpz, ch->g1,
+                    ch->spec, ch->stage, ch->tauw, ch->taub};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    if (ch->pinned) cudaFreeHost(ch->pinned);
+    if (ch->stream) cudaStreamDestroy(ch->stream);
+    if (ch->ev0) cudaEventDestroy(ch->ev0);
+    if (ch->ev1) cudaEventDestroy(ch->ev1);
+    delete ch;
+}
+
+// INIWAVE and METRICPOISSON (compact3d.f:9182-9263), restated on the host.
+void poisson_metrics(c3d_channel *ch, const c3d_grid *gr) {
+    const int N1M = gr->n1 - 1, N2M = gr->n2 - 1, N3M = gr->n3 - 1, N2 = gr->n2;
+    const double PI = acos(-1.0);
+    const double DX1Q = gr->dx1 * gr->dx1, DX3Q = gr->dx3 * gr->dx3;
+    // AK1 indexed by |kx| (0..N1M/2); the reference's table is even in kx.
+    ch->ak1.assign(N1M, 0.0);
+    for (int I = 1; I <= N1M; I++) {
+        int II = I;
+        if (I > N1M / 2 + 1) II = I - N1M;
+        double ani = (II - 1) * 2.0 * PI;
+        double cs = cos(ani / N1M);
+        double den = 11.0 + cs;
+        ch->ak1[I - 1] = 288.0 * DX1Q * (1.0 - cs) / (den * den);
+    }
+    const int N3MH = N3M / 2 + 1;
+    ch->ak3.assign(N3MH, 0.0);
+    for (int K = 1; K <= N3MH; K++) {
+        double ank = (K - 1) * 2.0 * PI;
+        double cs = cos(ank / N3M);
+        double den = 11.0 + cs;
+        ch->ak3[K - 1] = 288.0 * DX3Q * (1.0 - cs) / (den * den);
+    }
+    ch->pmjh.assign(N2 + 1, 0.0);
+    ch->pcj.assign(N2 + 1, 0.0);
+    ch->ppj.assign(N2 + 1, 0.0);
+    const double *DY = gr->dy;
+    auto H = [&](int J) { return gr->h[J - 1]; };
+    for (int JC = 1; JC <= N2M; JC++) {
+        int JP = JC + 1;
+        double FJUM = (JC == 1) ? 0.0 : 1.0, FJUP = (JC == N2M) ? 0.0 : 1.0;
+        ch->pmjh[JC] = FJUM * FJUP * (1.0 / DY[JC] / H(JC)) + (1. - FJUP) * (1.0 / DY[N2M] / H(N2M));
+        ch->pcj[JC] = FJUM * FJUP * (-1.0 / DY[JC] / H(JC) - 1.0 / DY[JC] / H(JP)) +
+                      (1. - FJUP) * (-1.0 / DY[N2M] / H(N2M)) + (1. - FJUM) * (-1.0 / DY[1] / H(2));
+        ch->ppj[JC] = FJUM * FJUP * (1.0 / DY[JC] / H(JP)) + (1. - FJUM) * (1.0 / DY[1] / H(2));
+    }
+}
+
+// Wall-normal Crank-Nicolson factors of GETUH1-3 / TDMAI for the current DT.
+int upload_ycn(c3d_channel *ch, double dt) {
+    const Geo &g = ch->g;
+    const int m = g.n2 + 1, N2M = g.n2m;
+    std::vector<double> t(9 * (size_t)m, 0.0), hm(m), hc(m), hp(m), dym(m), dyc(m), dyp(m);
+    std::vector<double> met(8 * (size_t)m);
+    CK(cudaMemcpy(met.data(), ch->metric, met.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    const double *HP = met.data() + 2 * m, *HC = met.data() + 3 * m, *HM = met.data() + 4 * m;
+    const double *DYP = met.data() + 5 * m, *DYC = met.data() + 6 * m, *DYM = met.data() + 7 * m;
+    const double RE = g.re;
+    for (int c = 0; c < 3; ++c) {
+        double *A = t.data() + (c * 3 + 0) * m, *RB = A + m, *GM = RB + m;
+        const int js = (c == 1) ? 2 : 1;
+        std::vector<double> Av(m), Bv(m), Cv(m);
+        for (int J = js; J <= N2M; ++J) {
+            double FJUP = (J == N2M) ? 0.0 : 1.0;
+            double FJUM = (c == 1) ? ((J == 2) ? 0.0 : 1.0) : ((J == 1) ? 0.0 : 1.0);
+            if (c == 1) {
+                Cv[J] = FJUP * (-0.5 * DYP[J] * (1. / RE)) * dt;
+                Bv[J] = 1.0 + (+0.5 * DYC[J] * (1. / RE)) * dt;
+                Av[J] = FJUM * (-0.5 * DYM[J] * (1. / RE)) * dt;
+            } else {
+                Cv[J] = FJUP * (-0.5 * HP[J] * (1. / RE)) * dt;
+                Bv[J] = 1.0 + (0.5 * HC[J] * (1. / RE)) * dt;
+                Av[J] = FJUM * (-0.5 * HM[J] * (1. / RE)) * dt;
+            }
+        }
+        double bet = 1.0 / Bv[js];
+        RB[js] = bet;
+        GM[js] = Cv[js] * bet;
+        A[js] = Av[js];
+        for (int J = js + 1; J <= N2M; ++J) {
+            bet = 1.0 / (Bv[J] - Av[J] * GM[J - 1]);
+            RB[J] = bet;
+            GM[J] = Cv[J] * bet;
+            A[J] = Av[J];
+        }
+    }
+    CK(cudaMemcpyAsync(ch->ycn, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    ch->dt_cached = dt;
+    return 0;
+}
+
+int check_grid(const c3d_grid *g) {
+    if (!g) { set_error("null grid"); return C3D_EINVAL; }
+    const int n1m = g->n1 - 1, n2m = g->n2 - 1, n3m = g->n3 - 1;
+    if (!n1_ok(n1m) || !fft_len_ok(n1m / 2)) {
+        set_error("N1-1 must be even, >= 16, factor as 2^a*3^b and split into 32 lane chunks of 1,2,3,4,6,8 or 12");
+        return C3D_EINVAL;
+    }
+    if (n3m < 16 || n3m % 16 != 0 || !fft_len_ok(n3m)) {
+        set_error("N3-1 must be a multiple of 16 that factors as 2^a*3^b");
+        return C3D_EINVAL;
+    }
+    if (n2m < 4 || n2m > 4096) { set_error("N2-1 must be in [4, 4096]"); return C3D_EINVAL; }
+    if (!g->y || !g->dy || !g->h || !g->hm || !g->hc || !g->hp || !g->dym || !g->dyc || !g->dyp) {
+        set_error("null metric array");
+        return C3D_EINVAL;
+    }
+    if (!(g->re > 0) || !(g->dx1 > 0) || !(g->dx3 > 0) || !(g->vol > 0) || !(g->alx > 0) || !(g->alz > 0)) {
+        set_error("RE, DX1, DX3, VOL, ALX, ALZ must be positive");
+        return C3D_EINVAL;
+    }
+    if (g->precision != C3D_FP64 && g->precision != C3D_MIXED) {
+        set_error("precision must be C3D_FP64 or C3D_MIXED");
+        return C3D_EINVAL;
+    }
+    if (g->files != 0 || g->wmodel != 0) {
+        set_error("SGS models and wall models are not available in this build (FILES=0, WMODEL=0 only)");
+        return C3D_EINVAL;
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int c3d_create(const c3d_grid *gr, c3d_channel **out) {
+    if (!out) { set_error("null output handle"); return C3D_EINVAL; }
+    *out = nullptr;
+    int rc = check_grid(gr);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        set_error("no CUDA device");
+        return C3D_ENODEV;
+    }
+    if (c3d::g_device >= 0) CK(cudaSetDevice(c3d::g_device));
+    c3d_channel *ch = new c3d_channel();
+    memset((void *)ch, 0, offsetof(c3d_channel, fx));
+    ch->fx = FftPlan();
+    ch->fz = FftPlan();
+    cudaGetDevice(&ch->device);
+    ch->precision = gr->precision;
+    Geo &g = ch->g;
+    g.n1m = gr->n1 - 1;
+    g.n2m = gr->n2 - 1;
+    g.n3m = gr->n3 - 1;
+    g.n2 = gr->n2;
+    g.np = g.n1m * g.n3m;
+    g.nf = (long long)(g.n2 + 1) * g.np;
+    g.n1h = g.n1m / 2 + 1;
+    g.dx1 = gr->dx1;
+    g.dx3 = gr->dx3;
+    g.dx1q = gr->dx1 * gr->dx1;
+    g.dx3q = gr->dx3 * gr->dx3;
+    g.re = gr->re;
+    g.alx = gr->alx;
+    g.aly = gr->aly;
+    g.alz = gr->alz;
+    g.vol = gr->vol;
+    const size_t nf = (size_t)g.nf;
+    const size_t rs = (ch->precision == C3D_MIXED) ? sizeof(float) : sizeof(double);
+    auto fail = [&](int code) {
+        free_channel(ch);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&ch->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(C3D_ECUDA);
+    if (cudaEventCreate(&ch->ev0) != cudaSuccess || cudaEventCreate(&ch->ev1) != cudaSuccess) return fail(C3D_ECUDA);
+    if (dalloc(&ch->u, nf) || dalloc(&ch->v, nf) || dalloc(&ch->w, nf) || dalloc(&ch->p, nf) ||
+        dalloc(&ch->dp, nf) || dalloc(&ch->scal, SCAL_COUNT) || dalloc(&ch->part, 2 * (size_t)g.n2m * g.n3m) ||
+        dalloc(&ch->metric, 8 * (size_t)(g.n2 + 1)) || dalloc(&ch->ycn, 9 * (size_t)(g.n2 + 1)) ||
+        dalloc(&ch->pmj, (size_t)(g.n2 + 1)))
+        return fail(C3D_ENOMEM);
+    const size_t nmodes = (size_t)g.n1h * g.n3m;
+    if (dalloc(&ch->prb, nmodes * g.n2m) || dalloc(&ch->pgam, nmodes * g.n2m)) return fail(C3D_ENOMEM);
+    void **work[] = {&ch->hh[0][0], &ch->hh[0][1], &ch->hh[0][2], &ch->hh[1][0], &ch->hh[1][1], &ch->hh[1][2],
+                     &ch->r[0], &ch->r[1], &ch->r[2], &ch->exy, &ch->exz, &ch->eyz, &ch->ww1, &ch->wsq,
+                     &ch->rdpz, &ch->g1};
+    for (void **q : work) {
+        if (cudaMalloc(q, nf * rs) != cudaSuccess) { set_error("cudaMalloc work"); return fail(C3D_ENOMEM); }
+        cudaMemset(*q, 0, nf * rs);
+    }
+    if (cudaMalloc(&ch->spec, nmodes * g.n2m * 2 * rs) != cudaSuccess) return fail(C3D_ENOMEM);
+    ch->stage_elems = (size_t)(gr->n1 + 1) * (gr->n2 + 1) * (gr->n3 + 1);
+    if (dalloc(&ch->stage, ch->stage_elems)) return fail(C3D_ENOMEM);
+    cudaMemset(ch->u, 0, nf * 8);
+    cudaMemset(ch->v, 0, nf * 8);
+    cudaMemset(ch->w, 0, nf * 8);
+    cudaMemset(ch->p, 0, nf * 8);
+    cudaMemset(ch->dp, 0, nf * 8);
+    cudaMemset(ch->scal, 0, SCAL_COUNT * 8);
+    // metrics indexed by Fortran J: dy(0..N2), h/hp/hc/hm/dyp/dyc/dym(1..N2) (entry 0 = 0)
+    const int m = g.n2 + 1;
+    std::vector<double> met(8 * (size_t)m, 0.0);
+    for (int j = 0; j <= g.n2; ++j) met[j] = gr->dy[j];
+    const double *src[7] = {gr->h, gr->hp, gr->hc, gr->hm, gr->dyp, gr->dyc, gr->dym};
+    for (int q = 0; q < 7; ++q)
+        for (int j = 1; j <= g.n2; ++j) met[(q + 1) * (size_t)m + j] = src[q][j - 1];
+    if (cudaMemcpy(ch->metric, met.data(), met.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) return fail(C3D_ECUDA);
+    g.dy = ch->metric;
+    g.h = ch->metric + m;
+    g.hp = ch->metric + 2 * m;
+    g.hc = ch->metric + 3 * m;
+    g.hm = ch->metric + 4 * m;
+    g.dyp = ch->metric + 5 * m;
+    g.dyc = ch->metric + 6 * m;
+    g.dym = ch->metric + 7 * m;
+    // Poisson metrics and factor tables
+    poisson_metrics(ch, gr);
+    if (cudaMemcpy(ch->pmj, ch->pmjh.data(), (size_t)m * 8, cudaMemcpyHostToDevice) != cudaSuccess) return fail(C3D_ECUDA);
+    rc = launch_poisson_tables(ch);
+    if (rc) return fail(rc);
+    // FFT plans and twiddles: [x: N1M/2][z: N3M][x post-processing: N1M/2+1]
+    ch->fx = make_plan(g.n1m / 2);
+    ch->fz = make_plan(g.n3m);
+    const int nx = g.n1m / 2, nz = g.n3m, np = g.n1m / 2 + 1;
+    std::vector<double2> tw(nx + nz + np);
+    std::vector<float2> tw32(nx + nz + np);
+    for (int q = 0; q < nx; ++q) tw[q] = make_double2(cos(2 * M_PI * q / nx), -sin(2 * M_PI * q / nx));
+    for (int q = 0; q < nz; ++q) tw[nx + q] = make_double2(cos(2 * M_PI * q / nz), -sin(2 * M_PI * q / nz));
+    for (int q = 0; q < np; ++q)
+        tw[nx + nz + q] = make_double2(cos(2 * M_PI * q / g.n1m), -sin(2 * M_PI * q / g.n1m));
+    for (size_t q = 0; q < tw.size(); ++q) tw32[q] = make_float2((float)tw[q].x, (float)tw[q].y);
+    if (dalloc(&ch->tw64, tw.size()) || dalloc(&ch->tw32, tw32.size())) return fail(C3D_ENOMEM);
+    cudaMemcpy(ch->tw64, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    cudaMemcpy(ch->tw32, tw32.data(), tw32.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    ch->fx.tw64 = ch->tw64;
+    ch->fx.tw32 = ch->tw32;
+    ch->fz.tw64 = ch->tw64 + nx;
+    ch->fz.tw32 = ch->tw32 + nx;
+    ch->dt_cached = -1.0;
+    ch->cur = 0;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        set_error(std::string("create: ") + cudaGetErrorString(e));
+        return fail(C3D_ECUDA);
+    }
+    *out = ch;
+    return 0;
+}
+
+int c3d_destroy(c3d_channel *ch) {
+    if (!ch) return C3D_EINVAL;
+    cudaSetDevice(ch->device);
+    cudaStreamSynchronize(ch->stream);
+    free_channel(ch);
+    return 0;
+}
+
+static int h2d(c3d_channel *ch, const double *src, size_t n) {
+    CK(cudaMemcpyAsync(ch->stage, src, n * sizeof(double), cudaMemcpyHostToDevice, ch->stream));
+    return 0;
+}
+static int d2h(c3d_channel *ch, double *dst, size_t n) {
+    CK(cudaMemcpyAsync(dst, ch->stage, n * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    return 0;
+}
+
+int c3d_upload(c3d_channel *ch, const double *u, const double *p, const double *hh, const double *sgsvis) {
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    if (sgsvis) { set_error("SGSVIS is not used when FILES=0; pass NULL"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    const size_t n3 = ch->stage_elems;   // one component of U / HH
+    const Geo &g = ch->g;
+    const size_t np_ = (size_t)(g.n1m + 1) * g.n2 * (g.n3m + 1);
+    for (int c = 0; c < 3; ++c) {
+        if (u) {
+            int rc = h2d(ch, u + c * n3, n3);
+            if (rc) return rc;
+            launch_repack(ch, 0, 0, c);
+        }
+    }
+    if (p) {
+        int rc = h2d(ch, p, np_);
+        if (rc) return rc;
+        launch_repack(ch, 0, 1, 0);
+    }
+    for (int c = 0; c < 3; ++c) {
+        if (hh) {
+            int rc = h2d(ch, hh + c * n3, n3);
+            if (rc) return rc;
+            launch_repack(ch, 0, 2, c);
+        }
+    }
+    CK(cudaStreamSynchronize(ch->stream));
+    CK(cudaGetLastError());
+    ch->have_state = 1;
+    return 0;
+}
+
+int c3d_download(c3d_channel *ch, double *u, double *p, double *hh, double *sgsvis) {
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    (void)sgsvis;
+    cudaSetDevice(ch->device);
+    const size_t n3 = ch->stage_elems;
+    const Geo &g = ch->g;
+    const size_t np_ = (size_t)(g.n1m + 1) * g.n2 * (g.n3m + 1);
+    for (int c = 0; c < 3; ++c) {
+        if (u) {
+            launch_repack(ch, 1, 0, c);
+            int rc = d2h(ch, u + c * n3, n3);
+            if (rc) return rc;
+        }
+    }
+    if (p) {
+        launch_repack(ch, 1, 1, 0);
+        int rc = d2h(ch, p, np_);
+        if (rc) return rc;
+    }
+    for (int c = 0; c < 3; ++c) {
+        if (hh) {
+            launch_repack(ch, 1, 2, c);
+            int rc = d2h(ch, hh + c * n3, n3);
+            if (rc) return rc;
+        }
+    }
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int c3d_host_register(void *ptr, size_t bytes) {
+    if (!ptr || !bytes) { set_error("null pointer or zero size"); return C3D_EINVAL; }
+    CK(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+    return 0;
+}
+
+int c3d_host_unregister(void *ptr) {
+    if (!ptr) { set_error("null pointer"); return C3D_EINVAL; }
+    CK(cudaHostUnregister(ptr));
+    return 0;
+}
+
+int c3d_upload_wall(c3d_channel *ch, const double *tauw, const double *taub) {
+    (void)tauw;
+    (void)taub;
+    if (!ch) return C3D_EINVAL;
+    set_error("wall models are not available in this build");
+    return C3D_EINVAL;
+}
+
+int c3d_download_wall(c3d_channel *ch, double *tauw, double *taub) {
+    return c3d_upload_wall(ch, tauw, taub);
+}
+
+static int step_common(c3d_channel *ch, double dt, double *presg, double *presg3, bool sync) {
+    if (!(dt > 0) || !isfinite(dt)) { set_error("dt must be positive and finite"); return C3D_EINVAL; }
+    if (dt != ch->dt_cached) {
+        int rc = upload_ycn(ch, dt);
+        if (rc) return rc;
+    }
+    double pg[2] = {presg ? *presg : 0.0, presg3 ? *presg3 : 0.0};
+    CK(cudaMemcpyAsync(ch->scal + SCAL_PRESG, pg, 2 * sizeof(double), cudaMemcpyHostToDevice, ch->stream));
+    CK(cudaEventRecord(ch->ev0, ch->stream));
+    int nl = 0;
+    int rc = launch_step(ch, dt, &nl);
+    if (rc) return rc;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ch->ev1, ch->stream));
+    ch->last_launches = nl;
+    if (sync) {
+        CK(cudaMemcpyAsync(pg, ch->scal + SCAL_PRESG, 2 * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
+        CK(cudaStreamSynchronize(ch->stream));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ch->ev0, ch->ev1);
+        ch->last_ms = ms;
+        if (presg) *presg = pg[0];
+        if (presg3) *presg3 = pg[1];
+    }
+    return 0;
+}
+
+int c3d_step(c3d_channel *ch, int ntime, double dt, double *presg, double *presg3) {
+    (void)ntime;
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    if (!presg || !presg3) { set_error("null PRESG/PRESG3"); return C3D_EINVAL; }
+    if (!ch->have_state) { set_error("c3d_upload must be called before c3d_step"); return C3D_ESTATE; }
+    cudaSetDevice(ch->device);
+    return step_common(ch, dt, presg, presg3, true);
+}
+
+int c3d_project(c3d_channel *ch) {
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    if (!ch->have_state) { set_error("c3d_upload must be called before c3d_project"); return C3D_ESTATE; }
+    cudaSetDevice(ch->device);
+    int nl = 0;
+    int rc = launch_project(ch, &nl);
+    if (rc) return rc;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ch->stream));
+    return 0;
+}
+
+int c3d_diagnose(c3d_channel *ch, c3d_diag *out) {
+    if (!ch || !out) { set_error("null argument"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    int nl = 0;
+    int rc = launch_diag(ch, &nl);
+    if (rc) return rc;
+    double s[SCAL_COUNT];
+    CK(cudaMemcpyAsync(s, ch->scal, sizeof(s), cudaMemcpyDeviceToHost, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    out->divmax = s[SCAL_DIVMAX];
+    out->cflm = s[SCAL_CFL];
+    out->flow1 = s[SCAL_FLOW1];
+    out->flow3 = s[SCAL_FLOW3];
+    out->wsm[0] = s[SCAL_WSM];
+    out->wsm[1] = s[SCAL_WSM + 1];
+    out->wsm[2] = s[SCAL_WSM + 2];
+    out->nonfinite = s[SCAL_NONFIN] != 0.0;
+    return out->nonfinite ? C3D_ENONFINITE : 0;
+}
+
+int c3d_getup(c3d_channel *ch, double *u, double *p, double *hh, double *sgsvis, int ntime, double dt,
+              double *presg, double *presg3) {
+    if (!ch || !u || !p || !hh) { set_error("null argument"); return C3D_EINVAL; }
+    int rc = c3d_upload(ch, u, p, hh, sgsvis);
+    if (rc) return rc;
+    rc = c3d_step(ch, ntime, dt, presg, presg3);
+    if (rc) return rc;
+    return c3d_download(ch, u, p, hh, nullptr);
+}
+
+int c3d_sync(c3d_channel *ch) {
+    if (!ch) return C3D_EINVAL;
+    CK(cudaStreamSynchronize(ch->stream));
+    return 0;
+}
+
+int c3d_last_step_stats(c3d_channel *ch, double *ms, int *launches) {
+    if (!ch) return C3D_EINVAL;
+    if (ms) *ms = ch->last_ms;
+    if (launches) *launches = ch->last_launches;
+    return 0;
+}
+
+// ---- batched ensemble ----------------------------------------------------------
+struct c3d_batch {
+    std::vector<c3d_channel *> ch;
+};
+
+int c3d_batch_create(int nchan, const c3d_grid *grids, c3d_batch **out) {
+    if (!out || !grids || nchan <= 0) { set_error("bad batch arguments"); return C3D_EINVAL; }
+    *out = nullptr;
+    c3d_batch *b = new c3d_batch();
+    for (int i = 0; i < nchan; ++i) {
+        c3d_channel *c = nullptr;
+        int rc = c3d_create(&grids[i], &c);
+        if (rc) {
+            for (auto *q : b->ch) c3d_destroy(q);
+            delete b;
+            return rc;
+        }
+        b->ch.push_back(c);
+    }
+    *out = b;
+    return 0;
+}
+
+int c3d_batch_destroy(c3d_batch *b) {
+    if (!b) return C3D_EINVAL;
+    for (auto *q : b->ch) c3d_destroy(q);
+    delete b;
+    return 0;
+}
+
+int c3d_batch_channel(c3d_batch *b, int index, c3d_channel **ch) {
+    if (!b || !ch || index < 0 || index >= (int)b->ch.size()) { set_error("bad batch index"); return C3D_EINVAL; }
+    *ch = b->ch[index];
+    return 0;
+}
+
+int c3d_batch_step(c3d_batch *b, int ntime, const double *dt, double *presg, double *presg3) {
+    if (!b || !dt || !presg || !presg3) { set_error("null argument"); return C3D_EINVAL; }
+    for (size_t i = 0; i < b->ch.size(); ++i) {
+        int rc = c3d_step(b->ch[i], ntime, dt[i], &presg[i], &presg3[i]);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+int c3d_batch_sync(c3d_batch *b) {
+    if (!b) return C3D_EINVAL;
+    for (auto *q : b->ch) {
+        int rc = c3d_sync(q);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,230 @@
+// c3d_dev.cuh -- device-side layout and line-solver primitives of the GB300 channel step.
+//
+// Layout in HBM.  Every 3-D field is plane-major: element (i, j, k) of a field lives at
+//   ((j * N3M) + k) * N1M + i,   i in [0,N1M), k in [0,N3M), j in [0, N2]
+// with i = I-1, k = K-1 and j = J of the reference's Fortran indices.  One x-z plane
+// (N1M*N3M values) is contiguous, rows along x are contiguous, and the wall planes
+// j = 0 and j = N2 are stored like interior planes.  The periodic x and z directions
+// carry no halo: the kernels wrap indices.
+//
+// Compact (Pade) operators.  The reference solves constant-coefficient cyclic systems
+//   a x_{i-1} + b x_i + a x_{i+1} = d_i                 (CTDMA11/33, CTDMA1J/3I)
+// by bordered LU.  With beta = b/a and r the root of r^2 + beta r + 1 = 0 with |r| < 1,
+//   tridiag(a, b, a) = (-a/r) (1 - r S)(1 - r S^-1)      (S = cyclic shift)
+// so x = s * B(F(d)) with s = -r/a, F: y_i = d_i + r y_{i-1} and B: z_i = y_i + r z_{i+1},
+// both cyclic.  The kernels evaluate these two first-order recurrences:
+//   * along x (contiguous rows): one warp per row, every lane owns C consecutive points,
+//     and the cyclic carries between lanes come from warp-shuffle scans of affine maps;
+//   * along z (strided columns): one thread per (column, segment of L points); the cyclic
+//     start values come from a warm-up of M points, M chosen so |r|^M is below the
+//     working precision's rounding unit.
+// The result equals the reference's bordered-LU solution to rounding.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace c3d {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Coefficients of one constant-coefficient cyclic operator in a given precision.
+template <typename R>
+struct Cyc {
+    R r;      // root of r^2 + (b/a) r + 1 = 0, |r| < 1
+    R s;      // output scale -r/a
+    int m;    // warm-up length for segment solves
+};
+
+// Geometry and constants handed to every kernel by value.
+struct Geo {
+    int n1m, n2m, n3m, n2;   // cells; n2 = N2 = n2m + 1
+    int np;                  // n1m * n3m (plane)
+    long long nf;            // (n2 + 1) * np (field)
+    int n1h;                 // n1m/2 + 1 (half spectrum along x)
+    double dx1, dx3, dx1q, dx3q, re, alx, aly, alz, vol;
+    // y metrics indexed by Fortran J (arrays of n2+1 values, entry 0 = DY(0) etc.)
+    const double *dy, *h, *hp, *hc, *hm, *dyp, *dyc, *dym;
+};
+
+__host__ __device__ inline long long fidx(const Geo &g, int i, int j, int k) {
+    return ((long long)j * g.n3m + k) * g.n1m + i;
+}
+
+// ---------------------------------------------------------------------------------
+// x direction: warp per row, lane chunks of C points, P = N1M / C active lanes.
+// ---------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T lane_prev(T last, int lane, int P) {
+    int src = (lane == 0) ? P - 1 : lane - 1;
+    return __shfl_sync(FULL, last, src);
+}
+template <typename T>
+__device__ __forceinline__ T lane_next(T first, int lane, int P) {
+    int src = (lane + 1 >= P) ? 0 : lane + 1;
+    return __shfl_sync(FULL, first, src);
+}
+
+// Cyclic solve on the warp's row held as lane chunks x[0..C); in place, returns s*B(F(x)).
+template <typename R, int C>
+__device__ __forceinline__ void xsolve(R (&x)[C], int lane, int P, const Cyc<R> &c) {
+    const bool act = lane < P;
+    const R r = c.r;
+    R y = R(0), m = R(1);
+#pragma unroll
+    for (int t = 0; t < C; ++t) {
+        y = x[t] + r * y;
+        m *= r;
+    }
+    R e = act ? y : R(0);
+    if (!act) m = R(1);
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        R ep = __shfl_up_sync(FULL, e, off), mp = __shfl_up_sync(FULL, m, off);
+        if (lane >= off) {
+            e = e + m * ep;
+            m = m * mp;
+        }
+    }
+    {
+        R et = __shfl_sync(FULL, e, 31), mt = __shfl_sync(FULL, m, 31);
+        R y0 = et / (R(1) - mt);
+        R ex = __shfl_up_sync(FULL, e, 1), mx = __shfl_up_sync(FULL, m, 1);
+        y = (lane == 0) ? y0 : ex + mx * y0;
+    }
+#pragma unroll
+    for (int t = 0; t < C; ++t) {
+        y = x[t] + r * y;
+        x[t] = y;
+    }
+    R z = R(0);
+    m = R(1);
+#pragma unroll
+    for (int t = C - 1; t >= 0; --t) {
+        z = x[t] + r * z;
+        m *= r;
+    }
+    e = act ? z : R(0);
+    if (!act) m = R(1);
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        R en = __shfl_down_sync(FULL, e, off), mn = __shfl_down_sync(FULL, m, off);
+        if (lane + off < 32) {
+            e = e + m * en;
+            m = m * mn;
+        }
+    }
+    {
+        R e0 = __shfl_sync(FULL, e, 0), m0 = __shfl_sync(FULL, m, 0);
+        R z0 = e0 / (R(1) - m0);
+        R en1 = __shfl_down_sync(FULL, e, 1), mn1 = __shfl_down_sync(FULL, m, 1);
+        z = (lane == 31) ? z0 : en1 + mn1 * z0;
+    }
+    const R s = c.s;
+#pragma unroll
+    for (int t = C - 1; t >= 0; --t) {
+        z = x[t] + r * z;
+        x[t] = s * z;
+    }
+}
+
+// Lane-chunk load/store of one row (row pointer + lane*C).  Inactive lanes are skipped.
+template <int C>
+__device__ __forceinline__ void row_load(double (&v)[C], const double *__restrict__ row, int lane, int P) {
+    if (lane < P) {
+        const double *p = row + lane * C;
+        if constexpr (C % 2 == 0) {
+#pragma unroll
+            for (int t = 0; t < C; t += 2) {
+                double2 q = __ldg(reinterpret_cast<const double2 *>(p + t));
+                v[t] = q.x;
+                v[t + 1] = q.y;
+            }
+        } else {
+#pragma unroll
+            for (int t = 0; t < C; ++t) v[t] = __ldg(p + t);
+        }
+    } else {
+#pragma unroll
+        for (int t = 0; t < C; ++t) v[t] = 0.0;
+    }
+}
+template <int C>
+__device__ __forceinline__ void row_load(float (&v)[C], const float *__restrict__ row, int lane, int P) {
+    if (lane < P) {
+        const float *p = row + lane * C;
+        if constexpr (C % 4 == 0) {
+#pragma unroll
+            for (int t = 0; t < C; t += 4) {
+                float4 q = __ldg(reinterpret_cast<const float4 *>(p + t));
+                v[t] = q.x; v[t + 1] = q.y; v[t + 2] = q.z; v[t + 3] = q.w;
+            }
+        } else if constexpr (C % 2 == 0) {
+#pragma unroll
+            for (int t = 0; t < C; t += 2) {
+                float2 q = __ldg(reinterpret_cast<const float2 *>(p + t));
+                v[t] = q.x; v[t + 1] = q.y;
+            }
+        } else {
+#pragma unroll
+            for (int t = 0; t < C; ++t) v[t] = __ldg(p + t);
+        }
+    } else {
+#pragma unroll
+        for (int t = 0; t < C; ++t) v[t] = 0.f;
+    }
+}
+template <typename T, int C>
+__device__ __forceinline__ void row_store(T *__restrict__ row, const T (&v)[C], int lane, int P) {
+    if (lane < P) {
+        T *p = row + lane * C;
+#pragma unroll
+        for (int t = 0; t < C; ++t) p[t] = v[t];
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// z direction: thread per (column, segment of L points) with warm-up M.
+// D(k) is a functor returning the right-hand side at wrapped index k in [0,n).
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ int wrapi(int q, int n) {
+    while (q < 0) q += n;
+    while (q >= n) q -= n;
+    return q;
+}
+
+template <typename R, int L, typename F>
+__device__ __forceinline__ void zseg(R (&out)[L], int k0, int n, const Cyc<R> &c, F D) {
+    const R r = c.r;
+    R y = R(0);
+    int kk = wrapi(k0 - c.m, n);
+    for (int q = 0; q < c.m; ++q) {
+        y = D(kk) + r * y;
+        kk = (kk + 1 == n) ? 0 : kk + 1;
+    }
+    R ys[L];
+#pragma unroll
+    for (int t = 0; t < L; ++t) {
+        y = D(kk) + r * y;
+        ys[t] = y;
+        kk = (kk + 1 == n) ? 0 : kk + 1;
+    }
+    R acc = R(0), pw = R(1);
+    for (int q = 0; q < c.m; ++q) {
+        y = D(kk) + r * y;
+        acc = acc + pw * y;
+        pw *= r;
+        kk = (kk + 1 == n) ? 0 : kk + 1;
+    }
+    R z = acc;
+    const R s = c.s;
+#pragma unroll
+    for (int t = L - 1; t >= 0; --t) {
+        z = ys[t] + r * z;
+        out[t] = s * z;
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ R to_r(double v) { return (R)v; }
+
+}  // namespace c3d

@@ -1,0 +1,108 @@
+// c3d_internal.h -- channel state shared by the C-ABI layer and the step kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+#include "../../include/c3d.h"
+#include "c3d_dev.cuh"
+
+namespace c3d {
+
+// Radix plan of one FFT length (radices 4, 2, 3 in that order) with its twiddle table
+// tw[q] = exp(-2 pi i q / n), q in [0, n).
+struct FftPlan {
+    int n;
+    int nst;
+    int rad[16];
+    const double2 *tw64;
+    const float2 *tw32;
+};
+
+// Everything one step's kernels need, passed by value.  R is the working precision of
+// the intermediates (double for the FP64 form, float for the mixed form); the velocity,
+// pressure and reductions are always FP64.
+template <typename R>
+struct StepArgs {
+    Geo g;
+    double *u, *v, *w, *p;              // state, FP64
+    R *hh[3];                           // nonlinear terms of this step (written)
+    const R *ho[3];                     // nonlinear terms of the previous step (AB2)
+    R *r[3];                            // RUH -> delta (CN increments)
+    R *exy, *exz, *eyz, *ww1, *wsq;     // edge products and interpolants
+    R *rdpz, *g1;                       // z part of div(UH)/DT; x-gradient of DP
+    double *dp;                         // pressure increment, FP64 (planes 1..N2M)
+    void *spec;                         // half spectrum [j][kz][kx] of RDP / DP (R complex)
+    double *scal;                       // device scalars (see SCAL_*)
+    double *part;                       // per-row partial sums for the bulk-flow forcing
+    Cyc<R> c6x, c10x, c22x, c6z, c10z, c22z, cnx, cnz;
+    // CN wall-normal factors, 3 components x (n2+1): A, RBET, GAM (FP64)
+    const double *ycn;
+    // Poisson factor tables [j][mode] (FP64): reciprocal pivots and multipliers
+    const double *prb, *pgam;
+    const double *pmj;                  // PMJ(J), n2+1 values
+    FftPlan fx, fz;                     // complex FFT of length N1M/2 (x) and N3M (z)
+    const double2 *twx64;               // exp(-2 pi i k / N1M), k in [0, N1M/2]
+    const float2 *twx32;
+    double dt;
+    int bulk;                           // apply the bulk-flow forcing (GETUP) or not (projection)
+    double dtproj;                      // DT used by the projection (1 for c3d_project)
+};
+
+enum {
+    SCAL_PRESG = 0,
+    SCAL_PRESG3 = 1,
+    SCAL_DMPRESG = 2,
+    SCAL_DMPRESG3 = 3,
+    SCAL_DIVMAX = 4,
+    SCAL_CFL = 5,
+    SCAL_FLOW1 = 6,
+    SCAL_FLOW3 = 7,
+    SCAL_WSM = 8,      // 3 values
+    SCAL_NONFIN = 11,
+    SCAL_COUNT = 16
+};
+
+}  // namespace c3d
+
+struct c3d_channel {
+    c3d::Geo g;
+    int precision;
+    int device;
+    cudaStream_t stream;
+    cudaEvent_t ev0, ev1;
+    // FP64 state and metrics
+    double *u, *v, *w, *p, *dp, *scal, *part;
+    double *metric;           // 8 arrays of n2+1: dy,h,hp,hc,hm,dyp,dyc,dym
+    double *ycn;              // 3 x 3 x (n2+1)
+    double *prb, *pgam, *pmj;
+    double2 *tw64;            // x-FFT table, z-FFT table, x post-processing table
+    float2 *tw32;
+    // working arrays (R = double or float), stored untyped
+    void *hh[2][3];
+    int cur;                  // index of the current HH set
+    void *r[3];
+    void *exy, *exz, *eyz, *ww1, *wsq, *rdpz, *g1;
+    void *spec;
+    double *stage;            // device staging for Fortran-layout transfers
+    size_t stage_elems;
+    double *pinned;           // pinned host bounce buffer for the host-array path
+    size_t pinned_elems;
+    double dt_cached;
+    int have_state;
+    float last_ms;
+    int last_launches;
+    c3d::FftPlan fx, fz;
+    std::vector<double> ak1, ak3, pcj, ppj, pmjh;
+    // wall model
+    double *tauw, *taub;      // (N1M*N3M*2) device, plane layout [w][k][i]
+};
+
+namespace c3d {
+// Step drivers (c3d_step.cu)
+int launch_step(c3d_channel *ch, double dt, int *launches);
+int launch_project(c3d_channel *ch, int *launches);
+int launch_diag(c3d_channel *ch, int *launches);
+int launch_poisson_tables(c3d_channel *ch);
+int launch_repack(c3d_channel *ch, int dir, int what, int comp);  // 0: Fortran->device
+void set_error(const std::string &msg);
+}  // namespace c3d

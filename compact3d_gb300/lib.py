@@ -1,0 +1,180 @@
+"""ctypes binding of libc3d.so and a Python mirror of the reference's step interface.
+
+The reference exposes no library API: the driver calls ``GETUP(U,P,HH,SS,NTIME,PRESG,
+PRESG3,SGSVIS)`` (compact3d.f:879) and the diagnostics ``DIVCHECK``, ``CFL``, ``CHKMF``
+and ``WALLSS`` with Fortran arrays.  ``Channel`` offers the same calls with numpy arrays in
+the same Fortran layouts, implemented by the CUDA library through its C-ABI.
+
+There is no CPU fallback: if libc3d.so cannot be loaded, or no CUDA device is present,
+the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .grid import C3D_FP64, C3D_MIXED, Grid, c3d_grid
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libc3d.so")
+
+C3D_OK = 0
+ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ENOTCONV", -5: "ENONFINITE",
+          -6: "ESTATE", -7: "ENODEV"}
+
+# Every function declared in include/c3d.h, with its ctypes signature.
+_vp, _ip, _dp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
+
+
+class c3d_diag(ctypes.Structure):
+    _fields_ = [("divmax", ctypes.c_double), ("cflm", ctypes.c_double),
+                ("flow1", ctypes.c_double), ("flow3", ctypes.c_double),
+                ("wsm", ctypes.c_double * 3), ("nonfinite", ctypes.c_int)]
+
+
+SIGNATURES = {
+    "c3d_error_string": (ctypes.c_char_p, [_ip]),
+    "c3d_last_error": (ctypes.c_char_p, []),
+    "c3d_version": (_ip, []),
+    "c3d_set_device": (_ip, [_ip]),
+    "c3d_create": (_ip, [ctypes.POINTER(c3d_grid), ctypes.POINTER(_vp)]),
+    "c3d_destroy": (_ip, [_vp]),
+    "c3d_upload": (_ip, [_vp, _dp, _dp, _dp, _dp]),
+    "c3d_download": (_ip, [_vp, _dp, _dp, _dp, _dp]),
+    "c3d_upload_wall": (_ip, [_vp, _dp, _dp]),
+    "c3d_download_wall": (_ip, [_vp, _dp, _dp]),
+    "c3d_step": (_ip, [_vp, _ip, ctypes.c_double, _dp, _dp]),
+    "c3d_diagnose": (_ip, [_vp, ctypes.POINTER(c3d_diag)]),
+    "c3d_getup": (_ip, [_vp, _dp, _dp, _dp, _dp, _ip, ctypes.c_double, _dp, _dp]),
+    "c3d_project": (_ip, [_vp]),
+    "c3d_host_register": (_ip, [_vp, ctypes.c_size_t]),
+    "c3d_host_unregister": (_ip, [_vp]),
+    "c3d_sync": (_ip, [_vp]),
+    "c3d_last_step_stats": (_ip, [_vp, _dp, ctypes.POINTER(_ip)]),
+    "c3d_batch_create": (_ip, [_ip, ctypes.POINTER(c3d_grid), ctypes.POINTER(_vp)]),
+    "c3d_batch_destroy": (_ip, [_vp]),
+    "c3d_batch_channel": (_ip, [_vp, _ip, ctypes.POINTER(_vp)]),
+    "c3d_batch_step": (_ip, [_vp, _ip, _dp, _dp, _dp]),
+    "c3d_batch_sync": (_ip, [_vp]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libc3d.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing; run __graft_entry__.build() or "
+                               "python -m compact3d_gb300.build")
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class C3DError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        L = load()
+        msg = L.c3d_last_error().decode(errors="replace")
+        super().__init__(f"{where}: {ERRORS.get(code, code)} ({msg})")
+        self.code = code
+
+
+def check(code: int, where: str):
+    if code != C3D_OK:
+        raise C3DError(code, where)
+
+
+def _p(a):
+    if a is None:
+        return None
+    if a.dtype != np.float64 or not (a.flags.f_contiguous or a.ndim == 1):
+        raise TypeError("arrays must be float64 in Fortran order")
+    return a.ctypes.data_as(_dp)
+
+
+class Channel:
+    """One channel on the GPU; arrays use the reference's Fortran layouts."""
+
+    def __init__(self, grid: Grid, precision: int | None = None):
+        self.grid = grid
+        self.precision = grid.precision if precision is None else precision
+        self._gs = grid.struct(self.precision)
+        h = _vp()
+        check(load().c3d_create(ctypes.byref(self._gs), ctypes.byref(h)), "c3d_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().c3d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, U, P, HH):
+        check(load().c3d_upload(self.h, _p(U), _p(P), _p(HH), None), "c3d_upload")
+
+    def download(self, U=None, P=None, HH=None):
+        g = self.grid
+        U = g.zeros_u() if U is None else U
+        P = g.zeros_p() if P is None else P
+        HH = g.zeros_u() if HH is None else HH
+        check(load().c3d_download(self.h, _p(U), _p(P), _p(HH), None), "c3d_download")
+        return U, P, HH
+
+    def step(self, ntime: int, dt: float, presg: float, presg3: float):
+        """GETUP on the device-resident state; returns the new (PRESG, PRESG3)."""
+        a = (ctypes.c_double * 1)(presg)
+        b = (ctypes.c_double * 1)(presg3)
+        check(load().c3d_step(self.h, ntime, dt, a, b), "c3d_step")
+        return a[0], b[0]
+
+    def getup(self, U, P, HH, ntime: int, dt: float, presg: float, presg3: float):
+        """GETUP(U,P,HH,SS,NTIME,PRESG,PRESG3,SGSVIS) with host arrays updated in place."""
+        a = (ctypes.c_double * 1)(presg)
+        b = (ctypes.c_double * 1)(presg3)
+        check(load().c3d_getup(self.h, _p(U), _p(P), _p(HH), None, ntime, dt, a, b), "c3d_getup")
+        return a[0], b[0]
+
+    def project(self):
+        check(load().c3d_project(self.h), "c3d_project")
+
+    def diagnose(self) -> dict:
+        d = c3d_diag()
+        rc = load().c3d_diagnose(self.h, ctypes.byref(d))
+        if rc not in (C3D_OK, -5):
+            check(rc, "c3d_diagnose")
+        return dict(divmax=d.divmax, cflm=d.cflm, flow1=d.flow1, flow3=d.flow3,
+                    wsm=np.array(d.wsm[:]), nonfinite=bool(d.nonfinite))
+
+    def sync(self):
+        check(load().c3d_sync(self.h), "c3d_sync")
+
+    def last_step_stats(self):
+        ms = (ctypes.c_double * 1)()
+        n = (ctypes.c_int * 1)()
+        check(load().c3d_last_step_stats(self.h, ms, n), "c3d_last_step_stats")
+        return ms[0], n[0]
+
+
+def host_register(a: np.ndarray):
+    check(load().c3d_host_register(a.ctypes.data, a.nbytes), "c3d_host_register")
+
+
+def host_unregister(a: np.ndarray):
+    check(load().c3d_host_unregister(a.ctypes.data), "c3d_host_unregister")
+
+
+__all__ = ["Channel", "load", "C3DError", "host_register", "host_unregister", "C3D_FP64",
+           "C3D_MIXED", "SIGNATURES"]

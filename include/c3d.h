@@ -24,6 +24,8 @@
 #ifndef C3D_H
 #define C3D_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -127,6 +129,10 @@ int c3d_getup(c3d_channel *ch, double *u, double *p, double *hh,
  * U taken as the intermediate velocity and DT = 1, no bulk-flow forcing).
  * Used to make a synthetic initial condition discretely divergence-free. */
 int c3d_project(c3d_channel *ch);
+/* Page-locks (pins) a host array so that c3d_upload / c3d_download / c3d_getup
+ * move it by DMA at full link bandwidth; a driver calls it once per field array. */
+int c3d_host_register(void *ptr, size_t bytes);
+int c3d_host_unregister(void *ptr);
 /* Blocks until all work queued on the channel's stream has finished. */
 int c3d_sync(c3d_channel *ch);
 /* Device time of the last c3d_step in milliseconds (CUDA events on the

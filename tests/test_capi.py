@@ -1,0 +1,82 @@
+"""The C-ABI library loads on a machine without a GPU, exports every function that
+include/c3d.h declares, and rejects bad arguments before touching a device."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from compact3d_gb300 import build, lib
+from compact3d_gb300.grid import c3d_grid, make_grid
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    build.build()
+    return lib.load()
+
+
+def declared():
+    src = open(os.path.join(ROOT, "include", "c3d.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(c3d_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_every_declared_symbol_is_exported(L):
+    names = declared()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(lib.SIGNATURES), "Python signatures out of sync with c3d.h"
+
+
+def test_error_strings(L):
+    for code in (0, -1, -2, -3, -4, -5, -6, -7, -99):
+        assert L.c3d_error_string(code)
+
+
+def test_version(L):
+    assert L.c3d_version() >= 10000
+
+
+@pytest.mark.parametrize("bad", [dict(n1m=50), dict(n3m=40), dict(n2m=2), dict(n1m=10)])
+def test_create_rejects_bad_extents(L, bad):
+    g, _ = make_grid("small32", **bad) if "n2m" not in bad or bad["n2m"] > 3 else (None, None)
+    if g is None:
+        g, _ = make_grid("small32")
+        s = g.struct()
+        s.n2 = 3
+    else:
+        s = g.struct()
+    h = ctypes.c_void_p()
+    assert L.c3d_create(ctypes.byref(s), ctypes.byref(h)) == -1
+    assert L.c3d_last_error()
+
+
+def test_create_rejects_null_metrics(L):
+    g, _ = make_grid("small32")
+    s = g.struct()
+    s.hp = None
+    h = ctypes.c_void_p()
+    assert L.c3d_create(ctypes.byref(s), ctypes.byref(h)) == -1
+
+
+def test_create_rejects_bad_precision_and_models(L):
+    g, _ = make_grid("small32")
+    for field, val in (("precision", 7), ("files", 3), ("re", -1.0)):
+        s = g.struct()
+        setattr(s, field, val)
+        h = ctypes.c_void_p()
+        assert L.c3d_create(ctypes.byref(s), ctypes.byref(h)) == -1
+
+
+def test_null_handles(L):
+    assert L.c3d_create(None, None) == -1
+    assert L.c3d_step(None, 1, 0.001, None, None) == -1
+    assert L.c3d_destroy(None) == -1
+    assert L.c3d_upload(None, None, None, None, None) == -1
+    assert L.c3d_diagnose(None, None) == -1
+    assert L.c3d_batch_step(None, 1, None, None, None) == -1
+    assert L.c3d_sync(None) == -1
