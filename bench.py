@@ -1,0 +1,388 @@
+#!/usr/bin/env python3
+"""Benchmark of the compact3d channel time step on GB300: grid-point-substeps/s.
+
+One "step" is one call of GETUP (compact3d.f:879-960) on the whole channel; the reference
+is single-stage AB2/Crank-Nicolson, so one substep is one step and the metric is
+N1M*N2M*N3M * steps / second.
+
+Arms
+  default (ours)     the CUDA library through its C-ABI, on the workload named by
+                     --workload (default channel384: 384 x 257 x 384 points, Re_tau ~550),
+                     in the FP32-mixed form (--form), with the plain FP64 form measured in
+                     the same run for comparison and the relative L2 error of the mixed form
+                     against the FP64 form after the same steps.
+  --impl reference   the FP64 OpenMP CPU restatement of the reference step (oracle/) on
+                     all host cores, on a bounded sample of the same workload.
+
+Multi-GPU: under torchrun every rank advances its own channel (independent replicas, no
+collective on the data path); the time is the max over ranks and ``value`` the sum of all
+ranks' points / that time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from compact3d_gb300 import ic  # noqa: E402
+from compact3d_gb300.grid import C3D_FP64, C3D_MIXED, WORKLOADS, make_grid  # noqa: E402
+
+METRIC = "grid-pt-substeps/s on 1 GB300: FP32-mixed & batched vs FP64, at stated L2 err"
+UNIT = "grid-pt-substeps/s"
+
+
+# ------------------------------------------------------------------------------------
+# distributed plumbing (only when launched by torchrun with WORLD_SIZE > 1)
+# ------------------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------------------------
+# clocks during the timed region
+# ------------------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_for(workload: str, form: str, kernel: str):
+    """DRAM bytes per launch of `kernel` from a committed ncu summary, if there is one."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    e = d.get(f"{workload}/{form}/{kernel}")
+    return None if e is None else float(e["bytes_per_launch"])
+
+
+# ------------------------------------------------------------------------------------
+# CPU reference (oracle restatement of the reference's OpenMP path)
+# ------------------------------------------------------------------------------------
+def cpu_reference(workload: str, steps: int, warmup: int, budget_s: float = 150.0):
+    """Run the FP64 OpenMP oracle on a bounded sample of `workload`: the same x-z plane
+    (line lengths, FFT sizes) with the wall-normal extent reduced so that the run fits the
+    budget.  Returns (rate pt-steps/s, cores, sample description)."""
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    w = WORKLOADS[workload]
+    n2s = w["n2m"]
+    # per-point cost is nearly independent of N2M; take a slab of at most 32 cells
+    n2s = min(n2s, 32)
+    g, dt = make_grid(workload, n2m=n2s)
+    orc = oracle.Oracle(g, threads=cores)
+    U, P, HH = ic.perturbed_laminar(g)
+    orc.project(U)
+    pg = pg3 = 0.0
+    n = 1
+    for _ in range(max(1, min(warmup, 1))):
+        pg, pg3 = orc.getup(U, P, HH, n, dt, pg, pg3)
+        n += 1
+    t0 = time.perf_counter()
+    done = 0
+    for _ in range(max(1, steps)):
+        pg, pg3 = orc.getup(U, P, HH, n, dt, pg, pg3)
+        n += 1
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    t = time.perf_counter() - t0
+    rate = g.points * done / t
+    sample = (f"{done} full GETUP steps on a {g.n1m}x{g.n2m}x{g.n3m} slab of {workload} "
+              f"(same x-z plane, {g.n2m} of {w['n2m']} wall-normal cells), FP64, {cores} OpenMP threads")
+    return rate, cores, sample
+
+
+# ------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------
+def make_channel(lib, g, form, U, P, HH):
+    ch = lib.Channel(g, C3D_MIXED if form == "mixed" else C3D_FP64)
+    ch.upload(U, P, HH)
+    ch.project()
+    ch.set_presg(0.0, 0.0)
+    return ch
+
+
+def run_ours(args, D: Dist):
+    from compact3d_gb300 import lib
+    lib.check(lib.load().c3d_set_device(D.local), "c3d_set_device")
+    g, dt = make_grid(args.workload)
+    U0, P0, HH0 = ic.perturbed_laminar(g, seed=ic.SEED0 + D.rank)
+    pts = g.points
+    K, W = args.steps, args.warmup
+
+    # ---- main form, device-resident (value) ----
+    ch = make_channel(lib, g, args.form, U0, P0, HH0)
+    n = 1
+    for _ in range(W):
+        ch.step_async(n, dt)
+        n += 1
+    ch.sync()
+    launches_per_step = ch.last_step_stats()[1]
+    clocks = Clocks(D.local)
+    D.barrier()
+    clocks.start()
+    ch.timer_start()
+    for _ in range(K):
+        ch.step_async(n, dt)
+        n += 1
+    ms = ch.timer_stop()
+    ck = clocks.stop()
+    D.barrier()
+    ms_max = D.max(ms)
+    total_pts = D.sum(pts)
+    value = total_pts * K / (ms_max / 1e3)
+    res = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=D.world, steps=K, warmup=W,
+               ms_per_step=ms_max / K, higher_is_better=True, scaling="weak", vs_baseline=None,
+               dtype="f32+f64 mixed" if args.form == "mixed" else "f64", data="synthetic")
+    res["config"] = dict(workload=f"{args.workload}: {g.n1m}x{g.n2m + 1}x{g.n3m} points "
+                                  f"(cells {g.n1m}x{g.n2m}x{g.n3m}), RE={g.re}, dt={dt}, "
+                                  f"y tanh-stretched beta={g.cks}",
+                         form=args.form, cells=[g.n1m, g.n2m, g.n3m],
+                         l2_policy=f"inputs larger than L2: each FP64 field is "
+                                   f"{8 * g.n1m * (g.n2m + 2) * g.n3m / 1e6:.0f} MB",
+                         parallelism=f"replicas x{D.world}")
+    res["gpu_launches"] = launches_per_step * K
+    if ck:
+        res["clocks"] = ck
+
+    # ---- per-kernel profile (separate short run, CUDA events around each launch) ----
+    ch.profile(True)
+    for _ in range(2):
+        ch.step_async(n, dt)
+        n += 1
+    ch.sync()
+    prof = ch.profile_read()
+    ch.profile(False)
+    dom = max(prof, key=lambda e: e["ms"])
+    peak, kind = peaks()
+    avg_ms = dom["ms"] / dom["launches"]
+    achieved = dom["bytes"] / (avg_ms / 1e3) / 1e9
+    res["roofline"] = dict(bound="hbm", kernel=dom["name"], achieved=achieved, peak=peak,
+                           unit="GB/s", frac=achieved / peak, peak_kind=kind,
+                           traffic=traffic_for(args.workload, args.form, dom["name"]),
+                           alg_bytes_per_launch=dom["bytes"], avg_launch_ms=avg_ms)
+    step_ms = sum(e["ms"] for e in prof) / 2
+    res["kernels"] = {e["name"]: dict(ms=e["ms"] / e["launches"], share=e["ms"] / (2 * step_ms),
+                                      gbs=e["bytes"] / (e["ms"] / e["launches"] / 1e3) / 1e9)
+                      for e in prof}
+
+    # ---- FP64 form in the same run, and the mixed form's error against it ----
+    if args.form == "mixed" and not args.no_fp64:
+        c64 = make_channel(lib, g, "fp64", U0, P0, HH0)
+        m = 1
+        for _ in range(W):
+            c64.step_async(m, dt)
+            m += 1
+        c64.sync()
+        k64 = max(2, min(K, args.fp64_steps))
+        c64.timer_start()
+        for _ in range(k64):
+            c64.step_async(m, dt)
+            m += 1
+        ms64 = D.max(c64.timer_stop())
+        res["fp64"] = dict(value=total_pts * k64 / (ms64 / 1e3), ms_per_step=ms64 / k64, steps=k64)
+        # error after the same number of steps from the same start
+        ref_steps = args.err_steps
+        cm = make_channel(lib, g, "mixed", U0, P0, HH0)
+        cf = make_channel(lib, g, "fp64", U0, P0, HH0)
+        for s in range(1, ref_steps + 1):
+            cm.step_async(s, dt)
+            cf.step_async(s, dt)
+        Um, Pm, _ = cm.download()
+        Uf, Pf, _ = cf.download()
+        n1, n2, n3 = g.n1m, g.n2m, g.n3m
+
+        def rl(a, b):
+            return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+        err = dict(u=rl(Um[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 0], Uf[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 0]),
+                   v=rl(Um[1:n1 + 1, 2:n2 + 1, 1:n3 + 1, 1], Uf[1:n1 + 1, 2:n2 + 1, 1:n3 + 1, 1]),
+                   w=rl(Um[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 2], Uf[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 2]),
+                   p=rl(Pm[:n1, :n2, :n3], Pf[:n1, :n2, :n3]), steps=ref_steps)
+        dm, df = cm.diagnose(), cf.diagnose()
+        pm, pf = cm.get_presg(), cf.get_presg()
+        err.update(divmax_mixed=dm["divmax"], divmax_fp64=df["divmax"],
+                   bulk_mixed=dm["flow1"] / g.aly, bulk_fp64=df["flow1"] / g.aly,
+                   wsm_mixed=float(dm["wsm"][0]), wsm_fp64=float(df["wsm"][0]),
+                   presg_mixed=pm[0], presg_fp64=pf[0])
+        res["err_vs_fp64"] = err
+        for c in (c64, cm, cf):
+            c.close()
+
+    # ---- end to end through the host-array drop-in (c3d_getup) ----
+    if not args.no_e2e:
+        from compact3d_gb300 import lib as L
+        U, P, HH = U0.copy(order="F"), P0.copy(order="F"), HH0.copy(order="F")
+        for a in (U, P, HH):
+            L.host_register(a)
+        ce = lib.Channel(g, C3D_MIXED if args.form == "mixed" else C3D_FP64)
+        ce.upload(U, P, HH)
+        ce.project()
+        ce.download(U, P, HH)
+        pg = pg3 = 0.0
+        m = 1
+        for _ in range(min(W, 2)):
+            pg, pg3 = ce.getup(U, P, HH, m, dt, pg, pg3)
+            m += 1
+        ke = max(2, min(K, args.e2e_steps))
+        D.barrier()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            pg, pg3 = ce.getup(U, P, HH, m, dt, pg, pg3)
+            m += 1
+        te = D.max(time.perf_counter() - t0)
+        bytes_io = U.nbytes + P.nbytes + HH.nbytes
+        res["e2e"] = dict(value=total_pts * ke / te, unit=UNIT, h2d_bytes_per_step=bytes_io,
+                          d2h_bytes_per_step=bytes_io, steps=ke,
+                          path="c3d_getup: Fortran-layout host arrays (pinned) -> device, step, -> host")
+        for a in (U, P, HH):
+            L.host_unregister(a)
+        ce.close()
+    ch.close()
+
+    # ---- CPU baseline (rank 0, N=1 only) ----
+    if D.rank == 0 and D.world == 1 and not args.no_cpu:
+        rate, cores, sample = cpu_reference(args.workload, steps=3, warmup=1, budget_s=40.0)
+        res["cpu_baseline"] = dict(value=rate, unit=UNIT, cores=cores, kind="port", sample=sample)
+    return res
+
+
+def run_reference(args, D: Dist):
+    if D.rank != 0:
+        return None
+    rate, cores, sample = cpu_reference(args.workload, steps=args.steps, warmup=args.warmup, budget_s=150.0)
+    g, dt = make_grid(args.workload)
+    res = dict(impl="reference", metric=METRIC, value=rate, unit=UNIT, n_gpus=D.world, steps=args.steps,
+               warmup=args.warmup, ms_per_step=g.points / rate * 1e3, higher_is_better=True,
+               scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+               config=dict(workload=f"{args.workload}: {g.n1m}x{g.n2m + 1}x{g.n3m} points, RE={g.re}, dt={dt}",
+                           form="fp64-cpu", cells=[g.n1m, g.n2m, g.n3m]))
+    res["cpu_baseline"] = dict(value=rate, unit=UNIT, cores=cores, kind="port", sample=sample)
+    res["e2e"] = dict(value=rate, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0)
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="channel384", choices=sorted(WORKLOADS))
+    ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--fp64-steps", type=int, default=5)
+    ap.add_argument("--err-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    D = Dist()
+    res = run_reference(args, D) if args.impl == "reference" else run_ours(args, D)
+    if D.rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+    D.close()
+
+
+if __name__ == "__main__":
+    main()

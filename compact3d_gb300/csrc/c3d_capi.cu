@@ -15,6 +15,54 @@ namespace c3d {
 static thread_local std::string g_last_error;
 static thread_local int g_device = -1;
 void set_error(const std::string &msg) { g_last_error = msg; }
+
+void mark(c3d_channel *ch, int *nl, const char *name, double bytes) {
+    (*nl)++;
+    if (!ch->prof_on) return;
+    int k = -1;
+    for (size_t q = 0; q < ch->prof_name.size(); ++q)
+        if (ch->prof_name[q] == name) { k = (int)q; break; }
+    if (k < 0) {
+        k = (int)ch->prof_name.size();
+        ch->prof_name.push_back(name);
+        ch->prof_ms.push_back(0.0);
+        ch->prof_cnt.push_back(0);
+        ch->prof_bytes.push_back(bytes);
+    }
+    if (ch->prof_n + 1 >= (int)ch->prof_ev.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        ch->prof_ev.push_back(e);
+    }
+    cudaEventRecord(ch->prof_ev[ch->prof_n + 1], ch->stream);
+    if ((int)ch->prof_iv.size() <= ch->prof_n) ch->prof_iv.resize(ch->prof_n + 1);
+    ch->prof_iv[ch->prof_n] = k;
+    ch->prof_n++;
+}
+
+void prof_begin(c3d_channel *ch) {
+    if (!ch->prof_on) return;
+    if (ch->prof_ev.empty()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        ch->prof_ev.push_back(e);
+    }
+    ch->prof_n = 0;
+    cudaEventRecord(ch->prof_ev[0], ch->stream);
+}
+
+int prof_collect(c3d_channel *ch) {
+    if (!ch->prof_on || ch->prof_n == 0) return 0;
+    if (cudaEventSynchronize(ch->prof_ev[ch->prof_n]) != cudaSuccess) return C3D_ECUDA;
+    for (int i = 0; i < ch->prof_n; ++i) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ch->prof_ev[i], ch->prof_ev[i + 1]);
+        ch->prof_ms[ch->prof_iv[i]] += ms;
+        ch->prof_cnt[ch->prof_iv[i]] += 1;
+    }
+    ch->prof_n = 0;
+    return 0;
+}
 }  // namespace c3d
 
 #define CK(call)                                                                        \
@@ -111,6 +159,9 @@ void free_channel(c3d_channel *ch) {
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (ch->pinned) cudaFreeHost(ch->pinned);
+    for (cudaEvent_t e : ch->prof_ev) cudaEventDestroy(e);
+    if (ch->tm0) cudaEventDestroy(ch->tm0);
+    if (ch->tm1) cudaEventDestroy(ch->tm1);
     if (ch->stream) cudaStreamDestroy(ch->stream);
     if (ch->ev0) cudaEventDestroy(ch->ev0);
     if (ch->ev1) cudaEventDestroy(ch->ev1);
@@ -275,7 +326,9 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
         return code;
     };
     if (cudaStreamCreateWithFlags(&ch->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(C3D_ECUDA);
-    if (cudaEventCreate(&ch->ev0) != cudaSuccess || cudaEventCreate(&ch->ev1) != cudaSuccess) return fail(C3D_ECUDA);
+    if (cudaEventCreate(&ch->ev0) != cudaSuccess || cudaEventCreate(&ch->ev1) != cudaSuccess ||
+        cudaEventCreate(&ch->tm0) != cudaSuccess || cudaEventCreate(&ch->tm1) != cudaSuccess)
+        return fail(C3D_ECUDA);
     if (dalloc(&ch->u, nf) || dalloc(&ch->v, nf) || dalloc(&ch->w, nf) || dalloc(&ch->p, nf) ||
         dalloc(&ch->dp, nf) || dalloc(&ch->scal, SCAL_COUNT) || dalloc(&ch->part, 2 * (size_t)g.n2m * g.n3m) ||
         dalloc(&ch->metric, 8 * (size_t)(g.n2 + 1)) || dalloc(&ch->ycn, 9 * (size_t)(g.n2 + 1)) ||
@@ -460,14 +513,20 @@ static int step_common(c3d_channel *ch, double dt, double *presg, double *presg3
         if (rc) return rc;
     }
     double pg[2] = {presg ? *presg : 0.0, presg3 ? *presg3 : 0.0};
-    CK(cudaMemcpyAsync(ch->scal + SCAL_PRESG, pg, 2 * sizeof(double), cudaMemcpyHostToDevice, ch->stream));
+    if (presg && presg3)
+        CK(cudaMemcpyAsync(ch->scal + SCAL_PRESG, pg, 2 * sizeof(double), cudaMemcpyHostToDevice, ch->stream));
     CK(cudaEventRecord(ch->ev0, ch->stream));
+    prof_begin(ch);
     int nl = 0;
     int rc = launch_step(ch, dt, &nl);
     if (rc) return rc;
     CK(cudaGetLastError());
     CK(cudaEventRecord(ch->ev1, ch->stream));
     ch->last_launches = nl;
+    if (ch->prof_on) {
+        rc = prof_collect(ch);
+        if (rc) return rc;
+    }
     if (sync) {
         CK(cudaMemcpyAsync(pg, ch->scal + SCAL_PRESG, 2 * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
         CK(cudaStreamSynchronize(ch->stream));
@@ -489,12 +548,82 @@ int c3d_step(c3d_channel *ch, int ntime, double dt, double *presg, double *presg
     return step_common(ch, dt, presg, presg3, true);
 }
 
+int c3d_step_async(c3d_channel *ch, int ntime, double dt) {
+    (void)ntime;
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    if (!ch->have_state) { set_error("c3d_upload must be called before c3d_step_async"); return C3D_ESTATE; }
+    cudaSetDevice(ch->device);
+    return step_common(ch, dt, nullptr, nullptr, false);
+}
+
+int c3d_set_presg(c3d_channel *ch, double presg, double presg3) {
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    double pg[2] = {presg, presg3};
+    CK(cudaMemcpyAsync(ch->scal + SCAL_PRESG, pg, sizeof(pg), cudaMemcpyHostToDevice, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    return 0;
+}
+
+int c3d_get_presg(c3d_channel *ch, double *presg, double *presg3) {
+    if (!ch || !presg || !presg3) { set_error("null argument"); return C3D_EINVAL; }
+    double pg[2];
+    CK(cudaMemcpyAsync(pg, ch->scal + SCAL_PRESG, sizeof(pg), cudaMemcpyDeviceToHost, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    *presg = pg[0];
+    *presg3 = pg[1];
+    return 0;
+}
+
+int c3d_timer_start(c3d_channel *ch) {
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    CK(cudaEventRecord(ch->tm0, ch->stream));
+    return 0;
+}
+
+int c3d_timer_stop(c3d_channel *ch, double *ms) {
+    if (!ch || !ms) { set_error("null argument"); return C3D_EINVAL; }
+    CK(cudaEventRecord(ch->tm1, ch->stream));
+    CK(cudaEventSynchronize(ch->tm1));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, ch->tm0, ch->tm1));
+    *ms = f;
+    return 0;
+}
+
+int c3d_profile(c3d_channel *ch, int enable) {
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    ch->prof_on = enable ? 1 : 0;
+    ch->prof_name.clear();
+    ch->prof_ms.clear();
+    ch->prof_cnt.clear();
+    ch->prof_bytes.clear();
+    ch->prof_n = 0;
+    return 0;
+}
+
+int c3d_profile_count(c3d_channel *ch) {
+    if (!ch) return C3D_EINVAL;
+    return (int)ch->prof_name.size();
+}
+
+int c3d_profile_get(c3d_channel *ch, int idx, const char **name, double *ms, int *launches,
+                    double *bytes_per_launch) {
+    if (!ch || idx < 0 || idx >= (int)ch->prof_name.size()) { set_error("bad profile index"); return C3D_EINVAL; }
+    if (name) *name = ch->prof_name[idx].c_str();
+    if (ms) *ms = ch->prof_ms[idx];
+    if (launches) *launches = ch->prof_cnt[idx];
+    if (bytes_per_launch) *bytes_per_launch = ch->prof_bytes[idx];
+    return 0;
+}
+
 int c3d_project(c3d_channel *ch) {
     if (!ch) { set_error("null channel"); return C3D_EINVAL; }
     if (!ch->have_state) { set_error("c3d_upload must be called before c3d_project"); return C3D_ESTATE; }
     cudaSetDevice(ch->device);
     int nl = 0;
+    prof_begin(ch);
     int rc = launch_project(ch, &nl);
+    if (!rc) rc = prof_collect(ch);
     if (rc) return rc;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(ch->stream));
@@ -505,7 +634,9 @@ int c3d_diagnose(c3d_channel *ch, c3d_diag *out) {
     if (!ch || !out) { set_error("null argument"); return C3D_EINVAL; }
     cudaSetDevice(ch->device);
     int nl = 0;
+    prof_begin(ch);
     int rc = launch_diag(ch, &nl);
+    if (!rc) rc = prof_collect(ch);
     if (rc) return rc;
     double s[SCAL_COUNT];
     CK(cudaMemcpyAsync(s, ch->scal, sizeof(s), cudaMemcpyDeviceToHost, ch->stream));

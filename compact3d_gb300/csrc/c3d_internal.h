@@ -95,6 +95,15 @@ struct c3d_channel {
     std::vector<double> ak1, ak3, pcj, ppj, pmjh;
     // wall model
     double *tauw, *taub;      // (N1M*N3M*2) device, plane layout [w][k][i]
+    // per-kernel profiler (CUDA events around every launch when enabled)
+    int prof_on;
+    int prof_n;                              // events recorded in the current step
+    std::vector<cudaEvent_t> prof_ev;        // event pool
+    std::vector<int> prof_iv;                // kernel index of interval i
+    std::vector<std::string> prof_name;
+    std::vector<double> prof_ms, prof_bytes;
+    std::vector<int> prof_cnt;
+    cudaEvent_t tm0, tm1;                    // c3d_timer_start/stop
 };
 
 namespace c3d {
@@ -105,4 +114,8 @@ int launch_diag(c3d_channel *ch, int *launches);
 int launch_poisson_tables(c3d_channel *ch);
 int launch_repack(c3d_channel *ch, int dir, int what, int comp);  // 0: Fortran->device
 void set_error(const std::string &msg);
+// Records a kernel-boundary mark for the profiler and counts the launch.
+void mark(c3d_channel *ch, int *nl, const char *name, double bytes);
+void prof_begin(c3d_channel *ch);
+int prof_collect(c3d_channel *ch);
 }  // namespace c3d

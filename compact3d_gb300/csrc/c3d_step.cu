@@ -1210,22 +1210,24 @@ static void launch_x_all(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0
     cudaStream_t st = ch->stream;
     const int M = ch->g.n1m / 2;
     typedef typename Cx<R>::T C2;
+    const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
     switch (which) {
-        case 0: k_xA<R, C><<<grid, TPB, 0, st>>>(a); break;
-        case 1: k_xB<R, C><<<grid, TPB, 0, st>>>(a); break;
+        case 0: k_xA<R, C><<<grid, TPB, 0, st>>>(a); mark(ch, nl, "xA", N * (32 + 7 * Rb)); return;
+        case 1: k_xB<R, C><<<grid, TPB, 0, st>>>(a); mark(ch, nl, "xB", N * 18 * Rb); return;
         case 2: {
             size_t sm = (size_t)(TPB / 32) * 2 * M * sizeof(C2);
             k_xC<R, C><<<grid, TPB, sm, st>>>(a, p0, p1);
-            break;
+            mark(ch, nl, "xC", N * (16 + 4 * Rb));
+            return;
         }
         case 3: {
             size_t sm = (size_t)(TPB / 32) * 2 * (M + 1) * sizeof(C2);
             k_xD<R, C><<<grid, TPB, sm, st>>>(a, p0, p1);
-            break;
+            mark(ch, nl, "xD", N * (8 + 4 * Rb));
+            return;
         }
-        case 4: k_diag_x<R, C><<<grid, TPB, 0, st>>>(a); break;
+        case 4: k_diag_x<R, C><<<grid, TPB, 0, st>>>(a); mark(ch, nl, "diag_x", N * 48); return;
     }
-    (*nl)++;
 }
 
 template <typename R>
@@ -1253,16 +1255,17 @@ static long long zthreads(const c3d_channel *ch) {
 template <typename R>
 static int run_projection_tail(c3d_channel *ch, StepArgs<R> &a, R *d0, R *d1, R *d2, int updp, int *nl) {
     cudaStream_t st = ch->stream;
+    const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
     constexpr int L = ZL<R>::L;
     typedef typename Cx<R>::T C2;
     const int nz = nblk(zthreads<R>(ch));
-    k_zD<R, L><<<nz, TPB, 0, st>>>(a, d2); (*nl)++;
+    k_zD<R, L><<<nz, TPB, 0, st>>>(a, d2); mark(ch, nl, "zD", N * (8 + 2 * Rb));
     if (launch_x<R>(ch, a, 2, d0, d1, nl)) return C3D_EINVAL;
     const int ntile = (ch->g.n1h + TWZ - 1) / TWZ;
     const size_t smz = 2 * (size_t)ch->g.n3m * TWZ * sizeof(C2);
-    k_fftz<R><<<ch->g.n2m * ntile, TPB, smz, st>>>(a, -1); (*nl)++;
-    k_poisson<R><<<nblk((long long)ch->g.n1h * ch->g.n3m), TPB, 0, st>>>(a); (*nl)++;
-    k_fftz<R><<<ch->g.n2m * ntile, TPB, smz, st>>>(a, +1); (*nl)++;
+    k_fftz<R><<<ch->g.n2m * ntile, TPB, smz, st>>>(a, -1); mark(ch, nl, "fftz_fwd", N * 2 * Rb);
+    k_poisson<R><<<nblk((long long)ch->g.n1h * ch->g.n3m), TPB, 0, st>>>(a); mark(ch, nl, "poisson", N * (2 * Rb + 8));
+    k_fftz<R><<<ch->g.n2m * ntile, TPB, smz, st>>>(a, +1); mark(ch, nl, "fftz_inv", N * 2 * Rb);
     if (launch_x<R>(ch, a, 3, d0, d2, nl)) return C3D_EINVAL;
     StepArgs<double> ad;
     StepArgs<float> af;
@@ -1270,8 +1273,8 @@ static int run_projection_tail(c3d_channel *ch, StepArgs<R> &a, R *d0, R *d1, R 
     memset(&af, 0, sizeof(af));
     if constexpr (sizeof(R) == 8) k_reduce<<<1, 1024, 0, st>>>(a, af, 0);
     else k_reduce<<<1, 1024, 0, st>>>(ad, a, 1);
-    (*nl)++;
-    k_zE<R, L><<<nz, TPB, 0, st>>>(a, d0, d1, d2, updp); (*nl)++;
+    mark(ch, nl, "reduce", 16.0 * ch->g.n2m * ch->g.n3m);
+    k_zE<R, L><<<nz, TPB, 0, st>>>(a, d0, d1, d2, updp); mark(ch, nl, "zE", N * (72 + 4 * Rb));
     return 0;
 }
 
@@ -1285,21 +1288,22 @@ static void set_smem_limits(c3d_channel *ch) {
 template <typename R>
 static int step_impl(c3d_channel *ch, double dt, int *nl) {
     cudaStream_t st = ch->stream;
+    const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
     constexpr int L = ZL<R>::L;
     set_smem_limits<R>(ch);
     // rotate the AB2 history: HH of the last step becomes HH_old
     ch->cur = 1 - ch->cur;
     StepArgs<R> a = make_args<R>(ch, dt);
-    k_bcond<<<nblk(ch->g.np), TPB, 0, st>>>(ch->g, ch->u, ch->v, ch->w); (*nl)++;
+    k_bcond<<<nblk(ch->g.np), TPB, 0, st>>>(ch->g, ch->u, ch->v, ch->w); mark(ch, nl, "bcond", 64.0 * ch->g.np);
     if (launch_x<R>(ch, a, 0, nullptr, nullptr, nl)) return C3D_EINVAL;
     const int nz = nblk(zthreads<R>(ch));
-    k_zA<R, L><<<nz, TPB, 0, st>>>(a); (*nl)++;
-    k_zB<R, L><<<nz, TPB, 0, st>>>(a); (*nl)++;
+    k_zA<R, L><<<nz, TPB, 0, st>>>(a); mark(ch, nl, "zA", N * (32 + 10 * Rb));
+    k_zB<R, L><<<nz, TPB, 0, st>>>(a); mark(ch, nl, "zB", N * 8 * Rb);
     if (launch_x<R>(ch, a, 1, nullptr, nullptr, nl)) return C3D_EINVAL;
-    k_ycn<R><<<nblk(3LL * ch->g.np), TPB, 0, st>>>(a); (*nl)++;
+    k_ycn<R><<<nblk(3LL * ch->g.np), TPB, 0, st>>>(a); mark(ch, nl, "ycn", N * 6 * Rb);
     // CN z factor: deltas go to exz/eyz/wsq, which the RHS passes no longer need
     R *dd0 = (R *)ch->exz, *dd1 = (R *)ch->eyz, *dd2 = (R *)ch->wsq;
-    k_zC<R, L><<<nz, TPB, 0, st>>>(a, dd0, dd1, dd2); (*nl)++;
+    k_zC<R, L><<<nz, TPB, 0, st>>>(a, dd0, dd1, dd2); mark(ch, nl, "zC", N * 6 * Rb);
     return run_projection_tail<R>(ch, a, dd0, dd1, dd2, 1, nl);
 }
 
@@ -1319,7 +1323,7 @@ static int project_impl(c3d_channel *ch, int *nl) {
     cudaMemsetAsync(dd0, 0, bytes, ch->stream);
     cudaMemsetAsync(dd1, 0, bytes, ch->stream);
     cudaMemsetAsync(dd2, 0, bytes, ch->stream);
-    k_bcond<<<nblk(ch->g.np), TPB, 0, ch->stream>>>(ch->g, ch->u, ch->v, ch->w); (*nl)++;
+    k_bcond<<<nblk(ch->g.np), TPB, 0, ch->stream>>>(ch->g, ch->u, ch->v, ch->w); mark(ch, nl, "bcond", 64.0 * ch->g.np);
     return run_projection_tail<R>(ch, a, dd0, dd1, dd2, 0, nl);
 }
 
@@ -1336,8 +1340,8 @@ static int diag_impl(c3d_channel *ch, int *nl) {
     cudaMemsetAsync(ch->scal + SCAL_DIVMAX, 0, 2 * sizeof(double), st);
     cudaMemsetAsync(ch->scal + SCAL_NONFIN, 0, sizeof(double), st);
     if (launch_x<R>(ch, a, 4, nullptr, nullptr, nl)) return C3D_EINVAL;
-    k_diag_z<R, L><<<nblk(zthreads<R>(ch)), TPB, 0, st>>>(a); (*nl)++;
-    k_diag_sums<<<1, 256, 0, st>>>(ch->g, ch->u, ch->v, ch->w, ch->scal); (*nl)++;
+    k_diag_z<R, L><<<nblk(zthreads<R>(ch)), TPB, 0, st>>>(a); mark(ch, nl, "diag_z", (double)ch->g.n1m * ch->g.n2m * ch->g.n3m * 16);
+    k_diag_sums<<<1, 256, 0, st>>>(ch->g, ch->u, ch->v, ch->w, ch->scal); mark(ch, nl, "diag_sums", 64.0 * ch->g.np);
     return 0;
 }
 

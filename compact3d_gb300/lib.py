@@ -53,6 +53,14 @@ SIGNATURES = {
     "c3d_host_unregister": (_ip, [_vp]),
     "c3d_sync": (_ip, [_vp]),
     "c3d_last_step_stats": (_ip, [_vp, _dp, ctypes.POINTER(_ip)]),
+    "c3d_step_async": (_ip, [_vp, _ip, ctypes.c_double]),
+    "c3d_set_presg": (_ip, [_vp, ctypes.c_double, ctypes.c_double]),
+    "c3d_get_presg": (_ip, [_vp, _dp, _dp]),
+    "c3d_timer_start": (_ip, [_vp]),
+    "c3d_timer_stop": (_ip, [_vp, _dp]),
+    "c3d_profile": (_ip, [_vp, _ip]),
+    "c3d_profile_count": (_ip, [_vp]),
+    "c3d_profile_get": (_ip, [_vp, _ip, ctypes.POINTER(ctypes.c_char_p), _dp, ctypes.POINTER(_ip), _dp]),
     "c3d_batch_create": (_ip, [_ip, ctypes.POINTER(c3d_grid), ctypes.POINTER(_vp)]),
     "c3d_batch_destroy": (_ip, [_vp]),
     "c3d_batch_channel": (_ip, [_vp, _ip, ctypes.POINTER(_vp)]),
@@ -160,6 +168,41 @@ class Channel:
 
     def sync(self):
         check(load().c3d_sync(self.h), "c3d_sync")
+
+    def step_async(self, ntime: int, dt: float):
+        check(load().c3d_step_async(self.h, ntime, dt), "c3d_step_async")
+
+    def set_presg(self, presg: float, presg3: float):
+        check(load().c3d_set_presg(self.h, presg, presg3), "c3d_set_presg")
+
+    def get_presg(self):
+        a = (ctypes.c_double * 1)()
+        b = (ctypes.c_double * 1)()
+        check(load().c3d_get_presg(self.h, a, b), "c3d_get_presg")
+        return a[0], b[0]
+
+    def timer_start(self):
+        check(load().c3d_timer_start(self.h), "c3d_timer_start")
+
+    def timer_stop(self) -> float:
+        ms = (ctypes.c_double * 1)()
+        check(load().c3d_timer_stop(self.h, ms), "c3d_timer_stop")
+        return ms[0]
+
+    def profile(self, enable: bool = True):
+        check(load().c3d_profile(self.h, int(enable)), "c3d_profile")
+
+    def profile_read(self) -> list[dict]:
+        L = load()
+        out = []
+        for i in range(L.c3d_profile_count(self.h)):
+            nm = ctypes.c_char_p()
+            ms = (ctypes.c_double * 1)()
+            n = (ctypes.c_int * 1)()
+            b = (ctypes.c_double * 1)()
+            check(L.c3d_profile_get(self.h, i, ctypes.byref(nm), ms, n, b), "c3d_profile_get")
+            out.append(dict(name=nm.value.decode(), ms=ms[0], launches=n[0], bytes=b[0]))
+        return out
 
     def last_step_stats(self):
         ms = (ctypes.c_double * 1)()

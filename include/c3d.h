@@ -139,6 +139,26 @@ int c3d_sync(c3d_channel *ch);
  * channel's stream), and the number of kernels that step launched. */
 int c3d_last_step_stats(c3d_channel *ch, double *ms, int *kernel_launches);
 
+/* Device-resident driving: c3d_step_async queues one GETUP on the channel's
+ * stream and returns without waiting; PRESG/PRESG3 stay on the device
+ * (c3d_set_presg before the first step, c3d_get_presg to read them, which
+ * waits for the queued work). */
+int c3d_step_async(c3d_channel *ch, int ntime, double dt);
+int c3d_set_presg(c3d_channel *ch, double presg, double presg3);
+int c3d_get_presg(c3d_channel *ch, double *presg, double *presg3);
+/* CUDA-event timer on the channel's stream: start, then stop returns the
+ * device time between the two marks in milliseconds (waits for the stop). */
+int c3d_timer_start(c3d_channel *ch);
+int c3d_timer_stop(c3d_channel *ch, double *ms);
+/* Per-kernel profile of subsequent steps (CUDA events around every launch).
+ * c3d_profile_get returns, for kernel index idx < c3d_profile_count(),
+ * its name, accumulated device time, launch count and the algorithmic bytes
+ * of one launch (compulsory reads + writes of that kernel). */
+int c3d_profile(c3d_channel *ch, int enable);
+int c3d_profile_count(c3d_channel *ch);
+int c3d_profile_get(c3d_channel *ch, int idx, const char **name, double *ms,
+                    int *launches, double *bytes_per_launch);
+
 /* ---- batched ensemble --------------------------------------------------
  * Many independent channels (any mix of grid sizes, RE and precision) that
  * advance together.  c3d_batch_step launches every channel's step work on one
