@@ -61,6 +61,7 @@ SIGNATURES = {
     "c3d_profile": (_ip, [_vp, _ip]),
     "c3d_profile_count": (_ip, [_vp]),
     "c3d_profile_get": (_ip, [_vp, _ip, ctypes.POINTER(ctypes.c_char_p), _dp, ctypes.POINTER(_ip), _dp]),
+    "c3d_divcheck_noalloc": (_ip, [ctypes.POINTER(c3d_grid), _dp, _dp]),
     "c3d_batch_create": (_ip, [_ip, ctypes.POINTER(c3d_grid), ctypes.POINTER(_vp)]),
     "c3d_batch_destroy": (_ip, [_vp]),
     "c3d_batch_channel": (_ip, [_vp, _ip, ctypes.POINTER(_vp)]),

@@ -159,6 +159,25 @@ int c3d_profile_count(c3d_channel *ch);
 int c3d_profile_get(c3d_channel *ch, int idx, const char **name, double *ms,
                     int *launches, double *bytes_per_launch);
 
+/* ---- allocation-free divergence check ----------------------------------
+ * No counterpart in the reference (it is an addition for callers of this
+ * library, not a replacement of a compact3d routine).  c3d_divcheck_noalloc
+ * computes DIVCHECK's max|div u| (the same operators as c3d_diagnose) for a
+ * host velocity U(0:N1,0:N2,0:N3,3) in the driver's Fortran layout, for callers
+ * that must not allocate device memory: drivers whose device memory belongs to
+ * their own pool allocator, and long-running loops whose footprint must stay
+ * fixed after start-up.  It calls no cudaMalloc/cudaFree; its scratch is one
+ * static __device__ array of C3D_NOALLOC_MAX_BYTES that every GPU loading the
+ * library keeps until exit, so grids whose working set (about 8 bytes x
+ * ((N1+1)(N2+1)(N3+1) + 4 (N2+1)(N1-1)(N3-1))) exceeds it return C3D_EINVAL.
+ * Only grid->n1..n3, dx1, dx3 and dy are read.  All calls share that scratch:
+ * calls that overlap on the GPU race, so serialise them.  The first call on a
+ * device looks up the scratch address (cudaGetSymbolAddress); make it before
+ * any stream capture starts on that device.  Work runs on the legacy default
+ * stream; the call returns when *divmax is ready. */
+#define C3D_NOALLOC_MAX_BYTES (64u * 1024u * 1024u)
+int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
+
 /* ---- batched ensemble --------------------------------------------------
  * Many independent channels (any mix of grid sizes, RE and precision) that
  * advance together.  c3d_batch_step launches every channel's step work on one
