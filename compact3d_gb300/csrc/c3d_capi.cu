@@ -152,7 +152,8 @@ int dalloc(T **p, size_t n) {
 void free_channel(c3d_channel *ch) {
     if (!ch) return;
     void *ptrs[] = {ch->u, ch->v, ch->w, ch->p, ch->dp, ch->scal, ch->part, ch->metric, ch->ycn,
-                    ch->prb, ch->pgam, ch->pmj, ch->tw64, ch->tw32, ch->hh[0][0], ch->hh[0][1],
+                    ch->prb, ch->pgam, ch->pmj, ch->ycn32, ch->metr, ch->prbdf, ch->pgamdf, ch->pmjdf, ch->diagbuf,
+                    ch->tw64, ch->tw32, ch->hh[0][0], ch->hh[0][1],
                     ch->hh[0][2], ch->hh[1][0], ch->hh[1][1], ch->hh[1][2], ch->r[0], ch->r[1],
                     ch->r[2], ch->exy, ch->exz, ch->eyz, ch->ww1, ch->wsq, ch->rdpz, ch->g1,
                     ch->spec, ch->stage, ch->tauw, ch->taub};
@@ -211,7 +212,7 @@ int upload_ycn(c3d_channel *ch, double dt) {
     const Geo &g = ch->g;
     const int m = g.n2 + 1, N2M = g.n2m;
     std::vector<double> t(9 * (size_t)m, 0.0), hm(m), hc(m), hp(m), dym(m), dyc(m), dyp(m);
-    std::vector<double> met(8 * (size_t)m);
+    std::vector<double> met(10 * (size_t)m);
     CK(cudaMemcpy(met.data(), ch->metric, met.size() * sizeof(double), cudaMemcpyDeviceToHost));
     const double *HP = met.data() + 2 * m, *HC = met.data() + 3 * m, *HM = met.data() + 4 * m;
     const double *DYP = met.data() + 5 * m, *DYC = met.data() + 6 * m, *DYM = met.data() + 7 * m;
@@ -244,7 +245,10 @@ int upload_ycn(c3d_channel *ch, double dt) {
             A[J] = Av[J];
         }
     }
+    std::vector<float> t32(t.size());
+    for (size_t q = 0; q < t.size(); ++q) t32[q] = (float)t[q];
     CK(cudaMemcpyAsync(ch->ycn, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, ch->stream));
+    CK(cudaMemcpyAsync(ch->ycn32, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice, ch->stream));
     CK(cudaStreamSynchronize(ch->stream));
     ch->dt_cached = dt;
     return 0;
@@ -301,6 +305,8 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
     ch->fx = FftPlan();
     ch->fz = FftPlan();
     cudaGetDevice(&ch->device);
+    cudaDeviceGetAttribute(&ch->nsm, cudaDevAttrMultiProcessorCount, ch->device);
+    if (ch->nsm <= 0) ch->nsm = 1;
     ch->precision = gr->precision;
     Geo &g = ch->g;
     g.n1m = gr->n1 - 1;
@@ -329,13 +335,24 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
     if (cudaEventCreate(&ch->ev0) != cudaSuccess || cudaEventCreate(&ch->ev1) != cudaSuccess ||
         cudaEventCreate(&ch->tm0) != cudaSuccess || cudaEventCreate(&ch->tm1) != cudaSuccess)
         return fail(C3D_ECUDA);
-    if (dalloc(&ch->u, nf) || dalloc(&ch->v, nf) || dalloc(&ch->w, nf) || dalloc(&ch->p, nf) ||
-        dalloc(&ch->dp, nf) || dalloc(&ch->scal, SCAL_COUNT) || dalloc(&ch->part, 2 * (size_t)g.n2m * g.n3m) ||
-        dalloc(&ch->metric, 8 * (size_t)(g.n2 + 1)) || dalloc(&ch->ycn, 9 * (size_t)(g.n2 + 1)) ||
-        dalloc(&ch->pmj, (size_t)(g.n2 + 1)))
+    // state: FP64 (FP64 form) or double-float pairs (mixed form), 8 bytes per value either way
+    if (cudaMalloc(&ch->u, nf * 8) != cudaSuccess || cudaMalloc(&ch->v, nf * 8) != cudaSuccess ||
+        cudaMalloc(&ch->w, nf * 8) != cudaSuccess || cudaMalloc(&ch->p, nf * 8) != cudaSuccess ||
+        cudaMalloc(&ch->dp, nf * rs) != cudaSuccess) {
+        set_error("cudaMalloc state");
+        return fail(C3D_ENOMEM);
+    }
+    if (dalloc(&ch->scal, SCAL_COUNT) || dalloc(&ch->part, 2 * (size_t)g.n2m * g.n3m) ||
+        dalloc(&ch->metric, 10 * (size_t)(g.n2 + 1)) || dalloc(&ch->ycn, 9 * (size_t)(g.n2 + 1)) ||
+        dalloc(&ch->ycn32, 9 * (size_t)(g.n2 + 1)) ||
+        dalloc(&ch->pmj, (size_t)(g.n2 + 1)) || dalloc(&ch->pmjdf, (size_t)(g.n2 + 1)) ||
+        dalloc(&ch->diagbuf, nf))
         return fail(C3D_ENOMEM);
     const size_t nmodes = (size_t)g.n1h * g.n3m;
     if (dalloc(&ch->prb, nmodes * g.n2m) || dalloc(&ch->pgam, nmodes * g.n2m)) return fail(C3D_ENOMEM);
+    if (ch->precision == C3D_MIXED) {
+        if (dalloc(&ch->prbdf, nmodes * g.n2m) || dalloc(&ch->pgamdf, nmodes * g.n2m)) return fail(C3D_ENOMEM);
+    }
     void **work[] = {&ch->hh[0][0], &ch->hh[0][1], &ch->hh[0][2], &ch->hh[1][0], &ch->hh[1][1], &ch->hh[1][2],
                      &ch->r[0], &ch->r[1], &ch->r[2], &ch->exy, &ch->exz, &ch->eyz, &ch->ww1, &ch->wsq,
                      &ch->rdpz, &ch->g1};
@@ -350,15 +367,21 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
     cudaMemset(ch->v, 0, nf * 8);
     cudaMemset(ch->w, 0, nf * 8);
     cudaMemset(ch->p, 0, nf * 8);
-    cudaMemset(ch->dp, 0, nf * 8);
+    cudaMemset(ch->dp, 0, nf * rs);
     cudaMemset(ch->scal, 0, SCAL_COUNT * 8);
     // metrics indexed by Fortran J: dy(0..N2), h/hp/hc/hm/dyp/dyc/dym(1..N2) (entry 0 = 0)
     const int m = g.n2 + 1;
-    std::vector<double> met(8 * (size_t)m, 0.0);
+    std::vector<double> met(10 * (size_t)m, 0.0);
     for (int j = 0; j <= g.n2; ++j) met[j] = gr->dy[j];
     const double *src[7] = {gr->h, gr->hp, gr->hc, gr->hm, gr->dyp, gr->dyc, gr->dym};
     for (int q = 0; q < 7; ++q)
         for (int j = 1; j <= g.n2; ++j) met[(q + 1) * (size_t)m + j] = src[q][j - 1];
+    // HP+HM-HC and DYP+DYM-DYC: zero up to rounding, they let the mixed form write the
+    // wall-normal viscous stencil without cancellation
+    for (int j = 1; j <= g.n2; ++j) {
+        met[8 * (size_t)m + j] = (gr->hp[j - 1] + gr->hm[j - 1]) - gr->hc[j - 1];
+        met[9 * (size_t)m + j] = (gr->dyp[j - 1] + gr->dym[j - 1]) - gr->dyc[j - 1];
+    }
     if (cudaMemcpy(ch->metric, met.data(), met.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) return fail(C3D_ECUDA);
     g.dy = ch->metric;
     g.h = ch->metric + m;
@@ -368,9 +391,43 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
     g.dyp = ch->metric + 5 * m;
     g.dyc = ch->metric + 6 * m;
     g.dym = ch->metric + 7 * m;
+    g.hz = ch->metric + 8 * m;
+    g.dyz = ch->metric + 9 * m;
+    {
+        // working-precision copies: hp,hc,hm,hz,dyp,dyc,dym,dyz,h,1/h,dy/2,1/dy,dy
+        std::vector<double> mr((size_t)NMETR * m, 0.0);
+        const int order[9] = {2, 3, 4, 8, 5, 6, 7, 9, 1};   // rows of `met`
+        for (int q = 0; q < 9; ++q)
+            for (int j = 0; j < m; ++j) mr[(size_t)q * m + j] = met[(size_t)order[q] * m + j];
+        for (int j = 0; j < m; ++j) {
+            const double hj = met[(size_t)1 * m + j], dyj = met[j];
+            mr[(size_t)9 * m + j] = hj != 0.0 ? 1.0 / hj : 0.0;
+            mr[(size_t)10 * m + j] = dyj / 2.0;
+            mr[(size_t)11 * m + j] = dyj != 0.0 ? 1.0 / dyj : 0.0;
+            mr[(size_t)12 * m + j] = dyj;
+        }
+        const size_t es = rs;
+        if (cudaMalloc(&ch->metr, mr.size() * es) != cudaSuccess) return fail(C3D_ENOMEM);
+        if (ch->precision == C3D_MIXED) {
+            std::vector<float> f(mr.size());
+            for (size_t q = 0; q < mr.size(); ++q) f[q] = (float)mr[q];
+            cudaMemcpy(ch->metr, f.data(), f.size() * 4, cudaMemcpyHostToDevice);
+        } else {
+            cudaMemcpy(ch->metr, mr.data(), mr.size() * 8, cudaMemcpyHostToDevice);
+        }
+    }
     // Poisson metrics and factor tables
     poisson_metrics(ch, gr);
     if (cudaMemcpy(ch->pmj, ch->pmjh.data(), (size_t)m * 8, cudaMemcpyHostToDevice) != cudaSuccess) return fail(C3D_ECUDA);
+    {
+        std::vector<float2> pdf(m);
+        for (int j = 0; j < m; ++j) {
+            float h = (float)ch->pmjh[j];
+            pdf[j] = make_float2(h, (float)(ch->pmjh[j] - (double)h));
+        }
+        if (cudaMemcpy(ch->pmjdf, pdf.data(), (size_t)m * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(C3D_ECUDA);
+    }
     rc = launch_poisson_tables(ch);
     if (rc) return fail(rc);
     // FFT plans and twiddles: [x: N1M/2][z: N3M][x post-processing: N1M/2+1]

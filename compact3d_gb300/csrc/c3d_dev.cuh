@@ -42,8 +42,9 @@ struct Geo {
     long long nf;            // (n2 + 1) * np (field)
     int n1h;                 // n1m/2 + 1 (half spectrum along x)
     double dx1, dx3, dx1q, dx3q, re, alx, aly, alz, vol;
-    // y metrics indexed by Fortran J (arrays of n2+1 values, entry 0 = DY(0) etc.)
-    const double *dy, *h, *hp, *hc, *hm, *dyp, *dyc, *dym;
+    // y metrics indexed by Fortran J (arrays of n2+1 values, entry 0 = DY(0) etc.);
+    // hz = HP+HM-HC and dyz = DYP+DYM-DYC are zero up to rounding (used by the mixed form)
+    const double *dy, *h, *hp, *hc, *hm, *dyp, *dyc, *dym, *hz, *dyz;
 };
 
 __host__ __device__ inline long long fidx(const Geo &g, int i, int j, int k) {
@@ -224,7 +225,98 @@ __device__ __forceinline__ void zseg(R (&out)[L], int k0, int n, const Cyc<R> &c
     }
 }
 
-template <typename R>
-__device__ __forceinline__ R to_r(double v) { return (R)v; }
+// The same with the warm-up length M a compile-time constant, so that every loop unrolls
+// and the loads of D can be issued ahead of the recurrence.
+template <typename R, int L, int M, typename F>
+__device__ __forceinline__ void zsegm(R (&out)[L], int k0, int n, const Cyc<R> &c, F D) {
+    const R r = c.r;
+    R y = R(0);
+    int kk = wrapi(k0 - M, n);
+#pragma unroll
+    for (int q = 0; q < M; ++q) {
+        y = D(kk) + r * y;
+        kk = (kk + 1 == n) ? 0 : kk + 1;
+    }
+    R ys[L];
+#pragma unroll
+    for (int t = 0; t < L; ++t) {
+        y = D(kk) + r * y;
+        ys[t] = y;
+        kk = (kk + 1 == n) ? 0 : kk + 1;
+    }
+    R acc = R(0), pw = R(1);
+#pragma unroll
+    for (int q = 0; q < M; ++q) {
+        y = D(kk) + r * y;
+        acc = acc + pw * y;
+        pw *= r;
+        kk = (kk + 1 == n) ? 0 : kk + 1;
+    }
+    R z = acc;
+    const R s = c.s;
+#pragma unroll
+    for (int t = L - 1; t >= 0; --t) {
+        z = ys[t] + r * z;
+        out[t] = s * z;
+    }
+}
+
+// Several cyclic solves along one column in a single sweep.  The functor f walks the
+// column once, in order, from position k0 - M (wrapped): f.start(k) positions it and
+// f.next(d) returns the NR right-hand sides at the current position and advances, so it
+// can keep a sliding window of the stencil inputs in registers and load one new value per
+// position.  Recurrence q uses root r[q] and scale s[q]; M is the largest warm-up needed.
+template <typename R, int L, int M, int NR, typename F>
+__device__ __forceinline__ void zsweep(R (&out)[NR][L], int k0, int n, const R (&r)[NR], const R (&s)[NR], F &f) {
+    f.start(wrapi(k0 - M, n));
+    R y[NR], d[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) y[q] = R(0);
+#pragma unroll 2
+    for (int t = 0; t < M; ++t) {
+        f.next(d);
+#pragma unroll
+        for (int q = 0; q < NR; ++q) y[q] = d[q] + r[q] * y[q];
+    }
+    R ys[NR][L];
+#pragma unroll
+    for (int t = 0; t < L; ++t) {
+        f.next(d);
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+            y[q] = d[q] + r[q] * y[q];
+            ys[q][t] = y[q];
+        }
+    }
+    R acc[NR], pw[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) { acc[q] = R(0); pw[q] = R(1); }
+#pragma unroll 2
+    for (int t = 0; t < M; ++t) {
+        f.next(d);
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+            y[q] = d[q] + r[q] * y[q];
+            acc[q] = acc[q] + pw[q] * y[q];
+            pw[q] *= r[q];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+        R z = acc[q];
+#pragma unroll
+        for (int t = L - 1; t >= 0; --t) {
+            z = ys[q][t] + r[q] * z;
+            out[q][t] = s[q] * z;
+        }
+    }
+}
+
+// Warm-up lengths M = ceil(log(tol)/log|r|) of the Pade operators (1,6,1), (1,10,1),
+// (1,22,1) and the Crank-Nicolson operators (b/a > 10, so M <= M10): tol = 1e-17 in FP64,
+// 3e-8 in FP32.
+template <typename R> struct WM;
+template <> struct WM<double> { static constexpr int M6 = 23, M10 = 18, M22 = 13, MCN = 18; };
+template <> struct WM<float> { static constexpr int M6 = 10, M10 = 8, M22 = 6, MCN = 8; };
 
 }  // namespace c3d

@@ -18,34 +18,52 @@ struct FftPlan {
     const float2 *tw32;
 };
 
+// Storage type of the state (u, v, w, P): FP64 in the FP64 form, double-float pairs
+// (hi, lo FP32) in the mixed form.
+template <typename R> struct SType;
+template <> struct SType<double> { typedef double S; };
+template <> struct SType<float> { typedef float2 S; };
+
+// Wall-normal metrics in the working precision, indexed by Fortran J (n2+1 values each):
+// the MESH arrays plus rh = 1/H, hdy = DY/2 and rdy = 1/DY, precomputed in FP64 on the
+// host (so the FP64 form sees exactly the reference's values) and converted once.
+template <typename R>
+struct MetR {
+    const R *hp, *hc, *hm, *hz, *dyp, *dyc, *dym, *dyz, *h, *rh, *hdy, *rdy, *dy;
+};
+constexpr int NMETR = 13;
+
 // Everything one step's kernels need, passed by value.  R is the working precision of
-// the intermediates (double for the FP64 form, float for the mixed form); the velocity,
-// pressure and reductions are always FP64.
+// the intermediates (double for the FP64 form, float for the mixed form).
 template <typename R>
 struct StepArgs {
+    typedef typename SType<R>::S S;
     Geo g;
-    double *u, *v, *w, *p;              // state, FP64
+    MetR<R> m;                          // wall-normal metrics in precision R
+    // constants in precision R, computed once on the host in FP64:
+    // 1/RE, 12 DX1^2, 24 DX1, 12 DX3^2, 24 DX3, 1/DT
+    R re1, f12x, f24x, f12z, f24z, rdt;
+    S *u, *v, *w, *p;                   // state
     R *hh[3];                           // nonlinear terms of this step (written)
     const R *ho[3];                     // nonlinear terms of the previous step (AB2)
-    R *r[3];                            // RUH -> delta (CN increments)
+    R *r[3];                            // RUH, then the x/y CN factors in place
     R *exy, *exz, *eyz, *ww1, *wsq;     // edge products and interpolants
     R *rdpz, *g1;                       // z part of div(UH)/DT; x-gradient of DP
-    double *dp;                         // pressure increment, FP64 (planes 1..N2M)
+    R *dp;                              // pressure increment (planes 1..N2M)
     void *spec;                         // half spectrum [j][kz][kx] of RDP / DP (R complex)
     double *scal;                       // device scalars (see SCAL_*)
     double *part;                       // per-row partial sums for the bulk-flow forcing
     Cyc<R> c6x, c10x, c22x, c6z, c10z, c22z, cnx, cnz;
-    // CN wall-normal factors, 3 components x (n2+1): A, RBET, GAM (FP64)
-    const double *ycn;
-    // Poisson factor tables [j][mode] (FP64): reciprocal pivots and multipliers
-    const double *prb, *pgam;
+    const double *ycn;                  // CN wall-normal factors: 3 comps x (A, RBET, GAM) x (n2+1)
+    const double *prb, *pgam;           // Poisson factor tables [j][mode], FP64
+    const float2 *prbdf, *pgamdf;       // the same as double-float pairs (mixed form)
     const double *pmj;                  // PMJ(J), n2+1 values
+    const float2 *pmjdf;                // the same as double-float pairs
     FftPlan fx, fz;                     // complex FFT of length N1M/2 (x) and N3M (z)
     const double2 *twx64;               // exp(-2 pi i k / N1M), k in [0, N1M/2]
     const float2 *twx32;
-    double dt;
+    double dt;                          // DT of the step (1 for the projection)
     int bulk;                           // apply the bulk-flow forcing (GETUP) or not (projection)
-    double dtproj;                      // DT used by the projection (1 for c3d_project)
 };
 
 enum {
@@ -70,11 +88,16 @@ struct c3d_channel {
     int device;
     cudaStream_t stream;
     cudaEvent_t ev0, ev1;
-    // FP64 state and metrics
-    double *u, *v, *w, *p, *dp, *scal, *part;
-    double *metric;           // 8 arrays of n2+1: dy,h,hp,hc,hm,dyp,dyc,dym
+    // state (double or float2 by precision), scalars and metrics
+    void *u, *v, *w, *p, *dp;
+    double *scal, *part;
+    double *metric;           // 10 arrays of n2+1: dy,h,hp,hc,hm,dyp,dyc,dym,hz,dyz
+    void *metr;               // NMETR arrays of n2+1 in the working precision (MetR)
     double *ycn;              // 3 x 3 x (n2+1)
+    float *ycn32;             // the same in FP32 (mixed form)
     double *prb, *pgam, *pmj;
+    float2 *prbdf, *pgamdf, *pmjdf;
+    double *diagbuf;          // FP64 scratch field of the diagnostics
     double2 *tw64;            // x-FFT table, z-FFT table, x post-processing table
     float2 *tw32;
     // working arrays (R = double or float), stored untyped
@@ -91,6 +114,7 @@ struct c3d_channel {
     int have_state;
     float last_ms;
     int last_launches;
+    int nsm;                  // streaming multiprocessors of the device
     c3d::FftPlan fx, fz;
     std::vector<double> ak1, ak3, pcj, ppj, pmjh;
     // wall model
@@ -107,6 +131,16 @@ struct c3d_channel {
 };
 
 namespace c3d {
+// Kernel launchers of the passes (c3d_xpass.cu, c3d_zpass.cu, c3d_spec.cu).
+// which: x passes 0=xA 1=xB 2=xC 3=xD 4=diag; z passes 0=zA 1=zB 2=zC 3=zD 4=zE 5=diag.
+template <typename R>
+int launch_xpass(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl);
+template <typename R>
+int launch_zpass(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *d1, R *d2, int flag, int *nl);
+template <typename R>
+int launch_spec(c3d_channel *ch, StepArgs<R> &a, int which, int *nl);   // 0=fwd z FFT 1=poisson 2=inv z FFT
+template <typename R>
+void set_spec_smem(c3d_channel *ch);
 // Step drivers (c3d_step.cu)
 int launch_step(c3d_channel *ch, double dt, int *launches);
 int launch_project(c3d_channel *ch, int *launches);

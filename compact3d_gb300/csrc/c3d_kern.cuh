@@ -1,0 +1,334 @@
+// c3d_kern.cuh -- device helpers shared by the step kernels: state representations,
+// coalesced row staging, complex arithmetic and the shared-memory Stockham FFT.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include "c3d_internal.h"
+
+namespace c3d {
+
+constexpr int TPB = 128;
+
+// ---------------------------------------------------------------------------------
+// State representation.
+//   FP64 form (R = double): u, v, w, P are FP64 and stencils follow the reference's
+//     expressions, e.g. (u_{i-1} - 2 u_i) + u_{i+1}.
+//   Mixed form (R = float): u, v, w, P are double-float pairs (hi, lo) of FP32 values,
+//     8 bytes like FP64, about 48 significant bits.  Differences of state values are
+//     formed exactly as (a.hi - b.hi) + (a.lo - b.lo) and the update U + delta is an FP32
+//     two-sum, so the mixed form executes no FP64 instruction on its step path; products
+//     and interpolants use hi.
+// ---------------------------------------------------------------------------------
+template <typename R> struct St;
+
+template <> struct St<double> {
+    typedef double S;
+    static __device__ __forceinline__ double hi(double a) { return a; }
+    static __device__ __forceinline__ double d(double a, double b) { return a - b; }
+    static __device__ __forceinline__ double d2(double l, double c, double r) { return (l - 2.0 * c) + r; }
+    static __device__ __forceinline__ double add(double a, double x) { return a + x; }
+    static __device__ __forceinline__ double dbl(double a) { return a; }
+    static __device__ __forceinline__ double scale(double a, double s) { return a * s; }
+    static __host__ __device__ __forceinline__ double from_double(double a) { return a; }
+    // y-viscous stencil HP u+ - HC u + HM u- as in compact3d.f:6119-6122
+    static __device__ __forceinline__ double yvisc(double hp, double hc, double hm, double c0, double up, double uc,
+                                                   double um) {
+        (void)c0;
+        return (hp * up - hc * uc) + hm * um;
+    }
+};
+
+template <> struct St<float> {
+    typedef float2 S;
+    static __device__ __forceinline__ float hi(float2 a) { return a.x; }
+    static __device__ __forceinline__ float d(float2 a, float2 b) { return (a.x - b.x) + (a.y - b.y); }
+    static __device__ __forceinline__ float d2(float2 l, float2 c, float2 r) { return d(l, c) - d(c, r); }
+    static __device__ __forceinline__ float2 add(float2 a, float x) {
+        float s = a.x + x;
+        float v = s - a.x;
+        float e = (a.x - (s - v)) + (x - v);   // two-sum error of a.hi + x
+        e = e + a.y;
+        float h = s + e;
+        float l = e - (h - s);
+        return make_float2(h, l);
+    }
+    static __device__ __forceinline__ double dbl(float2 a) { return (double)a.x + (double)a.y; }
+    static __device__ __forceinline__ float2 scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+    static __host__ __device__ __forceinline__ float2 from_double(double a) {
+        float h = (float)a;
+        return make_float2(h, (float)(a - (double)h));
+    }
+    // HP(u+ - u) - HM(u - u-) + (HP + HM - HC) u: the same stencil without cancellation;
+    // c0 = HP + HM - HC is zero up to rounding for every row of MESH.
+    static __device__ __forceinline__ float yvisc(float hp, float hc, float hm, float c0, float2 up, float2 uc,
+                                                  float2 um) {
+        (void)hc;
+        return (hp * d(up, uc) - hm * d(uc, um)) + c0 * uc.x;
+    }
+};
+
+// Double-float arithmetic (FP32 instructions only, about 48 significant bits), used by
+// the mixed form where a long recurrence must not lose accuracy (Poisson Thomas sweeps).
+__device__ __forceinline__ float2 df_norm(float s, float e) {
+    float h = s + e;
+    return make_float2(h, e - (h - s));
+}
+// a * b
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return df_norm(p, e);
+}
+// q - t with q a plain float
+__device__ __forceinline__ float2 df_fsub(float q, float2 t) {
+    float s = q - t.x;
+    float v = s - q;
+    float e = (q - (s - v)) + (-t.x - v);
+    e -= t.y;
+    return df_norm(s, e);
+}
+
+// Warp shuffles for every state/working type
+__device__ __forceinline__ double shfl_any(double v, int src) { return __shfl_sync(FULL, v, src); }
+__device__ __forceinline__ float shfl_any(float v, int src) { return __shfl_sync(FULL, v, src); }
+__device__ __forceinline__ float2 shfl_any(float2 v, int src) {
+    return make_float2(__shfl_sync(FULL, v.x, src), __shfl_sync(FULL, v.y, src));
+}
+template <typename T>
+__device__ __forceinline__ T sprev(T last, int lane, int P) { return shfl_any(last, (lane == 0) ? P - 1 : lane - 1); }
+template <typename T>
+__device__ __forceinline__ T snext(T first, int lane, int P) { return shfl_any(first, (lane + 1 >= P) ? 0 : lane + 1); }
+
+// Stencils shared by both forms, written once per representation.
+template <typename R> struct Sten;
+template <> struct Sten<double> {
+    // (V2^2 - V1^2) with V2 = (v+ + v)/2, V1 = (v + v-)/2  (compact3d.f:6852-6854)
+    static __device__ __forceinline__ double vv(double vp, double vc, double vm) {
+        double V2 = 0.5 * (vp + vc), V1 = 0.5 * (vc + vm);
+        return V2 * V2 - V1 * V1;
+    }
+    // (a1 + x1) - (a0 + x0): difference of intermediate velocities UH = U + delta
+    static __device__ __forceinline__ double dd(double a1, double x1, double a0, double x0) {
+        return (a1 + x1) - (a0 + x0);
+    }
+    // ((a + delta) - dt*g) - dt*dm, the UPCALC update (compact3d.f:1127)
+    static __device__ __forceinline__ double upd(double a, double delta, double dtg, double dtdm) {
+        return ((a + delta) - dtg) - dtdm;
+    }
+};
+template <> struct Sten<float> {
+    static __device__ __forceinline__ float vv(float2 vp, float2 vc, float2 vm) {
+        float dv = 0.5f * St<float>::d(vp, vm);
+        float sv = 0.5f * ((vp.x + vc.x) + (vc.x + vm.x));
+        return dv * sv;
+    }
+    static __device__ __forceinline__ float dd(float2 a1, float x1, float2 a0, float x0) {
+        return St<float>::d(a1, a0) + (x1 - x0);
+    }
+    static __device__ __forceinline__ float2 upd(float2 a, float delta, float dtg, float dtdm) {
+        return St<float>::add(a, (delta - dtg) - dtdm);
+    }
+};
+
+// ---------------------------------------------------------------------------------
+// Coalesced row I/O through a per-warp shared-memory buffer.  Lane l owns the C
+// consecutive points [l*C, l*C+C) of a row of n = P*C points; the buffer stores point e
+// at e + e/C (one pad slot per chunk) so the chunked reads avoid bank conflicts.
+// ---------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T ldro(const T *p) { return *p; }
+template <> __device__ __forceinline__ double ldro<double>(const double *p) { return __ldg(p); }
+template <> __device__ __forceinline__ float ldro<float>(const float *p) { return __ldg(p); }
+template <> __device__ __forceinline__ float2 ldro<float2>(const float2 *p) { return __ldg(p); }
+
+template <typename T, int C>
+__device__ __forceinline__ void srow_load(T (&v)[C], const T *__restrict__ g, T *sb, int lane, int P) {
+    const int n = P * C;
+#pragma unroll
+    for (int t = 0; t < C; ++t) {
+        int e = lane + 32 * t;
+        if (e < n) sb[e + e / C] = ldro(g + e);
+    }
+    __syncwarp();
+    if (lane < P) {
+#pragma unroll
+        for (int t = 0; t < C; ++t) v[t] = sb[lane * (C + 1) + t];
+    } else {
+#pragma unroll
+        for (int t = 0; t < C; ++t) v[t] = T();
+    }
+    __syncwarp();
+}
+
+template <typename T, int C>
+__device__ __forceinline__ void srow_store(T *__restrict__ g, const T (&v)[C], T *sb, int lane, int P) {
+    const int n = P * C;
+    if (lane < P) {
+#pragma unroll
+        for (int t = 0; t < C; ++t) sb[lane * (C + 1) + t] = v[t];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < C; ++t) {
+        int e = lane + 32 * t;
+        if (e < n) g[e] = sb[e + e / C];
+    }
+    __syncwarp();
+}
+
+// Bytes of the per-warp staging buffer for rows of n1m points.
+__host__ __device__ inline size_t stage_bytes(int n1m, int C) { return (size_t)(n1m + n1m / C + 2) * 8; }
+
+// ---------------------------------------------------------------------------------
+// Complex helpers and the shared-memory Stockham FFT (radices 4, 2, 3)
+// ---------------------------------------------------------------------------------
+template <typename R> struct Cx;
+template <> struct Cx<double> { typedef double2 T; };
+template <> struct Cx<float> { typedef float2 T; };
+
+template <typename C2>
+__device__ __forceinline__ C2 cmul(C2 a, C2 b) {
+    C2 r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+template <typename C2>
+__device__ __forceinline__ C2 cadd(C2 a, C2 b) { C2 r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C2>
+__device__ __forceinline__ C2 csub(C2 a, C2 b) { C2 r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C2>
+__device__ __forceinline__ C2 cconj(C2 a) { a.y = -a.y; return a; }
+template <typename C2>
+__device__ __forceinline__ C2 cmuli(C2 a, int sign) {
+    C2 r;
+    if (sign < 0) { r.x = a.y; r.y = -a.x; } else { r.x = -a.y; r.y = a.x; }
+    return r;
+}
+
+template <typename C2> __device__ __forceinline__ const C2 *twsel(const FftPlan &p);
+template <> __device__ __forceinline__ const double2 *twsel<double2>(const FftPlan &p) { return p.tw64; }
+template <> __device__ __forceinline__ const float2 *twsel<float2>(const FftPlan &p) { return p.tw32; }
+
+// X_s = sum_r v_r exp(sign 2 pi i r s / p), p in {2,3,4}
+template <typename C2>
+__device__ __forceinline__ void dftp(C2 (&v)[4], int p, int sign) {
+    typedef decltype(v[0].x) T;
+    if (p == 4) {
+        C2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+        C2 t2 = cadd(v[1], v[3]), t3 = cmuli(csub(v[1], v[3]), sign);
+        v[0] = cadd(t0, t2);
+        v[2] = csub(t0, t2);
+        v[1] = cadd(t1, t3);
+        v[3] = csub(t1, t3);
+    } else if (p == 2) {
+        C2 a = v[0];
+        v[0] = cadd(a, v[1]);
+        v[1] = csub(a, v[1]);
+    } else {
+        const T h = (T)0.8660254037844386467637;  // sqrt(3)/2
+        C2 t = cadd(v[1], v[2]), u = csub(v[1], v[2]);
+        C2 a;
+        a.x = v[0].x - (T)0.5 * t.x;
+        a.y = v[0].y - (T)0.5 * t.y;
+        C2 b = cmuli(u, sign);
+        b.x *= h;
+        b.y *= h;
+        v[0] = cadd(v[0], t);
+        v[1] = cadd(a, b);
+        v[2] = csub(a, b);
+    }
+}
+
+// Stockham FFT of `lines` sequences of length pl.n at buf[q*es + l*ls]; threads tid..nthr
+// of the warp (BLOCK=false) or block (BLOCK=true) cooperate.  Returns the result buffer.
+template <typename C2, bool BLOCK>
+__device__ C2 *fft_smem(C2 *a, C2 *b, const FftPlan &pl, int lines, int es, int ls, int sign, int tid, int nthr) {
+    const int n = pl.n;
+    const C2 *tw = twsel<C2>(pl);
+    int Ns = 1;
+    for (int s = 0; s < pl.nst; ++s) {
+        const int p = pl.rad[s];
+        const int np = n / p;
+        const int tstep = n / (Ns * p);
+        for (int idx = tid; idx < np * lines; idx += nthr) {
+            const int l = idx % lines, jj = idx / lines;
+            C2 v[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (r < p) v[r] = a[(jj + r * np) * es + l * ls];
+            const int kq = jj % Ns;
+            if (Ns > 1) {
+#pragma unroll
+                for (int r = 1; r < 4; ++r)
+                    if (r < p) {
+                        C2 t = __ldg(&tw[kq * r * tstep]);
+                        if (sign > 0) t.y = -t.y;
+                        v[r] = cmul(v[r], t);
+                    }
+            }
+            dftp(v, p, sign);
+            const int base = (jj / Ns) * Ns * p + kq;
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (r < p) b[(base + r * Ns) * es + l * ls] = v[r];
+        }
+        if (BLOCK) __syncthreads(); else __syncwarp();
+        C2 *t = a;
+        a = b;
+        b = t;
+        Ns *= p;
+    }
+    return a;
+}
+
+// L2 prefetch of one address (fire and forget)
+__device__ __forceinline__ void pf_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// The warp prefetches `bytes` contiguous bytes starting at p into L2 (128-byte lines).
+__device__ __forceinline__ void pf_row(const void *p, int bytes, int lane) {
+    const char *c = (const char *)p;
+    for (int off = lane * 128; off < bytes; off += 32 * 128) pf_l2(c + off);
+}
+
+// The warp prefetches into L2 the window of positions [k0-m, k0+len+m) of the columns it
+// covers: lane t takes positions t, t+32, ...; each position is `span` bytes starting at
+// base + k*stride_bytes (the warp's 32 consecutive columns).
+__device__ __forceinline__ void pf_cols(const void *base, long long stride_bytes, int span, int k0, int m,
+                                        int len, int n, int lane) {
+    const char *b = (const char *)base;
+    for (int t = lane; t < len + 2 * m; t += 32) {
+        int k = k0 - m + t;
+        k = (k % n + n) % n;
+        const char *p = b + (long long)k * stride_bytes;
+        pf_l2(p);
+        if (span > 128) pf_l2(p + 128);
+    }
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(double *addr, double v) {
+    atomicMax(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+inline int nblk(long long n, int b = TPB) { return (int)((n + b - 1) / b); }
+
+// z-direction thread mapping: thread per (i, segment of L points, plane j >= jlo)
+template <int L>
+__device__ __forceinline__ bool zcoord(const Geo &g, int jlo, int &i, int &j, int &k0) {
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nseg = g.n3m / L;
+    const long long tot = (long long)(g.n2m - jlo + 1) * nseg * g.n1m;
+    if (tid >= tot) return false;
+    i = (int)(tid % g.n1m);
+    long long rest = tid / g.n1m;
+    k0 = (int)(rest % nseg) * L;
+    j = jlo + (int)(rest / nseg);
+    return true;
+}
+
+constexpr int ZL = 16;   // z segment length
+constexpr int TWZ = 8;   // kx columns per CTA in the z FFT
+
+}  // namespace c3d

@@ -1,0 +1,217 @@
+// c3d_spec.cu -- the spectral part of GETDP (compact3d.f:9271-9441): complex FFT of the
+// half spectrum along z, and one wall-normal Thomas solve (TDMAP, 9444-9459) per (kx, kz).
+#include "c3d_kern.cuh"
+
+namespace c3d {
+
+// Complex FFT along kz of a tile of TWZ kx columns of one plane, in shared memory.
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_fftz(StepArgs<R> a, int sign) {
+    typedef typename Cx<R>::T C2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Geo g = a.g;
+    const int n = g.n3m;
+    C2 *A = reinterpret_cast<C2 *>(smem_raw), *B = A + n * TWZ;
+    const int ntile = (g.n1h + TWZ - 1) / TWZ;
+    const int plane = blockIdx.x / ntile, tile = blockIdx.x % ntile;
+    const int kx0 = tile * TWZ;
+    const int w = min(TWZ, g.n1h - kx0);
+    C2 *S = reinterpret_cast<C2 *>(a.spec) + (long long)plane * n * g.n1h + kx0;
+    for (int e = threadIdx.x; e < n * TWZ; e += blockDim.x) {
+        int q = e / TWZ, l = e % TWZ;
+        if (l < w) A[e] = S[(long long)q * g.n1h + l];
+        else { A[e].x = 0; A[e].y = 0; }
+    }
+    __syncthreads();
+    C2 *Z = fft_smem<C2, true>(A, B, a.fz, TWZ, TWZ, 1, sign, threadIdx.x, blockDim.x);
+    for (int e = threadIdx.x; e < n * TWZ; e += blockDim.x) {
+        int q = e / TWZ, l = e % TWZ;
+        if (l < w) S[(long long)q * g.n1h + l] = Z[e];
+    }
+}
+
+// One Thomas solve per mode (kx, kz) with A_J = PMJ, B_J = PCJ - AK3 - AK1, C_J = PPJ,
+// factors tabulated by k_ptables; the (0,0) mode has row 1 = (0, 1, 0 | 0) and the
+// imaginary parts of the self-conjugate modes are zero (compact3d.f:9363-9397).
+// FP64 form: FP64 arithmetic.  Mixed form: the same recurrences in double-float
+// arithmetic (FP32 instructions), with double-float factor tables: on stretched grids the
+// low-wavenumber systems are near-singular and an FP32 recurrence loses accuracy.  The
+// forward values are stored at the spectrum's precision between the two sweeps.
+// The j loops load UJ planes ahead so that the sequential chain does not wait on memory.
+constexpr int UJ = 8;
+
+__global__ void __launch_bounds__(TPB) k_poisson64(StepArgs<double> a) {
+    const Geo g = a.g;
+    const int nm = g.n1h * g.n3m;
+    const int mode = blockIdx.x * blockDim.x + threadIdx.x;
+    if (mode >= nm) return;
+    const int kx = mode % g.n1h, kz = mode / g.n1h;
+    const bool selfc = (kx == 0 || kx == g.n1m / 2) && (kz == 0 || kz == g.n3m / 2);
+    double2 *S = reinterpret_cast<double2 *>(a.spec) + mode;
+    const long long s = nm;
+    const int N = g.n2m;
+    const double *RB = a.prb + mode, *GM = a.pgam + mode;
+    double xr = 0.0, xi = 0.0;
+    for (int j0 = 0; j0 < N; j0 += UJ) {
+        double2 q[UJ];
+        double rb[UJ], am[UJ];
+#pragma unroll
+        for (int u = 0; u < UJ; ++u)
+            if (j0 + u < N) { q[u] = S[(j0 + u) * s]; rb[u] = RB[(j0 + u) * s]; am[u] = a.pmj[j0 + u + 1]; }
+#pragma unroll
+        for (int u = 0; u < UJ; ++u) {
+            const int jj = j0 + u;
+            if (jj < N) {
+                double fr = q[u].x;
+                if (jj == 0 && mode == 0) fr = 0.0;      // row 1 of the (1,1) mode: x_1 = 0
+                if (jj == 0) { xr = fr * rb[u]; xi = q[u].y * rb[u]; }
+                else { xr = (fr - am[u] * xr) * rb[u]; xi = (q[u].y - am[u] * xi) * rb[u]; }
+                q[u] = make_double2(xr, xi);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < UJ; ++u)
+            if (j0 + u < N) S[(j0 + u) * s] = q[u];
+    }
+    S[(N - 1) * s] = make_double2(xr, selfc ? 0.0 : xi);
+    for (int jt = N - 2; jt >= 0; jt -= UJ) {
+        double2 q[UJ];
+        double gm[UJ];
+#pragma unroll
+        for (int u = 0; u < UJ; ++u)
+            if (jt - u >= 0) { q[u] = S[(jt - u) * s]; gm[u] = GM[(jt - u + 1) * s]; }
+#pragma unroll
+        for (int u = 0; u < UJ; ++u)
+            if (jt - u >= 0) {
+                xr = q[u].x - gm[u] * xr;
+                xi = q[u].y - gm[u] * xi;
+                q[u] = make_double2(xr, selfc ? 0.0 : xi);
+            }
+#pragma unroll
+        for (int u = 0; u < UJ; ++u)
+            if (jt - u >= 0) S[(jt - u) * s] = q[u];
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_poisson32(StepArgs<float> a) {
+    const Geo g = a.g;
+    const int nm = g.n1h * g.n3m;
+    const int mode = blockIdx.x * blockDim.x + threadIdx.x;
+    if (mode >= nm) return;
+    const int kx = mode % g.n1h, kz = mode / g.n1h;
+    const bool selfc = (kx == 0 || kx == g.n1m / 2) && (kz == 0 || kz == g.n3m / 2);
+    float2 *S = reinterpret_cast<float2 *>(a.spec) + mode;
+    const long long s = nm;
+    const int N = g.n2m;
+    const float2 *RB = a.prbdf + mode, *GM = a.pgamdf + mode;
+    float2 xr = make_float2(0.f, 0.f), xi = xr;
+    for (int j0 = 0; j0 < N; j0 += UJ) {
+        float2 q[UJ], rb[UJ], am[UJ];
+#pragma unroll
+        for (int u = 0; u < UJ; ++u)
+            if (j0 + u < N) { q[u] = S[(j0 + u) * s]; rb[u] = RB[(j0 + u) * s]; am[u] = a.pmjdf[j0 + u + 1]; }
+#pragma unroll
+        for (int u = 0; u < UJ; ++u) {
+            const int jj = j0 + u;
+            if (jj < N) {
+                float fr = q[u].x;
+                if (jj == 0 && mode == 0) fr = 0.f;
+                if (jj == 0) { xr = df_mul(make_float2(fr, 0.f), rb[u]); xi = df_mul(make_float2(q[u].y, 0.f), rb[u]); }
+                else {
+                    xr = df_mul(df_fsub(fr, df_mul(am[u], xr)), rb[u]);
+                    xi = df_mul(df_fsub(q[u].y, df_mul(am[u], xi)), rb[u]);
+                }
+                q[u] = make_float2(xr.x, xi.x);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < UJ; ++u)
+            if (j0 + u < N) S[(j0 + u) * s] = q[u];
+    }
+    S[(N - 1) * s] = make_float2(xr.x, selfc ? 0.f : xi.x);
+    for (int jt = N - 2; jt >= 0; jt -= UJ) {
+        float2 q[UJ], gm[UJ];
+#pragma unroll
+        for (int u = 0; u < UJ; ++u)
+            if (jt - u >= 0) { q[u] = S[(jt - u) * s]; gm[u] = GM[(jt - u + 1) * s]; }
+#pragma unroll
+        for (int u = 0; u < UJ; ++u)
+            if (jt - u >= 0) {
+                xr = df_fsub(q[u].x, df_mul(gm[u], xr));
+                xi = df_fsub(q[u].y, df_mul(gm[u], xi));
+                q[u] = make_float2(xr.x, selfc ? 0.f : xi.x);
+            }
+#pragma unroll
+        for (int u = 0; u < UJ; ++u)
+            if (jt - u >= 0) S[(jt - u) * s] = q[u];
+    }
+}
+
+// Factor tables of TDMAP's recurrence for every mode (FP64; double-float copies when rb32 != 0).
+__global__ void k_ptables(Geo g, const double *ak1, const double *ak3, const double *pmj, const double *pcj,
+                          const double *ppj, double *rb, double *gam, float2 *rb32, float2 *gam32) {
+    const int nm = g.n1h * g.n3m;
+    const int mode = blockIdx.x * blockDim.x + threadIdx.x;
+    if (mode >= nm) return;
+    const int kx = mode % g.n1h, kz = mode / g.n1h;
+    const int kzs = kz <= g.n3m / 2 ? kz : g.n3m - kz;
+    const double lam3 = ak3[kzs], lam1 = ak1[kx];
+    double B1 = pcj[1] - lam3 - lam1, C1 = ppj[1];
+    if (mode == 0) { B1 = 1.0; C1 = 0.0; }
+    double bet = B1;
+    rb[mode] = 1.0 / bet;
+    gam[mode] = 0.0;
+    if (rb32) { rb32[mode] = St<float>::from_double(1.0 / bet); gam32[mode] = make_float2(0.f, 0.f); }
+    double cprev = C1;
+    for (int J = 2; J <= g.n2m; ++J) {
+        double gm = cprev / bet;
+        bet = (pcj[J] - lam3 - lam1) - pmj[J] * gm;
+        const long long q = (long long)(J - 1) * nm + mode;
+        gam[q] = gm;
+        rb[q] = 1.0 / bet;
+        if (rb32) { gam32[q] = St<float>::from_double(gm); rb32[q] = St<float>::from_double(1.0 / bet); }
+        cprev = ppj[J];
+    }
+}
+
+template <typename R>
+void set_spec_smem(c3d_channel *ch) {
+    typedef typename Cx<R>::T C2;
+    const size_t smz = 2 * (size_t)ch->g.n3m * TWZ * sizeof(C2);
+    cudaFuncSetAttribute(k_fftz<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+}
+
+template <typename R>
+int launch_spec(c3d_channel *ch, StepArgs<R> &a, int which, int *nl) {
+    typedef typename Cx<R>::T C2;
+    cudaStream_t st = ch->stream;
+    const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
+    const int ntile = (ch->g.n1h + TWZ - 1) / TWZ;
+    const size_t smz = 2 * (size_t)ch->g.n3m * TWZ * sizeof(C2);
+    switch (which) {
+        case 0: k_fftz<R><<<ch->g.n2m * ntile, TPB, smz, st>>>(a, -1); mark(ch, nl, "fftz_fwd", N * 2 * Rb); break;
+        case 1:
+            if constexpr (sizeof(R) == 8) k_poisson64<<<nblk((long long)ch->g.n1h * ch->g.n3m), TPB, 0, st>>>(a);
+            else k_poisson32<<<nblk((long long)ch->g.n1h * ch->g.n3m), TPB, 0, st>>>(a);
+            mark(ch, nl, "poisson", N * 2 * Rb + N * 8);
+            break;
+        case 2: k_fftz<R><<<ch->g.n2m * ntile, TPB, smz, st>>>(a, +1); mark(ch, nl, "fftz_inv", N * 2 * Rb); break;
+        default: return C3D_EINVAL;
+    }
+    return 0;
+}
+
+int launch_ptables(c3d_channel *ch, const double *ak1, const double *ak3, const double *pm, const double *pc,
+                   const double *pp) {
+    const int nm = ch->g.n1h * ch->g.n3m;
+    k_ptables<<<nblk(nm), TPB, 0, ch->stream>>>(ch->g, ak1, ak3, pm, pc, pp, ch->prb, ch->pgam, ch->prbdf,
+                                                ch->pgamdf);
+    return 0;
+}
+
+template void set_spec_smem<double>(c3d_channel *);
+template void set_spec_smem<float>(c3d_channel *);
+template int launch_spec<double>(c3d_channel *, StepArgs<double> &, int, int *);
+template int launch_spec<float>(c3d_channel *, StepArgs<float> &, int, int *);
+
+}  // namespace c3d

@@ -1,0 +1,576 @@
+// c3d_xpass.cu -- x-row passes of the step: one warp per row (j, k); lane l owns the C
+// consecutive points [l*C, l*C+C); rows move between HBM and registers through a
+// per-warp shared-memory buffer so every global access is coalesced.
+//   xA  RHS1/2/3 pieces along x (compact3d.f:6063-6334, 6784-6900, 7399-7470)
+//   xB  remaining convection terms, AB2 and the x factor of Crank-Nicolson
+//       (compact3d.f:6765-6775, 7385-7392, 8095-8104, 8218-8627)
+//   xC  RHSDP along x and the real-to-complex FFT of RDP along x (8117-8176, 9325-9345)
+//   xD  complex-to-real FFT along x, dDP/dx and the bulk-flow partial sums (9408-9441, 1052-1105)
+//   diag_x  DIVCHECK x part and CFL (9049-9169)
+#include <algorithm>
+#include "c3d_kern.cuh"
+
+namespace c3d {
+
+// ---------------------------------------------------------------------------------
+// xA
+// ---------------------------------------------------------------------------------
+template <typename R, int C>
+__global__ void __launch_bounds__(TPB) k_xA(StepArgs<R> a) {
+    typedef typename SType<R>::S S;
+    typedef St<R> ST;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Geo g = a.g;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int P = g.n1m / C;
+    S *sbS = reinterpret_cast<S *>(smem_raw + wid * stage_bytes(g.n1m, C));
+    R *sbR = reinterpret_cast<R *>(sbS);
+    const int nrows = g.n2m * g.n3m;
+    const R RE1 = a.re1, f12 = a.f12x, f24 = a.f24x, four = (R)4.0;
+    const R presg = (R)a.scal[SCAL_PRESG];
+    for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
+        const int j = 1 + row / g.n3m, k = row % g.n3m;
+        const long long o = fidx(g, 0, j, k), om = fidx(g, 0, j - 1, k), op = fidx(g, 0, j + 1, k);
+        {   // every row this warp reads, requested from DRAM at once
+            const int rb = g.n1m * (int)sizeof(S);
+            pf_row(a.u + om, rb, lane); pf_row(a.u + o, rb, lane); pf_row(a.u + op, rb, lane);
+            pf_row(a.p + o, rb, lane); pf_row(a.p + om, rb, lane);
+            pf_row(a.v + om, rb, lane); pf_row(a.v + o, rb, lane); pf_row(a.v + op, rb, lane);
+            pf_row(a.w + om, rb, lane); pf_row(a.w + o, rb, lane); pf_row(a.w + op, rb, lane);
+        }
+        R uy[C];
+        // ---- u: R1 = visc_y + visc_x/RE - dP/dx - PRESG ; HH1 = d(uu)/dx ----
+        {
+            S uc[C], um[C], up[C];
+            srow_load(uc, a.u + o, sbS, lane, P);
+            srow_load(um, a.u + om, sbS, lane, P);
+            srow_load(up, a.u + op, sbS, lane, P);
+            const R HPj = a.m.hp[j], HCj = a.m.hc[j], HMj = a.m.hm[j], Z0 = a.m.hz[j];
+            R acc[C], d[C];
+            S pv = sprev(uc[C - 1], lane, P), nx = snext(uc[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S l = (t == 0) ? pv : uc[t - 1], rr = (t == C - 1) ? nx : uc[t + 1];
+                d[t] = f12 * ST::d2(l, uc[t], rr);
+            }
+            xsolve(d, lane, P, a.c10x);
+#pragma unroll
+            for (int t = 0; t < C; ++t) acc[t] = RE1 * ST::yvisc(HPj, HCj, HMj, Z0, up[t], uc[t], um[t]) + RE1 * d[t];
+            {
+                S pc[C];
+                srow_load(pc, a.p + o, sbS, lane, P);
+                S pp = sprev(pc[C - 1], lane, P);
+#pragma unroll
+                for (int t = 0; t < C; ++t) {
+                    S l = (t == 0) ? pp : pc[t - 1];
+                    d[t] = f24 * ST::d(pc[t], l);
+                }
+                xsolve(d, lane, P, a.c22x);
+#pragma unroll
+                for (int t = 0; t < C; ++t) acc[t] = acc[t] - d[t] - presg;
+                srow_store(a.r[0] + o, acc, sbR, lane, P);
+            }
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S rr = (t == C - 1) ? nx : uc[t + 1];
+                d[t] = four * (ST::hi(uc[t]) + ST::hi(rr));
+            }
+            xsolve(d, lane, P, a.c6x);
+            R sq[C];
+#pragma unroll
+            for (int t = 0; t < C; ++t) sq[t] = d[t] * d[t];
+            R ps = sprev(sq[C - 1], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                R l = (t == 0) ? ps : sq[t - 1];
+                d[t] = f24 * (sq[t] - l);
+            }
+            xsolve(d, lane, P, a.c22x);
+            srow_store(a.hh[0] + o, d, sbR, lane, P);
+            if (j >= 2) {
+                const R Hj1 = a.m.rh[j], a1 = a.m.hdy[j], a2 = a.m.hdy[j - 1];
+#pragma unroll
+                for (int t = 0; t < C; ++t) uy[t] = Hj1 * (a1 * ST::hi(um[t]) + a2 * ST::hi(uc[t]));
+            }
+        }
+        // ---- v (faces J=2..N2M): R2, HH2 = d(vv)/dy, E_xy = VV1 * UY ----
+        if (j >= 2) {
+            S vc[C], vm[C], vp[C];
+            srow_load(vc, a.v + o, sbS, lane, P);
+            srow_load(vm, a.v + om, sbS, lane, P);
+            srow_load(vp, a.v + op, sbS, lane, P);
+            R d[C], acc[C], hh[C];
+            S pv = sprev(vc[C - 1], lane, P), nx = snext(vc[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S l = (t == 0) ? pv : vc[t - 1], rr = (t == C - 1) ? nx : vc[t + 1];
+                d[t] = f12 * ST::d2(l, vc[t], rr);
+            }
+            xsolve(d, lane, P, a.c10x);
+            const R DYPj = a.m.dyp[j], DYCj = a.m.dyc[j], DYMj = a.m.dym[j], Z0 = a.m.dyz[j];
+            const R Hj = a.m.h[j], Hj1 = a.m.rh[j];
+            {
+                S pc[C], pm[C];
+                srow_load(pc, a.p + o, sbS, lane, P);
+                srow_load(pm, a.p + om, sbS, lane, P);
+#pragma unroll
+                for (int t = 0; t < C; ++t) {
+                    R visc = RE1 * ST::yvisc(DYPj, DYCj, DYMj, Z0, vp[t], vc[t], vm[t]);
+                    R pg = ST::d(pc[t], pm[t]) / Hj;
+                    acc[t] = (-pg + visc) + RE1 * d[t];
+                    hh[t] = Hj1 * Sten<R>::vv(vp[t], vc[t], vm[t]);
+                }
+            }
+            srow_store(a.r[1] + o, acc, sbR, lane, P);
+            srow_store(a.hh[1] + o, hh, sbR, lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S l = (t == 0) ? pv : vc[t - 1];
+                d[t] = four * (ST::hi(l) + ST::hi(vc[t]));
+            }
+            xsolve(d, lane, P, a.c6x);
+#pragma unroll
+            for (int t = 0; t < C; ++t) d[t] = d[t] * uy[t];
+            srow_store(a.exy + o, d, sbR, lane, P);
+        }
+        // ---- w: R3 = visc_y + visc_x/RE ; WW1 = w at x faces ----
+        {
+            S wc[C], wm[C], wp[C];
+            srow_load(wc, a.w + o, sbS, lane, P);
+            srow_load(wm, a.w + om, sbS, lane, P);
+            srow_load(wp, a.w + op, sbS, lane, P);
+            R d[C], acc[C];
+            S pv = sprev(wc[C - 1], lane, P), nx = snext(wc[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S l = (t == 0) ? pv : wc[t - 1], rr = (t == C - 1) ? nx : wc[t + 1];
+                d[t] = f12 * ST::d2(l, wc[t], rr);
+            }
+            xsolve(d, lane, P, a.c10x);
+            const R HPj = a.m.hp[j], HCj = a.m.hc[j], HMj = a.m.hm[j], Z0 = a.m.hz[j];
+#pragma unroll
+            for (int t = 0; t < C; ++t) acc[t] = RE1 * ST::yvisc(HPj, HCj, HMj, Z0, wp[t], wc[t], wm[t]) + RE1 * d[t];
+            srow_store(a.r[2] + o, acc, sbR, lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S l = (t == 0) ? pv : wc[t - 1];
+                d[t] = four * (ST::hi(l) + ST::hi(wc[t]));
+            }
+            xsolve(d, lane, P, a.c6x);
+            srow_store(a.ww1 + o, d, sbR, lane, P);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// xB: remaining convective terms, AB2, x factor of Crank-Nicolson
+// ---------------------------------------------------------------------------------
+template <typename R, int C>
+__device__ __forceinline__ void ab2_cnx(const StepArgs<R> &a, int c, long long o, const R (&hc)[C], R *sb,
+                                        int lane, int P, R dt) {
+    R rr[C], ho[C], d[C];
+    srow_load(rr, a.r[c] + o, sb, lane, P);
+    srow_load(ho, a.ho[c] + o, sb, lane, P);
+#pragma unroll
+    for (int t = 0; t < C; ++t) rr[t] = (rr[t] - (R)1.5 * hc[t] + (R)0.5 * ho[t]) * dt;
+    R pv = sprev(rr[C - 1], lane, P), nx = snext(rr[0], lane, P);
+#pragma unroll
+    for (int t = 0; t < C; ++t) {
+        R l = (t == 0) ? pv : rr[t - 1], r2 = (t == C - 1) ? nx : rr[t + 1];
+        d[t] = (l + (R)10.0 * rr[t]) + r2;
+    }
+    xsolve(d, lane, P, a.cnx);
+    srow_store(a.r[c] + o, d, sb, lane, P);
+}
+
+template <typename R, int C>
+__global__ void __launch_bounds__(TPB) k_xB(StepArgs<R> a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Geo g = a.g;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int P = g.n1m / C;
+    R *sb = reinterpret_cast<R *>(smem_raw + wid * stage_bytes(g.n1m, C));
+    const int nrows = g.n2m * g.n3m;
+    const R f = a.f24x;
+    const R dt = (R)a.dt;
+    for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
+        const int j = 1 + row / g.n3m, k = row % g.n3m;
+        const long long o = fidx(g, 0, j, k), op = fidx(g, 0, j + 1, k);
+        {
+            const int rb = g.n1m * (int)sizeof(R);
+            pf_row(a.hh[0] + o, rb, lane); pf_row(a.hh[1] + o, rb, lane); pf_row(a.hh[2] + o, rb, lane);
+            pf_row(a.exy + o, rb, lane); pf_row(a.exy + op, rb, lane); pf_row(a.exz + o, rb, lane);
+            pf_row(a.eyz + o, rb, lane); pf_row(a.eyz + op, rb, lane);
+            for (int c = 0; c < 3; ++c) { pf_row(a.r[c] + o, rb, lane); pf_row(a.ho[c] + o, rb, lane); }
+        }
+        const R rdy = a.m.rdy[j];
+        R h1[C], h3[C], e[C], ep[C], d[C];
+        srow_load(h1, a.hh[0] + o, sb, lane, P);
+        srow_load(h3, a.hh[2] + o, sb, lane, P);
+        // E_xy at faces j and j+1 (zero on the walls)
+        if (j >= 2) srow_load(e, a.exy + o, sb, lane, P);
+        else {
+#pragma unroll
+            for (int t = 0; t < C; ++t) e[t] = R(0);
+        }
+        if (j + 1 <= g.n2m) srow_load(ep, a.exy + op, sb, lane, P);
+        else {
+#pragma unroll
+            for (int t = 0; t < C; ++t) ep[t] = R(0);
+        }
+#pragma unroll
+        for (int t = 0; t < C; ++t) h1[t] = h1[t] + rdy * (ep[t] - e[t]);   // d(uv)/dy
+        srow_store(a.hh[0] + o, h1, sb, lane, P);
+        ab2_cnx(a, 0, o, h1, sb, lane, P, dt);
+        if (j >= 2) {
+            R h2[C];
+            srow_load(h2, a.hh[1] + o, sb, lane, P);
+            R nx = snext(e[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                R rr = (t == C - 1) ? nx : e[t + 1];
+                d[t] = f * (rr - e[t]);
+            }
+            xsolve(d, lane, P, a.c22x);
+#pragma unroll
+            for (int t = 0; t < C; ++t) h2[t] = h2[t] + d[t];                 // d(uv)/dx
+            srow_store(a.hh[1] + o, h2, sb, lane, P);
+            ab2_cnx(a, 1, o, h2, sb, lane, P, dt);
+        }
+        // d(uw)/dx from E_xz, d(wv)/dy from E_yz at faces j, j+1
+        srow_load(e, a.exz + o, sb, lane, P);
+        {
+            R nx = snext(e[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                R rr = (t == C - 1) ? nx : e[t + 1];
+                d[t] = f * (rr - e[t]);
+            }
+        }
+        xsolve(d, lane, P, a.c22x);
+#pragma unroll
+        for (int t = 0; t < C; ++t) h3[t] = h3[t] + d[t];
+        if (j >= 2) srow_load(e, a.eyz + o, sb, lane, P);
+        else {
+#pragma unroll
+            for (int t = 0; t < C; ++t) e[t] = R(0);
+        }
+        if (j + 1 <= g.n2m) srow_load(ep, a.eyz + op, sb, lane, P);
+        else {
+#pragma unroll
+            for (int t = 0; t < C; ++t) ep[t] = R(0);
+        }
+#pragma unroll
+        for (int t = 0; t < C; ++t) h3[t] = h3[t] + rdy * (ep[t] - e[t]);
+        srow_store(a.hh[2] + o, h3, sb, lane, P);
+        ab2_cnx(a, 2, o, h3, sb, lane, P, dt);
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// xC: RDP = div(UH)/DT and its real-to-complex FFT along x
+// ---------------------------------------------------------------------------------
+template <typename R, int C>
+__global__ void __launch_bounds__(TPB) k_xC(StepArgs<R> a, const R *d0, const R *d1) {
+    typedef typename SType<R>::S S;
+    typedef typename Cx<R>::T C2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Geo g = a.g;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int P = g.n1m / C;
+    const int M = g.n1m / 2;
+    const size_t sbytes = stage_bytes(g.n1m, C), fbytes = 2 * (size_t)(M + 1) * sizeof(C2);
+    unsigned char *wb = smem_raw + wid * (sbytes + fbytes);
+    S *sbS = reinterpret_cast<S *>(wb);
+    R *sbR = reinterpret_cast<R *>(wb);
+    C2 *bufa = reinterpret_cast<C2 *>(wb + sbytes);
+    C2 *bufb = bufa + (M + 1);
+    R *rbuf = reinterpret_cast<R *>(bufa);
+    const int nrows = g.n2m * g.n3m;
+    const R rdt = a.rdt, f24 = a.f24x;
+    const R rdtp = (R)a.dt;
+    const C2 *twx;
+    if constexpr (sizeof(R) == 8) twx = reinterpret_cast<const C2 *>(a.twx64);
+    else twx = reinterpret_cast<const C2 *>(a.twx32);
+    for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
+        const int j = 1 + row / g.n3m, k = row % g.n3m;
+        const long long o = fidx(g, 0, j, k), op = fidx(g, 0, j + 1, k);
+        {
+            const int rs_ = g.n1m * (int)sizeof(S), rr_ = g.n1m * (int)sizeof(R);
+            pf_row(a.u + o, rs_, lane); pf_row(d0 + o, rr_, lane); pf_row(a.rdpz + o, rr_, lane);
+            if (j >= 2) { pf_row(a.v + o, rs_, lane); pf_row(d1 + o, rr_, lane); }
+            if (j + 1 <= g.n2m) { pf_row(a.v + op, rs_, lane); pf_row(d1 + op, rr_, lane); }
+        }
+        R d[C], base[C];
+        {
+            S uc[C];
+            R dd[C];
+            srow_load(uc, a.u + o, sbS, lane, P);
+            srow_load(dd, d0 + o, sbR, lane, P);
+            S nu = snext(uc[0], lane, P);
+            R nd = snext(dd[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S ru = (t == C - 1) ? nu : uc[t + 1];
+                R rd = (t == C - 1) ? nd : dd[t + 1];
+                d[t] = f24 * Sten<R>::dd(ru, rd, uc[t], dd[t]);
+            }
+            xsolve(d, lane, P, a.c22x);
+        }
+        {
+            const bool up = (j + 1 <= g.n2m), lo = (j >= 2);
+            S vp[C], vc[C];
+            R dp_[C], dc_[C];
+            if (up) { srow_load(vp, a.v + op, sbS, lane, P); srow_load(dp_, d1 + op, sbR, lane, P); }
+            if (lo) { srow_load(vc, a.v + o, sbS, lane, P); srow_load(dc_, d1 + o, sbR, lane, P); }
+            const R dyj = a.m.dy[j];
+            const S zs = S();
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                // (FJUP*UH2(J+1) - FJUM*UH2(J))/DY(J), UH2 = V + delta2, UH2 = 0 on the walls
+                R dv = Sten<R>::dd(up ? vp[t] : zs, up ? dp_[t] : R(0), lo ? vc[t] : zs, lo ? dc_[t] : R(0));
+                base[t] = dv / dyj * rdt;
+            }
+        }
+        {
+            R zc[C];
+            srow_load(zc, a.rdpz + o, sbR, lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) d[t] = (base[t] + d[t] / rdtp) + zc[t];
+        }
+        // real row -> shared memory as M complex values, FFT, post-process to N1M/2+1 modes
+        if (lane < P) {
+#pragma unroll
+            for (int t = 0; t < C; ++t) rbuf[lane * C + t] = d[t];
+        }
+        __syncwarp();
+        C2 *Z = fft_smem<C2, false>(bufa, bufb, a.fx, 1, 1, 0, -1, lane, 32);
+        C2 *Sp = reinterpret_cast<C2 *>(a.spec) + ((long long)(j - 1) * g.n3m + k) * g.n1h;
+        for (int kx = lane; kx <= M; kx += 32) {
+            C2 zk = Z[kx == M ? 0 : kx], zm = cconj(Z[kx == 0 ? 0 : M - kx]);
+            C2 E, O;
+            E.x = (R)0.5 * (zk.x + zm.x);
+            E.y = (R)0.5 * (zk.y + zm.y);
+            C2 df = csub(zk, zm);
+            O.x = (R)0.5 * df.y;
+            O.y = (R)-0.5 * df.x;
+            Sp[kx] = cadd(E, cmul(twx[kx], O));
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// xD: complex-to-real FFT -> DP, compact dDP/dx, bulk-flow partial sums
+// ---------------------------------------------------------------------------------
+template <typename R, int C>
+__global__ void __launch_bounds__(TPB) k_xD(StepArgs<R> a, const R *d0, const R *d2) {
+    typedef typename Cx<R>::T C2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Geo g = a.g;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int P = g.n1m / C;
+    const int M = g.n1m / 2;
+    const size_t sbytes = stage_bytes(g.n1m, C), fbytes = 2 * (size_t)(M + 1) * sizeof(C2);
+    unsigned char *wb = smem_raw + wid * (sbytes + fbytes);
+    R *sbR = reinterpret_cast<R *>(wb);
+    C2 *bufa = reinterpret_cast<C2 *>(wb + sbytes);
+    C2 *bufb = bufa + (M + 1);
+    const int nrows = g.n2m * g.n3m;
+    const C2 *twx;
+    if constexpr (sizeof(R) == 8) twx = reinterpret_cast<const C2 *>(a.twx64);
+    else twx = reinterpret_cast<const C2 *>(a.twx32);
+    const R scale = (R)(1.0 / ((double)g.n1m * (double)g.n3m)), f24 = a.f24x;
+    for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
+        const int j = 1 + row / g.n3m, k = row % g.n3m;
+        const long long o = fidx(g, 0, j, k);
+        const C2 *Sp = reinterpret_cast<const C2 *>(a.spec) + ((long long)(j - 1) * g.n3m + k) * g.n1h;
+        {
+            const int rr_ = g.n1m * (int)sizeof(R);
+            pf_row(d0 + o, rr_, lane); pf_row(d2 + o, rr_, lane);
+        }
+        for (int kx = lane; kx <= M; kx += 32) bufb[kx] = Sp[kx];
+        __syncwarp();
+        for (int kx = lane; kx < M; kx += 32) {
+            C2 xk = bufb[kx], xm = cconj(bufb[M - kx]);
+            C2 E = cadd(xk, xm);
+            C2 O = cmul(csub(xk, xm), cconj(twx[kx]));
+            C2 Z;
+            Z.x = E.x - O.y;
+            Z.y = E.y + O.x;
+            bufa[kx] = Z;
+        }
+        __syncwarp();
+        C2 *Zr = fft_smem<C2, false>(bufa, bufb, a.fx, 1, 1, 0, +1, lane, 32);
+        const R *rz = reinterpret_cast<const R *>(Zr);
+        R dpv[C];
+        if (lane < P) {
+#pragma unroll
+            for (int t = 0; t < C; ++t) dpv[t] = rz[lane * C + t] * scale;
+        } else {
+#pragma unroll
+            for (int t = 0; t < C; ++t) dpv[t] = R(0);
+        }
+        __syncwarp();
+        srow_store(a.dp + o, dpv, sbR, lane, P);
+        R d[C];
+        R pv = sprev(dpv[C - 1], lane, P);
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            R l = (t == 0) ? pv : dpv[t - 1];
+            d[t] = f24 * (dpv[t] - l);
+        }
+        xsolve(d, lane, P, a.c22x);
+        srow_store(a.g1 + o, d, sbR, lane, P);
+        // bulk-flow partial sums: sum_i delta * DY(J)/DX3/DX1 for u and w (FP64 across lanes)
+        R q1[C], q3[C];
+        srow_load(q1, d0 + o, sbR, lane, P);
+        srow_load(q3, d2 + o, sbR, lane, P);
+        R l1 = R(0), l3 = R(0);
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            l1 += q1[t];
+            l3 += q3[t];
+        }
+        double s1 = (double)l1, s3 = (double)l3;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            s1 += __shfl_down_sync(FULL, s1, off);
+            s3 += __shfl_down_sync(FULL, s3, off);
+        }
+        if (lane == 0) {
+            const double wgt = g.dy[j] / g.dx3 / g.dx1;
+            a.part[row] = s1 * wgt;
+            a.part[nrows + row] = s3 * wgt;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Diagnostics, x part: DIVCHECK's (V(J+1)-V(J))/DY + compact dU/dx into an FP64
+// scratch field, and the CFL maximum.  Always FP64.
+// ---------------------------------------------------------------------------------
+template <typename R, int C>
+__global__ void __launch_bounds__(TPB) k_diag_x(StepArgs<R> a, double *divx, Cyc<double> c22) {
+    typedef typename SType<R>::S S;
+    typedef St<R> ST;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Geo g = a.g;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int P = g.n1m / C;
+    S *sbS = reinterpret_cast<S *>(smem_raw + wid * stage_bytes(g.n1m, C));
+    double *sbD = reinterpret_cast<double *>(sbS);
+    const int nrows = g.n2m * g.n3m;
+    double cmax = 0.0;
+    int bad = 0;
+    for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
+        const int j = 1 + row / g.n3m, k = row % g.n3m;
+        const int kp = (k + 1 == g.n3m) ? 0 : k + 1;
+        const long long o = fidx(g, 0, j, k), op = fidx(g, 0, j + 1, k), okp = fidx(g, 0, j, kp);
+        S su[C], sv[C], svp[C], sw[C], swk[C];
+        srow_load(su, a.u + o, sbS, lane, P);
+        srow_load(sv, a.v + o, sbS, lane, P);
+        srow_load(svp, a.v + op, sbS, lane, P);
+        srow_load(sw, a.w + o, sbS, lane, P);
+        srow_load(swk, a.w + okp, sbS, lane, P);
+        double uc[C], d[C];
+#pragma unroll
+        for (int t = 0; t < C; ++t) uc[t] = ST::dbl(su[t]);
+        double nx = snext(uc[0], lane, P);
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            double rr = (t == C - 1) ? nx : uc[t + 1];
+            d[t] = 24.0 * g.dx1 * (rr - uc[t]);
+        }
+        xsolve(d, lane, P, c22);
+        const double dyj = g.dy[j];
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            double rr = (t == C - 1) ? nx : uc[t + 1];
+            double vc = ST::dbl(sv[t]), vp = ST::dbl(svp[t]);
+            d[t] = (vp - vc) / dyj + d[t];
+            double cf = fabs(uc[t] + rr) * 0.5 * g.dx1 + fabs(vc + vp) * 0.5 / dyj +
+                        fabs(ST::dbl(sw[t]) + ST::dbl(swk[t])) * 0.5 * g.dx3;
+            if (lane < P) {
+                if (!isfinite(cf)) bad = 1;
+                cmax = fmax(cmax, cf);
+            }
+        }
+        srow_store(divx + o, d, sbD, lane, P);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        cmax = fmax(cmax, __shfl_down_sync(FULL, cmax, off));
+        bad |= __shfl_down_sync(FULL, bad, off);
+    }
+    if (lane == 0) {
+        atomic_max_nonneg(&a.scal[SCAL_CFL], cmax);
+        if (bad) a.scal[SCAL_NONFIN] = 1.0;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// launcher
+// ---------------------------------------------------------------------------------
+template <typename R, int C>
+static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl) {
+    typedef typename Cx<R>::T C2;
+    const int nrows = ch->g.n2m * ch->g.n3m;
+    const int grid = nblk(nrows, TPB / 32);
+    cudaStream_t st = ch->stream;
+    const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
+    const size_t sb = stage_bytes(ch->g.n1m, C) * (TPB / 32);
+    const int M = ch->g.n1m / 2;
+    const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(M + 1) * sizeof(C2)) * (TPB / 32);
+    switch (which) {
+        case 0:
+            cudaFuncSetAttribute(k_xA<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
+            k_xA<R, C><<<grid, TPB, sb, st>>>(a);
+            mark(ch, nl, "xA", N * (32 + 7 * Rb));
+            break;
+        case 1:
+            cudaFuncSetAttribute(k_xB<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
+            k_xB<R, C><<<grid, TPB, sb, st>>>(a);
+            mark(ch, nl, "xB", N * 18 * Rb);
+            break;
+        case 2:
+            cudaFuncSetAttribute(k_xC<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
+            k_xC<R, C><<<grid, TPB, fb, st>>>(a, p0, p1);
+            mark(ch, nl, "xC", N * (16 + 4 * Rb));
+            break;
+        case 3:
+            cudaFuncSetAttribute(k_xD<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
+            k_xD<R, C><<<grid, TPB, fb, st>>>(a, p0, p1);
+            mark(ch, nl, "xD", N * 5 * Rb);
+            break;
+        case 4: {
+            const double b = 22.0, r = -2.0 / (b + sqrt(b * b - 4.0));
+            Cyc<double> c22 = {r, -r, (int)ceil(log(1e-17) / log(fabs(r)))};
+            cudaFuncSetAttribute(k_diag_x<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
+            k_diag_x<R, C><<<grid, TPB, sb, st>>>(a, (double *)p0, c22);
+            mark(ch, nl, "diag_x", N * 48);
+            break;
+        }
+        default: return C3D_EINVAL;
+    }
+    return 0;
+}
+
+template <typename R>
+int launch_xpass(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl) {
+    switch ((ch->g.n1m + 31) / 32) {
+        case 1: return launch_x_c<R, 1>(ch, a, which, p0, p1, nl);
+        case 2: return launch_x_c<R, 2>(ch, a, which, p0, p1, nl);
+        case 3: return launch_x_c<R, 3>(ch, a, which, p0, p1, nl);
+        case 4: return launch_x_c<R, 4>(ch, a, which, p0, p1, nl);
+        case 6: return launch_x_c<R, 6>(ch, a, which, p0, p1, nl);
+        case 8: return launch_x_c<R, 8>(ch, a, which, p0, p1, nl);
+        case 12: return launch_x_c<R, 12>(ch, a, which, p0, p1, nl);
+        default: set_error("unsupported N1M"); return C3D_EINVAL;
+    }
+}
+
+template int launch_xpass<double>(c3d_channel *, StepArgs<double> &, int, const double *, const double *, int *);
+template int launch_xpass<float>(c3d_channel *, StepArgs<float> &, int, const float *, const float *, int *);
+
+}  // namespace c3d

@@ -1,0 +1,377 @@
+// c3d_zpass.cu -- z-column passes of the step: one thread per (i, segment of ZL points,
+// plane j); consecutive threads take consecutive i, so every access is coalesced.  The
+// cyclic compact solves use the warm-up recurrences of zseg (c3d_dev.cuh).
+//   zA  RHS1/2/3 pieces along z (compact3d.f:6160-6185, 6337-6433, 6957-7060, 7474-7705)
+//   zB  d(uw)/dz, d(vw)/dz, d(ww)/dz (1,22,1)
+//   zC  z factor of Crank-Nicolson (CTDMA3I in GETUH1-3)
+//   zD  RHSDP along z (8187-8210)
+//   zE  UPCALC along z and the velocity / pressure update (1052-1238)
+//   diag_z  DIVCHECK z part and max|div| (9099-9128)
+#include "c3d_kern.cuh"
+
+namespace c3d {
+
+// ---------------------------------------------------------------------------------
+// Column walkers for zsweep: each keeps a sliding window of its stencil inputs in
+// registers and loads one new value per position.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ int znext(int k, int n) { return (k + 1 == n) ? 0 : k + 1; }
+__device__ __forceinline__ int zprev(int k, int n) { return (k == 0) ? n - 1 : k - 1; }
+
+// state column: (1,10,1) RHS f12*(u- - 2u + u+) and (1,6,1) RHS 4*(u- + u) (face k)
+template <typename R>
+struct WalkVisBack {
+    typedef typename SType<R>::S S;
+    const S *col; int n, s; R f12; S um, uc; int kn;
+    __device__ void start(int k) { um = col[zprev(k, n) * s]; uc = col[k * s]; kn = znext(k, n); }
+    __device__ void next(R (&d)[2]) {
+        S up = col[kn * s];
+        d[0] = f12 * St<R>::d2(um, uc, up);
+        d[1] = (R)4.0 * (St<R>::hi(um) + St<R>::hi(uc));
+        um = uc; uc = up; kn = znext(kn, n);
+    }
+};
+
+// W and P columns: f12*(w- - 2w + w+), 4*(w + w+) (centre k) and f24*(p - p-) (face k)
+template <typename R>
+struct WalkWP {
+    typedef typename SType<R>::S S;
+    const S *W, *P; int n, s; R f12, f24; S wm, wc, pm; int kn, kc;
+    __device__ void start(int k) {
+        wm = W[zprev(k, n) * s]; wc = W[k * s]; pm = P[zprev(k, n) * s]; kc = k; kn = znext(k, n);
+    }
+    __device__ void next(R (&d)[3]) {
+        S wp = W[kn * s], pc = P[kc * s];
+        d[0] = f12 * St<R>::d2(wm, wc, wp);
+        d[1] = (R)4.0 * (St<R>::hi(wc) + St<R>::hi(wp));
+        d[2] = f24 * St<R>::d(pc, pm);
+        wm = wc; wc = wp; pm = pc; kc = kn; kn = znext(kn, n);
+    }
+};
+
+// zB: f*(Exz+ - Exz), f*(Q - Q-), f*(Eyz+ - Eyz)
+template <typename R>
+struct WalkZB {
+    const R *E1, *Q, *E2; int n, s; R f; R e1, qm, e2; int kn, kc; bool v;
+    __device__ void start(int k) {
+        e1 = E1[k * s]; qm = Q[zprev(k, n) * s]; e2 = v ? E2[k * s] : R(0); kc = k; kn = znext(k, n);
+    }
+    __device__ void next(R (&d)[3]) {
+        R e1p = E1[kn * s], qc = Q[kc * s], e2p = v ? E2[kn * s] : R(0);
+        d[0] = f * (e1p - e1);
+        d[1] = f * (qc - qm);
+        d[2] = f * (e2p - e2);
+        e1 = e1p; qm = qc; e2 = e2p; kc = kn; kn = znext(kn, n);
+    }
+};
+
+// zC: (x- + 10x) + x+ for the three components
+template <typename R>
+struct WalkCN {
+    const R *X[3]; int n, s; R xm[3], xc[3]; int kn;
+    __device__ void start(int k) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { xm[c] = X[c][zprev(k, n) * s]; xc[c] = X[c][k * s]; }
+        kn = znext(k, n);
+    }
+    __device__ void next(R (&d)[3]) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            R xp = X[c][kn * s];
+            d[c] = (xm[c] + (R)10.0 * xc[c]) + xp;
+            xm[c] = xc[c]; xc[c] = xp;
+        }
+        kn = znext(kn, n);
+    }
+};
+
+// zD: f24*((W+ + D+) - (W + D))
+template <typename R>
+struct WalkDivZ {
+    typedef typename SType<R>::S S;
+    const S *W; const R *D; int n, s; R f24; S wc; R dc; int kn;
+    __device__ void start(int k) { wc = W[k * s]; dc = D[k * s]; kn = znext(k, n); }
+    __device__ void next(R (&d)[1]) {
+        S wp = W[kn * s]; R dp = D[kn * s];
+        d[0] = f24 * Sten<R>::dd(wp, dp, wc, dc);
+        wc = wp; dc = dp; kn = znext(kn, n);
+    }
+};
+
+// zE: f24*(DP - DP-)
+template <typename R>
+struct WalkGradZ {
+    const R *DP; int n, s; R f24; R pm; int kc;
+    __device__ void start(int k) { pm = DP[zprev(k, n) * s]; kc = k; }
+    __device__ void next(R (&d)[1]) {
+        R pc = DP[kc * s];
+        d[0] = f24 * (pc - pm);
+        pm = pc; kc = znext(kc, n);
+    }
+};
+
+template <typename R, int L>
+__global__ void __launch_bounds__(TPB) k_zA(StepArgs<R> a) {
+    typedef typename SType<R>::S S;
+    typedef St<R> ST;
+    const Geo g = a.g;
+    int i, j, k0;
+    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    const int n = g.n3m, s = g.n1m;
+    const R RE1 = a.re1;
+    const long long o = fidx(g, i, j, 0);
+    constexpr int M6 = WM<R>::M6;
+    if ((g.n1m & 31) == 0) {   // the warp's column windows (32 consecutive i), requested at once
+        const int lane = threadIdx.x & 31;
+        const long long o0 = fidx(g, i - lane, j, 0), sb = (long long)g.n1m;
+        const int ss = 32 * (int)sizeof(S), sr = 32 * (int)sizeof(R);
+        pf_cols(a.u + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
+        pf_cols(a.w + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
+        pf_cols(a.p + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
+        if (j >= 2) pf_cols(a.v + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
+        pf_cols(a.ww1 + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
+        for (int c = 0; c < 3; ++c) pf_cols(a.r[c] + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
+    }
+    {   // u: R1 += (1/RE) d2u/dz2 ; E_xz = UU3 * WW1
+        R out[2][L];
+        const R rr[2] = {a.c10z.r, a.c6z.r}, ss[2] = {a.c10z.s, a.c6z.s};
+        WalkVisBack<R> f{a.u + o, n, s, a.f12z};
+        zsweep<R, L, M6, 2>(out, k0, n, rr, ss, f);
+        R *Rp = a.r[0] + o, *E = a.exz + o;
+        const R *Wx = a.ww1 + o;
+#pragma unroll
+        for (int t = 0; t < L; ++t) {
+            const int kk = (k0 + t) * s;
+            Rp[kk] = Rp[kk] + RE1 * out[0][t];
+            E[kk] = out[1][t] * Wx[kk];
+        }
+    }
+    {   // w, P: R3 += (1/RE) d2w/dz2 - dP/dz - PRESG3 ; WW3^2
+        R out[3][L];
+        const R rr[3] = {a.c10z.r, a.c6z.r, a.c22z.r}, ss[3] = {a.c10z.s, a.c6z.s, a.c22z.s};
+        WalkWP<R> f{a.w + o, a.p + o, n, s, a.f12z, a.f24z};
+        zsweep<R, L, M6, 3>(out, k0, n, rr, ss, f);
+        const R presg3 = (R)a.scal[SCAL_PRESG3];
+        R *Rp = a.r[2] + o, *Q = a.wsq + o;
+#pragma unroll
+        for (int t = 0; t < L; ++t) {
+            const int kk = (k0 + t) * s;
+            Rp[kk] = Rp[kk] + RE1 * out[0][t] - out[2][t] - presg3;
+            Q[kk] = out[1][t] * out[1][t];
+        }
+    }
+    if (j >= 2) {   // v: R2 += (1/RE) d2v/dz2 ; E_yz = VV3 * (w at y face J)
+        R out[2][L];
+        const R rr[2] = {a.c10z.r, a.c6z.r}, ss[2] = {a.c10z.s, a.c6z.s};
+        WalkVisBack<R> f{a.v + o, n, s, a.f12z};
+        zsweep<R, L, M6, 2>(out, k0, n, rr, ss, f);
+        const R Hj1 = a.m.rh[j], a1 = a.m.hdy[j], a2 = a.m.hdy[j - 1];
+        const S *W = a.w + o, *Wm = a.w + fidx(g, i, j - 1, 0);
+        R *Rp = a.r[1] + o, *E = a.eyz + o;
+#pragma unroll
+        for (int t = 0; t < L; ++t) {
+            const int kk = (k0 + t) * s;
+            Rp[kk] = Rp[kk] + RE1 * out[0][t];
+            R wy = Hj1 * (a1 * ST::hi(Wm[kk]) + a2 * ST::hi(W[kk]));
+            E[kk] = out[1][t] * wy;
+        }
+    }
+}
+
+template <typename R, int L>
+__global__ void __launch_bounds__(TPB) k_zB(StepArgs<R> a) {
+    const Geo g = a.g;
+    int i, j, k0;
+    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    const int n = g.n3m, s = g.n1m;
+    const long long o = fidx(g, i, j, 0);
+    if ((g.n1m & 31) == 0) {
+        const int lane = threadIdx.x & 31;
+        const long long o0 = fidx(g, i - lane, j, 0), sb = (long long)g.n1m;
+        pf_cols(a.exz + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::M22 + 1, L, n, lane);
+        pf_cols(a.wsq + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::M22 + 1, L, n, lane);
+        pf_cols(a.eyz + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::M22 + 1, L, n, lane);
+        pf_cols(a.hh[0] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
+        pf_cols(a.hh[1] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
+    }
+    R out[3][L];
+    const R rr[3] = {a.c22z.r, a.c22z.r, a.c22z.r}, ss[3] = {a.c22z.s, a.c22z.s, a.c22z.s};
+    WalkZB<R> f{a.exz + o, a.wsq + o, a.eyz + o, n, s, a.f24z};
+    f.v = (j >= 2);
+    zsweep<R, L, WM<R>::M22, 3>(out, k0, n, rr, ss, f);
+    R *H1 = a.hh[0] + o, *H2 = a.hh[1] + o, *H3 = a.hh[2] + o;
+#pragma unroll
+    for (int t = 0; t < L; ++t) {
+        const int kk = (k0 + t) * s;
+        H1[kk] = H1[kk] + out[0][t];          // d(uw)/dz
+        H3[kk] = out[1][t];                   // d(ww)/dz
+        if (j >= 2) H2[kk] = H2[kk] + out[2][t];   // d(vw)/dz
+    }
+}
+
+// z factor of Crank-Nicolson: r[c] -> d[c] for the three components (the v component at
+// J=1 is computed from zeros and never read)
+template <typename R, int L>
+__global__ void __launch_bounds__(TPB) k_zC(StepArgs<R> a, R *d0, R *d1, R *d2) {
+    const Geo g = a.g;
+    int i, j, k0;
+    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    const int n = g.n3m, s = g.n1m;
+    const long long o = fidx(g, i, j, 0);
+    if ((g.n1m & 31) == 0) {
+        const int lane = threadIdx.x & 31;
+        const long long o0 = fidx(g, i - lane, j, 0), sb = (long long)g.n1m;
+        pf_cols(a.r[0] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::MCN + 1, L, n, lane);
+        pf_cols(a.r[1] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::MCN + 1, L, n, lane);
+        pf_cols(a.r[2] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::MCN + 1, L, n, lane);
+    }
+    R out[3][L];
+    const R rr[3] = {a.cnz.r, a.cnz.r, a.cnz.r}, ss[3] = {a.cnz.s, a.cnz.s, a.cnz.s};
+    WalkCN<R> f;
+    f.X[0] = a.r[0] + o; f.X[1] = a.r[1] + o; f.X[2] = a.r[2] + o;
+    f.n = n; f.s = s;
+    zsweep<R, L, WM<R>::MCN, 3>(out, k0, n, rr, ss, f);
+    R *D0 = d0 + o, *D1 = d1 + o, *D2 = d2 + o;
+#pragma unroll
+    for (int t = 0; t < L; ++t) {
+        const int kk = (k0 + t) * s;
+        D0[kk] = out[0][t];
+        D1[kk] = out[1][t];
+        D2[kk] = out[2][t];
+    }
+}
+
+// z part of RHSDP: rdpz = compact d(UH3)/dz / DT with UH3 = W + delta3
+template <typename R, int L>
+__global__ void __launch_bounds__(TPB) k_zD(StepArgs<R> a, const R *d2) {
+    const Geo g = a.g;
+    int i, j, k0;
+    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    const int n = g.n3m, s = g.n1m;
+    const long long o = fidx(g, i, j, 0);
+    if ((g.n1m & 31) == 0) {
+        const int lane = threadIdx.x & 31;
+        const long long o0 = fidx(g, i - lane, j, 0), sb = (long long)g.n1m;
+        pf_cols(a.w + o0, sb * sizeof(typename SType<R>::S), 32 * (int)sizeof(typename SType<R>::S), k0, WM<R>::M22 + 1, L, n, lane);
+        pf_cols(d2 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::M22 + 1, L, n, lane);
+    }
+    R out[1][L];
+    const R rr[1] = {a.c22z.r}, ss[1] = {a.c22z.s};
+    WalkDivZ<R> f{a.w + o, d2 + o, n, s, a.f24z};
+    zsweep<R, L, WM<R>::M22, 1>(out, k0, n, rr, ss, f);
+    const R rdt = (R)a.dt;
+    R *Q = a.rdpz + o;
+#pragma unroll
+    for (int t = 0; t < L; ++t) Q[(k0 + t) * s] = out[0][t] / rdt;
+}
+
+// UPCALC along z and the state update
+template <typename R, int L>
+__global__ void __launch_bounds__(TPB) k_zE(StepArgs<R> a, const R *d0, const R *d1, const R *d2, int updp) {
+    typedef typename SType<R>::S S;
+    typedef St<R> ST;
+    const Geo g = a.g;
+    int i, j, k0;
+    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    const int n = g.n3m, s = g.n1m;
+    const long long o = fidx(g, i, j, 0);
+    const R dt = (R)a.dt;
+    const R dtdm = dt * (R)a.scal[SCAL_DMPRESG], dtdm3 = dt * (R)a.scal[SCAL_DMPRESG3];
+    const R *DP = a.dp + o;
+    if ((g.n1m & 31) == 0) {
+        const int lane = threadIdx.x & 31;
+        const long long o0 = fidx(g, i - lane, j, 0), sb = (long long)g.n1m;
+        pf_cols(a.dp + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::M22 + 1, L, n, lane);
+        pf_cols(a.u + o0, sb * sizeof(S), 32 * (int)sizeof(S), k0, 0, L, n, lane);
+        pf_cols(a.v + o0, sb * sizeof(S), 32 * (int)sizeof(S), k0, 0, L, n, lane);
+        pf_cols(a.w + o0, sb * sizeof(S), 32 * (int)sizeof(S), k0, 0, L, n, lane);
+        pf_cols(a.p + o0, sb * sizeof(S), 32 * (int)sizeof(S), k0, 0, L, n, lane);
+        pf_cols(d0 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
+        pf_cols(d1 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
+        pf_cols(d2 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
+        pf_cols(a.g1 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
+    }
+    R out[1][L];
+    const R rr[1] = {a.c22z.r}, ss[1] = {a.c22z.s};
+    WalkGradZ<R> f{DP, n, s, a.f24z};
+    zsweep<R, L, WM<R>::M22, 1>(out, k0, n, rr, ss, f);
+    S *W = a.w + o, *U = a.u + o, *V = a.v + o, *Pp = a.p + o;
+    const R *D0 = d0 + o, *D1 = d1 + o, *D2 = d2 + o, *G1 = a.g1 + o;
+    const R *DPm = a.dp + fidx(g, i, j - 1, 0);
+    const R Hj = a.m.h[j];
+#pragma unroll
+    for (int t = 0; t < L; ++t) {
+        const int kk = (k0 + t) * s;
+        W[kk] = Sten<R>::upd(W[kk], D2[kk], dt * out[0][t], dtdm3);
+        U[kk] = Sten<R>::upd(U[kk], D0[kk], dt * G1[kk], dtdm);
+        if (j >= 2) V[kk] = Sten<R>::upd(V[kk], D1[kk], dt * (DP[kk] - DPm[kk]) / Hj, R(0));
+        if (updp) Pp[kk] = ST::add(Pp[kk], DP[kk]);
+    }
+}
+
+// DIVCHECK z part and max |div| (FP64)
+template <typename R, int L>
+__global__ void __launch_bounds__(TPB) k_diag_z(StepArgs<R> a, const double *divx, Cyc<double> c22) {
+    typedef typename SType<R>::S S;
+    typedef St<R> ST;
+    const Geo g = a.g;
+    int i, j, k0;
+    double m = 0.0;
+    int bad = 0;
+    if (zcoord<L>(g, 1, i, j, k0)) {
+        const int n = g.n3m, s = g.n1m;
+        const long long o = fidx(g, i, j, 0);
+        const S *W = a.w + o;
+        const double *DX = divx + o;
+        double out[L];
+        zseg<double, L>(out, k0, n, c22, [&](int kk) {
+            int kp = kk == n - 1 ? 0 : kk + 1;
+            return 24.0 * g.dx3 * (ST::dbl(W[kp * s]) - ST::dbl(W[kk * s]));
+        });
+#pragma unroll
+        for (int t = 0; t < L; ++t) {
+            double dv = DX[(k0 + t) * s] + out[t];
+            if (!isfinite(dv)) bad = 1;
+            m = fmax(m, fabs(dv));
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        m = fmax(m, __shfl_down_sync(FULL, m, off));
+        bad |= __shfl_down_sync(FULL, bad, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomic_max_nonneg(&a.scal[SCAL_DIVMAX], m);
+        if (bad) a.scal[SCAL_NONFIN] = 1.0;
+    }
+}
+
+template <typename R>
+int launch_zpass(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *d1, R *d2, int flag, int *nl) {
+    constexpr int L = ZL;
+    const long long nt = (long long)ch->g.n2m * (ch->g.n3m / L) * ch->g.n1m;
+    const int nb = nblk(nt);
+    cudaStream_t st = ch->stream;
+    const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
+    switch (which) {
+        case 0: k_zA<R, L><<<nb, TPB, 0, st>>>(a); mark(ch, nl, "zA", N * (32 + 10 * Rb)); break;
+        case 1: k_zB<R, L><<<nb, TPB, 0, st>>>(a); mark(ch, nl, "zB", N * 8 * Rb); break;
+        case 2: k_zC<R, L><<<nb, TPB, 0, st>>>(a, d0, d1, d2); mark(ch, nl, "zC", N * 6 * Rb); break;
+        case 3: k_zD<R, L><<<nb, TPB, 0, st>>>(a, d2); mark(ch, nl, "zD", N * (8 + 2 * Rb)); break;
+        case 4: k_zE<R, L><<<nb, TPB, 0, st>>>(a, d0, d1, d2, flag); mark(ch, nl, "zE", N * (64 + 5 * Rb)); break;
+        case 5: {
+            const double b = 22.0, r = -2.0 / (b + sqrt(b * b - 4.0));
+            Cyc<double> c22 = {r, -r, (int)ceil(log(1e-17) / log(fabs(r)))};
+            k_diag_z<R, L><<<nb, TPB, 0, st>>>(a, (const double *)d0, c22);
+            mark(ch, nl, "diag_z", N * 16);
+            break;
+        }
+        default: return C3D_EINVAL;
+    }
+    return 0;
+}
+
+template int launch_zpass<double>(c3d_channel *, StepArgs<double> &, int, double *, double *, double *, int, int *);
+template int launch_zpass<float>(c3d_channel *, StepArgs<float> &, int, float *, float *, float *, int, int *);
+
+}  // namespace c3d
