@@ -338,11 +338,92 @@ def run_ours(args, D: Dist):
         ce.close()
     ch.close()
 
+    # ---- batched ensemble (configs with many independent channels) ----
+    if not args.no_batch:
+        res["batched"] = run_batched(args, D)
+
     # ---- CPU baseline (rank 0, N=1 only) ----
     if D.rank == 0 and D.world == 1 and not args.no_cpu:
         rate, cores, sample = cpu_reference(args.workload, steps=3, warmup=1, budget_s=40.0)
         res["cpu_baseline"] = dict(value=rate, unit=UNIT, cores=cores, kind="port", sample=sample)
     return res
+
+
+def ensemble_grids(nchan: int, seed: int, precision: int):
+    """The batched ensemble workload: grids drawn uniformly from Nx, Nz in {48,64,96,128}
+    and Ny in {33,49,65,97} points, Re_bulk uniform in [3000, 12000] (RE = 3/4 Re_bulk),
+    domain 4pi x 2 x 4/3 pi, tanh stretching beta = 2, dt = 0.002."""
+    from compact3d_gb300.grid import Grid
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nchan):
+        nx = int(rng.choice([48, 64, 96, 128]))
+        nz = int(rng.choice([48, 64, 96, 128]))
+        ny = int(rng.choice([33, 49, 65, 97]))
+        reb = float(rng.uniform(3000.0, 12000.0))
+        g = Grid(n1m=nx, n2m=ny - 1, n3m=nz, alx=4 * math.pi, aly=2.0, alz=4 * math.pi / 3, re=0.75 * reb,
+                 cks=2.0, precision=precision)
+        out.append(g)
+    return out, 0.002
+
+
+def run_batched(args, D: Dist):
+    """Aggregate grid-point-substeps/s of the ensemble as one CUDA graph (mixed form), and
+    of the same channels stepped one after another in the plain FP64 form."""
+    from compact3d_gb300 import lib
+    grids, dt = ensemble_grids(args.nchan, ic.SEED0 + 1000 + D.rank, C3D_MIXED)
+    ics = [ic.perturbed_laminar(g, seed=ic.SEED0 + 2000 + i) for i, g in enumerate(grids)]
+    pts = sum(g.points for g in grids)
+    b = lib.Batch(grids)
+    for ch, (U, P, HH) in zip(b.channels, ics):
+        ch.upload(U, P, HH)
+        ch.project()
+    n = len(grids)
+    dts = [dt] * n
+    p, p3 = [0.0] * n, [0.0] * n
+    step = 1
+    for _ in range(max(3, args.warmup)):
+        p, p3 = b.step(step, dts, p, p3)
+        step += 1
+    K = args.steps
+    D.barrier()
+    t0 = time.perf_counter()
+    dev_ms = 0.0
+    for _ in range(K):
+        p, p3 = b.step(step, dts, p, p3)
+        step += 1
+        dev_ms += b.last_step_stats()[0]
+    wall = D.max(time.perf_counter() - t0)
+    dev_ms = D.max(dev_ms)
+    launches = b.last_step_stats()[1]
+    b.close()
+    tot = D.sum(pts)
+    out = dict(value=tot * K / (dev_ms / 1e3), unit=UNIT, channels=n, points=pts, steps=K,
+               ms_per_step=dev_ms / K, wall_value=tot * K / wall, kernels_per_step=launches,
+               form="mixed, one CUDA graph per ensemble step",
+               workload="32 channels: Nx,Nz in {48,64,96,128}, Ny in {33,49,65,97}, "
+                        "Re_bulk in [3000,12000], seeded")
+    # the same channels, one after another, plain FP64
+    t_seq = 0.0
+    k_seq = max(2, min(K, args.fp64_steps))
+    for i, g in enumerate(grids):
+        g64, _ = g, dt
+        c = lib.Channel(g64, C3D_FP64)
+        U, P, HH = ics[i]
+        c.upload(U, P, HH)
+        c.project()
+        c.set_presg(0.0, 0.0)
+        for s_ in range(1, 3):
+            c.step_async(s_, dt)
+        c.sync()
+        c.timer_start()
+        for s_ in range(k_seq):
+            c.step_async(3 + s_, dt)
+        t_seq += c.timer_stop()
+        c.close()
+    t_seq = D.max(t_seq)
+    out["fp64_sequential"] = dict(value=tot * k_seq / (t_seq / 1e3), ms_per_step=t_seq / k_seq, steps=k_seq)
+    return out
 
 
 def run_reference(args, D: Dist):
@@ -374,6 +455,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--nchan", type=int, default=32)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -5,6 +5,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <string>
+#include <algorithm>
 #include <vector>
 #include "../../include/c3d.h"
 #include "c3d_internal.h"
@@ -733,9 +734,105 @@ int c3d_last_step_stats(c3d_channel *ch, double *ms, int *launches) {
 }
 
 // ---- batched ensemble ----------------------------------------------------------
+// Every channel keeps its own stream.  One ensemble step is one CUDA graph: a copy of the
+// PRESG/PRESG3 values of all channels from pinned host memory, a scatter kernel, then a
+// fork to every channel's stream (the channels' step kernels run concurrently), a join,
+// a gather kernel and the copy back.  Graphs are captured per AB2 buffer parity and
+// recaptured when a channel's DT changes.
+}  // extern "C"
+
+namespace {
+__global__ void k_batch_scatter(int n, const double *src, double *const *scal) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        scal[i][SCAL_PRESG] = src[2 * i];
+        scal[i][SCAL_PRESG3] = src[2 * i + 1];
+    }
+}
+__global__ void k_batch_gather(int n, double *dst, double *const *scal) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        dst[2 * i] = scal[i][SCAL_PRESG];
+        dst[2 * i + 1] = scal[i][SCAL_PRESG3];
+    }
+}
+}  // namespace
+
 struct c3d_batch {
     std::vector<c3d_channel *> ch;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+    std::vector<cudaEvent_t> join;
+    double *hpres = nullptr, *dpres = nullptr;
+    double **dscal = nullptr;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    std::vector<double> gdt[2];
+    int launches = 0;
+    float last_ms = 0.f;
 };
+
+static void batch_free(c3d_batch *b) {
+    for (auto *q : b->ch) c3d_destroy(q);
+    for (int p = 0; p < 2; ++p)
+        if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
+    for (auto e : b->join) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->t0) cudaEventDestroy(b->t0);
+    if (b->t1) cudaEventDestroy(b->t1);
+    if (b->hpres) cudaFreeHost(b->hpres);
+    if (b->dpres) cudaFree(b->dpres);
+    if (b->dscal) cudaFree(b->dscal);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+// Captures the ensemble step for the parity the channels move to; leaves ch->cur there.
+static int batch_capture(c3d_batch *b, const double *dt, int par) {
+    const int n = (int)b->ch.size();
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
+    int nl = 0;
+    cudaMemcpyAsync(b->dpres, b->hpres, 2 * n * sizeof(double), cudaMemcpyHostToDevice, b->stream);
+    k_batch_scatter<<<(n + 127) / 128, 128, 0, b->stream>>>(n, b->dpres, b->dscal);
+    cudaEventRecord(b->fork, b->stream);
+    int rc = 0;
+    for (int i = 0; i < n && !rc; ++i) {
+        c3d_channel *c = b->ch[i];
+        cudaStreamWaitEvent(c->stream, b->fork, 0);
+        int keep = c->prof_on;
+        c->prof_on = 0;
+        rc = launch_step(c, dt[i], &nl);
+        c->prof_on = keep;
+        cudaEventRecord(b->join[i], c->stream);
+        cudaStreamWaitEvent(b->stream, b->join[i], 0);
+    }
+    k_batch_gather<<<(n + 127) / 128, 128, 0, b->stream>>>(n, b->dpres, b->dscal);
+    cudaMemcpyAsync(b->hpres, b->dpres, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) {
+        set_error(std::string("batch capture: ") + cudaGetErrorString(e));
+        return C3D_ECUDA;
+    }
+    if (b->exec[par]) cudaGraphExecDestroy(b->exec[par]);
+    b->exec[par] = nullptr;
+    e = cudaGraphInstantiate(&b->exec[par], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        set_error(std::string("batch graph instantiate: ") + cudaGetErrorString(e));
+        return C3D_ECUDA;
+    }
+    b->gdt[par].assign(dt, dt + n);
+    b->launches = nl + 2;
+    for (auto *c : b->ch)
+        if (c->cur != par) { set_error("batch parity mismatch"); return C3D_ESTATE; }
+    return 0;
+}
+
+extern "C" {
 
 int c3d_batch_create(int nchan, const c3d_grid *grids, c3d_batch **out) {
     if (!out || !grids || nchan <= 0) { set_error("bad batch arguments"); return C3D_EINVAL; }
@@ -745,11 +842,29 @@ int c3d_batch_create(int nchan, const c3d_grid *grids, c3d_batch **out) {
         c3d_channel *c = nullptr;
         int rc = c3d_create(&grids[i], &c);
         if (rc) {
-            for (auto *q : b->ch) c3d_destroy(q);
-            delete b;
+            batch_free(b);
             return rc;
         }
         b->ch.push_back(c);
+    }
+    b->join.resize(nchan, nullptr);
+    bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreate(&b->t0) == cudaSuccess && cudaEventCreate(&b->t1) == cudaSuccess &&
+              cudaHostAlloc((void **)&b->hpres, 2 * nchan * sizeof(double), cudaHostAllocDefault) == cudaSuccess &&
+              cudaMalloc((void **)&b->dpres, 2 * nchan * sizeof(double)) == cudaSuccess &&
+              cudaMalloc((void **)&b->dscal, nchan * sizeof(double *)) == cudaSuccess;
+    for (int i = 0; ok && i < nchan; ++i)
+        ok = cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) == cudaSuccess;
+    if (ok) {
+        std::vector<double *> ps(nchan);
+        for (int i = 0; i < nchan; ++i) ps[i] = b->ch[i]->scal;
+        ok = cudaMemcpy(b->dscal, ps.data(), nchan * sizeof(double *), cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    if (!ok) {
+        set_error("batch: stream/event/memory set-up failed");
+        batch_free(b);
+        return C3D_ECUDA;
     }
     *out = b;
     return 0;
@@ -757,8 +872,8 @@ int c3d_batch_create(int nchan, const c3d_grid *grids, c3d_batch **out) {
 
 int c3d_batch_destroy(c3d_batch *b) {
     if (!b) return C3D_EINVAL;
-    for (auto *q : b->ch) c3d_destroy(q);
-    delete b;
+    cudaStreamSynchronize(b->stream);
+    batch_free(b);
     return 0;
 }
 
@@ -769,20 +884,60 @@ int c3d_batch_channel(c3d_batch *b, int index, c3d_channel **ch) {
 }
 
 int c3d_batch_step(c3d_batch *b, int ntime, const double *dt, double *presg, double *presg3) {
+    (void)ntime;
     if (!b || !dt || !presg || !presg3) { set_error("null argument"); return C3D_EINVAL; }
-    for (size_t i = 0; i < b->ch.size(); ++i) {
-        int rc = c3d_step(b->ch[i], ntime, dt[i], &presg[i], &presg3[i]);
+    const int n = (int)b->ch.size();
+    const int cur = b->ch[0]->cur;
+    for (int i = 0; i < n; ++i) {
+        c3d_channel *c = b->ch[i];
+        if (!c->have_state) { set_error("batch channel without uploaded state"); return C3D_ESTATE; }
+        if (c->cur != cur) { set_error("batch channels were stepped separately"); return C3D_ESTATE; }
+        if (!(dt[i] > 0) || !isfinite(dt[i])) { set_error("dt must be positive and finite"); return C3D_EINVAL; }
+        if (dt[i] != c->dt_cached) {
+            int rc = upload_ycn(c, dt[i]);
+            if (rc) return rc;
+        }
+        // the channels' own streams must be idle before the graph runs
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    const int par = 1 - cur;
+    for (int i = 0; i < n; ++i) {
+        b->hpres[2 * i] = presg[i];
+        b->hpres[2 * i + 1] = presg3[i];
+    }
+    if (!b->exec[par] || b->gdt[par].size() != (size_t)n ||
+        !std::equal(b->gdt[par].begin(), b->gdt[par].end(), dt)) {
+        int rc = batch_capture(b, dt, par);   // leaves every channel at parity par
         if (rc) return rc;
+    } else {
+        for (auto *c : b->ch) c->cur = par;
+    }
+    CK(cudaEventRecord(b->t0, b->stream));
+    CK(cudaGraphLaunch(b->exec[par], b->stream));
+    CK(cudaEventRecord(b->t1, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    cudaEventElapsedTime(&b->last_ms, b->t0, b->t1);
+    for (int i = 0; i < n; ++i) {
+        presg[i] = b->hpres[2 * i];
+        presg3[i] = b->hpres[2 * i + 1];
     }
     return 0;
 }
 
 int c3d_batch_sync(c3d_batch *b) {
     if (!b) return C3D_EINVAL;
+    CK(cudaStreamSynchronize(b->stream));
     for (auto *q : b->ch) {
         int rc = c3d_sync(q);
         if (rc) return rc;
     }
+    return 0;
+}
+
+int c3d_batch_last_step_stats(c3d_batch *b, double *ms, int *kernel_launches) {
+    if (!b) return C3D_EINVAL;
+    if (ms) *ms = b->last_ms;
+    if (kernel_launches) *kernel_launches = b->launches;
     return 0;
 }
 

@@ -67,6 +67,7 @@ SIGNATURES = {
     "c3d_batch_channel": (_ip, [_vp, _ip, ctypes.POINTER(_vp)]),
     "c3d_batch_step": (_ip, [_vp, _ip, _dp, _dp, _dp]),
     "c3d_batch_sync": (_ip, [_vp]),
+    "c3d_batch_last_step_stats": (_ip, [_vp, _dp, ctypes.POINTER(_ip)]),
 }
 
 _lib = None
@@ -121,9 +122,9 @@ class Channel:
         self.h = h
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not getattr(self, "_owned_by_batch", False):
             load().c3d_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -212,6 +213,54 @@ class Channel:
         return ms[0], n[0]
 
 
+class Batch:
+    """An ensemble of independent channels stepped together as one CUDA graph."""
+
+    def __init__(self, grids, precision: int | None = None):
+        self.grids = list(grids)
+        self._gs = (c3d_grid * len(self.grids))()
+        for i, g in enumerate(self.grids):
+            self._gs[i] = g.struct(g.precision if precision is None else precision)
+        h = _vp()
+        check(load().c3d_batch_create(len(self.grids), self._gs, ctypes.byref(h)), "c3d_batch_create")
+        self.h = h
+        self.channels = []
+        for i, g in enumerate(self.grids):
+            c = _vp()
+            check(load().c3d_batch_channel(self.h, i, ctypes.byref(c)), "c3d_batch_channel")
+            ch = Channel.__new__(Channel)
+            ch.grid, ch.precision, ch.h = g, g.precision if precision is None else precision, c
+            ch._owned_by_batch = True
+            self.channels.append(ch)
+
+    def close(self):
+        if getattr(self, "h", None):
+            for ch in self.channels:
+                ch.h = None
+            load().c3d_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, ntime: int, dt, presg, presg3):
+        n = len(self.grids)
+        dta = (ctypes.c_double * n)(*dt)
+        a = (ctypes.c_double * n)(*presg)
+        b = (ctypes.c_double * n)(*presg3)
+        check(load().c3d_batch_step(self.h, ntime, dta, a, b), "c3d_batch_step")
+        return list(a), list(b)
+
+    def last_step_stats(self):
+        ms = (ctypes.c_double * 1)()
+        n = (ctypes.c_int * 1)()
+        check(load().c3d_batch_last_step_stats(self.h, ms, n), "c3d_batch_last_step_stats")
+        return ms[0], n[0]
+
+
 def host_register(a: np.ndarray):
     check(load().c3d_host_register(a.ctypes.data, a.nbytes), "c3d_host_register")
 
@@ -220,5 +269,5 @@ def host_unregister(a: np.ndarray):
     check(load().c3d_host_unregister(a.ctypes.data), "c3d_host_unregister")
 
 
-__all__ = ["Channel", "load", "C3DError", "host_register", "host_unregister", "C3D_FP64",
+__all__ = ["Channel", "Batch", "load", "C3DError", "host_register", "host_unregister", "C3D_FP64",
            "C3D_MIXED", "SIGNATURES"]

@@ -180,8 +180,11 @@ int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
 
 /* ---- batched ensemble --------------------------------------------------
  * Many independent channels (any mix of grid sizes, RE and precision) that
- * advance together.  c3d_batch_step launches every channel's step work on one
- * stream; after the first call the whole step is replayed as one CUDA graph.
+ * advance together.  c3d_batch_step runs one GETUP on every channel as a single
+ * CUDA graph (captured on the first call and whenever a channel's DT changes):
+ * the channels' kernels run concurrently on their own streams.  presg/presg3
+ * are in-out arrays of nchan values; the call returns when the step is done.
+ * Upload each channel's state with c3d_batch_channel + c3d_upload first.
  */
 int c3d_batch_create(int nchan, const c3d_grid *grids, c3d_batch **out);
 int c3d_batch_destroy(c3d_batch *b);
@@ -189,6 +192,9 @@ int c3d_batch_channel(c3d_batch *b, int index, c3d_channel **ch);
 int c3d_batch_step(c3d_batch *b, int ntime, const double *dt,
                    double *presg, double *presg3);
 int c3d_batch_sync(c3d_batch *b);
+/* Device time of the last ensemble step (CUDA events around the graph launch) and the
+ * number of kernels one ensemble step runs. */
+int c3d_batch_last_step_stats(c3d_batch *b, double *ms, int *kernel_launches);
 
 #ifdef __cplusplus
 }
