@@ -280,32 +280,8 @@ def run_ours(args, D: Dist):
             m += 1
         ms64 = D.max(c64.timer_stop())
         res["fp64"] = dict(value=total_pts * k64 / (ms64 / 1e3), ms_per_step=ms64 / k64, steps=k64)
-        # error after the same number of steps from the same start
-        ref_steps = args.err_steps
-        cm = make_channel(lib, g, "mixed", U0, P0, HH0)
-        cf = make_channel(lib, g, "fp64", U0, P0, HH0)
-        for s in range(1, ref_steps + 1):
-            cm.step_async(s, dt)
-            cf.step_async(s, dt)
-        Um, Pm, _ = cm.download()
-        Uf, Pf, _ = cf.download()
-        n1, n2, n3 = g.n1m, g.n2m, g.n3m
-
-        def rl(a, b):
-            return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
-        err = dict(u=rl(Um[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 0], Uf[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 0]),
-                   v=rl(Um[1:n1 + 1, 2:n2 + 1, 1:n3 + 1, 1], Uf[1:n1 + 1, 2:n2 + 1, 1:n3 + 1, 1]),
-                   w=rl(Um[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 2], Uf[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 2]),
-                   p=rl(Pm[:n1, :n2, :n3], Pf[:n1, :n2, :n3]), steps=ref_steps)
-        dm, df = cm.diagnose(), cf.diagnose()
-        pm, pf = cm.get_presg(), cf.get_presg()
-        err.update(divmax_mixed=dm["divmax"], divmax_fp64=df["divmax"],
-                   bulk_mixed=dm["flow1"] / g.aly, bulk_fp64=df["flow1"] / g.aly,
-                   wsm_mixed=float(dm["wsm"][0]), wsm_fp64=float(df["wsm"][0]),
-                   presg_mixed=pm[0], presg_fp64=pf[0])
-        res["err_vs_fp64"] = err
-        for c in (c64, cm, cf):
-            c.close()
+        c64.close()
+        res["err_vs_fp64"] = error_study(lib, g, dt, U0, P0, HH0, args.err_steps, floor=not args.no_floor)
 
     # ---- end to end through the host-array drop-in (c3d_getup) ----
     if not args.no_e2e:
@@ -347,6 +323,68 @@ def run_ours(args, D: Dist):
         rate, cores, sample = cpu_reference(args.workload, steps=3, warmup=1, budget_s=40.0)
         res["cpu_baseline"] = dict(value=rate, unit=UNIT, cores=cores, kind="port", sample=sample)
     return res
+
+
+def flow_stats(U, g):
+    """Plane statistics of a velocity field (host array U(0:M1,0:M2,0:M3,3)): the mean
+    streamwise profile and the RMS profiles of u', v', w' and the shear stress <u'v'>, all
+    at the cell centres j = 1..N2M (v averaged from the two faces)."""
+    n1, n2, n3 = g.n1m, g.n2m, g.n3m
+    u = U[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 0]
+    v = 0.5 * (U[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 1] + U[1:n1 + 1, 2:n2 + 2, 1:n3 + 1, 1])
+    w = U[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 2]
+    um = u.mean(axis=(0, 2))
+    up, vp, wp = u - um[None, :, None], v - v.mean(axis=(0, 2))[None, :, None], w - w.mean(axis=(0, 2))[None, :, None]
+    return dict(mean_u=um, urms=np.sqrt((up ** 2).mean(axis=(0, 2))), vrms=np.sqrt((vp ** 2).mean(axis=(0, 2))),
+                wrms=np.sqrt((wp ** 2).mean(axis=(0, 2))), uv=(up * vp).mean(axis=(0, 2)))
+
+
+def error_study(lib, g, dt, U0, P0, HH0, steps: int, floor: bool = True):
+    """Error of the mixed form against the FP64 GPU form after `steps` steps from the same
+    start: relative L2 of u, v, w (interiors) and of P, max |div u|, bulk velocity
+    FLOW1/ALY, plane-mean wall shear WSM(1), PRESG, and the relative L2 of the mean profile
+    and of the RMS and shear-stress profiles.  With `floor`, the same figures for an FP64
+    run whose start was perturbed by 1e-15 max|U| (projected): the chaotic growth of a
+    round-off-sized difference, below which no form can be compared."""
+    n1, n2, n3 = g.n1m, g.n2m, g.n3m
+
+    def rl(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    runs = {"mixed": make_channel(lib, g, "mixed", U0, P0, HH0), "fp64": make_channel(lib, g, "fp64", U0, P0, HH0)}
+    if floor:
+        rng = np.random.default_rng(ic.SEED0 + 77)
+        Up = U0 + 1e-15 * float(np.abs(U0).max()) * rng.standard_normal(U0.shape)
+        runs["fp64_perturbed"] = make_channel(lib, g, "fp64", np.asfortranarray(Up), P0, HH0)
+    for s in range(1, steps + 1):
+        for c in runs.values():
+            c.step_async(s, dt)
+    fields = {k: c.download() for k, c in runs.items()}
+    diags = {k: c.diagnose() for k, c in runs.items()}
+    presg = {k: c.get_presg() for k, c in runs.items()}
+    for c in runs.values():
+        c.close()
+    Uf, Pf, _ = fields["fp64"]
+    sf = flow_stats(Uf, g)
+    out = dict(steps=steps, reference="FP64 GPU form (per step within 1e-10 of the FP64 oracle)")
+    for name in [k for k in runs if k != "fp64"]:
+        Um, Pm, _ = fields[name]
+        sm = flow_stats(Um, g)
+        d = diags[name]
+        out[name] = dict(
+            u=rl(Um[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 0], Uf[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 0]),
+            v=rl(Um[1:n1 + 1, 2:n2 + 1, 1:n3 + 1, 1], Uf[1:n1 + 1, 2:n2 + 1, 1:n3 + 1, 1]),
+            w=rl(Um[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 2], Uf[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 2]),
+            p=rl(Pm[:n1, :n2, :n3], Pf[:n1, :n2, :n3]),
+            divmax=d["divmax"], bulk=d["flow1"] / g.aly, wsm=float(d["wsm"][0]), presg=presg[name][0],
+            mean_u=rl(sm["mean_u"], sf["mean_u"]),
+            rms=rl(np.concatenate([sm[k] for k in ("urms", "vrms", "wrms", "uv")]),
+                   np.concatenate([sf[k] for k in ("urms", "vrms", "wrms", "uv")])))
+        out[name]["bulk_rel"] = abs(out[name]["bulk"] - diags["fp64"]["flow1"] / g.aly) / abs(diags["fp64"]["flow1"] / g.aly)
+        out[name]["wsm_rel"] = abs(out[name]["wsm"] - float(diags["fp64"]["wsm"][0])) / abs(float(diags["fp64"]["wsm"][0]))
+    out["fp64"] = dict(divmax=diags["fp64"]["divmax"], bulk=diags["fp64"]["flow1"] / g.aly,
+                       wsm=float(diags["fp64"]["wsm"][0]), presg=presg["fp64"][0])
+    return out
 
 
 def ensemble_grids(nchan: int, seed: int, precision: int):
@@ -456,6 +494,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-floor", action="store_true")
     ap.add_argument("--nchan", type=int, default=32)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

@@ -153,7 +153,7 @@ int dalloc(T **p, size_t n) {
 void free_channel(c3d_channel *ch) {
     if (!ch) return;
     void *ptrs[] = {ch->u, ch->v, ch->w, ch->p, ch->dp, ch->scal, ch->part, ch->metric, ch->ycn,
-                    ch->prb, ch->pgam, ch->pmj, ch->ycn32, ch->metr, ch->prbdf, ch->pgamdf, ch->pmjdf, ch->diagbuf,
+                    ch->prb, ch->pgam, ch->pmj, ch->ycn32, ch->metr, ch->prbdf, ch->pgamdf, ch->pmjdf, ch->bulkw, ch->diagbuf,
                     ch->tw64, ch->tw32, ch->hh[0][0], ch->hh[0][1],
                     ch->hh[0][2], ch->hh[1][0], ch->hh[1][1], ch->hh[1][2], ch->r[0], ch->r[1],
                     ch->r[2], ch->exy, ch->exz, ch->eyz, ch->ww1, ch->wsq, ch->rdpz, ch->g1,
@@ -347,6 +347,7 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
         dalloc(&ch->metric, 10 * (size_t)(g.n2 + 1)) || dalloc(&ch->ycn, 9 * (size_t)(g.n2 + 1)) ||
         dalloc(&ch->ycn32, 9 * (size_t)(g.n2 + 1)) ||
         dalloc(&ch->pmj, (size_t)(g.n2 + 1)) || dalloc(&ch->pmjdf, (size_t)(g.n2 + 1)) ||
+        dalloc(&ch->bulkw, (size_t)(g.n2 + 1)) ||
         dalloc(&ch->diagbuf, nf))
         return fail(C3D_ENOMEM);
     const size_t nmodes = (size_t)g.n1h * g.n3m;
@@ -427,6 +428,14 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
             pdf[j] = make_float2(h, (float)(ch->pmjh[j] - (double)h));
         }
         if (cudaMemcpy(ch->pmjdf, pdf.data(), (size_t)m * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(C3D_ECUDA);
+        // weights of the bulk-flow sums (UPCALC): DY(J)/DX3/DX1, FP64 on the host
+        for (int j = 0; j < m; ++j) {
+            const double wj = gr->dy[j] / gr->dx3 / gr->dx1;
+            const float h = (float)wj;
+            pdf[j] = make_float2(h, (float)(wj - (double)h));
+        }
+        if (cudaMemcpy(ch->bulkw, pdf.data(), (size_t)m * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)
             return fail(C3D_ECUDA);
     }
     rc = launch_poisson_tables(ch);

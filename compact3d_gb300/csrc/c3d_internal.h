@@ -59,6 +59,7 @@ struct StepArgs {
     const float2 *prbdf, *pgamdf;       // the same as double-float pairs (mixed form)
     const double *pmj;                  // PMJ(J), n2+1 values
     const float2 *pmjdf;                // the same as double-float pairs
+    const float2 *bulkw;                // DY(J)/DX3/DX1 as double-float pairs (mixed form)
     FftPlan fx, fz;                     // complex FFT of length N1M/2 (x) and N3M (z)
     const double2 *twx64;               // exp(-2 pi i k / N1M), k in [0, N1M/2]
     const float2 *twx32;
@@ -96,7 +97,7 @@ struct c3d_channel {
     double *ycn;              // 3 x 3 x (n2+1)
     float *ycn32;             // the same in FP32 (mixed form)
     double *prb, *pgam, *pmj;
-    float2 *prbdf, *pgamdf, *pmjdf;
+    float2 *prbdf, *pgamdf, *pmjdf, *bulkw;
     double *diagbuf;          // FP64 scratch field of the diagnostics
     double2 *tw64;            // x-FFT table, z-FFT table, x post-processing table
     float2 *tw32;

@@ -89,6 +89,14 @@ __device__ __forceinline__ float2 df_fsub(float q, float2 t) {
     e -= t.y;
     return df_norm(s, e);
 }
+// a + b (two-sum of the high parts, low parts added to the error term)
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    float s = a.x + b.x;
+    float v = s - a.x;
+    float e = (a.x - (s - v)) + (b.x - v);
+    e += a.y + b.y;
+    return df_norm(s, e);
+}
 
 // Warp shuffles for every state/working type
 __device__ __forceinline__ double shfl_any(double v, int src) { return __shfl_sync(FULL, v, src); }

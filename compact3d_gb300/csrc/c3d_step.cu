@@ -94,6 +94,18 @@ __global__ void __launch_bounds__(TPB) k_ycn(StepArgs<R> a, const R *ycn) {
 }
 
 // DMPRESG / DMPRESG3 in FP64 with a fixed summation order; PRESG += DMPRESG (UPCALC)
+// UPCALC's forcing (compact3d.f:1052-1238) from the summed CN increments of u and w.
+__device__ __forceinline__ void finish_bulk(Geo g, double t1, double t3, double *scal, double dt, int bulk) {
+    double dm = bulk ? t1 / g.vol / dt : 0.0;
+    double dm3 = bulk ? t3 / g.vol / dt : 0.0;
+    scal[SCAL_DMPRESG] = dm;
+    scal[SCAL_DMPRESG3] = dm3;
+    if (bulk) {
+        scal[SCAL_PRESG] = scal[SCAL_PRESG] + dm;
+        scal[SCAL_PRESG3] = scal[SCAL_PRESG3] + dm3;
+    }
+}
+
 __global__ void k_reduce(Geo g, const double *part, double *scal, double dt, int bulk) {
     const int nrows = g.n2m * g.n3m;
     __shared__ double sh1[1024], sh3[1024];
@@ -112,16 +124,32 @@ __global__ void k_reduce(Geo g, const double *part, double *scal, double dt, int
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        double dm = bulk ? sh1[0] / g.vol / dt : 0.0;
-        double dm3 = bulk ? sh3[0] / g.vol / dt : 0.0;
-        scal[SCAL_DMPRESG] = dm;
-        scal[SCAL_DMPRESG3] = dm3;
-        if (bulk) {
-            scal[SCAL_PRESG] = scal[SCAL_PRESG] + dm;
-            scal[SCAL_PRESG3] = scal[SCAL_PRESG3] + dm3;
-        }
+    if (threadIdx.x == 0) finish_bulk(g, sh1[0], sh3[0], scal, dt, bulk);
+}
+
+// The same reduction for the mixed form, whose per-row partial sums are double-float
+// pairs: a fixed-order double-float tree in FP32 instructions (one SM would otherwise
+// spend tens of microseconds in FP64 adds), then the FP64 bulk-flow arithmetic.
+__global__ void k_reduce_df(Geo g, const float2 *part, double *scal, double dt, int bulk) {
+    const int nrows = g.n2m * g.n3m;
+    __shared__ float2 sh1[1024], sh3[1024];
+    float2 s1 = make_float2(0.f, 0.f), s3 = s1;
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+        s1 = df_add(s1, part[r]);
+        s3 = df_add(s3, part[nrows + r]);
     }
+    sh1[threadIdx.x] = s1;
+    sh3[threadIdx.x] = s3;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            sh1[threadIdx.x] = df_add(sh1[threadIdx.x], sh1[threadIdx.x + w]);
+            sh3[threadIdx.x] = df_add(sh3[threadIdx.x], sh3[threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        finish_bulk(g, (double)sh1[0].x + (double)sh1[0].y, (double)sh3[0].x + (double)sh3[0].y, scal, dt, bulk);
 }
 
 // CHKMF (compact3d.f:9463-9503) and WALLSS (11077-11143): one block, FP64, fixed order.
@@ -253,7 +281,7 @@ static StepArgs<R> make_args(c3d_channel *ch, double dt) {
     a.ww1 = (R *)ch->ww1; a.wsq = (R *)ch->wsq; a.rdpz = (R *)ch->rdpz; a.g1 = (R *)ch->g1;
     a.dp = (R *)ch->dp; a.spec = ch->spec; a.scal = ch->scal; a.part = ch->part;
     a.ycn = ch->ycn; a.prb = ch->prb; a.pgam = ch->pgam; a.prbdf = ch->prbdf; a.pgamdf = ch->pgamdf;
-    a.pmj = ch->pmj; a.pmjdf = ch->pmjdf;
+    a.pmj = ch->pmj; a.pmjdf = ch->pmjdf; a.bulkw = ch->bulkw;
     a.fx = ch->fx; a.fz = ch->fz;
     a.twx64 = ch->tw64 + (ch->g.n1m / 2) + ch->g.n3m;
     a.twx32 = ch->tw32 + (ch->g.n1m / 2) + ch->g.n3m;
@@ -298,7 +326,8 @@ static int pressure_and_update(c3d_channel *ch, StepArgs<R> &a, R *d0, R *d1, R 
     if ((rc = launch_spec<R>(ch, a, 1, nl))) return rc;                       // poisson
     if ((rc = launch_spec<R>(ch, a, 2, nl))) return rc;                       // fftz inv
     if ((rc = launch_xpass<R>(ch, a, 3, d0, d2, nl))) return rc;              // xD
-    k_reduce<<<1, 1024, 0, ch->stream>>>(ch->g, ch->part, ch->scal, a.dt, a.bulk);
+    if constexpr (sizeof(R) == 8) k_reduce<<<1, 1024, 0, ch->stream>>>(ch->g, ch->part, ch->scal, a.dt, a.bulk);
+    else k_reduce_df<<<1, 1024, 0, ch->stream>>>(ch->g, (const float2 *)ch->part, ch->scal, a.dt, a.bulk);
     mark(ch, nl, "reduce", 16.0 * ch->g.n2m * ch->g.n3m);
     return launch_zpass<R>(ch, a, 4, d0, d1, d2, updp, nl);                   // zE
 }

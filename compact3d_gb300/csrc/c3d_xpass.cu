@@ -422,26 +422,51 @@ __global__ void __launch_bounds__(TPB) k_xD(StepArgs<R> a, const R *d0, const R 
         }
         xsolve(d, lane, P, a.c22x);
         srow_store(a.g1 + o, d, sbR, lane, P);
-        // bulk-flow partial sums: sum_i delta * DY(J)/DX3/DX1 for u and w (FP64 across lanes)
+        // bulk-flow partial sums: sum_i delta * DY(J)/DX3/DX1 for u and w
         R q1[C], q3[C];
         srow_load(q1, d0 + o, sbR, lane, P);
         srow_load(q3, d2 + o, sbR, lane, P);
-        R l1 = R(0), l3 = R(0);
+        if constexpr (sizeof(R) == 8) {
+            R l1 = R(0), l3 = R(0);
 #pragma unroll
-        for (int t = 0; t < C; ++t) {
-            l1 += q1[t];
-            l3 += q3[t];
-        }
-        double s1 = (double)l1, s3 = (double)l3;
+            for (int t = 0; t < C; ++t) {
+                l1 += q1[t];
+                l3 += q3[t];
+            }
+            double s1 = (double)l1, s3 = (double)l3;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            s1 += __shfl_down_sync(FULL, s1, off);
-            s3 += __shfl_down_sync(FULL, s3, off);
-        }
-        if (lane == 0) {
-            const double wgt = g.dy[j] / g.dx3 / g.dx1;
-            a.part[row] = s1 * wgt;
-            a.part[nrows + row] = s3 * wgt;
+            for (int off = 16; off > 0; off >>= 1) {
+                s1 += __shfl_down_sync(FULL, s1, off);
+                s3 += __shfl_down_sync(FULL, s3, off);
+            }
+            if (lane == 0) {
+                const double wgt = g.dy[j] / g.dx3 / g.dx1;
+                a.part[row] = s1 * wgt;
+                a.part[nrows + row] = s3 * wgt;
+            }
+        } else {
+            // Mixed form: double-float sums (exact two-sums of the FP32 deltas, FP32
+            // instructions only) and a double-float weight; the slots of `part` hold
+            // float2 pairs that k_reduce combines in the same arithmetic.
+            float2 s1 = make_float2(0.f, 0.f), s3 = s1;
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                s1 = St<float>::add(s1, q1[t]);
+                s3 = St<float>::add(s3, q3[t]);
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                float2 o1 = make_float2(__shfl_down_sync(FULL, s1.x, off), __shfl_down_sync(FULL, s1.y, off));
+                float2 o3 = make_float2(__shfl_down_sync(FULL, s3.x, off), __shfl_down_sync(FULL, s3.y, off));
+                s1 = df_add(s1, o1);
+                s3 = df_add(s3, o3);
+            }
+            if (lane == 0) {
+                const float2 wgt = a.bulkw[j];
+                float2 *pp = reinterpret_cast<float2 *>(a.part);
+                pp[row] = df_mul(s1, wgt);
+                pp[nrows + row] = df_mul(s3, wgt);
+            }
         }
     }
 }
