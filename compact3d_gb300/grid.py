@@ -218,6 +218,11 @@ WORKLOADS = {
     # wall-modelled LES: 128 x 65 x 128 points, 8pi x 2 x 3pi, uniform y (wall model)
     "les128": dict(n1m=128, n2m=64, n3m=128, alx=8 * PI, aly=2.0, alz=3 * PI, cks=1.0,
                    re=round(re_from_retau(2000.0), 1), dt=0.001, wmodel=1, files=2),
+    # small wall-modelled LES grids for parity tests (Smagorinsky and dynamic)
+    "les32cs": dict(n1m=32, n2m=16, n3m=32, alx=8 * PI, aly=2.0, alz=3 * PI, cks=1.0,
+                    re=round(re_from_retau(2000.0), 1), dt=0.002, wmodel=1, files=2),
+    "les32dy": dict(n1m=32, n2m=16, n3m=32, alx=8 * PI, aly=2.0, alz=3 * PI, cks=1.0,
+                    re=round(re_from_retau(2000.0), 1), dt=0.002, wmodel=1, files=1),
     # small grids for parity tests
     "tiny16": dict(n1m=16, n2m=16, n3m=16, alx=2 * PI, aly=2.0, alz=PI, cks=2.0,
                    re=1000.0, dt=0.002),

@@ -8,6 +8,10 @@ initial fields cannot be reproduced.  This module builds seeded fields instead:
   zero slope at both walls, so the perturbation is divergence-free in the continuous
   sense and zero at the walls.  It is then made discretely divergence-free by one
   pressure projection (``c3d_project`` in the library, ``orc_project`` in the oracle).
+* ``loglaw``: the wall-modelled LES start: a log-law mean profile (Reichardt's composite
+  law of the wall, u+ = ln(1 + 0.41 y+)/0.41 + 7.8 (1 - exp(-y+/11) - y+/11 exp(-y+/3)),
+  with y+ from the nearest wall) plus ``amp`` times its centreline value in the same
+  divergence-free perturbation as ``perturbed_laminar``.
 * ``band_limited``: seeded N(0,1) fields band-limited to |k| <= N/3 in x and z with a
   smooth random wall-normal profile (the operator workload).
 
@@ -47,8 +51,10 @@ def _eval(S, n1m, n3m, sx, sz, dx_order=0, dz_order=0):
     return np.fft.irfft2(T, s=(n3m, n1m)) * (n1m * n3m)
 
 
-def perturbed_laminar(g: Grid, amp: float = 0.1, seed: int = SEED0, kmax: int = 4):
-    """U, P, HH (Fortran order) of the perturbed laminar start (before projection)."""
+def perturbed_laminar(g: Grid, amp: float = 0.1, seed: int = SEED0, kmax: int = 4, mean=None):
+    """U, P, HH (Fortran order) of the perturbed laminar start (before projection).
+    ``mean`` (a function of the cell-centre y array) replaces the laminar profile; the
+    perturbation is then scaled to ``amp`` times the profile's maximum."""
     rng = np.random.default_rng(seed)
     n1m, n2m, n3m = g.n1m, g.n2m, g.n3m
     a = g.arrays
@@ -82,10 +88,14 @@ def perturbed_laminar(g: Grid, amp: float = 0.1, seed: int = SEED0, kmax: int = 
     dxF2w = _eval(F[1], n1m, n3m, 0.5, 0.0, dx_order=1) * kx2
     F1w = _eval(F[0], n1m, n3m, 0.5, 0.0)
     pw = env(yc)[:, None, None] * dxF2w[None] - denv(yc)[:, None, None] * F1w[None]
-    scale = amp / max(np.abs(pu).max(), np.abs(pv).max(), np.abs(pw).max(), 1e-300)
-
     U = g.zeros_u()
-    realu = yc * (aly - yc) * (aly - 1.0) + yc * (2 * aly - yc) * (2.0 - aly)
+    if mean is None:
+        realu = yc * (aly - yc) * (aly - 1.0) + yc * (2 * aly - yc) * (2.0 - aly)
+        ref = 1.0
+    else:
+        realu = mean(yc)
+        ref = float(np.abs(realu).max())
+    scale = amp * ref / max(np.abs(pu).max(), np.abs(pv).max(), np.abs(pw).max(), 1e-300)
     # arrays pu[j,k,i] -> U[i,j,k]
     U[1:n1m + 1, 1:n2m + 1, 1:n3m + 1, 0] = (realu[:, None, None] + scale * pu).transpose(2, 0, 1)
     U[1:n1m + 1, 1:n2m + 2, 1:n3m + 1, 1] = (scale * pv).transpose(2, 0, 1)
@@ -95,6 +105,22 @@ def perturbed_laminar(g: Grid, amp: float = 0.1, seed: int = SEED0, kmax: int = 
     P = g.zeros_p()
     HH = g.zeros_u()
     return U, P, HH
+
+
+def loglaw(g: Grid, retau: float, amp: float = 0.05, seed: int = SEED0, kmax: int = 4):
+    """U, P, HH of the LES start: Reichardt's law of the wall at friction Reynolds number
+    ``retau`` (u_tau = retau / RE in the reference's units) plus a divergence-free
+    perturbation of ``amp`` times the centreline velocity."""
+    utau = retau / g.re
+    aly = g.arrays["aly"]
+
+    def prof(y):
+        yw = np.minimum(y, aly - y) if aly == 2.0 else y
+        yp = yw * retau
+        up = np.log1p(0.41 * yp) / 0.41 + 7.8 * (1.0 - np.exp(-yp / 11.0) - yp / 11.0 * np.exp(-yp / 3.0))
+        return utau * up
+
+    return perturbed_laminar(g, amp=amp, seed=seed, kmax=kmax, mean=prof)
 
 
 def band_limited(g: Grid, seed: int = SEED0, frac: float = 1.0 / 3.0):

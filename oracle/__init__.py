@@ -56,6 +56,15 @@ def lib():
         L.orc_chkmf.argtypes = [vp, dp, dp, dp]
         L.orc_wallss.argtypes = [vp, dp, dp]
         L.orc_set_wall.argtypes = [vp, dp, dp, ip]
+        L.orc_get_wall.argtypes = [vp, dp, dp, dp]
+        L.orc_set_wsm.argtypes = [vp, dp]
+        L.orc_set_wall_iter_cap.argtypes = [vp, ip]
+        L.orc_sgs.restype = ip
+        L.orc_sgs.argtypes = [vp, dp, dp, dp]
+        L.orc_wallmodel.restype = ip
+        L.orc_sgs_rhs.restype = ip
+        L.orc_sgs_rhs.argtypes = [vp, dp, dp, dp]
+        L.orc_wallmodel.argtypes = [vp, dp]
         for f in ("orc_ctdma11", "orc_ctdma_recip"):
             getattr(L, f).argtypes = [ip, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp, dp]
         L.orc_tdmap.argtypes = [ip, dp, dp, dp, dp, dp]
@@ -135,6 +144,45 @@ class Oracle:
         f1, f3 = self.chkmf(U)
         return dict(divmax=self.divcheck(U), cflm=self.cfl(U), flow1=f1, flow3=f3,
                     wsm=self.wallss(U))
+
+    # ---- LES: SGS models and the wall model (FILES != 0) ----
+    def sgs(self, U):
+        """SGSDY / SGSCS on U: returns (SGSVIS(0:M1,0:M2,0:M3), SMAGC(1:N2M))."""
+        g = self.grid
+        S = g.zeros_s()
+        sm = np.zeros(g.n2m)
+        rc = lib().orc_sgs(self.h, _p(U), _p(S), _p(sm))
+        if rc != 0:
+            raise RuntimeError(f"orc_sgs failed: {rc}")
+        return S, sm
+
+    def sgs_rhs(self, U, sgsvis):
+        """The SGS-flux terms RHS1/2/3 subtract from HH, for a given SGSVIS."""
+        HH = self.grid.zeros_u()
+        lib().orc_sgs_rhs(self.h, _p(U), _p(sgsvis), _p(HH))
+        return HH
+
+    def wallmodel(self, U):
+        """WALLMODEL_INSTANT on U; returns the status (0, or -4 if a point hit the cap)."""
+        return lib().orc_wallmodel(self.h, _p(U))
+
+    def set_wall(self, tauw=None, taub=None, ifwall=0):
+        lib().orc_set_wall(self.h, _p(tauw), _p(taub), ifwall)
+
+    def get_wall(self):
+        g = self.grid
+        tw = np.zeros(g.shape_tau(), order="F")
+        tb = np.zeros(g.shape_tau(), order="F")
+        w = np.zeros(3)
+        lib().orc_get_wall(self.h, _p(tw), _p(tb), _p(w))
+        return tw, tb, w
+
+    def set_wsm(self, wsm):
+        w = np.ascontiguousarray(wsm, dtype=np.float64)
+        lib().orc_set_wsm(self.h, _p(w))
+
+    def set_wall_iter_cap(self, cap: int):
+        lib().orc_set_wall_iter_cap(self.h, int(cap))
 
     def poisson_metrics(self):
         g = self.grid

@@ -51,6 +51,11 @@ struct Orc {
     std::vector<double> AK1, AK3, PMJ, PCJ, PPJ;
     std::vector<double> UBC;          // UBC(0:M1,0:M3,3,2)
     std::vector<double> TAUW, TAUB;   // (0:M1,0:M3,2)
+    double WSM[3] = {0.0, 0.0, 0.0};  // /WSMEM/ WSM(1:3) as the SGS model and wall model see it
+    double TAOW = 0.0;                // /WALLTAO/ TAOW
+    std::vector<double> SMAGC;        // /SGSMEAN/ SMAGC(1:N2M)
+    std::vector<double> SGS;          // SGSVIS when the caller passes none
+    int wall_iter_cap = 10000;        // Newton iterations allowed per wall point
     // work arrays of GETUP / UHCALC / DPCALC
     std::vector<double> UH, HH2, RUH1, RUH2, RUH3, DP, RDP;
     std::vector<double> FRDP, FDP;    // (M1,M2,M3MD)
@@ -355,8 +360,13 @@ void bcond(Orc &g, double *U, double *SGSVIS) {
 // RHS1 (compact3d.f:6063-6782), DNS terms.  The SGS-flux terms (6436-6763) add exact
 // zeros when SGSVIS == 0, which is the case for FILES == 0 (GETUP zeroes SGSVIS).
 // ----------------------------------------------------------------------------------
+void sgs_rhs1(Orc &g, const double *U, double *HH, const double *SGSVIS);
+void sgs_rhs2_vis22(Orc &g, const double *U, double *HH, const double *SGSVIS);
+void sgs_rhs2(Orc &g, const double *U, double *HH, const double *SGSVIS);
+void sgs_rhs3(Orc &g, const double *U, double *HH, const double *SGSVIS);
+
 void rhs1(Orc &g, const double *U, const double *P, double *HH, const double *HH2,
-          double *RUH1, double PRESG) {
+          double *RUH1, double PRESG, const double *SGSVIS) {
     const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
     const double RE = g.RE, DX1 = g.DX1, DX3 = g.DX3, DX1Q = g.DX1Q, DX3Q = g.DX3Q;
     const double *DY = g.DY.data(), *H = g.H.data(), *HP = g.HP.data(), *HC = g.HC.data(),
@@ -504,6 +514,8 @@ void rhs1(Orc &g, const double *U, const double *P, double *HH, const double *HH
             }
         }
     }
+    // 61-73: SGS-flux terms (only when an SGS model is active; otherwise they add zeros)
+    if (SGSVIS) sgs_rhs1(g, U, HH, SGSVIS);
     // 71/73: AB2 and wall-stress boundary term
 #pragma omp parallel for
     for (int K = 1; K <= N3M; K++)
@@ -520,7 +532,8 @@ void rhs1(Orc &g, const double *U, const double *P, double *HH, const double *HH
 }
 
 // RHS2 (compact3d.f:6784-7396), DNS terms.
-void rhs2(Orc &g, const double *U, const double *P, double *HH, const double *HH2, double *RUH2) {
+void rhs2(Orc &g, const double *U, const double *P, double *HH, const double *HH2, double *RUH2,
+          const double *SGSVIS) {
     const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
     const double RE = g.RE, DX1 = g.DX1, DX3 = g.DX3, DX1Q = g.DX1Q, DX3Q = g.DX3Q;
     const double *DY = g.DY.data(), *H = g.H.data(), *DYP = g.DYP.data(), *DYC = g.DYC.data(),
@@ -548,6 +561,8 @@ void rhs2(Orc &g, const double *U, const double *P, double *HH, const double *HH
                 HH[id] = HH[id] + 1. / H[J] * (V2 * V2 - V1 * V1);
             }
         }
+    // 10 (continued): D(SGS*DV/DY)/DY, after the convection term of the same point
+    if (SGSVIS) sgs_rhs2_vis22(g, U, HH, SGSVIS);
     // 20
 #pragma omp parallel for
     for (int K = 1; K <= N3M; K++) {
@@ -634,7 +649,8 @@ void rhs2(Orc &g, const double *U, const double *P, double *HH, const double *HH
             }
         }
     }
-    // 61-65: AB2
+    // SGS-flux terms, then 61-65: AB2
+    if (SGSVIS) sgs_rhs2(g, U, HH, SGSVIS);
 #pragma omp parallel for
     for (int K = 1; K <= N3M; K++)
         for (int J = 2; J <= N2M; J++)
@@ -646,7 +662,7 @@ void rhs2(Orc &g, const double *U, const double *P, double *HH, const double *HH
 
 // RHS3 (compact3d.f:7399-8114), DNS terms.
 void rhs3(Orc &g, const double *U, const double *P, double *HH, const double *HH2, double *RUH3,
-          double PRESG3) {
+          double PRESG3, const double *SGSVIS) {
     const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
     const double RE = g.RE, DX1 = g.DX1, DX3 = g.DX3, DX1Q = g.DX1Q, DX3Q = g.DX3Q;
     const double *DY = g.DY.data(), *H = g.H.data(), *HP = g.HP.data(), *HC = g.HC.data(),
@@ -783,6 +799,8 @@ void rhs3(Orc &g, const double *U, const double *P, double *HH, const double *HH
             }
         }
     }
+    // SGS-flux terms
+    if (SGSVIS) sgs_rhs3(g, U, HH, SGSVIS);
     // 71-73: AB2 and wall-stress boundary term
 #pragma omp parallel for
     for (int K = 1; K <= N3M; K++)
@@ -796,6 +814,786 @@ void rhs3(Orc &g, const double *U, const double *P, double *HH, const double *HH
                 RUH3[id] = RUH3[id] - 3. / 2. * HH[g.iuc(I, J, K, 3)] + 1. / 2. * HH2[g.iuc(I, J, K, 3)] + BC;
             }
         }
+}
+
+// ----------------------------------------------------------------------------------
+// SGS-flux terms of RHS1/2/3 (compact3d.f:6436-6770, 6857-6866 and 7088-7393,
+// 7774-8111).  SGSVIS(0:M1,0:M2,0:M3) holds the eddy viscosity at cell centres; its
+// wall planes J=0 and J=N2 are zero (GETUP zeroes them and no routine on the path
+// assigns them).  Work arrays the reference indexes one past their declared extent
+// (SGSVIS1(I,N2), UU12(I,N2), SGSVISW2(N2,K), VV32(N2,K) at J=N2M, and index 0 at J=1)
+// enter only multiplied by FJPA/FJMU = 0 or by a zero wall viscosity; they are zero here.
+// ----------------------------------------------------------------------------------
+void sgs_rhs1(Orc &g, const double *U, double *HH, const double *SGSVIS) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
+    const double DX1 = g.DX1, DX3 = g.DX3, ALY = g.ALY, IFWALL = g.IFWALL;
+    const double *DY = g.DY.data(), *H = g.H.data();
+    auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+    auto sv = [&](int i, int j, int k) { return SGSVIS[g.iu(i, j, k)]; };
+    ConstLine L6x, L6z, L22x, L22z;
+    L6x.set(N1M, 1.0, 6.0, 1.0);
+    L6z.set(N3M, 1.0, 6.0, 1.0);
+    L22x.set(N1M, 1.0, 22.0, 1.0);
+    L22z.set(N3M, 1.0, 22.0, 1.0);
+    // 61: D(SGS*(DU/DX))/DX
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++) {
+        std::vector<double> D11(N1M + 1), X11(N1M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int I = 1; I <= N1M - 1; I++) D11[I] = 24. * DX1 * (u(I + 1, J, K, 1) - u(I, J, K, 1));
+            D11[N1M] = 24. * DX1 * (u(1, J, K, 1) - u(N1M, J, K, 1));
+            ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+            for (int I = 2; I <= N1M; I++) D11[I] = 24. * DX1 * (sv(I, J, K) * X11[I] - sv(I - 1, J, K) * X11[I - 1]);
+            D11[1] = 24. * DX1 * (sv(1, J, K) * X11[1] - sv(N1M, J, K) * X11[N1M]);
+            ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+            for (int I = 1; I <= N1M; I++) HH[g.iuc(I, J, K, 1)] = HH[g.iuc(I, J, K, 1)] - 2. * X11[I];
+        }
+    }
+    // 65-67: D(SGS*(DU/DZ))/DZ
+    {
+        std::vector<double> S2((size_t)(N1M + 1) * (N3M + 1));
+        auto s2 = [&](int i, int k) -> double & { return S2[i + (size_t)(N1M + 1) * k]; };
+        for (int J = 1; J <= N2M; J++) {
+#pragma omp parallel for
+            for (int K = 1; K <= N3M; K++) {
+                std::vector<double> D1(N1M + 1), X1(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D1[I] = 4. * (sv(I, J, K) + sv(I - 1, J, K));
+                D1[1] = 4. * (sv(1, J, K) + sv(N1M, J, K));
+                ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+                for (int I = 1; I <= N1M; I++) s2(I, K) = X1[I];
+            }
+#pragma omp parallel for
+            for (int I = 1; I <= N1M; I++) {
+                std::vector<double> D3(N3M + 1), X3(N3M + 1), D33(N3M + 1), X33(N3M + 1);
+                for (int K = 2; K <= N3M; K++) D3[K] = 4. * (s2(I, K) + s2(I, K - 1));
+                D3[1] = 4. * (s2(I, 1) + s2(I, N3M));
+                ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+                for (int K = 2; K <= N3M; K++) D33[K] = 24. * DX3 * (u(I, J, K, 1) - u(I, J, K - 1, 1));
+                D33[1] = 24. * DX3 * (u(I, J, 1, 1) - u(I, J, N3M, 1));
+                ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+                for (int K = 1; K <= N3M - 1; K++) D33[K] = 24. * DX3 * (X33[K + 1] * X3[K + 1] - X33[K] * X3[K]);
+                D33[N3M] = 24. * DX3 * (X33[1] * X3[1] - X33[N3M] * X3[N3M]);
+                ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+                for (int K = 1; K <= N3M; K++) HH[g.iuc(I, J, K, 1)] = HH[g.iuc(I, J, K, 1)] - X33[K];
+            }
+        }
+    }
+    // 62-64: D(SGS*(DU/DY))/DY and 68-70: D(SGS*(DV/DX))/DY
+    {
+        std::vector<double> S1((size_t)(N1M + 1) * (N2 + 1), 0.0), S12((size_t)(N1M + 1) * (N2 + 1), 0.0),
+            UU12((size_t)(N1M + 1) * (N2 + 1), 0.0);
+        auto s1 = [&](int i, int j) -> double & { return S1[i + (size_t)(N1M + 1) * j]; };
+        auto s12 = [&](int i, int j) -> double & { return S12[i + (size_t)(N1M + 1) * j]; };
+        auto uu12 = [&](int i, int j) -> double & { return UU12[i + (size_t)(N1M + 1) * j]; };
+        for (int K = 1; K <= N3M; K++) {
+#pragma omp parallel for
+            for (int J = 1; J <= N2M; J++) {
+                std::vector<double> D1(N1M + 1), X1(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D1[I] = 4. * (sv(I, J, K) + sv(I - 1, J, K));
+                D1[1] = 4. * (sv(1, J, K) + sv(N1M, J, K));
+                ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+                for (int I = 1; I <= N1M; I++) s1(I, J) = X1[I];
+            }
+#pragma omp parallel for
+            for (int I = 1; I <= N1M; I++) {
+                const int IM = g.IMA[I];
+                for (int J = 1; J <= N2M; J++) {
+                    const int JP = J + 1, JM = J - 1;
+                    const double FJUM = g.FJMU[J], FJUP = g.FJPA[J];
+                    double SGSJ2 = FJUP * 1. / H[JP] * (DY[J] / 2. * s1(I, JP) + DY[JP] / 2. * s1(I, J)) +
+                                   (1. - FJUP) * 0.5 * (sv(I, N2, K) + sv(IM, N2, K));
+                    double SGSJ1 = FJUM * 1. / H[J] * (DY[JM] / 2. * s1(I, J) + DY[J] / 2. * s1(I, JM)) +
+                                   (1. - FJUM) * 0.5 * (sv(I, 0, K) + sv(IM, 0, K));
+                    double UU22 = (u(I, JP, K, 1) - u(I, J, K, 1)) / H[JP];
+                    double UU11 = (u(I, J, K, 1) - u(I, JM, K, 1)) / H[J];
+                    double SGSDUY = 1. / DY[J] * ((1. - IFWALL * (1. - FJUP) * (ALY - 1.)) * SGSJ2 * UU22 -
+                                                  (1. - IFWALL * (1. - FJUM)) * SGSJ1 * UU11);
+                    HH[g.iuc(I, J, K, 1)] = HH[g.iuc(I, J, K, 1)] - SGSDUY;
+                }
+            }
+        }
+        for (int K = 1; K <= N3M; K++) {
+#pragma omp parallel for
+            for (int J = 1; J <= N2M; J++) {
+                std::vector<double> D1(N1M + 1), X1(N1M + 1), D11(N1M + 1), X11(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D11[I] = 24. * DX1 * (u(I, J, K, 2) - u(I - 1, J, K, 2));
+                D11[1] = 24. * DX1 * (u(1, J, K, 2) - u(N1M, J, K, 2));
+                ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+                for (int I = 1; I <= N1M; I++) uu12(I, J) = X11[I];
+                for (int I = 2; I <= N1M; I++) D1[I] = 4. * (sv(I, J, K) + sv(I - 1, J, K));
+                D1[1] = 4. * (sv(1, J, K) + sv(N1M, J, K));
+                ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+                for (int I = 1; I <= N1M; I++) s12(I, J) = X1[I];
+            }
+#pragma omp parallel for
+            for (int I = 1; I <= N1M; I++) {
+                const int IM = g.IMA[I];
+                for (int J = 1; J <= N2M; J++) {
+                    const int JP = J + 1, JM = J - 1;
+                    const double FJUM = g.FJMU[J], FJUP = g.FJPA[J];
+                    double SGSJ2 = FJUP * 1.0 / H[JP] * (DY[J] / 2. * s12(I, JP) + DY[JP] / 2. * s12(I, J)) +
+                                   (1. - FJUP) * 0.5 * (sv(I, N2, K) + sv(IM, N2, K));
+                    double SGSJ1 = FJUM * 1.0 / H[J] * (DY[JM] / 2. * s12(I, J) + DY[J] / 2. * s12(I, JM)) +
+                                   (1. - FJUM) * 0.5 * (sv(I, 0, K) + sv(IM, 0, K));
+                    double SGSDUXY = 1.0 / DY[J] * ((1. - IFWALL * (1. - FJUP) * (ALY - 1.)) * SGSJ2 * uu12(I, JP) -
+                                                    (1. - IFWALL * (1. - FJUM)) * SGSJ1 * uu12(I, J));
+                    HH[g.iuc(I, J, K, 1)] = HH[g.iuc(I, J, K, 1)] - SGSDUXY;
+                }
+            }
+        }
+    }
+    // 71-73: D(SGS*(DW/DX))/DZ (the AB2 update and wall term follow in rhs1)
+    {
+        std::vector<double> S13((size_t)(N1M + 1) * (N3M + 1)), WW13((size_t)(N1M + 1) * (N3M + 1));
+        auto s13 = [&](int i, int k) -> double & { return S13[i + (size_t)(N1M + 1) * k]; };
+        auto ww13 = [&](int i, int k) -> double & { return WW13[i + (size_t)(N1M + 1) * k]; };
+        for (int J = 1; J <= N2M; J++) {
+#pragma omp parallel for
+            for (int K = 1; K <= N3M; K++) {
+                std::vector<double> D1(N1M + 1), X1(N1M + 1), D11(N1M + 1), X11(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D1[I] = 4. * (sv(I, J, K) + sv(I - 1, J, K));
+                D1[1] = 4. * (sv(1, J, K) + sv(N1M, J, K));
+                ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+                for (int I = 1; I <= N1M; I++) s13(I, K) = X1[I];
+                for (int I = 2; I <= N1M; I++) D11[I] = 24. * DX1 * (u(I, J, K, 3) - u(I - 1, J, K, 3));
+                D11[1] = 24. * DX1 * (u(1, J, K, 3) - u(N1M, J, K, 3));
+                ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+                for (int I = 1; I <= N1M; I++) ww13(I, K) = X11[I];
+            }
+#pragma omp parallel for
+            for (int I = 1; I <= N1M; I++) {
+                std::vector<double> D3(N3M + 1), X3(N3M + 1), D33(N3M + 1), X33(N3M + 1);
+                for (int K = 2; K <= N3M; K++) D3[K] = 4. * (s13(I, K) + s13(I, K - 1));
+                D3[1] = 4. * (s13(I, 1) + s13(I, N3M));
+                ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+                for (int K = 1; K <= N3M - 1; K++) D33[K] = 24. * DX3 * (ww13(I, K + 1) * X3[K + 1] - ww13(I, K) * X3[K]);
+                D33[N3M] = 24. * DX3 * (ww13(I, 1) * X3[1] - ww13(I, N3M) * X3[N3M]);
+                ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+                for (int K = 1; K <= N3M; K++) HH[g.iuc(I, J, K, 1)] = HH[g.iuc(I, J, K, 1)] - X33[K];
+            }
+        }
+    }
+}
+
+// RHS2 loop 10, second half (compact3d.f:6857-6866): D(SGS*DV/DY)/DY at the v faces.
+void sgs_rhs2_vis22(Orc &g, const double *U, double *HH, const double *SGSVIS) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double *DY = g.DY.data(), *H = g.H.data();
+    auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+#pragma omp parallel for
+    for (int K = 1; K <= N3M; K++)
+        for (int J = 2; J <= N2M; J++) {
+            const int JP = J + 1, JM = J - 1;
+            for (int I = 1; I <= N1M; I++) {
+                double SGSJ2 = SGSVIS[g.iu(I, J, K)];
+                double SGSJ1 = SGSVIS[g.iu(I, JM, K)];
+                double V2 = 1. / DY[J] * (u(I, JP, K, 2) - u(I, J, K, 2));
+                double V1 = 1. / DY[JM] * (u(I, J, K, 2) - u(I, JM, K, 2));
+                double VIS22 = 1.0 / H[J] * (SGSJ2 * V2 - SGSJ1 * V1);
+                HH[g.iuc(I, J, K, 2)] = HH[g.iuc(I, J, K, 2)] - 2. * VIS22;
+            }
+        }
+}
+
+// RHS2 (compact3d.f:7088-7393): the four cross-derivative SGS fluxes at the v faces.
+void sgs_rhs2(Orc &g, const double *U, double *HH, const double *SGSVIS) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double DX1 = g.DX1, DX3 = g.DX3;
+    const double *DY = g.DY.data(), *H = g.H.data();
+    auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+    auto sv = [&](int i, int j, int k) { return SGSVIS[g.iu(i, j, k)]; };
+    ConstLine L6x, L6z, L22x, L22z;
+    L6x.set(N1M, 1.0, 6.0, 1.0);
+    L6z.set(N3M, 1.0, 6.0, 1.0);
+    L22x.set(N1M, 1.0, 22.0, 1.0);
+    L22z.set(N3M, 1.0, 22.0, 1.0);
+    const size_t PX = (size_t)(N1M + 2), PJ = (size_t)(N2M + 2);
+    // D(SGS*(DU/DY))/DX
+    {
+        std::vector<double> SV1(PX * PJ), SV21(PX * PJ), VV21(PX * PJ);
+        auto sv1 = [&](int i, int j) -> double & { return SV1[i + PX * j]; };
+        auto sv21 = [&](int i, int j) -> double & { return SV21[i + PX * j]; };
+        auto vv21 = [&](int i, int j) -> double & { return VV21[i + PX * j]; };
+        for (int K = 1; K <= N3M; K++) {
+#pragma omp parallel for
+            for (int J = 1; J <= N2M; J++) {
+                std::vector<double> D1(N1M + 1), X1(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D1[I] = 4. * (sv(I, J, K) + sv(I - 1, J, K));
+                D1[1] = 4. * (sv(1, J, K) + sv(N1M, J, K));
+                ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+                for (int I = 1; I <= N1M; I++) sv1(I, J) = X1[I];
+            }
+#pragma omp parallel for
+            for (int I = 1; I <= N1M; I++)
+                for (int J = 2; J <= N2M; J++) {
+                    sv21(I, J) = 1. / H[J] * (DY[J - 1] / 2. * sv1(I, J) + DY[J] / 2. * sv1(I, J - 1));
+                    vv21(I, J) = 1. / H[J] * (u(I, J, K, 1) - u(I, J - 1, K, 1));
+                }
+#pragma omp parallel for
+            for (int J = 2; J <= N2M; J++) {
+                std::vector<double> D11(N1M + 1), X11(N1M + 1);
+                for (int I = 1; I <= N1M - 1; I++)
+                    D11[I] = 24. * DX1 * (sv21(I + 1, J) * vv21(I + 1, J) - sv21(I, J) * vv21(I, J));
+                D11[N1M] = 24. * DX1 * (sv21(1, J) * vv21(1, J) - sv21(N1M, J) * vv21(N1M, J));
+                ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+                for (int I = 1; I <= N1M; I++) HH[g.iuc(I, J, K, 2)] = HH[g.iuc(I, J, K, 2)] - X11[I];
+            }
+        }
+    }
+    // D(SGS*(DW/DY))/DZ
+    {
+        const size_t PK = (size_t)(N3M + 2);
+        std::vector<double> S3(PJ * PK), SV23(PJ * PK), VV32(PJ * PK);
+        auto s3 = [&](int j, int k) -> double & { return S3[j + PJ * k]; };
+        auto sv23 = [&](int j, int k) -> double & { return SV23[j + PJ * k]; };
+        auto vv32 = [&](int j, int k) -> double & { return VV32[j + PJ * k]; };
+        for (int I = 1; I <= N1M; I++) {
+#pragma omp parallel for
+            for (int J = 1; J <= N2M; J++) {
+                std::vector<double> D3(N3M + 1), X3(N3M + 1);
+                for (int K = 2; K <= N3M; K++) D3[K] = 4. * (sv(I, J, K - 1) + sv(I, J, K));
+                D3[1] = 4. * (sv(I, J, N3M) + sv(I, J, 1));
+                ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+                for (int K = 1; K <= N3M; K++) s3(J, K) = X3[K];
+            }
+#pragma omp parallel for
+            for (int K = 1; K <= N3M; K++)
+                for (int J = 2; J <= N2M; J++) {
+                    sv23(J, K) = 1. / H[J] * (DY[J] / 2. * s3(J - 1, K) + DY[J - 1] / 2. * s3(J, K));
+                    vv32(J, K) = 1. / H[J] * (u(I, J, K, 3) - u(I, J - 1, K, 3));
+                }
+#pragma omp parallel for
+            for (int J = 2; J <= N2M; J++) {
+                std::vector<double> D33(N3M + 1), X33(N3M + 1);
+                for (int K = 1; K <= N3M - 1; K++)
+                    D33[K] = 24. * DX3 * (sv23(J, K + 1) * vv32(J, K + 1) - sv23(J, K) * vv32(J, K));
+                D33[N3M] = 24. * DX3 * (sv23(J, 1) * vv32(J, 1) - sv23(J, N3M) * vv32(J, N3M));
+                ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+                for (int K = 1; K <= N3M; K++) HH[g.iuc(I, J, K, 2)] = HH[g.iuc(I, J, K, 2)] - X33[K];
+            }
+        }
+    }
+    // D(SGS*(DV/DZ))/DZ
+    {
+        const size_t PK = (size_t)(N3M + 2);
+        std::vector<double> SV3(PJ * PK), VV23(PJ * PK), SV32(PJ * PK);
+        auto sv3 = [&](int j, int k) -> double & { return SV3[j + PJ * k]; };
+        auto vv23 = [&](int j, int k) -> double & { return VV23[j + PJ * k]; };
+        auto sv32 = [&](int j, int k) -> double & { return SV32[j + PJ * k]; };
+        for (int I = 1; I <= N1M; I++) {
+#pragma omp parallel for
+            for (int J = 1; J <= N2M; J++) {
+                std::vector<double> D3(N3M + 1), X3(N3M + 1), D33(N3M + 1), X33(N3M + 1);
+                for (int K = 2; K <= N3M; K++) D3[K] = 4. * (sv(I, J, K - 1) + sv(I, J, K));
+                D3[1] = 4. * (sv(I, J, N3M) + sv(I, J, 1));
+                ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+                for (int K = 1; K <= N3M; K++) sv3(J, K) = X3[K];
+                for (int K = 2; K <= N3M; K++) D33[K] = 24. * DX3 * (u(I, J, K, 2) - u(I, J, K - 1, 2));
+                D33[1] = 24. * DX3 * (u(I, J, 1, 2) - u(I, J, N3M, 2));
+                ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+                for (int K = 1; K <= N3M; K++) vv23(J, K) = X33[K];
+            }
+#pragma omp parallel for
+            for (int K = 1; K <= N3M; K++)
+                for (int J = 2; J <= N2M; J++)
+                    sv32(J, K) = 1. / H[J] * (DY[J] / 2. * sv3(J - 1, K) + DY[J - 1] / 2. * sv3(J, K));
+#pragma omp parallel for
+            for (int J = 2; J <= N2M; J++) {
+                std::vector<double> D33(N3M + 1), X33(N3M + 1);
+                for (int K = 1; K <= N3M - 1; K++)
+                    D33[K] = 24. * DX3 * (sv32(J, K + 1) * vv23(J, K + 1) - sv32(J, K) * vv23(J, K));
+                D33[N3M] = 24. * DX3 * (sv32(J, 1) * vv23(J, 1) - sv32(J, N3M) * vv23(J, N3M));
+                ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+                for (int K = 1; K <= N3M; K++) HH[g.iuc(I, J, K, 2)] = HH[g.iuc(I, J, K, 2)] - X33[K];
+            }
+        }
+    }
+    // D(SGS*(DV/DX))/DX
+    {
+        std::vector<double> VV12(PX * PJ), SV12(PX * PJ), SV22(PX * PJ);
+        auto vv12 = [&](int i, int j) -> double & { return VV12[i + PX * j]; };
+        auto sv12 = [&](int i, int j) -> double & { return SV12[i + PX * j]; };
+        auto sv22 = [&](int i, int j) -> double & { return SV22[i + PX * j]; };
+        for (int K = 1; K <= N3M; K++) {
+#pragma omp parallel for
+            for (int J = 2; J <= N2M; J++) {
+                std::vector<double> D11(N1M + 1), X11(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D11[I] = 24. * DX1 * (u(I, J, K, 2) - u(I - 1, J, K, 2));
+                D11[1] = 24. * DX1 * (u(1, J, K, 2) - u(N1M, J, K, 2));
+                ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+                for (int I = 1; I <= N1M; I++) vv12(I, J) = X11[I];
+            }
+#pragma omp parallel for
+            for (int J = 1; J <= N2M; J++) {
+                std::vector<double> D1(N1M + 1), X1(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D1[I] = 4. * (sv(I, J, K) + sv(I - 1, J, K));
+                D1[1] = 4. * (sv(1, J, K) + sv(N1M, J, K));
+                ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+                for (int I = 1; I <= N1M; I++) sv12(I, J) = X1[I];
+            }
+#pragma omp parallel for
+            for (int I = 1; I <= N1M; I++)
+                for (int J = 2; J <= N2M; J++)
+                    sv22(I, J) = 1.0 / H[J] * (DY[J - 1] / 2. * sv12(I, J) + DY[J] / 2. * sv12(I, J - 1));
+#pragma omp parallel for
+            for (int J = 2; J <= N2M; J++) {
+                std::vector<double> D11(N1M + 1), X11(N1M + 1);
+                for (int I = 1; I <= N1M - 1; I++)
+                    D11[I] = 24. * DX1 * (sv22(I + 1, J) * vv12(I + 1, J) - sv22(I, J) * vv12(I, J));
+                D11[N1M] = 24. * DX1 * (sv22(1, J) * vv12(1, J) - sv22(N1M, J) * vv12(N1M, J));
+                ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+                for (int I = 1; I <= N1M; I++) HH[g.iuc(I, J, K, 2)] = HH[g.iuc(I, J, K, 2)] - X11[I];
+            }
+        }
+    }
+}
+
+// RHS3 (compact3d.f:7774-8111): SGS fluxes at the w faces.
+void sgs_rhs3(Orc &g, const double *U, double *HH, const double *SGSVIS) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
+    const double DX1 = g.DX1, DX3 = g.DX3, ALY = g.ALY, IFWALL = g.IFWALL;
+    const double *DY = g.DY.data(), *H = g.H.data();
+    auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+    auto sv = [&](int i, int j, int k) { return SGSVIS[g.iu(i, j, k)]; };
+    ConstLine L6x, L6z, L22x, L22z;
+    L6x.set(N1M, 1.0, 6.0, 1.0);
+    L6z.set(N3M, 1.0, 6.0, 1.0);
+    L22x.set(N1M, 1.0, 22.0, 1.0);
+    L22z.set(N3M, 1.0, 22.0, 1.0);
+    const size_t PX = (size_t)(N1M + 2), PK = (size_t)(N3M + 2), PJ = (size_t)(N2 + 2);
+    // 61-63: D(SGS*(DW/DX))/DX
+    {
+        std::vector<double> SW3(PX * PK);
+        auto sw3 = [&](int i, int k) -> double & { return SW3[i + PX * k]; };
+        for (int J = 1; J <= N2M; J++) {
+#pragma omp parallel for
+            for (int I = 1; I <= N1M; I++) {
+                std::vector<double> D3(N3M + 1), X3(N3M + 1);
+                for (int K = 2; K <= N3M; K++) D3[K] = 4. * (sv(I, J, K - 1) + sv(I, J, K));
+                D3[1] = 4. * (sv(I, J, N3M) + sv(I, J, 1));
+                ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+                for (int K = 1; K <= N3M; K++) sw3(I, K) = X3[K];
+            }
+#pragma omp parallel for
+            for (int K = 1; K <= N3M; K++) {
+                std::vector<double> D1(N1M + 1), X1(N1M + 1), D11(N1M + 1), X11(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D1[I] = 4. * (sw3(I - 1, K) + sw3(I, K));
+                D1[1] = 4. * (sw3(N1M, K) + sw3(1, K));
+                ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+                for (int I = 2; I <= N1M; I++) D11[I] = 24. * DX1 * (u(I, J, K, 3) - u(I - 1, J, K, 3));
+                D11[1] = 24. * DX1 * (u(1, J, K, 3) - u(N1M, J, K, 3));
+                ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+                for (int I = 1; I <= N1M - 1; I++) D11[I] = 24. * DX1 * (X1[I + 1] * X11[I + 1] - X1[I] * X11[I]);
+                D11[N1M] = 24. * DX1 * (X1[1] * X11[1] - X1[N1M] * X11[N1M]);
+                ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+                for (int I = 1; I <= N1M; I++) HH[g.iuc(I, J, K, 3)] = HH[g.iuc(I, J, K, 3)] - X11[I];
+            }
+        }
+    }
+    // 64-66: D(SGS*(DW/DY))/DY
+    {
+        std::vector<double> SW2(PJ * PK, 0.0);
+        auto sw2 = [&](int j, int k) -> double & { return SW2[j + PJ * k]; };
+        for (int I = 1; I <= N1M; I++) {
+#pragma omp parallel for
+            for (int J = 1; J <= N2M; J++) {
+                std::vector<double> D3(N3M + 1), X3(N3M + 1);
+                for (int K = 2; K <= N3M; K++) D3[K] = 4. * (sv(I, J, K) + sv(I, J, K - 1));
+                D3[1] = 4. * (sv(I, J, 1) + sv(I, J, N3M));
+                ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+                for (int K = 1; K <= N3M; K++) sw2(J, K) = X3[K];
+            }
+#pragma omp parallel for
+            for (int K = 1; K <= N3M; K++) {
+                const int KM = g.KMA[K];
+                for (int J = 1; J <= N2M; J++) {
+                    const int JP = J + 1, JM = J - 1;
+                    const double FJUM = g.FJMU[J], FJUP = g.FJPA[J];
+                    double WW22 = 1. / H[JP] * (u(I, JP, K, 3) - u(I, J, K, 3));
+                    double WW11 = 1. / H[J] * (u(I, J, K, 3) - u(I, JM, K, 3));
+                    double SGSJ1 = FJUM * 1. / H[J] * (DY[JM] / 2. * sw2(J, K) + DY[J] / 2. * sw2(JM, K)) +
+                                   (1. - FJUM) * 0.5 * (sv(I, 0, K) + sv(I, 0, KM));
+                    double SGSJ2 = FJUP * 1.0 / H[JP] * (DY[J] / 2. * sw2(JP, K) + DY[JP] / 2. * sw2(J, K)) +
+                                   (1. - FJUP) * 0.5 * (sv(I, N2, K) + sv(I, N2, KM));
+                    double SGSDWY = 1. / DY[J] * ((1. - IFWALL * (1. - FJUP) * (ALY - 1.)) * SGSJ2 * WW22 -
+                                                  (1. - IFWALL * (1. - FJUM)) * SGSJ1 * WW11);
+                    HH[g.iuc(I, J, K, 3)] = HH[g.iuc(I, J, K, 3)] - SGSDWY;
+                }
+            }
+        }
+    }
+    // 67: D(SGS*(DW/DZ))/DZ
+#pragma omp parallel for
+    for (int I = 1; I <= N1M; I++) {
+        std::vector<double> D33(N3M + 1), X33(N3M + 1);
+        for (int J = 1; J <= N2M; J++) {
+            for (int K = 1; K <= N3M - 1; K++) D33[K] = 24. * DX3 * (u(I, J, K + 1, 3) - u(I, J, K, 3));
+            D33[N3M] = 24. * DX3 * (u(I, J, 1, 3) - u(I, J, N3M, 3));
+            ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+            for (int K = 2; K <= N3M; K++) D33[K] = 24. * DX3 * (X33[K] * sv(I, J, K) - X33[K - 1] * sv(I, J, K - 1));
+            D33[1] = 24. * DX3 * (X33[1] * sv(I, J, 1) - X33[N3M] * sv(I, J, N3M));
+            ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+            for (int K = 1; K <= N3M; K++) HH[g.iuc(I, J, K, 3)] = HH[g.iuc(I, J, K, 3)] - 2. * X33[K];
+        }
+    }
+    // 68-70: D(SGS*(DU/DZ))/DX
+    {
+        std::vector<double> UU31(PX * PK), S31(PX * PK);
+        auto uu31 = [&](int i, int k) -> double & { return UU31[i + PX * k]; };
+        auto s31 = [&](int i, int k) -> double & { return S31[i + PX * k]; };
+        for (int J = 1; J <= N2M; J++) {
+#pragma omp parallel for
+            for (int I = 1; I <= N1M; I++) {
+                std::vector<double> D3(N3M + 1), X3(N3M + 1), D33(N3M + 1), X33(N3M + 1);
+                for (int K = 2; K <= N3M; K++) D33[K] = 24. * DX3 * (u(I, J, K, 1) - u(I, J, K - 1, 1));
+                D33[1] = 24. * DX3 * (u(I, J, 1, 1) - u(I, J, N3M, 1));
+                ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+                for (int K = 1; K <= N3M; K++) uu31(I, K) = X33[K];
+                for (int K = 2; K <= N3M; K++) D3[K] = 4. * (sv(I, J, K) + sv(I, J, K - 1));
+                D3[1] = 4. * (sv(I, J, 1) + sv(I, J, N3M));
+                ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+                for (int K = 1; K <= N3M; K++) s31(I, K) = X3[K];
+            }
+#pragma omp parallel for
+            for (int K = 1; K <= N3M; K++) {
+                std::vector<double> D1(N1M + 1), X1(N1M + 1), D11(N1M + 1), X11(N1M + 1);
+                for (int I = 2; I <= N1M; I++) D1[I] = 4. * (s31(I, K) + s31(I - 1, K));
+                D1[1] = 4. * (s31(1, K) + s31(N1M, K));
+                ctdma_bordered(N1M, L6x.A.data(), L6x.B.data(), L6x.C.data(), D1.data(), X1.data());
+                for (int I = 1; I <= N1M - 1; I++) D11[I] = 24. * DX1 * (X1[I + 1] * uu31(I + 1, K) - X1[I] * uu31(I, K));
+                D11[N1M] = 24. * DX1 * (X1[1] * uu31(1, K) - X1[N1M] * uu31(N1M, K));
+                ctdma_bordered(N1M, L22x.A.data(), L22x.B.data(), L22x.C.data(), D11.data(), X11.data());
+                for (int I = 1; I <= N1M; I++) HH[g.iuc(I, J, K, 3)] = HH[g.iuc(I, J, K, 3)] - X11[I];
+            }
+        }
+    }
+    // 71-73: D(SGS*(DV/DZ))/DY (the AB2 update and wall term follow in rhs3)
+    {
+        std::vector<double> VV32(PJ * PK, 0.0), S32(PJ * PK, 0.0);
+        auto vv32 = [&](int j, int k) -> double & { return VV32[j + PJ * k]; };
+        auto s32 = [&](int j, int k) -> double & { return S32[j + PJ * k]; };
+        for (int I = 1; I <= N1M; I++) {
+#pragma omp parallel for
+            for (int J = 1; J <= N2M; J++) {
+                std::vector<double> D3(N3M + 1), X3(N3M + 1), D33(N3M + 1), X33(N3M + 1);
+                for (int K = 2; K <= N3M; K++) D33[K] = 24. * DX3 * (u(I, J, K, 2) - u(I, J, K - 1, 2));
+                D33[1] = 24. * DX3 * (u(I, J, 1, 2) - u(I, J, N3M, 2));
+                ctdma_bordered(N3M, L22z.A.data(), L22z.B.data(), L22z.C.data(), D33.data(), X33.data());
+                for (int K = 1; K <= N3M; K++) vv32(J, K) = X33[K];
+                for (int K = 2; K <= N3M; K++) D3[K] = 4. * (sv(I, J, K) + sv(I, J, K - 1));
+                D3[1] = 4. * (sv(I, J, 1) + sv(I, J, N3M));
+                ctdma_bordered(N3M, L6z.A.data(), L6z.B.data(), L6z.C.data(), D3.data(), X3.data());
+                for (int K = 1; K <= N3M; K++) s32(J, K) = X3[K];
+            }
+#pragma omp parallel for
+            for (int K = 1; K <= N3M; K++) {
+                const int KM = g.KMA[K];
+                for (int J = 1; J <= N2M; J++) {
+                    const int JP = J + 1, JM = J - 1;
+                    const double FJUM = g.FJMU[J], FJUP = g.FJPA[J];
+                    double SGSJ2 = FJUP * 1.0 / H[JP] * (DY[J] / 2. * s32(JP, K) + DY[JP] / 2. * s32(J, K)) +
+                                   (1. - FJUP) * 0.5 * (sv(I, N2, K) + sv(I, N2, KM));
+                    double SGSJ1 = FJUM * 1.0 / H[J] * (DY[JM] / 2. * s32(J, K) + DY[J] / 2. * s32(JM, K)) +
+                                   (1. - FJUM) * 0.5 * (sv(I, 0, K) + sv(I, 0, KM));
+                    double SGSDVY = 1.0 / DY[J] * ((1. - IFWALL * (1. - FJUP) * (ALY - 1.)) * SGSJ2 * vv32(JP, K) -
+                                                   (1. - IFWALL * (1. - FJUM)) * SGSJ1 * vv32(J, K));
+                    HH[g.iuc(I, J, K, 3)] = HH[g.iuc(I, J, K, 3)] - SGSDVY;
+                }
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------------
+// SGS models and the wall model (compact3d.f:1250-1488, 5190-5228, 5558-5689,
+// 2319-2493, 11077-11143).
+// ----------------------------------------------------------------------------------
+
+// STRAIN (compact3d.f:5558-5689): strain-rate tensor at the cell centres of plane J,
+// SR(I,K,1..6) = S11, S12, S13, S22, S23, S33, stored SR[(I-1) + N1M*((K-1) + N3M*(c-1))].
+void strain(Orc &g, const double *U, std::vector<double> &SR, int J) {
+    const int N1M = g.N1M, N3M = g.N3M, N2 = g.N2, N2M = g.N2M;
+    const double DX1 = g.DX1, DX3 = g.DX3;
+    const double *DY = g.DY.data(), *H = g.H.data();
+    auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+    auto sr = [&](int i, int k, int c) -> double & { return SR[(i - 1) + (size_t)N1M * ((k - 1) + (size_t)N3M * (c - 1))]; };
+    const int JP = J + 1, JM = J - 1;
+    const int FJUM = (int)g.FJMU[J], FJUP = (int)g.FJPA[J];
+    const bool wm = g.WMODEL != 0;
+    for (int K = 1; K <= N3M; K++) {
+        const int KP = g.KPA[K], KM = g.KMA[K];
+        for (int I = 1; I <= N1M; I++) {
+            const int IP = g.IPA[I], IM = g.IMA[I];
+            double U2 = u(IP, J, K, 1), U1 = u(I, J, K, 1);
+            sr(I, K, 1) = DX1 * (U2 - U1);
+            double UJP = 0.5 * (u(I, JP, K, 1) + u(IP, JP, K, 1));
+            double UJC = 0.5 * (u(I, J, K, 1) + u(IP, J, K, 1));
+            double UJM = 0.5 * (u(I, JM, K, 1) + u(IP, JM, K, 1));
+            if (!wm) {
+                U2 = FJUP * 1.0 / H[JP] * (DY[J] / 2.0 * UJP + DY[JP] / 2.0 * UJC) +
+                     (1. - FJUP) * 0.5 * (u(I, N2, K, 1) + u(IP, N2, K, 1));
+                U1 = FJUM * 1.0 / H[J] * (DY[J] / 2.0 * UJM + DY[JM] / 2.0 * UJC) +
+                     (1. - FJUM) * 0.5 * (u(I, 0, K, 1) + u(IP, 0, K, 1));
+            } else {
+                U2 = FJUP * 1.0 / H[JP] * (DY[J] / 2.0 * UJP + DY[JP] / 2.0 * UJC) + (1. - FJUP) * UJC;
+                U1 = FJUM * 1.0 / H[J] * (DY[J] / 2.0 * UJM + DY[JM] / 2.0 * UJC) + (1. - FJUM) * UJC;
+            }
+            double VIP = 0.5 * (u(IP, J, K, 2) + u(IP, JP, K, 2));
+            double VIC = 0.5 * (u(I, J, K, 2) + u(I, JP, K, 2));
+            double VIM = 0.5 * (u(IM, J, K, 2) + u(IM, JP, K, 2));
+            double V2 = 0.5 * (VIP + VIC), V1 = 0.5 * (VIM + VIC);
+            if (!wm || (J != 1 && J != N2M)) sr(I, K, 2) = 0.5 * (DX1 * (V2 - V1) + 1.0 / DY[J] * (U2 - U1));
+            else sr(I, K, 2) = 0.5 * (DX1 * (V2 - V1) + 2.0 / DY[J] * (U2 - U1));
+            double UKP = 0.5 * (u(I, J, KP, 1) + u(IP, J, KP, 1));
+            double UKC = 0.5 * (u(I, J, K, 1) + u(IP, J, K, 1));
+            double UKM = 0.5 * (u(I, J, KM, 1) + u(IP, J, KM, 1));
+            U2 = 0.5 * (UKP + UKC);
+            U1 = 0.5 * (UKM + UKC);
+            double WIP = 0.5 * (u(IP, J, K, 3) + u(IP, J, KP, 3));
+            double WIC = 0.5 * (u(I, J, K, 3) + u(I, J, KP, 3));
+            double WIM = 0.5 * (u(IM, J, K, 3) + u(IM, J, KP, 3));
+            double W2 = 0.5 * (WIP + WIC), W1 = 0.5 * (WIM + WIC);
+            sr(I, K, 3) = 0.5 * (DX1 * (W2 - W1) + DX3 * (U2 - U1));
+            V2 = u(I, JP, K, 2);
+            V1 = u(I, J, K, 2);
+            sr(I, K, 4) = 1.0 / DY[J] * (V2 - V1);
+            double WJP = 0.5 * (u(I, JP, K, 3) + u(I, JP, KP, 3));
+            double WJC = 0.5 * (u(I, J, K, 3) + u(I, J, KP, 3));
+            double WJM = 0.5 * (u(I, JM, K, 3) + u(I, JM, KP, 3));
+            if (!wm) {
+                W2 = FJUP * 1.0 / H[JP] * (DY[J] / 2.0 * WJP + DY[JP] / 2.0 * WJC) +
+                     (1. - FJUP) * 0.5 * (u(I, N2, K, 3) + u(I, N2, KP, 3));
+                W1 = FJUM * 1.0 / H[J] * (DY[J] / 2.0 * WJM + DY[JM] / 2.0 * WJC) +
+                     (1. - FJUM) * 0.5 * (u(I, 0, K, 3) + u(I, 0, KP, 3));
+            } else {
+                W2 = FJUP * 1.0 / H[JP] * (DY[J] / 2.0 * WJP + DY[JP] / 2.0 * WJC) + (1. - FJUP) * WJC;
+                W1 = FJUM * 1.0 / H[J] * (DY[J] / 2.0 * WJM + DY[JM] / 2.0 * WJC) + (1. - FJUM) * WJC;
+            }
+            double VKP = 0.5 * (u(I, J, KP, 2) + u(I, JP, KP, 2));
+            double VKC = 0.5 * (u(I, J, K, 2) + u(I, JP, K, 2));
+            double VKM = 0.5 * (u(I, J, KM, 2) + u(I, JP, KM, 2));
+            V2 = 0.5 * (VKP + VKC);
+            V1 = 0.5 * (VKM + VKC);
+            if (!wm || (J != 1 && J != N2M)) sr(I, K, 5) = 0.5 * (1.0 / DY[J] * (W2 - W1) + DX3 * (V2 - V1));
+            else sr(I, K, 5) = 0.5 * (2.0 / DY[J] * (W2 - W1) + DX3 * (V2 - V1));
+            W2 = u(I, J, KP, 3);
+            W1 = u(I, J, K, 3);
+            sr(I, K, 6) = DX3 * (W2 - W1);
+        }
+    }
+}
+
+// FILTER (compact3d.f:5190-5228): Simpson (1,4,1)/6 in x, then in z, for N components.
+void filter(Orc &g, std::vector<double> &F, int N) {
+    const int N1M = g.N1M, N3M = g.N3M;
+    std::vector<double> T((size_t)N1M * N3M);
+    for (int L = 1; L <= N; L++) {
+        double *f = F.data() + (size_t)N1M * N3M * (L - 1);
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                const int IP = g.IPA[I], IM = g.IMA[I];
+                double FM = f[(IM - 1) + (size_t)N1M * (K - 1)], FC = f[(I - 1) + (size_t)N1M * (K - 1)],
+                       FP = f[(IP - 1) + (size_t)N1M * (K - 1)];
+                T[(I - 1) + (size_t)N1M * (K - 1)] = (FM + 4.0 * FC + FP) / 6.0;
+            }
+        for (int K = 1; K <= N3M; K++) {
+            const int KP = g.KPA[K], KM = g.KMA[K];
+            for (int I = 1; I <= N1M; I++) {
+                double FM = T[(I - 1) + (size_t)N1M * (KM - 1)], FC = T[(I - 1) + (size_t)N1M * (K - 1)],
+                       FP = T[(I - 1) + (size_t)N1M * (KP - 1)];
+                f[(I - 1) + (size_t)N1M * (K - 1)] = (FM + 4.0 * FC + FP) / 6.0;
+            }
+        }
+    }
+}
+
+inline double sumsq6(const double s1, const double s2, const double s3, const double s4, const double s5,
+                     const double s6) {
+    return 2. * s2 * s2 + s1 * s1 + 2. * s3 * s3 + s4 * s4 + 2. * s5 * s5 + s6 * s6;
+}
+
+// SGSDY (compact3d.f:1250-1400): dynamic Smagorinsky, plane-averaged coefficient, clipped.
+void sgsdy(Orc &g, const double *U, double *SGSVIS) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const size_t NP = (size_t)N1M * N3M;
+    const double NXZ = 1.0 / (double)(N1M * N3M), RENINV = 1. / g.RE;
+    std::vector<double> SR(NP * 6), COM(NP * 6), UC(NP * 3);
+    for (int J = 1; J <= N2M; J++) {
+        const double DXYZ = 1.0 / g.DX1 * g.DY[J] / g.DX3;
+        strain(g, U, SR, J);
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                const size_t q = (I - 1) + (size_t)N1M * (K - 1);
+                double DELTA2 = std::pow(DXYZ, 2. / 3.);
+                double SUMSR = sumsq6(SR[q], SR[q + NP], SR[q + 2 * NP], SR[q + 3 * NP], SR[q + 4 * NP], SR[q + 5 * NP]);
+                double ABSSR = std::sqrt(2. * SUMSR);
+                SGSVIS[g.iu(I, J, K)] = ABSSR;
+                double DELABS = DELTA2 * ABSSR;
+                for (int c = 0; c < 6; c++) COM[q + c * NP] = DELABS * SR[q + c * NP];
+            }
+        filter(g, COM, 6);
+        filter(g, SR, 6);
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                const size_t q = (I - 1) + (size_t)N1M * (K - 1);
+                double SUMFSR = sumsq6(SR[q], SR[q + NP], SR[q + 2 * NP], SR[q + 3 * NP], SR[q + 4 * NP], SR[q + 5 * NP]);
+                double ABSFSR = std::sqrt(2. * SUMFSR);
+                double FDXYZ = 4.0 * std::pow(DXYZ, 2. / 3.);
+                double FDABS = FDXYZ * ABSFSR;
+                for (int c = 0; c < 6; c++) SR[q + c * NP] = FDABS * SR[q + c * NP] - COM[q + c * NP];
+            }
+        const int JP = J + 1;
+        for (int K = 1; K <= N3M; K++) {
+            const int KP = g.KPA[K];
+            for (int I = 1; I <= N1M; I++) {
+                const int IP = g.IPA[I];
+                const size_t q = (I - 1) + (size_t)N1M * (K - 1);
+                double a = (U[g.iuc(I, J, K, 1)] + U[g.iuc(IP, J, K, 1)]) * 0.5;
+                double b = (U[g.iuc(I, J, K, 2)] + U[g.iuc(I, JP, K, 2)]) * 0.5;
+                double c = (U[g.iuc(I, J, K, 3)] + U[g.iuc(I, J, KP, 3)]) * 0.5;
+                UC[q] = a;
+                UC[q + NP] = b;
+                UC[q + 2 * NP] = c;
+                COM[q] = a * a;
+                COM[q + NP] = a * b;
+                COM[q + 2 * NP] = a * c;
+                COM[q + 3 * NP] = b * b;
+                COM[q + 4 * NP] = b * c;
+                COM[q + 5 * NP] = c * c;
+            }
+        }
+        filter(g, UC, 3);
+        filter(g, COM, 6);
+        // 40: the plane sums (an OpenMP reduction in the reference; fixed order here)
+        double SUMNUM = 0., SUMDEN = 0.;
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                const size_t q = (I - 1) + (size_t)N1M * (K - 1);
+                const double u1 = UC[q], u2 = UC[q + NP], u3 = UC[q + 2 * NP];
+                double XL11 = COM[q] - u1 * u1, XL12 = COM[q + NP] - u1 * u2, XL13 = COM[q + 2 * NP] - u1 * u3;
+                double XL22 = COM[q + 3 * NP] - u2 * u2, XL23 = COM[q + 4 * NP] - u2 * u3,
+                       XL33 = COM[q + 5 * NP] - u3 * u3;
+                const double *m = &SR[q];
+                double SQMM = sumsq6(m[0], m[NP], m[2 * NP], m[3 * NP], m[4 * NP], m[5 * NP]);
+                double SQLM = 2. * XL12 * m[NP] + XL11 * m[0] + 2. * XL13 * m[2 * NP] + XL22 * m[3 * NP] +
+                              2. * XL23 * m[4 * NP] + XL33 * m[5 * NP];
+                SUMDEN = SUMDEN + SQMM;
+                SUMNUM = SUMNUM + SQLM;
+            }
+        SUMNUM = SUMNUM * NXZ;
+        SUMDEN = SUMDEN * NXZ;
+        g.SMAGC[J] = -0.5 * SUMNUM / SUMDEN;
+        const double CS_DAMPING = 1.0;
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                double TURBV = g.SMAGC[J] * std::pow(DXYZ, 2. / 3.) * SGSVIS[g.iu(I, J, K)];
+                double s = std::max(TURBV, -RENINV);
+                SGSVIS[g.iu(I, J, K)] = s * CS_DAMPING;
+            }
+    }
+}
+
+// SGSCS (compact3d.f:1413-1488): Smagorinsky with Van Driest damping, C_s = 0.1.
+void sgscs(Orc &g, const double *U, double *SGSVIS) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const size_t NP = (size_t)N1M * N3M;
+    const double RENINV = 1. / g.RE;
+    std::vector<double> SR(NP * 6);
+    const double UTAU = std::sqrt(std::sqrt(g.WSM[0] * g.WSM[0] + g.WSM[2] * g.WSM[2]));
+    for (int J = 1; J <= N2M; J++) {
+        const double DXYZ = 1.0 / g.DX1 * g.DY[J] / g.DX3;
+        strain(g, U, SR, J);
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                const size_t q = (I - 1) + (size_t)N1M * (K - 1);
+                double SUMSR = sumsq6(SR[q], SR[q + NP], SR[q + 2 * NP], SR[q + 3 * NP], SR[q + 4 * NP], SR[q + 5 * NP]);
+                SGSVIS[g.iu(I, J, K)] = std::sqrt(2. * SUMSR);
+            }
+        double CS = 0.1;
+        const double A_plus = 26.0;
+        const double Y_plus = (g.Y[J] + g.DY[J] * 0.5) * UTAU * g.RE;
+        CS = CS * (1 - std::exp(-Y_plus / A_plus));
+        g.SMAGC[J] = CS * CS;
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                double TURBV = g.SMAGC[J] * std::pow(DXYZ, 2. / 3.) * SGSVIS[g.iu(I, J, K)];
+                SGSVIS[g.iu(I, J, K)] = std::max(TURBV, -RENINV);
+            }
+    }
+}
+
+// WALLSS (compact3d.f:11077-11143): plane-mean wall shear into wsm[0..2] (/WSMEM/ WSM),
+// one running sum in K, I order.  The reference adds the top wall's u-shear WST(I,K,1)
+// to all three components (scaled by ALY-1).
+void wallss_common(Orc &g, const double *U, double *wsm) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
+    double W1 = 0.0, W2 = 0.0, W3 = 0.0;
+    const double *DY = g.DY.data();
+    double NXZ = 1.0 / (double)(N1M * N3M);
+    auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+    for (int K = 1; K <= N3M; K++) {
+        int KP = g.KPA[K];
+        for (int I = 1; I <= N1M; I++) {
+            int IP = g.IPA[I];
+            double UHC = 0.5 * (u(I, 1, K, 1) + u(IP, 1, K, 1));
+            double UHW = 0.5 * (u(I, 0, K, 1) + u(IP, 0, K, 1));
+            double VHC = u(I, 2, K, 2);
+            double VHW = u(I, 1, K, 2);
+            double WHC = 0.5 * (u(I, 1, K, 3) + u(I, 1, KP, 3));
+            double WHW = 0.5 * (u(I, 0, K, 3) + u(I, 0, KP, 3));
+            double WSB1 = (UHC - UHW) / (DY[1] * 0.5);
+            double WSB2 = (VHC - VHW) / DY[1];
+            double WSB3 = (WHC - WHW) / (DY[1] * 0.5);
+            UHC = 0.5 * (u(I, N2M, K, 1) + u(IP, N2M, K, 1));
+            UHW = 0.5 * (u(I, N2, K, 1) + u(IP, N2, K, 1));
+            double WST1 = (UHC - UHW) / (DY[N2M] * 0.5);
+            W1 = W1 + WSB1 + WST1 * (g.ALY - 1.0);
+            W2 = W2 + WSB2 + WST1 * (g.ALY - 1.0);
+            W3 = W3 + WSB3 + WST1 * (g.ALY - 1.0);
+        }
+    }
+    wsm[0] = W1 * NXZ / g.RE / g.ALY;
+    wsm[1] = W2 * NXZ / g.RE / g.ALY;
+    wsm[2] = W3 * NXZ / g.RE / g.ALY;
+}
+
+// WALLMODEL_INSTANT (compact3d.f:2319-2493): per wall point, u_tau from the log law at
+// the third cell centre by damped Newton iterations; bottom wall only (the top-wall
+// stresses TAUW(.,.,2), TAUB(.,.,2) are left as they are).  The reference iterates
+// without a cap; here the cap `wall_iter_cap` makes a non-converging point an error.
+int wallmodel_instant(Orc &g, const double *U) {
+    const int N1M = g.N1M, N3M = g.N3M;
+    const double KAPA = 0.41, B = 5.2;
+    const double DELTAP = g.DY[1] + g.DY[2] + g.DY[3] / 2.0;
+    const double RE = g.RE;
+    int bad = 0;
+    double wsum = 0.0;
+    for (int K = 1; K <= N3M; K++)
+        for (int I = 1; I <= N1M; I++) {
+            const double u3 = U[g.iuc(I, 3, K, 1)], w3 = U[g.iuc(I, 3, K, 3)];
+            double U_ave = std::sqrt(u3 * u3 + w3 * w3);
+            double U_tau1 = 1.0, U_tau2 = 0.000001, FUtau3 = 1.0, FUtau1 = 0.1, LAMBDA = 1.0;
+            int it = 0;
+            while (std::fabs(U_tau2 - U_tau1) > 1.0E-6) {
+                if (++it > g.wall_iter_cap) {
+                    bad = 1;
+                    break;
+                }
+                U_tau1 = U_tau2;
+                FUtau1 = U_ave / U_tau1 - std::log(U_tau1 * DELTAP * RE) / KAPA - B;
+                double FUtau2 = -U_ave / (U_tau1 * U_tau1) - 1. / KAPA / U_tau1;
+                U_tau2 = U_tau1 - LAMBDA * FUtau1 / FUtau2;
+                FUtau3 = U_ave / U_tau2 - std::log(U_tau2 * DELTAP * RE) / KAPA - B;
+                if (std::fabs(FUtau3) > std::fabs(FUtau1)) LAMBDA = 0.5 * LAMBDA;
+            }
+            double TAUW1 = U_tau1 * U_tau1;
+            wsum = wsum + TAUW1;
+            g.TAUW[g.itw(I, K, 1)] = TAUW1 * u3 / U_ave;
+            g.TAUB[g.itw(I, K, 1)] = TAUW1 * w3 / U_ave;
+        }
+    g.WSM[0] = wsum / (double)(N1M * N3M);
+    g.TAOW = g.WSM[0];
+    return bad ? C3D_ENOTCONV : 0;
 }
 
 // ----------------------------------------------------------------------------------
@@ -1167,6 +1965,7 @@ void *orc_create(const c3d_grid *gr) {
     g->UBC.assign((size_t)(g->N1 + 1) * (g->N3 + 1) * 6, 0.0);
     g->TAUW.assign((size_t)(g->N1 + 1) * (g->N3 + 1) * 2, 0.0);
     g->TAUB.assign((size_t)(g->N1 + 1) * (g->N3 + 1) * 2, 0.0);
+    g->SMAGC.assign((size_t)g->N2 + 1, 0.0);
     g->UH.assign(nu, 0.0);
     g->HH2.assign(nu, 0.0);
     g->RUH1.assign(ns, 0.0);
@@ -1205,14 +2004,62 @@ void orc_set_wall(void *h, const double *tauw, const double *taub, int ifwall) {
     g.IFWALL = ifwall;
 }
 
-// GETUP (compact3d.f:879-960) for FILES == 0.  U, P, HH, SGSVIS are Fortran arrays.
+// TAUW, TAUB (0:M1,0:M3,2) and /WSMEM/ WSM(1:3) as the step left them (null: skip).
+void orc_get_wall(void *h, double *tauw, double *taub, double *wsm) {
+    Orc &g = *(Orc *)h;
+    if (tauw) std::memcpy(tauw, g.TAUW.data(), g.TAUW.size() * sizeof(double));
+    if (taub) std::memcpy(taub, g.TAUB.data(), g.TAUB.size() * sizeof(double));
+    if (wsm) std::memcpy(wsm, g.WSM, 3 * sizeof(double));
+}
+void orc_set_wsm(void *h, const double *wsm) { std::memcpy(((Orc *)h)->WSM, wsm, 3 * sizeof(double)); }
+void orc_set_wall_iter_cap(void *h, int cap) { ((Orc *)h)->wall_iter_cap = cap; }
+
+// The SGS model alone (SGSDY for FILES=1, SGSCS for FILES=2) on U, after GETUP's zeroing
+// of SGSVIS; smagc (length N2M, may be null) receives SMAGC(1:N2M).
+int orc_sgs(void *h, const double *U, double *SGSVIS, double *smagc) {
+    Orc &g = *(Orc *)h;
+    for (int K = 1; K <= g.N3; K++)
+        for (int J = 0; J <= g.N2; J++)
+            for (int I = 1; I <= g.N1; I++) SGSVIS[g.iu(I, J, K)] = 0.0;
+    if (g.FILES == 1) sgsdy(g, U, SGSVIS);
+    else if (g.FILES == 2) sgscs(g, U, SGSVIS);
+    else return C3D_EINVAL;
+    if (smagc)
+        for (int J = 1; J <= g.N2M; J++) smagc[J - 1] = g.SMAGC[J];
+    return 0;
+}
+
+// The SGS-flux contributions alone: HH (0:M1,0:M2,0:M3,3) is zeroed, then receives the
+// terms RHS1/2/3 subtract from HH for the given SGSVIS (wall planes as passed).
+int orc_sgs_rhs(void *h, const double *U, const double *SGSVIS, double *HH) {
+    Orc &g = *(Orc *)h;
+    std::memset(HH, 0, (size_t)g.su3 * 3 * sizeof(double));
+    sgs_rhs1(g, U, HH, SGSVIS);
+    sgs_rhs2_vis22(g, U, HH, SGSVIS);
+    sgs_rhs2(g, U, HH, SGSVIS);
+    sgs_rhs3(g, U, HH, SGSVIS);
+    return 0;
+}
+
+// WALLMODEL_INSTANT alone on U (TAUW, TAUB, WSM(1) are updated in the handle).
+int orc_wallmodel(void *h, const double *U) { return wallmodel_instant(*(Orc *)h, U); }
+
+// GETUP (compact3d.f:879-960).  U, P, HH, SGSVIS are Fortran arrays (SGSVIS may be null;
+// an internal array is used then).  With an SGS model (FILES != 0) the driver's WALLSS
+// call that precedes GETUP when WMODEL == 0 (compact3d.f:125) is folded in here, so
+// SGSCS sees the wall shear of the current field as in the reference's time loop.
 int orc_getup(void *h, double *U, double *P, double *HH, double *SGSVIS, int NTIME, double DT,
               double *PRESG, double *PRESG3) {
     Orc &g = *(Orc *)h;
     (void)NTIME;
-    if (g.FILES != 0) return C3D_EINVAL;
+    if (g.FILES < 0 || g.FILES > 2 || g.WMODEL < 0 || g.WMODEL > 1) return C3D_EINVAL;
     const int N1 = g.N1, N2 = g.N2, N3 = g.N3;
     double *UH = g.UH.data(), *HH2 = g.HH2.data();
+    if (g.FILES != 0 && !SGSVIS) {
+        g.SGS.assign((size_t)g.su3, 0.0);
+        SGSVIS = g.SGS.data();
+    }
+    if (g.FILES != 0 && g.WMODEL == 0) wallss_common(g, U, g.WSM);
     for (int NV = 1; NV <= 3; NV++) {
 #pragma omp parallel for
         for (int K = 1; K <= N3; K++)
@@ -1239,11 +2086,24 @@ int orc_getup(void *h, double *U, double *P, double *HH, double *SGSVIS, int NTI
                     HH[id] = 0.0;
                 }
     }
+    if (g.FILES == 1) sgsdy(g, U, SGSVIS);
+    if (g.FILES == 2) sgscs(g, U, SGSVIS);
+    int status = 0;
+    if (g.FILES != 0) {   // WALL_MODEL (compact3d.f:1952-2026)
+        if (g.WMODEL == 0) {
+            g.IFWALL = 0;
+            wallss_common(g, U, g.WSM);
+        } else {
+            status = wallmodel_instant(g, U);
+            g.IFWALL = 1;
+        }
+    }
+    const double *SV = g.FILES != 0 ? SGSVIS : nullptr;
     bcond(g, U, SGSVIS);
     // UHCALC
-    rhs1(g, U, P, HH, HH2, g.RUH1.data(), *PRESG);
-    rhs2(g, U, P, HH, HH2, g.RUH2.data());
-    rhs3(g, U, P, HH, HH2, g.RUH3.data(), *PRESG3);
+    rhs1(g, U, P, HH, HH2, g.RUH1.data(), *PRESG, SV);
+    rhs2(g, U, P, HH, HH2, g.RUH2.data(), SV);
+    rhs3(g, U, P, HH, HH2, g.RUH3.data(), *PRESG3, SV);
     getuh(g, U, UH, g.RUH1.data(), 1, DT);
     getuh(g, U, UH, g.RUH2.data(), 2, DT);
     getuh(g, U, UH, g.RUH3.data(), 3, DT);
@@ -1265,7 +2125,7 @@ int orc_getup(void *h, double *U, double *P, double *HH, double *SGSVIS, int NTI
     getdp(g, g.DP.data(), g.RDP.data());
     // UPCALC
     upcalc(g, U, P, UH, g.DP.data(), DT, PRESG, PRESG3, true);
-    return 0;
+    return status;
 }
 
 // Pressure projection of U (RHSDP + GETDP + UPCALC with UH = U, DT = 1, no bulk forcing);
@@ -1386,38 +2246,7 @@ void orc_chkmf(void *h, const double *U, double *flow1, double *flow3) {
 }
 
 // WALLSS (compact3d.f:11077-11143)
-void orc_wallss(void *h, const double *U, double *wsm) {
-    Orc &g = *(Orc *)h;
-    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
-    double W1 = 0.0, W2 = 0.0, W3 = 0.0;
-    const double *DY = g.DY.data();
-    double NXZ = 1.0 / (double)(N1M * N3M);
-    for (int K = 1; K <= N3M; K++) {
-        int KP = g.KPA[K];
-        for (int I = 1; I <= N1M; I++) {
-            int IP = g.IPA[I];
-            auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
-            double UHC = 0.5 * (u(I, 1, K, 1) + u(IP, 1, K, 1));
-            double UHW = 0.5 * (u(I, 0, K, 1) + u(IP, 0, K, 1));
-            double VHC = u(I, 2, K, 2);
-            double VHW = u(I, 1, K, 2);
-            double WHC = 0.5 * (u(I, 1, K, 3) + u(I, 1, KP, 3));
-            double WHW = 0.5 * (u(I, 0, K, 3) + u(I, 0, KP, 3));
-            double WSB1 = (UHC - UHW) / (DY[1] * 0.5);
-            double WSB2 = (VHC - VHW) / DY[1];
-            double WSB3 = (WHC - WHW) / (DY[1] * 0.5);
-            UHC = 0.5 * (u(I, N2M, K, 1) + u(IP, N2M, K, 1));
-            UHW = 0.5 * (u(I, N2, K, 1) + u(IP, N2, K, 1));
-            double WST1 = (UHC - UHW) / (DY[N2M] * 0.5);
-            W1 = W1 + WSB1 + WST1 * (g.ALY - 1.0);
-            W2 = W2 + WSB2 + WST1 * (g.ALY - 1.0);
-            W3 = W3 + WSB3 + WST1 * (g.ALY - 1.0);
-        }
-    }
-    wsm[0] = W1 * NXZ / g.RE / g.ALY;
-    wsm[1] = W2 * NXZ / g.RE / g.ALY;
-    wsm[2] = W3 * NXZ / g.RE / g.ALY;
-}
+void orc_wallss(void *h, const double *U, double *wsm) { wallss_common(*(Orc *)h, U, wsm); }
 
 // ---- unit-level entry points ----
 // CTDMA11 on one line with constant coefficients (a,b,c); d,x 0-based length n.

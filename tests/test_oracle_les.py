@@ -1,0 +1,232 @@
+"""Known-answer tests of the oracle's LES restatement (CPU only).
+
+The reference ships no tests for its SGS models or wall model, so the restatement of
+STRAIN (compact3d.f:5558-5689), SGSCS (1413-1488), SGSDY (1250-1400), FILTER
+(5190-5228), WALLMODEL_INSTANT (2319-2493) and the SGS fluxes of RHS1-3 is pinned by
+closed forms: linear shear, the law of the wall, invariances of the dynamic procedure and
+the modified wavenumbers of the compact operators for a constant eddy viscosity.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from compact3d_gb300 import ic
+from compact3d_gb300.grid import make_grid
+
+
+def _grid(name="les32cs", **over):
+    g, dt = make_grid(name, **over)
+    return g, dt
+
+
+def _xc(g):
+    return (np.arange(g.n1m) + 0.5) * g.alx / g.n1m
+
+
+def _xf(g):
+    return np.arange(g.n1m) * g.alx / g.n1m
+
+
+def _zf(g):
+    return np.arange(g.n3m) * g.alz / g.n3m
+
+
+def _yc(g):
+    Y = g.arrays["y"]
+    return 0.5 * (Y[1:g.n2m + 1] + Y[2:g.n2m + 2])
+
+
+def _ak(n, dxinv, m):
+    """(1,22,1) compact first derivative applied twice: modified wavenumber squared."""
+    th = 2 * math.pi * m / n
+    return 288.0 * dxinv ** 2 * (1 - math.cos(th)) / (11 + math.cos(th)) ** 2
+
+
+def test_sgscs_linear_shear_closed_form(oracle_mod):
+    """u = a*y (cell centres), v = w = 0: S12 = a/2 everywhere (the wall-model branch of
+    STRAIN included), |S| = a, and SGSCS gives C_s(J)^2 DXYZ^(2/3) a with the Van Driest
+    damping of y+ = (Y(J)+DY(J)/2) u_tau RE, u_tau = (WSM1^2+WSM3^2)^(1/4)."""
+    g, _ = _grid("les32cs")
+    o = oracle_mod.Oracle(g)
+    a = 0.37
+    U = g.zeros_u()
+    U[1:g.n1m + 1, 1:g.n2m + 1, 1:g.n3m + 1, 0] = a * _yc(g)[None, :, None]
+    wsm = np.array([4.1e-4, 0.0, 1.3e-4])
+    o.set_wsm(wsm)
+    S, smagc = o.sgs(U)
+    utau = math.sqrt(math.sqrt(wsm[0] ** 2 + wsm[2] ** 2))
+    Y, DY = g.arrays["y"], g.arrays["dy"]
+    for J in range(1, g.n2m + 1):
+        yp = (Y[J] + DY[J] * 0.5) * utau * g.re
+        cs = 0.1 * (1 - math.exp(-yp / 26.0))
+        assert smagc[J - 1] == pytest.approx(cs * cs, rel=1e-14)
+        dxyz = 1.0 / g.arrays["dx1"] * DY[J] / g.arrays["dx3"]
+        want = max(cs * cs * dxyz ** (2.0 / 3.0) * a, -1.0 / g.re)
+        got = S[1:g.n1m + 1, J, 1:g.n3m + 1]
+        np.testing.assert_allclose(got, want, rtol=1e-12)
+    # wall planes untouched (zero)
+    assert np.all(S[:, 0, :] == 0) and np.all(S[:, g.n2m + 1, :] == 0)
+
+
+def _smooth_field(g, seed=3):
+    U, P, HH = ic.loglaw(g, 2000.0, amp=0.2, seed=seed)
+    return U
+
+
+def test_sgsdy_galilean_and_scaling(oracle_mod):
+    """The dynamic coefficient is invariant to a uniform velocity shift (strain and
+    Leonard stress are differences) and to scaling of the field; the viscosity scales
+    with |S| where the clipping at -1/RE is inactive."""
+    g, _ = _grid("les32dy")
+    o = oracle_mod.Oracle(g)
+    U = _smooth_field(g)
+    S0, c0 = o.sgs(U)
+    U1 = U.copy(order="F")
+    U1[..., 0] += 0.3
+    U1[..., 2] -= 0.2
+    S1, c1 = o.sgs(U1)
+    np.testing.assert_allclose(c1, c0, rtol=1e-7, atol=1e-12)
+    U2 = (2.0 * U).copy(order="F")
+    S2, c2 = o.sgs(U2)
+    np.testing.assert_allclose(c2, c0, rtol=1e-10, atol=1e-14)
+    live = (S0 > -0.25 / g.re)
+    np.testing.assert_allclose(S2[live], 2.0 * S0[live], rtol=1e-10, atol=1e-18)
+    assert np.isfinite(S0).all() and np.any(S0 != 0)
+
+
+def test_sgsdy_shift_invariance(oracle_mod):
+    """FILTER and the plane sums of SGSDY commute with a periodic shift: moving the
+    field by one cell in x leaves every plane's dynamic coefficient unchanged."""
+    g, _ = _grid("les32dy")
+    o = oracle_mod.Oracle(g)
+    U = _smooth_field(g, seed=5)
+    S0, c0 = o.sgs(U)
+    Us = np.roll(U, 1, axis=0)
+    Us[0] = U[0]
+    Us[g.n1m + 1] = U[g.n1m + 1]
+    Us[1:g.n1m + 1] = np.roll(U[1:g.n1m + 1], 1, axis=0)
+    S1, c1 = o.sgs(np.asfortranarray(Us))
+    np.testing.assert_allclose(c1, c0, rtol=1e-10, atol=1e-14)
+
+
+def test_wallmodel_recovers_log_law(oracle_mod):
+    """u(I,3,K), w(I,3,K) on the log law for a known u_tau: TAUW1 = u_tau^2 (to the
+    Newton tolerance 1e-6 on u_tau), split along the velocity direction; WSM(1) is the
+    plane mean."""
+    g, _ = _grid("les32cs")
+    o = oracle_mod.Oracle(g)
+    DY = g.arrays["dy"]
+    deltap = DY[1] + DY[2] + DY[3] / 2.0
+    rng = np.random.default_rng(7)
+    ut = rng.uniform(0.01, 0.05, size=(g.n1m, g.n3m))
+    mag = ut * (np.log(ut * deltap * g.re) / 0.41 + 5.2)
+    ang = rng.uniform(-0.4, 0.4, size=(g.n1m, g.n3m))
+    U = g.zeros_u()
+    U[1:g.n1m + 1, 3, 1:g.n3m + 1, 0] = mag * np.cos(ang)
+    U[1:g.n1m + 1, 3, 1:g.n3m + 1, 2] = mag * np.sin(ang)
+    assert o.wallmodel(U) == 0
+    tw, tb, wsm = o.get_wall()
+    tau = np.hypot(tw[1:g.n1m + 1, 1:g.n3m + 1, 0], tb[1:g.n1m + 1, 1:g.n3m + 1, 0])
+    np.testing.assert_allclose(tau, ut ** 2, rtol=2e-4)
+    np.testing.assert_allclose(np.arctan2(tb[1:g.n1m + 1, 1:g.n3m + 1, 0], tw[1:g.n1m + 1, 1:g.n3m + 1, 0]),
+                               ang, atol=1e-12)
+    assert wsm[0] == pytest.approx(tau.mean(), rel=1e-12)
+    # the top-wall stresses are not modelled
+    assert np.all(tw[..., 1] == 0) and np.all(tb[..., 1] == 0)
+
+
+def test_wallmodel_iteration_cap_is_an_error(oracle_mod):
+    g, _ = _grid("les32cs")
+    o = oracle_mod.Oracle(g)
+    U = _smooth_field(g)
+    o.set_wall_iter_cap(2)
+    assert o.wallmodel(U) == -4
+
+
+def _const_nu(g, nu0):
+    S = g.zeros_s()
+    S[1:g.n1m + 1, 1:g.n2m + 1, 1:g.n3m + 1] = nu0
+    return S
+
+
+def test_sgs_flux_normal_terms_modified_wavenumber(oracle_mod):
+    """Constant eddy viscosity nu0, u = sin(m x) at x faces, v = cos(m' x) at cell
+    centres, w = sin(m'' z) at z faces, all uniform in y: the SGS fluxes are 2 nu0 k'^2 u,
+    nu0 k'^2 v and 2 nu0 k'^2 w with the (1,22,1) modified wavenumber squared
+    (compact3d.f:9211).  In the two wall cells of u the d/dy(nu dv/dx) flux through the
+    wall face is absent (zero wall viscosity), so u is compared inside them."""
+    g, _ = _grid("les32cs")
+    o = oracle_mod.Oracle(g)
+    nu0 = 3.0e-3
+    m1, m2, m3 = 3, 5, 2
+    U = g.zeros_u()
+    U[1:g.n1m + 1, :, 1:g.n3m + 1, 0] = np.sin(2 * math.pi * m1 * _xf(g) / g.alx)[:, None, None]
+    U[1:g.n1m + 1, :, 1:g.n3m + 1, 1] = np.cos(2 * math.pi * m2 * _xc(g) / g.alx)[:, None, None]
+    U[1:g.n1m + 1, :, 1:g.n3m + 1, 2] = np.sin(2 * math.pi * m3 * _zf(g) / g.alz)[None, None, :]
+    HH = o.sgs_rhs(U, _const_nu(g, nu0))
+    dx1, dx3 = g.arrays["dx1"], g.arrays["dx3"]
+    slu = (slice(1, g.n1m + 1), slice(2, g.n2m), slice(1, g.n3m + 1))
+    np.testing.assert_allclose(HH[slu + (0,)], 2 * nu0 * _ak(g.n1m, dx1, m1) * U[slu + (0,)], atol=1e-13)
+    sl = (slice(1, g.n1m + 1), slice(1, g.n2m + 1), slice(1, g.n3m + 1))
+    slv = (slice(1, g.n1m + 1), slice(2, g.n2m + 1), slice(1, g.n3m + 1))
+    np.testing.assert_allclose(HH[slv + (1,)], nu0 * _ak(g.n1m, dx1, m2) * U[slv + (1,)], atol=1e-13)
+    np.testing.assert_allclose(HH[sl + (2,)], 2 * nu0 * _ak(g.n3m, dx3, m3) * U[sl + (2,)], atol=1e-13)
+
+
+def test_sgs_flux_wall_normal_terms_fd(oracle_mod):
+    """Constant nu0 inside, zero on the wall planes; u = f(y), v = h(y), w = q(y): the
+    fluxes are the second-order FD forms of d/dy(nu du/dy) (zero flux through the walls)
+    and 2 d/dy(nu dv/dy)."""
+    g, _ = _grid("les32cs")
+    o = oracle_mod.Oracle(g)
+    nu0 = 2.0e-3
+    Y, DY = g.arrays["y"], g.arrays["dy"]
+    H = np.concatenate([[0.0], g.arrays["h"]])   # H(1..N2) at index J
+    yc = _yc(g)
+    f = np.sin(1.3 * yc) + 0.2 * yc ** 2
+    q = np.cos(0.7 * yc)
+    yf = Y[1:g.n2m + 2]
+    hv = np.sin(math.pi * yf / Y[g.n2m + 1]) * (1 + 0.3 * yf)
+    U = g.zeros_u()
+    U[1:g.n1m + 1, 1:g.n2m + 1, 1:g.n3m + 1, 0] = f[None, :, None]
+    U[1:g.n1m + 1, 1:g.n2m + 2, 1:g.n3m + 1, 1] = hv[None, :, None]
+    U[1:g.n1m + 1, 1:g.n2m + 1, 1:g.n3m + 1, 2] = q[None, :, None]
+    HH = o.sgs_rhs(U, _const_nu(g, nu0))
+    n2m = g.n2m
+    for comp, prof in ((0, f), (2, q)):
+        ext = np.concatenate([[0.0], prof, [0.0]])   # ghosts J=0, N2 are zero in U
+        for J in range(1, n2m + 1):
+            up = (ext[J + 1] - ext[J]) / H[J + 1] if J < n2m else 0.0
+            dn = (ext[J] - ext[J - 1]) / H[J] if J > 1 else 0.0
+            nup = nu0 if J < n2m else 0.0
+            nud = nu0 if J > 1 else 0.0
+            want = -(1.0 / DY[J]) * (nup * up - nud * dn)
+            np.testing.assert_allclose(HH[1:g.n1m + 1, J, 1:g.n3m + 1, comp], want, rtol=1e-11, atol=1e-15)
+    for J in range(2, n2m + 1):
+        v2 = (hv[J] - hv[J - 1]) / DY[J]
+        v1 = (hv[J - 1] - hv[J - 2]) / DY[J - 1]
+        want = -2.0 * (1.0 / H[J]) * (nu0 * v2 - nu0 * v1)
+        np.testing.assert_allclose(HH[1:g.n1m + 1, J, 1:g.n3m + 1, 1], want, rtol=1e-11, atol=1e-15)
+
+
+def test_les_step_runs_and_conserves(oracle_mod):
+    """A few GETUP steps of both LES models with the wall model: the field stays
+    discretely divergence-free and finite, the flow rate is held, and the wall stress is
+    near the log-law value of the start."""
+    for name in ("les32cs", "les32dy"):
+        g, dt = _grid(name)
+        o = oracle_mod.Oracle(g)
+        U, P, HH = ic.loglaw(g, 2000.0)
+        o.project(U)
+        f0 = o.chkmf(U)[0]
+        S = g.zeros_s()
+        pg = pg3 = 0.0
+        for n in range(1, 4):
+            pg, pg3 = o.getup(U, P, HH, n, dt, pg, pg3, S)
+        assert np.isfinite(U).all() and np.isfinite(S).all()
+        assert o.divcheck(U) < 1e-12
+        assert o.chkmf(U)[0] == pytest.approx(f0, rel=1e-10)
+        tw, tb, wsm = o.get_wall()
+        utau = math.sqrt(wsm[0])
+        assert 1500 < utau * g.re < 2600
