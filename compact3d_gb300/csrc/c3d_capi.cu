@@ -157,7 +157,9 @@ void free_channel(c3d_channel *ch) {
                     ch->tw64, ch->tw32, ch->hh[0][0], ch->hh[0][1],
                     ch->hh[0][2], ch->hh[1][0], ch->hh[1][1], ch->hh[1][2], ch->r[0], ch->r[1],
                     ch->r[2], ch->exy, ch->exz, ch->eyz, ch->ww1, ch->wsq, ch->rdpz, ch->g1,
-                    ch->spec, ch->stage, ch->tauw, ch->taub};
+                    ch->spec, ch->stage, ch->tauw, ch->taub, ch->les[0], ch->les[1], ch->les[2],
+                    ch->les[3], ch->les[4], ch->les[5], ch->les[6], ch->les[7], ch->dyn, ch->smagc,
+                    ch->d23, ch->ycs, ch->wpart, ch->coef, ch->d23r};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (ch->pinned) cudaFreeHost(ch->pinned);
@@ -279,8 +281,16 @@ int check_grid(const c3d_grid *g) {
         set_error("precision must be C3D_FP64 or C3D_MIXED");
         return C3D_EINVAL;
     }
-    if (g->files != 0 || g->wmodel != 0) {
-        set_error("SGS models and wall models are not available in this build (FILES=0, WMODEL=0 only)");
+    if (g->files < 0 || g->files > 2) {
+        set_error("FILES must be 0 (DNS), 1 (SGSDY) or 2 (SGSCS); the scale-dependent model (3) is not built");
+        return C3D_EINVAL;
+    }
+    if (g->wmodel < 0 || g->wmodel > 1) {
+        set_error("WMODEL must be 0 or 1 (WALLMODEL_INSTANT); the other wall models are not built");
+        return C3D_EINVAL;
+    }
+    if (g->wmodel == 1 && g->y[0] != 0.0) {
+        set_error("Y(0) = Y0 != 0 selects WALLMODEL_ROUGH, which is not built");
         return C3D_EINVAL;
     }
     return 0;
@@ -363,6 +373,44 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
         cudaMemset(*q, 0, nf * rs);
     }
     if (cudaMalloc(&ch->spec, nmodes * g.n2m * 2 * rs) != cudaSuccess) return fail(C3D_ENOMEM);
+    // wall stresses (any FILES/WMODEL: c3d_upload_wall may set them) and the LES fields
+    ch->files = gr->files;
+    ch->wmodel = gr->wmodel;
+    ch->wall_cap = 10000;
+    if (dalloc(&ch->tauw, 2 * (size_t)g.np) || dalloc(&ch->taub, 2 * (size_t)g.np)) return fail(C3D_ENOMEM);
+    cudaMemset(ch->tauw, 0, 2 * (size_t)g.np * 8);
+    cudaMemset(ch->taub, 0, 2 * (size_t)g.np * 8);
+    if (ch->files != 0) {
+        for (int q = 0; q < 8; ++q) {
+            if (cudaMalloc(&ch->les[q], nf * rs) != cudaSuccess) { set_error("cudaMalloc LES"); return fail(C3D_ENOMEM); }
+            cudaMemset(ch->les[q], 0, nf * rs);
+        }
+        if (ch->files == 1 && cudaMalloc(&ch->dyn, 21 * (size_t)g.n2m * g.np * rs) != cudaSuccess)
+            return fail(C3D_ENOMEM);
+        const int nbw = (g.np + 127) / 128;   // blocks of k_wall (TPB = 128 threads)
+        if (dalloc(&ch->smagc, (size_t)g.n2 + 1) || dalloc(&ch->d23, (size_t)g.n2 + 1) ||
+            dalloc(&ch->ycs, (size_t)g.n2 + 1) || dalloc(&ch->wpart, 2 * (size_t)nbw))
+            return fail(C3D_ENOMEM);
+        if (cudaMalloc(&ch->coef, ((size_t)g.n2 + 1) * rs) != cudaSuccess ||
+            cudaMalloc(&ch->d23r, ((size_t)g.n2 + 1) * rs) != cudaSuccess)
+            return fail(C3D_ENOMEM);
+        cudaMemset(ch->smagc, 0, ((size_t)g.n2 + 1) * 8);
+        // DXYZ^(2/3) and the Van Driest height per plane (SGSCS/SGSDY, compact3d.f:1283, 1469)
+        std::vector<double> d23(g.n2 + 1, 0.0), ycs(g.n2 + 1, 0.0);
+        for (int j = 1; j <= g.n2m; ++j) {
+            const double dxyz = 1.0 / gr->dx1 * gr->dy[j] / gr->dx3;
+            d23[j] = pow(dxyz, 2. / 3.);
+            ycs[j] = gr->y[j] + gr->dy[j] * 0.5;
+        }
+        cudaMemcpy(ch->d23, d23.data(), d23.size() * 8, cudaMemcpyHostToDevice);
+        cudaMemcpy(ch->ycs, ycs.data(), ycs.size() * 8, cudaMemcpyHostToDevice);
+        if (ch->precision == C3D_MIXED) {
+            std::vector<float> f(d23.begin(), d23.end());
+            cudaMemcpy(ch->d23r, f.data(), f.size() * 4, cudaMemcpyHostToDevice);
+        } else {
+            cudaMemcpy(ch->d23r, d23.data(), d23.size() * 8, cudaMemcpyHostToDevice);
+        }
+    }
     ch->stage_elems = (size_t)(gr->n1 + 1) * (gr->n2 + 1) * (gr->n3 + 1);
     if (dalloc(&ch->stage, ch->stage_elems)) return fail(C3D_ENOMEM);
     cudaMemset(ch->u, 0, nf * 8);
@@ -489,7 +537,9 @@ static int d2h(c3d_channel *ch, double *dst, size_t n) {
 
 int c3d_upload(c3d_channel *ch, const double *u, const double *p, const double *hh, const double *sgsvis) {
     if (!ch) { set_error("null channel"); return C3D_EINVAL; }
-    if (sgsvis) { set_error("SGSVIS is not used when FILES=0; pass NULL"); return C3D_EINVAL; }
+    if (sgsvis && ch->files == 0) { set_error("SGSVIS is not used when FILES=0; pass NULL"); return C3D_EINVAL; }
+    // With an SGS model, GETUP zeroes SGSVIS and recomputes it every step
+    // (compact3d.f:912-933), so an uploaded SGSVIS has no effect and is not copied.
     cudaSetDevice(ch->device);
     const size_t n3 = ch->stage_elems;   // one component of U / HH
     const Geo &g = ch->g;
@@ -521,7 +571,7 @@ int c3d_upload(c3d_channel *ch, const double *u, const double *p, const double *
 
 int c3d_download(c3d_channel *ch, double *u, double *p, double *hh, double *sgsvis) {
     if (!ch) { set_error("null channel"); return C3D_EINVAL; }
-    (void)sgsvis;
+    if (sgsvis && ch->files == 0) { set_error("SGSVIS exists only with an SGS model (FILES != 0)"); return C3D_EINVAL; }
     cudaSetDevice(ch->device);
     const size_t n3 = ch->stage_elems;
     const Geo &g = ch->g;
@@ -545,6 +595,11 @@ int c3d_download(c3d_channel *ch, double *u, double *p, double *hh, double *sgsv
             if (rc) return rc;
         }
     }
+    if (sgsvis) {
+        launch_repack(ch, 1, 3, 0);
+        int rc = d2h(ch, sgsvis, n3);
+        if (rc) return rc;
+    }
     CK(cudaGetLastError());
     return 0;
 }
@@ -561,16 +616,76 @@ int c3d_host_unregister(void *ptr) {
     return 0;
 }
 
+// TAUW/TAUB(0:M1,0:M3,2): interior I = 1..N1M, K = 1..N3M of both walls move.
+static int wall_copy(c3d_channel *ch, double *host, double *dev, bool up) {
+    const Geo &g = ch->g;
+    const long long N1 = g.n1m + 1, N3 = g.n3m + 1;
+    std::vector<double> plane(2 * (size_t)g.np);
+    if (up) {
+        for (int w = 0; w < 2; ++w)
+            for (int k = 0; k < g.n3m; ++k)
+                for (int i = 0; i < g.n1m; ++i)
+                    plane[(size_t)w * g.np + (size_t)k * g.n1m + i] = host[(i + 1) + (N1 + 1) * ((k + 1) + (N3 + 1) * w)];
+        CK(cudaMemcpy(dev, plane.data(), plane.size() * 8, cudaMemcpyHostToDevice));
+    } else {
+        CK(cudaMemcpy(plane.data(), dev, plane.size() * 8, cudaMemcpyDeviceToHost));
+        for (int w = 0; w < 2; ++w)
+            for (int k = 0; k < g.n3m; ++k)
+                for (int i = 0; i < g.n1m; ++i)
+                    host[(i + 1) + (N1 + 1) * ((k + 1) + (N3 + 1) * w)] = plane[(size_t)w * g.np + (size_t)k * g.n1m + i];
+    }
+    return 0;
+}
+
 int c3d_upload_wall(c3d_channel *ch, const double *tauw, const double *taub) {
-    (void)tauw;
-    (void)taub;
-    if (!ch) return C3D_EINVAL;
-    set_error("wall models are not available in this build");
-    return C3D_EINVAL;
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    CK(cudaStreamSynchronize(ch->stream));
+    int rc = 0;
+    if (tauw && (rc = wall_copy(ch, const_cast<double *>(tauw), ch->tauw, true))) return rc;
+    if (taub && (rc = wall_copy(ch, const_cast<double *>(taub), ch->taub, true))) return rc;
+    return 0;
 }
 
 int c3d_download_wall(c3d_channel *ch, double *tauw, double *taub) {
-    return c3d_upload_wall(ch, tauw, taub);
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    CK(cudaStreamSynchronize(ch->stream));
+    int rc = 0;
+    if (tauw && (rc = wall_copy(ch, tauw, ch->tauw, false))) return rc;
+    if (taub && (rc = wall_copy(ch, taub, ch->taub, false))) return rc;
+    return 0;
+}
+
+int c3d_set_wsm(c3d_channel *ch, const double *wsm) {
+    if (!ch || !wsm) { set_error("null argument"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    CK(cudaMemcpyAsync(ch->scal + SCAL_WSMC, wsm, 3 * sizeof(double), cudaMemcpyHostToDevice, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    return 0;
+}
+
+int c3d_get_wsm(c3d_channel *ch, double *wsm) {
+    if (!ch || !wsm) { set_error("null argument"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    CK(cudaMemcpyAsync(wsm, ch->scal + SCAL_WSMC, 3 * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    return 0;
+}
+
+int c3d_set_wall_iter_cap(c3d_channel *ch, int cap) {
+    if (!ch || cap < 1) { set_error("null channel or cap < 1"); return C3D_EINVAL; }
+    ch->wall_cap = cap;
+    return 0;
+}
+
+// After a completed step: the wall model's non-convergence flag (WMODEL = 1 with an SGS model).
+static int check_wall_flag(c3d_channel *ch, const double *scal_host) {
+    if (ch->files != 0 && ch->wmodel == 1 && scal_host[SCAL_WALLERR] != 0.0) {
+        set_error("wall model: the Newton iteration for u_tau did not converge within the iteration cap");
+        return C3D_ENOTCONV;
+    }
+    return 0;
 }
 
 static int step_common(c3d_channel *ch, double dt, double *presg, double *presg3, bool sync) {
@@ -595,13 +710,15 @@ static int step_common(c3d_channel *ch, double dt, double *presg, double *presg3
         if (rc) return rc;
     }
     if (sync) {
-        CK(cudaMemcpyAsync(pg, ch->scal + SCAL_PRESG, 2 * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
+        double sc[SCAL_COUNT];
+        CK(cudaMemcpyAsync(sc, ch->scal, sizeof(sc), cudaMemcpyDeviceToHost, ch->stream));
         CK(cudaStreamSynchronize(ch->stream));
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ch->ev0, ch->ev1);
         ch->last_ms = ms;
-        if (presg) *presg = pg[0];
-        if (presg3) *presg3 = pg[1];
+        if (presg) *presg = sc[SCAL_PRESG];
+        if (presg3) *presg3 = sc[SCAL_PRESG3];
+        return check_wall_flag(ch, sc);
     }
     return 0;
 }
@@ -726,12 +843,17 @@ int c3d_getup(c3d_channel *ch, double *u, double *p, double *hh, double *sgsvis,
     if (rc) return rc;
     rc = c3d_step(ch, ntime, dt, presg, presg3);
     if (rc) return rc;
-    return c3d_download(ch, u, p, hh, nullptr);
+    return c3d_download(ch, u, p, hh, ch->files != 0 ? sgsvis : nullptr);
 }
 
 int c3d_sync(c3d_channel *ch) {
     if (!ch) return C3D_EINVAL;
     CK(cudaStreamSynchronize(ch->stream));
+    if (ch->files != 0 && ch->wmodel == 1) {
+        double sc[SCAL_COUNT];
+        CK(cudaMemcpy(sc, ch->scal, sizeof(sc), cudaMemcpyDeviceToHost));
+        return check_wall_flag(ch, sc);
+    }
     return 0;
 }
 

@@ -78,7 +78,32 @@ enum {
     SCAL_FLOW3 = 7,
     SCAL_WSM = 8,      // 3 values
     SCAL_NONFIN = 11,
+    SCAL_WSMC = 12,    // 3 values: /WSMEM/ WSM as the SGS model and the wall model see it
+    SCAL_WALLERR = 15, // 1 when a wall point's Newton iteration hit its cap in the last step
     SCAL_COUNT = 16
+};
+
+// Arguments of the LES kernels (FILES != 0): fields in the working precision R, plane
+// layout like the state; face quantities are stored at the index of their Fortran owner.
+template <typename R>
+struct LesArgs {
+    R *nu;            // SGSVIS at the cell centres (wall planes j = 0, N2 stay zero)
+    R *nux, *nuz;     // nu interpolated to the x faces / z faces (1,6,1)
+    R *t13;           // tau13 = Ix(Iz(nu)) (du/dz + dw/dx) at (x face, z face)
+    R *nuwz;          // nu * Dz(w) at the cell centres
+    R *dvdx, *dvdz;   // Dx(v), Dz(v) at the v faces (J >= 2; J = 1, N2 stay zero)
+    R *dwdx;          // Dx(w) at (x face, z face)
+    R *dyn;           // SGSDY: 21 raw fields of N2M planes
+    double *smagc;    // SMAGC(J), n2+1
+    R *coef;          // SMAGC(J) * DXYZ^(2/3) in R (SGSCS)
+    const double *d23;   // DXYZ^(2/3) per J
+    const R *d23r;       // the same in R
+    const double *ycs;   // Y(J) + DY(J)/2 per J
+    double *tauw, *taub; // wall stresses [w][k][i], w = 0 bottom, 1 top
+    double *wpart;       // wall-model per-block partial sums
+    int files, wmodel, wall_cap;
+    double ifwall;
+    R reninv, dx1, dx3;
 };
 
 }  // namespace c3d
@@ -118,8 +143,14 @@ struct c3d_channel {
     int nsm;                  // streaming multiprocessors of the device
     c3d::FftPlan fx, fz;
     std::vector<double> ak1, ak3, pcj, ppj, pmjh;
-    // wall model
+    // LES (FILES != 0): SGS model, wall model and SGS-flux work fields
+    int files, wmodel;
     double *tauw, *taub;      // (N1M*N3M*2) device, plane layout [w][k][i]
+    void *les[8];             // nu, nux, nuz, t13, nuwz, dvdx, dwdx, dvdz (R, full fields)
+    void *dyn;                // SGSDY raw quantities (21 x N2M planes, R)
+    double *smagc, *d23, *ycs, *wpart;
+    void *coef, *d23r;        // per-J tables in R
+    int wall_cap;
     // per-kernel profiler (CUDA events around every launch when enabled)
     int prof_on;
     int prof_n;                              // events recorded in the current step
@@ -142,6 +173,9 @@ template <typename R>
 int launch_spec(c3d_channel *ch, StepArgs<R> &a, int which, int *nl);   // 0=fwd z FFT 1=poisson 2=inv z FFT
 template <typename R>
 void set_spec_smem(c3d_channel *ch);
+// LES stages (c3d_les.cu): 0 = WALLSS/SGS model/wall model before BCOND, 1 = SGS fluxes.
+template <typename R>
+int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *nl);
 // Step drivers (c3d_step.cu)
 int launch_step(c3d_channel *ch, double dt, int *launches);
 int launch_project(c3d_channel *ch, int *launches);

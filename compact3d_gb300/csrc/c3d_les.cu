@@ -1,0 +1,762 @@
+// c3d_les.cu -- wall-modelled LES on the GPU: the SGS models, the wall model and the SGS
+// fluxes of the momentum right-hand sides (FILES != 0, compact3d.f:931-937).
+//
+//   les_wallss  WALLSS (11077-11143) of the current field into /WSMEM/ WSM, which the
+//               driver computes right before GETUP when WMODEL = 0 (compact3d.f:125)
+//   sgs_coef    SGSCS's plane coefficient SMAGC(J) DXYZ^(2/3) (1413-1488)
+//   sgs_cs      SGSCS: nu = max(coef |S|, -1/RE) with |S| from STRAIN (5558-5689)
+//   sgs_raw     SGSDY (1250-1400): per point S_ij, |S|, DELTA^2 |S| S_ij, the cell-centre
+//               velocities and their products
+//   sgs_dyn     SGSDY: FILTER (5190-5228) of those, M_ij, L_ij, the plane sums, SMAGC(J)
+//               and nu, one block per plane
+//   wall        WALLMODEL_INSTANT (2319-2493): damped Newton for u_tau per wall point
+//   wall_sum    WSM(1) = plane mean of TAUW1; non-converged points -> error flag
+//   les_x1/z1/z2/x2   the SGS fluxes of RHS1/2/3 (6436-6770, 6857-6866, 7088-7393,
+//               7774-8111) and the wall-stress terms (6765-6770, 8095-8101)
+//
+// The reference solves each SGS flux separately (36 compact line solves per step).  The
+// sums of fluxes that share an edge viscosity are linear in it, so the kernels form the
+// edge stresses once and take one derivative of each:
+//   tau13 = Ix(Iz(nu)) (du/dz + dw/dx) at (x face, z face): RHS1 -= Dz(tau13), RHS3 -= Dx(tau13)
+//   tau12 = <Ix(nu)>_y (du/dy + dv/dx) at (x face, y face):  RHS2 -= Dx(tau12), RHS1 -= d/dy
+//   tau23 = <Iz(nu)>_y (dw/dy + dv/dz) at (y face, z face):  RHS2 -= Dz(tau23), RHS3 -= d/dy
+// plus the normal stresses 2 Dx(nu Dx u), 2 d/dy(nu dv/dy), 2 Dz(nu Dz w): 15 solves.  The
+// results equal the reference's to rounding.  In the mixed form every difference of the
+// state is taken cancellation-free, the strain is formed from values relative to the
+// point's own velocity and the Leonard stress from values relative to a per-plane
+// constant (the dynamic procedure is Galilean invariant), so FP32 keeps its relative
+// accuracy; plane sums, the coefficient and the wall model run in FP64.
+#include "c3d_kern.cuh"
+
+namespace c3d {
+
+__device__ __forceinline__ int wrapm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
+__device__ __forceinline__ int wrapp(int i, int n) { return i + 1 == n ? 0 : i + 1; }
+
+// ---------------------------------------------------------------------------------
+// STRAIN at the cell centre (i, j, k): SR = S11, S12, S13, S22, S23, S33.  Velocities are
+// taken relative to (u, v, w) at (i, j, k) (differences are exact in exact arithmetic:
+// every quantity below is a difference of averages with unit weight sums).
+// ---------------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void strain_at(const StepArgs<R> &a, const LesArgs<R> &l, int i, int j, int k,
+                                          R (&sr)[6]) {
+    typedef typename SType<R>::S S;
+    typedef St<R> ST;
+    const Geo &g = a.g;
+    const int n1 = g.n1m, n3 = g.n3m, N2 = g.n2;
+    const int ip = wrapp(i, n1), im = wrapm(i, n1), kp = wrapp(k, n3), km = wrapm(k, n3);
+    const int jp = j + 1, jm = j - 1;
+    const S cu = a.u[fidx(g, i, j, k)], cv = a.v[fidx(g, i, j, k)], cw = a.w[fidx(g, i, j, k)];
+    auto du = [&](int ii, int jj, int kk) { return ST::d(a.u[fidx(g, ii, jj, kk)], cu); };
+    auto dv = [&](int ii, int jj, int kk) { return ST::d(a.v[fidx(g, ii, jj, kk)], cv); };
+    auto dw = [&](int ii, int jj, int kk) { return ST::d(a.w[fidx(g, ii, jj, kk)], cw); };
+    const bool fjum = (j != 1), fjup = (j != g.n2m);
+    const R half = (R)0.5, DX1 = l.dx1, DX3 = l.dx3;
+    const R rdy = a.m.rdy[j];
+    sr[0] = DX1 * du(ip, j, k);                                   // (U(IP)-U(I))
+    {
+        R UJP = half * (du(i, jp, k) + du(ip, jp, k));
+        R UJC = half * (R(0) + du(ip, j, k));
+        R UJM = half * (du(i, jm, k) + du(ip, jm, k));
+        R U2, U1;
+        if (!l.wmodel) {
+            U2 = fjup ? a.m.rh[jp] * (a.m.hdy[j] * UJP + a.m.hdy[jp] * UJC) : half * (du(i, N2, k) + du(ip, N2, k));
+            U1 = fjum ? a.m.rh[j] * (a.m.hdy[j] * UJM + a.m.hdy[jm] * UJC) : half * (du(i, 0, k) + du(ip, 0, k));
+        } else {
+            U2 = fjup ? a.m.rh[jp] * (a.m.hdy[j] * UJP + a.m.hdy[jp] * UJC) : UJC;
+            U1 = fjum ? a.m.rh[j] * (a.m.hdy[j] * UJM + a.m.hdy[jm] * UJC) : UJC;
+        }
+        R VIP = half * (dv(ip, j, k) + dv(ip, jp, k));
+        R VIC = half * (R(0) + dv(i, jp, k));
+        R VIM = half * (dv(im, j, k) + dv(im, jp, k));
+        R V2 = half * (VIP + VIC), V1 = half * (VIM + VIC);
+        const R fy = (l.wmodel && (!fjum || !fjup)) ? (R)2.0 * rdy : rdy;
+        sr[1] = half * (DX1 * (V2 - V1) + fy * (U2 - U1));
+    }
+    {
+        R UKP = half * (du(i, j, kp) + du(ip, j, kp));
+        R UKC = half * (R(0) + du(ip, j, k));
+        R UKM = half * (du(i, j, km) + du(ip, j, km));
+        R U2 = half * (UKP + UKC), U1 = half * (UKM + UKC);
+        R WIP = half * (dw(ip, j, k) + dw(ip, j, kp));
+        R WIC = half * (R(0) + dw(i, j, kp));
+        R WIM = half * (dw(im, j, k) + dw(im, j, kp));
+        R W2 = half * (WIP + WIC), W1 = half * (WIM + WIC);
+        sr[2] = half * (DX1 * (W2 - W1) + DX3 * (U2 - U1));
+    }
+    sr[3] = rdy * dv(i, jp, k);                                    // (V(JP)-V(J))/DY
+    {
+        R WJP = half * (dw(i, jp, k) + dw(i, jp, kp));
+        R WJC = half * (R(0) + dw(i, j, kp));
+        R WJM = half * (dw(i, jm, k) + dw(i, jm, kp));
+        R W2, W1;
+        if (!l.wmodel) {
+            W2 = fjup ? a.m.rh[jp] * (a.m.hdy[j] * WJP + a.m.hdy[jp] * WJC) : half * (dw(i, N2, k) + dw(i, N2, kp));
+            W1 = fjum ? a.m.rh[j] * (a.m.hdy[j] * WJM + a.m.hdy[jm] * WJC) : half * (dw(i, 0, k) + dw(i, 0, kp));
+        } else {
+            W2 = fjup ? a.m.rh[jp] * (a.m.hdy[j] * WJP + a.m.hdy[jp] * WJC) : WJC;
+            W1 = fjum ? a.m.rh[j] * (a.m.hdy[j] * WJM + a.m.hdy[jm] * WJC) : WJC;
+        }
+        R VKP = half * (dv(i, j, kp) + dv(i, jp, kp));
+        R VKC = half * (R(0) + dv(i, jp, k));
+        R VKM = half * (dv(i, j, km) + dv(i, jp, km));
+        R V2 = half * (VKP + VKC), V1 = half * (VKM + VKC);
+        const R fy = (l.wmodel && (!fjum || !fjup)) ? (R)2.0 * rdy : rdy;
+        sr[4] = half * (fy * (W2 - W1) + DX3 * (V2 - V1));
+    }
+    sr[5] = DX3 * dw(i, j, kp);                                    // (W(KP)-W(K))
+}
+
+template <typename R>
+__device__ __forceinline__ R sumsq6(const R (&s)[6]) {
+    return (R)2.0 * s[1] * s[1] + s[0] * s[0] + (R)2.0 * s[2] * s[2] + s[3] * s[3] + (R)2.0 * s[4] * s[4] +
+           s[5] * s[5];
+}
+
+// WALLSS into WSM (the SGSCS input): one block, FP64, fixed order.
+template <typename R>
+__global__ void k_les_wallss(StepArgs<R> a) {
+    typedef St<R> ST;
+    const Geo g = a.g;
+    __shared__ double sh[3][256];
+    double w1 = 0.0, w2 = 0.0, w3 = 0.0;
+    const int n1 = g.n1m, n3 = g.n3m, N2 = g.n2, N2M = g.n2m;
+    const double rdy1 = 1.0 / (g.dy[1] * 0.5), rdyv = 1.0 / g.dy[1], rdyt = 1.0 / (g.dy[N2M] * 0.5);
+    for (int e = threadIdx.x; e < n1 * n3; e += blockDim.x) {
+        const int i = e % n1, k = e / n1, ip = wrapp(i, n1), kp = wrapp(k, n3);
+        auto U = [&](const typename SType<R>::S *f, int ii, int jj, int kk) { return ST::dbl(f[fidx(g, ii, jj, kk)]); };
+        double uhc = 0.5 * (U(a.u, i, 1, k) + U(a.u, ip, 1, k)), uhw = 0.5 * (U(a.u, i, 0, k) + U(a.u, ip, 0, k));
+        double vhc = U(a.v, i, 2, k), vhw = U(a.v, i, 1, k);
+        double whc = 0.5 * (U(a.w, i, 1, k) + U(a.w, i, 1, kp)), whw = 0.5 * (U(a.w, i, 0, k) + U(a.w, i, 0, kp));
+        double b1 = (uhc - uhw) * rdy1, b2 = (vhc - vhw) * rdyv, b3 = (whc - whw) * rdy1;
+        double tc = 0.5 * (U(a.u, i, N2M, k) + U(a.u, ip, N2M, k)), tw = 0.5 * (U(a.u, i, N2, k) + U(a.u, ip, N2, k));
+        double t1 = (tc - tw) * rdyt * (g.aly - 1.0);
+        w1 += b1 + t1;
+        w2 += b2 + t1;
+        w3 += b3 + t1;
+    }
+    sh[0][threadIdx.x] = w1;
+    sh[1][threadIdx.x] = w2;
+    sh[2][threadIdx.x] = w3;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double nxz = 1.0 / (double)(n1 * n3);
+        for (int c = 0; c < 3; ++c) a.scal[SCAL_WSMC + c] = sh[c][0] * nxz / g.re / g.aly;
+    }
+}
+
+// SGSCS's plane coefficients from WSM: SMAGC(J) = (0.1 (1 - exp(-y+/26)))^2.
+template <typename R>
+__global__ void k_sgs_coef(StepArgs<R> a, LesArgs<R> l) {
+    const Geo g = a.g;
+    const double w1 = a.scal[SCAL_WSMC], w3 = a.scal[SCAL_WSMC + 2];
+    const double utau = sqrt(sqrt(w1 * w1 + w3 * w3));
+    for (int j = 1 + threadIdx.x; j <= g.n2m; j += blockDim.x) {
+        const double yp = l.ycs[j] * utau * g.re;
+        double cs = 0.1 * (1.0 - exp(-yp / 26.0));
+        const double sm = cs * cs;
+        l.smagc[j] = sm;
+        l.coef[j] = (R)(sm * l.d23[j]);
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_sgs_cs(StepArgs<R> a, LesArgs<R> l) {
+    const Geo g = a.g;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (long long)g.n2m * g.np) return;
+    const int i = (int)(tid % g.n1m), k = (int)((tid / g.n1m) % g.n3m), j = 1 + (int)(tid / g.np);
+    R sr[6];
+    strain_at(a, l, i, j, k, sr);
+    const R abss = sqrt((R)2.0 * sumsq6(sr));
+    const R t = l.coef[j] * abss;
+    l.nu[fidx(g, i, j, k)] = t > -l.reninv ? t : -l.reninv;
+}
+
+// SGSDY raw quantities: q[0..5] S_ij, q[6..11] DELTA^2|S| S_ij, q[12..14] cell-centre
+// velocities (relative to the plane's velocity at (0, j, 0)), q[15..20] their products.
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_sgs_raw(StepArgs<R> a, LesArgs<R> l) {
+    typedef St<R> ST;
+    const Geo g = a.g;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (long long)g.n2m * g.np) return;
+    const int i = (int)(tid % g.n1m), k = (int)((tid / g.n1m) % g.n3m), j = 1 + (int)(tid / g.np);
+    R sr[6];
+    strain_at(a, l, i, j, k, sr);
+    const R abss = sqrt((R)2.0 * sumsq6(sr));
+    l.nu[fidx(g, i, j, k)] = abss;
+    const long long fs = (long long)g.n2m * g.np, q0 = tid;
+    const R delabs = l.d23r[j] * abss;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        l.dyn[c * fs + q0] = sr[c];
+        l.dyn[(6 + c) * fs + q0] = delabs * sr[c];
+    }
+    const int ip = wrapp(i, g.n1m), kp = wrapp(k, g.n3m);
+    const auto cu = a.u[fidx(g, 0, j, 0)], cv = a.v[fidx(g, 0, j, 0)], cw = a.w[fidx(g, 0, j, 0)];
+    const R half = (R)0.5;
+    const R u1 = (ST::d(a.u[fidx(g, i, j, k)], cu) + ST::d(a.u[fidx(g, ip, j, k)], cu)) * half;
+    const R u2 = (ST::d(a.v[fidx(g, i, j, k)], cv) + ST::d(a.v[fidx(g, i, j + 1, k)], cv)) * half;
+    const R u3 = (ST::d(a.w[fidx(g, i, j, k)], cw) + ST::d(a.w[fidx(g, i, j, kp)], cw)) * half;
+    l.dyn[12 * fs + q0] = u1;
+    l.dyn[13 * fs + q0] = u2;
+    l.dyn[14 * fs + q0] = u3;
+    l.dyn[15 * fs + q0] = u1 * u1;
+    l.dyn[16 * fs + q0] = u1 * u2;
+    l.dyn[17 * fs + q0] = u1 * u3;
+    l.dyn[18 * fs + q0] = u2 * u2;
+    l.dyn[19 * fs + q0] = u2 * u3;
+    l.dyn[20 * fs + q0] = u3 * u3;
+}
+
+// FILTER of one raw quantity at (i, k): Simpson (1,4,1)/6 along x, then along z.
+template <typename R>
+__device__ __forceinline__ R filt(const R *f, int n1, int n3, int i, int k) {
+    const int ip = wrapp(i, n1), im = wrapm(i, n1), kp = wrapp(k, n3), km = wrapm(k, n3);
+    const R six = (R)6.0, four = (R)4.0;
+    auto T = [&](int kk) {
+        const R *r = f + (long long)kk * n1;
+        return (r[im] + four * r[i] + r[ip]) / six;
+    };
+    return (T(km) + four * T(k) + T(kp)) / six;
+}
+
+// SGSDY's test-filter stage, the plane sums (FP64, fixed order) and nu, one block per plane.
+template <typename R>
+__global__ void __launch_bounds__(256) k_sgs_dyn(StepArgs<R> a, LesArgs<R> l) {
+    const Geo g = a.g;
+    const int j = 1 + blockIdx.x;
+    const long long fs = (long long)g.n2m * g.np, pb = (long long)(j - 1) * g.np;
+    __shared__ double sn[256], sd[256];
+    __shared__ R coefj;
+    double snum = 0.0, sden = 0.0;
+    const R fd = (R)4.0 * l.d23r[j];
+    for (int e = threadIdx.x; e < g.np; e += blockDim.x) {
+        const int i = e % g.n1m, k = e / g.n1m;
+        R m[6], cf[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            m[c] = filt(l.dyn + c * fs + pb, g.n1m, g.n3m, i, k);
+            cf[c] = filt(l.dyn + (6 + c) * fs + pb, g.n1m, g.n3m, i, k);
+        }
+        const R fdabs = fd * sqrt((R)2.0 * sumsq6(m));
+#pragma unroll
+        for (int c = 0; c < 6; ++c) m[c] = fdabs * m[c] - cf[c];
+        R uc[3], up[6];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) uc[c] = filt(l.dyn + (12 + c) * fs + pb, g.n1m, g.n3m, i, k);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) up[c] = filt(l.dyn + (15 + c) * fs + pb, g.n1m, g.n3m, i, k);
+        const R L11 = up[0] - uc[0] * uc[0], L12 = up[1] - uc[0] * uc[1], L13 = up[2] - uc[0] * uc[2];
+        const R L22 = up[3] - uc[1] * uc[1], L23 = up[4] - uc[1] * uc[2], L33 = up[5] - uc[2] * uc[2];
+        const R two = (R)2.0;
+        const R sqmm = sumsq6(m);
+        const R sqlm = two * L12 * m[1] + L11 * m[0] + two * L13 * m[2] + L22 * m[3] + two * L23 * m[4] + L33 * m[5];
+        sden += (double)sqmm;
+        snum += (double)sqlm;
+    }
+    sn[threadIdx.x] = snum;
+    sd[threadIdx.x] = sden;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sn[threadIdx.x] += sn[threadIdx.x + s];
+            sd[threadIdx.x] += sd[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double nxz = 1.0 / (double)g.np;
+        const double sm = -0.5 * (sn[0] * nxz) / (sd[0] * nxz);
+        l.smagc[j] = sm;
+        coefj = (R)(sm * l.d23[j]);
+    }
+    __syncthreads();
+    const R c = coefj;
+    R *nup = l.nu + fidx(g, 0, j, 0);
+    for (int e = threadIdx.x; e < g.np; e += blockDim.x) {
+        const R t = c * nup[e];
+        nup[e] = t > -l.reninv ? t : -l.reninv;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// WALLMODEL_INSTANT: one thread per bottom-wall point; FP64.  The reference's Newton loop
+// has no cap; here a point that has not converged after l.wall_cap iterations is counted
+// and the step reports C3D_ENOTCONV.
+// ---------------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_wall(StepArgs<R> a, LesArgs<R> l) {
+    typedef St<R> ST;
+    const Geo g = a.g;
+    __shared__ double ssum[TPB], sbad[TPB];
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double tw1 = 0.0, bad = 0.0;
+    if (e < g.np) {
+        const int i = e % g.n1m, k = e / g.n1m;
+        const double u3 = ST::dbl(a.u[fidx(g, i, 3, k)]), w3 = ST::dbl(a.w[fidx(g, i, 3, k)]);
+        const double KAPA = 0.41, B = 5.2, RE = g.re;
+        const double DELTAP = g.dy[1] + g.dy[2] + g.dy[3] / 2.0;
+        const double uave = sqrt(u3 * u3 + w3 * w3);
+        double ut1 = 1.0, ut2 = 0.000001, lambda = 1.0;
+        int it = 0;
+        while (fabs(ut2 - ut1) > 1.0e-6) {
+            if (++it > l.wall_cap) {
+                bad = 1.0;
+                break;
+            }
+            ut1 = ut2;
+            const double f1 = uave / ut1 - log(ut1 * DELTAP * RE) / KAPA - B;
+            const double f2 = -uave / (ut1 * ut1) - 1.0 / KAPA / ut1;
+            ut2 = ut1 - lambda * f1 / f2;
+            const double f3 = uave / ut2 - log(ut2 * DELTAP * RE) / KAPA - B;
+            if (fabs(f3) > fabs(f1)) lambda = 0.5 * lambda;
+        }
+        tw1 = ut1 * ut1;
+        l.tauw[e] = tw1 * u3 / uave;
+        l.taub[e] = tw1 * w3 / uave;
+    }
+    ssum[threadIdx.x] = tw1;
+    sbad[threadIdx.x] = bad;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            ssum[threadIdx.x] += ssum[threadIdx.x + s];
+            sbad[threadIdx.x] += sbad[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        l.wpart[blockIdx.x] = ssum[0];
+        l.wpart[gridDim.x + blockIdx.x] = sbad[0];
+    }
+}
+
+template <typename R>
+__global__ void k_wall_sum(StepArgs<R> a, LesArgs<R> l, int nb) {
+    __shared__ double s[256], b[256];
+    double x = 0.0, y = 0.0;
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+        x += l.wpart[q];
+        y += l.wpart[nb + q];
+    }
+    s[threadIdx.x] = x;
+    b[threadIdx.x] = y;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            s[threadIdx.x] += s[threadIdx.x + w];
+            b[threadIdx.x] += b[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        a.scal[SCAL_WSMC] = s[0] / (double)a.g.np;
+        a.scal[SCAL_WALLERR] = b[0] > 0.0 ? 1.0 : 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// les_x1: rows (j, k), j = 1..N2M.  nux = Ix(nu); HH1 -= 2 Dx(nu Dx u); dvdx = Dx(v)
+// at the x faces of the v faces J >= 2; dwdx = Dx(w) at the x faces.
+// ---------------------------------------------------------------------------------
+template <typename R, int C>
+__global__ void __launch_bounds__(TPB) k_les_x1(StepArgs<R> a, LesArgs<R> l) {
+    typedef typename SType<R>::S S;
+    typedef St<R> ST;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Geo g = a.g;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int P = g.n1m / C;
+    S *sbS = reinterpret_cast<S *>(smem_raw + wid * stage_bytes(g.n1m, C));
+    R *sbR = reinterpret_cast<R *>(sbS);
+    const int nrows = g.n2m * g.n3m;
+    const R f24 = a.f24x, four = (R)4.0, two = (R)2.0;
+    for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
+        const int j = 1 + row / g.n3m, k = row % g.n3m;
+        const long long o = fidx(g, 0, j, k);
+        R nv[C], d[C];
+        srow_load(nv, l.nu + o, sbR, lane, P);
+        {
+            R pv = sprev(nv[C - 1], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) d[t] = four * (nv[t] + (t == 0 ? pv : nv[t - 1]));
+            xsolve(d, lane, P, a.c6x);
+            srow_store(l.nux + o, d, sbR, lane, P);
+        }
+        {
+            S uc[C];
+            srow_load(uc, a.u + o, sbS, lane, P);
+            S nx = snext(uc[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) d[t] = f24 * ST::d(t == C - 1 ? nx : uc[t + 1], uc[t]);
+            xsolve(d, lane, P, a.c22x);
+#pragma unroll
+            for (int t = 0; t < C; ++t) d[t] = nv[t] * d[t];
+            R pv = sprev(d[C - 1], lane, P);
+            R e[C];
+#pragma unroll
+            for (int t = 0; t < C; ++t) e[t] = f24 * (d[t] - (t == 0 ? pv : d[t - 1]));
+            xsolve(e, lane, P, a.c22x);
+            R h[C];
+            srow_load(h, a.hh[0] + o, sbR, lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) h[t] = h[t] - two * e[t];
+            srow_store(a.hh[0] + o, h, sbR, lane, P);
+        }
+        if (j >= 2) {
+            S vc[C];
+            srow_load(vc, a.v + o, sbS, lane, P);
+            S pv = sprev(vc[C - 1], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) d[t] = f24 * ST::d(vc[t], t == 0 ? pv : vc[t - 1]);
+            xsolve(d, lane, P, a.c22x);
+            srow_store(l.dvdx + o, d, sbR, lane, P);
+        }
+        {
+            S wc[C];
+            srow_load(wc, a.w + o, sbS, lane, P);
+            S pv = sprev(wc[C - 1], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) d[t] = f24 * ST::d(wc[t], t == 0 ? pv : wc[t - 1]);
+            xsolve(d, lane, P, a.c22x);
+            srow_store(l.dwdx + o, d, sbR, lane, P);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// les_z1: columns (i, j), j = 1..N2M.  nuz = Iz(nu); tau13 = Iz(nux) (Dz u + dwdx);
+// nuwz = nu Dz(w) at the cell centres; dvdz = Dz(v) at the z faces of the v faces J >= 2.
+// ---------------------------------------------------------------------------------
+template <typename R>
+struct WalkLesZ1 {
+    typedef typename SType<R>::S S;
+    const R *NU, *NUX; const S *U, *V, *W; int n, s; R f24; bool hv;
+    R num, nuxm; S um, vm, wc; int kn, kc;
+    __device__ void start(int k) {
+        const int kp = zprev(k, n);
+        num = NU[kp * s]; nuxm = NUX[kp * s]; um = U[kp * s]; vm = hv ? V[kp * s] : S(); wc = W[k * s];
+        kc = k; kn = znext(k, n);
+    }
+    __device__ void next(R (&d)[5]) {
+        const R nuc = NU[kc * s], nuxc = NUX[kc * s];
+        const S uc = U[kc * s], wp = W[kn * s];
+        d[0] = (R)4.0 * (num + nuc);
+        d[1] = (R)4.0 * (nuxm + nuxc);
+        d[2] = f24 * St<R>::d(uc, um);
+        d[3] = f24 * St<R>::d(wp, wc);
+        if (hv) {
+            const S vc = V[kc * s];
+            d[4] = f24 * St<R>::d(vc, vm);
+            vm = vc;
+        } else {
+            d[4] = R(0);
+        }
+        num = nuc; nuxm = nuxc; um = uc; wc = wp; kc = kn; kn = znext(kn, n);
+    }
+    __device__ static int zprev(int k, int n) { return k == 0 ? n - 1 : k - 1; }
+    __device__ static int znext(int k, int n) { return k + 1 == n ? 0 : k + 1; }
+};
+
+template <typename R, int L>
+__global__ void __launch_bounds__(TPB) k_les_z1(StepArgs<R> a, LesArgs<R> l) {
+    const Geo g = a.g;
+    int i, j, k0;
+    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    const int n = g.n3m, s = g.n1m;
+    const long long o = fidx(g, i, j, 0);
+    R out[5][L];
+    const R rr[5] = {a.c6z.r, a.c6z.r, a.c22z.r, a.c22z.r, a.c22z.r};
+    const R ss[5] = {a.c6z.s, a.c6z.s, a.c22z.s, a.c22z.s, a.c22z.s};
+    WalkLesZ1<R> f{l.nu + o, l.nux + o, a.u + o, a.v + o, a.w + o, n, s, a.f24z, j >= 2};
+    zsweep<R, L, WM<R>::M6, 5>(out, k0, n, rr, ss, f);
+#pragma unroll
+    for (int t = 0; t < L; ++t) {
+        const long long kk = o + (long long)(k0 + t) * s;
+        l.nuz[kk] = out[0][t];
+        l.t13[kk] = out[1][t] * (out[2][t] + l.dwdx[kk]);
+        l.nuwz[kk] = l.nu[kk] * out[3][t];
+        if (j >= 2) l.dvdz[kk] = out[4][t];
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// les_z2: columns (i, j).  HH1 -= Dz(tau13); HH3 -= 2 Dz(nuwz) + d/dy(nu_yz (dw/dy + dv/dz));
+// HH2 -= Dz(tau23) at the v faces J >= 2.
+// ---------------------------------------------------------------------------------
+template <typename R>
+struct WalkLesZ2 {
+    typedef typename SType<R>::S S;
+    const R *T13, *NWZ, *NZc, *NZm, *DVZ; const S *Wc, *Wm; int n, s; R f24, rhj, hdj, hdjm; bool hv;
+    R tc, nwm, t23c; int kn, kc;
+    __device__ R tau23(int k) const {
+        const R nyz = rhj * (hdj * NZm[k * s] + hdjm * NZc[k * s]);
+        return nyz * (rhj * St<R>::d(Wc[k * s], Wm[k * s]) + DVZ[k * s]);
+    }
+    __device__ void start(int k) {
+        tc = T13[k * s]; nwm = NWZ[(k == 0 ? n - 1 : k - 1) * s]; t23c = hv ? tau23(k) : R(0);
+        kc = k; kn = (k + 1 == n) ? 0 : k + 1;
+    }
+    __device__ void next(R (&d)[3]) {
+        const R tp = T13[kn * s], nwc = NWZ[kc * s];
+        const R t23p = hv ? tau23(kn) : R(0);
+        d[0] = f24 * (tp - tc);
+        d[1] = f24 * (nwc - nwm);
+        d[2] = f24 * (t23p - t23c);
+        tc = tp; nwm = nwc; t23c = t23p; kc = kn; kn = (kn + 1 == n) ? 0 : kn + 1;
+    }
+};
+
+template <typename R, int L>
+__global__ void __launch_bounds__(TPB) k_les_z2(StepArgs<R> a, LesArgs<R> l) {
+    typedef St<R> ST;
+    const Geo g = a.g;
+    int i, j, k0;
+    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    const int n = g.n3m, s = g.n1m;
+    const long long o = fidx(g, i, j, 0), om = fidx(g, i, j - 1, 0), op = fidx(g, i, j + 1, 0);
+    const bool hv = j >= 2;
+    R out[3][L];
+    const R rr[3] = {a.c22z.r, a.c22z.r, a.c22z.r}, ss[3] = {a.c22z.s, a.c22z.s, a.c22z.s};
+    WalkLesZ2<R> f{l.t13 + o, l.nuwz + o, l.nuz + o, l.nuz + om, l.dvdz + o, a.w + o, a.w + om,
+                   n, s, a.f24z, a.m.rh[j], a.m.hdy[j], a.m.hdy[j - 1], hv};
+    zsweep<R, L, WM<R>::M22, 3>(out, k0, n, rr, ss, f);
+    const bool fjum = (j != 1), fjup = (j != g.n2m);
+    const R half = (R)0.5, two = (R)2.0;
+    const R f2 = (R)(1.0 - l.ifwall * (fjup ? 0.0 : 1.0) * (g.aly - 1.0));
+    const R f1 = (R)(1.0 - l.ifwall * (fjum ? 0.0 : 1.0));
+    const R rdy = a.m.rdy[j], rh = a.m.rh[j], rhp = a.m.rh[j + 1];
+    const R hdj = a.m.hdy[j], hdjm = a.m.hdy[j - 1], hdjp = a.m.hdy[j + 1];
+    const long long w0 = fidx(g, i, 0, 0), wt = fidx(g, i, g.n2, 0);
+#pragma unroll
+    for (int t = 0; t < L; ++t) {
+        const int k = k0 + t, km = (k == 0) ? n - 1 : k - 1;
+        const long long kk = (long long)k * s, kkm = (long long)km * s;
+        const R sj2 = fjup ? rhp * (hdj * l.nuz[op + kk] + hdjp * l.nuz[o + kk])
+                           : half * (l.nu[wt + kk] + l.nu[wt + kkm]);
+        const R sj1 = fjum ? rh * (hdjm * l.nuz[o + kk] + hdj * l.nuz[om + kk])
+                           : half * (l.nu[w0 + kk] + l.nu[w0 + kkm]);
+        const R ww22 = rhp * ST::d(a.w[op + kk], a.w[o + kk]);
+        const R ww11 = rh * ST::d(a.w[o + kk], a.w[om + kk]);
+        const R yflux = rdy * ((f2 * sj2) * (ww22 + l.dvdz[op + kk]) - (f1 * sj1) * (ww11 + l.dvdz[o + kk]));
+        R *H1 = a.hh[0] + o + kk, *H2 = a.hh[1] + o + kk, *H3 = a.hh[2] + o + kk;
+        *H1 = *H1 - out[0][t];
+        *H3 = *H3 - two * out[1][t] - yflux;
+        if (hv) *H2 = *H2 - out[2][t];
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// les_x2: rows (j, k).  HH3 -= Dx(tau13); HH2 -= Dx(tau12) + 2 d/dy(nu dv/dy) (J >= 2);
+// HH1 -= d/dy(nu_xy (du/dy + dv/dx)); the wall-stress terms of RUH1, RUH3 (IFWALL).
+// ---------------------------------------------------------------------------------
+template <typename R, int C>
+__global__ void __launch_bounds__(TPB) k_les_x2(StepArgs<R> a, LesArgs<R> l) {
+    typedef typename SType<R>::S S;
+    typedef St<R> ST;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Geo g = a.g;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int P = g.n1m / C;
+    S *sbS = reinterpret_cast<S *>(smem_raw + wid * stage_bytes(g.n1m, C));
+    R *sbR = reinterpret_cast<R *>(sbS);
+    const int nrows = g.n2m * g.n3m;
+    const R f24 = a.f24x, half = (R)0.5, two = (R)2.0;
+    for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
+        const int j = 1 + row / g.n3m, k = row % g.n3m;
+        const long long o = fidx(g, 0, j, k), om = fidx(g, 0, j - 1, k), op = fidx(g, 0, j + 1, k);
+        const bool fjum = (j != 1), fjup = (j != g.n2m);
+        R d[C];
+        {   // HH3 -= Dx(tau13)
+            R tc[C];
+            srow_load(tc, l.t13 + o, sbR, lane, P);
+            R nx = snext(tc[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) d[t] = f24 * ((t == C - 1 ? nx : tc[t + 1]) - tc[t]);
+            xsolve(d, lane, P, a.c22x);
+            R h[C];
+            srow_load(h, a.hh[2] + o, sbR, lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) h[t] = h[t] - d[t];
+            srow_store(a.hh[2] + o, h, sbR, lane, P);
+        }
+        S uc[C], um[C];
+        srow_load(uc, a.u + o, sbS, lane, P);
+        srow_load(um, a.u + om, sbS, lane, P);
+        R nxc[C], nxm[C], dvc[C];
+        srow_load(nxc, l.nux + o, sbR, lane, P);
+        if (j >= 2) {
+            srow_load(nxm, l.nux + om, sbR, lane, P);
+            srow_load(dvc, l.dvdx + o, sbR, lane, P);
+        } else {
+#pragma unroll
+            for (int t = 0; t < C; ++t) { nxm[t] = R(0); dvc[t] = R(0); }
+        }
+        if (j >= 2) {   // HH2 -= Dx(tau12) + 2 d/dy(nu dv/dy)
+            const R rh = a.m.rh[j], hd = a.m.hdy[j], hdm = a.m.hdy[j - 1];
+            R tau[C];
+#pragma unroll
+            for (int t = 0; t < C; ++t) tau[t] = (rh * (hdm * nxc[t] + hd * nxm[t])) * (rh * ST::d(uc[t], um[t]) + dvc[t]);
+            R nx = snext(tau[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) d[t] = f24 * ((t == C - 1 ? nx : tau[t + 1]) - tau[t]);
+            xsolve(d, lane, P, a.c22x);
+            S vc[C], vm[C], vp[C];
+            srow_load(vc, a.v + o, sbS, lane, P);
+            srow_load(vm, a.v + om, sbS, lane, P);
+            srow_load(vp, a.v + op, sbS, lane, P);
+            R nc[C], nm[C], h[C];
+            srow_load(nc, l.nu + o, sbR, lane, P);
+            srow_load(nm, l.nu + om, sbR, lane, P);
+            srow_load(h, a.hh[1] + o, sbR, lane, P);
+            const R rdy = a.m.rdy[j], rdym = a.m.rdy[j - 1];
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                const R vis22 = rh * (nc[t] * (rdy * ST::d(vp[t], vc[t])) - nm[t] * (rdym * ST::d(vc[t], vm[t])));
+                h[t] = h[t] - d[t] - two * vis22;
+            }
+            srow_store(a.hh[1] + o, h, sbR, lane, P);
+        }
+        {   // HH1 -= d/dy(nu_xy (du/dy + dv/dx))
+            S up[C];
+            srow_load(up, a.u + op, sbS, lane, P);
+            R nxp[C], dvp[C], nw[C];
+            if (fjup) {
+                srow_load(nxp, l.nux + op, sbR, lane, P);
+                srow_load(dvp, l.dvdx + op, sbR, lane, P);
+            } else {
+#pragma unroll
+                for (int t = 0; t < C; ++t) { nxp[t] = R(0); dvp[t] = R(0); }
+            }
+            // wall viscosity (x average of the ghost plane) where the face is a wall
+            if (!fjup || !fjum) srow_load(nw, l.nu + (fjup ? fidx(g, 0, 0, k) : fidx(g, 0, g.n2, k)), sbR, lane, P);
+            R pw = sprev((!fjup || !fjum) ? nw[C - 1] : R(0), lane, P);
+            const R rh = a.m.rh[j], rhp = a.m.rh[j + 1], hd = a.m.hdy[j], hdm = a.m.hdy[j - 1], hdp = a.m.hdy[j + 1];
+            const R f2 = (R)(1.0 - l.ifwall * (fjup ? 0.0 : 1.0) * (g.aly - 1.0));
+            const R f1 = (R)(1.0 - l.ifwall * (fjum ? 0.0 : 1.0));
+            const R rdy = a.m.rdy[j];
+            R h[C];
+            srow_load(h, a.hh[0] + o, sbR, lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                const R wv = (!fjup || !fjum) ? half * (nw[t] + (t == 0 ? pw : nw[t - 1])) : R(0);
+                const R sj2 = fjup ? rhp * (hd * nxp[t] + hdp * nxc[t]) : wv;
+                const R sj1 = fjum ? rh * (hdm * nxc[t] + hd * nxm[t]) : wv;
+                const R uu22 = rhp * ST::d(up[t], uc[t]);
+                const R uu11 = rh * ST::d(uc[t], um[t]);
+                h[t] = h[t] - rdy * ((f2 * sj2) * (uu22 + dvp[t]) - (f1 * sj1) * (uu11 + dvc[t]));
+            }
+            srow_store(a.hh[0] + o, h, sbR, lane, P);
+        }
+        if (l.ifwall && (!fjum || !fjup)) {   // wall-stress terms (IFWALL)
+            const double rdy1 = 1.0 / g.dy[1], rdyt = 1.0 / g.dy[g.n2m];
+            R r0[C], r2[C];
+            srow_load(r0, a.r[0] + o, sbR, lane, P);
+            srow_load(r2, a.r[2] + o, sbR, lane, P);
+            if (lane < P) {
+#pragma unroll
+                for (int t = 0; t < C; ++t) {
+                    const int i = lane * C + t;
+                    const long long e0 = (long long)k * g.n1m + i, e1 = e0 + g.np;
+                    double b1 = 0.0, b3 = 0.0;
+                    if (!fjum) { b1 += -l.tauw[e0] * rdy1; b3 += -l.taub[e0] * rdy1; }
+                    if (!fjup) { b1 += -l.tauw[e1] * rdyt * (g.aly - 1.0); b3 += -l.taub[e1] * rdyt * (g.aly - 1.0); }
+                    r0[t] = r0[t] + (R)b1;
+                    r2[t] = r2[t] + (R)b3;
+                }
+            }
+            srow_store(a.r[0] + o, r0, sbR, lane, P);
+            srow_store(a.r[2] + o, r2, sbR, lane, P);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Host-side launch of the LES stages of one step.  stage 0: WALLSS (WMODEL = 0), the SGS
+// model and the wall model (before BCOND); stage 1: the SGS fluxes (after zB).
+// ---------------------------------------------------------------------------------
+template <typename R, int C>
+static void launch_les_x(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int which, int *nl) {
+    const size_t sb = (TPB / 32) * stage_bytes(ch->g.n1m, C);
+    const int grid = nblk((long long)ch->g.n2m * ch->g.n3m, TPB / 32);
+    const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
+    if (which == 0) {
+        cudaFuncSetAttribute(k_les_x1<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
+        k_les_x1<R, C><<<grid, TPB, sb, ch->stream>>>(a, l);
+        mark(ch, nl, "les_x1", N * (24 + 6 * Rb));
+    } else {
+        cudaFuncSetAttribute(k_les_x2<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
+        k_les_x2<R, C><<<grid, TPB, sb, ch->stream>>>(a, l);
+        mark(ch, nl, "les_x2", N * (16 + 14 * Rb));
+    }
+}
+
+template <typename R>
+int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *nl) {
+    cudaStream_t st = ch->stream;
+    const Geo &g = ch->g;
+    const double N = (double)g.n1m * g.n2m * g.n3m, Rb = sizeof(R);
+    if (stage == 0) {
+        if (g.n2m < 1) return C3D_EINVAL;
+        if (ch->files != 0 && ch->wmodel == 0) {
+            k_les_wallss<R><<<1, 256, 0, st>>>(a);
+            mark(ch, nl, "les_wallss", 64.0 * g.np);
+        }
+        if (ch->files == 2) {
+            k_sgs_coef<R><<<1, 128, 0, st>>>(a, l);
+            k_sgs_cs<R><<<nblk((long long)g.n2m * g.np), TPB, 0, st>>>(a, l);
+            mark(ch, nl, "sgs_cs", N * (6 * 8 + Rb));
+        } else if (ch->files == 1) {
+            k_sgs_raw<R><<<nblk((long long)g.n2m * g.np), TPB, 0, st>>>(a, l);
+            mark(ch, nl, "sgs_raw", N * (6 * 8 + 22 * Rb));
+            k_sgs_dyn<R><<<g.n2m, 256, 0, st>>>(a, l);
+            mark(ch, nl, "sgs_dyn", N * 23 * Rb);
+        }
+        if (ch->files != 0 && ch->wmodel == 1) {
+            const int nb = nblk(g.np);
+            k_wall<R><<<nb, TPB, 0, st>>>(a, l);
+            k_wall_sum<R><<<1, 256, 0, st>>>(a, l, nb);
+            mark(ch, nl, "wall", 32.0 * g.np);
+        }
+        return 0;
+    }
+    switch ((g.n1m + 31) / 32) {
+        case 1: launch_les_x<R, 1>(ch, a, l, 0, nl); break;
+        case 2: launch_les_x<R, 2>(ch, a, l, 0, nl); break;
+        case 3: launch_les_x<R, 3>(ch, a, l, 0, nl); break;
+        case 4: launch_les_x<R, 4>(ch, a, l, 0, nl); break;
+        case 6: launch_les_x<R, 6>(ch, a, l, 0, nl); break;
+        case 8: launch_les_x<R, 8>(ch, a, l, 0, nl); break;
+        case 12: launch_les_x<R, 12>(ch, a, l, 0, nl); break;
+        default: set_error("unsupported N1M"); return C3D_EINVAL;
+    }
+    const long long nz = (long long)g.n2m * (g.n3m / ZL) * g.n1m;
+    k_les_z1<R, ZL><<<nblk(nz), TPB, 0, st>>>(a, l);
+    mark(ch, nl, "les_z1", N * (24 + 7 * Rb));
+    k_les_z2<R, ZL><<<nblk(nz), TPB, 0, st>>>(a, l);
+    mark(ch, nl, "les_z2", N * (16 + 12 * Rb));
+    switch ((g.n1m + 31) / 32) {
+        case 1: launch_les_x<R, 1>(ch, a, l, 1, nl); break;
+        case 2: launch_les_x<R, 2>(ch, a, l, 1, nl); break;
+        case 3: launch_les_x<R, 3>(ch, a, l, 1, nl); break;
+        case 4: launch_les_x<R, 4>(ch, a, l, 1, nl); break;
+        case 6: launch_les_x<R, 6>(ch, a, l, 1, nl); break;
+        case 8: launch_les_x<R, 8>(ch, a, l, 1, nl); break;
+        case 12: launch_les_x<R, 12>(ch, a, l, 1, nl); break;
+        default: set_error("unsupported N1M"); return C3D_EINVAL;
+    }
+    return 0;
+}
+
+template int launch_les<double>(c3d_channel *, StepArgs<double> &, LesArgs<double> &, int, int *);
+template int launch_les<float>(c3d_channel *, StepArgs<float> &, LesArgs<float> &, int, int *);
+
+}  // namespace c3d

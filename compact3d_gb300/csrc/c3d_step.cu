@@ -333,17 +333,47 @@ static int pressure_and_update(c3d_channel *ch, StepArgs<R> &a, R *d0, R *d1, R 
 }
 
 template <typename R>
+static LesArgs<R> make_les_args(c3d_channel *ch) {
+    LesArgs<R> l;
+    memset((void *)&l, 0, sizeof(l));
+    if (ch->files == 0) return l;
+    R **f[8] = {&l.nu, &l.nux, &l.nuz, &l.t13, &l.nuwz, &l.dvdx, &l.dwdx, &l.dvdz};
+    for (int q = 0; q < 8; ++q) *f[q] = (R *)ch->les[q];
+    l.dyn = (R *)ch->dyn;
+    l.smagc = ch->smagc;
+    l.coef = (R *)ch->coef;
+    l.d23 = ch->d23;
+    l.d23r = (const R *)ch->d23r;
+    l.ycs = ch->ycs;
+    l.tauw = ch->tauw;
+    l.taub = ch->taub;
+    l.wpart = ch->wpart;
+    l.files = ch->files;
+    l.wmodel = ch->wmodel;
+    l.wall_cap = ch->wall_cap;
+    l.ifwall = ch->wmodel != 0 ? 1.0 : 0.0;   // WALL_MODEL sets IFWALL = 1 (compact3d.f:1993)
+    l.reninv = (R)(1.0 / ch->g.re);
+    l.dx1 = (R)ch->g.dx1;
+    l.dx3 = (R)ch->g.dx3;
+    return l;
+}
+
+template <typename R>
 static int step_impl(c3d_channel *ch, double dt, int *nl) {
     typedef typename SType<R>::S S;
     set_spec_smem<R>(ch);
     ch->cur = 1 - ch->cur;   // HH of the last step becomes HH_old (GETUP's HH2 <- HH)
     StepArgs<R> a = make_args<R>(ch, dt);
+    int rc;
+    LesArgs<R> l = make_les_args<R>(ch);
+    // GETUP order (compact3d.f:931-940): SGS model and wall model, then BCOND
+    if (ch->files != 0 && (rc = launch_les<R>(ch, a, l, 0, nl))) return rc;
     k_bcond<R><<<nblk(ch->g.np), TPB, 0, ch->stream>>>(ch->g, (S *)ch->u, (S *)ch->v, (S *)ch->w);
     mark(ch, nl, "bcond", 64.0 * ch->g.np);
-    int rc;
     if ((rc = launch_xpass<R>(ch, a, 0, nullptr, nullptr, nl))) return rc;    // xA
     if ((rc = launch_zpass<R>(ch, a, 0, nullptr, nullptr, nullptr, 0, nl))) return rc;   // zA
     if ((rc = launch_zpass<R>(ch, a, 1, nullptr, nullptr, nullptr, 0, nl))) return rc;   // zB
+    if (ch->files != 0 && (rc = launch_les<R>(ch, a, l, 1, nl))) return rc;   // SGS fluxes into HH
     if ((rc = launch_xpass<R>(ch, a, 1, nullptr, nullptr, nl))) return rc;    // xB
     k_ycn<R><<<nblk(3LL * ch->g.np), TPB, 0, ch->stream>>>(a, sizeof(R) == 8 ? (const R *)ch->ycn : (const R *)ch->ycn32);
     mark(ch, nl, "ycn", (double)ch->g.n1m * ch->g.n2m * ch->g.n3m * 6 * sizeof(R));
@@ -421,15 +451,21 @@ int launch_poisson_tables(c3d_channel *ch) {
 
 int launch_repack(c3d_channel *ch, int dir, int what, int comp) {
     const Geo &g = ch->g;
-    const int j0 = (what == 0) ? 0 : 1, j1 = (what == 0) ? g.n2 : g.n2m;
+    const int j0 = (what == 0 || what == 3) ? 0 : 1, j1 = (what == 0 || what == 3) ? g.n2 : g.n2m;
     const long long tot_dev = (long long)(j1 - j0 + 1) * g.np;
     const long long N1 = g.n1m + 1, N2 = g.n2, N3 = g.n3m + 1;
     const long long tot_f = (what == 1) ? N1 * N2 * N3 : (N1 + 1) * (N2 + 1) * (N3 + 1);
     cudaStream_t st = ch->stream;
     const bool mixed = ch->precision == C3D_MIXED;
+    const int nb = nblk(dir == 0 ? tot_dev : tot_f);
+    if (what == 3) {   // SGSVIS (0:M1,0:M2,0:M3), device to host only, working precision
+        if (dir == 0 || !ch->les[0]) return C3D_EINVAL;
+        if (!mixed) k_pack<double><<<nb, TPB, 0, st>>>(g, 0, (const double *)ch->les[0], ch->stage, FromF64());
+        else k_pack<float><<<nb, TPB, 0, st>>>(g, 0, (const float *)ch->les[0], ch->stage, FromF32());
+        return 0;
+    }
     void *dev = (what == 2) ? ch->hh[ch->cur][comp]
                             : (what == 1) ? ch->p : (comp == 0 ? ch->u : comp == 1 ? ch->v : ch->w);
-    const int nb = nblk(dir == 0 ? tot_dev : tot_f);
     if (!mixed) {
         if (dir == 0) k_unpack<double><<<nb, TPB, 0, st>>>(g, what, (double *)dev, ch->stage, ToF64());
         else k_pack<double><<<nb, TPB, 0, st>>>(g, what, (const double *)dev, ch->stage, FromF64());

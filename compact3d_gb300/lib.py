@@ -45,6 +45,9 @@ SIGNATURES = {
     "c3d_download": (_ip, [_vp, _dp, _dp, _dp, _dp]),
     "c3d_upload_wall": (_ip, [_vp, _dp, _dp]),
     "c3d_download_wall": (_ip, [_vp, _dp, _dp]),
+    "c3d_set_wsm": (_ip, [_vp, _dp]),
+    "c3d_get_wsm": (_ip, [_vp, _dp]),
+    "c3d_set_wall_iter_cap": (_ip, [_vp, _ip]),
     "c3d_step": (_ip, [_vp, _ip, ctypes.c_double, _dp, _dp]),
     "c3d_diagnose": (_ip, [_vp, ctypes.POINTER(c3d_diag)]),
     "c3d_getup": (_ip, [_vp, _dp, _dp, _dp, _dp, _ip, ctypes.c_double, _dp, _dp]),
@@ -143,6 +146,35 @@ class Channel:
         check(load().c3d_download(self.h, _p(U), _p(P), _p(HH), None), "c3d_download")
         return U, P, HH
 
+    # ---- LES (FILES != 0) ----
+    def download_sgsvis(self):
+        """SGSVIS(0:M1,0:M2,0:M3) of the last step (periodic ghost columns filled)."""
+        S = self.grid.zeros_s()
+        check(load().c3d_download(self.h, None, None, None, _p(S)), "c3d_download")
+        return S
+
+    def upload_wall(self, tauw=None, taub=None):
+        check(load().c3d_upload_wall(self.h, _p(tauw), _p(taub)), "c3d_upload_wall")
+
+    def download_wall(self):
+        g = self.grid
+        tw = np.zeros(g.shape_tau(), order="F")
+        tb = np.zeros(g.shape_tau(), order="F")
+        check(load().c3d_download_wall(self.h, _p(tw), _p(tb)), "c3d_download_wall")
+        return tw, tb
+
+    def set_wsm(self, wsm):
+        w = np.ascontiguousarray(wsm, dtype=np.float64)
+        check(load().c3d_set_wsm(self.h, _p(w)), "c3d_set_wsm")
+
+    def get_wsm(self):
+        w = np.zeros(3)
+        check(load().c3d_get_wsm(self.h, _p(w)), "c3d_get_wsm")
+        return w
+
+    def set_wall_iter_cap(self, cap: int):
+        check(load().c3d_set_wall_iter_cap(self.h, int(cap)), "c3d_set_wall_iter_cap")
+
     def step(self, ntime: int, dt: float, presg: float, presg3: float):
         """GETUP on the device-resident state; returns the new (PRESG, PRESG3)."""
         a = (ctypes.c_double * 1)(presg)
@@ -150,11 +182,11 @@ class Channel:
         check(load().c3d_step(self.h, ntime, dt, a, b), "c3d_step")
         return a[0], b[0]
 
-    def getup(self, U, P, HH, ntime: int, dt: float, presg: float, presg3: float):
+    def getup(self, U, P, HH, ntime: int, dt: float, presg: float, presg3: float, sgsvis=None):
         """GETUP(U,P,HH,SS,NTIME,PRESG,PRESG3,SGSVIS) with host arrays updated in place."""
         a = (ctypes.c_double * 1)(presg)
         b = (ctypes.c_double * 1)(presg3)
-        check(load().c3d_getup(self.h, _p(U), _p(P), _p(HH), None, ntime, dt, a, b), "c3d_getup")
+        check(load().c3d_getup(self.h, _p(U), _p(P), _p(HH), _p(sgsvis), ntime, dt, a, b), "c3d_getup")
         return a[0], b[0]
 
     def project(self):

@@ -57,7 +57,9 @@ extern "C" {
  *   /MESH4/ DYM,DYC,DYP(1:N2)              -> dym,dyc,dyp (n2 values, index J-1)
  *   /PARA/  RE                             -> re
  *   /FINOUT/ FILES (SGS model)             -> files  (0 none, 1 SGSDY, 2 SGSCS)
- *   /WALLMODEL/ WMODEL                     -> wmodel (0 none, 1 WALLMODEL_INSTANT)
+ *   /WALLMODEL/ WMODEL                     -> wmodel (0 none, 1 WALLMODEL_INSTANT;
+ *                                             Y(0) must be 0: Y0 != 0 selects the
+ *                                             rough-wall model, which is not built)
  * The library takes the driver's metric arrays as given; it recomputes only
  * the Poisson metrics of INIWAVE / METRICPOISSON (compact3d.f:9182-9263),
  * which depend on nothing else.
@@ -110,6 +112,22 @@ int c3d_set_device(int device);
  * c3d_diagnose  DIVCHECK + CFL + CHKMF + WALLSS on the current device state.
  * c3d_getup     drop-in for a driver that keeps the fields on the host:
  *               upload, step, download in one call.
+ *
+ * LES (files != 0, compact3d.f:931-937): each step zeroes SGSVIS and runs the SGS
+ * model (SGSDY or SGSCS) and, with wmodel = 1, WALLMODEL_INSTANT before BCOND; the
+ * SGS fluxes and the wall-stress terms enter RHS1-3.  SGSVIS passed to c3d_upload
+ * is not used (the step recomputes it); c3d_download / c3d_getup return it.  With
+ * wmodel = 0 the step first evaluates WALLSS on the current field, which is what the
+ * driver's time loop does right before GETUP (compact3d.f:125), so SGSCS sees the
+ * same WSM.  A wall point whose Newton iteration for u_tau exceeds the iteration cap
+ * (default 10000; the reference iterates without one) makes c3d_step / c3d_sync
+ * return C3D_ENOTCONV after the step completes.
+ * c3d_upload_wall / c3d_download_wall  TAUW, TAUB (0:M1,0:M3,2) of /TAUXYZ/ (the
+ *               interior I = 1..N1M, K = 1..N3M of both walls; either may be NULL).
+ *               The wall model updates the bottom wall (index 1); the top wall keeps
+ *               what was uploaded, as in the reference.
+ * c3d_set_wsm / c3d_get_wsm  /WSMEM/ WSM(1:3) as the SGS model reads it and the
+ *               wall model writes WSM(1).
  */
 int c3d_create(const c3d_grid *grid, c3d_channel **out);
 int c3d_destroy(c3d_channel *ch);
@@ -119,6 +137,11 @@ int c3d_download(c3d_channel *ch, double *u, double *p, double *hh,
                  double *sgsvis);
 int c3d_upload_wall(c3d_channel *ch, const double *tauw, const double *taub);
 int c3d_download_wall(c3d_channel *ch, double *tauw, double *taub);
+int c3d_set_wsm(c3d_channel *ch, const double *wsm);
+int c3d_get_wsm(c3d_channel *ch, double *wsm);
+/* Newton iterations allowed per wall point (>= 1).  No counterpart in the reference,
+ * whose loop is unbounded; the cap turns a non-converging point into an error. */
+int c3d_set_wall_iter_cap(c3d_channel *ch, int cap);
 int c3d_step(c3d_channel *ch, int ntime, double dt,
              double *presg, double *presg3);
 int c3d_diagnose(c3d_channel *ch, c3d_diag *out);
