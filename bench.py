@@ -11,6 +11,14 @@ Arms
                      in the FP32-mixed form (--form), with the plain FP64 form measured in
                      the same run for comparison and the relative L2 error of the mixed form
                      against the FP64 form after the same steps.
+                     Further sections of the same JSON line: "batched" (32 uneven
+                     channels as one CUDA graph per ensemble step, against the same
+                     channels stepped one after another in FP64) and "les" (the
+                     wall-modelled LES workload les128 in both forms, with the mixed
+                     form's wall stress, bulk velocity and velocity error against FP64
+                     after --les-steps steps) and "operators" (each compact operator, y
+                     stencil and the Poisson solve alone on the 256 x 193 x 256 field,
+                     FP64 and mixed, with GB/s against the HBM peak).
   --impl reference   the FP64 OpenMP CPU restatement of the reference step (oracle/) on
                      all host cores, on a bounded sample of the same workload.
 
@@ -131,6 +139,20 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
+
+
+class L2Flush:
+    """Overwrites a 512 MB device buffer (4x the 129 MB L2) between timed iterations of
+    the workloads whose working set fits in L2; the channel stream is idle meanwhile."""
+
+    def __init__(self, device: int):
+        import torch
+        self.torch = torch
+        self.buf = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
+
+    def __call__(self):
+        self.buf.add_(1.0)
+        self.torch.cuda.synchronize()
 
 
 def peaks():
@@ -318,6 +340,14 @@ def run_ours(args, D: Dist):
     if not args.no_batch:
         res["batched"] = run_batched(args, D)
 
+    # ---- wall-modelled LES ----
+    if not args.no_les:
+        res["les"] = run_les(args, D)
+
+    # ---- operators one at a time (compact derivatives, y stencils, Poisson) ----
+    if not args.no_ops:
+        res["operators"] = run_operators(args, D)
+
     # ---- CPU baseline (rank 0, N=1 only) ----
     if D.rank == 0 and D.world == 1 and not args.no_cpu:
         rate, cores, sample = cpu_reference(args.workload, steps=3, warmup=1, budget_s=40.0)
@@ -384,6 +414,119 @@ def error_study(lib, g, dt, U0, P0, HH0, steps: int, floor: bool = True):
         out[name]["wsm_rel"] = abs(out[name]["wsm"] - float(diags["fp64"]["wsm"][0])) / abs(float(diags["fp64"]["wsm"][0]))
     out["fp64"] = dict(divmax=diags["fp64"]["divmax"], bulk=diags["fp64"]["flow1"] / g.aly,
                        wsm=float(diags["fp64"]["wsm"][0]), presg=presg["fp64"][0])
+    return out
+
+
+def run_les(args, D: Dist):
+    """The wall-modelled LES workload (les128: 128 x 65 x 128 points, 8pi x 2 x 3pi,
+    Re_tau ~2000, SGSCS + WALLMODEL_INSTANT, seeded log-law start with a 5% perturbation):
+    grid-pt-substeps/s of the mixed and FP64 forms, and after `les_steps` steps from the
+    same start the mixed form's wall stress WSM(1), bulk velocity and velocity error
+    against the FP64 form."""
+    from compact3d_gb300 import lib
+    g, dt = make_grid("les128")
+    U0, P0, HH0 = ic.loglaw(g, 2000.0, amp=0.05, seed=ic.SEED0 + 3000 + D.rank)
+    out = dict(workload=f"les128: {g.n1m}x{g.n2m + 1}x{g.n3m} points, 8pi x 2 x 3pi, uniform y, "
+                        f"RE={g.re} (Re_tau ~2000), dt={dt}, SGSCS + WALLMODEL_INSTANT, log-law start + 5%",
+               l2_policy="L2 flushed (512 MB written) before every timed step; each step timed alone")
+    flush = L2Flush(D.local)
+    for form in ("mixed", "fp64"):
+        ch = make_channel(lib, g, form, U0, P0, HH0)
+        n = 1
+        for _ in range(max(3, args.warmup)):
+            ch.step_async(n, dt)
+            n += 1
+        ch.sync()
+        K = args.steps
+        ms = 0.0
+        for _ in range(K):   # the working set is about L2-sized: flush before every step
+            flush()
+            ch.timer_start()
+            ch.step_async(n, dt)
+            n += 1
+            ms += ch.timer_stop()
+        ms = D.max(ms)
+        out[form] = dict(value=D.sum(g.points) * K / (ms / 1e3), unit=UNIT, ms_per_step=ms / K, steps=K,
+                         kernels_per_step=ch.last_step_stats()[1])
+        ch.close()
+    ns = args.les_steps
+    if ns > 0:
+        runs = {f: make_channel(lib, g, f, U0, P0, HH0) for f in ("mixed", "fp64")}
+        hist = {f: [] for f in runs}
+        every = max(1, ns // 10)
+        for s_ in range(1, ns + 1):
+            for c in runs.values():
+                c.step_async(s_, dt)
+            if s_ % every == 0 or s_ == ns:
+                for f, c in runs.items():
+                    d = c.diagnose()
+                    hist[f].append((s_, float(c.get_wsm()[0]), d["flow1"] / g.aly))
+        Um, _, _ = runs["mixed"].download()
+        Uf, _, _ = runs["fp64"].download()
+        n1, n2, n3 = g.n1m, g.n2m, g.n3m
+
+        def rl(a, b):
+            return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+        wm, wf = hist["mixed"][-1][1], hist["fp64"][-1][1]
+        bm, bf = hist["mixed"][-1][2], hist["fp64"][-1][2]
+        out["err_vs_fp64"] = dict(
+            steps=ns, u=rl(Um[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 0], Uf[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 0]),
+            v=rl(Um[1:n1 + 1, 2:n2 + 1, 1:n3 + 1, 1], Uf[1:n1 + 1, 2:n2 + 1, 1:n3 + 1, 1]),
+            w=rl(Um[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 2], Uf[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 2]),
+            wall_stress_mixed=wm, wall_stress_fp64=wf, wall_stress_rel=abs(wm - wf) / abs(wf),
+            bulk_mixed=bm, bulk_fp64=bf, bulk_rel=abs(bm - bf) / abs(bf),
+            history=dict(step=[h[0] for h in hist["fp64"]],
+                         wall_stress_mixed=[h[1] for h in hist["mixed"]],
+                         wall_stress_fp64=[h[1] for h in hist["fp64"]]))
+        for c in runs.values():
+            c.close()
+    return out
+
+
+def run_operators(args, D: Dist):
+    """The isolated operators on the field256 workload (256 x 193 x 256 points, seeded
+    band-limited input): for each operator the FP64 and mixed time per application,
+    algorithmic GB/s (operand read + result written; the Poisson solve also moves the
+    half spectrum through its five passes) against the measured HBM peak, and the mixed
+    result's relative L2 error against the FP64 result."""
+    from compact3d_gb300 import lib
+    g, _ = make_grid("field256")
+    U, _P = ic.band_limited(g, seed=ic.SEED0 + 4000 + D.rank)
+    F = np.asfortranarray(U[..., 0])
+    peak, kind = peaks()
+    N = g.points
+    K = max(5, args.steps)
+    chans = {f: lib.Channel(g, C3D_MIXED if f == "mixed" else C3D_FP64) for f in ("fp64", "mixed")}
+    out = dict(workload=f"field256: {g.n1m}x{g.n2m + 1}x{g.n3m} points, band-limited |k| <= N/3 in x, z, "
+                        f"smooth random y profile", peak_gbs=peak, peak_kind=kind, applications=K, ops={})
+    flush = L2Flush(D.local)
+    out["l2_policy"] = "L2 flushed (512 MB written) before every timed application; each timed alone"
+    for name, op in lib.OPS.items():
+        row = {}
+        res = {}
+        for form, ch in chans.items():
+            R = 4 if form == "mixed" else 8
+            ch.op_set(F)
+            ch.op_apply(op, 3)
+            ch.sync()
+            ms = 0.0
+            for _ in range(K):
+                flush()
+                ch.timer_start()
+                ch.op_apply(op, 1)
+                ms += ch.timer_stop()
+            ms = D.max(ms) / K
+            alg = N * (10 * R + 8) if name == "POISSON" else N * 2 * R
+            gbs = alg / (ms / 1e3) / 1e9
+            row[form] = dict(ms=ms, gbs=gbs, frac=gbs / peak, alg_bytes=alg)
+            res[form] = ch.op_get()
+        j0 = 2 if name == "DY1" else 1
+        a = res["mixed"][1:g.n1m + 1, j0:g.n2m + 1, 1:g.n3m + 1]
+        b = res["fp64"][1:g.n1m + 1, j0:g.n2m + 1, 1:g.n3m + 1]
+        row["mixed_rel_l2_vs_fp64"] = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+        out["ops"][name] = row
+    for c in chans.values():
+        c.close()
     return out
 
 
@@ -495,6 +638,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-floor", action="store_true")
+    ap.add_argument("--no-les", action="store_true")
+    ap.add_argument("--no-ops", action="store_true")
+    ap.add_argument("--les-steps", type=int, default=200)
     ap.add_argument("--nchan", type=int, default=32)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

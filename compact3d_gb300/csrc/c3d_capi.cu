@@ -159,7 +159,7 @@ void free_channel(c3d_channel *ch) {
                     ch->r[2], ch->exy, ch->exz, ch->eyz, ch->ww1, ch->wsq, ch->rdpz, ch->g1,
                     ch->spec, ch->stage, ch->tauw, ch->taub, ch->les[0], ch->les[1], ch->les[2],
                     ch->les[3], ch->les[4], ch->les[5], ch->les[6], ch->les[7], ch->dyn, ch->smagc,
-                    ch->d23, ch->ycs, ch->wpart, ch->coef, ch->d23r};
+                    ch->d23, ch->ycs, ch->wpart, ch->coef, ch->d23r, ch->opbuf[0], ch->opbuf[1]};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (ch->pinned) cudaFreeHost(ch->pinned);
@@ -844,6 +844,50 @@ int c3d_getup(c3d_channel *ch, double *u, double *p, double *hh, double *sgsvis,
     rc = c3d_step(ch, ntime, dt, presg, presg3);
     if (rc) return rc;
     return c3d_download(ch, u, p, hh, ch->files != 0 ? sgsvis : nullptr);
+}
+
+int c3d_op_set(c3d_channel *ch, const double *f) {
+    if (!ch || !f) { set_error("null argument"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    const size_t rs = ch->precision == C3D_MIXED ? 4 : 8, nf = (size_t)ch->g.nf;
+    for (int q = 0; q < 2; ++q) {
+        if (!ch->opbuf[q]) {
+            if (cudaMalloc(&ch->opbuf[q], nf * rs) != cudaSuccess) { set_error("cudaMalloc operand"); return C3D_ENOMEM; }
+            CK(cudaMemset(ch->opbuf[q], 0, nf * rs));
+        }
+    }
+    int rc = h2d(ch, f, ch->stage_elems);
+    if (rc) return rc;
+    launch_repack(ch, 0, 4, 0);
+    CK(cudaStreamSynchronize(ch->stream));
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int c3d_op_apply(c3d_channel *ch, int op, int count) {
+    if (!ch || count < 0) { set_error("null channel or negative count"); return C3D_EINVAL; }
+    if (!ch->opbuf[0]) { set_error("c3d_op_set must be called before c3d_op_apply"); return C3D_ESTATE; }
+    if (op < C3D_OP_DX1 || op > C3D_OP_POISSON) { set_error("unknown operator"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    int nl = 0;
+    for (int q = 0; q < count; ++q) {
+        int rc = launch_operator(ch, op, &nl);
+        if (rc) return rc;
+    }
+    CK(cudaGetLastError());
+    ch->last_launches = count > 0 ? nl / count : 0;
+    return 0;
+}
+
+int c3d_op_get(c3d_channel *ch, double *f) {
+    if (!ch || !f) { set_error("null argument"); return C3D_EINVAL; }
+    if (!ch->opbuf[1]) { set_error("no operator result"); return C3D_ESTATE; }
+    cudaSetDevice(ch->device);
+    launch_repack(ch, 1, 5, 0);
+    int rc = d2h(ch, f, ch->stage_elems);
+    if (rc) return rc;
+    CK(cudaGetLastError());
+    return 0;
 }
 
 int c3d_sync(c3d_channel *ch) {

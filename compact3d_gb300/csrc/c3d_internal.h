@@ -151,6 +151,7 @@ struct c3d_channel {
     double *smagc, *d23, *ycs, *wpart;
     void *coef, *d23r;        // per-J tables in R
     int wall_cap;
+    void *opbuf[2];           // operand and result of c3d_op_* (R, full fields)
     // per-kernel profiler (CUDA events around every launch when enabled)
     int prof_on;
     int prof_n;                              // events recorded in the current step
@@ -178,9 +179,14 @@ template <typename R>
 int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *nl);
 // Step drivers (c3d_step.cu)
 int launch_step(c3d_channel *ch, double dt, int *launches);
+int launch_operator(c3d_channel *ch, int op, int *launches);
+template <typename R>
+int launch_op(c3d_channel *ch, StepArgs<R> &a, int op, const R *in, R *out, int *nl);   // c3d_ops.cu
 int launch_project(c3d_channel *ch, int *launches);
 int launch_diag(c3d_channel *ch, int *launches);
 int launch_poisson_tables(c3d_channel *ch);
+// what: 0 U component, 1 P, 2 HH component, 3 SGSVIS (to host), 4 operand (to device),
+// 5 operator result (to host)
 int launch_repack(c3d_channel *ch, int dir, int what, int comp);  // 0: Fortran->device
 void set_error(const std::string &msg);
 // Records a kernel-boundary mark for the profiler and counts the launch.

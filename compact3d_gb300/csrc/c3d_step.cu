@@ -383,6 +383,17 @@ static int step_impl(c3d_channel *ch, double dt, int *nl) {
     return pressure_and_update<R>(ch, a, dd0, dd1, dd2, 1, nl);
 }
 
+template <typename R>
+static int operator_impl(c3d_channel *ch, int op, int *nl) {
+    StepArgs<R> a = make_args<R>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
+    return launch_op<R>(ch, a, op, (const R *)ch->opbuf[0], (R *)ch->opbuf[1], nl);
+}
+
+int launch_operator(c3d_channel *ch, int op, int *nl) {
+    if (ch->precision == C3D_MIXED) return operator_impl<float>(ch, op, nl);
+    return operator_impl<double>(ch, op, nl);
+}
+
 int launch_step(c3d_channel *ch, double dt, int *nl) {
     if (ch->precision == C3D_MIXED) return step_impl<float>(ch, dt, nl);
     return step_impl<double>(ch, dt, nl);
@@ -458,6 +469,18 @@ int launch_repack(c3d_channel *ch, int dir, int what, int comp) {
     cudaStream_t st = ch->stream;
     const bool mixed = ch->precision == C3D_MIXED;
     const int nb = nblk(dir == 0 ? tot_dev : tot_f);
+    if (what == 4 || what == 5) {   // operator operand (to device) / result (to host), working precision
+        void *buf = ch->opbuf[what == 4 ? 0 : 1];
+        if (!buf || (what == 4) != (dir == 0)) return C3D_EINVAL;
+        if (!mixed) {
+            if (dir == 0) k_unpack<double><<<nblk((long long)(g.n2 + 1) * g.np), TPB, 0, st>>>(g, 0, (double *)buf, ch->stage, ToF64());
+            else k_pack<double><<<nb, TPB, 0, st>>>(g, 0, (const double *)buf, ch->stage, FromF64());
+        } else {
+            if (dir == 0) k_unpack<float><<<nblk((long long)(g.n2 + 1) * g.np), TPB, 0, st>>>(g, 0, (float *)buf, ch->stage, ToF32());
+            else k_pack<float><<<nb, TPB, 0, st>>>(g, 0, (const float *)buf, ch->stage, FromF32());
+        }
+        return 0;
+    }
     if (what == 3) {   // SGSVIS (0:M1,0:M2,0:M3), device to host only, working precision
         if (dir == 0 || !ch->les[0]) return C3D_EINVAL;
         if (!mixed) k_pack<double><<<nb, TPB, 0, st>>>(g, 0, (const double *)ch->les[0], ch->stage, FromF64());

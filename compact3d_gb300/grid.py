@@ -217,7 +217,7 @@ WORKLOADS = {
                        re=15000.0, dt=0.001),
     # wall-modelled LES: 128 x 65 x 128 points, 8pi x 2 x 3pi, uniform y (wall model)
     "les128": dict(n1m=128, n2m=64, n3m=128, alx=8 * PI, aly=2.0, alz=3 * PI, cks=1.0,
-                   re=round(re_from_retau(2000.0), 1), dt=0.001, wmodel=1, files=2),
+                   re=round(re_from_retau(2000.0), 1), dt=0.005, wmodel=1, files=2),
     # small wall-modelled LES grids for parity tests (Smagorinsky and dynamic)
     "les32cs": dict(n1m=32, n2m=16, n3m=32, alx=8 * PI, aly=2.0, alz=3 * PI, cks=1.0,
                     re=round(re_from_retau(2000.0), 1), dt=0.002, wmodel=1, files=2),

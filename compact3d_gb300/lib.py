@@ -48,6 +48,9 @@ SIGNATURES = {
     "c3d_set_wsm": (_ip, [_vp, _dp]),
     "c3d_get_wsm": (_ip, [_vp, _dp]),
     "c3d_set_wall_iter_cap": (_ip, [_vp, _ip]),
+    "c3d_op_set": (_ip, [_vp, _dp]),
+    "c3d_op_apply": (_ip, [_vp, _ip, _ip]),
+    "c3d_op_get": (_ip, [_vp, _dp]),
     "c3d_step": (_ip, [_vp, _ip, ctypes.c_double, _dp, _dp]),
     "c3d_diagnose": (_ip, [_vp, ctypes.POINTER(c3d_diag)]),
     "c3d_getup": (_ip, [_vp, _dp, _dp, _dp, _dp, _ip, ctypes.c_double, _dp, _dp]),
@@ -90,6 +93,10 @@ def load(path: str = LIB_PATH):
             f.argtypes = args
         _lib = L
     return _lib
+
+
+# Operators of c3d_op_apply (include/c3d.h)
+OPS = {"DX1": 1, "DX2": 2, "IX": 3, "DZ1": 4, "DZ2": 5, "IZ": 6, "DY1": 7, "DY2": 8, "POISSON": 9}
 
 
 class C3DError(RuntimeError):
@@ -171,6 +178,24 @@ class Channel:
         w = np.zeros(3)
         check(load().c3d_get_wsm(self.h, _p(w)), "c3d_get_wsm")
         return w
+
+    # ---- operators one at a time ----
+    def op_set(self, F):
+        check(load().c3d_op_set(self.h, _p(F)), "c3d_op_set")
+
+    def op_apply(self, op: int, count: int = 1):
+        check(load().c3d_op_apply(self.h, int(op), int(count)), "c3d_op_apply")
+
+    def op_get(self):
+        F = self.grid.zeros_s()
+        check(load().c3d_op_get(self.h, _p(F)), "c3d_op_get")
+        return F
+
+    def operator(self, op: int, F):
+        """One operator on a host field F(0:M1,0:M2,0:M3); returns the result."""
+        self.op_set(F)
+        self.op_apply(op, 1)
+        return self.op_get()
 
     def set_wall_iter_cap(self, cap: int):
         check(load().c3d_set_wall_iter_cap(self.h, int(cap)), "c3d_set_wall_iter_cap")

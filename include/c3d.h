@@ -201,6 +201,38 @@ int c3d_profile_get(c3d_channel *ch, int idx, const char **name, double *ms,
 #define C3D_NOALLOC_MAX_BYTES (64u * 1024u * 1024u)
 int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
 
+/* ---- operators one at a time ---------------------------------------------
+ * No single routine of the reference corresponds: these are the operators inside
+ * RHS1-3 / RHSDP / GETDP, exposed for operator-level checks and measurement.
+ * c3d_op_set    loads one field F(0:M1,0:M2,0:M3) (the layout of one component of U)
+ *               as the operand, converted to the channel's working precision.
+ * c3d_op_apply  applies operator `op` `count` times, each time from the operand to
+ *               the result, asynchronously on the channel's stream (time it with
+ *               c3d_timer_start / c3d_timer_stop).  The result holds J = 1..N2M
+ *               (J = 2..N2M for C3D_OP_DY1); other planes are zero.
+ * c3d_op_get    copies the result back in the same layout (periodic ghost columns
+ *               filled, wall planes zero).
+ *   C3D_OP_DX1  (1,22,1) X = 24 DX1 (F(I+1) - F(I))            CTDMA11, e.g. RHS1 loop 50
+ *   C3D_OP_DX2  (1,10,1) X = 12 DX1^2 (F(I-1) - 2F(I) + F(I+1))  CTDMA11, RHS1 loop 20
+ *   C3D_OP_IX   (1,6,1)  X = 4 (F(I) + F(I+1))                  CTDMA11, RHS1 loop 50
+ *   C3D_OP_DZ1, C3D_OP_DZ2, C3D_OP_IZ   the same along z        CTDMA33
+ *   C3D_OP_DY1  (F(J) - F(J-1)) / H(J)                          RHS2 loop 10
+ *   C3D_OP_DY2  HP(J) F(J+1) - HC(J) F(J) + HM(J) F(J-1)         RHS1 loop 10
+ *   C3D_OP_POISSON  GETDP: DP from RDP = F at J = 1..N2M        compact3d.f:9271-9441
+ */
+#define C3D_OP_DX1      1
+#define C3D_OP_DX2      2
+#define C3D_OP_IX       3
+#define C3D_OP_DZ1      4
+#define C3D_OP_DZ2      5
+#define C3D_OP_IZ       6
+#define C3D_OP_DY1      7
+#define C3D_OP_DY2      8
+#define C3D_OP_POISSON  9
+int c3d_op_set(c3d_channel *ch, const double *f);
+int c3d_op_apply(c3d_channel *ch, int op, int count);
+int c3d_op_get(c3d_channel *ch, double *f);
+
 /* ---- batched ensemble --------------------------------------------------
  * Many independent channels (any mix of grid sizes, RE and precision) that
  * advance together.  c3d_batch_step runs one GETUP on every channel as a single

@@ -63,6 +63,8 @@ def lib():
         L.orc_sgs.argtypes = [vp, dp, dp, dp]
         L.orc_wallmodel.restype = ip
         L.orc_sgs_rhs.restype = ip
+        L.orc_operator.restype = ip
+        L.orc_operator.argtypes = [vp, ip, dp, dp]
         L.orc_sgs_rhs.argtypes = [vp, dp, dp, dp]
         L.orc_wallmodel.argtypes = [vp, dp]
         for f in ("orc_ctdma11", "orc_ctdma_recip"):
@@ -161,6 +163,14 @@ class Oracle:
         HH = self.grid.zeros_u()
         lib().orc_sgs_rhs(self.h, _p(U), _p(sgsvis), _p(HH))
         return HH
+
+    def operator(self, op: int, F):
+        """The operator `op` (C3D_OP_* numbering) on F(0:M1,0:M2,0:M3)."""
+        X = self.grid.zeros_s()
+        rc = lib().orc_operator(self.h, int(op), _p(np.asfortranarray(F)), _p(X))
+        if rc != 0:
+            raise RuntimeError(f"orc_operator failed: {rc}")
+        return X
 
     def wallmodel(self, U):
         """WALLMODEL_INSTANT on U; returns the status (0, or -4 if a point hit the cap)."""

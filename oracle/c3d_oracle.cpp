@@ -2041,6 +2041,72 @@ int orc_sgs_rhs(void *h, const double *U, const double *SGSVIS, double *HH) {
     return 0;
 }
 
+// The operators of c3d_op_apply in the reference's arithmetic: the compact solves by
+// bordered LU (CTDMA11/CTDMA33, compact3d.f:8952-9046) with the right-hand sides of
+// RHS1 loops 20/50, the y stencils of RHS1 loop 10 / RHS2 loop 10, and GETDP.  F and X
+// are (0:M1,0:M2,0:M3); X receives J = 1..N2M (2..N2M for DY1) and zeros elsewhere.
+int orc_operator(void *h, int op, const double *F, double *X) {
+    Orc &g = *(Orc *)h;
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double DX1 = g.DX1, DX3 = g.DX3, DX1Q = g.DX1Q, DX3Q = g.DX3Q;
+    std::memset(X, 0, (size_t)g.su3 * sizeof(double));
+    auto f = [&](int i, int j, int k) { return F[g.iu(i, j, k)]; };
+    ConstLine L;
+    if (op >= 1 && op <= 3) {
+        L.set(N1M, 1.0, op == 1 ? 22.0 : op == 2 ? 10.0 : 6.0, 1.0);
+#pragma omp parallel for
+        for (int K = 1; K <= N3M; K++) {
+            std::vector<double> D(N1M + 1), Y(N1M + 1);
+            for (int J = 1; J <= N2M; J++) {
+                for (int I = 1; I <= N1M; I++) {
+                    const int IP = g.IPA[I], IM = g.IMA[I];
+                    if (op == 1) D[I] = 24. * DX1 * (f(IP, J, K) - f(I, J, K));
+                    else if (op == 2) D[I] = 12. * DX1Q * (f(IM, J, K) - 2. * f(I, J, K) + f(IP, J, K));
+                    else D[I] = 4. * (f(I, J, K) + f(IP, J, K));
+                }
+                ctdma_bordered(N1M, L.A.data(), L.B.data(), L.C.data(), D.data(), Y.data());
+                for (int I = 1; I <= N1M; I++) X[g.iu(I, J, K)] = Y[I];
+            }
+        }
+    } else if (op >= 4 && op <= 6) {
+        L.set(N3M, 1.0, op == 4 ? 22.0 : op == 5 ? 10.0 : 6.0, 1.0);
+#pragma omp parallel for
+        for (int I = 1; I <= N1M; I++) {
+            std::vector<double> D(N3M + 1), Y(N3M + 1);
+            for (int J = 1; J <= N2M; J++) {
+                for (int K = 1; K <= N3M; K++) {
+                    const int KP = g.KPA[K], KM = g.KMA[K];
+                    if (op == 4) D[K] = 24. * DX3 * (f(I, J, KP) - f(I, J, K));
+                    else if (op == 5) D[K] = 12. * DX3Q * (f(I, J, KM) - 2. * f(I, J, K) + f(I, J, KP));
+                    else D[K] = 4. * (f(I, J, K) + f(I, J, KP));
+                }
+                ctdma_bordered(N3M, L.A.data(), L.B.data(), L.C.data(), D.data(), Y.data());
+                for (int K = 1; K <= N3M; K++) X[g.iu(I, J, K)] = Y[K];
+            }
+        }
+    } else if (op == 7 || op == 8) {
+#pragma omp parallel for
+        for (int K = 1; K <= N3M; K++)
+            for (int J = (op == 7 ? 2 : 1); J <= N2M; J++)
+                for (int I = 1; I <= N1M; I++) {
+                    if (op == 7) X[g.iu(I, J, K)] = (f(I, J, K) - f(I, J - 1, K)) / g.H[J];
+                    else X[g.iu(I, J, K)] = g.HP[J] * f(I, J + 1, K) - g.HC[J] * f(I, J, K) + g.HM[J] * f(I, J - 1, K);
+                }
+    } else if (op == 9) {
+        std::vector<double> RDP((size_t)g.sp2 * g.N3, 0.0), DP((size_t)g.sp2 * g.N3, 0.0);
+        for (int K = 1; K <= N3M; K++)
+            for (int J = 1; J <= N2M; J++)
+                for (int I = 1; I <= N1M; I++) RDP[g.ip(I, J, K)] = f(I, J, K);
+        getdp(g, DP.data(), RDP.data());
+        for (int K = 1; K <= N3M; K++)
+            for (int J = 1; J <= N2M; J++)
+                for (int I = 1; I <= N1M; I++) X[g.iu(I, J, K)] = DP[g.ip(I, J, K)];
+    } else {
+        return C3D_EINVAL;
+    }
+    return 0;
+}
+
 // WALLMODEL_INSTANT alone on U (TAUW, TAUB, WSM(1) are updated in the handle).
 int orc_wallmodel(void *h, const double *U) { return wallmodel_instant(*(Orc *)h, U); }
 
