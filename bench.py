@@ -45,7 +45,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 from compact3d_gb300 import ic  # noqa: E402
-from compact3d_gb300.grid import C3D_FP64, C3D_MIXED, WORKLOADS, make_grid  # noqa: E402
+from compact3d_gb300.grid import C3D_FP64, C3D_MIXED, C3D_MIXED_IR, WORKLOADS, make_grid  # noqa: E402
 
 METRIC = "grid-pt-substeps/s on 1 GB300: FP32-mixed & batched vs FP64, at stated L2 err"
 UNIT = "grid-pt-substeps/s"
@@ -215,8 +215,11 @@ def cpu_reference(workload: str, steps: int, warmup: int, budget_s: float = 150.
 # ------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------
+FORMS = {"mixed": C3D_MIXED, "fp64": C3D_FP64, "mixed_ir": C3D_MIXED_IR}
+
+
 def make_channel(lib, g, form, U, P, HH):
-    ch = lib.Channel(g, C3D_MIXED if form == "mixed" else C3D_FP64)
+    ch = lib.Channel(g, FORMS[form])
     ch.upload(U, P, HH)
     ch.project()
     ch.set_presg(0.0, 0.0)
@@ -254,7 +257,7 @@ def run_ours(args, D: Dist):
     value = total_pts * K / (ms_max / 1e3)
     res = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=D.world, steps=K, warmup=W,
                ms_per_step=ms_max / K, higher_is_better=True, scaling="weak", vs_baseline=None,
-               dtype="f32+f64 mixed" if args.form == "mixed" else "f64", data="synthetic")
+               dtype="f64" if args.form == "fp64" else "f32+f64 mixed", data="synthetic")
     res["config"] = dict(workload=f"{args.workload}: {g.n1m}x{g.n2m + 1}x{g.n3m} points "
                                   f"(cells {g.n1m}x{g.n2m}x{g.n3m}), RE={g.re}, dt={dt}, "
                                   f"y tanh-stretched beta={g.cks}",
@@ -288,7 +291,7 @@ def run_ours(args, D: Dist):
                       for e in prof}
 
     # ---- FP64 form in the same run, and the mixed form's error against it ----
-    if args.form == "mixed" and not args.no_fp64:
+    if args.form != "fp64" and not args.no_fp64:
         c64 = make_channel(lib, g, "fp64", U0, P0, HH0)
         m = 1
         for _ in range(W):
@@ -302,6 +305,21 @@ def run_ours(args, D: Dist):
             m += 1
         ms64 = D.max(c64.timer_stop())
         res["fp64"] = dict(value=total_pts * k64 / (ms64 / 1e3), ms_per_step=ms64 / k64, steps=k64)
+        # the other mixed variant (with / without the pressure refinement step)
+        other = "mixed_ir" if args.form == "mixed" else "mixed"
+        co = make_channel(lib, g, other, U0, P0, HH0)
+        m = 1
+        for _ in range(W):
+            co.step_async(m, dt)
+            m += 1
+        co.sync()
+        co.timer_start()
+        for _ in range(K):
+            co.step_async(m, dt)
+            m += 1
+        mso = D.max(co.timer_stop())
+        res[other] = dict(value=total_pts * K / (mso / 1e3), ms_per_step=mso / K, steps=K)
+        co.close()
         c64.close()
         res["err_vs_fp64"] = error_study(lib, g, dt, U0, P0, HH0, args.err_steps, floor=not args.no_floor)
 
@@ -311,7 +329,7 @@ def run_ours(args, D: Dist):
         U, P, HH = U0.copy(order="F"), P0.copy(order="F"), HH0.copy(order="F")
         for a in (U, P, HH):
             L.host_register(a)
-        ce = lib.Channel(g, C3D_MIXED if args.form == "mixed" else C3D_FP64)
+        ce = lib.Channel(g, FORMS[args.form])
         ce.upload(U, P, HH)
         ce.project()
         ce.download(U, P, HH)
@@ -381,7 +399,8 @@ def error_study(lib, g, dt, U0, P0, HH0, steps: int, floor: bool = True):
     def rl(a, b):
         return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
-    runs = {"mixed": make_channel(lib, g, "mixed", U0, P0, HH0), "fp64": make_channel(lib, g, "fp64", U0, P0, HH0)}
+    runs = {"mixed": make_channel(lib, g, "mixed", U0, P0, HH0), "fp64": make_channel(lib, g, "fp64", U0, P0, HH0),
+            "mixed_ir": make_channel(lib, g, "mixed_ir", U0, P0, HH0)}
     if floor:
         rng = np.random.default_rng(ic.SEED0 + 77)
         Up = U0 + 1e-15 * float(np.abs(U0).max()) * rng.standard_normal(U0.shape)
@@ -629,7 +648,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="channel384", choices=sorted(WORKLOADS))
-    ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--form", default="mixed", choices=["mixed", "fp64", "mixed_ir"])
     ap.add_argument("--fp64-steps", type=int, default=5)
     ap.add_argument("--err-steps", type=int, default=20)
     ap.add_argument("--e2e-steps", type=int, default=5)

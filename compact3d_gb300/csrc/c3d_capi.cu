@@ -159,7 +159,7 @@ void free_channel(c3d_channel *ch) {
                     ch->r[2], ch->exy, ch->exz, ch->eyz, ch->ww1, ch->wsq, ch->rdpz, ch->g1,
                     ch->spec, ch->stage, ch->tauw, ch->taub, ch->les[0], ch->les[1], ch->les[2],
                     ch->les[3], ch->les[4], ch->les[5], ch->les[6], ch->les[7], ch->dyn, ch->smagc,
-                    ch->d23, ch->ycs, ch->wpart, ch->coef, ch->d23r, ch->opbuf[0], ch->opbuf[1]};
+                    ch->d23, ch->ycs, ch->wpart, ch->coef, ch->d23r, ch->opbuf[0], ch->opbuf[1], ch->rdydf};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (ch->pinned) cudaFreeHost(ch->pinned);
@@ -277,8 +277,8 @@ int check_grid(const c3d_grid *g) {
         set_error("RE, DX1, DX3, VOL, ALX, ALZ must be positive");
         return C3D_EINVAL;
     }
-    if (g->precision != C3D_FP64 && g->precision != C3D_MIXED) {
-        set_error("precision must be C3D_FP64 or C3D_MIXED");
+    if (g->precision != C3D_FP64 && g->precision != C3D_MIXED && g->precision != C3D_MIXED_IR) {
+        set_error("precision must be C3D_FP64, C3D_MIXED or C3D_MIXED_IR");
         return C3D_EINVAL;
     }
     if (g->files < 0 || g->files > 2) {
@@ -318,7 +318,8 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
     cudaGetDevice(&ch->device);
     cudaDeviceGetAttribute(&ch->nsm, cudaDevAttrMultiProcessorCount, ch->device);
     if (ch->nsm <= 0) ch->nsm = 1;
-    ch->precision = gr->precision;
+    ch->precision = gr->precision == C3D_MIXED_IR ? C3D_MIXED : gr->precision;
+    ch->refine = gr->precision == C3D_MIXED_IR;
     Geo &g = ch->g;
     g.n1m = gr->n1 - 1;
     g.n2m = gr->n2 - 1;
@@ -485,6 +486,13 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
         }
         if (cudaMemcpy(ch->bulkw, pdf.data(), (size_t)m * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)
             return fail(C3D_ECUDA);
+        if (ch->refine) {   // 1/DY(J) for the refinement's residual
+            std::vector<dfl> r(m);
+            for (int j = 1; j < m - 1; ++j) r[j] = dfl::from(1.0 / gr->dy[j]);
+            if (cudaMalloc(&ch->rdydf, (size_t)m * sizeof(dfl)) != cudaSuccess) return fail(C3D_ENOMEM);
+            if (cudaMemcpy(ch->rdydf, r.data(), (size_t)m * sizeof(dfl), cudaMemcpyHostToDevice) != cudaSuccess)
+                return fail(C3D_ECUDA);
+        }
     }
     rc = launch_poisson_tables(ch);
     if (rc) return fail(rc);

@@ -65,6 +65,63 @@ __device__ __forceinline__ T lane_next(T first, int lane, int P) {
     return __shfl_sync(FULL, first, src);
 }
 
+// Double-float value hi + lo (about 48 significant bits) made of FP32 operations: error-
+// free two-sum (Knuth) and FMA-based two-product.  The line solvers are templates on the
+// value type, so the same recurrences run in double-float where a result must be
+// accurate well below FP32 rounding (the residual of the pressure refinement).
+struct dfl {
+    float h, l;
+    __host__ __device__ dfl() : h(0.f), l(0.f) {}
+    __host__ __device__ dfl(float x) : h(x), l(0.f) {}
+    __host__ __device__ dfl(float a, float b) : h(a), l(b) {}
+    static __host__ dfl from(double x) {
+        float a = (float)x;
+        return dfl(a, (float)(x - (double)a));
+    }
+};
+__device__ __forceinline__ dfl dfl_norm(float s, float e) {
+    float h = s + e;
+    return dfl(h, e - (h - s));
+}
+__device__ __forceinline__ dfl operator+(dfl a, dfl b) {
+    float s = a.h + b.h, v = s - a.h;
+    float e = (a.h - (s - v)) + (b.h - v);
+    return dfl_norm(s, e + (a.l + b.l));
+}
+__device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + dfl(-b.h, -b.l); }
+__device__ __forceinline__ dfl operator*(dfl a, dfl b) {
+    float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return dfl_norm(p, e);
+}
+__device__ __forceinline__ dfl operator/(dfl a, dfl b) {
+    float q1 = a.h / b.h;
+    dfl r = a - dfl(q1) * b;
+    float q2 = r.h / b.h;
+    dfl q = dfl_norm(q1, q2);
+    r = a - q * b;
+    return q + dfl(r.h / b.h);
+}
+__device__ __forceinline__ dfl &operator+=(dfl &a, dfl b) { return a = a + b; }
+__device__ __forceinline__ dfl &operator*=(dfl &a, dfl b) { return a = a * b; }
+
+// Warp shuffles for every value type of the line solvers.
+__device__ __forceinline__ double shfl_up(double v, int d) { return __shfl_up_sync(FULL, v, d); }
+__device__ __forceinline__ float shfl_up(float v, int d) { return __shfl_up_sync(FULL, v, d); }
+__device__ __forceinline__ dfl shfl_up(dfl v, int d) {
+    return dfl(__shfl_up_sync(FULL, v.h, d), __shfl_up_sync(FULL, v.l, d));
+}
+__device__ __forceinline__ double shfl_down(double v, int d) { return __shfl_down_sync(FULL, v, d); }
+__device__ __forceinline__ float shfl_down(float v, int d) { return __shfl_down_sync(FULL, v, d); }
+__device__ __forceinline__ dfl shfl_down(dfl v, int d) {
+    return dfl(__shfl_down_sync(FULL, v.h, d), __shfl_down_sync(FULL, v.l, d));
+}
+__device__ __forceinline__ double shfl_idx(double v, int s) { return __shfl_sync(FULL, v, s); }
+__device__ __forceinline__ float shfl_idx(float v, int s) { return __shfl_sync(FULL, v, s); }
+__device__ __forceinline__ dfl shfl_idx(dfl v, int s) { return dfl(__shfl_sync(FULL, v.h, s), __shfl_sync(FULL, v.l, s)); }
+
 // Cyclic solve on the warp's row held as lane chunks x[0..C); in place, returns s*B(F(x)).
 template <typename R, int C>
 __device__ __forceinline__ void xsolve(R (&x)[C], int lane, int P, const Cyc<R> &c) {
@@ -80,16 +137,16 @@ __device__ __forceinline__ void xsolve(R (&x)[C], int lane, int P, const Cyc<R> 
     if (!act) m = R(1);
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-        R ep = __shfl_up_sync(FULL, e, off), mp = __shfl_up_sync(FULL, m, off);
+        R ep = shfl_up(e, off), mp = shfl_up(m, off);
         if (lane >= off) {
             e = e + m * ep;
             m = m * mp;
         }
     }
     {
-        R et = __shfl_sync(FULL, e, 31), mt = __shfl_sync(FULL, m, 31);
+        R et = shfl_idx(e, 31), mt = shfl_idx(m, 31);
         R y0 = et / (R(1) - mt);
-        R ex = __shfl_up_sync(FULL, e, 1), mx = __shfl_up_sync(FULL, m, 1);
+        R ex = shfl_up(e, 1), mx = shfl_up(m, 1);
         y = (lane == 0) ? y0 : ex + mx * y0;
     }
 #pragma unroll
@@ -108,16 +165,16 @@ __device__ __forceinline__ void xsolve(R (&x)[C], int lane, int P, const Cyc<R> 
     if (!act) m = R(1);
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-        R en = __shfl_down_sync(FULL, e, off), mn = __shfl_down_sync(FULL, m, off);
+        R en = shfl_down(e, off), mn = shfl_down(m, off);
         if (lane + off < 32) {
             e = e + m * en;
             m = m * mn;
         }
     }
     {
-        R e0 = __shfl_sync(FULL, e, 0), m0 = __shfl_sync(FULL, m, 0);
+        R e0 = shfl_idx(e, 0), m0 = shfl_idx(m, 0);
         R z0 = e0 / (R(1) - m0);
-        R en1 = __shfl_down_sync(FULL, e, 1), mn1 = __shfl_down_sync(FULL, m, 1);
+        R en1 = shfl_down(e, 1), mn1 = shfl_down(m, 1);
         z = (lane == 31) ? z0 : en1 + mn1 * z0;
     }
     const R s = c.s;

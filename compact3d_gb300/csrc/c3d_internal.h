@@ -83,6 +83,16 @@ enum {
     SCAL_COUNT = 16
 };
 
+// Arguments of the pressure refinement (mixed form with C3D_MIXED_IR): double-float
+// constants of RHSDP's operators and the scratch for the z part of the residual.
+struct RefArgs {
+    dfl f24x, f24z, rdt;       // 24 DX1, 24 DX3, 1/DT
+    Cyc<dfl> c22x, c22z;       // (1,22,1) solves
+    const dfl *rdy;            // 1/DY(J)
+    float *rzh, *rzl;          // Dz(w) as double-float pairs
+    int updp;                  // add DP2 to P (GETUP) or not (projection)
+};
+
 // Arguments of the LES kernels (FILES != 0): fields in the working precision R, plane
 // layout like the state; face quantities are stored at the index of their Fortran owner.
 template <typename R>
@@ -152,6 +162,8 @@ struct c3d_channel {
     void *coef, *d23r;        // per-J tables in R
     int wall_cap;
     void *opbuf[2];           // operand and result of c3d_op_* (R, full fields)
+    int refine;               // mixed form: one refinement step of the pressure solve
+    c3d::dfl *rdydf;          // 1/DY(J) as double-float pairs (refinement)
     // per-kernel profiler (CUDA events around every launch when enabled)
     int prof_on;
     int prof_n;                              // events recorded in the current step
@@ -182,6 +194,7 @@ int launch_step(c3d_channel *ch, double dt, int *launches);
 int launch_operator(c3d_channel *ch, int op, int *launches);
 template <typename R>
 int launch_op(c3d_channel *ch, StepArgs<R> &a, int op, const R *in, R *out, int *nl);   // c3d_ops.cu
+int launch_refine(c3d_channel *ch, StepArgs<float> &a, RefArgs &r, int *nl);            // c3d_refine.cu
 int launch_project(c3d_channel *ch, int *launches);
 int launch_diag(c3d_channel *ch, int *launches);
 int launch_poisson_tables(c3d_channel *ch);

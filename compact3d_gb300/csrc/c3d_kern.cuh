@@ -101,6 +101,7 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
 // Warp shuffles for every state/working type
 __device__ __forceinline__ double shfl_any(double v, int src) { return __shfl_sync(FULL, v, src); }
 __device__ __forceinline__ float shfl_any(float v, int src) { return __shfl_sync(FULL, v, src); }
+__device__ __forceinline__ dfl shfl_any(dfl v, int src) { return shfl_idx(v, src); }
 __device__ __forceinline__ float2 shfl_any(float2 v, int src) {
     return make_float2(__shfl_sync(FULL, v.x, src), __shfl_sync(FULL, v.y, src));
 }

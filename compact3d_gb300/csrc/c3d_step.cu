@@ -332,6 +332,36 @@ static int pressure_and_update(c3d_channel *ch, StepArgs<R> &a, R *d0, R *d1, R 
     return launch_zpass<R>(ch, a, 4, d0, d1, d2, updp, nl);                   // zE
 }
 
+static RefArgs make_ref_args(c3d_channel *ch, double dt, int updp) {
+    RefArgs r;
+    r.updp = updp;
+    const double b = 22.0, rt = -2.0 / (b + sqrt(b * b - 4.0));
+    r.f24x = dfl::from(24.0 * ch->g.dx1);
+    r.f24z = dfl::from(24.0 * ch->g.dx3);
+    r.rdt = dfl::from(1.0 / dt);
+    r.c22x.r = dfl::from(rt);
+    r.c22x.s = dfl::from(-rt);
+    r.c22x.m = 13;
+    r.c22z = r.c22x;
+    r.rdy = ch->rdydf;
+    r.rzh = (float *)ch->exz;
+    r.rzl = (float *)ch->eyz;
+    return r;
+}
+
+// One refinement step of the pressure solve after UPCALC (mixed form, C3D_MIXED_IR).
+template <typename R>
+static int refine_pressure(c3d_channel *ch, StepArgs<R> &a, int updp, int *nl) {
+    if constexpr (sizeof(R) == 4) {
+        if (!ch->refine) return 0;
+        RefArgs r = make_ref_args(ch, a.dt, updp);
+        return launch_refine(ch, a, r, nl);
+    } else {
+        (void)ch; (void)a; (void)updp; (void)nl;
+        return 0;
+    }
+}
+
 template <typename R>
 static LesArgs<R> make_les_args(c3d_channel *ch) {
     LesArgs<R> l;
@@ -380,7 +410,8 @@ static int step_impl(c3d_channel *ch, double dt, int *nl) {
     // deltas go to exz/eyz/wsq, which the RHS passes no longer need
     R *dd0 = (R *)ch->exz, *dd1 = (R *)ch->eyz, *dd2 = (R *)ch->wsq;
     if ((rc = launch_zpass<R>(ch, a, 2, dd0, dd1, dd2, 0, nl))) return rc;    // zC
-    return pressure_and_update<R>(ch, a, dd0, dd1, dd2, 1, nl);
+    if ((rc = pressure_and_update<R>(ch, a, dd0, dd1, dd2, 1, nl))) return rc;
+    return refine_pressure<R>(ch, a, 1, nl);
 }
 
 template <typename R>
@@ -412,7 +443,9 @@ static int project_impl(c3d_channel *ch, int *nl) {
     cudaMemsetAsync(dd2, 0, bytes, ch->stream);
     k_bcond<R><<<nblk(ch->g.np), TPB, 0, ch->stream>>>(ch->g, (S *)ch->u, (S *)ch->v, (S *)ch->w);
     mark(ch, nl, "bcond", 64.0 * ch->g.np);
-    return pressure_and_update<R>(ch, a, dd0, dd1, dd2, 0, nl);
+    int rc = pressure_and_update<R>(ch, a, dd0, dd1, dd2, 0, nl);
+    if (rc) return rc;
+    return refine_pressure<R>(ch, a, 0, nl);
 }
 
 int launch_project(c3d_channel *ch, int *nl) {

@@ -20,6 +20,7 @@ import numpy as np
 
 C3D_FP64 = 0
 C3D_MIXED = 1
+C3D_MIXED_IR = 2
 
 
 class c3d_grid(ctypes.Structure):

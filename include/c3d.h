@@ -44,6 +44,11 @@ extern "C" {
 #define C3D_FP64   0   /* every operation in FP64                              */
 #define C3D_MIXED  1   /* FP32 line solves / RHS / FFT; FP64 state, reductions,
                           low-wavenumber Poisson modes and bulk-flow constraint */
+#define C3D_MIXED_IR 2 /* C3D_MIXED plus one step of iterative refinement of the
+                          pressure solve: the residual div(U)/DT of the corrected
+                          field in double-float arithmetic, a second solve and
+                          update; the projected field is divergence-free to about
+                          FP64 rounding */
 
 /*
  * Grid and model description.  It carries the values the reference keeps in
