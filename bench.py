@@ -236,6 +236,7 @@ def run_ours(args, D: Dist):
 
     # ---- main form, device-resident (value) ----
     ch = make_channel(lib, g, args.form, U0, P0, HH0)
+    schedule = ch.autotune() if not args.no_tune else ch.get_schedule()
     n = 1
     for _ in range(W):
         ch.step_async(n, dt)
@@ -266,6 +267,7 @@ def run_ours(args, D: Dist):
                                    f"{8 * g.n1m * (g.n2m + 2) * g.n3m / 1e6:.0f} MB",
                          parallelism=f"replicas x{D.world}")
     res["gpu_launches"] = launches_per_step * K
+    res["schedule"] = schedule
     if ck:
         res["clocks"] = ck
 
@@ -293,6 +295,8 @@ def run_ours(args, D: Dist):
     # ---- FP64 form in the same run, and the mixed form's error against it ----
     if args.form != "fp64" and not args.no_fp64:
         c64 = make_channel(lib, g, "fp64", U0, P0, HH0)
+        if not args.no_tune:
+            c64.autotune()
         m = 1
         for _ in range(W):
             c64.step_async(m, dt)
@@ -308,6 +312,8 @@ def run_ours(args, D: Dist):
         # the other mixed variant (with / without the pressure refinement step)
         other = "mixed_ir" if args.form == "mixed" else "mixed"
         co = make_channel(lib, g, other, U0, P0, HH0)
+        if not args.no_tune:
+            co.autotune()
         m = 1
         for _ in range(W):
             co.step_async(m, dt)
@@ -451,6 +457,8 @@ def run_les(args, D: Dist):
     flush = L2Flush(D.local)
     for form in ("mixed", "fp64"):
         ch = make_channel(lib, g, form, U0, P0, HH0)
+        if not args.no_tune:
+            ch.autotune()
         n = 1
         for _ in range(max(3, args.warmup)):
             ch.step_async(n, dt)
@@ -578,6 +586,8 @@ def run_batched(args, D: Dist):
     for ch, (U, P, HH) in zip(b.channels, ics):
         ch.upload(U, P, HH)
         ch.project()
+        if not args.no_tune:
+            ch.autotune()   # per grid shape, cached; before the first step captures the graph
     n = len(grids)
     dts = [dt] * n
     p, p3 = [0.0] * n, [0.0] * n
@@ -612,6 +622,8 @@ def run_batched(args, D: Dist):
         U, P, HH = ics[i]
         c.upload(U, P, HH)
         c.project()
+        if not args.no_tune:
+            c.autotune()
         c.set_presg(0.0, 0.0)
         for s_ in range(1, 3):
             c.step_async(s_, dt)
@@ -659,6 +671,7 @@ def main():
     ap.add_argument("--no-floor", action="store_true")
     ap.add_argument("--no-les", action="store_true")
     ap.add_argument("--no-ops", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--les-steps", type=int, default=200)
     ap.add_argument("--nchan", type=int, default=32)
     args = ap.parse_args()

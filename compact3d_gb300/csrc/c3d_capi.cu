@@ -6,6 +6,9 @@
 #include <string.h>
 #include <string>
 #include <algorithm>
+#include <array>
+#include <map>
+#include <mutex>
 #include <vector>
 #include "../../include/c3d.h"
 #include "c3d_internal.h"
@@ -121,14 +124,23 @@ bool fft_len_ok(int n) {
     return n == 1;
 }
 
-FftPlan make_plan(int n) {
+// Stockham plan of length n = 2^a 3^b: the radices in the order the passes run.
+//   variant 0: radix 4 while possible, then 2, then 3
+//   variant 1: radix 3 first, then 4, then 2
+//   variant 2: radix 2 only, then 3
+FftPlan make_plan(int n, int variant) {
     FftPlan p;
     memset(&p, 0, sizeof(p));
     p.n = n;
-    int m = n;
-    while (m % 4 == 0) { p.rad[p.nst++] = 4; m /= 4; }
+    int m = n, e3 = 0;
+    while (m % 3 == 0) { m /= 3; ++e3; }
+    if (variant == 1)
+        for (int q = 0; q < e3; ++q) p.rad[p.nst++] = 3;
+    if (variant != 2)
+        while (m % 4 == 0) { p.rad[p.nst++] = 4; m /= 4; }
     while (m % 2 == 0) { p.rad[p.nst++] = 2; m /= 2; }
-    while (m % 3 == 0) { p.rad[p.nst++] = 3; m /= 3; }
+    if (variant != 1)
+        for (int q = 0; q < e3; ++q) p.rad[p.nst++] = 3;
     return p;
 }
 
@@ -320,6 +332,22 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
     if (ch->nsm <= 0) ch->nsm = 1;
     ch->precision = gr->precision == C3D_MIXED_IR ? C3D_MIXED : gr->precision;
     ch->refine = gr->precision == C3D_MIXED_IR;
+    {   // the creation grid, with its metric arrays copied (scratch channels of the autotuner)
+        const int n2 = gr->n2;
+        ch->grid_arrays.resize(2 * (size_t)(n2 + 1) + 7 * (size_t)n2);
+        double *q = ch->grid_arrays.data();
+        ch->grid_copy = *gr;
+        auto cp = [&](const double *src, size_t n) { std::copy(src, src + n, q); const double *r = q; q += n; return r; };
+        ch->grid_copy.y = cp(gr->y, n2 + 1);
+        ch->grid_copy.dy = cp(gr->dy, n2 + 1);
+        ch->grid_copy.h = cp(gr->h, n2);
+        ch->grid_copy.hm = cp(gr->hm, n2);
+        ch->grid_copy.hc = cp(gr->hc, n2);
+        ch->grid_copy.hp = cp(gr->hp, n2);
+        ch->grid_copy.dym = cp(gr->dym, n2);
+        ch->grid_copy.dyc = cp(gr->dyc, n2);
+        ch->grid_copy.dyp = cp(gr->dyp, n2);
+    }
     Geo &g = ch->g;
     g.n1m = gr->n1 - 1;
     g.n2m = gr->n2 - 1;
@@ -497,8 +525,9 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
     rc = launch_poisson_tables(ch);
     if (rc) return fail(rc);
     // FFT plans and twiddles: [x: N1M/2][z: N3M][x post-processing: N1M/2+1]
-    ch->fx = make_plan(g.n1m / 2);
-    ch->fz = make_plan(g.n3m);
+    ch->tune = Tune{{16, 16, 16, 16, 16}, 4, 8, 0, 0};
+    ch->fx = make_plan(g.n1m / 2, 0);
+    ch->fz = make_plan(g.n3m, 0);
     const int nx = g.n1m / 2, nz = g.n3m, np = g.n1m / 2 + 1;
     std::vector<double2> tw(nx + nz + np);
     std::vector<float2> tw32(nx + nz + np);
@@ -914,6 +943,144 @@ int c3d_last_step_stats(c3d_channel *ch, double *ms, int *launches) {
     if (ms) *ms = ch->last_ms;
     if (launches) *launches = ch->last_launches;
     return 0;
+}
+
+// ---- launch-schedule autotuner --------------------------------------------------
+// The knobs of Tune are tried one group at a time on a scratch channel of the same grid
+// and form holding a copy of the channel's state; each candidate runs one warm-up step
+// and three profiled steps, and the candidate with the least summed time of the kernels
+// the knob affects is kept.  Results are cached per (grid shape, form, models, device).
+}  // extern "C"
+
+namespace {
+std::mutex g_tune_mu;
+std::map<std::array<int, 8>, Tune> g_tune_cache;
+
+std::array<int, 8> tune_key(const c3d_channel *ch) {
+    return {ch->g.n1m, ch->g.n2m, ch->g.n3m, ch->precision, ch->refine, ch->files, ch->wmodel, ch->device};
+}
+
+bool tune_ok(const c3d_channel *ch, const Tune &t) {
+    bool zl = true;
+    for (int q = 0; q < 5; ++q) zl = zl && (t.zl[q] == 8 || t.zl[q] == 16 || (t.zl[q] == 32 && ch->g.n3m % 32 == 0));
+    const bool xw = t.xw == 2 || t.xw == 4 || t.xw == 8;
+    const bool tw = t.twz == 4 || t.twz == 8 || t.twz == 16;
+    return zl && xw && tw && t.fxp >= 0 && t.fxp <= 2 && t.fzp >= 0 && t.fzp <= 2;
+}
+
+// Sets the schedule; the FFT plans get the new radix order and keep their twiddle tables.
+void apply_tune(c3d_channel *ch, const Tune &t) {
+    ch->tune = t;
+    FftPlan fx = make_plan(ch->g.n1m / 2, t.fxp), fz = make_plan(ch->g.n3m, t.fzp);
+    fx.tw64 = ch->fx.tw64;
+    fx.tw32 = ch->fx.tw32;
+    fz.tw64 = ch->fz.tw64;
+    fz.tw32 = ch->fz.tw32;
+    ch->fx = fx;
+    ch->fz = fz;
+}
+
+int time_schedule(c3d_channel *sc, const Tune &t, double dt, const std::vector<std::string> &names, double *cost) {
+    apply_tune(sc, t);
+    int rc = step_common(sc, dt, nullptr, nullptr, true);
+    if (rc && rc != C3D_ENOTCONV) return rc;
+    c3d_profile(sc, 1);
+    for (int q = 0; q < 3 && !rc; ++q) rc = step_common(sc, dt, nullptr, nullptr, false);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(sc->stream));
+    double c = 0.0;
+    for (size_t q = 0; q < sc->prof_name.size(); ++q)
+        for (const std::string &n : names)
+            if (sc->prof_name[q] == n) c += sc->prof_ms[q];
+    c3d_profile(sc, 0);
+    *cost = c;
+    return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int c3d_get_schedule(c3d_channel *ch, int *sched) {
+    if (!ch || !sched) { set_error("null argument"); return C3D_EINVAL; }
+    const Tune &t = ch->tune;
+    for (int q = 0; q < 5; ++q) sched[q] = t.zl[q];
+    sched[5] = t.xw; sched[6] = t.twz; sched[7] = t.fxp; sched[8] = t.fzp;
+    return 0;
+}
+
+int c3d_set_schedule(c3d_channel *ch, const int *sched) {
+    if (!ch || !sched) { set_error("null argument"); return C3D_EINVAL; }
+    Tune t{{sched[0], sched[1], sched[2], sched[3], sched[4]}, sched[5], sched[6], sched[7], sched[8]};
+    if (!tune_ok(ch, t)) { set_error("invalid schedule"); return C3D_EINVAL; }
+    apply_tune(ch, t);
+    return 0;
+}
+
+int c3d_autotune(c3d_channel *ch, int *sched) {
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    if (!ch->have_state) { set_error("c3d_upload must be called before c3d_autotune"); return C3D_ESTATE; }
+    cudaSetDevice(ch->device);
+    const std::array<int, 8> key = tune_key(ch);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            apply_tune(ch, it->second);
+            return sched ? c3d_get_schedule(ch, sched) : 0;
+        }
+    }
+    CK(cudaStreamSynchronize(ch->stream));
+    c3d_grid gs = ch->grid_copy;
+    c3d_channel *sc = nullptr;
+    int rc = c3d_create(&gs, &sc);
+    if (rc) return rc;
+    const size_t rs = ch->precision == C3D_MIXED ? 4 : 8, nf = (size_t)ch->g.nf;
+    void *src[] = {ch->u, ch->v, ch->w, ch->p}, *dst[] = {sc->u, sc->v, sc->w, sc->p};
+    for (int q = 0; q < 4; ++q) cudaMemcpy(dst[q], src[q], nf * 8, cudaMemcpyDeviceToDevice);
+    for (int b = 0; b < 2; ++b)
+        for (int c = 0; c < 3; ++c) cudaMemcpy(sc->hh[b][c], ch->hh[b][c], nf * rs, cudaMemcpyDeviceToDevice);
+    cudaMemcpy(sc->scal, ch->scal, SCAL_COUNT * 8, cudaMemcpyDeviceToDevice);
+    if (ch->files != 0) {
+        cudaMemcpy(sc->tauw, ch->tauw, 2 * (size_t)ch->g.np * 8, cudaMemcpyDeviceToDevice);
+        cudaMemcpy(sc->taub, ch->taub, 2 * (size_t)ch->g.np * 8, cudaMemcpyDeviceToDevice);
+    }
+    sc->have_state = 1;
+    const double dt = ch->dt_cached > 0 ? ch->dt_cached : 1e-3;
+    // knob q: 0-4 the segment length of zA..zE, 5 x rows per block, 6 z-FFT tile, 7/8 plans
+    struct Group { int knob; std::vector<int> cand; std::vector<std::string> kernels; };
+    const Group groups[] = {
+        {0, {8, 16, 32}, {"zA"}}, {1, {8, 16, 32}, {"zB"}}, {2, {8, 16, 32}, {"zC"}},
+        {3, {8, 16, 32}, {"zD"}}, {4, {8, 16, 32}, {"zE"}},
+        {5, {2, 4, 8}, {"xA", "xB", "xC", "xD"}},
+        {6, {4, 8, 16}, {"fftz_fwd", "fftz_inv"}},
+        {8, {0, 1, 2}, {"fftz_fwd", "fftz_inv"}},
+        {7, {0, 1, 2}, {"xC", "xD"}},
+    };
+    auto knob = [](Tune &t, int q) -> int & {
+        return q < 5 ? t.zl[q] : q == 5 ? t.xw : q == 6 ? t.twz : q == 7 ? t.fxp : t.fzp;
+    };
+    Tune best = ch->tune;
+    for (const Group &gp : groups) {
+        double bcost = 1e300;
+        int bval = knob(best, gp.knob);
+        for (int v : gp.cand) {
+            Tune t = best;
+            knob(t, gp.knob) = v;
+            if (!tune_ok(ch, t)) continue;
+            double cost = 0.0;
+            rc = time_schedule(sc, t, dt, gp.kernels, &cost);
+            if (rc) { c3d_destroy(sc); return rc; }
+            if (cost < bcost) { bcost = cost; bval = v; }
+        }
+        knob(best, gp.knob) = bval;
+    }
+    c3d_destroy(sc);
+    apply_tune(ch, best);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = best;
+    }
+    return sched ? c3d_get_schedule(ch, sched) : 0;
 }
 
 // ---- batched ensemble ----------------------------------------------------------

@@ -83,6 +83,19 @@ enum {
     SCAL_COUNT = 16
 };
 
+// Launch schedule of one channel, chosen by c3d_autotune per grid shape.
+//   zl   z-line segment length of each z pass (zA, zB, zC, zD, zE): each thread runs the
+//        recurrences sequentially over zl points (plus the warm-up), the N3M/zl segments
+//        of a line run in parallel; this is the split between the sequential (Thomas)
+//        and the parallel part of the z solves
+//   xw   rows (warps) per block of the x passes
+//   twz  kx columns per block of the z FFT
+//   fxp, fzp  radix order of the x and z FFT plans (0: radix 4 first, 1: radix 3 first,
+//        2: radix 2 only before 3)
+struct Tune {
+    int zl[5], xw, twz, fxp, fzp;
+};
+
 // Arguments of the pressure refinement (mixed form with C3D_MIXED_IR): double-float
 // constants of RHSDP's operators and the scratch for the z part of the residual.
 struct RefArgs {
@@ -163,6 +176,9 @@ struct c3d_channel {
     int wall_cap;
     void *opbuf[2];           // operand and result of c3d_op_* (R, full fields)
     int refine;               // mixed form: one refinement step of the pressure solve
+    c3d::Tune tune;           // launch schedule (c3d_autotune)
+    c3d_grid grid_copy;       // the creation grid with copies of its metric arrays,
+    std::vector<double> grid_arrays;   // used to build scratch channels for tuning
     c3d::dfl *rdydf;          // 1/DY(J) as double-float pairs (refinement)
     // per-kernel profiler (CUDA events around every launch when enabled)
     int prof_on;

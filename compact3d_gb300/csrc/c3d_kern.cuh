@@ -8,6 +8,7 @@
 namespace c3d {
 
 constexpr int TPB = 128;
+constexpr int XMAXT = 256;   // largest block of the tunable x passes (8 rows)
 
 // ---------------------------------------------------------------------------------
 // State representation.
@@ -338,6 +339,5 @@ __device__ __forceinline__ bool zcoord(const Geo &g, int jlo, int &i, int &j, in
 }
 
 constexpr int ZL = 16;   // z segment length
-constexpr int TWZ = 8;   // kx columns per CTA in the z FFT
 
 }  // namespace c3d

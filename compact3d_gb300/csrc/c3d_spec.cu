@@ -4,28 +4,28 @@
 
 namespace c3d {
 
-// Complex FFT along kz of a tile of TWZ kx columns of one plane, in shared memory.
+// Complex FFT along kz of a tile of `tw` kx columns of one plane, in shared memory.
 template <typename R>
-__global__ void __launch_bounds__(TPB) k_fftz(StepArgs<R> a, int sign) {
+__global__ void __launch_bounds__(TPB) k_fftz(StepArgs<R> a, int sign, int tw) {
     typedef typename Cx<R>::T C2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Geo g = a.g;
     const int n = g.n3m;
-    C2 *A = reinterpret_cast<C2 *>(smem_raw), *B = A + n * TWZ;
-    const int ntile = (g.n1h + TWZ - 1) / TWZ;
+    C2 *A = reinterpret_cast<C2 *>(smem_raw), *B = A + n * tw;
+    const int ntile = (g.n1h + tw - 1) / tw;
     const int plane = blockIdx.x / ntile, tile = blockIdx.x % ntile;
-    const int kx0 = tile * TWZ;
-    const int w = min(TWZ, g.n1h - kx0);
+    const int kx0 = tile * tw;
+    const int w = min(tw, g.n1h - kx0);
     C2 *S = reinterpret_cast<C2 *>(a.spec) + (long long)plane * n * g.n1h + kx0;
-    for (int e = threadIdx.x; e < n * TWZ; e += blockDim.x) {
-        int q = e / TWZ, l = e % TWZ;
+    for (int e = threadIdx.x; e < n * tw; e += blockDim.x) {
+        int q = e / tw, l = e % tw;
         if (l < w) A[e] = S[(long long)q * g.n1h + l];
         else { A[e].x = 0; A[e].y = 0; }
     }
     __syncthreads();
-    C2 *Z = fft_smem<C2, true>(A, B, a.fz, TWZ, TWZ, 1, sign, threadIdx.x, blockDim.x);
-    for (int e = threadIdx.x; e < n * TWZ; e += blockDim.x) {
-        int q = e / TWZ, l = e % TWZ;
+    C2 *Z = fft_smem<C2, true>(A, B, a.fz, tw, tw, 1, sign, threadIdx.x, blockDim.x);
+    for (int e = threadIdx.x; e < n * tw; e += blockDim.x) {
+        int q = e / tw, l = e % tw;
         if (l < w) S[(long long)q * g.n1h + l] = Z[e];
     }
 }
@@ -174,10 +174,12 @@ __global__ void k_ptables(Geo g, const double *ak1, const double *ak3, const dou
     }
 }
 
+constexpr int TWZ_MAX = 16;   // widest z-FFT tile the autotuner tries
+
 template <typename R>
 void set_spec_smem(c3d_channel *ch) {
     typedef typename Cx<R>::T C2;
-    const size_t smz = 2 * (size_t)ch->g.n3m * TWZ * sizeof(C2);
+    const size_t smz = 2 * (size_t)ch->g.n3m * TWZ_MAX * sizeof(C2);
     cudaFuncSetAttribute(k_fftz<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
 }
 
@@ -186,16 +188,17 @@ int launch_spec(c3d_channel *ch, StepArgs<R> &a, int which, int *nl) {
     typedef typename Cx<R>::T C2;
     cudaStream_t st = ch->stream;
     const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
-    const int ntile = (ch->g.n1h + TWZ - 1) / TWZ;
-    const size_t smz = 2 * (size_t)ch->g.n3m * TWZ * sizeof(C2);
+    const int tw = ch->tune.twz;
+    const int ntile = (ch->g.n1h + tw - 1) / tw;
+    const size_t smz = 2 * (size_t)ch->g.n3m * tw * sizeof(C2);
     switch (which) {
-        case 0: k_fftz<R><<<ch->g.n2m * ntile, TPB, smz, st>>>(a, -1); mark(ch, nl, "fftz_fwd", N * 2 * Rb); break;
+        case 0: k_fftz<R><<<ch->g.n2m * ntile, TPB, smz, st>>>(a, -1, tw); mark(ch, nl, "fftz_fwd", N * 2 * Rb); break;
         case 1:
             if constexpr (sizeof(R) == 8) k_poisson64<<<nblk((long long)ch->g.n1h * ch->g.n3m), TPB, 0, st>>>(a);
             else k_poisson32<<<nblk((long long)ch->g.n1h * ch->g.n3m), TPB, 0, st>>>(a);
             mark(ch, nl, "poisson", N * 2 * Rb + N * 8);
             break;
-        case 2: k_fftz<R><<<ch->g.n2m * ntile, TPB, smz, st>>>(a, +1); mark(ch, nl, "fftz_inv", N * 2 * Rb); break;
+        case 2: k_fftz<R><<<ch->g.n2m * ntile, TPB, smz, st>>>(a, +1, tw); mark(ch, nl, "fftz_inv", N * 2 * Rb); break;
         default: return C3D_EINVAL;
     }
     return 0;

@@ -16,7 +16,7 @@ namespace c3d {
 // xA
 // ---------------------------------------------------------------------------------
 template <typename R, int C>
-__global__ void __launch_bounds__(TPB) k_xA(StepArgs<R> a) {
+__global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
     typedef typename SType<R>::S S;
     typedef St<R> ST;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(TPB) k_xA(StepArgs<R> a) {
     const int nrows = g.n2m * g.n3m;
     const R RE1 = a.re1, f12 = a.f12x, f24 = a.f24x, four = (R)4.0;
     const R presg = (R)a.scal[SCAL_PRESG];
-    for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
+    for (int row = blockIdx.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += gridDim.x * (int)(blockDim.x >> 5)) {
         const int j = 1 + row / g.n3m, k = row % g.n3m;
         const long long o = fidx(g, 0, j, k), om = fidx(g, 0, j - 1, k), op = fidx(g, 0, j + 1, k);
         {   // every row this warp reads, requested from DRAM at once
@@ -184,7 +184,7 @@ __device__ __forceinline__ void ab2_cnx(const StepArgs<R> &a, int c, long long o
 }
 
 template <typename R, int C>
-__global__ void __launch_bounds__(TPB) k_xB(StepArgs<R> a) {
+__global__ void __launch_bounds__(XMAXT) k_xB(StepArgs<R> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Geo g = a.g;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(TPB) k_xB(StepArgs<R> a) {
     const int nrows = g.n2m * g.n3m;
     const R f = a.f24x;
     const R dt = (R)a.dt;
-    for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
+    for (int row = blockIdx.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += gridDim.x * (int)(blockDim.x >> 5)) {
         const int j = 1 + row / g.n3m, k = row % g.n3m;
         const long long o = fidx(g, 0, j, k), op = fidx(g, 0, j + 1, k);
         {
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(TPB) k_xB(StepArgs<R> a) {
 // xC: RDP = div(UH)/DT and its real-to-complex FFT along x
 // ---------------------------------------------------------------------------------
 template <typename R, int C>
-__global__ void __launch_bounds__(TPB) k_xC(StepArgs<R> a, const R *d0, const R *d1) {
+__global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const R *d1) {
     typedef typename SType<R>::S S;
     typedef typename Cx<R>::T C2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(TPB) k_xC(StepArgs<R> a, const R *d0, const R 
     const C2 *twx;
     if constexpr (sizeof(R) == 8) twx = reinterpret_cast<const C2 *>(a.twx64);
     else twx = reinterpret_cast<const C2 *>(a.twx32);
-    for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
+    for (int row = blockIdx.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += gridDim.x * (int)(blockDim.x >> 5)) {
         const int j = 1 + row / g.n3m, k = row % g.n3m;
         const long long o = fidx(g, 0, j, k), op = fidx(g, 0, j + 1, k);
         {
@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(TPB) k_xC(StepArgs<R> a, const R *d0, const R 
 // xD: complex-to-real FFT -> DP, compact dDP/dx, bulk-flow partial sums
 // ---------------------------------------------------------------------------------
 template <typename R, int C>
-__global__ void __launch_bounds__(TPB) k_xD(StepArgs<R> a, const R *d0, const R *d2) {
+__global__ void __launch_bounds__(XMAXT) k_xD(StepArgs<R> a, const R *d0, const R *d2) {
     typedef typename Cx<R>::T C2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Geo g = a.g;
@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(TPB) k_xD(StepArgs<R> a, const R *d0, const R 
     if constexpr (sizeof(R) == 8) twx = reinterpret_cast<const C2 *>(a.twx64);
     else twx = reinterpret_cast<const C2 *>(a.twx32);
     const R scale = (R)(1.0 / ((double)g.n1m * (double)g.n3m)), f24 = a.f24x;
-    for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
+    for (int row = blockIdx.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += gridDim.x * (int)(blockDim.x >> 5)) {
         const int j = 1 + row / g.n3m, k = row % g.n3m;
         const long long o = fidx(g, 0, j, k);
         const C2 *Sp = reinterpret_cast<const C2 *>(a.spec) + ((long long)(j - 1) * g.n3m + k) * g.n1h;
@@ -541,31 +541,32 @@ template <typename R, int C>
 static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl) {
     typedef typename Cx<R>::T C2;
     const int nrows = ch->g.n2m * ch->g.n3m;
-    const int grid = nblk(nrows, TPB / 32);
+    const int xw = (which == 4) ? TPB / 32 : ch->tune.xw;   // rows (warps) per block
+    const int grid = nblk(nrows, xw), nt = xw * 32;
     cudaStream_t st = ch->stream;
     const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
-    const size_t sb = stage_bytes(ch->g.n1m, C) * (TPB / 32);
+    const size_t sb = stage_bytes(ch->g.n1m, C) * xw;
     const int M = ch->g.n1m / 2;
-    const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(M + 1) * sizeof(C2)) * (TPB / 32);
+    const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(M + 1) * sizeof(C2)) * xw;
     switch (which) {
         case 0:
             cudaFuncSetAttribute(k_xA<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
-            k_xA<R, C><<<grid, TPB, sb, st>>>(a);
+            k_xA<R, C><<<grid, nt, sb, st>>>(a);
             mark(ch, nl, "xA", N * (32 + 7 * Rb));
             break;
         case 1:
             cudaFuncSetAttribute(k_xB<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
-            k_xB<R, C><<<grid, TPB, sb, st>>>(a);
+            k_xB<R, C><<<grid, nt, sb, st>>>(a);
             mark(ch, nl, "xB", N * 18 * Rb);
             break;
         case 2:
             cudaFuncSetAttribute(k_xC<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
-            k_xC<R, C><<<grid, TPB, fb, st>>>(a, p0, p1);
+            k_xC<R, C><<<grid, nt, fb, st>>>(a, p0, p1);
             mark(ch, nl, "xC", N * (16 + 4 * Rb));
             break;
         case 3:
             cudaFuncSetAttribute(k_xD<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
-            k_xD<R, C><<<grid, TPB, fb, st>>>(a, p0, p1);
+            k_xD<R, C><<<grid, nt, fb, st>>>(a, p0, p1);
             mark(ch, nl, "xD", N * 5 * Rb);
             break;
         case 4: {

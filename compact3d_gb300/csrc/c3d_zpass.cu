@@ -346,9 +346,21 @@ __global__ void __launch_bounds__(TPB) k_diag_z(StepArgs<R> a, const double *div
     }
 }
 
+template <typename R, int L>
+static int launch_zpass_l(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *d1, R *d2, int flag, int *nl);
+
 template <typename R>
 int launch_zpass(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *d1, R *d2, int flag, int *nl) {
-    constexpr int L = ZL;
+    if (which == 5) return launch_zpass_l<R, ZL>(ch, a, which, d0, d1, d2, flag, nl);
+    switch (ch->tune.zl[which]) {
+        case 8: return launch_zpass_l<R, 8>(ch, a, which, d0, d1, d2, flag, nl);
+        case 32: return launch_zpass_l<R, 32>(ch, a, which, d0, d1, d2, flag, nl);
+        default: return launch_zpass_l<R, 16>(ch, a, which, d0, d1, d2, flag, nl);
+    }
+}
+
+template <typename R, int L>
+static int launch_zpass_l(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *d1, R *d2, int flag, int *nl) {
     const long long nt = (long long)ch->g.n2m * (ch->g.n3m / L) * ch->g.n1m;
     const int nb = nblk(nt);
     cudaStream_t st = ch->stream;

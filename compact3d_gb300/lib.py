@@ -48,6 +48,9 @@ SIGNATURES = {
     "c3d_set_wsm": (_ip, [_vp, _dp]),
     "c3d_get_wsm": (_ip, [_vp, _dp]),
     "c3d_set_wall_iter_cap": (_ip, [_vp, _ip]),
+    "c3d_autotune": (_ip, [_vp, ctypes.POINTER(_ip)]),
+    "c3d_get_schedule": (_ip, [_vp, ctypes.POINTER(_ip)]),
+    "c3d_set_schedule": (_ip, [_vp, ctypes.POINTER(_ip)]),
     "c3d_op_set": (_ip, [_vp, _dp]),
     "c3d_op_apply": (_ip, [_vp, _ip, _ip]),
     "c3d_op_get": (_ip, [_vp, _dp]),
@@ -178,6 +181,24 @@ class Channel:
         w = np.zeros(3)
         check(load().c3d_get_wsm(self.h, _p(w)), "c3d_get_wsm")
         return w
+
+    # ---- launch schedule ----
+    SCHEDULE_KEYS = ("z_segment_zA", "z_segment_zB", "z_segment_zC", "z_segment_zD", "z_segment_zE",
+                     "x_rows_per_block", "fft_z_tile", "fft_x_plan", "fft_z_plan")
+
+    def autotune(self) -> dict:
+        sch = (_ip * 9)()
+        check(load().c3d_autotune(self.h, sch), "c3d_autotune")
+        return dict(zip(self.SCHEDULE_KEYS, sch[:]))
+
+    def get_schedule(self) -> dict:
+        sch = (_ip * 9)()
+        check(load().c3d_get_schedule(self.h, sch), "c3d_get_schedule")
+        return dict(zip(self.SCHEDULE_KEYS, sch[:]))
+
+    def set_schedule(self, sched: dict):
+        sch = (_ip * 9)(*[int(sched[k]) for k in self.SCHEDULE_KEYS])
+        check(load().c3d_set_schedule(self.h, sch), "c3d_set_schedule")
 
     # ---- operators one at a time ----
     def op_set(self, F):

@@ -206,6 +206,27 @@ int c3d_profile_get(c3d_channel *ch, int idx, const char **name, double *ms,
 #define C3D_NOALLOC_MAX_BYTES (64u * 1024u * 1024u)
 int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
 
+/* ---- launch schedule -----------------------------------------------------
+ * The kernels' launch shapes are chosen per grid shape by an autotuner written for
+ * this library (no counterpart in the reference).  A schedule is nine ints:
+ *   [0..4] z-line segment length (8, 16, 32) of each z pass: the points each thread
+ *       solves sequentially (Thomas-like) before the parallel segments of a z line
+ *       meet
+ *   [5] rows per block of the x passes (2, 4, 8)
+ *   [6] kx columns per block of the z FFT (4, 8, 16)
+ *   [7], [8] radix order of the x and z FFT plans (0: radix 4 first, 1: radix 3
+ *       first, 2: radix 2 only, then 3)
+ * c3d_autotune  times the candidates on a scratch channel of the same grid holding a
+ *               copy of this channel's state (so the channel needs its state), keeps
+ *               the fastest per kernel group, applies it, and caches it per grid
+ *               shape, form and models for the process; `sched` (may be NULL)
+ *               receives the result.
+ * c3d_set_schedule / c3d_get_schedule  set or read a schedule directly.
+ * Channels of a batch are tuned before the batch's first step captures its graph. */
+int c3d_autotune(c3d_channel *ch, int *sched);
+int c3d_get_schedule(c3d_channel *ch, int *sched);
+int c3d_set_schedule(c3d_channel *ch, const int *sched);
+
 /* ---- operators one at a time ---------------------------------------------
  * No single routine of the reference corresponds: these are the operators inside
  * RHS1-3 / RHSDP / GETDP, exposed for operator-level checks and measurement.

@@ -1,0 +1,80 @@
+"""Launch schedules: every schedule the autotuner can choose computes the same step.
+
+Each schedule knob (z segment length, x rows per block, z-FFT tile width, x/z FFT radix
+order) changes only the order of floating-point operations, so one FP64 step under any
+schedule stays within the parity tolerance of the FP64 oracle (1e-10 relative L2 for
+U, V, W).  The autotuner returns a valid schedule and caches it per grid shape.
+"""
+import numpy as np
+import pytest
+
+from compact3d_gb300 import ic
+from compact3d_gb300.grid import C3D_FP64, C3D_MIXED, make_grid
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def libc3d():
+    from compact3d_gb300 import build, lib
+    build.build()
+    lib.load()
+    return lib
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _sched(zl, xw, tw, fx, fz):
+    d = {f"z_segment_z{c}": z for c, z in zip("ABCDE", zl)}
+    d.update(x_rows_per_block=xw, fft_z_tile=tw, fft_x_plan=fx, fft_z_plan=fz)
+    return d
+
+
+SCHEDULES = [
+    _sched((8, 8, 8, 8, 8), 2, 4, 1, 2),
+    _sched((32, 32, 32, 32, 32), 8, 16, 2, 1),
+    _sched((16, 8, 32, 16, 8), 4, 8, 0, 0),
+]
+
+
+@pytest.mark.parametrize("sched", SCHEDULES)
+def test_every_schedule_matches_oracle(libc3d, oracle_mod, sched):
+    g, dt = make_grid("small32", n3m=64)
+    orc = oracle_mod.Oracle(g)
+    U, P, HH = ic.perturbed_laminar(g)
+    orc.project(U)
+    pg = pg3 = 0.0
+    pg, pg3 = orc.getup(U, P, HH, 1, dt, pg, pg3)
+    ch = libc3d.Channel(g, C3D_FP64)
+    ch.upload(U, P, HH)
+    ch.set_schedule(sched)
+    assert ch.get_schedule() == sched
+    orc.getup(U, P, HH, 2, dt, pg, pg3)
+    ch.step(2, dt, pg, pg3)
+    Ug, _, _ = ch.download()
+    n1, n2, n3 = g.n1m, g.n2m, g.n3m
+    for c, j0 in ((0, 1), (1, 2), (2, 1)):
+        e = rel(Ug[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c], U[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c])
+        assert e < 1e-10, (sched, c, e)
+
+
+def test_autotune_valid_and_cached(libc3d):
+    g, dt = make_grid("channel64")
+    U, P, HH = ic.perturbed_laminar(g)
+    a = libc3d.Channel(g, C3D_MIXED)
+    a.upload(U, P, HH)
+    a.project()
+    s1 = a.autotune()
+    assert all(s1[f"z_segment_z{c}"] in (8, 16, 32) for c in "ABCDE") and s1["x_rows_per_block"] in (2, 4, 8)
+    assert s1["fft_z_tile"] in (4, 8, 16) and s1["fft_x_plan"] in (0, 1, 2) and s1["fft_z_plan"] in (0, 1, 2)
+    b = libc3d.Channel(g, C3D_MIXED)
+    b.upload(U, P, HH)
+    assert b.autotune() == s1          # cached for the same grid shape and form
+    a.step_async(1, dt)
+    a.sync()
+    d = a.diagnose()
+    assert np.isfinite(d["divmax"]) and d["divmax"] < 1e-4
+    with pytest.raises(libc3d.C3DError):
+        a.set_schedule(dict(s1, z_segment_zA=12))
