@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdint.h>
+#include <string.h>
 #include "c3d_internal.h"
 
 namespace c3d {
@@ -153,8 +155,80 @@ template <> __device__ __forceinline__ double ldro<double>(const double *p) { re
 template <> __device__ __forceinline__ float ldro<float>(const float *p) { return __ldg(p); }
 template <> __device__ __forceinline__ float2 ldro<float2>(const float2 *p) { return __ldg(p); }
 
+// Direct lane-chunk row I/O: lane l moves its C consecutive elements with the widest
+// vector accesses the alignment allows (16, 8 or 4 bytes), without shared memory.
+template <typename T, int C>
+__device__ __forceinline__ void drow_load(T (&v)[C], const T *__restrict__ g, int lane, int P) {
+    constexpr int B = (int)sizeof(T) * C;
+    if (lane < P) {
+        const T *p = g + lane * C;
+        const uintptr_t a = (uintptr_t)p;
+        if constexpr (B % 16 == 0) {
+            if ((a & 15) == 0) {
+                uint4 q[B / 16];
+#pragma unroll
+                for (int i = 0; i < B / 16; ++i) q[i] = __ldg(reinterpret_cast<const uint4 *>(p) + i);
+                memcpy(v, q, B);
+                return;
+            }
+        }
+        if constexpr (B % 8 == 0) {
+            if ((a & 7) == 0) {
+                uint2 q[B / 8];
+#pragma unroll
+                for (int i = 0; i < B / 8; ++i) q[i] = __ldg(reinterpret_cast<const uint2 *>(p) + i);
+                memcpy(v, q, B);
+                return;
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < C; ++t) v[t] = ldro(p + t);
+    } else {
+#pragma unroll
+        for (int t = 0; t < C; ++t) v[t] = T();
+    }
+}
+
+template <typename T, int C>
+__device__ __forceinline__ void drow_store(T *__restrict__ g, const T (&v)[C], int lane, int P) {
+    constexpr int B = (int)sizeof(T) * C;
+    if (lane < P) {
+        T *p = g + lane * C;
+        const uintptr_t a = (uintptr_t)p;
+        if constexpr (B % 16 == 0) {
+            if ((a & 15) == 0) {
+                uint4 q[B / 16];
+                memcpy(q, v, B);
+#pragma unroll
+                for (int i = 0; i < B / 16; ++i) reinterpret_cast<uint4 *>(p)[i] = q[i];
+                return;
+            }
+        }
+        if constexpr (B % 8 == 0) {
+            if ((a & 7) == 0) {
+                uint2 q[B / 8];
+                memcpy(q, v, B);
+#pragma unroll
+                for (int i = 0; i < B / 8; ++i) reinterpret_cast<uint2 *>(p)[i] = q[i];
+                return;
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < C; ++t) p[t] = v[t];
+    }
+}
+
+#ifndef C3D_STAGED_ROWS
+#define C3D_STAGED_ROWS 0
+#endif
+
 template <typename T, int C>
 __device__ __forceinline__ void srow_load(T (&v)[C], const T *__restrict__ g, T *sb, int lane, int P) {
+    if (!C3D_STAGED_ROWS) {
+        (void)sb;
+        drow_load(v, g, lane, P);
+        return;
+    }
     const int n = P * C;
 #pragma unroll
     for (int t = 0; t < C; ++t) {
@@ -174,6 +248,11 @@ __device__ __forceinline__ void srow_load(T (&v)[C], const T *__restrict__ g, T 
 
 template <typename T, int C>
 __device__ __forceinline__ void srow_store(T *__restrict__ g, const T (&v)[C], T *sb, int lane, int P) {
+    if (!C3D_STAGED_ROWS) {
+        (void)sb;
+        drow_store(g, v, lane, P);
+        return;
+    }
     const int n = P * C;
     if (lane < P) {
 #pragma unroll
