@@ -236,7 +236,11 @@ def run_ours(args, D: Dist):
 
     # ---- main form, device-resident (value) ----
     ch = make_channel(lib, g, args.form, U0, P0, HH0)
-    schedule = ch.autotune() if not args.no_tune else ch.get_schedule()
+    if args.schedule:
+        ch.set_schedule(json.loads(args.schedule))
+        schedule = ch.get_schedule()
+    else:
+        schedule = ch.autotune() if not args.no_tune else ch.get_schedule()
     n = 1
     for _ in range(W):
         ch.step_async(n, dt)
@@ -672,6 +676,7 @@ def main():
     ap.add_argument("--no-les", action="store_true")
     ap.add_argument("--no-ops", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--schedule", default="", help="JSON launch schedule for the main channel instead of autotuning")
     ap.add_argument("--les-steps", type=int, default=200)
     ap.add_argument("--nchan", type=int, default=32)
     args = ap.parse_args()

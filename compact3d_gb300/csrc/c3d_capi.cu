@@ -141,6 +141,16 @@ FftPlan make_plan(int n, int variant) {
     while (m % 2 == 0) { p.rad[p.nst++] = 2; m /= 2; }
     if (variant != 1)
         for (int q = 0; q < e3; ++q) p.rad[p.nst++] = 3;
+    // reciprocals ceil(2^32 / Ns) for the index arithmetic of every stage (Ns > 1)
+    unsigned ns = 1;
+    for (int s = 0; s < p.nst; ++s) {
+        p.dmag[s] = ns == 1 ? 0u : (unsigned)(((1ull << 32) + ns - 1) / ns);
+        for (unsigned jj = 0; ns > 1 && jj < (unsigned)n; ++jj) {   // exact for every index the stage uses
+            const unsigned q = (unsigned)(((unsigned long long)jj * p.dmag[s]) >> 32);
+            if (q != jj / ns) { p.nst = -1; return p; }
+        }
+        ns *= (unsigned)p.rad[s];
+    }
     return p;
 }
 
@@ -528,6 +538,7 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
     ch->tune = Tune{{16, 16, 16, 16, 16}, 4, 8, 0, 0};
     ch->fx = make_plan(g.n1m / 2, 0);
     ch->fz = make_plan(g.n3m, 0);
+    if (ch->fx.nst < 0 || ch->fz.nst < 0) { set_error("FFT plan index arithmetic"); return fail(C3D_EINVAL); }
     const int nx = g.n1m / 2, nz = g.n3m, np = g.n1m / 2 + 1;
     std::vector<double2> tw(nx + nz + np);
     std::vector<float2> tw32(nx + nz + np);
@@ -972,6 +983,7 @@ bool tune_ok(const c3d_channel *ch, const Tune &t) {
 void apply_tune(c3d_channel *ch, const Tune &t) {
     ch->tune = t;
     FftPlan fx = make_plan(ch->g.n1m / 2, t.fxp), fz = make_plan(ch->g.n3m, t.fzp);
+    if (fx.nst < 0 || fz.nst < 0) return;   // cannot happen for N <= 4096; keep the old plans
     fx.tw64 = ch->fx.tw64;
     fx.tw32 = ch->fx.tw32;
     fz.tw64 = ch->fz.tw64;

@@ -14,6 +14,10 @@ struct FftPlan {
     int n;
     int nst;
     int rad[16];
+    // jj / Ns at stage s (Ns = product of the earlier radices, > 1) as
+    // __umulhi(jj, dmag[s]) with dmag = ceil(2^32 / Ns): exact for jj < 2^20 and
+    // Ns <= 2^12, and checked for every jj < n when the plan is made
+    unsigned dmag[16];
     const double2 *tw64;
     const float2 *tw32;
 };

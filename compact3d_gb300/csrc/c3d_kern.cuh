@@ -331,24 +331,26 @@ __device__ __forceinline__ void dftp(C2 (&v)[4], int p, int sign) {
     }
 }
 
-// Stockham FFT of `lines` sequences of length pl.n at buf[q*es + l*ls]; threads tid..nthr
+// Stockham FFT of 2^lsh sequences of length pl.n at buf[q*es + l*ls]; threads tid..nthr
 // of the warp (BLOCK=false) or block (BLOCK=true) cooperate.  Returns the result buffer.
 template <typename C2, bool BLOCK>
-__device__ C2 *fft_smem(C2 *a, C2 *b, const FftPlan &pl, int lines, int es, int ls, int sign, int tid, int nthr) {
-    const int n = pl.n;
+__device__ C2 *fft_smem(C2 *a, C2 *b, const FftPlan &pl, int lsh, int es, int ls, int sign, int tid, int nthr) {
+    const int n = pl.n, lmask = (1 << lsh) - 1;
     const C2 *tw = twsel<C2>(pl);
     int Ns = 1;
     for (int s = 0; s < pl.nst; ++s) {
         const int p = pl.rad[s];
         const int np = n / p;
         const int tstep = n / (Ns * p);
-        for (int idx = tid; idx < np * lines; idx += nthr) {
-            const int l = idx % lines, jj = idx / lines;
+        const unsigned mg = pl.dmag[s];
+        for (int idx = tid; idx < (np << lsh); idx += nthr) {
+            const int l = idx & lmask, jj = idx >> lsh;
+            const int q = Ns == 1 ? jj : (int)__umulhi((unsigned)jj, mg);   // jj / Ns
+            const int kq = jj - q * Ns;
             C2 v[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r)
                 if (r < p) v[r] = a[(jj + r * np) * es + l * ls];
-            const int kq = jj % Ns;
             if (Ns > 1) {
 #pragma unroll
                 for (int r = 1; r < 4; ++r)
@@ -359,7 +361,7 @@ __device__ C2 *fft_smem(C2 *a, C2 *b, const FftPlan &pl, int lines, int es, int 
                     }
             }
             dftp(v, p, sign);
-            const int base = (jj / Ns) * Ns * p + kq;
+            const int base = q * Ns * p + kq;
 #pragma unroll
             for (int r = 0; r < 4; ++r)
                 if (r < p) b[(base + r * Ns) * es + l * ls] = v[r];

@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(TPB) k_op_x(StepArgs<R> a, int op, const R *in
                 bufa[kx] = Z;
             }
             __syncwarp();
-            C2 *Zr = fft_smem<C2, false>(bufa, bufb, a.fx, 1, 1, 0, +1, lane, 32);
+            C2 *Zr = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, +1, lane, 32);
             const R *rz = reinterpret_cast<const R *>(Zr);
             const R scale = (R)(1.0 / ((double)g.n1m * (double)g.n3m));
             R v[C];
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(TPB) k_op_x(StepArgs<R> a, int op, const R *in
                 for (int t = 0; t < C; ++t) rbuf[lane * C + t] = f[t];
             }
             __syncwarp();
-            C2 *Z = fft_smem<C2, false>(bufa, bufb, a.fx, 1, 1, 0, -1, lane, 32);
+            C2 *Z = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, -1, lane, 32);
             for (int kx = lane; kx <= M; kx += 32) {
                 C2 zk = Z[kx == M ? 0 : kx], zm = cconj(Z[kx == 0 ? 0 : M - kx]);
                 C2 E, O;

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(TPB) k_ir_x(StepArgs<float> a, RefArgs r) {
             for (int t = 0; t < C; ++t) rbuf[lane * C + t] = res[t];
         }
         __syncwarp();
-        C2 *Z = fft_smem<C2, false>(bufa, bufb, a.fx, 1, 1, 0, -1, lane, 32);
+        C2 *Z = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, -1, lane, 32);
         C2 *Sp = reinterpret_cast<C2 *>(a.spec) + ((long long)(j - 1) * g.n3m + k) * g.n1h;
         for (int kx = lane; kx <= M; kx += 32) {
             C2 zk = Z[kx == M ? 0 : kx], zm = cconj(Z[kx == 0 ? 0 : M - kx]);
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(TPB) k_ir_d(StepArgs<float> a) {
             bufa[kx] = Zv;
         }
         __syncwarp();
-        C2 *Zr = fft_smem<C2, false>(bufa, bufb, a.fx, 1, 1, 0, +1, lane, 32);
+        C2 *Zr = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, +1, lane, 32);
         const float *rz = reinterpret_cast<const float *>(Zr);
         float dpv[C], d[C];
 #pragma unroll

@@ -23,7 +23,7 @@ __global__ void __launch_bounds__(TPB) k_fftz(StepArgs<R> a, int sign, int tw) {
         else { A[e].x = 0; A[e].y = 0; }
     }
     __syncthreads();
-    C2 *Z = fft_smem<C2, true>(A, B, a.fz, tw, tw, 1, sign, threadIdx.x, blockDim.x);
+    C2 *Z = fft_smem<C2, true>(A, B, a.fz, __ffs(tw) - 1, tw, 1, sign, threadIdx.x, blockDim.x);   // tw is a power of 2
     for (int e = threadIdx.x; e < n * tw; e += blockDim.x) {
         int q = e / tw, l = e % tw;
         if (l < w) S[(long long)q * g.n1h + l] = Z[e];

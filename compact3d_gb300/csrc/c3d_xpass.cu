@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const 
             for (int t = 0; t < C; ++t) rbuf[lane * C + t] = d[t];
         }
         __syncwarp();
-        C2 *Z = fft_smem<C2, false>(bufa, bufb, a.fx, 1, 1, 0, -1, lane, 32);
+        C2 *Z = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, -1, lane, 32);
         C2 *Sp = reinterpret_cast<C2 *>(a.spec) + ((long long)(j - 1) * g.n3m + k) * g.n1h;
         for (int kx = lane; kx <= M; kx += 32) {
             C2 zk = Z[kx == M ? 0 : kx], zm = cconj(Z[kx == 0 ? 0 : M - kx]);
@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(XMAXT) k_xD(StepArgs<R> a, const R *d0, const 
             bufa[kx] = Z;
         }
         __syncwarp();
-        C2 *Zr = fft_smem<C2, false>(bufa, bufb, a.fx, 1, 1, 0, +1, lane, 32);
+        C2 *Zr = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, +1, lane, 32);
         const R *rz = reinterpret_cast<const R *>(Zr);
         R dpv[C];
         if (lane < P) {
