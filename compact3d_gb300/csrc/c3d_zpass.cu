@@ -18,17 +18,43 @@ namespace c3d {
 __device__ __forceinline__ int znext(int k, int n) { return (k + 1 == n) ? 0 : k + 1; }
 __device__ __forceinline__ int zprev(int k, int n) { return (k == 0) ? n - 1 : k - 1; }
 
+// Prefetch ring of a column: the values at the D positions after the walker's current
+// one, loaded D steps before they are used so the loads of consecutive steps overlap.
+constexpr int ZPF = 4;
+template <typename T>
+struct ZRing {
+    T v[ZPF];
+    int kf;   // position of v[ZPF-1]
+    __device__ void fill(const T *col, int k, int n, int s) {
+        kf = k;
+#pragma unroll
+        for (int d = 0; d < ZPF; ++d) {
+            kf = znext(kf, n);
+            v[d] = col[kf * s];
+        }
+    }
+    // value at the next position; the ring advances by one
+    __device__ T pop(const T *col, int n, int s) {
+        const T r = v[0];
+#pragma unroll
+        for (int d = 0; d < ZPF - 1; ++d) v[d] = v[d + 1];
+        kf = znext(kf, n);
+        v[ZPF - 1] = col[kf * s];
+        return r;
+    }
+};
+
 // state column: (1,10,1) RHS f12*(u- - 2u + u+) and (1,6,1) RHS 4*(u- + u) (face k)
 template <typename R>
 struct WalkVisBack {
     typedef typename SType<R>::S S;
-    const S *col; int n, s; R f12; S um, uc; int kn;
-    __device__ void start(int k) { um = col[zprev(k, n) * s]; uc = col[k * s]; kn = znext(k, n); }
+    const S *col; int n, s; R f12; S um, uc; ZRing<S> ru;
+    __device__ void start(int k) { um = col[zprev(k, n) * s]; uc = col[k * s]; ru.fill(col, k, n, s); }
     __device__ void next(R (&d)[2]) {
-        S up = col[kn * s];
+        S up = ru.pop(col, n, s);
         d[0] = f12 * St<R>::d2(um, uc, up);
         d[1] = (R)4.0 * (St<R>::hi(um) + St<R>::hi(uc));
-        um = uc; uc = up; kn = znext(kn, n);
+        um = uc; uc = up;
     }
 };
 
@@ -36,16 +62,18 @@ struct WalkVisBack {
 template <typename R>
 struct WalkWP {
     typedef typename SType<R>::S S;
-    const S *W, *P; int n, s; R f12, f24; S wm, wc, pm; int kn, kc;
+    const S *W, *P; int n, s; R f12, f24; S wm, wc, pm, pc; ZRing<S> rw, rp;
     __device__ void start(int k) {
-        wm = W[zprev(k, n) * s]; wc = W[k * s]; pm = P[zprev(k, n) * s]; kc = k; kn = znext(k, n);
+        wm = W[zprev(k, n) * s]; wc = W[k * s]; pm = P[zprev(k, n) * s]; pc = P[k * s];
+        rw.fill(W, k, n, s);
+        rp.fill(P, k, n, s);
     }
     __device__ void next(R (&d)[3]) {
-        S wp = W[kn * s], pc = P[kc * s];
+        S wp = rw.pop(W, n, s);
         d[0] = f12 * St<R>::d2(wm, wc, wp);
         d[1] = (R)4.0 * (St<R>::hi(wc) + St<R>::hi(wp));
         d[2] = f24 * St<R>::d(pc, pm);
-        wm = wc; wc = wp; pm = pc; kc = kn; kn = znext(kn, n);
+        wm = wc; wc = wp; pm = pc; pc = rp.pop(P, n, s);
     }
 };
 
