@@ -138,7 +138,9 @@ struct WalkGradZ {
     }
 };
 
-template <typename R, int L>
+// PART 0 runs the three sweeps in one kernel; PART 1, 2, 3 run only the u, the (w, P) or
+// the v sweep (the split form has fewer registers per thread and moves the same bytes).
+template <typename R, int L, int PART>
 __global__ void __launch_bounds__(TPB) k_zA(StepArgs<R> a) {
     typedef typename SType<R>::S S;
     typedef St<R> ST;
@@ -153,14 +155,22 @@ __global__ void __launch_bounds__(TPB) k_zA(StepArgs<R> a) {
         const int lane = threadIdx.x & 31;
         const long long o0 = fidx(g, i - lane, j, 0), sb = (long long)g.n1m;
         const int ss = 32 * (int)sizeof(S), sr = 32 * (int)sizeof(R);
-        pf_cols(a.u + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
-        pf_cols(a.w + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
-        pf_cols(a.p + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
-        if (j >= 2) pf_cols(a.v + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
-        pf_cols(a.ww1 + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
-        for (int c = 0; c < 3; ++c) pf_cols(a.r[c] + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
+        if (PART <= 1) {
+            pf_cols(a.u + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
+            pf_cols(a.ww1 + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
+            pf_cols(a.r[0] + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
+        }
+        if (PART == 0 || PART == 2) {
+            pf_cols(a.w + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
+            pf_cols(a.p + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
+            pf_cols(a.r[2] + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
+        }
+        if ((PART == 0 || PART == 3) && j >= 2) {
+            pf_cols(a.v + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
+            pf_cols(a.r[1] + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
+        }
     }
-    {   // u: R1 += (1/RE) d2u/dz2 ; E_xz = UU3 * WW1
+    if (PART == 0 || PART == 1) {   // u: R1 += (1/RE) d2u/dz2 ; E_xz = UU3 * WW1
         R out[2][L];
         const R rr[2] = {a.c10z.r, a.c6z.r}, ss[2] = {a.c10z.s, a.c6z.s};
         WalkVisBack<R> f{a.u + o, n, s, a.f12z};
@@ -174,7 +184,7 @@ __global__ void __launch_bounds__(TPB) k_zA(StepArgs<R> a) {
             E[kk] = out[1][t] * Wx[kk];
         }
     }
-    {   // w, P: R3 += (1/RE) d2w/dz2 - dP/dz - PRESG3 ; WW3^2
+    if (PART == 0 || PART == 2) {   // w, P: R3 += (1/RE) d2w/dz2 - dP/dz - PRESG3 ; WW3^2
         R out[3][L];
         const R rr[3] = {a.c10z.r, a.c6z.r, a.c22z.r}, ss[3] = {a.c10z.s, a.c6z.s, a.c22z.s};
         WalkWP<R> f{a.w + o, a.p + o, n, s, a.f12z, a.f24z};
@@ -188,7 +198,7 @@ __global__ void __launch_bounds__(TPB) k_zA(StepArgs<R> a) {
             Q[kk] = out[1][t] * out[1][t];
         }
     }
-    if (j >= 2) {   // v: R2 += (1/RE) d2v/dz2 ; E_yz = VV3 * (w at y face J)
+    if ((PART == 0 || PART == 3) && j >= 2) {   // v: R2 += (1/RE) d2v/dz2 ; E_yz = VV3 * (w at y face J)
         R out[2][L];
         const R rr[2] = {a.c10z.r, a.c6z.r}, ss[2] = {a.c10z.s, a.c6z.s};
         WalkVisBack<R> f{a.v + o, n, s, a.f12z};
@@ -394,7 +404,19 @@ static int launch_zpass_l(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *
     cudaStream_t st = ch->stream;
     const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
     switch (which) {
-        case 0: k_zA<R, L><<<nb, TPB, 0, st>>>(a); mark(ch, nl, "zA", N * (32 + 10 * Rb)); break;
+        case 0:
+            if (ch->tune.zsplit) {   // u, (w, P), v sweeps as three kernels
+                k_zA<R, L, 1><<<nb, TPB, 0, st>>>(a);
+                mark(ch, nl, "zA", N * (8 + 4 * Rb));
+                k_zA<R, L, 2><<<nb, TPB, 0, st>>>(a);
+                mark(ch, nl, "zA", N * (16 + 3 * Rb));
+                k_zA<R, L, 3><<<nb, TPB, 0, st>>>(a);
+                mark(ch, nl, "zA", N * (8 + 3 * Rb));
+            } else {
+                k_zA<R, L, 0><<<nb, TPB, 0, st>>>(a);
+                mark(ch, nl, "zA", N * (32 + 10 * Rb));
+            }
+            break;
         case 1: k_zB<R, L><<<nb, TPB, 0, st>>>(a); mark(ch, nl, "zB", N * 8 * Rb); break;
         case 2: k_zC<R, L><<<nb, TPB, 0, st>>>(a, d0, d1, d2); mark(ch, nl, "zC", N * 6 * Rb); break;
         case 3: k_zD<R, L><<<nb, TPB, 0, st>>>(a, d2); mark(ch, nl, "zD", N * (8 + 2 * Rb)); break;
