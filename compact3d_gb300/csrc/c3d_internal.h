@@ -97,9 +97,11 @@ enum {
 //   fxp, fzp  radix order of the x and z FFT plans (0: radix 4 first, 1: radix 3 first,
 //        2: radix 2 only before 3)
 //   zsplit  zA fused or split into its three sweeps
+//   xsplit  xA fused or split into its u, v and w pieces
 struct Tune {
     int zl[5], xw, twz, fxp, fzp;
     int zsplit;   // zA as one kernel (0) or as its three sweeps in three kernels (1)
+    int xsplit;   // xA as one kernel (0) or as its u, v, w pieces in three kernels (1)
 };
 
 // Arguments of the pressure refinement (mixed form with C3D_MIXED_IR): double-float

@@ -15,7 +15,10 @@ namespace c3d {
 // ---------------------------------------------------------------------------------
 // xA
 // ---------------------------------------------------------------------------------
-template <typename R, int C>
+// PART 0 computes the u, v and w pieces in one kernel; PART 1, 2, 3 compute one of them
+// (the split form has fewer registers per thread; PART 2 reads the two u rows of the
+// y-face interpolant again).
+template <typename R, int C, int PART>
 __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
     typedef typename SType<R>::S S;
     typedef St<R> ST;
@@ -33,14 +36,25 @@ __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
         const long long o = fidx(g, 0, j, k), om = fidx(g, 0, j - 1, k), op = fidx(g, 0, j + 1, k);
         {   // every row this warp reads, requested from DRAM at once
             const int rb = g.n1m * (int)sizeof(S);
-            pf_row(a.u + om, rb, lane); pf_row(a.u + o, rb, lane); pf_row(a.u + op, rb, lane);
-            pf_row(a.p + o, rb, lane); pf_row(a.p + om, rb, lane);
-            pf_row(a.v + om, rb, lane); pf_row(a.v + o, rb, lane); pf_row(a.v + op, rb, lane);
-            pf_row(a.w + om, rb, lane); pf_row(a.w + o, rb, lane); pf_row(a.w + op, rb, lane);
+            if (PART <= 2) { pf_row(a.u + om, rb, lane); pf_row(a.u + o, rb, lane); pf_row(a.p + o, rb, lane); }
+            if (PART <= 1) pf_row(a.u + op, rb, lane);
+            if (PART == 0 || PART == 2) {
+                pf_row(a.p + om, rb, lane);
+                pf_row(a.v + om, rb, lane); pf_row(a.v + o, rb, lane); pf_row(a.v + op, rb, lane);
+            }
+            if (PART == 0 || PART == 3) { pf_row(a.w + om, rb, lane); pf_row(a.w + o, rb, lane); pf_row(a.w + op, rb, lane); }
         }
         R uy[C];
+        if (PART == 2 && j >= 2) {   // u at the y faces, for E_xy
+            S uc[C], um[C];
+            srow_load(uc, a.u + o, sbS, lane, P);
+            srow_load(um, a.u + om, sbS, lane, P);
+            const R Hj1 = a.m.rh[j], a1 = a.m.hdy[j], a2 = a.m.hdy[j - 1];
+#pragma unroll
+            for (int t = 0; t < C; ++t) uy[t] = Hj1 * (a1 * ST::hi(um[t]) + a2 * ST::hi(uc[t]));
+        }
         // ---- u: R1 = visc_y + visc_x/RE - dP/dx - PRESG ; HH1 = d(uu)/dx ----
-        {
+        if (PART == 0 || PART == 1) {
             S uc[C], um[C], up[C];
             srow_load(uc, a.u + o, sbS, lane, P);
             srow_load(um, a.u + om, sbS, lane, P);
@@ -87,14 +101,14 @@ __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
             }
             xsolve(d, lane, P, a.c22x);
             srow_store(a.hh[0] + o, d, sbR, lane, P);
-            if (j >= 2) {
+            if (PART == 0 && j >= 2) {
                 const R Hj1 = a.m.rh[j], a1 = a.m.hdy[j], a2 = a.m.hdy[j - 1];
 #pragma unroll
                 for (int t = 0; t < C; ++t) uy[t] = Hj1 * (a1 * ST::hi(um[t]) + a2 * ST::hi(uc[t]));
             }
         }
         // ---- v (faces J=2..N2M): R2, HH2 = d(vv)/dy, E_xy = VV1 * UY ----
-        if (j >= 2) {
+        if ((PART == 0 || PART == 2) && j >= 2) {
             S vc[C], vm[C], vp[C];
             srow_load(vc, a.v + o, sbS, lane, P);
             srow_load(vm, a.v + om, sbS, lane, P);
@@ -134,7 +148,7 @@ __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
             srow_store(a.exy + o, d, sbR, lane, P);
         }
         // ---- w: R3 = visc_y + visc_x/RE ; WW1 = w at x faces ----
-        {
+        if (PART == 0 || PART == 3) {
             S wc[C], wm[C], wp[C];
             srow_load(wc, a.w + o, sbS, lane, P);
             srow_load(wm, a.w + om, sbS, lane, P);
@@ -550,8 +564,20 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
     const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(M + 1) * sizeof(C2)) * xw;
     switch (which) {
         case 0:
-            cudaFuncSetAttribute(k_xA<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
-            k_xA<R, C><<<grid, nt, sb, st>>>(a);
+            if (ch->tune.xsplit) {   // the u, v and w pieces as three kernels
+                cudaFuncSetAttribute(k_xA<R, C, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
+                cudaFuncSetAttribute(k_xA<R, C, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
+                cudaFuncSetAttribute(k_xA<R, C, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
+                k_xA<R, C, 1><<<grid, nt, sb, st>>>(a);
+                mark(ch, nl, "xA", N * (16 + 2 * Rb));   // u, P; R1, HH1
+                k_xA<R, C, 2><<<grid, nt, sb, st>>>(a);
+                mark(ch, nl, "xA", N * (24 + 3 * Rb));   // v, P, u; R2, HH2, E_xy
+                k_xA<R, C, 3><<<grid, nt, sb, st>>>(a);
+                mark(ch, nl, "xA", N * (8 + 2 * Rb));    // w; R3, WW1
+                break;
+            }
+            cudaFuncSetAttribute(k_xA<R, C, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
+            k_xA<R, C, 0><<<grid, nt, sb, st>>>(a);
             mark(ch, nl, "xA", N * (32 + 7 * Rb));
             break;
         case 1:

@@ -208,7 +208,7 @@ int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
 
 /* ---- launch schedule -----------------------------------------------------
  * The kernels' launch shapes are chosen per grid shape by an autotuner written for
- * this library (no counterpart in the reference).  A schedule is ten ints:
+ * this library (no counterpart in the reference).  A schedule is eleven ints:
  *   [0..4] z-line segment length (8, 16, 32) of each z pass: the points each thread
  *       solves sequentially (Thomas-like) before the parallel segments of a z line
  *       meet
@@ -218,6 +218,8 @@ int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
  *       first, 2: radix 2 only, then 3)
  *   [9] the z pass of the explicit terms as one kernel (0) or as its three sweeps
  *       in three kernels (1)
+ *   [10] the x pass of the explicit terms as one kernel (0) or as its u, v and w
+ *       pieces in three kernels (1)
  * c3d_autotune  times the candidates on a scratch channel of the same grid holding a
  *               copy of this channel's state (so the channel needs its state), keeps
  *               the fastest per kernel group, applies it, and caches it per grid

@@ -26,16 +26,17 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def _sched(zl, xw, tw, fx, fz, split):
+def _sched(zl, xw, tw, fx, fz, split, xsplit):
     d = {f"z_segment_z{c}": z for c, z in zip("ABCDE", zl)}
-    d.update(x_rows_per_block=xw, fft_z_tile=tw, fft_x_plan=fx, fft_z_plan=fz, z_split_zA=split)
+    d.update(x_rows_per_block=xw, fft_z_tile=tw, fft_x_plan=fx, fft_z_plan=fz, z_split_zA=split,
+             x_split_xA=xsplit)
     return d
 
 
 SCHEDULES = [
-    _sched((8, 8, 8, 8, 8), 2, 4, 1, 2, 1),
-    _sched((32, 32, 32, 32, 32), 8, 16, 2, 1, 0),
-    _sched((16, 8, 32, 16, 8), 4, 8, 0, 0, 1),
+    _sched((8, 8, 8, 8, 8), 2, 4, 1, 2, 1, 1),
+    _sched((32, 32, 32, 32, 32), 8, 16, 2, 1, 0, 0),
+    _sched((16, 8, 32, 16, 8), 4, 8, 0, 0, 1, 0),
 ]
 
 
