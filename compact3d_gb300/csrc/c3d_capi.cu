@@ -1003,8 +1003,8 @@ int time_schedule(c3d_channel *sc, const Tune &t, double dt, const std::vector<s
     CK(cudaStreamSynchronize(sc->stream));
     double c = 0.0;
     for (size_t q = 0; q < sc->prof_name.size(); ++q)
-        for (const std::string &n : names)
-            if (sc->prof_name[q] == n) c += sc->prof_ms[q];
+        for (const std::string &n : names)   // a name covers its split pieces (zA -> zA_u, ...)
+            if (sc->prof_name[q] == n || sc->prof_name[q].rfind(n + "_", 0) == 0) c += sc->prof_ms[q];
     c3d_profile(sc, 0);
     *cost = c;
     return 0;

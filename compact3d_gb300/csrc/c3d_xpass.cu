@@ -569,11 +569,11 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
                 cudaFuncSetAttribute(k_xA<R, C, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
                 cudaFuncSetAttribute(k_xA<R, C, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
                 k_xA<R, C, 1><<<grid, nt, sb, st>>>(a);
-                mark(ch, nl, "xA", N * (16 + 2 * Rb));   // u, P; R1, HH1
+                mark(ch, nl, "xA_u", N * (16 + 2 * Rb));   // u, P; R1, HH1
                 k_xA<R, C, 2><<<grid, nt, sb, st>>>(a);
-                mark(ch, nl, "xA", N * (24 + 3 * Rb));   // v, P, u; R2, HH2, E_xy
+                mark(ch, nl, "xA_v", N * (24 + 3 * Rb));   // v, P, u; R2, HH2, E_xy
                 k_xA<R, C, 3><<<grid, nt, sb, st>>>(a);
-                mark(ch, nl, "xA", N * (8 + 2 * Rb));    // w; R3, WW1
+                mark(ch, nl, "xA_w", N * (8 + 2 * Rb));    // w; R3, WW1
                 break;
             }
             cudaFuncSetAttribute(k_xA<R, C, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);

@@ -407,11 +407,11 @@ static int launch_zpass_l(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *
         case 0:
             if (ch->tune.zsplit) {   // u, (w, P), v sweeps as three kernels
                 k_zA<R, L, 1><<<nb, TPB, 0, st>>>(a);
-                mark(ch, nl, "zA", N * (8 + 4 * Rb));    // u; WW1, R1 -> R1, E_xz
+                mark(ch, nl, "zA_u", N * (8 + 4 * Rb));    // u; WW1, R1 -> R1, E_xz
                 k_zA<R, L, 2><<<nb, TPB, 0, st>>>(a);
-                mark(ch, nl, "zA", N * (16 + 3 * Rb));   // w, P; R3 -> R3, WW3^2
+                mark(ch, nl, "zA_wp", N * (16 + 3 * Rb));  // w, P; R3 -> R3, WW3^2
                 k_zA<R, L, 3><<<nb, TPB, 0, st>>>(a);
-                mark(ch, nl, "zA", N * (16 + 3 * Rb));   // v, w; R2 -> R2, E_yz
+                mark(ch, nl, "zA_v", N * (16 + 3 * Rb));   // v, w; R2 -> R2, E_yz
             } else {
                 k_zA<R, L, 0><<<nb, TPB, 0, st>>>(a);
                 mark(ch, nl, "zA", N * (32 + 10 * Rb));
