@@ -155,6 +155,28 @@ class L2Flush:
         self.torch.cuda.synchronize()
 
 
+def host_link_gbs(device: int, nbytes: int = 1 << 30):
+    """Copy rate of the host link in each direction (GB/s): one pinned 1 GiB buffer
+    copied to and from the device with cudaMemcpyAsync, best of three, CUDA events."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device=f"cuda:{device}")
+    out = {}
+    for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        best = None
+        for _ in range(3):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            dst.copy_(src, non_blocking=True)
+            b.record()
+            b.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        out[name] = nbytes / best / 1e6
+    del h, d
+    return out
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -356,9 +378,17 @@ def run_ours(args, D: Dist):
             m += 1
         te = D.max(time.perf_counter() - t0)
         bytes_io = U.nbytes + P.nbytes + HH.nbytes
+        link = host_link_gbs(D.local)
+        # Floor of a getup that moves its arrays over the link one direction at a time
+        # around the device step: in / h2d rate + step + out / d2h rate.
+        floor_ms = bytes_io / link["h2d"] / 1e6 + res["ms_per_step"] + bytes_io / link["d2h"] / 1e6
+        e2e_ms = te / ke * 1e3
         res["e2e"] = dict(value=total_pts * ke / te, unit=UNIT, h2d_bytes_per_step=bytes_io,
-                          d2h_bytes_per_step=bytes_io, steps=ke,
-                          path="c3d_getup: Fortran-layout host arrays (pinned) -> device, step, -> host")
+                          d2h_bytes_per_step=bytes_io, steps=ke, ms_per_step=e2e_ms,
+                          link_gbs={k: round(v, 1) for k, v in link.items()},
+                          floor_ms=floor_ms, frac_of_floor=floor_ms / e2e_ms,
+                          path="c3d_getup: Fortran-layout host arrays (pinned, mapped) read and written "
+                               "in place by the repacking kernels, step between")
         for a in (U, P, HH):
             L.host_unregister(a)
         ce.close()

@@ -573,6 +573,23 @@ int c3d_destroy(c3d_channel *ch) {
     return 0;
 }
 
+// Device address of a host array registered with c3d_host_register (mapped), or null
+// when [h, h + bytes) is not mapped host memory (then the staged copy is used).  Both ends
+// of the range are checked so the repack kernels only touch mapped addresses.
+static double *host_mapped(const void *h, size_t bytes) {
+    if (!h || !bytes) return nullptr;
+    cudaPointerAttributes a0, a1;
+    const char *last = (const char *)h + bytes - 1;
+    if (cudaPointerGetAttributes(&a0, h) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+        return nullptr;
+    if ((const char *)a1.devicePointer - (const char *)a0.devicePointer != (long long)(bytes - 1)) return nullptr;
+    return (double *)a0.devicePointer;
+}
+
 static int h2d(c3d_channel *ch, const double *src, size_t n) {
     CK(cudaMemcpyAsync(ch->stage, src, n * sizeof(double), cudaMemcpyHostToDevice, ch->stream));
     return 0;
@@ -592,20 +609,25 @@ int c3d_upload(c3d_channel *ch, const double *u, const double *p, const double *
     const size_t n3 = ch->stage_elems;   // one component of U / HH
     const Geo &g = ch->g;
     const size_t np_ = (size_t)(g.n1m + 1) * g.n2 * (g.n3m + 1);
+    // Mapped host arrays are read by the repack kernels directly (no staging copy).
+    double *mu = host_mapped(u, 3 * n3 * 8), *mp = host_mapped(p, np_ * 8), *mh = host_mapped(hh, 3 * n3 * 8);
     for (int c = 0; c < 3; ++c) {
-        if (u) {
+        if (u && mu) launch_repack(ch, 0, 0, c, mu + c * n3);
+        else if (u) {
             int rc = h2d(ch, u + c * n3, n3);
             if (rc) return rc;
             launch_repack(ch, 0, 0, c);
         }
     }
-    if (p) {
+    if (p && mp) launch_repack(ch, 0, 1, 0, mp);
+    else if (p) {
         int rc = h2d(ch, p, np_);
         if (rc) return rc;
         launch_repack(ch, 0, 1, 0);
     }
     for (int c = 0; c < 3; ++c) {
-        if (hh) {
+        if (hh && mh) launch_repack(ch, 0, 2, c, mh + c * n3);
+        else if (hh) {
             int rc = h2d(ch, hh + c * n3, n3);
             if (rc) return rc;
             launch_repack(ch, 0, 2, c);
@@ -624,37 +646,45 @@ int c3d_download(c3d_channel *ch, double *u, double *p, double *hh, double *sgsv
     const size_t n3 = ch->stage_elems;
     const Geo &g = ch->g;
     const size_t np_ = (size_t)(g.n1m + 1) * g.n2 * (g.n3m + 1);
+    // Mapped host arrays are written by the repack kernels directly.
+    double *mu = host_mapped(u, 3 * n3 * 8), *mp = host_mapped(p, np_ * 8), *mh = host_mapped(hh, 3 * n3 * 8);
+    double *ms = host_mapped(sgsvis, n3 * 8);
     for (int c = 0; c < 3; ++c) {
-        if (u) {
+        if (u && mu) launch_repack(ch, 1, 0, c, mu + c * n3);
+        else if (u) {
             launch_repack(ch, 1, 0, c);
             int rc = d2h(ch, u + c * n3, n3);
             if (rc) return rc;
         }
     }
-    if (p) {
+    if (p && mp) launch_repack(ch, 1, 1, 0, mp);
+    else if (p) {
         launch_repack(ch, 1, 1, 0);
         int rc = d2h(ch, p, np_);
         if (rc) return rc;
     }
     for (int c = 0; c < 3; ++c) {
-        if (hh) {
+        if (hh && mh) launch_repack(ch, 1, 2, c, mh + c * n3);
+        else if (hh) {
             launch_repack(ch, 1, 2, c);
             int rc = d2h(ch, hh + c * n3, n3);
             if (rc) return rc;
         }
     }
-    if (sgsvis) {
+    if (sgsvis && ms) launch_repack(ch, 1, 3, 0, ms);
+    else if (sgsvis) {
         launch_repack(ch, 1, 3, 0);
         int rc = d2h(ch, sgsvis, n3);
         if (rc) return rc;
     }
+    CK(cudaStreamSynchronize(ch->stream));
     CK(cudaGetLastError());
     return 0;
 }
 
 int c3d_host_register(void *ptr, size_t bytes) {
     if (!ptr || !bytes) { set_error("null pointer or zero size"); return C3D_EINVAL; }
-    CK(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+    CK(cudaHostRegister(ptr, bytes, cudaHostRegisterMapped));
     return 0;
 }
 
@@ -904,9 +934,12 @@ int c3d_op_set(c3d_channel *ch, const double *f) {
             CK(cudaMemset(ch->opbuf[q], 0, nf * rs));
         }
     }
-    int rc = h2d(ch, f, ch->stage_elems);
-    if (rc) return rc;
-    launch_repack(ch, 0, 4, 0);
+    if (double *mf = host_mapped(f, ch->stage_elems * 8)) launch_repack(ch, 0, 4, 0, mf);
+    else {
+        int rc = h2d(ch, f, ch->stage_elems);
+        if (rc) return rc;
+        launch_repack(ch, 0, 4, 0);
+    }
     CK(cudaStreamSynchronize(ch->stream));
     CK(cudaGetLastError());
     return 0;
@@ -931,9 +964,14 @@ int c3d_op_get(c3d_channel *ch, double *f) {
     if (!ch || !f) { set_error("null argument"); return C3D_EINVAL; }
     if (!ch->opbuf[1]) { set_error("no operator result"); return C3D_ESTATE; }
     cudaSetDevice(ch->device);
-    launch_repack(ch, 1, 5, 0);
-    int rc = d2h(ch, f, ch->stage_elems);
-    if (rc) return rc;
+    if (double *mf = host_mapped(f, ch->stage_elems * 8)) {
+        launch_repack(ch, 1, 5, 0, mf);
+        CK(cudaStreamSynchronize(ch->stream));
+    } else {
+        launch_repack(ch, 1, 5, 0);
+        int rc = d2h(ch, f, ch->stage_elems);
+        if (rc) return rc;
+    }
     CK(cudaGetLastError());
     return 0;
 }

@@ -224,7 +224,8 @@ int launch_diag(c3d_channel *ch, int *launches);
 int launch_poisson_tables(c3d_channel *ch);
 // what: 0 U component, 1 P, 2 HH component, 3 SGSVIS (to host), 4 operand (to device),
 // 5 operator result (to host)
-int launch_repack(c3d_channel *ch, int dir, int what, int comp);  // 0: Fortran->device
+// fort: the Fortran-layout array (device staging buffer by default, or a mapped host array)
+int launch_repack(c3d_channel *ch, int dir, int what, int comp, double *fort = nullptr);  // dir 0: Fortran->device
 void set_error(const std::string &msg);
 // Records a kernel-boundary mark for the profiler and counts the launch.
 void mark(c3d_channel *ch, int *nl, const char *name, double bytes);

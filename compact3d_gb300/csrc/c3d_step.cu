@@ -493,7 +493,8 @@ int launch_poisson_tables(c3d_channel *ch) {
     return e == cudaSuccess ? 0 : C3D_ECUDA;
 }
 
-int launch_repack(c3d_channel *ch, int dir, int what, int comp) {
+int launch_repack(c3d_channel *ch, int dir, int what, int comp, double *fort) {
+    double *F = fort ? fort : ch->stage;
     const Geo &g = ch->g;
     const int j0 = (what == 0 || what == 3) ? 0 : 1, j1 = (what == 0 || what == 3) ? g.n2 : g.n2m;
     const long long tot_dev = (long long)(j1 - j0 + 1) * g.np;
@@ -506,31 +507,31 @@ int launch_repack(c3d_channel *ch, int dir, int what, int comp) {
         void *buf = ch->opbuf[what == 4 ? 0 : 1];
         if (!buf || (what == 4) != (dir == 0)) return C3D_EINVAL;
         if (!mixed) {
-            if (dir == 0) k_unpack<double><<<nblk((long long)(g.n2 + 1) * g.np), TPB, 0, st>>>(g, 0, (double *)buf, ch->stage, ToF64());
-            else k_pack<double><<<nb, TPB, 0, st>>>(g, 0, (const double *)buf, ch->stage, FromF64());
+            if (dir == 0) k_unpack<double><<<nblk((long long)(g.n2 + 1) * g.np), TPB, 0, st>>>(g, 0, (double *)buf, F, ToF64());
+            else k_pack<double><<<nb, TPB, 0, st>>>(g, 0, (const double *)buf, F, FromF64());
         } else {
-            if (dir == 0) k_unpack<float><<<nblk((long long)(g.n2 + 1) * g.np), TPB, 0, st>>>(g, 0, (float *)buf, ch->stage, ToF32());
-            else k_pack<float><<<nb, TPB, 0, st>>>(g, 0, (const float *)buf, ch->stage, FromF32());
+            if (dir == 0) k_unpack<float><<<nblk((long long)(g.n2 + 1) * g.np), TPB, 0, st>>>(g, 0, (float *)buf, F, ToF32());
+            else k_pack<float><<<nb, TPB, 0, st>>>(g, 0, (const float *)buf, F, FromF32());
         }
         return 0;
     }
     if (what == 3) {   // SGSVIS (0:M1,0:M2,0:M3), device to host only, working precision
         if (dir == 0 || !ch->les[0]) return C3D_EINVAL;
-        if (!mixed) k_pack<double><<<nb, TPB, 0, st>>>(g, 0, (const double *)ch->les[0], ch->stage, FromF64());
-        else k_pack<float><<<nb, TPB, 0, st>>>(g, 0, (const float *)ch->les[0], ch->stage, FromF32());
+        if (!mixed) k_pack<double><<<nb, TPB, 0, st>>>(g, 0, (const double *)ch->les[0], F, FromF64());
+        else k_pack<float><<<nb, TPB, 0, st>>>(g, 0, (const float *)ch->les[0], F, FromF32());
         return 0;
     }
     void *dev = (what == 2) ? ch->hh[ch->cur][comp]
                             : (what == 1) ? ch->p : (comp == 0 ? ch->u : comp == 1 ? ch->v : ch->w);
     if (!mixed) {
-        if (dir == 0) k_unpack<double><<<nb, TPB, 0, st>>>(g, what, (double *)dev, ch->stage, ToF64());
-        else k_pack<double><<<nb, TPB, 0, st>>>(g, what, (const double *)dev, ch->stage, FromF64());
+        if (dir == 0) k_unpack<double><<<nb, TPB, 0, st>>>(g, what, (double *)dev, F, ToF64());
+        else k_pack<double><<<nb, TPB, 0, st>>>(g, what, (const double *)dev, F, FromF64());
     } else if (what == 2) {
-        if (dir == 0) k_unpack<float><<<nb, TPB, 0, st>>>(g, what, (float *)dev, ch->stage, ToF32());
-        else k_pack<float><<<nb, TPB, 0, st>>>(g, what, (const float *)dev, ch->stage, FromF32());
+        if (dir == 0) k_unpack<float><<<nb, TPB, 0, st>>>(g, what, (float *)dev, F, ToF32());
+        else k_pack<float><<<nb, TPB, 0, st>>>(g, what, (const float *)dev, F, FromF32());
     } else {
-        if (dir == 0) k_unpack<float2><<<nb, TPB, 0, st>>>(g, what, (float2 *)dev, ch->stage, ToDF());
-        else k_pack<float2><<<nb, TPB, 0, st>>>(g, what, (const float2 *)dev, ch->stage, FromDF());
+        if (dir == 0) k_unpack<float2><<<nb, TPB, 0, st>>>(g, what, (float2 *)dev, F, ToDF());
+        else k_pack<float2><<<nb, TPB, 0, st>>>(g, what, (const float2 *)dev, F, FromDF());
     }
     return 0;
 }
