@@ -535,7 +535,7 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
     rc = launch_poisson_tables(ch);
     if (rc) return fail(rc);
     // FFT plans and twiddles: [x: N1M/2][z: N3M][x post-processing: N1M/2+1]
-    ch->tune = Tune{{16, 16, 16, 16, 16}, 4, 8, 0, 0, 0, 0};
+    ch->tune = Tune{{16, 16, 16, 16, 16}, 4, 8, 0, 0, 0, 0, 0};
     ch->fx = make_plan(g.n1m / 2, 0);
     ch->fz = make_plan(g.n3m, 0);
     if (ch->fx.nst < 0 || ch->fz.nst < 0) { set_error("FFT plan index arithmetic"); return fail(C3D_EINVAL); }
@@ -759,6 +759,10 @@ int c3d_set_wall_iter_cap(c3d_channel *ch, int cap) {
 
 // After a completed step: the wall model's non-convergence flag (WMODEL = 1 with an SGS model).
 static int check_wall_flag(c3d_channel *ch, const double *scal_host) {
+    if (scal_host[SCAL_PIPEERR] != 0.0) {
+        set_error("a shared-memory bulk-copy stage did not complete within its wait limit");
+        return C3D_ECUDA;
+    }
     if (ch->files != 0 && ch->wmodel == 1 && scal_host[SCAL_WALLERR] != 0.0) {
         set_error("wall model: the Newton iteration for u_tau did not converge within the iteration cap");
         return C3D_ENOTCONV;
@@ -979,12 +983,9 @@ int c3d_op_get(c3d_channel *ch, double *f) {
 int c3d_sync(c3d_channel *ch) {
     if (!ch) return C3D_EINVAL;
     CK(cudaStreamSynchronize(ch->stream));
-    if (ch->files != 0 && ch->wmodel == 1) {
-        double sc[SCAL_COUNT];
-        CK(cudaMemcpy(sc, ch->scal, sizeof(sc), cudaMemcpyDeviceToHost));
-        return check_wall_flag(ch, sc);
-    }
-    return 0;
+    double sc[SCAL_COUNT];
+    CK(cudaMemcpy(sc, ch->scal, sizeof(sc), cudaMemcpyDeviceToHost));
+    return check_wall_flag(ch, sc);
 }
 
 int c3d_last_step_stats(c3d_channel *ch, double *ms, int *launches) {
@@ -1015,7 +1016,7 @@ bool tune_ok(const c3d_channel *ch, const Tune &t) {
     const bool xw = t.xw == 2 || t.xw == 4 || t.xw == 8;
     const bool tw = t.twz == 4 || t.twz == 8 || t.twz == 16;
     return zl && xw && tw && t.fxp >= 0 && t.fxp <= 2 && t.fzp >= 0 && t.fzp <= 2 && (t.zsplit == 0 || t.zsplit == 1) &&
-           (t.xsplit == 0 || t.xsplit == 1);
+           (t.xsplit == 0 || t.xsplit == 1) && (t.xbulk == 0 || t.xbulk == 2 || t.xbulk == 3);
 }
 
 // Sets the schedule; the FFT plans get the new radix order and keep their twiddle tables.
@@ -1056,13 +1057,14 @@ int c3d_get_schedule(c3d_channel *ch, int *sched) {
     const Tune &t = ch->tune;
     for (int q = 0; q < 5; ++q) sched[q] = t.zl[q];
     sched[5] = t.xw; sched[6] = t.twz; sched[7] = t.fxp; sched[8] = t.fzp; sched[9] = t.zsplit; sched[10] = t.xsplit;
+    sched[11] = t.xbulk;
     return 0;
 }
 
 int c3d_set_schedule(c3d_channel *ch, const int *sched) {
     if (!ch || !sched) { set_error("null argument"); return C3D_EINVAL; }
     Tune t{{sched[0], sched[1], sched[2], sched[3], sched[4]}, sched[5], sched[6], sched[7], sched[8], sched[9],
-           sched[10]};
+           sched[10], sched[11]};
     if (!tune_ok(ch, t)) { set_error("invalid schedule"); return C3D_EINVAL; }
     apply_tune(ch, t);
     return 0;
@@ -1099,7 +1101,7 @@ int c3d_autotune(c3d_channel *ch, int *sched) {
     sc->have_state = 1;
     const double dt = ch->dt_cached > 0 ? ch->dt_cached : 1e-3;
     // knob q: 0-4 the segment length of zA..zE, 5 x rows per block, 6 z-FFT tile, 7/8 plans,
-    // 9 zA split, 10 xA split
+    // 9 zA split, 10 xA split, 11 bulk-copy stages of the x passes
     struct Group { int knob; std::vector<int> cand; std::vector<std::string> kernels; };
     const Group groups[] = {
         {9, {0, 1}, {"zA"}}, {10, {0, 1}, {"xA"}},
@@ -1109,9 +1111,10 @@ int c3d_autotune(c3d_channel *ch, int *sched) {
         {6, {4, 8, 16}, {"fftz_fwd", "fftz_inv"}},
         {8, {0, 1, 2}, {"fftz_fwd", "fftz_inv"}},
         {7, {0, 1, 2}, {"xC", "xD"}},
+        {11, {0, 2, 3}, {"xC"}},
     };
     auto knob = [](Tune &t, int q) -> int & {
-        return q < 5 ? t.zl[q] : q == 5 ? t.xw : q == 6 ? t.twz : q == 7 ? t.fxp : q == 8 ? t.fzp : q == 9 ? t.zsplit : t.xsplit;
+        return q < 5 ? t.zl[q] : q == 5 ? t.xw : q == 6 ? t.twz : q == 7 ? t.fxp : q == 8 ? t.fzp : q == 9 ? t.zsplit : q == 10 ? t.xsplit : t.xbulk;
     };
     Tune best = ch->tune;
     for (const Group &gp : groups) {

@@ -45,8 +45,8 @@ struct StepArgs {
     Geo g;
     MetR<R> m;                          // wall-normal metrics in precision R
     // constants in precision R, computed once on the host in FP64:
-    // 1/RE, 12 DX1^2, 24 DX1, 12 DX3^2, 24 DX3, 1/DT
-    R re1, f12x, f24x, f12z, f24z, rdt;
+    // 1/RE, 12 DX1^2, 24 DX1, 12 DX3^2, 24 DX3, 1/DT, 1/(N1M N3M) (inverse-FFT scale)
+    R re1, f12x, f24x, f12z, f24z, rdt, xscale;
     S *u, *v, *w, *p;                   // state
     R *hh[3];                           // nonlinear terms of this step (written)
     const R *ho[3];                     // nonlinear terms of the previous step (AB2)
@@ -84,7 +84,8 @@ enum {
     SCAL_NONFIN = 11,
     SCAL_WSMC = 12,    // 3 values: /WSMEM/ WSM as the SGS model and the wall model see it
     SCAL_WALLERR = 15, // 1 when a wall point's Newton iteration hit its cap in the last step
-    SCAL_COUNT = 16
+    SCAL_PIPEERR = 16, // 1 when a bulk-copy stage wait gave up (sticky)
+    SCAL_COUNT = 17
 };
 
 // Launch schedule of one channel, chosen by c3d_autotune per grid shape.
@@ -102,6 +103,7 @@ struct Tune {
     int zl[5], xw, twz, fxp, fzp;
     int zsplit;   // zA as one kernel (0) or as its three sweeps in three kernels (1)
     int xsplit;   // xA as one kernel (0) or as its u, v, w pieces in three kernels (1)
+    int xbulk;    // x passes with rows staged by a bulk-copy ring of this many stages (0: off)
 };
 
 // Arguments of the pressure refinement (mixed form with C3D_MIXED_IR): double-float

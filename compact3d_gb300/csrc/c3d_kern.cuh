@@ -267,6 +267,77 @@ __device__ __forceinline__ void srow_store(T *__restrict__ g, const T (&v)[C], T
     __syncwarp();
 }
 
+// Lane-chunk row load from a 16-byte aligned shared-memory row (a bulk-copy stage).
+template <typename T, int C>
+__device__ __forceinline__ void crow_load(T (&v)[C], const T *s, int lane, int P) {
+    constexpr int B = (int)sizeof(T) * C;
+    if (lane < P) {
+        const T *p = s + lane * C;
+        if constexpr (B % 16 == 0) {
+            uint4 q[B / 16];
+#pragma unroll
+            for (int i = 0; i < B / 16; ++i) q[i] = reinterpret_cast<const uint4 *>(p)[i];
+            memcpy(v, q, B);
+        } else if constexpr (B % 8 == 0) {
+            uint2 q[B / 8];
+#pragma unroll
+            for (int i = 0; i < B / 8; ++i) q[i] = reinterpret_cast<const uint2 *>(p)[i];
+            memcpy(v, q, B);
+        } else {
+#pragma unroll
+            for (int t = 0; t < C; ++t) v[t] = p[t];
+        }
+    } else {
+#pragma unroll
+        for (int t = 0; t < C; ++t) v[t] = T();
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Bulk-copy ring: one lane of a warp streams whole rows (contiguous byte runs) from
+// global memory into shared-memory stages with cp.async.bulk; each stage completes on
+// its own mbarrier (transaction count = the stage's bytes).  Waits are bounded by the
+// global timer and report failure instead of spinning forever.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+// Makes initialised barriers visible to the bulk-copy (async) proxy.
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// Orders this thread's earlier shared-memory accesses before later async-proxy writes.
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+// Global -> shared bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned).
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *b) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_addr(b))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(smem_addr(b)), "r"(parity) : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ unsigned long long gtimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// Waits for phase `parity` of barrier b to complete; false after about one second.
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity) {
+    if (mbar_try_wait(b, parity)) return true;
+    const unsigned long long t0 = gtimer_ns();
+    while (!mbar_try_wait(b, parity))
+        if (gtimer_ns() - t0 > 1000000000ull) return false;
+    return true;
+}
+
 // Bytes of the per-warp staging buffer for rows of n1m points.
 __host__ __device__ inline size_t stage_bytes(int n1m, int C) { return (size_t)(n1m + n1m / C + 2) * 8; }
 
@@ -301,18 +372,19 @@ template <typename C2> __device__ __forceinline__ const C2 *twsel(const FftPlan 
 template <> __device__ __forceinline__ const double2 *twsel<double2>(const FftPlan &p) { return p.tw64; }
 template <> __device__ __forceinline__ const float2 *twsel<float2>(const FftPlan &p) { return p.tw32; }
 
-// X_s = sum_r v_r exp(sign 2 pi i r s / p), p in {2,3,4}
-template <typename C2>
-__device__ __forceinline__ void dftp(C2 (&v)[4], int p, int sign) {
+// X_s = sum_r v_r exp(SIGN 2 pi i r s / P), P in {2,3,4}, radix and direction fixed at
+// compile time.
+template <int P, int SIGN, typename C2>
+__device__ __forceinline__ void dftc(C2 (&v)[P]) {
     typedef decltype(v[0].x) T;
-    if (p == 4) {
+    if constexpr (P == 4) {
         C2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
-        C2 t2 = cadd(v[1], v[3]), t3 = cmuli(csub(v[1], v[3]), sign);
+        C2 t2 = cadd(v[1], v[3]), t3 = cmuli(csub(v[1], v[3]), SIGN);
         v[0] = cadd(t0, t2);
         v[2] = csub(t0, t2);
         v[1] = cadd(t1, t3);
         v[3] = csub(t1, t3);
-    } else if (p == 2) {
+    } else if constexpr (P == 2) {
         C2 a = v[0];
         v[0] = cadd(a, v[1]);
         v[1] = csub(a, v[1]);
@@ -322,7 +394,7 @@ __device__ __forceinline__ void dftp(C2 (&v)[4], int p, int sign) {
         C2 a;
         a.x = v[0].x - (T)0.5 * t.x;
         a.y = v[0].y - (T)0.5 * t.y;
-        C2 b = cmuli(u, sign);
+        C2 b = cmuli(u, SIGN);
         b.x *= h;
         b.y *= h;
         v[0] = cadd(v[0], t);
@@ -331,41 +403,50 @@ __device__ __forceinline__ void dftp(C2 (&v)[4], int p, int sign) {
     }
 }
 
-// Stockham FFT of 2^lsh sequences of length pl.n at buf[q*es + l*ls]; threads tid..nthr
-// of the warp (BLOCK=false) or block (BLOCK=true) cooperate.  Returns the result buffer.
-template <typename C2, bool BLOCK>
-__device__ C2 *fft_smem(C2 *a, C2 *b, const FftPlan &pl, int lsh, int es, int ls, int sign, int tid, int nthr) {
-    const int n = pl.n, lmask = (1 << lsh) - 1;
+// One radix-P Stockham stage: a -> b over 2^lsh interleaved sequences of length n
+// (element q of sequence l at q*es + l*ls).  BLOCK = false is one warp on one
+// sequence (lsh = 0, es = 1, ls = 0, 32 threads), so its index arithmetic folds.
+template <int P, int SIGN, bool BLOCK, typename C2>
+__device__ __forceinline__ void fft_stage(const C2 *__restrict__ a, C2 *__restrict__ b, const C2 *__restrict__ tw,
+                                          int n, int Ns, unsigned mg, int tstep, int lsh, int es, int ls, int tid,
+                                          int nthr) {
+    if constexpr (!BLOCK) { lsh = 0; es = 1; ls = 0; nthr = 32; }
+    const int np = n / P, lmask = (1 << lsh) - 1;
+    for (int idx = tid; idx < (np << lsh); idx += nthr) {
+        const int l = idx & lmask, jj = idx >> lsh;
+        const int q = Ns == 1 ? jj : (int)__umulhi((unsigned)jj, mg);   // jj / Ns
+        const int kq = jj - q * Ns;
+        C2 v[P];
+#pragma unroll
+        for (int r = 0; r < P; ++r) v[r] = a[(jj + r * np) * es + l * ls];
+        if (Ns > 1) {
+            const int t1 = kq * tstep;
+#pragma unroll
+            for (int r = 1; r < P; ++r) {
+                C2 t = __ldg(&tw[r * t1]);
+                if constexpr (SIGN > 0) t.y = -t.y;
+                v[r] = cmul(v[r], t);
+            }
+        }
+        dftc<P, SIGN>(v);
+        const int base = q * Ns * P + kq;
+#pragma unroll
+        for (int r = 0; r < P; ++r) b[(base + r * Ns) * es + l * ls] = v[r];
+    }
+}
+
+template <typename C2, bool BLOCK, int SIGN>
+__device__ __forceinline__ C2 *fft_run(C2 *a, C2 *b, const FftPlan &pl, int lsh, int es, int ls, int tid, int nthr) {
+    const int n = pl.n;
     const C2 *tw = twsel<C2>(pl);
     int Ns = 1;
     for (int s = 0; s < pl.nst; ++s) {
         const int p = pl.rad[s];
-        const int np = n / p;
         const int tstep = n / (Ns * p);
         const unsigned mg = pl.dmag[s];
-        for (int idx = tid; idx < (np << lsh); idx += nthr) {
-            const int l = idx & lmask, jj = idx >> lsh;
-            const int q = Ns == 1 ? jj : (int)__umulhi((unsigned)jj, mg);   // jj / Ns
-            const int kq = jj - q * Ns;
-            C2 v[4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-                if (r < p) v[r] = a[(jj + r * np) * es + l * ls];
-            if (Ns > 1) {
-#pragma unroll
-                for (int r = 1; r < 4; ++r)
-                    if (r < p) {
-                        C2 t = __ldg(&tw[kq * r * tstep]);
-                        if (sign > 0) t.y = -t.y;
-                        v[r] = cmul(v[r], t);
-                    }
-            }
-            dftp(v, p, sign);
-            const int base = q * Ns * p + kq;
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-                if (r < p) b[(base + r * Ns) * es + l * ls] = v[r];
-        }
+        if (p == 4) fft_stage<4, SIGN, BLOCK>(a, b, tw, n, Ns, mg, tstep, lsh, es, ls, tid, nthr);
+        else if (p == 2) fft_stage<2, SIGN, BLOCK>(a, b, tw, n, Ns, mg, tstep, lsh, es, ls, tid, nthr);
+        else fft_stage<3, SIGN, BLOCK>(a, b, tw, n, Ns, mg, tstep, lsh, es, ls, tid, nthr);
         if (BLOCK) __syncthreads(); else __syncwarp();
         C2 *t = a;
         a = b;
@@ -373,6 +454,16 @@ __device__ C2 *fft_smem(C2 *a, C2 *b, const FftPlan &pl, int lsh, int es, int ls
         Ns *= p;
     }
     return a;
+}
+
+// Stockham FFT of 2^lsh sequences of length pl.n at buf[q*es + l*ls]; threads tid..nthr
+// of the warp (BLOCK=false: one sequence, lsh = 0, es = 1, ls = 0) or block (BLOCK=true)
+// cooperate.  Returns the result buffer.
+template <typename C2, bool BLOCK>
+__device__ __forceinline__ C2 *fft_smem(C2 *a, C2 *b, const FftPlan &pl, int lsh, int es, int ls, int sign, int tid,
+                                        int nthr) {
+    if (sign < 0) return fft_run<C2, BLOCK, -1>(a, b, pl, lsh, es, ls, tid, nthr);
+    return fft_run<C2, BLOCK, +1>(a, b, pl, lsh, es, ls, tid, nthr);
 }
 
 // L2 prefetch of one address (fire and forget)

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(TPB) k_op_x(StepArgs<R> a, int op, const R *in
             __syncwarp();
             C2 *Zr = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, +1, lane, 32);
             const R *rz = reinterpret_cast<const R *>(Zr);
-            const R scale = (R)(1.0 / ((double)g.n1m * (double)g.n3m));
+            const R scale = a.xscale;
             R v[C];
 #pragma unroll
             for (int t = 0; t < C; ++t) v[t] = lane < P ? rz[lane * C + t] * scale : R(0);

@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(TPB) k_ir_d(StepArgs<float> a) {
     C2 *bufa = reinterpret_cast<C2 *>(wb + sbytes);
     C2 *bufb = bufa + (M + 1);
     const C2 *twx = reinterpret_cast<const C2 *>(a.twx32);
-    const float scale = (float)(1.0 / ((double)g.n1m * (double)g.n3m)), f24 = a.f24x;
+    const float scale = a.xscale, f24 = a.f24x;
     const int nrows = g.n2m * g.n3m;
     for (int row = blockIdx.x * (TPB / 32) + wid; row < nrows; row += gridDim.x * (TPB / 32)) {
         const int j = 1 + row / g.n3m, k = row % g.n3m;

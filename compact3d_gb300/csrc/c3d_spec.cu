@@ -17,16 +17,17 @@ __global__ void __launch_bounds__(TPB) k_fftz(StepArgs<R> a, int sign, int tw) {
     const int kx0 = tile * tw;
     const int w = min(tw, g.n1h - kx0);
     C2 *S = reinterpret_cast<C2 *>(a.spec) + (long long)plane * n * g.n1h + kx0;
+    const int lsh = __ffs(tw) - 1, lm = tw - 1;   // tw is a power of 2
     for (int e = threadIdx.x; e < n * tw; e += blockDim.x) {
-        int q = e / tw, l = e % tw;
-        if (l < w) A[e] = S[(long long)q * g.n1h + l];
+        const int q = e >> lsh, l = e & lm;
+        if (l < w) A[e] = S[q * g.n1h + l];
         else { A[e].x = 0; A[e].y = 0; }
     }
     __syncthreads();
-    C2 *Z = fft_smem<C2, true>(A, B, a.fz, __ffs(tw) - 1, tw, 1, sign, threadIdx.x, blockDim.x);   // tw is a power of 2
+    C2 *Z = fft_smem<C2, true>(A, B, a.fz, lsh, tw, 1, sign, threadIdx.x, blockDim.x);
     for (int e = threadIdx.x; e < n * tw; e += blockDim.x) {
-        int q = e / tw, l = e % tw;
-        if (l < w) S[(long long)q * g.n1h + l] = Z[e];
+        const int q = e >> lsh, l = e & lm;
+        if (l < w) S[q * g.n1h + l] = Z[e];
     }
 }
 

@@ -293,6 +293,7 @@ static StepArgs<R> make_args(c3d_channel *ch, double dt) {
     a.f12z = (R)(12.0 * ch->g.dx3q);
     a.f24z = (R)(24.0 * ch->g.dx3);
     a.rdt = (R)(1.0 / dt);
+    a.xscale = (R)(1.0 / ((double)ch->g.n1m * (double)ch->g.n3m));
     auto mk = [&](double A, double B, bool fp32) {
         Cyc<R> c;
         double beta = B / A;

@@ -10,6 +10,11 @@
 #include <algorithm>
 #include "c3d_kern.cuh"
 
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <algorithm>
+
 namespace c3d {
 
 // ---------------------------------------------------------------------------------
@@ -130,7 +135,7 @@ __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
 #pragma unroll
                 for (int t = 0; t < C; ++t) {
                     R visc = RE1 * ST::yvisc(DYPj, DYCj, DYMj, Z0, vp[t], vc[t], vm[t]);
-                    R pg = ST::d(pc[t], pm[t]) / Hj;
+                    R pg = ST::d(pc[t], pm[t]) * Hj1;
                     acc[t] = (-pg + visc) + RE1 * d[t];
                     hh[t] = Hj1 * Sten<R>::vv(vp[t], vc[t], vm[t]);
                 }
@@ -284,93 +289,182 @@ __global__ void __launch_bounds__(XMAXT) k_xB(StepArgs<R> a) {
 // ---------------------------------------------------------------------------------
 // xC: RDP = div(UH)/DT and its real-to-complex FFT along x
 // ---------------------------------------------------------------------------------
-template <typename R, int C>
+// Row operand of an x pass: a global row (read through the read-only path) or a row
+// already staged in shared memory by the bulk-copy ring.
+template <bool SH, typename T, int C>
+__device__ __forceinline__ void xrow(T (&v)[C], const T *p, T *sb, int lane, int P) {
+    if constexpr (SH) crow_load(v, p, lane, P);
+    else srow_load(v, p, sb, lane, P);
+}
+
+// Shared-memory layout of one xC stage (mixed and FP64 forms alike): the rows
+// U(J), DH1(J), RDPZ(J), V(J), DH2(J), V(J+1), DH2(J+1) of one (J, K).
+template <typename R>
+struct XcStage {
+    typedef typename SType<R>::S S;
+    int u, d0, z, vc, dc, vp, dp, bytes;
+    __host__ __device__ XcStage(int n) {
+        const int sS = n * (int)sizeof(S), sR = n * (int)sizeof(R);
+        u = 0; d0 = sS; z = d0 + sR; vc = z + sR; dc = vc + sS; vp = dc + sR; dp = vp + sS; bytes = dp + sR;
+    }
+};
+
+// One row of xC: the x part of div(UH)/DT from U + DH1 (compact (1,22,1) derivative),
+// the y part from V + DH2 on planes J and J+1, plus RDPZ; then the real-to-complex FFT.
+template <bool SH, typename R, int C>
+__device__ __forceinline__ void xc_row(const StepArgs<R> &a, int j, int k, const typename SType<R>::S *u,
+                                       const R *d0, const typename SType<R>::S *vc, const R *dc,
+                                       const typename SType<R>::S *vp, const R *dp, const R *zr,
+                                       unsigned char *sbuf, typename Cx<R>::T *bufa, typename Cx<R>::T *bufb,
+                                       int lane) {
+    typedef typename SType<R>::S S;
+    typedef typename Cx<R>::T C2;
+    const Geo &g = a.g;
+    const int P = g.n1m / C, M = g.n1m / 2;
+    S *sbS = reinterpret_cast<S *>(sbuf);
+    R *sbR = reinterpret_cast<R *>(sbuf);
+    R *rbuf = reinterpret_cast<R *>(bufa);
+    const R rdt = a.rdt, f24 = a.f24x;
+    R d[C], base[C];
+    {
+        S uc[C];
+        R dd[C];
+        xrow<SH>(uc, u, sbS, lane, P);
+        xrow<SH>(dd, d0, sbR, lane, P);
+        S nu = snext(uc[0], lane, P);
+        R nd = snext(dd[0], lane, P);
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            S ru = (t == C - 1) ? nu : uc[t + 1];
+            R rd = (t == C - 1) ? nd : dd[t + 1];
+            d[t] = f24 * Sten<R>::dd(ru, rd, uc[t], dd[t]);
+        }
+        xsolve(d, lane, P, a.c22x);
+    }
+    {
+        const bool up = (j + 1 <= g.n2m), lo = (j >= 2);
+        S vpv[C], vcv[C];
+        R dpv[C], dcv[C];
+        if (up) { xrow<SH>(vpv, vp, sbS, lane, P); xrow<SH>(dpv, dp, sbR, lane, P); }
+        if (lo) { xrow<SH>(vcv, vc, sbS, lane, P); xrow<SH>(dcv, dc, sbR, lane, P); }
+        const R ry = a.m.rdy[j] * rdt;   // 1/(DY(J) DT)
+        const S zs = S();
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            // (FJUP*UH2(J+1) - FJUM*UH2(J))/DY(J), UH2 = V + delta2, UH2 = 0 on the walls
+            R dv = Sten<R>::dd(up ? vpv[t] : zs, up ? dpv[t] : R(0), lo ? vcv[t] : zs, lo ? dcv[t] : R(0));
+            base[t] = dv * ry;
+        }
+    }
+    {
+        R zc[C];
+        xrow<SH>(zc, zr, sbR, lane, P);
+#pragma unroll
+        for (int t = 0; t < C; ++t) d[t] = (base[t] + d[t] * rdt) + zc[t];
+    }
+    // real row -> shared memory as M complex values, FFT, post-process to N1M/2+1 modes
+    if (lane < P) {
+#pragma unroll
+        for (int t = 0; t < C; ++t) rbuf[lane * C + t] = d[t];
+    }
+    __syncwarp();
+    C2 *Z = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, -1, lane, 32);
+    const C2 *twx;
+    if constexpr (sizeof(R) == 8) twx = reinterpret_cast<const C2 *>(a.twx64);
+    else twx = reinterpret_cast<const C2 *>(a.twx32);
+    C2 *Sp = reinterpret_cast<C2 *>(a.spec) + ((long long)(j - 1) * g.n3m + k) * g.n1h;
+    for (int kx = lane; kx <= M; kx += 32) {
+        C2 zk = Z[kx == M ? 0 : kx], zm = cconj(Z[kx == 0 ? 0 : M - kx]);
+        C2 E, O;
+        E.x = (R)0.5 * (zk.x + zm.x);
+        E.y = (R)0.5 * (zk.y + zm.y);
+        C2 df = csub(zk, zm);
+        O.x = (R)0.5 * df.y;
+        O.y = (R)-0.5 * df.x;
+        Sp[kx] = cadd(E, cmul(twx[kx], O));
+    }
+    __syncwarp();
+}
+
+// ---------------------------------------------------------------------------------
+// xC: RDP = div(UH)/DT and its real-to-complex FFT along x.  NS = 0: every warp reads
+// its rows from global memory (one row per warp).  NS >= 2: persistent warps, each with
+// an NS-stage bulk-copy ring that fetches the rows of its next NS-1 (J, K) while it
+// computes the current one.
+// ---------------------------------------------------------------------------------
+template <typename R, int C, int NS>
 __global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const R *d1) {
     typedef typename SType<R>::S S;
     typedef typename Cx<R>::T C2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Geo g = a.g;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int P = g.n1m / C;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, wpb = (int)(blockDim.x >> 5);
     const int M = g.n1m / 2;
-    const size_t sbytes = stage_bytes(g.n1m, C), fbytes = 2 * (size_t)(M + 1) * sizeof(C2);
-    unsigned char *wb = smem_raw + wid * (sbytes + fbytes);
-    S *sbS = reinterpret_cast<S *>(wb);
-    R *sbR = reinterpret_cast<R *>(wb);
-    C2 *bufa = reinterpret_cast<C2 *>(wb + sbytes);
-    C2 *bufb = bufa + (M + 1);
-    R *rbuf = reinterpret_cast<R *>(bufa);
     const int nrows = g.n2m * g.n3m;
-    const R rdt = a.rdt, f24 = a.f24x;
-    const R rdtp = (R)a.dt;
-    const C2 *twx;
-    if constexpr (sizeof(R) == 8) twx = reinterpret_cast<const C2 *>(a.twx64);
-    else twx = reinterpret_cast<const C2 *>(a.twx32);
-    for (int row = blockIdx.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += gridDim.x * (int)(blockDim.x >> 5)) {
-        const int j = 1 + row / g.n3m, k = row % g.n3m;
-        const long long o = fidx(g, 0, j, k), op = fidx(g, 0, j + 1, k);
-        {
-            const int rs_ = g.n1m * (int)sizeof(S), rr_ = g.n1m * (int)sizeof(R);
-            pf_row(a.u + o, rs_, lane); pf_row(d0 + o, rr_, lane); pf_row(a.rdpz + o, rr_, lane);
-            if (j >= 2) { pf_row(a.v + o, rs_, lane); pf_row(d1 + o, rr_, lane); }
-            if (j + 1 <= g.n2m) { pf_row(a.v + op, rs_, lane); pf_row(d1 + op, rr_, lane); }
-        }
-        R d[C], base[C];
-        {
-            S uc[C];
-            R dd[C];
-            srow_load(uc, a.u + o, sbS, lane, P);
-            srow_load(dd, d0 + o, sbR, lane, P);
-            S nu = snext(uc[0], lane, P);
-            R nd = snext(dd[0], lane, P);
-#pragma unroll
-            for (int t = 0; t < C; ++t) {
-                S ru = (t == C - 1) ? nu : uc[t + 1];
-                R rd = (t == C - 1) ? nd : dd[t + 1];
-                d[t] = f24 * Sten<R>::dd(ru, rd, uc[t], dd[t]);
+    const size_t fbytes = 2 * (size_t)(M + 1) * sizeof(C2);
+    if constexpr (NS == 0) {
+        const size_t sbytes = stage_bytes(g.n1m, C);
+        unsigned char *wb = smem_raw + wid * (sbytes + fbytes);
+        C2 *bufa = reinterpret_cast<C2 *>(wb + sbytes);
+        for (int row = blockIdx.x * wpb + wid; row < nrows; row += gridDim.x * wpb) {
+            const int j = 1 + row / g.n3m, k = row % g.n3m;
+            const long long o = fidx(g, 0, j, k), op = fidx(g, 0, j + 1, k);
+            {
+                const int rs_ = g.n1m * (int)sizeof(S), rr_ = g.n1m * (int)sizeof(R);
+                pf_row(a.u + o, rs_, lane); pf_row(d0 + o, rr_, lane); pf_row(a.rdpz + o, rr_, lane);
+                if (j >= 2) { pf_row(a.v + o, rs_, lane); pf_row(d1 + o, rr_, lane); }
+                if (j + 1 <= g.n2m) { pf_row(a.v + op, rs_, lane); pf_row(d1 + op, rr_, lane); }
             }
-            xsolve(d, lane, P, a.c22x);
+            xc_row<false, R, C>(a, j, k, a.u + o, d0 + o, a.v + o, d1 + o, a.v + op, d1 + op, a.rdpz + o, wb,
+                                bufa, bufa + (M + 1), lane);
         }
-        {
+    } else {
+        const XcStage<R> L(g.n1m);
+        // per warp: NS barriers (16 bytes reserved each), NS stages, the FFT buffers
+        const size_t wbytes = 16 * NS + (size_t)NS * L.bytes + fbytes;
+        unsigned char *wb = smem_raw + wid * wbytes;
+        uint64_t *bar = reinterpret_cast<uint64_t *>(wb);
+        unsigned char *stg = wb + 16 * NS;
+        C2 *bufa = reinterpret_cast<C2 *>(stg + (size_t)NS * L.bytes);
+        const int nw = gridDim.x * wpb, gw = blockIdx.x * wpb + wid;
+        const uint32_t sS = g.n1m * (uint32_t)sizeof(S), sR = g.n1m * (uint32_t)sizeof(R);
+        if (lane == 0) {
+            for (int s = 0; s < NS; ++s) mbar_init(bar + s, 1);
+            mbar_init_fence();
+        }
+        __syncwarp();
+        auto issue = [&](int row, int s) {   // lane 0 only
+            const int j = 1 + row / g.n3m, k = row % g.n3m;
+            const long long o = fidx(g, 0, j, k), op = fidx(g, 0, j + 1, k);
             const bool up = (j + 1 <= g.n2m), lo = (j >= 2);
-            S vp[C], vc[C];
-            R dp_[C], dc_[C];
-            if (up) { srow_load(vp, a.v + op, sbS, lane, P); srow_load(dp_, d1 + op, sbR, lane, P); }
-            if (lo) { srow_load(vc, a.v + o, sbS, lane, P); srow_load(dc_, d1 + o, sbR, lane, P); }
-            const R dyj = a.m.dy[j];
-            const S zs = S();
-#pragma unroll
-            for (int t = 0; t < C; ++t) {
-                // (FJUP*UH2(J+1) - FJUM*UH2(J))/DY(J), UH2 = V + delta2, UH2 = 0 on the walls
-                R dv = Sten<R>::dd(up ? vp[t] : zs, up ? dp_[t] : R(0), lo ? vc[t] : zs, lo ? dc_[t] : R(0));
-                base[t] = dv / dyj * rdt;
+            unsigned char *st = stg + (size_t)s * L.bytes;
+            fence_async_smem();
+            mbar_expect_tx(bar + s, sS + 2 * sR + (lo ? sS + sR : 0u) + (up ? sS + sR : 0u));
+            bulk_g2s(st + L.u, a.u + o, sS, bar + s);
+            bulk_g2s(st + L.d0, d0 + o, sR, bar + s);
+            bulk_g2s(st + L.z, a.rdpz + o, sR, bar + s);
+            if (lo) { bulk_g2s(st + L.vc, a.v + o, sS, bar + s); bulk_g2s(st + L.dc, d1 + o, sR, bar + s); }
+            if (up) { bulk_g2s(st + L.vp, a.v + op, sS, bar + s); bulk_g2s(st + L.dp, d1 + op, sR, bar + s); }
+        };
+        if (lane == 0)
+            for (int s = 0; s < NS - 1; ++s)
+                if (gw + s * nw < nrows) issue(gw + s * nw, s);
+        int it = 0;
+        for (int row = gw; row < nrows; row += nw, ++it) {
+            const int s = it % NS;
+            const int nrow = row + (NS - 1) * nw;
+            if (lane == 0 && nrow < nrows) issue(nrow, (it + NS - 1) % NS);
+            if (!mbar_wait(bar + s, (uint32_t)(it / NS) & 1u)) {
+                if (lane == 0) a.scal[SCAL_PIPEERR] = 1.0;
+                return;
             }
+            const int j = 1 + row / g.n3m, k = row % g.n3m;
+            const unsigned char *st = stg + (size_t)s * L.bytes;
+            xc_row<true, R, C>(a, j, k, reinterpret_cast<const S *>(st + L.u), reinterpret_cast<const R *>(st + L.d0),
+                               reinterpret_cast<const S *>(st + L.vc), reinterpret_cast<const R *>(st + L.dc),
+                               reinterpret_cast<const S *>(st + L.vp), reinterpret_cast<const R *>(st + L.dp),
+                               reinterpret_cast<const R *>(st + L.z), nullptr, bufa, bufa + (M + 1), lane);
         }
-        {
-            R zc[C];
-            srow_load(zc, a.rdpz + o, sbR, lane, P);
-#pragma unroll
-            for (int t = 0; t < C; ++t) d[t] = (base[t] + d[t] / rdtp) + zc[t];
-        }
-        // real row -> shared memory as M complex values, FFT, post-process to N1M/2+1 modes
-        if (lane < P) {
-#pragma unroll
-            for (int t = 0; t < C; ++t) rbuf[lane * C + t] = d[t];
-        }
-        __syncwarp();
-        C2 *Z = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, -1, lane, 32);
-        C2 *Sp = reinterpret_cast<C2 *>(a.spec) + ((long long)(j - 1) * g.n3m + k) * g.n1h;
-        for (int kx = lane; kx <= M; kx += 32) {
-            C2 zk = Z[kx == M ? 0 : kx], zm = cconj(Z[kx == 0 ? 0 : M - kx]);
-            C2 E, O;
-            E.x = (R)0.5 * (zk.x + zm.x);
-            E.y = (R)0.5 * (zk.y + zm.y);
-            C2 df = csub(zk, zm);
-            O.x = (R)0.5 * df.y;
-            O.y = (R)-0.5 * df.x;
-            Sp[kx] = cadd(E, cmul(twx[kx], O));
-        }
-        __syncwarp();
     }
 }
 
@@ -394,7 +488,7 @@ __global__ void __launch_bounds__(XMAXT) k_xD(StepArgs<R> a, const R *d0, const 
     const C2 *twx;
     if constexpr (sizeof(R) == 8) twx = reinterpret_cast<const C2 *>(a.twx64);
     else twx = reinterpret_cast<const C2 *>(a.twx32);
-    const R scale = (R)(1.0 / ((double)g.n1m * (double)g.n3m)), f24 = a.f24x;
+    const R scale = a.xscale, f24 = a.f24x;
     for (int row = blockIdx.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += gridDim.x * (int)(blockDim.x >> 5)) {
         const int j = 1 + row / g.n3m, k = row % g.n3m;
         const long long o = fidx(g, 0, j, k);
@@ -551,6 +645,49 @@ __global__ void __launch_bounds__(TPB) k_diag_x(StepArgs<R> a, double *divx, Cyc
 // ---------------------------------------------------------------------------------
 // launcher
 // ---------------------------------------------------------------------------------
+// Grid of a persistent kernel: as many blocks as fit on the device at once (at most
+// `want`), from the occupancy calculator, cached per (kernel, block, shared memory).
+static int persistent_grid(const void *fn, int nt, size_t smem, int want, int device) {
+    static std::mutex mu;
+    static std::map<std::tuple<const void *, int, size_t, int>, int> cache;
+    const auto key = std::make_tuple(fn, nt, smem, device);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    int per_sm;
+    if (it != cache.end()) per_sm = it->second;
+    else {
+        int nsm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, smem) != cudaSuccess) per_sm = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+        per_sm *= nsm;
+        cache[key] = per_sm;
+    }
+    return per_sm > 0 ? std::min(want, per_sm) : 0;
+}
+
+// xC through the bulk-copy ring (mixed form); false when this shape cannot use it (rows
+// not a multiple of 16 bytes, or the stages do not fit in shared memory).
+template <typename R, int C, int NS>
+static bool launch_xc_bulk(c3d_channel *ch, StepArgs<R> &a, int xw, const R *p0, const R *p1) {
+    typedef typename Cx<R>::T C2;
+    const Geo &g = ch->g;
+    if (g.n1m % 4 != 0) return false;
+    const XcStage<R> L(g.n1m);
+    const size_t wbytes = 16 * NS + (size_t)NS * L.bytes + 2 * (size_t)(g.n1m / 2 + 1) * sizeof(C2);
+    const size_t smem = wbytes * xw;
+    if (smem > 227 * 1024) return false;
+    auto fn = k_xC<R, C, NS>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    const int nrows = g.n2m * g.n3m;
+    const int grid = persistent_grid((const void *)fn, xw * 32, smem, nblk(nrows, xw), ch->device);
+    if (grid <= 0) return false;
+    fn<<<grid, xw * 32, smem, ch->stream>>>(a, p0, p1);
+    return true;
+}
+
 template <typename R, int C>
 static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl) {
     typedef typename Cx<R>::T C2;
@@ -585,11 +722,19 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
             k_xB<R, C><<<grid, nt, sb, st>>>(a);
             mark(ch, nl, "xB", N * 18 * Rb);
             break;
-        case 2:
-            cudaFuncSetAttribute(k_xC<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
-            k_xC<R, C><<<grid, nt, fb, st>>>(a, p0, p1);
+        case 2: {
+            bool done = false;
+            if constexpr (sizeof(R) == 4) {
+                if (ch->tune.xbulk == 2) done = launch_xc_bulk<R, C, 2>(ch, a, xw, p0, p1);
+                else if (ch->tune.xbulk == 3) done = launch_xc_bulk<R, C, 3>(ch, a, xw, p0, p1);
+            }
+            if (!done) {
+                cudaFuncSetAttribute(k_xC<R, C, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
+                k_xC<R, C, 0><<<grid, nt, fb, st>>>(a, p0, p1);
+            }
             mark(ch, nl, "xC", N * (16 + 4 * Rb));
             break;
+        }
         case 3:
             cudaFuncSetAttribute(k_xD<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
             k_xD<R, C><<<grid, nt, fb, st>>>(a, p0, p1);

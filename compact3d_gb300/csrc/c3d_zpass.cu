@@ -297,10 +297,10 @@ __global__ void __launch_bounds__(TPB) k_zD(StepArgs<R> a, const R *d2) {
     const R rr[1] = {a.c22z.r}, ss[1] = {a.c22z.s};
     WalkDivZ<R> f{a.w + o, d2 + o, n, s, a.f24z};
     zsweep<R, L, WM<R>::M22, 1>(out, k0, n, rr, ss, f);
-    const R rdt = (R)a.dt;
+    const R rdt = a.rdt;
     R *Q = a.rdpz + o;
 #pragma unroll
-    for (int t = 0; t < L; ++t) Q[(k0 + t) * s] = out[0][t] / rdt;
+    for (int t = 0; t < L; ++t) Q[(k0 + t) * s] = out[0][t] * rdt;
 }
 
 // UPCALC along z and the state update
@@ -336,13 +336,13 @@ __global__ void __launch_bounds__(TPB) k_zE(StepArgs<R> a, const R *d0, const R 
     S *W = a.w + o, *U = a.u + o, *V = a.v + o, *Pp = a.p + o;
     const R *D0 = d0 + o, *D1 = d1 + o, *D2 = d2 + o, *G1 = a.g1 + o;
     const R *DPm = a.dp + fidx(g, i, j - 1, 0);
-    const R Hj = a.m.h[j];
+    const R rHj = a.m.rh[j];
 #pragma unroll
     for (int t = 0; t < L; ++t) {
         const int kk = (k0 + t) * s;
         W[kk] = Sten<R>::upd(W[kk], D2[kk], dt * out[0][t], dtdm3);
         U[kk] = Sten<R>::upd(U[kk], D0[kk], dt * G1[kk], dtdm);
-        if (j >= 2) V[kk] = Sten<R>::upd(V[kk], D1[kk], dt * (DP[kk] - DPm[kk]) / Hj, R(0));
+        if (j >= 2) V[kk] = Sten<R>::upd(V[kk], D1[kk], dt * (DP[kk] - DPm[kk]) * rHj, R(0));
         if (updp) Pp[kk] = ST::add(Pp[kk], DP[kk]);
     }
 }

@@ -185,20 +185,20 @@ class Channel:
     # ---- launch schedule ----
     SCHEDULE_KEYS = ("z_segment_zA", "z_segment_zB", "z_segment_zC", "z_segment_zD", "z_segment_zE",
                      "x_rows_per_block", "fft_z_tile", "fft_x_plan", "fft_z_plan", "z_split_zA",
-                     "x_split_xA")
+                     "x_split_xA", "x_bulk_stages")
 
     def autotune(self) -> dict:
-        sch = (_ip * 11)()
+        sch = (_ip * 12)()
         check(load().c3d_autotune(self.h, sch), "c3d_autotune")
         return dict(zip(self.SCHEDULE_KEYS, sch[:]))
 
     def get_schedule(self) -> dict:
-        sch = (_ip * 11)()
+        sch = (_ip * 12)()
         check(load().c3d_get_schedule(self.h, sch), "c3d_get_schedule")
         return dict(zip(self.SCHEDULE_KEYS, sch[:]))
 
     def set_schedule(self, sched: dict):
-        sch = (_ip * 11)(*[int(sched[k]) for k in self.SCHEDULE_KEYS])
+        sch = (_ip * 12)(*[int(sched[k]) for k in self.SCHEDULE_KEYS])
         check(load().c3d_set_schedule(self.h, sch), "c3d_set_schedule")
 
     # ---- operators one at a time ----

@@ -211,7 +211,7 @@ int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
 
 /* ---- launch schedule -----------------------------------------------------
  * The kernels' launch shapes are chosen per grid shape by an autotuner written for
- * this library (no counterpart in the reference).  A schedule is eleven ints:
+ * this library (no counterpart in the reference).  A schedule is twelve ints:
  *   [0..4] z-line segment length (8, 16, 32) of each z pass: the points each thread
  *       solves sequentially (Thomas-like) before the parallel segments of a z line
  *       meet
@@ -223,6 +223,9 @@ int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
  *       in three kernels (1)
  *   [10] the x pass of the explicit terms as one kernel (0) or as its u, v and w
  *       pieces in three kernels (1)
+ *   [11] x passes whose rows each warp reads from global memory (0) or streams into
+ *       shared memory through a ring of 2 or 3 bulk-copy stages (persistent warps;
+ *       mixed form, N1M a multiple of 4)
  * c3d_autotune  times the candidates on a scratch channel of the same grid holding a
  *               copy of this channel's state (so the channel needs its state), keeps
  *               the fastest per kernel group, applies it, and caches it per grid

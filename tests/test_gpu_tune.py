@@ -26,17 +26,17 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def _sched(zl, xw, tw, fx, fz, split, xsplit):
+def _sched(zl, xw, tw, fx, fz, split, xsplit, xbulk=0):
     d = {f"z_segment_z{c}": z for c, z in zip("ABCDE", zl)}
     d.update(x_rows_per_block=xw, fft_z_tile=tw, fft_x_plan=fx, fft_z_plan=fz, z_split_zA=split,
-             x_split_xA=xsplit)
+             x_split_xA=xsplit, x_bulk_stages=xbulk)
     return d
 
 
 SCHEDULES = [
     _sched((8, 8, 8, 8, 8), 2, 4, 1, 2, 1, 1),
     _sched((32, 32, 32, 32, 32), 8, 16, 2, 1, 0, 0),
-    _sched((16, 8, 32, 16, 8), 4, 8, 0, 0, 1, 0),
+    _sched((16, 8, 32, 16, 8), 4, 8, 0, 0, 1, 0, 2),
 ]
 
 
@@ -79,3 +79,27 @@ def test_autotune_valid_and_cached(libc3d):
     assert np.isfinite(d["divmax"]) and d["divmax"] < 1e-4
     with pytest.raises(libc3d.C3DError):
         a.set_schedule(dict(s1, z_segment_zA=12))
+
+
+@pytest.mark.parametrize("shape", [(32, 128, 256), (96, 64, 64)])
+def test_bulk_rows_bit_identical(libc3d, shape):
+    """The bulk-copy ring only changes where a row is read from: the mixed step is
+    bit-identical with 0, 2 or 3 stages.  (32, 128, 256) gives every persistent warp
+    several rows, so each stage's barrier runs through several phases."""
+    n1m, n2m, n3m = shape
+    g, dt = make_grid("small32", n1m=n1m, n2m=n2m, n3m=n3m)
+    U, P, HH = ic.perturbed_laminar(g)
+    out = []
+    for xb in (0, 2, 3):
+        ch = libc3d.Channel(g, C3D_MIXED)
+        ch.upload(U, P, HH)
+        s = ch.get_schedule()
+        s.update(x_bulk_stages=xb)
+        ch.set_schedule(s)
+        for m in (1, 2, 3):
+            ch.step(m, dt, 0.0, 0.0)
+        out.append(ch.download())
+        ch.close()
+    for r in out[1:]:
+        for a, b in zip(r, out[0]):
+            assert np.array_equal(a, b)
