@@ -106,11 +106,17 @@ __global__ void __launch_bounds__(TPB) k_poisson32(StepArgs<float> a) {
     const int N = g.n2m;
     const float2 *RB = a.prbdf + mode, *GM = a.pgamdf + mode;
     float2 xr = make_float2(0.f, 0.f), xi = xr;
+    // loads issued one batch ahead: (q, rb, am) hold batch j0, (qn, rbn, amn) batch j0+UJ
+    float2 q[UJ], rb[UJ], am[UJ], qn[UJ], rbn[UJ], amn[UJ];
+#pragma unroll
+    for (int u = 0; u < UJ; ++u)
+        if (u < N) { q[u] = S[u * s]; rb[u] = RB[u * s]; am[u] = a.pmjdf[u + 1]; }
     for (int j0 = 0; j0 < N; j0 += UJ) {
-        float2 q[UJ], rb[UJ], am[UJ];
 #pragma unroll
         for (int u = 0; u < UJ; ++u)
-            if (j0 + u < N) { q[u] = S[(j0 + u) * s]; rb[u] = RB[(j0 + u) * s]; am[u] = a.pmjdf[j0 + u + 1]; }
+            if (j0 + UJ + u < N) {
+                qn[u] = S[(j0 + UJ + u) * s]; rbn[u] = RB[(j0 + UJ + u) * s]; amn[u] = a.pmjdf[j0 + UJ + u + 1];
+            }
 #pragma unroll
         for (int u = 0; u < UJ; ++u) {
             const int jj = j0 + u;
@@ -126,15 +132,21 @@ __global__ void __launch_bounds__(TPB) k_poisson32(StepArgs<float> a) {
             }
         }
 #pragma unroll
-        for (int u = 0; u < UJ; ++u)
+        for (int u = 0; u < UJ; ++u) {
             if (j0 + u < N) S[(j0 + u) * s] = q[u];
+            q[u] = qn[u]; rb[u] = rbn[u]; am[u] = amn[u];
+        }
     }
     S[(N - 1) * s] = make_float2(xr.x, selfc ? 0.f : xi.x);
+    // backward sweep; its first batch reads values this thread stored above
+    float2 gm[UJ], gmn[UJ];
+#pragma unroll
+    for (int u = 0; u < UJ; ++u)
+        if (N - 2 - u >= 0) { q[u] = S[(N - 2 - u) * s]; gm[u] = GM[(N - 1 - u) * s]; }
     for (int jt = N - 2; jt >= 0; jt -= UJ) {
-        float2 q[UJ], gm[UJ];
 #pragma unroll
         for (int u = 0; u < UJ; ++u)
-            if (jt - u >= 0) { q[u] = S[(jt - u) * s]; gm[u] = GM[(jt - u + 1) * s]; }
+            if (jt - UJ - u >= 0) { qn[u] = S[(jt - UJ - u) * s]; gmn[u] = GM[(jt - UJ - u + 1) * s]; }
 #pragma unroll
         for (int u = 0; u < UJ; ++u)
             if (jt - u >= 0) {
@@ -143,8 +155,10 @@ __global__ void __launch_bounds__(TPB) k_poisson32(StepArgs<float> a) {
                 q[u] = make_float2(xr.x, selfc ? 0.f : xi.x);
             }
 #pragma unroll
-        for (int u = 0; u < UJ; ++u)
+        for (int u = 0; u < UJ; ++u) {
             if (jt - u >= 0) S[(jt - u) * s] = q[u];
+            q[u] = qn[u]; gm[u] = gmn[u];
+        }
     }
 }
 

@@ -50,16 +50,157 @@ __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
             if (PART == 0 || PART == 3) { pf_row(a.w + om, rb, lane); pf_row(a.w + o, rb, lane); pf_row(a.w + op, rb, lane); }
         }
         R uy[C];
-        if (PART == 2 && j >= 2) {   // u at the y faces, for E_xy
-            S uc[C], um[C];
-            srow_load(uc, a.u + o, sbS, lane, P);
-            srow_load(um, a.u + om, sbS, lane, P);
-            const R Hj1 = a.m.rh[j], a1 = a.m.hdy[j], a2 = a.m.hdy[j - 1];
+        if (PART == 2 && j >= 2) {
+            // The v piece on its own, ordered so that few rows are live at once: the y
+            // stencils of V (HH2 stored), then -dP/dy, then the x terms of V (R2 stored),
+            // then E_xy with u at the y faces.
+            const R DYPj = a.m.dyp[j], DYCj = a.m.dyc[j], DYMj = a.m.dym[j], Z0 = a.m.dyz[j];
+            const R Hj1 = a.m.rh[j];
+            R acc[C];
+            {
+                S vc[C], vm[C], vp[C];
+                srow_load(vc, a.v + o, sbS, lane, P);
+                srow_load(vm, a.v + om, sbS, lane, P);
+                srow_load(vp, a.v + op, sbS, lane, P);
+                R hh[C];
 #pragma unroll
-            for (int t = 0; t < C; ++t) uy[t] = Hj1 * (a1 * ST::hi(um[t]) + a2 * ST::hi(uc[t]));
+                for (int t = 0; t < C; ++t) {
+                    acc[t] = RE1 * ST::yvisc(DYPj, DYCj, DYMj, Z0, vp[t], vc[t], vm[t]);
+                    hh[t] = Hj1 * Sten<R>::vv(vp[t], vc[t], vm[t]);
+                }
+                srow_store(a.hh[1] + o, hh, sbR, lane, P);
+            }
+            {
+                S pc[C], pm[C];
+                srow_load(pc, a.p + o, sbS, lane, P);
+                srow_load(pm, a.p + om, sbS, lane, P);
+#pragma unroll
+                for (int t = 0; t < C; ++t) {
+                    R pg = ST::d(pc[t], pm[t]) * Hj1;
+                    acc[t] = -pg + acc[t];
+                }
+            }
+            S vc[C];
+            srow_load(vc, a.v + o, sbS, lane, P);
+            R d[C];
+            S pv = sprev(vc[C - 1], lane, P), nx = snext(vc[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S l = (t == 0) ? pv : vc[t - 1], rr = (t == C - 1) ? nx : vc[t + 1];
+                d[t] = f12 * ST::d2(l, vc[t], rr);
+            }
+            xsolve(d, lane, P, a.c10x);
+#pragma unroll
+            for (int t = 0; t < C; ++t) acc[t] = acc[t] + RE1 * d[t];
+            srow_store(a.r[1] + o, acc, sbR, lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S l = (t == 0) ? pv : vc[t - 1];
+                d[t] = four * (ST::hi(l) + ST::hi(vc[t]));
+            }
+            xsolve(d, lane, P, a.c6x);
+            {   // u at the y faces
+                S uc[C], um[C];
+                srow_load(uc, a.u + o, sbS, lane, P);
+                srow_load(um, a.u + om, sbS, lane, P);
+                const R a1 = a.m.hdy[j], a2 = a.m.hdy[j - 1];
+#pragma unroll
+                for (int t = 0; t < C; ++t) d[t] = d[t] * (Hj1 * (a1 * ST::hi(um[t]) + a2 * ST::hi(uc[t])));
+            }
+            srow_store(a.exy + o, d, sbR, lane, P);
+        }
+        if (PART == 1) {
+            // The u piece on its own, ordered so that few rows are live at once: the y
+            // stencil of U, the x terms of U (HH1 stored), then -dP/dx (R1 stored).
+            const R HPj = a.m.hp[j], HCj = a.m.hc[j], HMj = a.m.hm[j], Z0 = a.m.hz[j];
+            R acc[C];
+            {
+                S um[C], up[C], uc0[C];
+                srow_load(uc0, a.u + o, sbS, lane, P);
+                srow_load(um, a.u + om, sbS, lane, P);
+                srow_load(up, a.u + op, sbS, lane, P);
+#pragma unroll
+                for (int t = 0; t < C; ++t) acc[t] = RE1 * ST::yvisc(HPj, HCj, HMj, Z0, up[t], uc0[t], um[t]);
+            }
+            S uc[C];
+            srow_load(uc, a.u + o, sbS, lane, P);
+            R d[C];
+            S pv = sprev(uc[C - 1], lane, P), nx = snext(uc[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S l = (t == 0) ? pv : uc[t - 1], rr = (t == C - 1) ? nx : uc[t + 1];
+                d[t] = f12 * ST::d2(l, uc[t], rr);
+            }
+            xsolve(d, lane, P, a.c10x);
+#pragma unroll
+            for (int t = 0; t < C; ++t) acc[t] = acc[t] + RE1 * d[t];
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S rr = (t == C - 1) ? nx : uc[t + 1];
+                d[t] = four * (ST::hi(uc[t]) + ST::hi(rr));
+            }
+            xsolve(d, lane, P, a.c6x);
+            R sq[C];
+#pragma unroll
+            for (int t = 0; t < C; ++t) sq[t] = d[t] * d[t];
+            R ps = sprev(sq[C - 1], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                R l = (t == 0) ? ps : sq[t - 1];
+                d[t] = f24 * (sq[t] - l);
+            }
+            xsolve(d, lane, P, a.c22x);
+            srow_store(a.hh[0] + o, d, sbR, lane, P);
+            {
+                S pc[C];
+                srow_load(pc, a.p + o, sbS, lane, P);
+                S pp = sprev(pc[C - 1], lane, P);
+#pragma unroll
+                for (int t = 0; t < C; ++t) {
+                    S l = (t == 0) ? pp : pc[t - 1];
+                    d[t] = f24 * ST::d(pc[t], l);
+                }
+            }
+            xsolve(d, lane, P, a.c22x);
+#pragma unroll
+            for (int t = 0; t < C; ++t) acc[t] = acc[t] - d[t] - presg;
+            srow_store(a.r[0] + o, acc, sbR, lane, P);
+        }
+        if (PART == 3) {
+            // The w piece on its own: the y stencil first, then the x terms.
+            const R HPj = a.m.hp[j], HCj = a.m.hc[j], HMj = a.m.hm[j], Z0 = a.m.hz[j];
+            R acc[C];
+            {
+                S wm[C], wp[C], wc0[C];
+                srow_load(wc0, a.w + o, sbS, lane, P);
+                srow_load(wm, a.w + om, sbS, lane, P);
+                srow_load(wp, a.w + op, sbS, lane, P);
+#pragma unroll
+                for (int t = 0; t < C; ++t) acc[t] = RE1 * ST::yvisc(HPj, HCj, HMj, Z0, wp[t], wc0[t], wm[t]);
+            }
+            S wc[C];
+            srow_load(wc, a.w + o, sbS, lane, P);
+            R d[C];
+            S pv = sprev(wc[C - 1], lane, P), nx = snext(wc[0], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S l = (t == 0) ? pv : wc[t - 1], rr = (t == C - 1) ? nx : wc[t + 1];
+                d[t] = f12 * ST::d2(l, wc[t], rr);
+            }
+            xsolve(d, lane, P, a.c10x);
+#pragma unroll
+            for (int t = 0; t < C; ++t) acc[t] = acc[t] + RE1 * d[t];
+            srow_store(a.r[2] + o, acc, sbR, lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S l = (t == 0) ? pv : wc[t - 1];
+                d[t] = four * (ST::hi(l) + ST::hi(wc[t]));
+            }
+            xsolve(d, lane, P, a.c6x);
+            srow_store(a.ww1 + o, d, sbR, lane, P);
         }
         // ---- u: R1 = visc_y + visc_x/RE - dP/dx - PRESG ; HH1 = d(uu)/dx ----
-        if (PART == 0 || PART == 1) {
+        if (PART == 0) {
             S uc[C], um[C], up[C];
             srow_load(uc, a.u + o, sbS, lane, P);
             srow_load(um, a.u + om, sbS, lane, P);
@@ -113,7 +254,7 @@ __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
             }
         }
         // ---- v (faces J=2..N2M): R2, HH2 = d(vv)/dy, E_xy = VV1 * UY ----
-        if ((PART == 0 || PART == 2) && j >= 2) {
+        if (PART == 0 && j >= 2) {
             S vc[C], vm[C], vp[C];
             srow_load(vc, a.v + o, sbS, lane, P);
             srow_load(vm, a.v + om, sbS, lane, P);
@@ -153,7 +294,7 @@ __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
             srow_store(a.exy + o, d, sbR, lane, P);
         }
         // ---- w: R3 = visc_y + visc_x/RE ; WW1 = w at x faces ----
-        if (PART == 0 || PART == 3) {
+        if (PART == 0) {
             S wc[C], wm[C], wp[C];
             srow_load(wc, a.w + o, sbS, lane, P);
             srow_load(wm, a.w + om, sbS, lane, P);
