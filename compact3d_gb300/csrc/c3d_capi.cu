@@ -291,6 +291,10 @@ int check_grid(const c3d_grid *g) {
         return C3D_EINVAL;
     }
     if (n2m < 4 || n2m > 4096) { set_error("N2-1 must be in [4, 4096]"); return C3D_EINVAL; }
+    if ((long long)(n2m + 2) * n1m * n3m >= (1LL << 31)) {   // kernels index points in 32 bits
+        set_error("a field of (N2+1) x (N1-1) x (N3-1) points must have fewer than 2^31 points");
+        return C3D_EINVAL;
+    }
     if (!g->y || !g->dy || !g->h || !g->hm || !g->hc || !g->hp || !g->dym || !g->dyc || !g->dyp) {
         set_error("null metric array");
         return C3D_EINVAL;

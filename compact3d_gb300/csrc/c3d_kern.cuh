@@ -499,14 +499,16 @@ inline int nblk(long long n, int b = TPB) { return (int)((n + b - 1) / b); }
 // z-direction thread mapping: thread per (i, segment of L points, plane j >= jlo)
 template <int L>
 __device__ __forceinline__ bool zcoord(const Geo &g, int jlo, int &i, int &j, int &k0) {
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int nseg = g.n3m / L;
-    const long long tot = (long long)(g.n2m - jlo + 1) * nseg * g.n1m;
+    // 32-bit index arithmetic: a grid has fewer than 2^32 threads (N / L points)
+    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nseg = (unsigned)(g.n3m / L), n1 = (unsigned)g.n1m;
+    const unsigned tot = (unsigned)(g.n2m - jlo + 1) * nseg * n1;
     if (tid >= tot) return false;
-    i = (int)(tid % g.n1m);
-    long long rest = tid / g.n1m;
-    k0 = (int)(rest % nseg) * L;
-    j = jlo + (int)(rest / nseg);
+    const unsigned rest = tid / n1;
+    i = (int)(tid - rest * n1);
+    const unsigned jq = rest / nseg;
+    k0 = (int)(rest - jq * nseg) * L;
+    j = jlo + (int)jq;
     return true;
 }
 

@@ -169,9 +169,11 @@ __global__ void k_sgs_coef(StepArgs<R> a, LesArgs<R> l) {
 template <typename R>
 __global__ void __launch_bounds__(TPB) k_sgs_cs(StepArgs<R> a, LesArgs<R> l) {
     const Geo g = a.g;
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= (long long)g.n2m * g.np) return;
-    const int i = (int)(tid % g.n1m), k = (int)((tid / g.n1m) % g.n3m), j = 1 + (int)(tid / g.np);
+    // 32-bit index arithmetic (a field has fewer than 2^31 points)
+    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (unsigned)g.n2m * (unsigned)g.np) return;
+    const unsigned rw = tid / (unsigned)g.n1m, pj = rw / (unsigned)g.n3m;
+    const int i = (int)(tid - rw * g.n1m), k = (int)(rw - pj * g.n3m), j = 1 + (int)pj;
     R sr[6];
     strain_at(a, l, i, j, k, sr);
     const R abss = sqrt((R)2.0 * sumsq6(sr));
@@ -185,9 +187,11 @@ template <typename R>
 __global__ void __launch_bounds__(TPB) k_sgs_raw(StepArgs<R> a, LesArgs<R> l) {
     typedef St<R> ST;
     const Geo g = a.g;
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= (long long)g.n2m * g.np) return;
-    const int i = (int)(tid % g.n1m), k = (int)((tid / g.n1m) % g.n3m), j = 1 + (int)(tid / g.np);
+    // 32-bit index arithmetic (a field has fewer than 2^31 points)
+    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (unsigned)g.n2m * (unsigned)g.np) return;
+    const unsigned rw = tid / (unsigned)g.n1m, pj = rw / (unsigned)g.n3m;
+    const int i = (int)(tid - rw * g.n1m), k = (int)(rw - pj * g.n3m), j = 1 + (int)pj;
     R sr[6];
     strain_at(a, l, i, j, k, sr);
     const R abss = sqrt((R)2.0 * sumsq6(sr));

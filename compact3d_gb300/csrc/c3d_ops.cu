@@ -127,14 +127,14 @@ __global__ void __launch_bounds__(TPB) k_op_z(StepArgs<R> a, int op, const R *in
     for (int t = 0; t < L; ++t) out[o + (long long)(k0 + t) * s] = res[0][t];
 }
 
-// wall-normal finite differences, one thread per point
+// wall-normal finite differences, one thread per point; blockIdx.y is the plane J - 1
 template <typename R>
 __global__ void __launch_bounds__(TPB) k_op_y(StepArgs<R> a, int op, const R *in, R *out) {
     const Geo g = a.g;
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= (long long)g.n2m * g.np) return;
-    const int j = 1 + (int)(tid / g.np);
-    const long long e = tid % g.np, o = (long long)j * g.np + e;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= g.np) return;
+    const int j = 1 + (int)blockIdx.y;
+    const long long o = (long long)j * g.np + e;
     if (op == C3D_OP_DY1) {
         out[o] = j >= 2 ? (in[o] - in[o - g.np]) / a.m.h[j] : R(0);
     } else {
@@ -180,7 +180,7 @@ int launch_op(c3d_channel *ch, StepArgs<R> &a, int op, const R *in, R *out, int 
             mark(ch, nl, "op_z", N * 2 * Rb);
             break;
         case C3D_OP_DY1: case C3D_OP_DY2:
-            k_op_y<R><<<nblk((long long)g.n2m * g.np), TPB, 0, ch->stream>>>(a, op, in, out);
+            k_op_y<R><<<dim3(nblk(g.np), g.n2m), TPB, 0, ch->stream>>>(a, op, in, out);
             mark(ch, nl, "op_y", N * 2 * Rb);
             break;
         case C3D_OP_POISSON:
