@@ -369,6 +369,116 @@ __device__ __forceinline__ void zsweep(R (&out)[NR][L], int k0, int n, const R (
     }
 }
 
+// Cyclic carries of the segments of the block's z lines (zblock): for every recurrence q
+// and line l, a warp takes the nseg segment values v[p] = sh[(q*32 + l)*(nseg+1) + p] in
+// its lanes and replaces them by the state entering each segment.  Forward (BACK false):
+// Y(p) = v(p-1) + rL Y(p-1) cyclically, i.e. Y(p) = E(p-1) + rL^p Y(0) with the prefix
+// E(p) = v(p) + rL E(p-1) and Y(0) = E(nseg-1) / (1 - rL^nseg).  Backward: the mirror
+// image, Z(p) = v(p+1) + rL Z(p+1) from the right.  Warp-shuffle scans, log2(32) steps.
+template <typename R, int L, int NR, bool BACK>
+__device__ __forceinline__ void zcarry(const R (&r)[NR], R *sh) {
+    const int lane = threadIdx.x, w = threadIdx.y, nw = blockDim.y, nseg = blockDim.y;
+    const int pitch = nseg + 1;
+    for (int sidx = w; sidx < 32 * NR; sidx += nw) {
+        const int q = sidx >> 5, l = sidx & 31;
+        R rq = R(0);
+#pragma unroll
+        for (int t = 0; t < NR; ++t)
+            if (t == q) rq = r[t];
+        R rL = R(1);
+#pragma unroll
+        for (int t = 0; t < L; ++t) rL *= rq;
+        R *v = sh + (q * 32 + l) * pitch;
+        const int p = BACK ? nseg - 1 - lane : lane;   // position along the scan direction
+        const bool act = lane < nseg;
+        R e = act ? v[p] : R(0);
+        R pw = rL;   // rL^off
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const R ep = shfl_up(e, off);
+            if (lane >= off) e = e + pw * ep;
+            pw = pw * pw;
+        }
+        // rL^lane and rL^nseg by repeated squaring
+        R pl = R(1), pn = R(1), b = rL;
+#pragma unroll
+        for (int bit = 0; bit < 6; ++bit) {
+            if ((lane >> bit) & 1) pl = pl * b;
+            if ((nseg >> bit) & 1) pn = pn * b;
+            b = b * b;
+        }
+        const R tot = shfl_idx(e, nseg - 1);
+        const R y0 = tot / (R(1) - pn);
+        const R eprev = shfl_up(e, 1);
+        const R yin = (lane == 0 ? R(0) : eprev) + pl * y0;
+        if (act) v[p] = yin;
+    }
+}
+
+// Exact cyclic solve of NR recurrences on z lines by one block of 32 lines (threadIdx.x,
+// consecutive i) x nseg segments of L points (threadIdx.y; nseg = blockDim.y = N / L,
+// at most 32).  Each thread walks only its own segment: a local forward recurrence from
+// zero, the carries across the segments of its line (zcarry), the correction
+// y(t) += r^(t+1) Y, and the same backward.  sh holds NR*32*(nseg+1) values.  Every
+// thread of the block calls it (it synchronises the block).
+template <typename R, int L, int NR, typename F>
+__device__ __forceinline__ void zblock(R (&out)[NR][L], int k0, const R (&r)[NR], const R (&s)[NR], F &f, R *sh) {
+    const int lx = threadIdx.x, seg = threadIdx.y, pitch = blockDim.y + 1;
+    f.start(k0);
+    R y[NR], d[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) y[q] = R(0);
+#pragma unroll
+    for (int t = 0; t < L; ++t) {
+        f.next(d);
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+            y[q] = d[q] + r[q] * y[q];
+            out[q][t] = y[q];
+        }
+    }
+    __syncthreads();   // a previous call's readers of sh are done
+#pragma unroll
+    for (int q = 0; q < NR; ++q) sh[(q * 32 + lx) * pitch + seg] = y[q];
+    __syncthreads();
+    zcarry<R, L, NR, false>(r, sh);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+        const R yin = sh[(q * 32 + lx) * pitch + seg];
+        R pw = r[q];
+#pragma unroll
+        for (int t = 0; t < L; ++t) {
+            out[q][t] = out[q][t] + pw * yin;
+            pw *= r[q];
+        }
+    }
+    __syncthreads();   // sh is reused
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+        R z = R(0);
+#pragma unroll
+        for (int t = L - 1; t >= 0; --t) {
+            z = out[q][t] + r[q] * z;
+            out[q][t] = z;
+        }
+        sh[(q * 32 + lx) * pitch + seg] = z;
+    }
+    __syncthreads();
+    zcarry<R, L, NR, true>(r, sh);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+        const R zin = sh[(q * 32 + lx) * pitch + seg];
+        R pw = r[q];
+#pragma unroll
+        for (int t = L - 1; t >= 0; --t) {
+            out[q][t] = s[q] * (out[q][t] + pw * zin);
+            pw *= r[q];
+        }
+    }
+}
+
 // Warm-up lengths M = ceil(log(tol)/log|r|) of the Pade operators (1,6,1), (1,10,1),
 // (1,22,1) and the Crank-Nicolson operators (b/a > 10, so M <= M10): tol = 1e-17 in FP64,
 // 3e-8 in FP32.

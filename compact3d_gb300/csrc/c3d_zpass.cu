@@ -44,6 +44,34 @@ struct ZRing {
     }
 };
 
+// Thread coordinates and the line solve of the two z-pass forms: MODE 0, one thread per
+// (i, segment of L points, plane) with warm-up recurrences (zsweep); MODE 1, one block per
+// (32 consecutive i, plane) with blockDim.y = N3M / L segments and the exact cyclic
+// solve (zblock).
+template <int L, int MODE>
+__device__ __forceinline__ bool zcoords(const Geo &g, int jlo, int &i, int &j, int &k0) {
+    if constexpr (MODE == 1) {
+        i = (int)blockIdx.x * 32 + (int)threadIdx.x;
+        j = jlo + (int)blockIdx.y;
+        k0 = (int)threadIdx.y * L;
+        return true;
+    } else {
+        return zcoord<L>(g, jlo, i, j, k0);
+    }
+}
+template <typename R, int L, int M, int NR, int MODE, typename F>
+__device__ __forceinline__ void zsolve(R (&out)[NR][L], int k0, int n, const R (&r)[NR], const R (&s)[NR], F &f) {
+    if constexpr (MODE == 1) {
+        extern __shared__ __align__(16) unsigned char zsh_raw[];
+        zblock<R, L, NR>(out, k0, r, s, f, reinterpret_cast<R *>(zsh_raw));
+    } else {
+        zsweep<R, L, M, NR>(out, k0, n, r, s, f);
+    }
+}
+// L2 prefetch margin around a thread's positions: the warm-up length (MODE 0) or one point.
+template <int MODE>
+constexpr int zmargin(int m) { return MODE == 1 ? 1 : m + 1; }
+
 // state column: (1,10,1) RHS f12*(u- - 2u + u+) and (1,6,1) RHS 4*(u- + u) (face k)
 template <typename R>
 struct WalkVisBack {
@@ -140,13 +168,13 @@ struct WalkGradZ {
 
 // PART 0 runs the three sweeps in one kernel; PART 1, 2, 3 run only the u, the (w, P) or
 // the v sweep (the split form has fewer registers per thread and moves the same bytes).
-template <typename R, int L, int PART>
-__global__ void __launch_bounds__(TPB) k_zA(StepArgs<R> a) {
+template <typename R, int L, int PART, int MODE>
+__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zA(StepArgs<R> a) {
     typedef typename SType<R>::S S;
     typedef St<R> ST;
     const Geo g = a.g;
     int i, j, k0;
-    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    if (!zcoords<L, MODE>(g, 1, i, j, k0)) return;
     const int n = g.n3m, s = g.n1m;
     const R RE1 = a.re1;
     const long long o = fidx(g, i, j, 0);
@@ -156,17 +184,17 @@ __global__ void __launch_bounds__(TPB) k_zA(StepArgs<R> a) {
         const long long o0 = fidx(g, i - lane, j, 0), sb = (long long)g.n1m;
         const int ss = 32 * (int)sizeof(S), sr = 32 * (int)sizeof(R);
         if (PART <= 1) {
-            pf_cols(a.u + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
+            pf_cols(a.u + o0, sb * sizeof(S), ss, k0, zmargin<MODE>(M6), L, n, lane);
             pf_cols(a.ww1 + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
             pf_cols(a.r[0] + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
         }
         if (PART == 0 || PART == 2) {
-            pf_cols(a.w + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
-            pf_cols(a.p + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
+            pf_cols(a.w + o0, sb * sizeof(S), ss, k0, zmargin<MODE>(M6), L, n, lane);
+            pf_cols(a.p + o0, sb * sizeof(S), ss, k0, zmargin<MODE>(M6), L, n, lane);
             pf_cols(a.r[2] + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
         }
         if ((PART == 0 || PART == 3) && j >= 2) {
-            pf_cols(a.v + o0, sb * sizeof(S), ss, k0, M6 + 1, L, n, lane);
+            pf_cols(a.v + o0, sb * sizeof(S), ss, k0, zmargin<MODE>(M6), L, n, lane);
             pf_cols(a.r[1] + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
         }
     }
@@ -174,7 +202,7 @@ __global__ void __launch_bounds__(TPB) k_zA(StepArgs<R> a) {
         R out[2][L];
         const R rr[2] = {a.c10z.r, a.c6z.r}, ss[2] = {a.c10z.s, a.c6z.s};
         WalkVisBack<R> f{a.u + o, n, s, a.f12z};
-        zsweep<R, L, M6, 2>(out, k0, n, rr, ss, f);
+        zsolve<R, L, M6, 2, MODE>(out, k0, n, rr, ss, f);
         R *Rp = a.r[0] + o, *E = a.exz + o;
         const R *Wx = a.ww1 + o;
 #pragma unroll
@@ -188,7 +216,7 @@ __global__ void __launch_bounds__(TPB) k_zA(StepArgs<R> a) {
         R out[3][L];
         const R rr[3] = {a.c10z.r, a.c6z.r, a.c22z.r}, ss[3] = {a.c10z.s, a.c6z.s, a.c22z.s};
         WalkWP<R> f{a.w + o, a.p + o, n, s, a.f12z, a.f24z};
-        zsweep<R, L, M6, 3>(out, k0, n, rr, ss, f);
+        zsolve<R, L, M6, 3, MODE>(out, k0, n, rr, ss, f);
         const R presg3 = (R)a.scal[SCAL_PRESG3];
         R *Rp = a.r[2] + o, *Q = a.wsq + o;
 #pragma unroll
@@ -202,7 +230,7 @@ __global__ void __launch_bounds__(TPB) k_zA(StepArgs<R> a) {
         R out[2][L];
         const R rr[2] = {a.c10z.r, a.c6z.r}, ss[2] = {a.c10z.s, a.c6z.s};
         WalkVisBack<R> f{a.v + o, n, s, a.f12z};
-        zsweep<R, L, M6, 2>(out, k0, n, rr, ss, f);
+        zsolve<R, L, M6, 2, MODE>(out, k0, n, rr, ss, f);
         const R Hj1 = a.m.rh[j], a1 = a.m.hdy[j], a2 = a.m.hdy[j - 1];
         const S *W = a.w + o, *Wm = a.w + fidx(g, i, j - 1, 0);
         R *Rp = a.r[1] + o, *E = a.eyz + o;
@@ -216,19 +244,19 @@ __global__ void __launch_bounds__(TPB) k_zA(StepArgs<R> a) {
     }
 }
 
-template <typename R, int L>
-__global__ void __launch_bounds__(TPB) k_zB(StepArgs<R> a) {
+template <typename R, int L, int MODE>
+__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zB(StepArgs<R> a) {
     const Geo g = a.g;
     int i, j, k0;
-    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    if (!zcoords<L, MODE>(g, 1, i, j, k0)) return;
     const int n = g.n3m, s = g.n1m;
     const long long o = fidx(g, i, j, 0);
     if ((g.n1m & 31) == 0) {
         const int lane = threadIdx.x & 31;
         const long long o0 = fidx(g, i - lane, j, 0), sb = (long long)g.n1m;
-        pf_cols(a.exz + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::M22 + 1, L, n, lane);
-        pf_cols(a.wsq + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::M22 + 1, L, n, lane);
-        pf_cols(a.eyz + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::M22 + 1, L, n, lane);
+        pf_cols(a.exz + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, zmargin<MODE>(WM<R>::M22), L, n, lane);
+        pf_cols(a.wsq + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, zmargin<MODE>(WM<R>::M22), L, n, lane);
+        pf_cols(a.eyz + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, zmargin<MODE>(WM<R>::M22), L, n, lane);
         pf_cols(a.hh[0] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
         pf_cols(a.hh[1] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
     }
@@ -236,7 +264,7 @@ __global__ void __launch_bounds__(TPB) k_zB(StepArgs<R> a) {
     const R rr[3] = {a.c22z.r, a.c22z.r, a.c22z.r}, ss[3] = {a.c22z.s, a.c22z.s, a.c22z.s};
     WalkZB<R> f{a.exz + o, a.wsq + o, a.eyz + o, n, s, a.f24z};
     f.v = (j >= 2);
-    zsweep<R, L, WM<R>::M22, 3>(out, k0, n, rr, ss, f);
+    zsolve<R, L, WM<R>::M22, 3, MODE>(out, k0, n, rr, ss, f);
     R *H1 = a.hh[0] + o, *H2 = a.hh[1] + o, *H3 = a.hh[2] + o;
 #pragma unroll
     for (int t = 0; t < L; ++t) {
@@ -249,26 +277,26 @@ __global__ void __launch_bounds__(TPB) k_zB(StepArgs<R> a) {
 
 // z factor of Crank-Nicolson: r[c] -> d[c] for the three components (the v component at
 // J=1 is computed from zeros and never read)
-template <typename R, int L>
-__global__ void __launch_bounds__(TPB) k_zC(StepArgs<R> a, R *d0, R *d1, R *d2) {
+template <typename R, int L, int MODE>
+__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zC(StepArgs<R> a, R *d0, R *d1, R *d2) {
     const Geo g = a.g;
     int i, j, k0;
-    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    if (!zcoords<L, MODE>(g, 1, i, j, k0)) return;
     const int n = g.n3m, s = g.n1m;
     const long long o = fidx(g, i, j, 0);
     if ((g.n1m & 31) == 0) {
         const int lane = threadIdx.x & 31;
         const long long o0 = fidx(g, i - lane, j, 0), sb = (long long)g.n1m;
-        pf_cols(a.r[0] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::MCN + 1, L, n, lane);
-        pf_cols(a.r[1] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::MCN + 1, L, n, lane);
-        pf_cols(a.r[2] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::MCN + 1, L, n, lane);
+        pf_cols(a.r[0] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, zmargin<MODE>(WM<R>::MCN), L, n, lane);
+        pf_cols(a.r[1] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, zmargin<MODE>(WM<R>::MCN), L, n, lane);
+        pf_cols(a.r[2] + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, zmargin<MODE>(WM<R>::MCN), L, n, lane);
     }
     R out[3][L];
     const R rr[3] = {a.cnz.r, a.cnz.r, a.cnz.r}, ss[3] = {a.cnz.s, a.cnz.s, a.cnz.s};
     WalkCN<R> f;
     f.X[0] = a.r[0] + o; f.X[1] = a.r[1] + o; f.X[2] = a.r[2] + o;
     f.n = n; f.s = s;
-    zsweep<R, L, WM<R>::MCN, 3>(out, k0, n, rr, ss, f);
+    zsolve<R, L, WM<R>::MCN, 3, MODE>(out, k0, n, rr, ss, f);
     R *D0 = d0 + o, *D1 = d1 + o, *D2 = d2 + o;
 #pragma unroll
     for (int t = 0; t < L; ++t) {
@@ -280,23 +308,23 @@ __global__ void __launch_bounds__(TPB) k_zC(StepArgs<R> a, R *d0, R *d1, R *d2) 
 }
 
 // z part of RHSDP: rdpz = compact d(UH3)/dz / DT with UH3 = W + delta3
-template <typename R, int L>
-__global__ void __launch_bounds__(TPB) k_zD(StepArgs<R> a, const R *d2) {
+template <typename R, int L, int MODE>
+__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zD(StepArgs<R> a, const R *d2) {
     const Geo g = a.g;
     int i, j, k0;
-    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    if (!zcoords<L, MODE>(g, 1, i, j, k0)) return;
     const int n = g.n3m, s = g.n1m;
     const long long o = fidx(g, i, j, 0);
     if ((g.n1m & 31) == 0) {
         const int lane = threadIdx.x & 31;
         const long long o0 = fidx(g, i - lane, j, 0), sb = (long long)g.n1m;
-        pf_cols(a.w + o0, sb * sizeof(typename SType<R>::S), 32 * (int)sizeof(typename SType<R>::S), k0, WM<R>::M22 + 1, L, n, lane);
-        pf_cols(d2 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::M22 + 1, L, n, lane);
+        pf_cols(a.w + o0, sb * sizeof(typename SType<R>::S), 32 * (int)sizeof(typename SType<R>::S), k0, zmargin<MODE>(WM<R>::M22), L, n, lane);
+        pf_cols(d2 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, zmargin<MODE>(WM<R>::M22), L, n, lane);
     }
     R out[1][L];
     const R rr[1] = {a.c22z.r}, ss[1] = {a.c22z.s};
     WalkDivZ<R> f{a.w + o, d2 + o, n, s, a.f24z};
-    zsweep<R, L, WM<R>::M22, 1>(out, k0, n, rr, ss, f);
+    zsolve<R, L, WM<R>::M22, 1, MODE>(out, k0, n, rr, ss, f);
     const R rdt = a.rdt;
     R *Q = a.rdpz + o;
 #pragma unroll
@@ -304,13 +332,13 @@ __global__ void __launch_bounds__(TPB) k_zD(StepArgs<R> a, const R *d2) {
 }
 
 // UPCALC along z and the state update
-template <typename R, int L>
-__global__ void __launch_bounds__(TPB) k_zE(StepArgs<R> a, const R *d0, const R *d1, const R *d2, int updp) {
+template <typename R, int L, int MODE>
+__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zE(StepArgs<R> a, const R *d0, const R *d1, const R *d2, int updp) {
     typedef typename SType<R>::S S;
     typedef St<R> ST;
     const Geo g = a.g;
     int i, j, k0;
-    if (!zcoord<L>(g, 1, i, j, k0)) return;
+    if (!zcoords<L, MODE>(g, 1, i, j, k0)) return;
     const int n = g.n3m, s = g.n1m;
     const long long o = fidx(g, i, j, 0);
     const R dt = (R)a.dt;
@@ -319,7 +347,7 @@ __global__ void __launch_bounds__(TPB) k_zE(StepArgs<R> a, const R *d0, const R 
     if ((g.n1m & 31) == 0) {
         const int lane = threadIdx.x & 31;
         const long long o0 = fidx(g, i - lane, j, 0), sb = (long long)g.n1m;
-        pf_cols(a.dp + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, WM<R>::M22 + 1, L, n, lane);
+        pf_cols(a.dp + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, zmargin<MODE>(WM<R>::M22), L, n, lane);
         pf_cols(a.u + o0, sb * sizeof(S), 32 * (int)sizeof(S), k0, 0, L, n, lane);
         pf_cols(a.v + o0, sb * sizeof(S), 32 * (int)sizeof(S), k0, 0, L, n, lane);
         pf_cols(a.w + o0, sb * sizeof(S), 32 * (int)sizeof(S), k0, 0, L, n, lane);
@@ -332,7 +360,7 @@ __global__ void __launch_bounds__(TPB) k_zE(StepArgs<R> a, const R *d0, const R 
     R out[1][L];
     const R rr[1] = {a.c22z.r}, ss[1] = {a.c22z.s};
     WalkGradZ<R> f{DP, n, s, a.f24z};
-    zsweep<R, L, WM<R>::M22, 1>(out, k0, n, rr, ss, f);
+    zsolve<R, L, WM<R>::M22, 1, MODE>(out, k0, n, rr, ss, f);
     S *W = a.w + o, *U = a.u + o, *V = a.v + o, *Pp = a.p + o;
     const R *D0 = d0 + o, *D1 = d1 + o, *D2 = d2 + o, *G1 = a.g1 + o;
     const R *DPm = a.dp + fidx(g, i, j - 1, 0);
@@ -384,47 +412,68 @@ __global__ void __launch_bounds__(TPB) k_diag_z(StepArgs<R> a, const double *div
     }
 }
 
-template <typename R, int L>
+template <typename R, int L, int MODE>
 static int launch_zpass_l(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *d1, R *d2, int flag, int *nl);
+
+// Segment length of the block form (MODE 1) for N3M points: the smallest of 8, 12, 16
+// that divides N3M into at most 32 segments, or 0 when none does.
+int zblock_len(int n3m) {
+    for (int L : {8, 12, 16})
+        if (n3m % L == 0 && n3m / L <= 32) return L;
+    return 0;
+}
 
 template <typename R>
 int launch_zpass(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *d1, R *d2, int flag, int *nl) {
-    if (which == 5) return launch_zpass_l<R, ZL>(ch, a, which, d0, d1, d2, flag, nl);
-    switch (ch->tune.zl[which]) {
-        case 8: return launch_zpass_l<R, 8>(ch, a, which, d0, d1, d2, flag, nl);
-        case 32: return launch_zpass_l<R, 32>(ch, a, which, d0, d1, d2, flag, nl);
-        default: return launch_zpass_l<R, 16>(ch, a, which, d0, d1, d2, flag, nl);
+    if (which == 5) return launch_zpass_l<R, ZL, 0>(ch, a, which, d0, d1, d2, flag, nl);
+    const int zl = ch->tune.zl[which];
+    if (zl == 0) {   // block form; a shape it cannot take runs the segment form with L = 16
+        switch (zblock_len(ch->g.n3m)) {
+            case 8: return launch_zpass_l<R, 8, 1>(ch, a, which, d0, d1, d2, flag, nl);
+            case 12: return launch_zpass_l<R, 12, 1>(ch, a, which, d0, d1, d2, flag, nl);
+            case 16: return launch_zpass_l<R, 16, 1>(ch, a, which, d0, d1, d2, flag, nl);
+            default: return launch_zpass_l<R, 16, 0>(ch, a, which, d0, d1, d2, flag, nl);
+        }
+    }
+    switch (zl) {
+        case 8: return launch_zpass_l<R, 8, 0>(ch, a, which, d0, d1, d2, flag, nl);
+        case 32: return launch_zpass_l<R, 32, 0>(ch, a, which, d0, d1, d2, flag, nl);
+        default: return launch_zpass_l<R, 16, 0>(ch, a, which, d0, d1, d2, flag, nl);
     }
 }
 
-template <typename R, int L>
+template <typename R, int L, int MODE>
 static int launch_zpass_l(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *d1, R *d2, int flag, int *nl) {
     const long long nt = (long long)ch->g.n2m * (ch->g.n3m / L) * ch->g.n1m;
-    const int nb = nblk(nt);
+    // MODE 0: TPB-thread blocks over all threads; MODE 1: (N1M/32, N2M) blocks of 32 x N3M/L
+    const dim3 nb = MODE == 1 ? dim3(ch->g.n1m / 32, ch->g.n2m) : dim3(nblk(nt));
+    const dim3 TB = MODE == 1 ? dim3(32, ch->g.n3m / L) : dim3(TPB);
+    const size_t zsm = MODE == 1 ? 3 * 32 * (size_t)(ch->g.n3m / L + 1) * sizeof(R) : 0;
     cudaStream_t st = ch->stream;
     const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
     switch (which) {
         case 0:
             if (ch->tune.zsplit) {   // u, (w, P), v sweeps as three kernels
-                k_zA<R, L, 1><<<nb, TPB, 0, st>>>(a);
+                k_zA<R, L, 1, MODE><<<nb, TB, zsm, st>>>(a);
                 mark(ch, nl, "zA_u", N * (8 + 4 * Rb));    // u; WW1, R1 -> R1, E_xz
-                k_zA<R, L, 2><<<nb, TPB, 0, st>>>(a);
+                k_zA<R, L, 2, MODE><<<nb, TB, zsm, st>>>(a);
                 mark(ch, nl, "zA_wp", N * (16 + 3 * Rb));  // w, P; R3 -> R3, WW3^2
-                k_zA<R, L, 3><<<nb, TPB, 0, st>>>(a);
+                k_zA<R, L, 3, MODE><<<nb, TB, zsm, st>>>(a);
                 mark(ch, nl, "zA_v", N * (16 + 3 * Rb));   // v, w; R2 -> R2, E_yz
             } else {
-                k_zA<R, L, 0><<<nb, TPB, 0, st>>>(a);
+                k_zA<R, L, 0, MODE><<<nb, TB, zsm, st>>>(a);
                 mark(ch, nl, "zA", N * (32 + 10 * Rb));
             }
             break;
-        case 1: k_zB<R, L><<<nb, TPB, 0, st>>>(a); mark(ch, nl, "zB", N * 8 * Rb); break;
-        case 2: k_zC<R, L><<<nb, TPB, 0, st>>>(a, d0, d1, d2); mark(ch, nl, "zC", N * 6 * Rb); break;
-        case 3: k_zD<R, L><<<nb, TPB, 0, st>>>(a, d2); mark(ch, nl, "zD", N * (8 + 2 * Rb)); break;
-        case 4: k_zE<R, L><<<nb, TPB, 0, st>>>(a, d0, d1, d2, flag); mark(ch, nl, "zE", N * (64 + 5 * Rb)); break;
+        case 1: k_zB<R, L, MODE><<<nb, TB, zsm, st>>>(a); mark(ch, nl, "zB", N * 8 * Rb); break;
+        case 2: k_zC<R, L, MODE><<<nb, TB, zsm, st>>>(a, d0, d1, d2); mark(ch, nl, "zC", N * 6 * Rb); break;
+        case 3: k_zD<R, L, MODE><<<nb, TB, zsm, st>>>(a, d2); mark(ch, nl, "zD", N * (8 + 2 * Rb)); break;
+        case 4: k_zE<R, L, MODE><<<nb, TB, zsm, st>>>(a, d0, d1, d2, flag); mark(ch, nl, "zE", N * (64 + 5 * Rb)); break;
         case 5: {
+            if (MODE == 1) return C3D_EINVAL;   // the diagnostics run the segment form only
             const double b = 22.0, r = -2.0 / (b + sqrt(b * b - 4.0));
             Cyc<double> c22 = {r, -r, (int)ceil(log(1e-17) / log(fabs(r)))};
-            k_diag_z<R, L><<<nb, TPB, 0, st>>>(a, (const double *)d0, c22);
+            k_diag_z<R, L><<<nb, TB, zsm, st>>>(a, (const double *)d0, c22);
             mark(ch, nl, "diag_z", N * 16);
             break;
         }

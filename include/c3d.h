@@ -214,7 +214,9 @@ int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
  * this library (no counterpart in the reference).  A schedule is twelve ints:
  *   [0..4] z-line segment length (8, 16, 32) of each z pass: the points each thread
  *       solves sequentially (Thomas-like) before the parallel segments of a z line
- *       meet
+ *       meet; or 0: one block per 32 z lines of a plane, each thread one segment of
+ *       8, 12 or 16 points, the segments of a line joined exactly through shared
+ *       memory (N3M / segment length <= 32; otherwise segments of 16)
  *   [5] rows per block of the x passes (2, 4, 8)
  *   [6] kx columns per block of the z FFT (4, 8, 16)
  *   [7], [8] radix order of the x and z FFT plans (0: radix 4 first, 1: radix 3

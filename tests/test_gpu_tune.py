@@ -33,16 +33,20 @@ def _sched(zl, xw, tw, fx, fz, split, xsplit, xbulk=0):
     return d
 
 
+# (schedule, N3M); z segment length 0 is the block form (segments of 8 points for N3M = 64,
+# 12 points in 32 segments for N3M = 384)
 SCHEDULES = [
-    _sched((8, 8, 8, 8, 8), 2, 4, 1, 2, 1, 1),
-    _sched((32, 32, 32, 32, 32), 8, 16, 2, 1, 0, 0),
-    _sched((16, 8, 32, 16, 8), 4, 8, 0, 0, 1, 0, 2),
+    (_sched((8, 8, 8, 8, 8), 2, 4, 1, 2, 1, 1), 64),
+    (_sched((32, 32, 32, 32, 32), 8, 16, 2, 1, 0, 0), 64),
+    (_sched((16, 8, 32, 16, 8), 4, 8, 0, 0, 1, 0, 2), 64),
+    (_sched((0, 0, 0, 0, 0), 2, 4, 0, 1, 1, 1), 64),
+    (_sched((0, 0, 0, 0, 0), 2, 4, 0, 1, 0, 0), 384),
 ]
 
 
-@pytest.mark.parametrize("sched", SCHEDULES)
-def test_every_schedule_matches_oracle(libc3d, oracle_mod, sched):
-    g, dt = make_grid("small32", n3m=64)
+@pytest.mark.parametrize("sched,n3m", SCHEDULES)
+def test_every_schedule_matches_oracle(libc3d, oracle_mod, sched, n3m):
+    g, dt = make_grid("small32", n3m=n3m)
     orc = oracle_mod.Oracle(g)
     U, P, HH = ic.perturbed_laminar(g)
     orc.project(U)
@@ -68,7 +72,7 @@ def test_autotune_valid_and_cached(libc3d):
     a.upload(U, P, HH)
     a.project()
     s1 = a.autotune()
-    assert all(s1[f"z_segment_z{c}"] in (8, 16, 32) for c in "ABCDE") and s1["x_rows_per_block"] in (2, 4, 8)
+    assert all(s1[f"z_segment_z{c}"] in (0, 8, 16, 32) for c in "ABCDE") and s1["x_rows_per_block"] in (2, 4, 8)
     assert s1["fft_z_tile"] in (4, 8, 16) and s1["fft_x_plan"] in (0, 1, 2) and s1["fft_z_plan"] in (0, 1, 2)
     b = libc3d.Channel(g, C3D_MIXED)
     b.upload(U, P, HH)
@@ -103,3 +107,26 @@ def test_bulk_rows_bit_identical(libc3d, shape):
     for r in out[1:]:
         for a, b in zip(r, out[0]):
             assert np.array_equal(a, b)
+
+
+def test_block_z_solve_mixed_close_to_segments(libc3d):
+    """The block form of the z passes solves the cyclic systems exactly, the segment form to
+    the FP32 warm-up tolerance: three mixed steps agree to FP32 rounding."""
+    g, dt = make_grid("small32", n1m=64, n2m=48, n3m=384)
+    U, P, HH = ic.perturbed_laminar(g)
+    res = []
+    for zl in (16, 0):
+        ch = libc3d.Channel(g, C3D_MIXED)
+        ch.upload(U, P, HH)
+        s = ch.get_schedule()
+        s.update({f"z_segment_z{c}": zl for c in "ABCDE"})
+        ch.set_schedule(s)
+        for m in (1, 2, 3):
+            ch.step(m, dt, 0.0, 0.0)
+        res.append(ch.download())
+        ch.close()
+    n1, n2, n3 = g.n1m, g.n2m, g.n3m
+    for c, j0 in ((0, 1), (1, 2), (2, 1)):
+        a = res[1][0][1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c]
+        b = res[0][0][1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c]
+        assert rel(a, b) < 1e-5, (c, rel(a, b))
