@@ -1019,8 +1019,8 @@ bool tune_ok(const c3d_channel *ch, const Tune &t) {
     for (int q = 0; q < 5; ++q)
         zl = zl && (t.zl[q] == 0 || t.zl[q] == 8 || t.zl[q] == 16 || (t.zl[q] == 32 && ch->g.n3m % 32 == 0));
     const bool xw = t.xw == 2 || t.xw == 4 || t.xw == 8;
-    const bool tw = t.twz == 4 || t.twz == 8 || t.twz == 16;
-    return zl && xw && tw && t.fxp >= 0 && t.fxp <= 2 && t.fzp >= 0 && t.fzp <= 2 && (t.zsplit == 0 || t.zsplit == 1) &&
+    const bool tw = t.twz == 0 || t.twz == 4 || t.twz == 8 || t.twz == 16;
+    return zl && xw && tw && t.fxp >= 0 && t.fxp <= 3 && t.fzp >= 0 && t.fzp <= 2 && (t.zsplit == 0 || t.zsplit == 1) &&
            (t.xsplit == 0 || t.xsplit == 1) && (t.xbulk == 0 || t.xbulk == 2 || t.xbulk == 3);
 }
 
@@ -1113,9 +1113,9 @@ int c3d_autotune(c3d_channel *ch, int *sched) {
         {0, {0, 8, 16, 32}, {"zA"}}, {1, {0, 8, 16, 32}, {"zB"}}, {2, {0, 8, 16, 32}, {"zC"}},
         {3, {0, 8, 16, 32}, {"zD"}}, {4, {0, 8, 16, 32}, {"zE"}},
         {5, {2, 4, 8}, {"xA", "xB", "xC", "xD"}},
-        {6, {4, 8, 16}, {"fftz_fwd", "fftz_inv"}},
+        {6, {0, 4, 8, 16}, {"fftz_fwd", "fftz_inv"}},
         {8, {0, 1, 2}, {"fftz_fwd", "fftz_inv"}},
-        {7, {0, 1, 2}, {"xC", "xD"}},
+        {7, {0, 1, 2, 3}, {"xC", "xD"}},
         {11, {0, 2, 3}, {"xC"}},
     };
     auto knob = [](Tune &t, int q) -> int & {

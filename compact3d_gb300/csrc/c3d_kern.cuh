@@ -293,6 +293,20 @@ __device__ __forceinline__ void crow_load(T (&v)[C], const T *s, int lane, int P
     }
 }
 
+// Asynchronous global -> shared copy of one complex value (8 or 16 bytes, naturally
+// aligned), and the wait for all of this thread's outstanding copies.
+template <typename C2>
+__device__ __forceinline__ void cp_async_c2(C2 *dst, const C2 *src) {
+    static_assert(sizeof(C2) == 8 || sizeof(C2) == 16, "complex of float or double");
+    if constexpr (sizeof(C2) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                     "l"(__cvta_generic_to_global(src)) : "memory");
+    else
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                     "l"(__cvta_generic_to_global(src)) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // ---------------------------------------------------------------------------------
 // Bulk-copy ring: one lane of a warp streams whole rows (contiguous byte runs) from
 // global memory into shared-memory stages with cp.async.bulk; each stage completes on
@@ -401,6 +415,150 @@ __device__ __forceinline__ void dftc(C2 (&v)[P]) {
         v[1] = cadd(a, b);
         v[2] = csub(a, b);
     }
+}
+
+// In-register DFT of N points (N = 2^a 3^b dividing NT), natural order in and out, by
+// recursive radix-4/2/3 decimation in time.  w[j] = exp(SIGN 2 pi i j / NT); every index
+// is a compile-time constant, so the recursion unrolls into straight-line code.
+template <int N, int SIGN, int NT, typename C2>
+__device__ __forceinline__ void rdft(C2 (&x)[N], const C2 (&w)[NT]) {
+    if constexpr (N > 1) {
+        constexpr int P = (N % 4 == 0) ? 4 : (N % 2 == 0) ? 2 : 3;
+        constexpr int M = N / P;
+        C2 sub[P][M];
+#pragma unroll
+        for (int r = 0; r < P; ++r)
+#pragma unroll
+            for (int m = 0; m < M; ++m) sub[r][m] = x[P * m + r];
+#pragma unroll
+        for (int r = 0; r < P; ++r) rdft<M, SIGN, NT>(sub[r], w);
+#pragma unroll
+        for (int k = 0; k < M; ++k) {
+            C2 t[P];
+#pragma unroll
+            for (int r = 0; r < P; ++r) t[r] = (r * k == 0) ? sub[r][k] : cmul(sub[r][k], w[(r * k * (NT / N)) % NT]);
+            dftc<P, SIGN>(t);
+#pragma unroll
+            for (int s = 0; s < P; ++s) x[k + M * s] = t[s];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Row FFTs of the x passes in registers (four-step form), for N1M = 64 Q (C = 2Q points
+// per lane).  The packed complex row z[m] = x[2m] + i x[2m+1], m < M = 32 Q, sits in the
+// lane chunks as z[Q lane + j], j < Q.  Forward: per j a 32-point DFT across the lanes
+// (decimation in frequency, five shuffle stages; lane l ends with k1 = bitrev5(l)), the
+// twiddle W_M^(j k1), a Q-point DFT over j in registers: lane l holds Z[k1 + 32 k2].
+// Inverse: the same steps in reverse order with conjugate twiddles, ending in the lane
+// chunks again.  tabM[j] = exp(-2 pi i j / M) is the x plan's table.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ int brev5(int l) { return (int)(__brev((unsigned)l) >> 27); }
+
+// Real row (lane chunks) -> half spectrum Sp[0..M] (R2C post-processing as in the x pass
+// of RHSDP: E + exp(-2 pi i kx / N1M) O).
+template <typename R, int C>
+__device__ __forceinline__ void xrow_r2c(const R (&d)[C], const typename Cx<R>::T *__restrict__ tabM,
+                                         const typename Cx<R>::T *__restrict__ twx, typename Cx<R>::T *Sp, int lane) {
+    typedef typename Cx<R>::T C2;
+    constexpr int Q = C / 2, M = 32 * Q;
+    C2 x[Q];
+#pragma unroll
+    for (int j = 0; j < Q; ++j) { x[j].x = d[2 * j]; x[j].y = d[2 * j + 1]; }
+#pragma unroll
+    for (int st = 0; st < 5; ++st) {
+        const int h = 16 >> st;
+        const bool hi = (lane & h) != 0;
+        const C2 w = __ldg(&tabM[(lane & (h - 1)) * (16 * Q / h)]);
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            C2 o;
+            o.x = __shfl_xor_sync(0xffffffffu, x[j].x, h);
+            o.y = __shfl_xor_sync(0xffffffffu, x[j].y, h);
+            x[j] = hi ? cmul(csub(o, x[j]), w) : cadd(x[j], o);
+        }
+    }
+    const int k1 = brev5(lane);
+    if constexpr (Q > 1) {
+#pragma unroll
+        for (int j = 1; j < Q; ++j) x[j] = cmul(x[j], __ldg(&tabM[j * k1]));
+        C2 wq[Q];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) wq[j] = __ldg(&tabM[32 * j]);
+        rdft<Q, -1, Q>(x, wq);
+    }
+    const int pl = brev5((32 - k1) & 31);   // lane holding k1' = 32 - k1
+#pragma unroll
+    for (int k2 = 0; k2 < Q; ++k2) {
+        C2 zo;
+        zo.x = __shfl_sync(0xffffffffu, x[Q - 1 - k2].x, pl);
+        zo.y = __shfl_sync(0xffffffffu, x[Q - 1 - k2].y, pl);
+        if (lane == 0) zo = x[(Q - k2) % Q];   // k1 = 0: Z[M - 32 k2] = Z[32 ((Q - k2) mod Q)]
+        const C2 zk = x[k2], zm = cconj(zo);
+        const int kx = k1 + 32 * k2;
+        C2 E, O;
+        E.x = (zk.x + zm.x) * 0.5f;
+        E.y = (zk.y + zm.y) * 0.5f;
+        const C2 df = csub(zk, zm);
+        O.x = df.y * 0.5f;
+        O.y = -df.x * 0.5f;
+        Sp[kx] = cadd(E, cmul(__ldg(&twx[kx]), O));
+    }
+    if (lane == 0) {   // Nyquist mode kx = M from Z[0]
+        const C2 zk = x[0], zm = cconj(x[0]);
+        C2 E, O;
+        E.x = (zk.x + zm.x) * 0.5f;
+        E.y = (zk.y + zm.y) * 0.5f;
+        const C2 df = csub(zk, zm);
+        O.x = df.y * 0.5f;
+        O.y = -df.x * 0.5f;
+        Sp[M] = cadd(E, cmul(__ldg(&twx[M]), O));
+    }
+}
+
+// Half spectrum Sp[0..M] -> real row in the lane chunks (unscaled; C2R pre-processing as
+// in the x pass of GETDP's inverse transform).
+template <typename R, int C>
+__device__ __forceinline__ void xrow_c2r(R (&d)[C], const typename Cx<R>::T *__restrict__ tabM,
+                                         const typename Cx<R>::T *__restrict__ twx, const typename Cx<R>::T *Sp,
+                                         int lane) {
+    typedef typename Cx<R>::T C2;
+    constexpr int Q = C / 2, M = 32 * Q;
+    const int k1 = brev5(lane);
+    C2 x[Q];
+#pragma unroll
+    for (int k2 = 0; k2 < Q; ++k2) {
+        const int kx = k1 + 32 * k2;
+        const C2 xk = Sp[kx], xm = cconj(Sp[M - kx]);
+        const C2 E = cadd(xk, xm);
+        const C2 O = cmul(csub(xk, xm), cconj(__ldg(&twx[kx])));
+        x[k2].x = E.x - O.y;
+        x[k2].y = E.y + O.x;
+    }
+    if constexpr (Q > 1) {
+        C2 wq[Q];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) wq[j] = cconj(__ldg(&tabM[32 * j]));
+        rdft<Q, +1, Q>(x, wq);
+#pragma unroll
+        for (int j = 1; j < Q; ++j) x[j] = cmul(x[j], cconj(__ldg(&tabM[j * k1])));
+    }
+#pragma unroll
+    for (int st = 4; st >= 0; --st) {
+        const int h = 16 >> st;
+        const bool hi = (lane & h) != 0;
+        const C2 w = cconj(__ldg(&tabM[(lane & (h - 1)) * (16 * Q / h)]));
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const C2 t = hi ? cmul(x[j], w) : x[j];
+            C2 o;
+            o.x = __shfl_xor_sync(0xffffffffu, t.x, h);
+            o.y = __shfl_xor_sync(0xffffffffu, t.y, h);
+            x[j] = hi ? csub(o, t) : cadd(t, o);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < Q; ++j) { d[2 * j] = x[j].x; d[2 * j + 1] = x[j].y; }
 }
 
 // One radix-P Stockham stage: a -> b over 2^lsh interleaved sequences of length n

@@ -31,6 +31,79 @@ __global__ void __launch_bounds__(TPB) k_fftz(StepArgs<R> a, int sign, int tw) {
     }
 }
 
+// Complex FFT along kz, one warp per kx column, for N3M = 32 N1 (four-step form).  The
+// block stages a tile of TWW kx columns of one plane in shared memory (coalesced rows,
+// padded pitch); a warp holds its column as x[n1] = X(32 n1 + lane), takes the N1-point
+// DFT over n1 in registers, multiplies by exp(sign 2 pi i lane k1 / N3M), and finishes
+// with a 32-point DFT across the lanes (five decimation-in-frequency shuffle stages),
+// after which lane l holds the outputs k1 + N1 bitrev5(l).  Twiddles come from the z
+// plan's table exp(-2 pi i j / N3M).
+constexpr int TWW = 16;    // kx columns per block
+constexpr int FZW = 8;     // warps per block
+template <typename R, int N1, int SIGN>
+__global__ void __launch_bounds__(FZW * 32) k_fftz4(StepArgs<R> a) {
+    typedef typename Cx<R>::T C2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2 *T = reinterpret_cast<C2 *>(smem_raw);
+    const Geo g = a.g;
+    constexpr int n = 32 * N1, pitch = TWW + 1;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int ntile = (g.n1h + TWW - 1) / TWW;
+    const int plane = blockIdx.x / ntile, kx0 = (blockIdx.x % ntile) * TWW;
+    const int w = min(TWW, g.n1h - kx0);
+    C2 *S = reinterpret_cast<C2 *>(a.spec) + (long long)plane * n * g.n1h + kx0;
+    const C2 *tw = twsel<C2>(a.fz);
+    auto twd = [&](int j) {   // exp(SIGN 2 pi i j / n)
+        C2 t = __ldg(&tw[j]);
+        if constexpr (SIGN > 0) t.y = -t.y;
+        return t;
+    };
+    // the tile arrives by asynchronous copies (no register staging), all in flight at once
+    for (int e = threadIdx.x; e < n * TWW; e += FZW * 32) {
+        const int q = e >> 4, l = e & (TWW - 1);
+        if (l < w) cp_async_c2(&T[q * pitch + l], &S[q * g.n1h + l]);
+    }
+    cp_async_wait_all();
+    C2 wn1[N1], tl[N1], ts[5];
+#pragma unroll
+    for (int j = 0; j < N1; ++j) { wn1[j] = twd(32 * j); tl[j] = twd(lane * j); }
+#pragma unroll
+    for (int st = 0; st < 5; ++st) {   // stage with half-distance h = 16 >> st: exp(SIGN 2 pi i (lane mod h) / 2h)
+        const int h = 16 >> st;
+        ts[st] = twd((lane & (h - 1)) * (n / (2 * h)));
+    }
+    __syncthreads();
+    const int rl = __brev((unsigned)lane) >> 27;   // bitrev5(lane)
+    for (int c = wid; c < w; c += FZW) {
+        C2 x[N1];
+#pragma unroll
+        for (int m = 0; m < N1; ++m) x[m] = T[(32 * m + lane) * pitch + c];
+        rdft<N1, SIGN, N1>(x, wn1);
+#pragma unroll
+        for (int k = 1; k < N1; ++k) x[k] = cmul(x[k], tl[k]);
+#pragma unroll
+        for (int st = 0; st < 5; ++st) {
+            const int h = 16 >> st;
+            const bool hi = (lane & h) != 0;
+#pragma unroll
+            for (int k = 0; k < N1; ++k) {
+                C2 o;
+                o.x = __shfl_xor_sync(0xffffffffu, x[k].x, h);
+                o.y = __shfl_xor_sync(0xffffffffu, x[k].y, h);
+                x[k] = hi ? cmul(csub(o, x[k]), ts[st]) : cadd(x[k], o);
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < N1; ++k) T[(k + N1 * rl) * pitch + c] = x[k];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * TWW; e += FZW * 32) {
+        const int q = e >> 4, l = e & (TWW - 1);
+        if (l < w) S[q * g.n1h + l] = T[q * pitch + l];
+    }
+}
+
 // One Thomas solve per mode (kx, kz) with A_J = PMJ, B_J = PCJ - AK3 - AK1, C_J = PPJ,
 // factors tabulated by k_ptables; the (0,0) mode has row 1 = (0, 1, 0 | 0) and the
 // imaginary parts of the self-conjugate modes are zero (compact3d.f:9363-9397).
@@ -198,12 +271,47 @@ void set_spec_smem(c3d_channel *ch) {
     cudaFuncSetAttribute(k_fftz<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
 }
 
+// The four-step z FFT for N3M = 32 N1; false when N3M is not of that form.
+template <typename R, int SIGN>
+static bool launch_fftz4(c3d_channel *ch, StepArgs<R> &a) {
+    typedef typename Cx<R>::T C2;
+    const Geo &g = ch->g;
+    if (g.n3m % 32 != 0) return false;
+    const int ntile = (g.n1h + TWW - 1) / TWW;
+    const size_t sm = (size_t)g.n3m * (TWW + 1) * sizeof(C2);
+    const dim3 grid(g.n2m * ntile), blk(FZW * 32);
+    void (*fn)(StepArgs<R>) = nullptr;
+    switch (g.n3m / 32) {
+        case 2: fn = k_fftz4<R, 2, SIGN>; break;
+        case 3: fn = k_fftz4<R, 3, SIGN>; break;
+        case 4: fn = k_fftz4<R, 4, SIGN>; break;
+        case 6: fn = k_fftz4<R, 6, SIGN>; break;
+        case 8: fn = k_fftz4<R, 8, SIGN>; break;
+        case 12: fn = k_fftz4<R, 12, SIGN>; break;
+        case 16: fn = k_fftz4<R, 16, SIGN>; break;
+        default: return false;
+    }
+    if (sm > 227 * 1024) return false;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    fn<<<grid, blk, sm, ch->stream>>>(a);
+    return true;
+}
+
 template <typename R>
 int launch_spec(c3d_channel *ch, StepArgs<R> &a, int which, int *nl) {
     typedef typename Cx<R>::T C2;
     cudaStream_t st = ch->stream;
     const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
-    const int tw = ch->tune.twz;
+    if (ch->tune.twz == 0 && (which == 0 || which == 2)) {   // four-step form when N3M allows
+        if (which == 0 ? launch_fftz4<R, -1>(ch, a) : launch_fftz4<R, +1>(ch, a)) {
+            mark(ch, nl, which == 0 ? "fftz_fwd" : "fftz_inv", N * 2 * Rb);
+            return 0;
+        }
+    }
+    const int tw = ch->tune.twz == 0 ? 8 : ch->tune.twz;
     const int ntile = (ch->g.n1h + tw - 1) / tw;
     const size_t smz = 2 * (size_t)ch->g.n3m * tw * sizeof(C2);
     switch (which) {

@@ -452,7 +452,7 @@ struct XcStage {
 
 // One row of xC: the x part of div(UH)/DT from U + DH1 (compact (1,22,1) derivative),
 // the y part from V + DH2 on planes J and J+1, plus RDPZ; then the real-to-complex FFT.
-template <bool SH, typename R, int C>
+template <bool SH, typename R, int C, bool X4 = false>
 __device__ __forceinline__ void xc_row(const StepArgs<R> &a, int j, int k, const typename SType<R>::S *u,
                                        const R *d0, const typename SType<R>::S *vc, const R *dc,
                                        const typename SType<R>::S *vp, const R *dp, const R *zr,
@@ -503,6 +503,14 @@ __device__ __forceinline__ void xc_row(const StepArgs<R> &a, int j, int k, const
 #pragma unroll
         for (int t = 0; t < C; ++t) d[t] = (base[t] + d[t] * rdt) + zc[t];
     }
+    const C2 *twx;
+    if constexpr (sizeof(R) == 8) twx = reinterpret_cast<const C2 *>(a.twx64);
+    else twx = reinterpret_cast<const C2 *>(a.twx32);
+    C2 *Sp = reinterpret_cast<C2 *>(a.spec) + ((long long)(j - 1) * g.n3m + k) * g.n1h;
+    if constexpr (X4) {   // four-step row FFT in registers
+        xrow_r2c<R, C>(d, twsel<C2>(a.fx), twx, Sp, lane);
+        return;
+    }
     // real row -> shared memory as M complex values, FFT, post-process to N1M/2+1 modes
     if (lane < P) {
 #pragma unroll
@@ -510,10 +518,6 @@ __device__ __forceinline__ void xc_row(const StepArgs<R> &a, int j, int k, const
     }
     __syncwarp();
     C2 *Z = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, -1, lane, 32);
-    const C2 *twx;
-    if constexpr (sizeof(R) == 8) twx = reinterpret_cast<const C2 *>(a.twx64);
-    else twx = reinterpret_cast<const C2 *>(a.twx32);
-    C2 *Sp = reinterpret_cast<C2 *>(a.spec) + ((long long)(j - 1) * g.n3m + k) * g.n1h;
     for (int kx = lane; kx <= M; kx += 32) {
         C2 zk = Z[kx == M ? 0 : kx], zm = cconj(Z[kx == 0 ? 0 : M - kx]);
         C2 E, O;
@@ -533,7 +537,7 @@ __device__ __forceinline__ void xc_row(const StepArgs<R> &a, int j, int k, const
 // an NS-stage bulk-copy ring that fetches the rows of its next NS-1 (J, K) while it
 // computes the current one.
 // ---------------------------------------------------------------------------------
-template <typename R, int C, int NS>
+template <typename R, int C, int NS, bool X4 = false>
 __global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const R *d1) {
     typedef typename SType<R>::S S;
     typedef typename Cx<R>::T C2;
@@ -556,8 +560,8 @@ __global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const 
                 if (j >= 2) { pf_row(a.v + o, rs_, lane); pf_row(d1 + o, rr_, lane); }
                 if (j + 1 <= g.n2m) { pf_row(a.v + op, rs_, lane); pf_row(d1 + op, rr_, lane); }
             }
-            xc_row<false, R, C>(a, j, k, a.u + o, d0 + o, a.v + o, d1 + o, a.v + op, d1 + op, a.rdpz + o, wb,
-                                bufa, bufa + (M + 1), lane);
+            xc_row<false, R, C, X4>(a, j, k, a.u + o, d0 + o, a.v + o, d1 + o, a.v + op, d1 + op, a.rdpz + o, wb,
+                                    bufa, bufa + (M + 1), lane);
         }
     } else {
         const XcStage<R> L(g.n1m);
@@ -612,7 +616,7 @@ __global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const 
 // ---------------------------------------------------------------------------------
 // xD: complex-to-real FFT -> DP, compact dDP/dx, bulk-flow partial sums
 // ---------------------------------------------------------------------------------
-template <typename R, int C>
+template <typename R, int C, bool X4 = false>
 __global__ void __launch_bounds__(XMAXT) k_xD(StepArgs<R> a, const R *d0, const R *d2) {
     typedef typename Cx<R>::T C2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -638,29 +642,35 @@ __global__ void __launch_bounds__(XMAXT) k_xD(StepArgs<R> a, const R *d0, const 
             const int rr_ = g.n1m * (int)sizeof(R);
             pf_row(d0 + o, rr_, lane); pf_row(d2 + o, rr_, lane);
         }
-        for (int kx = lane; kx <= M; kx += 32) bufb[kx] = Sp[kx];
-        __syncwarp();
-        for (int kx = lane; kx < M; kx += 32) {
-            C2 xk = bufb[kx], xm = cconj(bufb[M - kx]);
-            C2 E = cadd(xk, xm);
-            C2 O = cmul(csub(xk, xm), cconj(twx[kx]));
-            C2 Z;
-            Z.x = E.x - O.y;
-            Z.y = E.y + O.x;
-            bufa[kx] = Z;
-        }
-        __syncwarp();
-        C2 *Zr = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, +1, lane, 32);
-        const R *rz = reinterpret_cast<const R *>(Zr);
         R dpv[C];
-        if (lane < P) {
+        if constexpr (X4) {   // four-step row FFT in registers
+            xrow_c2r<R, C>(dpv, twsel<C2>(a.fx), twx, Sp, lane);
 #pragma unroll
-            for (int t = 0; t < C; ++t) dpv[t] = rz[lane * C + t] * scale;
+            for (int t = 0; t < C; ++t) dpv[t] *= scale;
         } else {
+            for (int kx = lane; kx <= M; kx += 32) bufb[kx] = Sp[kx];
+            __syncwarp();
+            for (int kx = lane; kx < M; kx += 32) {
+                C2 xk = bufb[kx], xm = cconj(bufb[M - kx]);
+                C2 E = cadd(xk, xm);
+                C2 O = cmul(csub(xk, xm), cconj(twx[kx]));
+                C2 Z;
+                Z.x = E.x - O.y;
+                Z.y = E.y + O.x;
+                bufa[kx] = Z;
+            }
+            __syncwarp();
+            C2 *Zr = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, +1, lane, 32);
+            const R *rz = reinterpret_cast<const R *>(Zr);
+            if (lane < P) {
 #pragma unroll
-            for (int t = 0; t < C; ++t) dpv[t] = R(0);
+                for (int t = 0; t < C; ++t) dpv[t] = rz[lane * C + t] * scale;
+            } else {
+#pragma unroll
+                for (int t = 0; t < C; ++t) dpv[t] = R(0);
+            }
+            __syncwarp();
         }
-        __syncwarp();
         srow_store(a.dp + o, dpv, sbR, lane, P);
         R d[C];
         R pv = sprev(dpv[C - 1], lane, P);
@@ -869,6 +879,10 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
                 if (ch->tune.xbulk == 2) done = launch_xc_bulk<R, C, 2>(ch, a, xw, p0, p1);
                 else if (ch->tune.xbulk == 3) done = launch_xc_bulk<R, C, 3>(ch, a, xw, p0, p1);
             }
+            if (!done && C % 2 == 0 && ch->tune.fxp == 3) {   // register row FFT: no shared memory
+                k_xC<R, C, 0, (C % 2 == 0)><<<grid, nt, sb, st>>>(a, p0, p1);
+                done = true;
+            }
             if (!done) {
                 cudaFuncSetAttribute(k_xC<R, C, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
                 k_xC<R, C, 0><<<grid, nt, fb, st>>>(a, p0, p1);
@@ -877,8 +891,12 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
             break;
         }
         case 3:
-            cudaFuncSetAttribute(k_xD<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
-            k_xD<R, C><<<grid, nt, fb, st>>>(a, p0, p1);
+            if (C % 2 == 0 && ch->tune.fxp == 3) {
+                k_xD<R, C, (C % 2 == 0)><<<grid, nt, sb, st>>>(a, p0, p1);
+            } else {
+                cudaFuncSetAttribute(k_xD<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
+                k_xD<R, C><<<grid, nt, fb, st>>>(a, p0, p1);
+            }
             mark(ch, nl, "xD", N * 5 * Rb);
             break;
         case 4: {

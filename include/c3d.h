@@ -218,9 +218,12 @@ int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
  *       8, 12 or 16 points, the segments of a line joined exactly through shared
  *       memory (N3M / segment length <= 32; otherwise segments of 16)
  *   [5] rows per block of the x passes (2, 4, 8)
- *   [6] kx columns per block of the z FFT (4, 8, 16)
+ *   [6] kx columns per block of the z FFT (4, 8, 16), or 0: one warp per kx column,
+ *       four-step form (N3M / 32 points per lane in registers, then a 32-point
+ *       shuffle FFT across the lanes) when N3M is 32 x 2, 3, 4, 6, 8, 12 or 16
  *   [7], [8] radix order of the x and z FFT plans (0: radix 4 first, 1: radix 3
- *       first, 2: radix 2 only, then 3)
+ *       first, 2: radix 2 only, then 3); [7] = 3 runs the row FFTs of the pressure
+ *       x passes in registers (four-step form, no shared memory) when N1M / 32 is even
  *   [9] the z pass of the explicit terms as one kernel (0) or as its three sweeps
  *       in three kernels (1)
  *   [10] the x pass of the explicit terms as one kernel (0) or as its u, v and w

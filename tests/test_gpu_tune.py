@@ -34,14 +34,39 @@ def _sched(zl, xw, tw, fx, fz, split, xsplit, xbulk=0):
 
 
 # (schedule, N3M); z segment length 0 is the block form (segments of 8 points for N3M = 64,
-# 12 points in 32 segments for N3M = 384)
+# 12 points in 32 segments for N3M = 384); z-FFT tile 0 is the four-step warp FFT
+# (N1 = N3M / 32 = 2 and 12 points per lane)
 SCHEDULES = [
     (_sched((8, 8, 8, 8, 8), 2, 4, 1, 2, 1, 1), 64),
     (_sched((32, 32, 32, 32, 32), 8, 16, 2, 1, 0, 0), 64),
     (_sched((16, 8, 32, 16, 8), 4, 8, 0, 0, 1, 0, 2), 64),
-    (_sched((0, 0, 0, 0, 0), 2, 4, 0, 1, 1, 1), 64),
-    (_sched((0, 0, 0, 0, 0), 2, 4, 0, 1, 0, 0), 384),
+    (_sched((0, 0, 0, 0, 0), 2, 0, 0, 1, 1, 1), 64),
+    (_sched((0, 0, 0, 0, 0), 2, 0, 0, 1, 0, 0), 384),
+    (_sched((16, 16, 16, 16, 16), 2, 0, 0, 1, 1, 1), 96),
+    (_sched((8, 8, 32, 16, 8), 2, 0, 3, 1, 1, 1), 64),
 ]
+
+
+@pytest.mark.parametrize("n1m", [64, 128, 192, 256, 384])
+def test_register_row_fft_matches_oracle(libc3d, oracle_mod, n1m):
+    """The four-step register row FFT (x plan 3) for every even N1M / 32: one FP64 step
+    within 1e-10 of the oracle."""
+    g, dt = make_grid("small32", n1m=n1m, n2m=16, n3m=32)
+    orc = oracle_mod.Oracle(g)
+    U, P, HH = ic.perturbed_laminar(g)
+    orc.project(U)
+    ch = libc3d.Channel(g, C3D_FP64)
+    ch.upload(U, P, HH)
+    s = ch.get_schedule()
+    s.update(fft_x_plan=3)
+    ch.set_schedule(s)
+    orc.getup(U, P, HH, 1, dt, 0.0, 0.0)
+    ch.step(1, dt, 0.0, 0.0)
+    Ug, Pg, _ = ch.download()
+    n1, n2, n3 = g.n1m, g.n2m, g.n3m
+    for c, j0 in ((0, 1), (1, 2), (2, 1)):
+        e = rel(Ug[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c], U[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c])
+        assert e < 1e-10, (n1m, c, e)
 
 
 @pytest.mark.parametrize("sched,n3m", SCHEDULES)
@@ -73,7 +98,7 @@ def test_autotune_valid_and_cached(libc3d):
     a.project()
     s1 = a.autotune()
     assert all(s1[f"z_segment_z{c}"] in (0, 8, 16, 32) for c in "ABCDE") and s1["x_rows_per_block"] in (2, 4, 8)
-    assert s1["fft_z_tile"] in (4, 8, 16) and s1["fft_x_plan"] in (0, 1, 2) and s1["fft_z_plan"] in (0, 1, 2)
+    assert s1["fft_z_tile"] in (0, 4, 8, 16) and s1["fft_x_plan"] in (0, 1, 2, 3) and s1["fft_z_plan"] in (0, 1, 2)
     b = libc3d.Channel(g, C3D_MIXED)
     b.upload(U, P, HH)
     assert b.autotune() == s1          # cached for the same grid shape and form
