@@ -566,7 +566,8 @@ __global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const 
     } else {
         const XcStage<R> L(g.n1m);
         // per warp: NS barriers (16 bytes reserved each), NS stages, the FFT buffers
-        const size_t wbytes = 16 * NS + (size_t)NS * L.bytes + fbytes;
+        // (none for the register row FFT)
+        const size_t wbytes = 16 * NS + (size_t)NS * L.bytes + (X4 ? 0 : fbytes);
         unsigned char *wb = smem_raw + wid * wbytes;
         uint64_t *bar = reinterpret_cast<uint64_t *>(wb);
         unsigned char *stg = wb + 16 * NS;
@@ -605,7 +606,7 @@ __global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const 
             }
             const int j = 1 + row / g.n3m, k = row % g.n3m;
             const unsigned char *st = stg + (size_t)s * L.bytes;
-            xc_row<true, R, C>(a, j, k, reinterpret_cast<const S *>(st + L.u), reinterpret_cast<const R *>(st + L.d0),
+            xc_row<true, R, C, X4>(a, j, k, reinterpret_cast<const S *>(st + L.u), reinterpret_cast<const R *>(st + L.d0),
                                reinterpret_cast<const S *>(st + L.vc), reinterpret_cast<const R *>(st + L.dc),
                                reinterpret_cast<const S *>(st + L.vp), reinterpret_cast<const R *>(st + L.dp),
                                reinterpret_cast<const R *>(st + L.z), nullptr, bufa, bufa + (M + 1), lane);
@@ -818,16 +819,16 @@ static int persistent_grid(const void *fn, int nt, size_t smem, int want, int de
 
 // xC through the bulk-copy ring (mixed form); false when this shape cannot use it (rows
 // not a multiple of 16 bytes, or the stages do not fit in shared memory).
-template <typename R, int C, int NS>
+template <typename R, int C, int NS, bool X4>
 static bool launch_xc_bulk(c3d_channel *ch, StepArgs<R> &a, int xw, const R *p0, const R *p1) {
     typedef typename Cx<R>::T C2;
     const Geo &g = ch->g;
     if (g.n1m % 4 != 0) return false;
     const XcStage<R> L(g.n1m);
-    const size_t wbytes = 16 * NS + (size_t)NS * L.bytes + 2 * (size_t)(g.n1m / 2 + 1) * sizeof(C2);
+    const size_t wbytes = 16 * NS + (size_t)NS * L.bytes + (X4 ? 0 : 2 * (size_t)(g.n1m / 2 + 1) * sizeof(C2));
     const size_t smem = wbytes * xw;
     if (smem > 227 * 1024) return false;
-    auto fn = k_xC<R, C, NS>;
+    auto fn = k_xC<R, C, NS, X4>;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
         cudaGetLastError();
         return false;
@@ -876,8 +877,14 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
         case 2: {
             bool done = false;
             if constexpr (sizeof(R) == 4) {
-                if (ch->tune.xbulk == 2) done = launch_xc_bulk<R, C, 2>(ch, a, xw, p0, p1);
-                else if (ch->tune.xbulk == 3) done = launch_xc_bulk<R, C, 3>(ch, a, xw, p0, p1);
+                constexpr bool X4 = (C % 2 == 0);
+                if (X4 && ch->tune.fxp == 3) {
+                    if (ch->tune.xbulk == 2) done = launch_xc_bulk<R, C, 2, X4>(ch, a, xw, p0, p1);
+                    else if (ch->tune.xbulk == 3) done = launch_xc_bulk<R, C, 3, X4>(ch, a, xw, p0, p1);
+                } else {
+                    if (ch->tune.xbulk == 2) done = launch_xc_bulk<R, C, 2, false>(ch, a, xw, p0, p1);
+                    else if (ch->tune.xbulk == 3) done = launch_xc_bulk<R, C, 3, false>(ch, a, xw, p0, p1);
+                }
             }
             if (!done && C % 2 == 0 && ch->tune.fxp == 3) {   // register row FFT: no shared memory
                 k_xC<R, C, 0, (C % 2 == 0)><<<grid, nt, sb, st>>>(a, p0, p1);

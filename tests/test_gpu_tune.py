@@ -110,8 +110,8 @@ def test_autotune_valid_and_cached(libc3d):
         a.set_schedule(dict(s1, z_segment_zA=12))
 
 
-@pytest.mark.parametrize("shape", [(32, 128, 256), (96, 64, 64)])
-def test_bulk_rows_bit_identical(libc3d, shape):
+@pytest.mark.parametrize("shape,fxp", [((32, 128, 256), 0), ((96, 64, 64), 0), ((64, 128, 128), 3)])
+def test_bulk_rows_bit_identical(libc3d, shape, fxp):
     """The bulk-copy ring only changes where a row is read from: the mixed step is
     bit-identical with 0, 2 or 3 stages.  (32, 128, 256) gives every persistent warp
     several rows, so each stage's barrier runs through several phases."""
@@ -123,7 +123,7 @@ def test_bulk_rows_bit_identical(libc3d, shape):
         ch = libc3d.Channel(g, C3D_MIXED)
         ch.upload(U, P, HH)
         s = ch.get_schedule()
-        s.update(x_bulk_stages=xb)
+        s.update(x_bulk_stages=xb, fft_x_plan=fxp)
         ch.set_schedule(s)
         for m in (1, 2, 3):
             ch.step(m, dt, 0.0, 0.0)
