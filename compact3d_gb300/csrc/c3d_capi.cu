@@ -396,7 +396,7 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
         set_error("cudaMalloc state");
         return fail(C3D_ENOMEM);
     }
-    if (dalloc(&ch->scal, SCAL_COUNT) || dalloc(&ch->part, 2 * (size_t)g.n2m * g.n3m) ||
+    if (dalloc(&ch->scal, SCAL_COUNT) || dalloc(&ch->part, 2 * (size_t)g.n2m * g.n3m + 2 * RB) ||
         dalloc(&ch->metric, 10 * (size_t)(g.n2 + 1)) || dalloc(&ch->ycn, 9 * (size_t)(g.n2 + 1)) ||
         dalloc(&ch->ycn32, 9 * (size_t)(g.n2 + 1)) ||
         dalloc(&ch->pmj, (size_t)(g.n2 + 1)) || dalloc(&ch->pmjdf, (size_t)(g.n2 + 1)) ||

@@ -329,7 +329,7 @@ __device__ __forceinline__ void zsweep(R (&out)[NR][L], int k0, int n, const R (
     R y[NR], d[NR];
 #pragma unroll
     for (int q = 0; q < NR; ++q) y[q] = R(0);
-#pragma unroll 2
+#pragma unroll
     for (int t = 0; t < M; ++t) {
         f.next(d);
 #pragma unroll
@@ -348,7 +348,7 @@ __device__ __forceinline__ void zsweep(R (&out)[NR][L], int k0, int n, const R (
     R acc[NR], pw[NR];
 #pragma unroll
     for (int q = 0; q < NR; ++q) { acc[q] = R(0); pw[q] = R(1); }
-#pragma unroll 2
+#pragma unroll
     for (int t = 0; t < M; ++t) {
         f.next(d);
 #pragma unroll

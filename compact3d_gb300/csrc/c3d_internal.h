@@ -71,6 +71,10 @@ struct StepArgs {
     int bulk;                           // apply the bulk-flow forcing (GETUP) or not (projection)
 };
 
+// Blocks of the first level of the bulk-flow reduction; `part` holds 2 N2M N3M per-row
+// partials followed by 2 RB block sums.
+constexpr int RB = 64;
+
 enum {
     SCAL_PRESG = 0,
     SCAL_PRESG3 = 1,

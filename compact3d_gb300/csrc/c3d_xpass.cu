@@ -707,7 +707,7 @@ __global__ void __launch_bounds__(XMAXT) k_xD(StepArgs<R> a, const R *d0, const 
         } else {
             // Mixed form: double-float sums (exact two-sums of the FP32 deltas, FP32
             // instructions only) and a double-float weight; the slots of `part` hold
-            // float2 pairs that k_reduce combines in the same arithmetic.
+            // float2 pairs that k_reduce1/k_reduce2 combine in the same arithmetic.
             float2 s1 = make_float2(0.f, 0.f), s3 = s1;
 #pragma unroll
             for (int t = 0; t < C; ++t) {
