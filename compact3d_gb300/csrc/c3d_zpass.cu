@@ -124,20 +124,21 @@ struct WalkZB {
 // zC: (x- + 10x) + x+ for the three components
 template <typename R>
 struct WalkCN {
-    const R *X[3]; int n, s; R xm[3], xc[3]; int kn;
+    const R *X[3]; int n, s; R xm[3], xc[3]; ZRing<R> rx[3];
     __device__ void start(int k) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) { xm[c] = X[c][zprev(k, n) * s]; xc[c] = X[c][k * s]; }
-        kn = znext(k, n);
+        for (int c = 0; c < 3; ++c) {
+            xm[c] = X[c][zprev(k, n) * s]; xc[c] = X[c][k * s];
+            rx[c].fill(X[c], k, n, s);
+        }
     }
     __device__ void next(R (&d)[3]) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            R xp = X[c][kn * s];
+            R xp = rx[c].pop(X[c], n, s);
             d[c] = (xm[c] + (R)10.0 * xc[c]) + xp;
             xm[c] = xc[c]; xc[c] = xp;
         }
-        kn = znext(kn, n);
     }
 };
 
@@ -145,24 +146,24 @@ struct WalkCN {
 template <typename R>
 struct WalkDivZ {
     typedef typename SType<R>::S S;
-    const S *W; const R *D; int n, s; R f24; S wc; R dc; int kn;
-    __device__ void start(int k) { wc = W[k * s]; dc = D[k * s]; kn = znext(k, n); }
+    const S *W; const R *D; int n, s; R f24; S wc; R dc; ZRing<S> rw; ZRing<R> rd;
+    __device__ void start(int k) { wc = W[k * s]; dc = D[k * s]; rw.fill(W, k, n, s); rd.fill(D, k, n, s); }
     __device__ void next(R (&d)[1]) {
-        S wp = W[kn * s]; R dp = D[kn * s];
+        S wp = rw.pop(W, n, s); R dp = rd.pop(D, n, s);
         d[0] = f24 * Sten<R>::dd(wp, dp, wc, dc);
-        wc = wp; dc = dp; kn = znext(kn, n);
+        wc = wp; dc = dp;
     }
 };
 
 // zE: f24*(DP - DP-)
 template <typename R>
 struct WalkGradZ {
-    const R *DP; int n, s; R f24; R pm; int kc;
-    __device__ void start(int k) { pm = DP[zprev(k, n) * s]; kc = k; }
+    const R *DP; int n, s; R f24; R pm; ZRing<R> rp;
+    __device__ void start(int k) { pm = DP[zprev(k, n) * s]; rp.fill(DP, zprev(k, n), n, s); }
     __device__ void next(R (&d)[1]) {
-        R pc = DP[kc * s];
+        R pc = rp.pop(DP, n, s);
         d[0] = f24 * (pc - pm);
-        pm = pc; kc = znext(kc, n);
+        pm = pc;
     }
 };
 
