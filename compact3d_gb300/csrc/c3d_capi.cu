@@ -189,6 +189,13 @@ void free_channel(c3d_channel *ch) {
     if (ch->tm0) cudaEventDestroy(ch->tm0);
     if (ch->tm1) cudaEventDestroy(ch->tm1);
     if (ch->stream) cudaStreamDestroy(ch->stream);
+    if (ch->side) cudaStreamDestroy(ch->side);
+    if (ch->cs) cudaStreamDestroy(ch->cs);
+    for (cudaEvent_t e : ch->xev)
+        if (e) cudaEventDestroy(e);
+    if (ch->xfer) cudaFree(ch->xfer);
+    if (ch->hh_in) cudaEventDestroy(ch->hh_in);
+    if (ch->hh_out) cudaEventDestroy(ch->hh_out);
     if (ch->ev0) cudaEventDestroy(ch->ev0);
     if (ch->ev1) cudaEventDestroy(ch->ev1);
     delete ch;
@@ -291,8 +298,8 @@ int check_grid(const c3d_grid *g) {
         return C3D_EINVAL;
     }
     if (n2m < 4 || n2m > 4096) { set_error("N2-1 must be in [4, 4096]"); return C3D_EINVAL; }
-    if ((long long)(n2m + 2) * n1m * n3m >= (1LL << 31)) {   // kernels index points in 32 bits
-        set_error("a field of (N2+1) x (N1-1) x (N3-1) points must have fewer than 2^31 points");
+    if ((long long)(n1m + 2) * (n2m + 2) * (n3m + 2) >= (1LL << 31)) {   // kernels index points in 32 bits
+        set_error("the arrays U(0:N1,0:N2,0:N3) must have fewer than 2^31 points per component");
         return C3D_EINVAL;
     }
     if (!g->y || !g->dy || !g->h || !g->hm || !g->hc || !g->hp || !g->dym || !g->dyc || !g->dyp) {
@@ -577,21 +584,85 @@ int c3d_destroy(c3d_channel *ch) {
     return 0;
 }
 
-// Device address of a host array registered with c3d_host_register (mapped), or null
-// when [h, h + bytes) is not mapped host memory (then the staged copy is used).  Both ends
-// of the range are checked so the repack kernels only touch mapped addresses.
-static double *host_mapped(const void *h, size_t bytes) {
-    if (!h || !bytes) return nullptr;
+// True when [h, h + bytes) lies in one host allocation registered with c3d_host_register
+// (page-locked): such arrays move by DMA at the link's rate.
+static bool host_pinned(const void *h, size_t bytes) {
+    if (!h || !bytes) return false;
     cudaPointerAttributes a0, a1;
     const char *last = (const char *)h + bytes - 1;
     if (cudaPointerGetAttributes(&a0, h) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
         cudaGetLastError();
-        return nullptr;
+        return false;
     }
     if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
-        return nullptr;
-    if ((const char *)a1.devicePointer - (const char *)a0.devicePointer != (long long)(bytes - 1)) return nullptr;
-    return (double *)a0.devicePointer;
+        return false;
+    return (const char *)a1.devicePointer - (const char *)a0.devicePointer == (long long)(bytes - 1);
+}
+
+// Device staging area for the DMA transfers of pinned arrays, one slot per Fortran field:
+// U(3 components), P, HH(3), SGSVIS; allocated on first use.
+struct Xfer {
+    size_t n3, np;
+    double *base;
+    double *u(int c) const { return base + c * n3; }
+    double *p() const { return base + 3 * n3; }
+    double *hh(int c) const { return base + 3 * n3 + np + c * n3; }
+    double *sgs() const { return base + 6 * n3 + np; }
+};
+static int xfer_area(c3d_channel *ch, Xfer *x) {
+    const Geo &g = ch->g;
+    x->n3 = ch->stage_elems;
+    x->np = (size_t)(g.n1m + 1) * g.n2 * (g.n3m + 1);
+    if (!ch->xfer) {
+        if (cudaMalloc(&ch->xfer, (7 * x->n3 + x->np) * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            ch->xfer = nullptr;
+            set_error("cudaMalloc of the transfer staging area");
+            return C3D_ENOMEM;
+        }
+    }
+    x->base = ch->xfer;
+    return 0;
+}
+// Streams and events of the pipelined DMA transfers (created on first use).
+static int xfer_streams(c3d_channel *ch) {
+    if (!ch->side) {
+        CK(cudaStreamCreateWithFlags(&ch->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ch->hh_in, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ch->hh_out, cudaEventDisableTiming));
+    }
+    if (!ch->cs) {
+        CK(cudaStreamCreateWithFlags(&ch->cs, cudaStreamNonBlocking));
+        for (cudaEvent_t &e : ch->xev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    return 0;
+}
+// Host -> device of one field: DMA into its slot on the copy stream, then the unpacking
+// kernel on stream st once the copy is done (event ev), so the next field's copy overlaps
+// this field's unpacking.
+static int up_field(c3d_channel *ch, cudaStream_t st, cudaEvent_t ev, double *slot, const double *h, size_t n,
+                    int what, int comp) {
+    CK(cudaMemcpyAsync(slot, h, n * sizeof(double), cudaMemcpyHostToDevice, ch->cs));
+    CK(cudaEventRecord(ev, ch->cs));
+    CK(cudaStreamWaitEvent(st, ev, 0));
+    cudaStream_t keep = ch->stream;
+    ch->stream = st;
+    launch_repack(ch, 0, what, comp, slot);
+    ch->stream = keep;
+    return 0;
+}
+// Device -> host of one field: the packing kernel into its slot on stream st, then the DMA
+// on the copy stream once it is done (event ev).
+static int dn_field(c3d_channel *ch, cudaStream_t st, cudaEvent_t ev, double *slot, double *h, size_t n, int what,
+                    int comp) {
+    cudaStream_t keep = ch->stream;
+    ch->stream = st;
+    launch_repack(ch, 1, what, comp, slot);
+    ch->stream = keep;
+    CK(cudaEventRecord(ev, st));
+    CK(cudaStreamWaitEvent(ch->cs, ev, 0));
+    CK(cudaMemcpyAsync(h, slot, n * sizeof(double), cudaMemcpyDeviceToHost, ch->cs));
+    return 0;
 }
 
 static int h2d(c3d_channel *ch, const double *src, size_t n) {
@@ -613,27 +684,32 @@ int c3d_upload(c3d_channel *ch, const double *u, const double *p, const double *
     const size_t n3 = ch->stage_elems;   // one component of U / HH
     const Geo &g = ch->g;
     const size_t np_ = (size_t)(g.n1m + 1) * g.n2 * (g.n3m + 1);
-    // Mapped host arrays are read by the repack kernels directly (no staging copy).
-    double *mu = host_mapped(u, 3 * n3 * 8), *mp = host_mapped(p, np_ * 8), *mh = host_mapped(hh, 3 * n3 * 8);
-    for (int c = 0; c < 3; ++c) {
-        if (u && mu) launch_repack(ch, 0, 0, c, mu + c * n3);
-        else if (u) {
-            int rc = h2d(ch, u + c * n3, n3);
-            if (rc) return rc;
+    const bool pinned = (!u || host_pinned(u, 3 * n3 * 8)) && (!p || host_pinned(p, np_ * 8)) &&
+                        (!hh || host_pinned(hh, 3 * n3 * 8));
+    int rc = 0;
+    Xfer x;
+    if (pinned && (rc = xfer_area(ch, &x)) == 0 && (rc = xfer_streams(ch)) == 0) {
+        // every field by DMA on the copy stream, each unpacked as soon as it has arrived
+        CK(cudaEventRecord(ch->xev[15], ch->stream));   // after earlier work on the slots
+        CK(cudaStreamWaitEvent(ch->cs, ch->xev[15], 0));
+        for (int c = 0; c < 3 && u; ++c)
+            if ((rc = up_field(ch, ch->stream, ch->xev[c], x.u(c), u + c * n3, n3, 0, c))) return rc;
+        if (p && (rc = up_field(ch, ch->stream, ch->xev[3], x.p(), p, np_, 1, 0))) return rc;
+        for (int c = 0; c < 3 && hh; ++c)
+            if ((rc = up_field(ch, ch->stream, ch->xev[4 + c], x.hh(c), hh + c * n3, n3, 2, c))) return rc;
+    } else if (rc && rc != C3D_ENOMEM) {
+        return rc;
+    } else {   // pageable arrays: one field at a time through the one-field staging buffer
+        for (int c = 0; c < 3 && u; ++c) {
+            if ((rc = h2d(ch, u + c * n3, n3))) return rc;
             launch_repack(ch, 0, 0, c);
         }
-    }
-    if (p && mp) launch_repack(ch, 0, 1, 0, mp);
-    else if (p) {
-        int rc = h2d(ch, p, np_);
-        if (rc) return rc;
-        launch_repack(ch, 0, 1, 0);
-    }
-    for (int c = 0; c < 3; ++c) {
-        if (hh && mh) launch_repack(ch, 0, 2, c, mh + c * n3);
-        else if (hh) {
-            int rc = h2d(ch, hh + c * n3, n3);
-            if (rc) return rc;
+        if (p) {
+            if ((rc = h2d(ch, p, np_))) return rc;
+            launch_repack(ch, 0, 1, 0);
+        }
+        for (int c = 0; c < 3 && hh; ++c) {
+            if ((rc = h2d(ch, hh + c * n3, n3))) return rc;
             launch_repack(ch, 0, 2, c);
         }
     }
@@ -650,36 +726,38 @@ int c3d_download(c3d_channel *ch, double *u, double *p, double *hh, double *sgsv
     const size_t n3 = ch->stage_elems;
     const Geo &g = ch->g;
     const size_t np_ = (size_t)(g.n1m + 1) * g.n2 * (g.n3m + 1);
-    // Mapped host arrays are written by the repack kernels directly.
-    double *mu = host_mapped(u, 3 * n3 * 8), *mp = host_mapped(p, np_ * 8), *mh = host_mapped(hh, 3 * n3 * 8);
-    double *ms = host_mapped(sgsvis, n3 * 8);
-    for (int c = 0; c < 3; ++c) {
-        if (u && mu) launch_repack(ch, 1, 0, c, mu + c * n3);
-        else if (u) {
+    const bool pinned = (!u || host_pinned(u, 3 * n3 * 8)) && (!p || host_pinned(p, np_ * 8)) &&
+                        (!hh || host_pinned(hh, 3 * n3 * 8)) && (!sgsvis || host_pinned(sgsvis, n3 * 8));
+    int rc = 0;
+    Xfer x;
+    if (pinned && (rc = xfer_area(ch, &x)) == 0 && (rc = xfer_streams(ch)) == 0) {
+        // every field packed on the channel's stream and sent by DMA as soon as it is packed
+        for (int c = 0; c < 3 && u; ++c)
+            if ((rc = dn_field(ch, ch->stream, ch->xev[c], x.u(c), u + c * n3, n3, 0, c))) return rc;
+        if (p && (rc = dn_field(ch, ch->stream, ch->xev[3], x.p(), p, np_, 1, 0))) return rc;
+        for (int c = 0; c < 3 && hh; ++c)
+            if ((rc = dn_field(ch, ch->stream, ch->xev[4 + c], x.hh(c), hh + c * n3, n3, 2, c))) return rc;
+        if (sgsvis && (rc = dn_field(ch, ch->stream, ch->xev[7], x.sgs(), sgsvis, n3, 3, 0))) return rc;
+        CK(cudaStreamSynchronize(ch->cs));
+    } else if (rc && rc != C3D_ENOMEM) {
+        return rc;
+    } else {
+        for (int c = 0; c < 3 && u; ++c) {
             launch_repack(ch, 1, 0, c);
-            int rc = d2h(ch, u + c * n3, n3);
-            if (rc) return rc;
+            if ((rc = d2h(ch, u + c * n3, n3))) return rc;
         }
-    }
-    if (p && mp) launch_repack(ch, 1, 1, 0, mp);
-    else if (p) {
-        launch_repack(ch, 1, 1, 0);
-        int rc = d2h(ch, p, np_);
-        if (rc) return rc;
-    }
-    for (int c = 0; c < 3; ++c) {
-        if (hh && mh) launch_repack(ch, 1, 2, c, mh + c * n3);
-        else if (hh) {
+        if (p) {
+            launch_repack(ch, 1, 1, 0);
+            if ((rc = d2h(ch, p, np_))) return rc;
+        }
+        for (int c = 0; c < 3 && hh; ++c) {
             launch_repack(ch, 1, 2, c);
-            int rc = d2h(ch, hh + c * n3, n3);
-            if (rc) return rc;
+            if ((rc = d2h(ch, hh + c * n3, n3))) return rc;
         }
-    }
-    if (sgsvis && ms) launch_repack(ch, 1, 3, 0, ms);
-    else if (sgsvis) {
-        launch_repack(ch, 1, 3, 0);
-        int rc = d2h(ch, sgsvis, n3);
-        if (rc) return rc;
+        if (sgsvis) {
+            launch_repack(ch, 1, 3, 0);
+            if ((rc = d2h(ch, sgsvis, n3))) return rc;
+        }
     }
     CK(cudaStreamSynchronize(ch->stream));
     CK(cudaGetLastError());
@@ -922,9 +1000,73 @@ int c3d_diagnose(c3d_channel *ch, c3d_diag *out) {
     return out->nonfinite ? C3D_ENONFINITE : 0;
 }
 
+// c3d_getup with every array mapped: the transfers of HH overlap the step.  The main
+// stream unpacks U and P and runs the step; a side stream unpacks HH_old, which the step
+// waits for before xB (its first reader), and packs the new HH back once xB (its last
+// writer) is done, while the step continues; U, P and SGSVIS are packed after the step.
+// c3d_getup with every array pinned: the transfers of HH overlap the step.  The host link
+// is the bottleneck (2 x 2.15 GB per step on channel384), so the DMA copies run back to
+// back: U and P first on the channel's stream (unpacked, then the step starts), HH_old
+// next on a side stream (unpacked there; the step waits for it before xB, its first
+// reader), and the new HH back to the host on the side stream as soon as xB (its last
+// writer) is done, while the step continues; U, P and SGSVIS follow after the step.
+static int getup_overlapped(c3d_channel *ch, const double *u, double *uo, const double *p, double *po,
+                            const double *hh, double *hho, double *sgs, double dt, double *presg, double *presg3) {
+    int rc;
+    Xfer x;
+    if ((rc = xfer_area(ch, &x)) || (rc = xfer_streams(ch))) return rc;
+    const size_t n3 = x.n3;
+    CK(cudaEventRecord(ch->xev[15], ch->stream));   // after earlier work on the slots
+    CK(cudaStreamWaitEvent(ch->cs, ch->xev[15], 0));
+    for (int c = 0; c < 3; ++c)
+        if ((rc = up_field(ch, ch->stream, ch->xev[c], x.u(c), u + c * n3, n3, 0, c))) return rc;
+    if ((rc = up_field(ch, ch->stream, ch->xev[3], x.p(), p, x.np, 1, 0))) return rc;
+    for (int c = 0; c < 3; ++c)   // HH_old to the buffer the step reads as HH_old (the current one)
+        if ((rc = up_field(ch, ch->side, ch->xev[4 + c], x.hh(c), hh + c * n3, n3, 2, c))) return rc;
+    CK(cudaEventRecord(ch->hh_in, ch->side));
+    ch->have_state = 1;
+    ch->hh_hooks = true;
+    rc = step_common(ch, dt, presg, presg3, false);
+    ch->hh_hooks = false;
+    if (rc) return rc;
+    CK(cudaStreamWaitEvent(ch->side, ch->hh_out, 0));   // recorded by the step after xB
+    for (int c = 0; c < 3; ++c)
+        if ((rc = dn_field(ch, ch->side, ch->xev[8 + c], x.hh(c), hho + c * n3, n3, 2, c))) return rc;
+    for (int c = 0; c < 3; ++c)
+        if ((rc = dn_field(ch, ch->stream, ch->xev[11 + c], x.u(c), uo + c * n3, n3, 0, c))) return rc;
+    if ((rc = dn_field(ch, ch->stream, ch->xev[14], x.p(), po, x.np, 1, 0))) return rc;
+    if (sgs && (rc = dn_field(ch, ch->stream, ch->xev[7], x.sgs(), sgs, n3, 3, 0))) return rc;
+    double sc[SCAL_COUNT];
+    CK(cudaMemcpyAsync(sc, ch->scal, sizeof(sc), cudaMemcpyDeviceToHost, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    CK(cudaStreamSynchronize(ch->side));
+    CK(cudaStreamSynchronize(ch->cs));
+    CK(cudaGetLastError());
+    float ms_ = 0.f;
+    cudaEventElapsedTime(&ms_, ch->ev0, ch->ev1);
+    ch->last_ms = ms_;
+    *presg = sc[SCAL_PRESG];
+    *presg3 = sc[SCAL_PRESG3];
+    return check_wall_flag(ch, sc);
+}
+
 int c3d_getup(c3d_channel *ch, double *u, double *p, double *hh, double *sgsvis, int ntime, double dt,
               double *presg, double *presg3) {
     if (!ch || !u || !p || !hh) { set_error("null argument"); return C3D_EINVAL; }
+    if (!presg || !presg3) { set_error("null PRESG/PRESG3"); return C3D_EINVAL; }
+    {
+        cudaSetDevice(ch->device);
+        const size_t n3 = ch->stage_elems;
+        const Geo &g = ch->g;
+        const size_t np_ = (size_t)(g.n1m + 1) * g.n2 * (g.n3m + 1);
+        double *sg = ch->files != 0 ? sgsvis : nullptr;
+        if (host_pinned(u, 3 * n3 * 8) && host_pinned(p, np_ * 8) && host_pinned(hh, 3 * n3 * 8) &&
+            (!sg || host_pinned(sg, n3 * 8)) && !ch->prof_on) {
+            (void)ntime;
+            if (!(dt > 0) || !isfinite(dt)) { set_error("dt must be positive and finite"); return C3D_EINVAL; }
+            return getup_overlapped(ch, u, u, p, p, hh, hh, sg, dt, presg, presg3);
+        }
+    }
     int rc = c3d_upload(ch, u, p, hh, sgsvis);
     if (rc) return rc;
     rc = c3d_step(ch, ntime, dt, presg, presg3);
@@ -942,12 +1084,9 @@ int c3d_op_set(c3d_channel *ch, const double *f) {
             CK(cudaMemset(ch->opbuf[q], 0, nf * rs));
         }
     }
-    if (double *mf = host_mapped(f, ch->stage_elems * 8)) launch_repack(ch, 0, 4, 0, mf);
-    else {
-        int rc = h2d(ch, f, ch->stage_elems);
-        if (rc) return rc;
-        launch_repack(ch, 0, 4, 0);
-    }
+    int rc = h2d(ch, f, ch->stage_elems);
+    if (rc) return rc;
+    launch_repack(ch, 0, 4, 0);
     CK(cudaStreamSynchronize(ch->stream));
     CK(cudaGetLastError());
     return 0;
@@ -972,14 +1111,9 @@ int c3d_op_get(c3d_channel *ch, double *f) {
     if (!ch || !f) { set_error("null argument"); return C3D_EINVAL; }
     if (!ch->opbuf[1]) { set_error("no operator result"); return C3D_ESTATE; }
     cudaSetDevice(ch->device);
-    if (double *mf = host_mapped(f, ch->stage_elems * 8)) {
-        launch_repack(ch, 1, 5, 0, mf);
-        CK(cudaStreamSynchronize(ch->stream));
-    } else {
-        launch_repack(ch, 1, 5, 0);
-        int rc = d2h(ch, f, ch->stage_elems);
-        if (rc) return rc;
-    }
+    launch_repack(ch, 1, 5, 0);
+    int rc = d2h(ch, f, ch->stage_elems);
+    if (rc) return rc;
     CK(cudaGetLastError());
     return 0;
 }

@@ -151,6 +151,14 @@ struct c3d_channel {
     int device;
     cudaStream_t stream;
     cudaEvent_t ev0, ev1;
+    // overlapped host transfers of c3d_getup: a side stream and the events the step waits
+    // for before xB (HH of the previous step uploaded) and records after it (new HH final)
+    cudaStream_t side = nullptr;
+    cudaEvent_t hh_in = nullptr, hh_out = nullptr;
+    bool hh_hooks = false;
+    double *xfer = nullptr;   // DMA staging area of pinned host arrays (one slot per field)
+    cudaStream_t cs = nullptr;          // copy stream of the DMA transfers
+    cudaEvent_t xev[16] = {};           // per-field hand-offs between the copy and compute streams
     // state (double or float2 by precision), scalars and metrics
     void *u, *v, *w, *p, *dp;
     double *scal, *part;
@@ -230,7 +238,7 @@ int launch_diag(c3d_channel *ch, int *launches);
 int launch_poisson_tables(c3d_channel *ch);
 // what: 0 U component, 1 P, 2 HH component, 3 SGSVIS (to host), 4 operand (to device),
 // 5 operator result (to host)
-// fort: the Fortran-layout array (device staging buffer by default, or a mapped host array)
+// fort: the Fortran-layout array on the device (the one-field staging buffer by default)
 int launch_repack(c3d_channel *ch, int dir, int what, int comp, double *fort = nullptr);  // dir 0: Fortran->device
 void set_error(const std::string &msg);
 // Records a kernel-boundary mark for the profiler and counts the launch.

@@ -19,6 +19,15 @@
 #include <vector>
 #include "c3d_kern.cuh"
 
+#define CK_RC(call)                                                                     \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));             \
+            return C3D_ECUDA;                                                           \
+        }                                                                               \
+    } while (0)
+
 namespace c3d {
 
 int launch_ptables(c3d_channel *ch, const double *ak1, const double *ak3, const double *pm, const double *pc,
@@ -228,41 +237,58 @@ __global__ void k_diag_sums(Geo g, const typename SType<R>::S *u, const typename
 // Fortran <-> device repacking.  what: 0 = velocity component of U(0:N1,0:N2,0:N3,3)
 // (device planes 0..N2), 1 = P(N1,N2,N3) (planes 1..N2M), 2 = HH component (planes 1..N2M).
 // ---------------------------------------------------------------------------------
+// Grid-stride loops with 32-bit indices (every Fortran array has fewer than 2^31
+// elements), four elements per thread and pass with their loads issued first.
 template <typename T, typename Conv>
-__global__ void k_unpack(Geo g, int what, T *dev, const double *fort, Conv cv) {
+__global__ void k_unpack(Geo g, int what, T *__restrict__ dev, const double *__restrict__ fort, Conv cv) {
     const int j0 = (what == 0) ? 0 : 1, j1 = (what == 0) ? g.n2 : g.n2m;
-    const long long tot = (long long)(j1 - j0 + 1) * g.np;
-    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= tot) return;
-    const int i = (int)(id % g.n1m);
-    const int k = (int)((id / g.n1m) % g.n3m);
-    const int j = j0 + (int)(id / g.np);
-    const long long N1 = g.n1m + 1, N2 = g.n2;
-    long long f;
-    if (what == 1) f = i + N1 * ((j - 1) + N2 * (long long)k);
-    else f = (i + 1) + (N1 + 1) * (j + (N2 + 1) * (long long)(k + 1));
-    dev[fidx(g, i, j, k)] = cv(fort[f]);
+    const unsigned tot = (unsigned)(j1 - j0 + 1) * (unsigned)g.np;
+    const unsigned n1 = g.n1m, n3 = g.n3m, N1 = g.n1m + 1, N2 = g.n2;
+    const unsigned st = gridDim.x * blockDim.x;
+    for (unsigned b = blockIdx.x * blockDim.x + threadIdx.x; b < tot; b += 4 * st) {
+        double v[4];
+        unsigned dst[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const unsigned id = b + u * st;
+            if (id < tot) {
+                const unsigned q = id / n1, i = id - q * n1, jj = q / n3, k = q - jj * n3, j = j0 + jj;
+                const unsigned f = (what == 1) ? i + N1 * ((j - 1) + N2 * k) : (i + 1) + (N1 + 1) * (j + (N2 + 1) * (k + 1));
+                v[u] = fort[f];
+                dst[u] = (j * n3 + k) * n1 + i;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (b + u * st < tot) dev[dst[u]] = cv(v[u]);
+    }
 }
 
 // Periodic ghost cells (I=0, I=N1, K=0, K=N3) receive the periodic copies; entries
 // outside the device planes receive 0.
 template <typename T, typename Conv>
-__global__ void k_pack(Geo g, int what, const T *dev, double *fort, Conv cv) {
-    const long long N1 = g.n1m + 1, N2 = g.n2, N3 = g.n3m + 1;
-    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long I, J, K;
-    if (what == 1) {
-        if (id >= N1 * N2 * N3) return;
-        I = 1 + id % N1; J = 1 + (id / N1) % N2; K = 1 + id / (N1 * N2);
-    } else {
-        if (id >= (N1 + 1) * (N2 + 1) * (N3 + 1)) return;
-        I = id % (N1 + 1); J = (id / (N1 + 1)) % (N2 + 1); K = id / ((N1 + 1) * (N2 + 1));
-    }
-    int i = (int)((I + g.n1m - 1) % g.n1m), k = (int)((K + g.n3m - 1) % g.n3m);
+__global__ void k_pack(Geo g, int what, const T *__restrict__ dev, double *__restrict__ fort, Conv cv) {
+    const unsigned N1 = g.n1m + 1, N2 = g.n2, N3 = g.n3m + 1;
+    const unsigned A1 = (what == 1) ? N1 : N1 + 1, A2 = (what == 1) ? N2 : N2 + 1, A3 = (what == 1) ? N3 : N3 + 1;
+    const unsigned tot = A1 * A2 * A3, o = (what == 1) ? 1 : 0;
     const int j0 = (what == 0) ? 0 : 1, j1 = (what == 0) ? g.n2 : g.n2m;
-    double v = 0.0;
-    if (J >= j0 && J <= j1) v = cv(dev[fidx(g, i, (int)J, k)]);
-    fort[id] = v;
+    const unsigned st = gridDim.x * blockDim.x;
+    for (unsigned b = blockIdx.x * blockDim.x + threadIdx.x; b < tot; b += 4 * st) {
+        double v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const unsigned id = b + u * st;
+            v[u] = 0.0;
+            if (id < tot) {
+                const unsigned q = id / A1, I = id - q * A1 + o, K = q / A2 + o, J = q - (q / A2) * A2 + o;
+                const int i = (int)((I + g.n1m - 1) % g.n1m), k = (int)((K + g.n3m - 1) % g.n3m);
+                if ((int)J >= j0 && (int)J <= j1) v[u] = cv(dev[fidx(g, i, (int)J, k)]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (b + u * st < tot) fort[b + u * st] = v[u];
+    }
 }
 
 struct ToF64 { __device__ double operator()(double x) const { return x; } };
@@ -429,7 +455,11 @@ static int step_impl(c3d_channel *ch, double dt, int *nl) {
     if ((rc = launch_zpass<R>(ch, a, 0, nullptr, nullptr, nullptr, 0, nl))) return rc;   // zA
     if ((rc = launch_zpass<R>(ch, a, 1, nullptr, nullptr, nullptr, 0, nl))) return rc;   // zB
     if (ch->files != 0 && (rc = launch_les<R>(ch, a, l, 1, nl))) return rc;   // SGS fluxes into HH
+    // xB is the first reader of HH_old and the last writer of the new HH: the overlapped
+    // transfers of c3d_getup upload the one and download the other around it
+    if (ch->hh_hooks) CK_RC(cudaStreamWaitEvent(ch->stream, ch->hh_in, 0));
     if ((rc = launch_xpass<R>(ch, a, 1, nullptr, nullptr, nl))) return rc;    // xB
+    if (ch->hh_hooks) CK_RC(cudaEventRecord(ch->hh_out, ch->stream));
     k_ycn<R><<<nblk(3LL * ch->g.np), TPB, 0, ch->stream>>>(a, sizeof(R) == 8 ? (const R *)ch->ycn : (const R *)ch->ycn32);
     mark(ch, nl, "ycn", (double)ch->g.n1m * ch->g.n2m * ch->g.n3m * 6 * sizeof(R));
     // deltas go to exz/eyz/wsq, which the RHS passes no longer need
@@ -520,6 +550,10 @@ int launch_poisson_tables(c3d_channel *ch) {
 
 int launch_repack(c3d_channel *ch, int dir, int what, int comp, double *fort) {
     double *F = fort ? fort : ch->stage;
+    // the repacking kernels loop with four elements per thread and pass: a grid of 16
+    // blocks per SM keeps them all active (a full one-element-per-thread grid would
+    // evaluate the three idle slots of every thread)
+    auto cap = [](int b) { return b < 152 * 16 ? b : 152 * 16; };
     const Geo &g = ch->g;
     const int j0 = (what == 0 || what == 3) ? 0 : 1, j1 = (what == 0 || what == 3) ? g.n2 : g.n2m;
     const long long tot_dev = (long long)(j1 - j0 + 1) * g.np;
@@ -527,15 +561,15 @@ int launch_repack(c3d_channel *ch, int dir, int what, int comp, double *fort) {
     const long long tot_f = (what == 1) ? N1 * N2 * N3 : (N1 + 1) * (N2 + 1) * (N3 + 1);
     cudaStream_t st = ch->stream;
     const bool mixed = ch->precision == C3D_MIXED;
-    const int nb = nblk(dir == 0 ? tot_dev : tot_f);
+    const int nb = cap(nblk(dir == 0 ? tot_dev : tot_f));
     if (what == 4 || what == 5) {   // operator operand (to device) / result (to host), working precision
         void *buf = ch->opbuf[what == 4 ? 0 : 1];
         if (!buf || (what == 4) != (dir == 0)) return C3D_EINVAL;
         if (!mixed) {
-            if (dir == 0) k_unpack<double><<<nblk((long long)(g.n2 + 1) * g.np), TPB, 0, st>>>(g, 0, (double *)buf, F, ToF64());
+            if (dir == 0) k_unpack<double><<<cap(nblk((long long)(g.n2 + 1) * g.np)), TPB, 0, st>>>(g, 0, (double *)buf, F, ToF64());
             else k_pack<double><<<nb, TPB, 0, st>>>(g, 0, (const double *)buf, F, FromF64());
         } else {
-            if (dir == 0) k_unpack<float><<<nblk((long long)(g.n2 + 1) * g.np), TPB, 0, st>>>(g, 0, (float *)buf, F, ToF32());
+            if (dir == 0) k_unpack<float><<<cap(nblk((long long)(g.n2 + 1) * g.np)), TPB, 0, st>>>(g, 0, (float *)buf, F, ToF32());
             else k_pack<float><<<nb, TPB, 0, st>>>(g, 0, (const float *)buf, F, FromF32());
         }
         return 0;

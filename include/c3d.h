@@ -157,11 +157,12 @@ int c3d_getup(c3d_channel *ch, double *u, double *p, double *hh,
  * U taken as the intermediate velocity and DT = 1, no bulk-flow forcing).
  * Used to make a synthetic initial condition discretely divergence-free. */
 int c3d_project(c3d_channel *ch);
-/* Page-locks (pins) a host array and maps it into the device address space; a
- * driver calls it once per field array.  c3d_upload / c3d_download / c3d_getup /
- * c3d_op_set / c3d_op_get then read and write a registered array directly from
- * the repacking kernels (no staging copy); an unregistered array goes through a
- * device staging buffer one field at a time. */
+/* Page-locks (pins) a host array; a driver calls it once per field array.
+ * c3d_upload / c3d_download / c3d_getup then move registered arrays by DMA at the
+ * host link's rate through a device staging area with one slot per field (U, P, HH,
+ * SGSVIS: about 2.2 GB for 384x257x384, allocated on first use), and c3d_getup
+ * overlaps the transfers of HH with the step.  Unregistered arrays go through a
+ * one-field staging buffer, one field at a time. */
 int c3d_host_register(void *ptr, size_t bytes);
 int c3d_host_unregister(void *ptr);
 /* Blocks until all work queued on the channel's stream has finished. */

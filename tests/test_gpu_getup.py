@@ -1,0 +1,77 @@
+"""c3d_getup with host arrays registered (mapped, transfers of HH overlapping the step) and
+unregistered (staged copies around the step): the same kernels in the same order on the
+device, so the host arrays after each call are bitwise equal, and equal to c3d_upload +
+c3d_step + c3d_download; the LES form returns SGSVIS the same way."""
+import numpy as np
+import pytest
+
+from compact3d_gb300 import ic
+from compact3d_gb300.grid import C3D_FP64, C3D_MIXED, make_grid
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def libc3d():
+    from compact3d_gb300 import build, lib
+    build.build()
+    lib.load()
+    return lib
+
+
+def _run(lib, g, dt, U0, P0, HH0, register, steps=3, sgs=False):
+    U, P, HH = U0.copy(order="F"), P0.copy(order="F"), HH0.copy(order="F")
+    S = np.zeros(U.shape[:3], order="F") if sgs else None
+    arrs = [U, P, HH] + ([S] if sgs else [])
+    if register:
+        for a in arrs:
+            lib.host_register(a)
+    ch = lib.Channel(g, g.precision)
+    pg = pg3 = 0.0
+    try:
+        for m in range(1, steps + 1):
+            pg, pg3 = ch.getup(U, P, HH, m, dt, pg, pg3, sgsvis=S)
+    finally:
+        ch.close()
+        if register:
+            for a in arrs:
+                lib.host_unregister(a)
+    return U, P, HH, S, pg, pg3
+
+
+@pytest.mark.parametrize("prec", [C3D_FP64, C3D_MIXED])
+def test_getup_mapped_equals_staged(libc3d, prec):
+    g, dt = make_grid("small32", prec, n1m=64, n2m=32, n3m=64)
+    U0, P0, HH0 = ic.perturbed_laminar(g)
+    a = _run(libc3d, g, dt, U0, P0, HH0, True)
+    b = _run(libc3d, g, dt, U0, P0, HH0, False)
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x, y)
+    assert a[4] == b[4] and a[5] == b[5]
+
+
+def test_getup_mapped_equals_step_path(libc3d):
+    # FP64: the host arrays carry the state exactly, so re-uploading it every step changes
+    # nothing (a double-float state may come back as another pair for the same value)
+    g, dt = make_grid("small32", C3D_FP64, n1m=64, n2m=32, n3m=64)
+    U0, P0, HH0 = ic.perturbed_laminar(g)
+    a = _run(libc3d, g, dt, U0, P0, HH0, True, steps=2)
+    ch = libc3d.Channel(g, C3D_FP64)
+    ch.upload(U0, P0, HH0)
+    pg = pg3 = 0.0
+    for m in (1, 2):
+        pg, pg3 = ch.step(m, dt, pg, pg3)
+    U, P, HH = ch.download()
+    ch.close()
+    for x, y in zip(a[:3], (U, P, HH)):
+        assert np.array_equal(x, y)
+
+
+def test_getup_mapped_les_sgsvis(libc3d):
+    g, dt = make_grid("les32cs")
+    U0, P0, HH0 = ic.loglaw(g, 395.0, 0.05, 7)
+    a = _run(libc3d, g, dt, U0, P0, HH0, True, steps=2, sgs=True)
+    b = _run(libc3d, g, dt, U0, P0, HH0, False, steps=2, sgs=True)
+    for x, y in zip(a[:4], b[:4]):
+        assert np.array_equal(x, y)
+    assert np.abs(a[3]).max() > 0.0
