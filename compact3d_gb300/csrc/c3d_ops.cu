@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(TPB) k_op_y(StepArgs<R> a, int op, const R *in
     const int j = 1 + (int)blockIdx.y;
     const long long o = (long long)j * g.np + e;
     if (op == C3D_OP_DY1) {
-        out[o] = j >= 2 ? (in[o] - in[o - g.np]) / a.m.h[j] : R(0);
+        out[o] = j >= 2 ? (in[o] - in[o - g.np]) * a.m.rh[j] : R(0);
     } else {
         out[o] = (a.m.hp[j] * in[o + g.np] - a.m.hc[j] * in[o]) + a.m.hm[j] * in[o - g.np];
     }
