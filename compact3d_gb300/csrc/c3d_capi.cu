@@ -194,6 +194,7 @@ void free_channel(c3d_channel *ch) {
     for (cudaEvent_t e : ch->xev)
         if (e) cudaEventDestroy(e);
     if (ch->xfer) cudaFree(ch->xfer);
+    if (ch->wtaue) cudaFree(ch->wtaue);
     if (ch->hh_in) cudaEventDestroy(ch->hh_in);
     if (ch->hh_out) cudaEventDestroy(ch->hh_out);
     if (ch->ev0) cudaEventDestroy(ch->ev0);
@@ -318,8 +319,12 @@ int check_grid(const c3d_grid *g) {
         set_error("FILES must be 0 (DNS), 1 (SGSDY) or 2 (SGSCS); the scale-dependent model (3) is not built");
         return C3D_EINVAL;
     }
-    if (g->wmodel < 0 || g->wmodel > 1) {
-        set_error("WMODEL must be 0 or 1 (WALLMODEL_INSTANT); the other wall models are not built");
+    if (!(g->wmodel == 0 || g->wmodel == 1 || g->wmodel == 4)) {
+        set_error("WMODEL must be 0, 1 (WALLMODEL_INSTANT) or 4 (WALLMODEL_WERNER); the other wall models are not built");
+        return C3D_EINVAL;
+    }
+    if (g->wmodel == 4 && n3m > n1m) {
+        set_error("WMODEL 4 (WALLMODEL_WERNER) takes the x neighbour with the z index, so it needs N3-1 <= N1-1");
         return C3D_EINVAL;
     }
     if (g->wmodel == 1 && g->y[0] != 0.0) {
@@ -441,6 +446,7 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
         if (dalloc(&ch->smagc, (size_t)g.n2 + 1) || dalloc(&ch->d23, (size_t)g.n2 + 1) ||
             dalloc(&ch->ycs, (size_t)g.n2 + 1) || dalloc(&ch->wpart, 2 * (size_t)nbw))
             return fail(C3D_ENOMEM);
+        if (gr->wmodel == 4 && dalloc(&ch->wtaue, 4 * (size_t)g.np)) return fail(C3D_ENOMEM);
         if (cudaMalloc(&ch->coef, ((size_t)g.n2 + 1) * rs) != cudaSuccess ||
             cudaMalloc(&ch->d23r, ((size_t)g.n2 + 1) * rs) != cudaSuccess)
             return fail(C3D_ENOMEM);

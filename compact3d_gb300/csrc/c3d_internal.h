@@ -157,6 +157,7 @@ struct c3d_channel {
     cudaEvent_t hh_in = nullptr, hh_out = nullptr;
     bool hh_hooks = false;
     double *xfer = nullptr;   // DMA staging area of pinned host arrays (one slot per field)
+    double *wtaue = nullptr;  // WALLMODEL_WERNER: TAUWE(I,K,1..4) at the cell centres (4 x N1M N3M)
     cudaStream_t cs = nullptr;          // copy stream of the DMA transfers
     cudaEvent_t xev[16] = {};           // per-field hand-offs between the copy and compute streams
     // state (double or float2 by precision), scalars and metrics

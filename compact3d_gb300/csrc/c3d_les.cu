@@ -343,6 +343,72 @@ __global__ void __launch_bounds__(TPB) k_wall(StepArgs<R> a, LesArgs<R> l) {
     }
 }
 
+// WALLMODEL_WERNER (compact3d.f:4815-4958), FP64: the Werner-Wengle power law at the first
+// cell centre of both walls into tw4 (TAUWE(I,K,1..4), four planes of N1M x N3M), with
+// per-block sums of the bottom u-stress for WSM(1); the reference's x neighbour taken with
+// the z index (IPA(K), F:4852) is kept.  VCASE uses WSM(1) of the step before.
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_wall_werner(StepArgs<R> a, LesArgs<R> l, double *tw4) {
+    typedef St<R> ST;
+    const Geo g = a.g;
+    __shared__ double ssum[TPB];
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double t1 = 0.0;
+    if (e < g.np) {
+        const int i = e % g.n1m, k = e / g.n1m;
+        const int ik = (k + 1) % g.n1m;            // IPA(K) - 1 (0-based), N3M <= N1M
+        const int kp = (k + 1) % g.n3m;
+        const double B = 0.1428571429, AB1 = 7.202125274, AB3 = 69.74057973, AB4 = 0.1376936317, AB5 = 1.75;
+        const double VCASE = AB3 * (sqrt(fabs(a.scal[SCAL_WSMC])) / 11.81);
+        for (int wall = 0; wall < 2; ++wall) {
+            const int jw = wall == 0 ? 1 : g.n2m;
+            const double DELTAP = g.dy[jw];
+            const double U1 = 0.5 * (ST::dbl(a.u[fidx(g, i, jw, k)]) + ST::dbl(a.u[fidx(g, ik, jw, k)]));
+            const double U2 = 0.5 * (ST::dbl(a.w[fidx(g, i, jw, k)]) + ST::dbl(a.w[fidx(g, i, jw, kp)]));
+            const double VELOCP = sqrt(U1 * U1 + U2 * U2);
+            double TAUW1;
+            if (VELOCP <= VCASE) {
+                TAUW1 = 2. * VELOCP / DELTAP / g.re;
+            } else {
+                TAUW1 = AB1 * pow(1.0 / DELTAP / g.re, 1. + B);
+                TAUW1 = TAUW1 + AB4 * pow(1.0 / DELTAP / g.re, B) * VELOCP;
+                TAUW1 = pow(TAUW1, AB5);
+            }
+            tw4[(2 * wall) * g.np + e] = TAUW1 * (U1 / VELOCP);
+            tw4[(2 * wall + 1) * g.np + e] = TAUW1 * (U2 / VELOCP);
+            if (wall == 0) t1 = TAUW1 * (U1 / VELOCP);
+        }
+    }
+    ssum[threadIdx.x] = t1;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) ssum[threadIdx.x] += ssum[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        l.wpart[blockIdx.x] = ssum[0];
+        l.wpart[gridDim.x + blockIdx.x] = 0.0;
+    }
+}
+
+// WERNER's averaging to the stress points: TAUW = (TAUWE(I) + TAUWE(IMA(K))) / 2 (the x
+// neighbour with the z index again, F:4924), TAUB = (TAUWE(K) + TAUWE(K-1)) / 2, both walls.
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_wall_werner_avg(StepArgs<R> a, LesArgs<R> l, const double *tw4) {
+    const Geo g = a.g;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= g.np) return;
+    const int i = e % g.n1m, k = e / g.n1m;
+    const int im = (k + g.n1m - 1) % g.n1m;       // IMA(K) - 1
+    const int km = (k + g.n3m - 1) % g.n3m;
+    const int ei = k * g.n1m + im, ek = km * g.n1m + i;
+    for (int wall = 0; wall < 2; ++wall) {
+        const double *tu = tw4 + (2 * wall) * g.np, *tw = tw4 + (2 * wall + 1) * g.np;
+        l.tauw[wall * g.np + e] = 0.5 * (tu[e] + tu[ei]);
+        l.taub[wall * g.np + e] = 0.5 * (tw[e] + tw[ek]);
+    }
+}
+
 template <typename R>
 __global__ void k_wall_sum(StepArgs<R> a, LesArgs<R> l, int nb) {
     __shared__ double s[256], b[256];
@@ -364,6 +430,10 @@ __global__ void k_wall_sum(StepArgs<R> a, LesArgs<R> l, int nb) {
     if (threadIdx.x == 0) {
         a.scal[SCAL_WSMC] = s[0] / (double)a.g.np;
         a.scal[SCAL_WALLERR] = b[0] > 0.0 ? 1.0 : 0.0;
+        if (l.wmodel == 4) {   // WERNER zeroes WSM(2), WSM(3) (compact3d.f:4938-4940)
+            a.scal[SCAL_WSMC + 1] = 0.0;
+            a.scal[SCAL_WSMC + 2] = 0.0;
+        }
     }
 }
 
@@ -729,6 +799,13 @@ int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *n
             k_wall<R><<<nb, TPB, 0, st>>>(a, l);
             k_wall_sum<R><<<1, 256, 0, st>>>(a, l, nb);
             mark(ch, nl, "wall", 32.0 * g.np);
+        } else if (ch->files != 0 && ch->wmodel == 4) {
+            const int nb = nblk(g.np);
+            k_wall_werner<R><<<nb, TPB, 0, st>>>(a, l, ch->wtaue);
+            k_wall_sum<R><<<1, 256, 0, st>>>(a, l, nb);
+            k_wall_werner_avg<R><<<nb, TPB, 0, st>>>(a, l, ch->wtaue);
+            *nl += 2;
+            mark(ch, nl, "wall", 96.0 * g.np);
         }
         return 0;
     }

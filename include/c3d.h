@@ -62,9 +62,11 @@ extern "C" {
  *   /MESH4/ DYM,DYC,DYP(1:N2)              -> dym,dyc,dyp (n2 values, index J-1)
  *   /PARA/  RE                             -> re
  *   /FINOUT/ FILES (SGS model)             -> files  (0 none, 1 SGSDY, 2 SGSCS)
- *   /WALLMODEL/ WMODEL                     -> wmodel (0 none, 1 WALLMODEL_INSTANT;
- *                                             Y(0) must be 0: Y0 != 0 selects the
- *                                             rough-wall model, which is not built)
+ *   /WALLMODEL/ WMODEL                     -> wmodel (0 none, 1 WALLMODEL_INSTANT,
+ *                                             4 WALLMODEL_WERNER; with 1, Y(0) must
+ *                                             be 0: Y0 != 0 selects the rough-wall
+ *                                             model, which is not built; 4 needs
+ *                                             N3 <= N1, see below)
  * The library takes the driver's metric arrays as given; it recomputes only
  * the Poisson metrics of INIWAVE / METRICPOISSON (compact3d.f:9182-9263),
  * which depend on nothing else.
@@ -119,14 +121,19 @@ int c3d_set_device(int device);
  *               upload, step, download in one call.
  *
  * LES (files != 0, compact3d.f:931-937): each step zeroes SGSVIS and runs the SGS
- * model (SGSDY or SGSCS) and, with wmodel = 1, WALLMODEL_INSTANT before BCOND; the
+ * model (SGSDY or SGSCS) and, with wmodel = 1 or 4, WALLMODEL_INSTANT or
+ * WALLMODEL_WERNER before BCOND; the
  * SGS fluxes and the wall-stress terms enter RHS1-3.  SGSVIS passed to c3d_upload
  * is not used (the step recomputes it); c3d_download / c3d_getup return it.  With
  * wmodel = 0 the step first evaluates WALLSS on the current field, which is what the
  * driver's time loop does right before GETUP (compact3d.f:125), so SGSCS sees the
  * same WSM.  A wall point whose Newton iteration for u_tau exceeds the iteration cap
  * (default 10000; the reference iterates without one) makes c3d_step / c3d_sync
- * return C3D_ENOTCONV after the step completes.
+ * return C3D_ENOTCONV after the step completes.  WALLMODEL_WERNER (compact3d.f:
+ * 4815-4958) sets both walls' stresses from the Werner-Wengle power law and WSM(1)
+ * from the bottom wall; like the reference it takes the x neighbour of a wall point
+ * with the z index (IPA(K), IMA(K)), which the reference's index arrays allow only for
+ * N3 <= N1, so c3d_create refuses wmodel = 4 on other grids.
  * c3d_upload_wall / c3d_download_wall  TAUW, TAUB (0:M1,0:M3,2) of /TAUXYZ/ (the
  *               interior I = 1..N1M, K = 1..N3M of both walls; either may be NULL).
  *               The wall model updates the bottom wall (index 1); the top wall keeps

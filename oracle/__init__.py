@@ -173,7 +173,8 @@ class Oracle:
         return X
 
     def wallmodel(self, U):
-        """WALLMODEL_INSTANT on U; returns the status (0, or -4 if a point hit the cap)."""
+        """The grid's wall model (WMODEL 1: WALLMODEL_INSTANT, 4: WALLMODEL_WERNER) on U;
+        returns the status (0, or -4 if an INSTANT point hit the iteration cap)."""
         return lib().orc_wallmodel(self.h, _p(U))
 
     def set_wall(self, tauw=None, taub=None, ifwall=0):

@@ -1596,6 +1596,68 @@ int wallmodel_instant(Orc &g, const double *U) {
     return bad ? C3D_ENOTCONV : 0;
 }
 
+// WALLMODEL_WERNER (compact3d.f:4815-4958): Werner-Wengle power law at the first cell
+// centre of both walls, TAUWE(I,K,1..4) at the cell centres, then averaged to the stress
+// points; WSM(1) = plane mean of the bottom u-stress.  The reference takes the x neighbour
+// with the z loop variable (IP = IPA(J) and IP = IMA(J), J the z index; F:4852, 4881, 4924),
+// which this restatement keeps; the INDX arrays have N1M entries, so it needs N3M <= N1M.
+int wallmodel_werner(Orc &g, const double *U) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double B = 0.1428571429, AB1 = 7.202125274, AB3 = 69.74057973, AB4 = 0.1376936317, AB5 = 1.75;
+    const double RE = g.RE;
+    auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+    std::vector<double> TAUWE((size_t)(N1M + 1) * (N3M + 1) * 4, 0.0);
+    auto te = [&](int i, int k, int q) -> double & { return TAUWE[((size_t)q * (N3M + 1) + k) * (N1M + 1) + i]; };
+    const double TEMP = std::sqrt(std::fabs(g.WSM[0])) / 11.81;   // WSM(1) of the step before
+    const double VCASE = AB3 * TEMP;
+    for (int wall = 0; wall < 2; ++wall) {
+        const int JW = wall == 0 ? 1 : N2M;
+        const double DELTAP = g.DY[JW];
+        for (int J = 1; J <= N3M; J++) {
+            const int KP = g.KPA[J];
+            for (int I = 1; I <= N1M; I++) {
+                const int IP = g.IPA[J];
+                const double U1 = 0.5 * (u(I, JW, J, 1) + u(IP, JW, J, 1));
+                const double U2 = 0.5 * (u(I, JW, J, 3) + u(I, JW, KP, 3));
+                const double VELOCP = std::sqrt(U1 * U1 + U2 * U2);
+                double TAUW1;
+                if (VELOCP <= VCASE) {
+                    TAUW1 = 2. * VELOCP / DELTAP / RE;
+                } else {
+                    TAUW1 = AB1 * std::pow(1.0 / DELTAP / RE, 1. + B);
+                    TAUW1 = TAUW1 + AB4 * std::pow(1.0 / DELTAP / RE, B) * VELOCP;
+                    TAUW1 = std::pow(TAUW1, AB5);
+                }
+                te(I, J, 2 * wall) = TAUW1 * (U1 / VELOCP);
+                te(I, J, 2 * wall + 1) = TAUW1 * (U2 / VELOCP);
+            }
+        }
+    }
+    for (int J = 1; J <= N3M; J++) {
+        const int KP = g.KMA[J];
+        for (int I = 1; I <= N1M; I++) {
+            const int IP = g.IMA[J];
+            g.TAUW[g.itw(I, J, 1)] = 0.5 * (te(I, J, 0) + te(IP, J, 0));
+            g.TAUB[g.itw(I, J, 1)] = 0.5 * (te(I, J, 1) + te(I, KP, 1));
+            g.TAUW[g.itw(I, J, 2)] = 0.5 * (te(I, J, 2) + te(IP, J, 2));
+            g.TAUB[g.itw(I, J, 2)] = 0.5 * (te(I, J, 3) + te(I, KP, 3));
+        }
+    }
+    double w1 = 0.0;
+    for (int J = 1; J <= N3M; J++)
+        for (int I = 1; I <= N1M; I++) w1 = w1 + te(I, J, 0);
+    g.WSM[0] = w1 / (double)(N1M * N3M);
+    g.WSM[1] = 0.0;
+    g.WSM[2] = 0.0;
+    g.TAOW = g.WSM[0];
+    return 0;
+}
+
+// The wall model WALL_MODEL dispatches to (compact3d.f:1982-2011) for WMODEL = 1 or 4.
+int wallmodel(Orc &g, const double *U) {
+    return g.WMODEL == 4 ? wallmodel_werner(g, U) : wallmodel_instant(g, U);
+}
+
 // ----------------------------------------------------------------------------------
 // GETUH1/2/3 (compact3d.f:8218-8627): Crank-Nicolson delta form, approximate
 // factorisation y -> x -> z (u, v) and y -> z -> x (w), then UH = U + delta.
@@ -2108,7 +2170,7 @@ int orc_operator(void *h, int op, const double *F, double *X) {
 }
 
 // WALLMODEL_INSTANT alone on U (TAUW, TAUB, WSM(1) are updated in the handle).
-int orc_wallmodel(void *h, const double *U) { return wallmodel_instant(*(Orc *)h, U); }
+int orc_wallmodel(void *h, const double *U) { return wallmodel(*(Orc *)h, U); }
 
 // GETUP (compact3d.f:879-960).  U, P, HH, SGSVIS are Fortran arrays (SGSVIS may be null;
 // an internal array is used then).  With an SGS model (FILES != 0) the driver's WALLSS
@@ -2118,7 +2180,8 @@ int orc_getup(void *h, double *U, double *P, double *HH, double *SGSVIS, int NTI
               double *PRESG, double *PRESG3) {
     Orc &g = *(Orc *)h;
     (void)NTIME;
-    if (g.FILES < 0 || g.FILES > 2 || g.WMODEL < 0 || g.WMODEL > 1) return C3D_EINVAL;
+    if (g.FILES < 0 || g.FILES > 2 || !(g.WMODEL == 0 || g.WMODEL == 1 || g.WMODEL == 4)) return C3D_EINVAL;
+    if (g.WMODEL == 4 && g.N3M > g.N1M) return C3D_EINVAL;   // WERNER indexes INDX(N1M) with K
     const int N1 = g.N1, N2 = g.N2, N3 = g.N3;
     double *UH = g.UH.data(), *HH2 = g.HH2.data();
     if (g.FILES != 0 && !SGSVIS) {
@@ -2160,7 +2223,7 @@ int orc_getup(void *h, double *U, double *P, double *HH, double *SGSVIS, int NTI
             g.IFWALL = 0;
             wallss_common(g, U, g.WSM);
         } else {
-            status = wallmodel_instant(g, U);
+            status = wallmodel(g, U);
             g.IFWALL = 1;
         }
     }

@@ -67,6 +67,8 @@ def gpu_from(libc3d, orc, g, U, P, HH, precision=C3D_FP64):
     ("les32dy", {}),                        # dynamic + WALLMODEL_INSTANT
     ("les32cs", dict(wmodel=0, cks=2.0)),   # Smagorinsky, no-slip walls, stretched y
     ("les32dy", dict(wmodel=0, cks=2.0)),   # dynamic, no-slip walls, stretched y
+    ("les32cs", dict(wmodel=4)),            # Smagorinsky + WALLMODEL_WERNER (both walls)
+    ("les32dy", dict(wmodel=4)),            # dynamic + WALLMODEL_WERNER
 ])
 def test_les_one_step_fp64(libc3d, oracle_mod, name, over):
     g, dt, orc, U, P, HH, S, pg, pg3 = warm_start(oracle_mod, name, **over)

@@ -136,6 +136,65 @@ def test_wallmodel_recovers_log_law(oracle_mod):
     assert np.all(tw[..., 1] == 0) and np.all(tb[..., 1] == 0)
 
 
+WW = dict(B=0.1428571429, AB1=7.202125274, AB3=69.74057973, AB4=0.1376936317, AB5=1.75)
+
+
+def _werner_tau(vel, dy, re, wsm1):
+    """Werner-Wengle stress magnitude at the first cell centre (compact3d.f:4855-4869)."""
+    vcase = WW["AB3"] * np.sqrt(abs(wsm1)) / 11.81
+    visc = 2.0 * vel / dy / re
+    power = (WW["AB1"] * (1.0 / dy / re) ** (1.0 + WW["B"]) + WW["AB4"] * (1.0 / dy / re) ** WW["B"] * vel) ** WW["AB5"]
+    return np.where(vel <= vcase, visc, power)
+
+
+@pytest.mark.parametrize("wsm1", [1e-6, 10.0])   # power-law branch, viscous branch
+def test_werner_matches_numpy_restatement(oracle_mod, wsm1):
+    """WALLMODEL_WERNER on a random field against an independent numpy restatement with
+    the reference's indexing (x neighbour IPA(K)/IMA(K) taken with the z index, F:4852,
+    4881, 4924), both walls, both branches of the power law; WSM(1) is the plane mean of
+    the bottom u-stress at the cell centres and WSM(2), WSM(3) are zeroed."""
+    g, _ = _grid("les32cs", wmodel=4)
+    o = oracle_mod.Oracle(g)
+    U = _smooth_field(g, seed=11)
+    o.set_wsm([wsm1, 0.3, 0.4])
+    assert o.wallmodel(U) == 0
+    tw, tb, wsm = o.get_wall()
+    n1, n2, n3 = g.n1m, g.n2m, g.n3m
+    DY = g.arrays["dy"]
+    i = np.arange(1, n1 + 1)[:, None]
+    k = np.arange(1, n3 + 1)[None, :]
+    ipa = lambda q: np.where(q == n1, 1, q + 1)
+    ima = lambda q: np.where(q == 1, n1, q - 1)
+    kpa = lambda q: np.where(q == n3, 1, q + 1)
+    kma = lambda q: np.where(q == 1, n3, q - 1)
+    te = []
+    for jw in (1, n2):
+        u1 = 0.5 * (U[i, jw, k, 0] + U[ipa(k) + 0 * i, jw, k, 0])
+        u2 = 0.5 * (U[i, jw, k, 2] + U[i, jw, kpa(k), 2])
+        vel = np.sqrt(u1 ** 2 + u2 ** 2)
+        t = _werner_tau(vel, DY[jw], g.re, wsm1)
+        te.append((t * u1 / vel, t * u2 / vel))
+    for wall, (tu, tw_) in enumerate(te):
+        full_u = np.zeros((n1 + 1, n3 + 1)); full_u[1:, 1:] = tu
+        full_w = np.zeros((n1 + 1, n3 + 1)); full_w[1:, 1:] = tw_
+        exp_tw = 0.5 * (full_u[i, k] + full_u[ima(k) + 0 * i, k])
+        exp_tb = 0.5 * (full_w[i, k] + full_w[i, kma(k)])
+        np.testing.assert_allclose(tw[1:n1 + 1, 1:n3 + 1, wall], exp_tw, rtol=1e-12)
+        np.testing.assert_allclose(tb[1:n1 + 1, 1:n3 + 1, wall], exp_tb, rtol=1e-12, atol=1e-18)
+    assert wsm[0] == pytest.approx(te[0][0].mean(), rel=1e-12)
+    assert wsm[1] == 0.0 and wsm[2] == 0.0
+
+
+def test_werner_needs_n3_le_n1(oracle_mod):
+    """The reference's IPA(K) indexing reads past the x index arrays when N3M > N1M; the
+    restatement refuses such grids."""
+    g, dt = _grid("les32cs", wmodel=4, n3m=64)
+    o = oracle_mod.Oracle(g)
+    U, P, HH = ic.loglaw(g, 2000.0)
+    with pytest.raises(Exception):
+        o.getup(U, P, HH, 1, dt, 0.0, 0.0, g.zeros_s())
+
+
 def test_wallmodel_iteration_cap_is_an_error(oracle_mod):
     g, _ = _grid("les32cs")
     o = oracle_mod.Oracle(g)
