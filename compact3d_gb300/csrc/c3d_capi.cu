@@ -1,3 +1,4 @@
+#include <cstdio>
 // c3d_capi.cu -- the C-ABI of include/c3d.h: channel lifecycle, host<->device transfers,
 // the GETUP drop-in step, diagnostics and the batched ensemble.
 #include <cuda_runtime.h>
@@ -90,6 +91,7 @@ const char *c3d_error_string(int code) {
         case C3D_ENONFINITE: return "non-finite value in the fields";
         case C3D_ESTATE: return "call made in the wrong state";
         case C3D_ENODEV: return "no usable CUDA device";
+        case C3D_EIO: return "checkpoint file could not be written or read";
         default: return "unknown error";
     }
 }
@@ -1078,6 +1080,123 @@ int c3d_getup(c3d_channel *ch, double *u, double *p, double *hh, double *sgsvis,
     rc = c3d_step(ch, ntime, dt, presg, presg3);
     if (rc) return rc;
     return c3d_download(ch, u, p, hh, ch->files != 0 ? sgsvis : nullptr);
+}
+
+// ---- checkpoint -----------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+// One Fortran sequential unformatted record: length, payload, length (4-byte markers).
+int rec_write(FILE *f, const void *p, size_t bytes) {
+    if (bytes > 0x7fffffffu) { set_error("checkpoint record longer than 2^31-1 bytes"); return C3D_EINVAL; }
+    const int32_t m = (int32_t)bytes;
+    if (fwrite(&m, 4, 1, f) != 1 || (bytes && fwrite(p, 1, bytes, f) != bytes) || fwrite(&m, 4, 1, f) != 1) {
+        set_error("checkpoint write failed");
+        return C3D_EIO;
+    }
+    return 0;
+}
+int rec_read(FILE *f, void *p, size_t bytes) {
+    int32_t m0 = 0, m1 = 0;
+    if (fread(&m0, 4, 1, f) != 1 || (size_t)(uint32_t)m0 != bytes) {
+        set_error("checkpoint record length does not match the channel's grid");
+        return C3D_EIO;
+    }
+    if ((bytes && fread(p, 1, bytes, f) != bytes) || fread(&m1, 4, 1, f) != 1 || m1 != m0) {
+        set_error("checkpoint read failed (truncated file or bad record marker)");
+        return C3D_EIO;
+    }
+    return 0;
+}
+// A device record through the staging area: packed on the device, copied, written.
+int rec_write_dev(c3d_channel *ch, FILE *f, int what, double *slot, size_t n, std::vector<double> &hb) {
+    int rc = launch_ckpt(ch, 0, what, slot);
+    if (rc) return rc;
+    hb.resize(n);
+    CK(cudaMemcpyAsync(hb.data(), slot, n * 8, cudaMemcpyDeviceToHost, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    return rec_write(f, hb.data(), n * 8);
+}
+int rec_read_dev(c3d_channel *ch, FILE *f, int what, double *slot, size_t n, std::vector<double> &hb) {
+    hb.resize(n);
+    int rc = rec_read(f, hb.data(), n * 8);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(slot, hb.data(), n * 8, cudaMemcpyHostToDevice, ch->stream));
+    rc = launch_ckpt(ch, 1, what, slot);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ch->stream));
+    return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int c3d_checkpoint_write(c3d_channel *ch, const char *path, int ntime, double time, double presg,
+                         double presg3) {
+    if (!ch || !path) { set_error("null argument"); return C3D_EINVAL; }
+    if (!ch->have_state) { set_error("the channel has no state to write"); return C3D_ESTATE; }
+    cudaSetDevice(ch->device);
+    CK(cudaStreamSynchronize(ch->stream));
+    Xfer x;
+    int rc = xfer_area(ch, &x);
+    if (rc) return rc;
+    const Geo &g = ch->g;
+    const size_t nu = 3 * (size_t)g.n1m * (g.n2 + 1) * g.n3m, np_ = (size_t)g.n1m * g.n2m * g.n3m;
+    FILE *f = fopen(path, "wb");
+    if (!f) { set_error(std::string("cannot open ") + path + " for writing"); return C3D_EIO; }
+    std::vector<double> hb;
+    const int32_t dims[3] = {g.n1m, g.n2m, g.n3m};
+    const double pg[2] = {presg, presg3};
+    const int32_t nt = ntime;
+    if (!(rc = rec_write(f, dims, sizeof(dims))) && !(rc = rec_write(f, pg, sizeof(pg))) &&
+        !(rc = rec_write(f, &nt, 4)) && !(rc = rec_write(f, &time, 8)) &&
+        !(rc = rec_write_dev(ch, f, 0, x.u(0), nu, hb)) && !(rc = rec_write_dev(ch, f, 1, x.p(), np_, hb)) &&
+        !(rc = rec_write_dev(ch, f, 2, x.hh(0), 3 * np_, hb)) && ch->files != 0) {
+        const size_t nt_ = (size_t)(g.n1m + 2) * (g.n3m + 2) * 2;
+        std::vector<double> w(2 * nt_ + 3);
+        if (!(rc = c3d_download_wall(ch, w.data(), w.data() + nt_)) && !(rc = c3d_get_wsm(ch, w.data() + 2 * nt_)))
+            rc = rec_write(f, w.data(), w.size() * 8);
+    }
+    if (fclose(f) != 0 && !rc) { set_error("checkpoint close failed"); rc = C3D_EIO; }
+    return rc;
+}
+
+int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *time, double *presg,
+                        double *presg3) {
+    if (!ch || !path) { set_error("null argument"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    CK(cudaStreamSynchronize(ch->stream));
+    Xfer x;
+    int rc = xfer_area(ch, &x);
+    if (rc) return rc;
+    const Geo &g = ch->g;
+    const size_t nu = 3 * (size_t)g.n1m * (g.n2 + 1) * g.n3m, np_ = (size_t)g.n1m * g.n2m * g.n3m;
+    FILE *f = fopen(path, "rb");
+    if (!f) { set_error(std::string("cannot open ") + path); return C3D_EIO; }
+    std::vector<double> hb;
+    int32_t dims[3] = {0, 0, 0}, nt = 0;
+    double pg[2] = {0.0, 0.0}, tm = 0.0;
+    rc = rec_read(f, dims, sizeof(dims));
+    if (!rc && (dims[0] != g.n1m || dims[1] != g.n2m || dims[2] != g.n3m)) {
+        set_error("checkpoint grid does not match the channel's");
+        rc = C3D_EINVAL;
+    }
+    if (!rc && !(rc = rec_read(f, pg, sizeof(pg))) && !(rc = rec_read(f, &nt, 4)) && !(rc = rec_read(f, &tm, 8)) &&
+        !(rc = rec_read_dev(ch, f, 0, x.u(0), nu, hb)) && !(rc = rec_read_dev(ch, f, 1, x.p(), np_, hb)) &&
+        !(rc = rec_read_dev(ch, f, 2, x.hh(0), 3 * np_, hb)) && ch->files != 0) {
+        const size_t nt_ = (size_t)(g.n1m + 2) * (g.n3m + 2) * 2;
+        std::vector<double> w(2 * nt_ + 3);
+        if (!(rc = rec_read(f, w.data(), w.size() * 8)) && !(rc = c3d_upload_wall(ch, w.data(), w.data() + nt_)))
+            rc = c3d_set_wsm(ch, w.data() + 2 * nt_);
+    }
+    fclose(f);
+    if (rc) return rc;
+    ch->have_state = 1;
+    if (ntime) *ntime = nt;
+    if (time) *time = tm;
+    if (presg) *presg = pg[0];
+    if (presg3) *presg3 = pg[1];
+    return 0;
 }
 
 int c3d_op_set(c3d_channel *ch, const double *f) {

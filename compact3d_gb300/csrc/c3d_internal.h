@@ -239,6 +239,9 @@ int launch_diag(c3d_channel *ch, int *launches);
 int launch_poisson_tables(c3d_channel *ch);
 // what: 0 U component, 1 P, 2 HH component, 3 SGSVIS (to host), 4 operand (to device),
 // 5 operator result (to host)
+// Checkpoint records (CWRITE's order) between the device state and buf; dir 0 packs,
+// what 0 U, 1 P, 2 HH (three components)
+int launch_ckpt(c3d_channel *ch, int dir, int what, double *buf);
 // fort: the Fortran-layout array on the device (the one-field staging buffer by default)
 int launch_repack(c3d_channel *ch, int dir, int what, int comp, double *fort = nullptr);  // dir 0: Fortran->device
 void set_error(const std::string &msg);

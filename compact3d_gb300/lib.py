@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(HERE, "libc3d.so")
 
 C3D_OK = 0
 ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ENOTCONV", -5: "ENONFINITE",
-          -6: "ESTATE", -7: "ENODEV"}
+          -6: "ESTATE", -7: "ENODEV", -8: "EIO"}
 
 # Every function declared in include/c3d.h, with its ctypes signature.
 _vp, _ip, _dp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
@@ -54,6 +54,8 @@ SIGNATURES = {
     "c3d_op_set": (_ip, [_vp, _dp]),
     "c3d_op_apply": (_ip, [_vp, _ip, _ip]),
     "c3d_op_get": (_ip, [_vp, _dp]),
+    "c3d_checkpoint_write": (_ip, [_vp, ctypes.c_char_p, _ip, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
+    "c3d_checkpoint_read": (_ip, [_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), _dp, _dp, _dp]),
     "c3d_step": (_ip, [_vp, _ip, ctypes.c_double, _dp, _dp]),
     "c3d_diagnose": (_ip, [_vp, ctypes.POINTER(c3d_diag)]),
     "c3d_getup": (_ip, [_vp, _dp, _dp, _dp, _dp, _ip, ctypes.c_double, _dp, _dp]),
@@ -200,6 +202,19 @@ class Channel:
     def set_schedule(self, sched: dict):
         sch = (_ip * 12)(*[int(sched[k]) for k in self.SCHEDULE_KEYS])
         check(load().c3d_set_schedule(self.h, sch), "c3d_set_schedule")
+
+    # ---- checkpoint (CWRITE / READUP in a format that round-trips) ----
+    def checkpoint_write(self, path, ntime: int, time: float, presg: float, presg3: float):
+        check(load().c3d_checkpoint_write(self.h, str(path).encode(), int(ntime), float(time), float(presg),
+                                          float(presg3)), "c3d_checkpoint_write")
+
+    def checkpoint_read(self, path):
+        """Loads the state of a checkpoint; returns (ntime, time, presg, presg3)."""
+        nt = ctypes.c_int(0)
+        t, a, b = ((ctypes.c_double * 1)() for _ in range(3))
+        check(load().c3d_checkpoint_read(self.h, str(path).encode(), ctypes.byref(nt), t, a, b),
+              "c3d_checkpoint_read")
+        return nt.value, t[0], a[0], b[0]
 
     # ---- operators one at a time ----
     def op_set(self, F):

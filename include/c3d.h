@@ -39,6 +39,7 @@ extern "C" {
 #define C3D_ENONFINITE  (-5)   /* NaN/Inf found by the diagnostics              */
 #define C3D_ESTATE      (-6)   /* call made in the wrong state                  */
 #define C3D_ENODEV      (-7)   /* no usable CUDA device                         */
+#define C3D_EIO         (-8)   /* a checkpoint file could not be written or read */
 
 /* ---- precision forms -------------------------------------------------- */
 #define C3D_FP64   0   /* every operation in FP64                              */
@@ -216,6 +217,31 @@ int c3d_profile_get(c3d_channel *ch, int idx, const char **name, double *ms,
  * stream; the call returns when *divmax is ready. */
 #define C3D_NOALLOC_MAX_BYTES (64u * 1024u * 1024u)
 int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
+
+/* ---- checkpoint ------------------------------------------------------------
+ * The restart pair of the reference, CWRITE / READUP (compact3d.f:741-872), writes a
+ * list-directed text file and reads it back unformatted in another loop order, so the
+ * two do not round-trip.  These write and read one fixed format that does, straight
+ * from and into the device state: Fortran sequential unformatted records (a 4-byte
+ * little-endian length before and after each record), REAL*8 values, CWRITE's content
+ * and loop order:
+ *   1. N1M, N2M, N3M                                    (INTEGER*4 x 3)
+ *   2. PRESG, PRESG3                                    (REAL*8 x 2)
+ *   3. NTIME                                            (INTEGER*4)
+ *   4. TIME                                             (REAL*8)
+ *   5. ((( U(I,J,K,1), U(I,J,K,2), U(I,J,K,3), I=1,N1M), J=0,N2), K=1,N3M)
+ *   6. ((( P(I,J,K), I=1,N1M), J=1,N2M), K=1,N3M)
+ *   7. (((( HH(I,J,K,NV), I=1,N1M), J=1,N2M), K=1,N3M), NV=1,3)   (AB2 history)
+ *   8. with an SGS model only: TAUW(0:M1,0:M3,2), TAUB(0:M1,0:M3,2), WSM(3)
+ * Records 1 and 7-8 extend CWRITE so that a restart continues the run exactly (the
+ * reference restarts with HH = 0).  A record longer than 2^31 - 1 bytes (more than
+ * 89 M points per component) is refused with C3D_EINVAL.  c3d_checkpoint_read checks
+ * the extents against the channel's grid and leaves the channel's state as read.
+ * INTEGRATION.md shows the matching Fortran READ statements. */
+int c3d_checkpoint_write(c3d_channel *ch, const char *path, int ntime, double time, double presg,
+                         double presg3);
+int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *time, double *presg,
+                        double *presg3);
 
 /* ---- launch schedule -----------------------------------------------------
  * The kernels' launch shapes are chosen per grid shape by an autotuner written for

@@ -33,7 +33,7 @@ def test_every_declared_symbol_is_exported(L):
 
 
 def test_error_strings(L):
-    for code in (0, -1, -2, -3, -4, -5, -6, -7, -99):
+    for code in (0, -1, -2, -3, -4, -5, -6, -7, -8, -99):
         assert L.c3d_error_string(code)
 
 
@@ -65,7 +65,7 @@ def test_create_rejects_null_metrics(L):
 
 def test_create_rejects_bad_precision_and_models(L):
     g, _ = make_grid("small32")
-    for field, val in (("precision", 7), ("files", 3), ("re", -1.0)):
+    for field, val in (("precision", 7), ("files", 3), ("re", -1.0), ("wmodel", 2), ("wmodel", 3), ("wmodel", 5)):
         s = g.struct()
         setattr(s, field, val)
         h = ctypes.c_void_p()
@@ -80,3 +80,14 @@ def test_null_handles(L):
     assert L.c3d_diagnose(None, None) == -1
     assert L.c3d_batch_step(None, 1, None, None, None) == -1
     assert L.c3d_sync(None) == -1
+    assert L.c3d_checkpoint_write(None, b"x", 1, 0.0, 0.0, 0.0) == -1
+    assert L.c3d_checkpoint_read(None, b"x", None, None, None, None) == -1
+
+
+def test_werner_needs_n3_not_above_n1(L):
+    """WMODEL 4 (WALLMODEL_WERNER) indexes x with the z index, as the reference does;
+    grids with N3M > N1M are refused before any device work."""
+    g, _ = make_grid("les32cs", wmodel=4, n3m=64)
+    s = g.struct()
+    h = ctypes.c_void_p()
+    assert L.c3d_create(ctypes.byref(s), ctypes.byref(h)) == -1
