@@ -197,6 +197,7 @@ void free_channel(c3d_channel *ch) {
         if (e) cudaEventDestroy(e);
     if (ch->xfer) cudaFree(ch->xfer);
     if (ch->wtaue) cudaFree(ch->wtaue);
+    if (ch->stats) cudaFree(ch->stats);
     if (ch->hh_in) cudaEventDestroy(ch->hh_in);
     if (ch->hh_out) cudaEventDestroy(ch->hh_out);
     if (ch->ev0) cudaEventDestroy(ch->ev0);
@@ -1130,6 +1131,19 @@ int rec_read_dev(c3d_channel *ch, FILE *f, int what, double *slot, size_t n, std
 }  // namespace
 
 extern "C" {
+
+int c3d_plane_stats(c3d_channel *ch, double *out) {
+    if (!ch || !out) { set_error("null argument"); return C3D_EINVAL; }
+    if (!ch->have_state) { set_error("c3d_upload must be called before c3d_plane_stats"); return C3D_ESTATE; }
+    cudaSetDevice(ch->device);
+    const size_t ns = stats_scratch_doubles(ch->g), nout = (size_t)ch->g.n2m * 29;
+    if (!ch->stats && dalloc(&ch->stats, ns)) return C3D_ENOMEM;
+    int rc = launch_stats(ch, ch->stats, ch->stats + nout);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(out, ch->stats, nout * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    return 0;
+}
 
 int c3d_checkpoint_write(c3d_channel *ch, const char *path, int ntime, double time, double presg,
                          double presg3) {

@@ -158,6 +158,7 @@ struct c3d_channel {
     bool hh_hooks = false;
     double *xfer = nullptr;   // DMA staging area of pinned host arrays (one slot per field)
     double *wtaue = nullptr;  // WALLMODEL_WERNER: TAUWE(I,K,1..4) at the cell centres (4 x N1M N3M)
+    double *stats = nullptr;  // plane statistics table and partial sums (allocated on first use)
     cudaStream_t cs = nullptr;          // copy stream of the DMA transfers
     cudaEvent_t xev[16] = {};           // per-field hand-offs between the copy and compute streams
     // state (double or float2 by precision), scalars and metrics
@@ -239,6 +240,10 @@ int launch_diag(c3d_channel *ch, int *launches);
 int launch_poisson_tables(c3d_channel *ch);
 // what: 0 U component, 1 P, 2 HH component, 3 SGSVIS (to host), 4 operand (to device),
 // 5 operator result (to host)
+// ENERGY's plane statistics of the current state into out (N2M x 29, device), with
+// `part` as scratch (stats_scratch_doubles(g) doubles hold both)
+int launch_stats(c3d_channel *ch, double *out, double *part);
+size_t stats_scratch_doubles(const c3d::Geo &g);
 // Checkpoint records (CWRITE's order) between the device state and buf; dir 0 packs,
 // what 0 U, 1 P, 2 HH (three components)
 int launch_ckpt(c3d_channel *ch, int dir, int what, double *buf);

@@ -1,0 +1,179 @@
+// c3d_stats.cu -- ENERGY's plane statistics (compact3d.f:10003-10232) on the device, FP64:
+// per plane J the cell-centre means, second moments, vorticity statistics, the two third
+// moments ENERGY keeps, the third and fourth central moments and the mean wall-normal
+// gradients (29 values; the column order is that of c3d_plane_stats in include/c3d.h).
+// Each plane is split over SB blocks; partial sums are combined in a fixed order.
+#include "c3d_kern.cuh"
+
+namespace c3d {
+
+constexpr int SB = 8;        // blocks per plane
+constexpr int STB = 128;     // threads per block
+constexpr int NS1 = 23;      // first-pass sums: 20 moments + 3 gradients
+
+template <typename R>
+__device__ __forceinline__ double sv(const typename SType<R>::S *a, const Geo &g, int i, int j, int k) {
+    return St<R>::dbl(a[fidx(g, i, j, k)]);
+}
+
+// Cell-centre velocities, pressure, vorticity and the wall-normal gradients at (i, j, k)
+// (0-based i, k; plane j = 1..N2M), as ENERGY's loops 10, 20 and 40.
+template <typename R>
+__device__ void point_terms(const StepArgs<R> &a, int i, int j, int k, double v[3], double &pp, double w[3],
+                            double d[3]) {
+    typedef typename SType<R>::S S;
+    const Geo &g = a.g;
+    const S *U = a.u, *V = a.v, *W = a.w;
+    const int ip = i + 1 == g.n1m ? 0 : i + 1, im = i == 0 ? g.n1m - 1 : i - 1;
+    const int kp = k + 1 == g.n3m ? 0 : k + 1, km = k == 0 ? g.n3m - 1 : k - 1;
+    const int jp = j + 1, jm = j - 1, n2 = g.n2;
+    const double FJUM = j > 1 ? 1.0 : 0.0, FJUP = j < g.n2m ? 1.0 : 0.0;
+    const double *DY = g.dy, *H = g.h;
+    const double DX1 = g.dx1, DX3 = g.dx3;
+    // loop 10: vorticity
+    double U1KP = 0.5 * (sv<R>(U, g, i, j, kp) + sv<R>(U, g, ip, j, kp));
+    double U1KM = 0.5 * (sv<R>(U, g, i, j, km) + sv<R>(U, g, ip, j, km));
+    double U2KP = 0.5 * (sv<R>(V, g, i, j, kp) + sv<R>(V, g, i, jp, kp));
+    double U2KM = 0.5 * (sv<R>(V, g, i, j, km) + sv<R>(V, g, i, jp, km));
+    double U2IP = 0.5 * (sv<R>(V, g, ip, j, k) + sv<R>(V, g, ip, jp, k));
+    double U2IM = 0.5 * (sv<R>(V, g, im, j, k) + sv<R>(V, g, im, jp, k));
+    double U3IP = 0.5 * (sv<R>(W, g, ip, j, k) + sv<R>(W, g, ip, j, kp));
+    double U3IM = 0.5 * (sv<R>(W, g, im, j, k) + sv<R>(W, g, im, j, kp));
+    double U1JP = 0.5 * (sv<R>(U, g, i, jp, k) + sv<R>(U, g, ip, jp, k));
+    double U1JC = 0.5 * (sv<R>(U, g, i, j, k) + sv<R>(U, g, ip, j, k));
+    double U1JM = 0.5 * (sv<R>(U, g, i, jm, k) + sv<R>(U, g, ip, jm, k));
+    double U12 = 0.5 / H[jp] * (DY[jp] * U1JC + DY[j] * U1JP);
+    double U11 = 0.5 / H[j] * (DY[j] * U1JM + DY[jm] * U1JC);
+    const double U1N2 = (sv<R>(U, g, i, n2, k) + sv<R>(U, g, ip, n2, k)) * 0.5;
+    const double U10 = (sv<R>(U, g, i, 0, k) + sv<R>(U, g, ip, 0, k)) * 0.5;
+    U12 = U12 * FJUP + (1. - FJUP) * U1N2;
+    U11 = U11 * FJUM + (1. - FJUM) * U10;
+    double U3JP = 0.5 * (sv<R>(W, g, i, jp, k) + sv<R>(W, g, i, jp, kp));
+    double U3JC = 0.5 * (sv<R>(W, g, i, j, k) + sv<R>(W, g, i, j, kp));
+    double U3JM = 0.5 * (sv<R>(W, g, i, jm, k) + sv<R>(W, g, i, jm, kp));
+    double U32 = 0.5 / H[jp] * (DY[jp] * U3JC + DY[j] * U3JP);
+    double U31 = 0.5 / H[j] * (DY[j] * U3JM + DY[jm] * U3JC);
+    const double U3N2 = (sv<R>(W, g, i, n2, k) + sv<R>(W, g, i, n2, kp)) * 0.5;
+    const double U30 = (sv<R>(W, g, i, 0, k) + sv<R>(W, g, i, 0, kp)) * 0.5;
+    U32 = U32 * FJUP + (1. - FJUP) * U3N2;
+    U31 = U31 * FJUM + (1. - FJUM) * U30;
+    const double DV3DX2 = (U32 - U31) / DY[j];
+    const double DV2DX3 = (U2KP - U2KM) * 0.5 * DX3;
+    const double DV3DX1 = (U3IP - U3IM) * 0.5 * DX1;
+    const double DV1DX3 = (U1KP - U1KM) * 0.5 * DX3;
+    const double DV2DX1 = (U2IP - U2IM) * 0.5 * DX1;
+    const double DV1DX2 = (U12 - U11) / DY[j];
+    w[0] = DV3DX2 - DV2DX3;
+    w[1] = DV1DX3 - DV3DX1;
+    w[2] = DV2DX1 - DV1DX2;
+    // loop 20: cell-centre values
+    v[0] = U1JC;
+    v[1] = (sv<R>(V, g, i, j, k) + sv<R>(V, g, i, jp, k)) * 0.5;
+    v[2] = U3JC;
+    pp = St<R>::dbl(a.p[fidx(g, i, j, k)]);
+    // loop 40: wall-normal gradients (ENERGY writes these interpolants in another order)
+    const double U_JP = U1JP, U_JC = U1JC, U_JM = U1JM, W_JP = U3JP, W_JC = U3JC, W_JM = U3JM;
+    const double G1 = FJUM * (1.0 / H[j] * (DY[j] * U_JM / 2.0 + DY[jm] * U_JC / 2.0)) + (1. - FJUM) * U10;
+    const double G2 = FJUP * (1.0 / H[jp] * (DY[j] * U_JP / 2.0 + DY[jp] * U_JC / 2.0)) + (1. - FJUP) * U1N2;
+    const double E1 = FJUM * (1.0 / H[j] * (DY[j] * W_JM / 2.0 + DY[jm] * W_JC / 2.0)) + (1. - FJUM) * U30;
+    const double E2 = FJUP * (1.0 / H[jp] * (DY[j] * W_JP / 2.0 + DY[jp] * W_JC / 2.0)) + (1. - FJUP) * U3N2;
+    d[0] = (G2 - G1) / DY[j];
+    d[1] = (sv<R>(V, g, i, jp, k) - sv<R>(V, g, i, j, k)) / DY[j];
+    d[2] = (E2 - E1) / DY[j];
+}
+
+__device__ __forceinline__ void block_sums(double *acc, int n, double *sh, double *outp) {
+    for (int q = 0; q < n; ++q) sh[q * STB + threadIdx.x] = acc[q];
+    __syncthreads();
+    for (int s = STB / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s)
+            for (int q = 0; q < n; ++q) sh[q * STB + threadIdx.x] += sh[q * STB + threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < n; ++q) outp[q] = sh[q * STB];
+}
+
+// pass 1: blockIdx.y = plane J - 1, blockIdx.x = part of the plane; partial sums
+template <typename R>
+__global__ void __launch_bounds__(STB) k_stats1(StepArgs<R> a, double *part) {
+    __shared__ double sh[NS1 * STB];
+    const Geo &g = a.g;
+    const int j = 1 + blockIdx.y;
+    const int chunk = (g.np + SB - 1) / SB, e0 = blockIdx.x * chunk, e1 = min(g.np, e0 + chunk);
+    double acc[NS1];
+#pragma unroll
+    for (int q = 0; q < NS1; ++q) acc[q] = 0.0;
+    for (int e = e0 + threadIdx.x; e < e1; e += STB) {
+        const int i = e % g.n1m, k = e / g.n1m;
+        double v[3], w[3], d[3], pp;
+        point_terms<R>(a, i, j, k, v, pp, w, d);
+        acc[0] += v[0]; acc[1] += v[1]; acc[2] += v[2]; acc[3] += pp;
+        acc[4] += w[0]; acc[5] += w[1]; acc[6] += w[2];
+        acc[7] += v[0] * v[0]; acc[8] += v[1] * v[1]; acc[9] += v[2] * v[2];
+        acc[10] += v[0] * v[1]; acc[11] += v[0] * v[2]; acc[12] += v[1] * v[2];
+        acc[13] += pp * pp; acc[14] += pp * v[1];
+        acc[15] += w[0] * w[0]; acc[16] += w[1] * w[1]; acc[17] += w[2] * w[2];
+        acc[18] += v[0] * v[0] * v[1]; acc[19] += v[1] * v[2] * v[2];
+        acc[20] += d[0]; acc[21] += d[1]; acc[22] += d[2];
+    }
+    block_sums(acc, NS1, sh, part + ((size_t)blockIdx.y * SB + blockIdx.x) * NS1);
+}
+
+// combine pass 1 (fixed order) into the plane's means: out[J][0..19], [26..28]
+__global__ void k_stats1_fin(Geo g, const double *part, double *out) {
+    const int j = blockIdx.x, q = threadIdx.x;
+    if (q >= NS1) return;
+    double s = 0.0;
+    for (int b = 0; b < SB; ++b) s += part[((size_t)j * SB + b) * NS1 + q];
+    const double m = s / ((double)g.n1m * (double)g.n3m);
+    out[(size_t)j * 29 + (q < 20 ? q : q + 6)] = m;
+}
+
+// pass 2: third and fourth central moments of the cell-centre velocities
+template <typename R>
+__global__ void __launch_bounds__(STB) k_stats2(StepArgs<R> a, const double *out, double *part) {
+    __shared__ double sh[6 * STB];
+    const Geo &g = a.g;
+    const int j = 1 + blockIdx.y;
+    const double m0 = out[(size_t)(j - 1) * 29 + 0], m1 = out[(size_t)(j - 1) * 29 + 1], m2 = out[(size_t)(j - 1) * 29 + 2];
+    const int chunk = (g.np + SB - 1) / SB, e0 = blockIdx.x * chunk, e1 = min(g.np, e0 + chunk);
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int e = e0 + threadIdx.x; e < e1; e += STB) {
+        const int i = e % g.n1m, k = e / g.n1m;
+        const int ip = i + 1 == g.n1m ? 0 : i + 1, kp = k + 1 == g.n3m ? 0 : k + 1;
+        const double V1 = (sv<R>(a.u, g, i, j, k) + sv<R>(a.u, g, ip, j, k)) * 0.5 - m0;
+        const double V2 = (sv<R>(a.v, g, i, j, k) + sv<R>(a.v, g, i, j + 1, k)) * 0.5 - m1;
+        const double V3 = (sv<R>(a.w, g, i, j, k) + sv<R>(a.w, g, i, j, kp)) * 0.5 - m2;
+        acc[0] += V1 * V1 * V1; acc[1] += V2 * V2 * V2; acc[2] += V3 * V3 * V3;
+        acc[3] += V1 * V1 * V1 * V1; acc[4] += V2 * V2 * V2 * V2; acc[5] += V3 * V3 * V3 * V3;
+    }
+    block_sums(acc, 6, sh, part + ((size_t)blockIdx.y * SB + blockIdx.x) * 6);
+}
+
+__global__ void k_stats2_fin(Geo g, const double *part, double *out) {
+    const int j = blockIdx.x, q = threadIdx.x;
+    if (q >= 6) return;
+    double s = 0.0;
+    for (int b = 0; b < SB; ++b) s += part[((size_t)j * SB + b) * 6 + q];
+    out[(size_t)j * 29 + 20 + q] = s / ((double)g.n1m * (double)g.n3m);
+}
+
+template <typename R>
+int launch_stats_t(c3d_channel *ch, StepArgs<R> &a, double *out, double *part) {
+    const Geo &g = ch->g;
+    const dim3 grid(SB, g.n2m);
+    k_stats1<R><<<grid, STB, 0, ch->stream>>>(a, part);
+    k_stats1_fin<<<g.n2m, 32, 0, ch->stream>>>(g, part, out);
+    k_stats2<R><<<grid, STB, 0, ch->stream>>>(a, out, part);
+    k_stats2_fin<<<g.n2m, 32, 0, ch->stream>>>(g, part, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : C3D_ECUDA;
+}
+
+template int launch_stats_t<double>(c3d_channel *, StepArgs<double> &, double *, double *);
+template int launch_stats_t<float>(c3d_channel *, StepArgs<float> &, double *, double *);
+
+// Scratch the statistics need on the device: the output table and the partial sums.
+size_t stats_scratch_doubles(const Geo &g) { return (size_t)g.n2m * 29 + (size_t)g.n2m * SB * NS1; }
+
+}  // namespace c3d

@@ -470,6 +470,18 @@ static int step_impl(c3d_channel *ch, double dt, int *nl) {
 }
 
 template <typename R>
+int launch_stats_t(c3d_channel *ch, StepArgs<R> &a, double *out, double *part);
+
+int launch_stats(c3d_channel *ch, double *out, double *part) {
+    if (ch->precision == C3D_MIXED) {
+        StepArgs<float> a = make_args<float>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
+        return launch_stats_t<float>(ch, a, out, part);
+    }
+    StepArgs<double> a = make_args<double>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
+    return launch_stats_t<double>(ch, a, out, part);
+}
+
+template <typename R>
 static int operator_impl(c3d_channel *ch, int op, int *nl) {
     StepArgs<R> a = make_args<R>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
     return launch_op<R>(ch, a, op, (const R *)ch->opbuf[0], (R *)ch->opbuf[1], nl);

@@ -54,6 +54,7 @@ SIGNATURES = {
     "c3d_op_set": (_ip, [_vp, _dp]),
     "c3d_op_apply": (_ip, [_vp, _ip, _ip]),
     "c3d_op_get": (_ip, [_vp, _dp]),
+    "c3d_plane_stats": (_ip, [_vp, _dp]),
     "c3d_checkpoint_write": (_ip, [_vp, ctypes.c_char_p, _ip, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     "c3d_checkpoint_read": (_ip, [_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), _dp, _dp, _dp]),
     "c3d_step": (_ip, [_vp, _ip, ctypes.c_double, _dp, _dp]),
@@ -202,6 +203,17 @@ class Channel:
     def set_schedule(self, sched: dict):
         sch = (_ip * 12)(*[int(sched[k]) for k in self.SCHEDULE_KEYS])
         check(load().c3d_set_schedule(self.h, sch), "c3d_set_schedule")
+
+    # ---- ENERGY's plane statistics ----
+    STAT_NAMES = ("u", "v", "w", "p", "wx", "wy", "wz", "uu", "vv", "ww", "uv", "uw", "vw", "pp", "pv",
+                  "wxwx", "wywy", "wzwz", "uuv", "vww", "skew_u", "skew_v", "skew_w", "flat_u", "flat_v",
+                  "flat_w", "dudy", "dvdy", "dwdy")
+
+    def plane_stats(self):
+        """(N2M, 29) array of ENERGY's plane statistics; columns as STAT_NAMES."""
+        out = np.zeros(self.grid.n2m * 29)
+        check(load().c3d_plane_stats(self.h, _p(out)), "c3d_plane_stats")
+        return out.reshape(self.grid.n2m, 29)
 
     # ---- checkpoint (CWRITE / READUP in a format that round-trips) ----
     def checkpoint_write(self, path, ntime: int, time: float, presg: float, presg3: float):

@@ -218,6 +218,24 @@ int c3d_profile_get(c3d_channel *ch, int idx, const char **name, double *ms,
 #define C3D_NOALLOC_MAX_BYTES (64u * 1024u * 1024u)
 int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
 
+/* ---- plane statistics --------------------------------------------------------
+ * c3d_plane_stats computes, on the device and in FP64, the plane statistics of
+ * ENERGY (compact3d.f:10003-10232) for the current state: out[(J-1)*29 + q] for
+ * J = 1..N2M with q =
+ *    0-2  VM(J,1..3)   mean cell-centre u, v, w
+ *    3    PM(J)        mean P
+ *    4-6  WM(J,1..3)   mean vorticity (cell centres, ENERGY's stencils)
+ *    7-12 VRMS(J,1..6) mean uu, vv, ww, uv, uw, vw
+ *    13   PRMS(J)      mean pp          14  PV(J)   mean pv
+ *    15-17 WRMS(J,1..3) mean squared vorticity components
+ *    18   U2V(J)       mean uuv         19  VW2(J)  mean vww
+ *    20-22 VSKEW(J,1..3), 23-25 VFLAT(J,1..3)  third and fourth central moments
+ *    26-28 DUDY, DVDY, DWDY mean wall-normal gradients
+ * (raw moments as ENERGY stores them; the time averaging of TAVER and the output of
+ * WRITEAVG stay with the driver).  The spectra, correlations, quadrant and budget
+ * terms of ENERGY are not computed. */
+int c3d_plane_stats(c3d_channel *ch, double *out);
+
 /* ---- checkpoint ------------------------------------------------------------
  * The restart pair of the reference, CWRITE / READUP (compact3d.f:741-872), writes a
  * list-directed text file and reads it back unformatted in another loop order, so the

@@ -55,6 +55,7 @@ def lib():
         L.orc_cfl.argtypes = [vp, dp]
         L.orc_chkmf.argtypes = [vp, dp, dp, dp]
         L.orc_wallss.argtypes = [vp, dp, dp]
+        L.orc_plane_stats.argtypes = [vp, dp, dp, dp]
         L.orc_set_wall.argtypes = [vp, dp, dp, ip]
         L.orc_get_wall.argtypes = [vp, dp, dp, dp]
         L.orc_set_wsm.argtypes = [vp, dp]
@@ -141,6 +142,12 @@ class Oracle:
         w = (ctypes.c_double * 3)()
         lib().orc_wallss(self.h, _p(U), w)
         return np.array(w[:])
+
+    def plane_stats(self, U, P):
+        """ENERGY's plane statistics (N2M, 29); columns as c3d_plane_stats."""
+        out = np.zeros(self.grid.n2m * 29)
+        lib().orc_plane_stats(self.h, _p(U), _p(P), _p(out))
+        return out.reshape(self.grid.n2m, 29)
 
     def diagnose(self, U):
         f1, f3 = self.chkmf(U)

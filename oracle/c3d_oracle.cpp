@@ -2377,6 +2377,133 @@ void orc_chkmf(void *h, const double *U, double *flow1, double *flow3) {
 // WALLSS (compact3d.f:11077-11143)
 void orc_wallss(void *h, const double *U, double *wsm) { wallss_common(*(Orc *)h, U, wsm); }
 
+// ENERGY's plane statistics (compact3d.f:10003-10232), 29 per plane J = 1..N2M into
+// out[(J-1)*29 + q]: 0-2 VM (cell-centre u, v, w), 3 PM, 4-6 WM (vorticity), 7-12 VRMS
+// (uu, vv, ww, uv, uw, vw), 13 PRMS (pp), 14 PV (pv), 15-17 WRMS (vorticity squares),
+// 18 U2V (uuv), 19 VW2 (vww), 20-22 VSKEW and 23-25 VFLAT (third and fourth central
+// moments), 26-28 DUDY, DVDY, DWDY.  Plane means over K, I in that order, as the loops.
+void orc_plane_stats(void *h, const double *U, const double *P, double *out) {
+    Orc &g = *(Orc *)h;
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
+    const double NXZ = 1.0 / (double)(N1M * N3M), DX1 = g.DX1, DX3 = g.DX3;
+    const double *DY = g.DY.data(), *H = g.H.data();
+    auto u = [&](int i, int j, int k, int c) { return U[g.iuc(i, j, k, c)]; };
+    auto p = [&](int i, int j, int k) { return P[g.ip(i, j, k)]; };
+    std::vector<double> VOR((size_t)3 * N1M * N2M * N3M);
+    auto vor = [&](int i, int j, int k, int c) -> double & {
+        return VOR[(((size_t)(c - 1) * N3M + (k - 1)) * N2M + (j - 1)) * N1M + (i - 1)];
+    };
+    for (int K = 1; K <= N3M; K++) {   // loop 10: vorticity at the cell centres
+        const int KP = g.KPA[K], KM = g.KMA[K];
+        for (int J = 1; J <= N2M; J++) {
+            const int JP = J + 1, JM = J - 1;
+            const double FJUM = g.FJMU[J], FJUP = g.FJPA[J];
+            for (int I = 1; I <= N1M; I++) {
+                const int IP = g.IPA[I], IM = g.IMA[I];
+                double U1KP = 0.5 * (u(I, J, KP, 1) + u(IP, J, KP, 1));
+                double U1KM = 0.5 * (u(I, J, KM, 1) + u(IP, J, KM, 1));
+                double U2KP = 0.5 * (u(I, J, KP, 2) + u(I, JP, KP, 2));
+                double U2KM = 0.5 * (u(I, J, KM, 2) + u(I, JP, KM, 2));
+                double U2IP = 0.5 * (u(IP, J, K, 2) + u(IP, JP, K, 2));
+                double U2IM = 0.5 * (u(IM, J, K, 2) + u(IM, JP, K, 2));
+                double U3IP = 0.5 * (u(IP, J, K, 3) + u(IP, J, KP, 3));
+                double U3IM = 0.5 * (u(IM, J, K, 3) + u(IM, J, KP, 3));
+                double U1JP = 0.5 * (u(I, JP, K, 1) + u(IP, JP, K, 1));
+                double U1JC = 0.5 * (u(I, J, K, 1) + u(IP, J, K, 1));
+                double U1JM = 0.5 * (u(I, JM, K, 1) + u(IP, JM, K, 1));
+                double U12 = 0.5 / H[JP] * (DY[JP] * U1JC + DY[J] * U1JP);
+                double U11 = 0.5 / H[J] * (DY[J] * U1JM + DY[JM] * U1JC);
+                U12 = U12 * FJUP + (1. - FJUP) * (u(I, N2, K, 1) + u(IP, N2, K, 1)) * 0.5;
+                U11 = U11 * FJUM + (1. - FJUM) * (u(I, 0, K, 1) + u(IP, 0, K, 1)) * 0.5;
+                double U3JP = 0.5 * (u(I, JP, K, 3) + u(I, JP, KP, 3));
+                double U3JC = 0.5 * (u(I, J, K, 3) + u(I, J, KP, 3));
+                double U3JM = 0.5 * (u(I, JM, K, 3) + u(I, JM, KP, 3));
+                double U32 = 0.5 / H[JP] * (DY[JP] * U3JC + DY[J] * U3JP);
+                double U31 = 0.5 / H[J] * (DY[J] * U3JM + DY[JM] * U3JC);
+                U32 = U32 * FJUP + (1. - FJUP) * (u(I, N2, K, 3) + u(I, N2, KP, 3)) * 0.5;
+                U31 = U31 * FJUM + (1. - FJUM) * (u(I, 0, K, 3) + u(I, 0, KP, 3)) * 0.5;
+                double DV3DX2 = (U32 - U31) / DY[J];
+                double DV2DX3 = (U2KP - U2KM) * 0.5 * DX3;
+                double DV3DX1 = (U3IP - U3IM) * 0.5 * DX1;
+                double DV1DX3 = (U1KP - U1KM) * 0.5 * DX3;
+                double DV2DX1 = (U2IP - U2IM) * 0.5 * DX1;
+                double DV1DX2 = (U12 - U11) / DY[J];
+                vor(I, J, K, 1) = DV3DX2 - DV2DX3;
+                vor(I, J, K, 2) = DV1DX3 - DV3DX1;
+                vor(I, J, K, 3) = DV2DX1 - DV1DX2;
+            }
+        }
+    }
+    for (int J = 1; J <= N2M; J++) {   // loops 20, 21 and 40
+        const int JP = J + 1, JM = J - 1;
+        double s[23] = {0.0};
+        for (int K = 1; K <= N3M; K++) {
+            const int KP = g.KPA[K];
+            for (int I = 1; I <= N1M; I++) {
+                const int IP = g.IPA[I];
+                double V1 = (u(I, J, K, 1) + u(IP, J, K, 1)) * 0.5;
+                double V2 = (u(I, J, K, 2) + u(I, JP, K, 2)) * 0.5;
+                double V3 = (u(I, J, K, 3) + u(I, J, KP, 3)) * 0.5;
+                const double PP = p(I, J, K);
+                s[0] = s[0] + V1; s[1] = s[1] + V2; s[2] = s[2] + V3; s[3] = s[3] + PP;
+                s[4] = s[4] + vor(I, J, K, 1); s[5] = s[5] + vor(I, J, K, 2); s[6] = s[6] + vor(I, J, K, 3);
+                s[7] = s[7] + V1 * V1; s[8] = s[8] + V2 * V2; s[9] = s[9] + V3 * V3;
+                s[10] = s[10] + V1 * V2; s[11] = s[11] + V1 * V3; s[12] = s[12] + V2 * V3;
+                s[13] = s[13] + PP * PP; s[14] = s[14] + PP * V2;
+                s[15] = s[15] + vor(I, J, K, 1) * vor(I, J, K, 1);
+                s[16] = s[16] + vor(I, J, K, 2) * vor(I, J, K, 2);
+                s[17] = s[17] + vor(I, J, K, 3) * vor(I, J, K, 3);
+                s[18] = s[18] + V1 * V1 * V2;
+                s[19] = s[19] + V2 * V3 * V3;
+            }
+        }
+        double *o = out + (size_t)(J - 1) * 29;
+        for (int q = 0; q < 20; ++q) o[q] = s[q] * NXZ;
+        double sk[6] = {0.0};
+        for (int K = 1; K <= N3M; K++) {
+            const int KP = g.KPA[K];
+            for (int I = 1; I <= N1M; I++) {
+                const int IP = g.IPA[I];
+                double V1 = (u(I, J, K, 1) + u(IP, J, K, 1)) * 0.5 - o[0];
+                double V2 = (u(I, J, K, 2) + u(I, JP, K, 2)) * 0.5 - o[1];
+                double V3 = (u(I, J, K, 3) + u(I, J, KP, 3)) * 0.5 - o[2];
+                sk[0] = sk[0] + V1 * V1 * V1; sk[1] = sk[1] + V2 * V2 * V2; sk[2] = sk[2] + V3 * V3 * V3;
+                sk[3] = sk[3] + V1 * V1 * V1 * V1; sk[4] = sk[4] + V2 * V2 * V2 * V2; sk[5] = sk[5] + V3 * V3 * V3 * V3;
+            }
+        }
+        for (int q = 0; q < 6; ++q) o[20 + q] = sk[q] * NXZ;
+        const double FJUM = g.FJMU[J], FJUP = g.FJPA[J];
+        double du = 0.0, dv = 0.0, dw = 0.0;
+        for (int K = 1; K <= N3M; K++) {
+            const int KP = g.KPA[K];
+            for (int I = 1; I <= N1M; I++) {
+                const int IP = g.IPA[I];
+                double U_JP = (u(I, JP, K, 1) + u(IP, JP, K, 1)) * 0.5;
+                double U_JC = (u(I, J, K, 1) + u(IP, J, K, 1)) * 0.5;
+                double U_JM = (u(I, JM, K, 1) + u(IP, JM, K, 1)) * 0.5;
+                double W_JP = (u(I, JP, K, 3) + u(I, JP, KP, 3)) * 0.5;
+                double W_JC = (u(I, J, K, 3) + u(I, J, KP, 3)) * 0.5;
+                double W_JM = (u(I, JM, K, 3) + u(I, JM, KP, 3)) * 0.5;
+                double U1 = FJUM * (1.0 / H[J] * (DY[J] * U_JM / 2.0 + DY[JM] * U_JC / 2.0)) +
+                            (1. - FJUM) * (u(I, 0, K, 1) + u(IP, 0, K, 1)) * 0.5;
+                double U2 = FJUP * (1.0 / H[JP] * (DY[J] * U_JP / 2.0 + DY[JP] * U_JC / 2.0)) +
+                            (1. - FJUP) * (u(I, N2, K, 1) + u(IP, N2, K, 1)) * 0.5;
+                double V1 = u(I, J, K, 2), V2 = u(I, JP, K, 2);
+                double W1 = FJUM * (1.0 / H[J] * (DY[J] * W_JM / 2.0 + DY[JM] * W_JC / 2.0)) +
+                            (1. - FJUM) * (u(I, 0, K, 3) + u(I, 0, KP, 3)) * 0.5;
+                double W2 = FJUP * (1.0 / H[JP] * (DY[J] * W_JP / 2.0 + DY[JP] * W_JC / 2.0)) +
+                            (1. - FJUP) * (u(I, N2, K, 3) + u(I, N2, KP, 3)) * 0.5;
+                du = du + (U2 - U1) / DY[J];
+                dv = dv + (V2 - V1) / DY[J];
+                dw = dw + (W2 - W1) / DY[J];
+            }
+        }
+        o[26] = du * NXZ;
+        o[27] = dv * NXZ;
+        o[28] = dw * NXZ;
+    }
+}
+
 // ---- unit-level entry points ----
 // CTDMA11 on one line with constant coefficients (a,b,c); d,x 0-based length n.
 void orc_ctdma11(int n, double a, double b, double c, const double *d, double *x) {

@@ -173,3 +173,27 @@ def test_flow_rate_conserved_turbulent_start(oracle_mod):
         pg, pg3 = orc.getup(U, P, HH, n, dt, pg, pg3)
         assert orc.divcheck(U) < 1e-11
     assert orc.chkmf(U)[0] == pytest.approx(f0, rel=1e-11)
+
+
+def test_plane_stats_laminar_profile(oracle_mod):
+    """ENERGY's plane statistics of a laminar profile u = U(y), v = w = 0: the moments of a
+    constant plane (uu = u^2, central moments 0), wz = -dU/dy at the cell centres with
+    ENERGY's interpolants, and pressure statistics of a plane-constant P."""
+    from compact3d_gb300.grid import make_grid
+    g, _ = make_grid("small32")
+    o = oracle_mod.Oracle(g)
+    U = g.zeros_u()
+    y = g.arrays["y"]
+    yc = 0.5 * (y[1:g.n2m + 1] + y[2:g.n2m + 2])
+    for j in range(0, g.n2m + 2):
+        yy = yc[j - 1] if 1 <= j <= g.n2m else (y[1] if j == 0 else y[g.n2m + 1])
+        U[:, j, :, 0] = yy * (2.0 - yy)
+    P = g.zeros_p()
+    P[:, :g.n2m, :] = np.arange(g.n2m)[None, :, None] * 0.1
+    s = o.plane_stats(U, P)
+    u = s[:, 0]
+    np.testing.assert_allclose(s[:, 7], u * u, rtol=1e-13)
+    assert np.abs(s[:, [1, 2, 8, 9, 10, 11, 12, 18, 19, 20, 21, 22, 23, 24, 25]]).max() < 1e-20
+    np.testing.assert_allclose(s[:, 6], -s[:, 26], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(s[:, 3], np.arange(g.n2m) * 0.1, atol=1e-15)
+    np.testing.assert_allclose(s[:, 13], (np.arange(g.n2m) * 0.1) ** 2, atol=1e-15)
