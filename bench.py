@@ -408,6 +408,10 @@ def run_ours(args, D: Dist):
     if not args.no_ops:
         res["operators"] = run_operators(args, D)
 
+    # ---- the rows after the step: plane statistics, checkpoint, a second wall model ----
+    if not args.no_next:
+        res["next_rows"] = run_next(args, D, g, dt, U0, P0, HH0)
+
     # ---- CPU baseline (rank 0, N=1 only) ----
     if D.rank == 0 and D.world == 1 and not args.no_cpu:
         rate, cores, sample = cpu_reference(args.workload, steps=3, warmup=1, budget_s=40.0)
@@ -475,6 +479,70 @@ def error_study(lib, g, dt, U0, P0, HH0, steps: int, floor: bool = True):
         out[name]["wsm_rel"] = abs(out[name]["wsm"] - float(diags["fp64"]["wsm"][0])) / abs(float(diags["fp64"]["wsm"][0]))
     out["fp64"] = dict(divmax=diags["fp64"]["divmax"], bulk=diags["fp64"]["flow1"] / g.aly,
                        wsm=float(diags["fp64"]["wsm"][0]), presg=presg["fp64"][0])
+    return out
+
+
+def run_next(args, D: Dist, g, dt, U0, P0, HH0):
+    """ENERGY's plane statistics and a checkpoint write + read on the main workload (mixed
+    form), and the LES step with WALLMODEL_WERNER on les128 (mixed form)."""
+    import shutil
+    import tempfile
+    from compact3d_gb300 import lib
+    out = {}
+    ch = make_channel(lib, g, "mixed", U0, P0, HH0)
+    ch.step(1, dt, 0.0, 0.0)
+    ch.plane_stats()
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ch.plane_stats()
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    # two passes over the plane: u, v, w, P (double-float) and u, v, w again
+    alg = 7 * 8.0 * g.points
+    out["plane_stats"] = dict(ms_per_call=ms, alg_bytes=alg, gbs=alg / ms / 1e6, values_per_plane=29,
+                              note="FP64 arithmetic on the double-float state; host-timed call incl. copy-out")
+    d = tempfile.mkdtemp(prefix="c3d_ckpt_")
+    try:
+        path = os.path.join(d, "ckpt.bin")
+        t0 = time.perf_counter()
+        ch.checkpoint_write(path, 1, dt, 0.0, 0.0)
+        tw = time.perf_counter() - t0
+        nbytes = os.path.getsize(path)
+        r = lib.Channel(g, FORMS["mixed"])
+        t0 = time.perf_counter()
+        r.checkpoint_read(path)
+        tr = time.perf_counter() - t0
+        r.close()
+        out["checkpoint"] = dict(bytes=nbytes, write_ms=tw * 1e3, read_ms=tr * 1e3,
+                                 write_gbs=nbytes / tw / 1e9, read_gbs=nbytes / tr / 1e9,
+                                 note="file in a temporary directory of the host; includes device packing, copies, fwrite/fread")
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    ch.close()
+    gl, dtl = make_grid("les128", wmodel=4)
+    Ul, Pl, Hl = ic.loglaw(gl, 2000.0, amp=0.05, seed=ic.SEED0 + 3000 + D.rank)
+    c = make_channel(lib, gl, "mixed", Ul, Pl, Hl)
+    if not args.no_tune:
+        c.autotune()
+    flush = L2Flush(D.local)
+    n = 1
+    for _ in range(max(3, args.warmup)):
+        c.step_async(n, dtl)
+        n += 1
+    c.sync()
+    K = args.steps
+    msl = 0.0
+    for _ in range(K):
+        flush()
+        c.timer_start()
+        c.step_async(n, dtl)
+        n += 1
+        msl += c.timer_stop()
+    msl = D.max(msl)
+    out["les_werner"] = dict(workload="les128, SGSCS + WALLMODEL_WERNER (WMODEL 4), mixed form, L2 flushed per step",
+                             value=D.sum(gl.points) * K / (msl / 1e3), unit=UNIT, ms_per_step=msl / K, steps=K,
+                             wsm=float(c.get_wsm()[0]))
+    c.close()
     return out
 
 
@@ -707,6 +775,7 @@ def main():
     ap.add_argument("--no-floor", action="store_true")
     ap.add_argument("--no-les", action="store_true")
     ap.add_argument("--no-ops", action="store_true")
+    ap.add_argument("--no-next", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--schedule", default="", help="JSON launch schedule for the main channel instead of autotuning")
     ap.add_argument("--les-steps", type=int, default=200)
