@@ -484,7 +484,8 @@ def error_study(lib, g, dt, U0, P0, HH0, steps: int, floor: bool = True):
 
 def run_next(args, D: Dist, g, dt, U0, P0, HH0):
     """ENERGY's plane statistics and a checkpoint write + read on the main workload (mixed
-    form), and the LES step with WALLMODEL_WERNER on les128 (mixed form)."""
+    form), and the LES step with the algebraic wall models WERNER, MARUSIC1 and PIOMELLI on
+    les128 (mixed form)."""
     import shutil
     import tempfile
     from compact3d_gb300 import lib
@@ -519,30 +520,32 @@ def run_next(args, D: Dist, g, dt, U0, P0, HH0):
     finally:
         shutil.rmtree(d, ignore_errors=True)
     ch.close()
-    gl, dtl = make_grid("les128", wmodel=4)
-    Ul, Pl, Hl = ic.loglaw(gl, 2000.0, amp=0.05, seed=ic.SEED0 + 3000 + D.rank)
-    c = make_channel(lib, gl, "mixed", Ul, Pl, Hl)
-    if not args.no_tune:
-        c.autotune()
-    flush = L2Flush(D.local)
-    n = 1
-    for _ in range(max(3, args.warmup)):
-        c.step_async(n, dtl)
-        n += 1
-    c.sync()
-    K = args.steps
-    msl = 0.0
-    for _ in range(K):
-        flush()
-        c.timer_start()
-        c.step_async(n, dtl)
-        n += 1
-        msl += c.timer_stop()
-    msl = D.max(msl)
-    out["les_werner"] = dict(workload="les128, SGSCS + WALLMODEL_WERNER (WMODEL 4), mixed form, L2 flushed per step",
-                             value=D.sum(gl.points) * K / (msl / 1e3), unit=UNIT, ms_per_step=msl / K, steps=K,
-                             wsm=float(c.get_wsm()[0]))
-    c.close()
+    for key, wm, label in (("les_werner", 4, "WALLMODEL_WERNER (WMODEL 4)"), ("les_marusic", 3, "MARUSIC1 (WMODEL 3)"),
+                           ("les_piomelli", 5, "PIOMELLI (WMODEL 5)")):
+        gl, dtl = make_grid("les128", wmodel=wm)
+        Ul, Pl, Hl = ic.loglaw(gl, 2000.0, amp=0.05, seed=ic.SEED0 + 3000 + D.rank)
+        c = make_channel(lib, gl, "mixed", Ul, Pl, Hl)
+        if not args.no_tune:
+            c.autotune()
+        flush = L2Flush(D.local)
+        n = 1
+        for _ in range(max(3, args.warmup)):
+            c.step_async(n, dtl)
+            n += 1
+        c.sync()
+        K = args.steps
+        msl = 0.0
+        for _ in range(K):
+            flush()
+            c.timer_start()
+            c.step_async(n, dtl)
+            n += 1
+            msl += c.timer_stop()
+        msl = D.max(msl)
+        out[key] = dict(workload=f"les128, SGSCS + {label}, mixed form, L2 flushed per step",
+                        value=D.sum(gl.points) * K / (msl / 1e3), unit=UNIT, ms_per_step=msl / K, steps=K,
+                        wsm=float(c.get_wsm()[0]))
+        c.close()
     return out
 
 

@@ -197,6 +197,10 @@ void free_channel(c3d_channel *ch) {
         if (e) cudaEventDestroy(e);
     if (ch->xfer) cudaFree(ch->xfer);
     if (ch->wtaue) cudaFree(ch->wtaue);
+    if (ch->wshift) cudaFree(ch->wshift);
+    if (ch->wfork) cudaEventDestroy(ch->wfork);
+    if (ch->wjoin) cudaEventDestroy(ch->wjoin);
+    if (ch->wside) cudaStreamDestroy(ch->wside);
     if (ch->stats) cudaFree(ch->stats);
     if (ch->hh_in) cudaEventDestroy(ch->hh_in);
     if (ch->hh_out) cudaEventDestroy(ch->hh_out);
@@ -290,6 +294,16 @@ int upload_ycn(c3d_channel *ch, double dt) {
     return 0;
 }
 
+// MARUSIC1's reference plane ZS (compact3d.f:4380-4385): the last J in 1..N2M whose Y(J)
+// is no farther from 0.06 than Y(J-1) and Y(J+1); 0 if there is none
+int marusic_plane(const double *y, int n2m) {
+    const double ZO = 0.06;
+    int zs = 0;
+    for (int j = 1; j <= n2m; ++j)
+        if (std::fabs(y[j] - ZO) <= std::fabs(y[j + 1] - ZO) && std::fabs(y[j] - ZO) <= std::fabs(y[j - 1] - ZO)) zs = j;
+    return zs;
+}
+
 int check_grid(const c3d_grid *g) {
     if (!g) { set_error("null grid"); return C3D_EINVAL; }
     const int n1m = g->n1 - 1, n2m = g->n2 - 1, n3m = g->n3 - 1;
@@ -322,9 +336,27 @@ int check_grid(const c3d_grid *g) {
         set_error("FILES must be 0 (DNS), 1 (SGSDY) or 2 (SGSCS); the scale-dependent model (3) is not built");
         return C3D_EINVAL;
     }
-    if (!(g->wmodel == 0 || g->wmodel == 1 || g->wmodel == 4)) {
-        set_error("WMODEL must be 0, 1 (WALLMODEL_INSTANT) or 4 (WALLMODEL_WERNER); the other wall models are not built");
+    if (!(g->wmodel == 0 || g->wmodel == 1 || g->wmodel == 3 || g->wmodel == 4 || g->wmodel == 5)) {
+        set_error("WMODEL must be 0, 1 (WALLMODEL_INSTANT), 3 (MARUSIC1), 4 (WALLMODEL_WERNER) or 5 (PIOMELLI); "
+                  "the other wall models are not built");
         return C3D_EINVAL;
+    }
+    if (g->wmodel == 3 || g->wmodel == 5) {
+        for (int j = 1; j <= n2m; ++j)
+            if (!(g->y[j + 1] > g->y[j])) {
+                set_error("WMODEL 3 / 5 (MARUSIC1 / PIOMELLI) search the Y faces: Y(1:N2) must increase");
+                return C3D_EINVAL;
+            }
+        if (g->wmodel == 3 && marusic_plane(g->y, n2m) < 1) {
+            set_error("WMODEL 3 (MARUSIC1) needs a plane J in 1..N2-1 whose Y(J) is nearest 0.06");
+            return C3D_EINVAL;
+        }
+        // PIOMELLI's bottom height H(1) climbs by about 1e-6 per wall point while it lies
+        // below YC(1); bound that climb (it is zero when Y(1) = 0)
+        if (g->wmodel == 5 && 0.5 * (g->y[2] + g->y[1]) - g->h[0] > 2e-3) {
+            set_error("WMODEL 5 (PIOMELLI) needs H(1) within 2e-3 of YC(1) = (Y(1) + Y(2)) / 2");
+            return C3D_EINVAL;
+        }
     }
     if (g->wmodel == 4 && n3m > n1m) {
         set_error("WMODEL 4 (WALLMODEL_WERNER) takes the x neighbour with the z index, so it needs N3-1 <= N1-1");
@@ -450,6 +482,24 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
             dalloc(&ch->ycs, (size_t)g.n2 + 1) || dalloc(&ch->wpart, 2 * (size_t)nbw))
             return fail(C3D_ENOMEM);
         if (gr->wmodel == 4 && dalloc(&ch->wtaue, 4 * (size_t)g.np)) return fail(C3D_ENOMEM);
+        if (gr->wmodel != 0 &&
+            (cudaStreamCreateWithFlags(&ch->wside, cudaStreamNonBlocking) != cudaSuccess ||
+             cudaEventCreateWithFlags(&ch->wfork, cudaEventDisableTiming) != cudaSuccess ||
+             cudaEventCreateWithFlags(&ch->wjoin, cudaEventDisableTiming) != cudaSuccess))
+            return fail(C3D_ECUDA);
+        if (gr->wmodel == 3 || gr->wmodel == 5) {
+            const size_t ny = (size_t)g.n2 + 1;
+            if (dalloc(&ch->wshift, c3d::wall_shift_doubles(g))) return fail(C3D_ENOMEM);
+            std::vector<double> yy(2 * ny, 0.0);
+            for (size_t j = 0; j < ny; ++j) yy[j] = gr->y[j];
+            yy[ny] = gr->y[0];
+            for (int j = 1; j <= g.n2m; ++j) yy[ny + j] = 0.5 * (gr->y[j + 1] + gr->y[j]);
+            yy[ny + g.n2] = gr->y[g.n2];
+            cudaMemcpy(ch->wshift, yy.data(), 2 * ny * 8, cudaMemcpyHostToDevice);
+            c3d::launch_wall_shift_init(ch);
+            ch->wzs = marusic_plane(gr->y, g.n2m);
+            ch->wtan16 = std::tan(16.0 * std::acos(-1.0) / 180);
+        }
         if (cudaMalloc(&ch->coef, ((size_t)g.n2 + 1) * rs) != cudaSuccess ||
             cudaMalloc(&ch->d23r, ((size_t)g.n2 + 1) * rs) != cudaSuccess)
             return fail(C3D_ENOMEM);

@@ -92,6 +92,11 @@ enum {
     SCAL_COUNT = 17
 };
 
+// the shifted-point wall models' scratch: per wall U_ave, UTAU2, TAUW1, CC, DELTS, nfix
+// (WS_NPAR slots) and WS_TABN heights YP (the grid check bounds their drift)
+constexpr int WS_NPAR = 8;
+constexpr int WS_TABN = 4096;
+
 // Launch schedule of one channel, chosen by c3d_autotune per grid shape.
 //   zl   z-line segment length of each z pass (zA, zB, zC, zD, zE): each thread runs the
 //        recurrences sequentially over zl points (plus the warm-up), the N3M/zl segments
@@ -158,6 +163,16 @@ struct c3d_channel {
     bool hh_hooks = false;
     double *xfer = nullptr;   // DMA staging area of pinned host arrays (one slot per field)
     double *wtaue = nullptr;  // WALLMODEL_WERNER: TAUWE(I,K,1..4) at the cell centres (4 x N1M N3M)
+    // MARUSIC1 / PIOMELLI: Y(0:N2), YC(0:N2), per-wall constants and YP heights; the
+    // reference plane ZS of MARUSIC1 (the Y(J) nearest 0.06) and tan(16 deg)
+    double *wshift = nullptr;
+    // the wall model runs on its own stream beside the SGS model and the RHS passes: forked
+    // after the last reader of WSM, joined before the first reader of TAUW/TAUB
+    cudaStream_t wside = nullptr;
+    cudaEvent_t wfork = nullptr, wjoin = nullptr;
+    int wjoin_pending = 0;
+    int wzs = 0;
+    double wtan16 = 0.0;
     double *stats = nullptr;  // plane statistics table and partial sums (allocated on first use)
     cudaStream_t cs = nullptr;          // copy stream of the DMA transfers
     cudaEvent_t xev[16] = {};           // per-field hand-offs between the copy and compute streams
@@ -252,6 +267,18 @@ int launch_repack(c3d_channel *ch, int dir, int what, int comp, double *fort = n
 void set_error(const std::string &msg);
 // Records a kernel-boundary mark for the profiler and counts the launch.
 void mark(c3d_channel *ch, int *nl, const char *name, double bytes);
+// returns C3D_ECUDA with the failing call named when a CUDA runtime call fails
+#define CK_RC(call)                                                                     \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));             \
+            return C3D_ECUDA;                                                           \
+        }                                                                               \
+    } while (0)
+// the shifted-point wall models' scratch: its size in doubles and the mesh tables
+size_t wall_shift_doubles(const Geo &g);
+void launch_wall_shift_init(c3d_channel *ch);
 void prof_begin(c3d_channel *ch);
 int prof_collect(c3d_channel *ch);
 }  // namespace c3d

@@ -310,6 +310,9 @@ __global__ void __launch_bounds__(TPB) k_wall(StepArgs<R> a, LesArgs<R> l) {
         const double DELTAP = g.dy[1] + g.dy[2] + g.dy[3] / 2.0;
         const double uave = sqrt(u3 * u3 + w3 * w3);
         double ut1 = 1.0, ut2 = 0.000001, lambda = 1.0;
+        // f(ut1) of an iteration is f(ut2) of the one before (same expression, same
+        // argument), so each iteration evaluates the log law once
+        double f3 = uave / ut2 - log(ut2 * DELTAP * RE) / KAPA - B;
         int it = 0;
         while (fabs(ut2 - ut1) > 1.0e-6) {
             if (++it > l.wall_cap) {
@@ -317,10 +320,10 @@ __global__ void __launch_bounds__(TPB) k_wall(StepArgs<R> a, LesArgs<R> l) {
                 break;
             }
             ut1 = ut2;
-            const double f1 = uave / ut1 - log(ut1 * DELTAP * RE) / KAPA - B;
+            const double f1 = f3;
             const double f2 = -uave / (ut1 * ut1) - 1.0 / KAPA / ut1;
             ut2 = ut1 - lambda * f1 / f2;
-            const double f3 = uave / ut2 - log(ut2 * DELTAP * RE) / KAPA - B;
+            f3 = uave / ut2 - log(ut2 * DELTAP * RE) / KAPA - B;
             if (fabs(f3) > fabs(f1)) lambda = 0.5 * lambda;
         }
         tw1 = ut1 * ut1;
@@ -407,6 +410,341 @@ __global__ void __launch_bounds__(TPB) k_wall_werner_avg(StepArgs<R> a, LesArgs<
         l.tauw[wall * g.np + e] = 0.5 * (tu[e] + tu[ei]);
         l.taub[wall * g.np + e] = 0.5 * (tw[e] + tw[ek]);
     }
+}
+
+// ---------------------------------------------------------------------------------
+// The shifted-point models, FP64: MARUSIC1 (WMODEL 3, compact3d.f:4336-4495) and PIOMELLI
+// (WMODEL 5, 4960-5110).  u_tau of each wall from the log law on the plane mean of u at a
+// reference plane (bisection), then per wall point the velocity interpolated trilinearly
+// (INTERPOLAT, 12602-12760) at a point shifted downstream by DELTS (MARUSIC1: DELTAP /
+// tan 16 deg; PIOMELLI: 0, its DELTP is never set) at the height YP.  The mesh of MESH02
+// (uniform XG/ZG faces, cell centres XC/YC/ZC) is formed from the grid on the fly with
+// the reference's operation order and no contractions, so the cell search and the
+// interpolation weights are those of the FP64 restatement.
+//
+// The scratch ws (layout in WsMesh) holds Y(0:N2), YC(0:N2), per wall WS_NPAR parameters,
+// per wall the heights INDEX_IJK leaves in YP call after call, and XG, XC, ZG, ZC(0:N+1)
+// (formed once by k_wall_shift_init).  The reference moves YP up by about 1e-6 on every
+// call while it is below YC(1) (its arguments are by reference and YP is set once per
+// wall), so call c of a wall uses tab[min(c, nfix)].
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ double nudge_up(double x) {   // ANINT(X*1E06+0.5)/1E06
+    return __ddiv_rn(round(__dadd_rn(__dmul_rn(x, 1E06), 0.5)), 1E06);
+}
+__device__ __forceinline__ double nudge_dn(double x) {   // ANINT(X*1E06-0.5)/1E06
+    return __ddiv_rn(round(__dsub_rn(__dmul_rn(x, 1E06), 0.5)), 1E06);
+}
+// XG(I) of MESH02 on a uniform grid of n cells over [0, L], I = 1..n+1
+__device__ __forceinline__ double ws_face(int I, int n, double L) {
+    return I > n ? L : __ddiv_rn(__dmul_rn((double)(I - 1), L), (double)n);
+}
+// XC(I) = (XG(I+1) + XG(I)) / 2, XC(n+1) = L
+__device__ __forceinline__ double ws_ctr(int I, int n, double L) {
+    return I > n ? L : __dmul_rn(0.5, __dadd_rn(ws_face(I + 1, n, L), ws_face(I, n, L)));
+}
+// (B - A) / (HI - LO) * (X - LO) + A, rounded step by step
+__device__ __forceinline__ double ws_lerp(double A, double B, double LO, double HI, double X) {
+    return __dadd_rn(__dmul_rn(__ddiv_rn(__dsub_rn(B, A), __dsub_rn(HI, LO)), __dsub_rn(X, LO)), A);
+}
+
+struct WsMesh {
+    const double *Y, *YC, *XG, *XC, *ZG, *ZC;
+    const double *V1;  // V(I,1,K) as the step found it (BCOND zeroes it before the model ends)
+    double rx, rz;     // N1M / ALX, N3M / ALZ (first guesses of the x and z cells)
+    double ix1, ix3;   // 1 / DX1, 1 / DX3
+    __host__ __device__ static size_t off_par(const Geo &g) { return 2 * ((size_t)g.n2 + 1); }
+    __host__ __device__ static size_t off_tab(const Geo &g) { return off_par(g) + 2 * WS_NPAR; }
+    __host__ __device__ static size_t off_xg(const Geo &g) { return off_tab(g) + 2 * (size_t)WS_TABN; }
+    __host__ __device__ static size_t off_v1(const Geo &g) { return off_xg(g) + 2 * ((size_t)g.n1m + 2) + 2 * ((size_t)g.n3m + 2); }
+    __host__ __device__ static size_t size(const Geo &g) { return off_v1(g) + (size_t)g.np; }
+    __host__ static WsMesh of(const Geo &g, const double *ws) {
+        WsMesh m;
+        m.Y = ws;
+        m.YC = ws + g.n2 + 1;
+        m.XG = ws + off_xg(g);
+        m.XC = m.XG + g.n1m + 2;
+        m.ZG = m.XC + g.n1m + 2;
+        m.ZC = m.ZG + g.n3m + 2;
+        m.V1 = ws + off_v1(g);
+        m.rx = g.n1m / g.alx;
+        m.rz = g.n3m / g.alz;
+        m.ix1 = 1. / g.dx1;
+        m.ix3 = 1. / g.dx3;
+        return m;
+    }
+};
+
+// XG, XC (0:N1M+1) and ZG, ZC (0:N3M+1) of MESH02
+__global__ void k_wall_shift_init(Geo g, double *ws) {
+    double *XG = ws + WsMesh::off_xg(g), *XC = XG + g.n1m + 2, *ZG = XC + g.n1m + 2, *ZC = ZG + g.n3m + 2;
+    for (int I = threadIdx.x; I <= g.n1m + 1; I += blockDim.x) {
+        XG[I] = I == 0 ? 0.0 : ws_face(I, g.n1m, g.alx);
+        XC[I] = I == 0 ? 0.0 : ws_ctr(I, g.n1m, g.alx);
+    }
+    for (int K = threadIdx.x; K <= g.n3m + 1; K += blockDim.x) {
+        ZG[K] = K == 0 ? 0.0 : ws_face(K, g.n3m, g.alz);
+        ZC[K] = K == 0 ? 0.0 : ws_ctr(K, g.n3m, g.alz);
+    }
+}
+
+// PIOMELLI interpolates V between the faces J = 1 and 2 at the bottom wall; the step's
+// BCOND sets V(J=1) while the model may still run beside it, so the plane is copied first
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_wall_shift_v1(StepArgs<R> a, double *ws) {
+    typedef St<R> ST;
+    const Geo g = a.g;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < g.np) ws[WsMesh::off_v1(g) + e] = ST::dbl(a.v[(long long)g.np + e]);
+}
+
+// INDEX_IJK in one direction: the first cell I in 1..n with F(I) <= X <= F(I+1) of the
+// increasing faces F(1..n+1); r n / (F(n+1) - F(1)) gives the first guess
+__device__ __forceinline__ int ws_cell(double X, const double *F, int n, double r) {
+    if (!(X >= F[1] && X <= F[n + 1])) return -1;
+    int I = min(n, max(1, (int)((X - F[1]) * r) + 1));
+    while (I > 1 && X <= F[I]) --I;
+    while (I < n && X > F[I + 1]) ++I;
+    return (X >= F[I] && X <= F[I + 1]) ? I : -1;
+}
+
+// ... in y (non-uniform): bisection over Y(1..N2)
+__device__ __forceinline__ int ws_ycell(double YP, const double *Y, int n2m) {
+    int lo = 1, hi = n2m;   // the first J with YP <= Y(J+1)
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (YP <= Y[mid + 1]) hi = mid;
+        else lo = mid + 1;
+    }
+    return (YP >= Y[lo] && YP <= Y[lo + 1]) ? lo : -1;
+}
+
+// INTERPOLAT of component C (1 u at x faces, 2 v at y faces, 3 w at z faces) at
+// (XP, YP, ZP) in cell (IP, JP, KP), Fortran indices; JPA(N2M) = N2M and JMU(1) = 1.
+template <typename R>
+__device__ double ws_interp(const StepArgs<R> &a, const WsMesh &m, double XP, double YP, double ZP, int IP, int JP,
+                            int KP, int C) {
+    typedef St<R> ST;
+    const Geo &g = a.g;
+    const int n1 = g.n1m, n2m = g.n2m, n3 = g.n3m, N2 = g.n2;
+    int IUM, IUP, JUM, JUP, KUM, KUP;
+    double XUM, XUP, YUM, YUP, ZUM, ZUP;
+    const int IPA = IP == n1 ? 1 : IP + 1, IMA = IP == 1 ? n1 : IP - 1;
+    if (C == 1) {
+        IUM = IP; IUP = IPA; XUM = m.XG[IP]; XUP = m.XG[IUP];
+        if (IP == n1) XUP = m.XG[n1 + 1];
+    } else if (XP >= m.XC[IP]) {
+        IUM = IP; IUP = IPA; XUM = m.XC[IP]; XUP = m.XC[IUP];
+        if (IP == n1) XUP = __dadd_rn(m.XC[n1], m.ix1);
+    } else {
+        IUM = IMA; IUP = IP; XUM = m.XC[IUM]; XUP = m.XC[IP];
+        if (IP == 1) XUM = __dsub_rn(m.XC[1], m.ix1);
+    }
+    const int JPA = JP == n2m ? n2m : JP + 1, JMU = JP == 1 ? 1 : JP - 1;
+    if (C == 2) {
+        JUM = JP; JUP = JPA; YUM = m.Y[JP]; YUP = m.Y[JUP];
+        if (JP == n2m) YUP = m.YC[N2];
+    } else if (YP >= m.YC[JP]) {
+        JUM = JP; JUP = JPA; YUM = m.YC[JP]; YUP = m.YC[JUP];
+        if (JP == n2m) YUP = m.YC[N2];
+    } else {
+        JUM = JMU; JUP = JP; YUM = m.YC[JUM]; YUP = m.YC[JP];
+        if (JP == 1) YUM = m.Y[1];
+    }
+    const int KPA = KP == n3 ? 1 : KP + 1, KMA = KP == 1 ? n3 : KP - 1;
+    if (C == 3) {
+        KUM = KP; KUP = KPA; ZUM = m.ZG[KP]; ZUP = m.ZG[KUP];
+        if (KP == n3) ZUP = m.ZG[n3 + 1];
+    } else if (ZP >= m.ZC[KP]) {
+        KUM = KP; KUP = KPA; ZUM = m.ZC[KP]; ZUP = m.ZC[KUP];
+        if (KP == n3) ZUP = __dadd_rn(m.ZC[n3], m.ix3);
+    } else {
+        KUM = KMA; KUP = KP; ZUM = m.ZC[KUM]; ZUP = m.ZC[KP];
+        if (KP == 1) ZUM = __dsub_rn(m.ZC[1], m.ix3);
+    }
+    const typename StepArgs<R>::S *F = C == 1 ? a.u : (C == 2 ? a.v : a.w);
+    auto f = [&](int I, int J, int K) {
+        return C == 2 && J == 1 ? m.V1[(K - 1) * n1 + (I - 1)] : ST::dbl(F[fidx(g, I - 1, J, K - 1)]);
+    };
+    const double PHA = f(IUM, JUM, KUM), PHB = f(IUP, JUM, KUM), PHC = f(IUP, JUP, KUM), PHD = f(IUM, JUP, KUM);
+    const double PHE = f(IUM, JUM, KUP), PHF = f(IUP, JUM, KUP), PHG = f(IUP, JUP, KUP), PHH = f(IUM, JUP, KUP);
+    const double PHAB = ws_lerp(PHA, PHB, XUM, XUP, XP), PHCD = ws_lerp(PHD, PHC, XUM, XUP, XP);
+    const double PHEF = ws_lerp(PHE, PHF, XUM, XUP, XP), PHGH = ws_lerp(PHH, PHG, XUM, XUP, XP);
+    const double PHABCD = ws_lerp(PHAB, PHCD, YUM, YUP, YP), PHEFGH = ws_lerp(PHEF, PHGH, YUM, YUP, YP);
+    return ws_lerp(PHABCD, PHEFGH, ZUM, ZUP, ZP);
+}
+
+// per-block sums of u on the two reference planes (jd: bottom, ju: top)
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_wall_shift_mean(StepArgs<R> a, LesArgs<R> l, int jd, int ju) {
+    typedef St<R> ST;
+    const Geo g = a.g;
+    __shared__ double sd[TPB], su[TPB];
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double d = 0.0, u = 0.0;
+    if (e < g.np) {
+        const int i = e % g.n1m, k = e / g.n1m;
+        d = ST::dbl(a.u[fidx(g, i, jd, k)]);
+        u = ST::dbl(a.u[fidx(g, i, ju, k)]);
+    }
+    sd[threadIdx.x] = d;
+    su[threadIdx.x] = u;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sd[threadIdx.x] += sd[threadIdx.x + s];
+            su[threadIdx.x] += su[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        l.wpart[blockIdx.x] = sd[0];
+        l.wpart[gridDim.x + blockIdx.x] = su[0];
+    }
+}
+
+// The log-law bisection (compact3d.f:4390-4402, 5017-5029) run by one warp.  The reference
+// keeps an anchor end a = U_tau1 and the other end b = U_tau2 and, while |b - a| > 1e-7,
+// halves the bracket at m = b/2 + a/2 toward the sign change of f(a) f(m), returning a.
+// Each round here covers five of those steps: lane q (1..31) forms the bracket of node q
+// of the five-level decision tree with the same midpoint arithmetic and evaluates f at
+// its midpoint; the warp then walks the tree with the sequential rule.  Every midpoint
+// and every f value is the one the sequential loop computes (f(a) of a step is the f of
+// the midpoint that became a), so the result is the same.
+__device__ __forceinline__ double loglaw_f(double U_ave, double ut, double DELTAP, double RE) {
+    const double KAPA = 0.41, B = 5.2;
+    return U_ave / ut - log(ut * DELTAP * RE) / KAPA - B;
+}
+__device__ __forceinline__ double mid_rn(double a, double b) {
+    return __dadd_rn(__dmul_rn(0.5, b), __dmul_rn(0.5, a));
+}
+__device__ double ws_bisect_warp(double U_ave, double DELTAP, double RE, double a, double b) {
+    const int lane = threadIdx.x & 31;
+    double fa = loglaw_f(U_ave, a, DELTAP, RE);
+    const int depth = lane ? 31 - __clz(lane) : 0;
+    for (int round = 0; round < 64 && fabs(b - a) > 0.0000001; ++round) {
+        double na = a, nb = b;
+        for (int q = depth - 1; q >= 0; --q) {
+            const double m = mid_rn(na, nb);
+            if ((lane >> q) & 1) na = m;
+            else nb = m;
+        }
+        const double m = mid_rn(na, nb);
+        const double fm = lane ? loglaw_f(U_ave, m, DELTAP, RE) : 0.0;
+        int node = 1;
+        for (int q = 0; q < 5 && fabs(b - a) > 0.0000001; ++q) {
+            const double mm = __shfl_sync(FULL, m, node), fmm = __shfl_sync(FULL, fm, node);
+            if (fa * fmm <= 0.0) {
+                b = mm;
+                node = 2 * node;
+            } else {
+                a = mm;
+                fa = fmm;
+                node = 2 * node + 1;
+            }
+        }
+    }
+    return a;
+}
+
+// plane means, u_tau, the per-wall constants and the YP heights; one block of 256
+template <typename R>
+__global__ void k_wall_shift_fin(StepArgs<R> a, LesArgs<R> l, int nb, double *ws, int zs, double tan16) {
+    const Geo g = a.g;
+    __shared__ double s[256], b[256];
+    double x = 0.0, y = 0.0;
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+        x += l.wpart[q];
+        y += l.wpart[nb + q];
+    }
+    s[threadIdx.x] = x;
+    b[threadIdx.x] = y;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            s[threadIdx.x] += s[threadIdx.x + w];
+            b[threadIdx.x] += b[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    const int wall = threadIdx.x >> 5;   // warp 0: bottom wall, warp 1: top wall
+    if (wall >= 2) return;
+    const double *YC = ws + (g.n2 + 1);
+    double *par = ws + WsMesh::off_par(g) + WS_NPAR * wall;
+    double *tab = ws + WsMesh::off_tab(g) + (size_t)WS_TABN * wall;
+    const double U_ave = (wall == 0 ? s[0] : b[0]) / (double)(g.n1m * g.n3m);
+    const bool mar = l.wmodel == 3;
+    double DELTAP, UTAU2, CC = 1.0, DELTS, YP;
+    if (mar) {
+        DELTAP = YC[zs];
+        UTAU2 = ws_bisect_warp(U_ave, DELTAP, g.re, 1.0, 0.000001);
+        const double YPLUSML = DELTAP * UTAU2 * g.re, YPLUS1 = g.dy[1] / 2.0 * UTAU2 * g.re;
+        const double lg = log(YPLUS1 / YPLUSML);
+        CC = __dadd_rn(1.0, __dmul_rn(0.05, __dmul_rn(lg, lg)));
+        DELTS = DELTAP / tan16;
+        YP = wall == 0 ? DELTAP : YC[g.n2m - zs + 1];
+    } else {
+        DELTAP = (wall == 0 ? g.dy[1] : g.dy[g.n2m]) / 2.0;
+        UTAU2 = ws_bisect_warp(U_ave, DELTAP, g.re, 0.000001, 0.2);
+        DELTS = 0.0;
+        YP = wall == 0 ? g.h[1] : YC[g.n2m];
+    }
+    if ((threadIdx.x & 31) != 0) return;
+    const double TAUW1 = UTAU2 * UTAU2;
+    // YP after each INDEX_IJK call until a call leaves it unchanged
+    int nfix = 0;
+    for (;; ++nfix) {
+        double yn = YP;
+        if (yn < YC[1]) yn = nudge_up(yn);
+        if (yn > YC[g.n2m]) yn = nudge_dn(yn);
+        const bool moved = yn != YP;
+        YP = yn;
+        tab[nfix] = YP;
+        if (!moved || nfix == WS_TABN - 1) break;
+    }
+    par[0] = U_ave;
+    par[1] = UTAU2;
+    par[2] = TAUW1;
+    par[3] = CC;
+    par[4] = DELTS;
+    par[5] = (double)nfix;
+    if (wall == 0) {
+        a.scal[SCAL_WSMC] = TAUW1;
+        a.scal[SCAL_WALLERR] = 0.0;
+    }
+}
+
+// TAUW and TAUB of one wall point per thread (2 N1M N3M threads: wall-major)
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_wall_shift(StepArgs<R> a, LesArgs<R> l, const double *ws, WsMesh m) {
+    const Geo g = a.g;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * g.np) return;
+    const int wall = t / g.np, e = t - wall * g.np;
+    const int I = e % g.n1m + 1, K = e / g.n1m + 1;
+    const double *par = ws + WsMesh::off_par(g) + WS_NPAR * wall;
+    const double *tab = ws + WsMesh::off_tab(g) + (size_t)WS_TABN * wall;
+    const double U_ave = par[0], UTAU2 = par[1], TAUW1 = par[2], CC = par[3], DELTS = par[4];
+    const int nfix = (int)par[5];
+    const bool mar = l.wmodel == 3;
+    const long long call = 2LL * ((long long)(I - 1) * g.n3m + (K - 1));   // I outer, K inner
+    auto point = [&](double XP, double ZP, long long c, int C) -> double {
+        if (XP > g.alx) XP = __dsub_rn(XP, g.alx);
+        if (XP < m.XC[1]) XP = nudge_up(XP);
+        if (XP > m.XC[g.n1m]) XP = nudge_dn(XP);
+        if (ZP < m.ZC[1]) ZP = nudge_up(ZP);
+        if (ZP > m.ZC[g.n3m]) ZP = nudge_dn(ZP);
+        const double YP = tab[c < nfix ? c : nfix];
+        const int IP = ws_cell(XP, m.XG, g.n1m, m.rx), KP = ws_cell(ZP, m.ZG, g.n3m, m.rz);
+        const int JP = ws_ycell(YP, m.Y, g.n2m);
+        if (IP < 0 || JP < 0 || KP < 0) return __longlong_as_double(0x7ff8000000000000LL);   // NaN
+        return ws_interp(a, m, XP, YP, ZP, IP, JP, KP, C);
+    };
+    const double F = point(__dadd_rn(m.XG[I], DELTS), m.ZC[K], call, mar ? 1 : 2);
+    const double TW = mar ? __dadd_rn(TAUW1, __dmul_rn(__dmul_rn(__dmul_rn(CC, 0.1), UTAU2), __dsub_rn(F, U_ave)))
+                          : __dadd_rn(TAUW1, __dmul_rn(__dmul_rn(0.1, UTAU2), F));
+    const double WF = point(__dadd_rn(m.XC[I], DELTS), m.ZG[K], call + 1, 3);
+    l.tauw[wall * g.np + e] = TW;
+    l.taub[wall * g.np + e] = __dmul_rn(TAUW1, WF) / U_ave;
 }
 
 template <typename R>
@@ -773,6 +1111,12 @@ static void launch_les_x(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int whi
     }
 }
 
+void launch_wall_shift_init(c3d_channel *ch) {
+    k_wall_shift_init<<<1, 256, 0, ch->stream>>>(ch->g, ch->wshift);
+}
+
+size_t wall_shift_doubles(const Geo &g) { return WsMesh::size(g); }
+
 template <typename R>
 int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *nl) {
     cudaStream_t st = ch->stream;
@@ -780,33 +1124,70 @@ int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *n
     const double N = (double)g.n1m * g.n2m * g.n3m, Rb = sizeof(R);
     if (stage == 0) {
         if (g.n2m < 1) return C3D_EINVAL;
+        if (ch->wjoin_pending) {   // a step that stopped between the fork and the join
+            CK_RC(cudaStreamWaitEvent(st, ch->wjoin, 0));
+            ch->wjoin_pending = 0;
+        }
         if (ch->files != 0 && ch->wmodel == 0) {
             k_les_wallss<R><<<1, 256, 0, st>>>(a);
             mark(ch, nl, "les_wallss", 64.0 * g.np);
         }
+        // The wall model reads the state and WSM and writes TAUW, TAUB and WSM(1); the SGS
+        // model reads WSM (SGSCS's coefficient) and the state, so it runs on a side stream
+        // forked after k_sgs_coef and joined before k_les_x2, the first reader of TAUW/TAUB.
+        // Of the planes BCOND writes (0, N2 and V at J = 1) the models read only V(J=1)
+        // (PIOMELLI), from a copy taken on the main stream before the fork.
+        const bool fork = ch->wside && !ch->prof_on && ch->files != 0 && ch->wmodel != 0;
+        const cudaStream_t wst = fork ? ch->wside : st;
+        auto wall_model = [&]() -> int {
+            if (ch->files != 0 && ch->wmodel == 5) {
+                k_wall_shift_v1<R><<<nblk(g.np), TPB, 0, st>>>(a, ch->wshift);
+                *nl += 1;
+            }
+            if (fork) {
+                CK_RC(cudaEventRecord(ch->wfork, st));
+                CK_RC(cudaStreamWaitEvent(wst, ch->wfork, 0));
+            }
+            if (ch->files != 0 && ch->wmodel == 1) {
+                const int nb = nblk(g.np);
+                k_wall<R><<<nb, TPB, 0, wst>>>(a, l);
+                k_wall_sum<R><<<1, 256, 0, wst>>>(a, l, nb);
+                mark(ch, nl, "wall", 32.0 * g.np);
+            } else if (ch->files != 0 && ch->wmodel == 4) {
+                const int nb = nblk(g.np);
+                k_wall_werner<R><<<nb, TPB, 0, wst>>>(a, l, ch->wtaue);
+                k_wall_sum<R><<<1, 256, 0, wst>>>(a, l, nb);
+                k_wall_werner_avg<R><<<nb, TPB, 0, wst>>>(a, l, ch->wtaue);
+                *nl += 2;
+                mark(ch, nl, "wall", 96.0 * g.np);
+            } else if (ch->files != 0 && (ch->wmodel == 3 || ch->wmodel == 5)) {
+                const int nb = nblk(g.np);
+                const int jd = ch->wmodel == 3 ? ch->wzs : 1, ju = ch->wmodel == 3 ? g.n2m - ch->wzs + 1 : g.n2m;
+                k_wall_shift_mean<R><<<nb, TPB, 0, wst>>>(a, l, jd, ju);
+                k_wall_shift_fin<R><<<1, 256, 0, wst>>>(a, l, nb, ch->wshift, ch->wzs, ch->wtan16);
+                k_wall_shift<R><<<nblk(2LL * g.np), TPB, 0, wst>>>(a, l, ch->wshift, WsMesh::of(g, ch->wshift));
+                *nl += 2;
+                // per wall point: u on two planes, eight corners of two components, two stresses
+                const double Sb = sizeof(typename StepArgs<R>::S);
+                mark(ch, nl, "wall", (2.0 * Sb + 2 * (16 * Sb + 16)) * g.np);
+            }
+            if (fork) CK_RC(cudaEventRecord(ch->wjoin, wst));
+            return 0;
+        };
+        int rc = 0;
         if (ch->files == 2) {
             k_sgs_coef<R><<<1, 128, 0, st>>>(a, l);
+            if ((rc = wall_model())) return rc;
             k_sgs_cs<R><<<nblk((long long)g.n2m * g.np), TPB, 0, st>>>(a, l);
             mark(ch, nl, "sgs_cs", N * (6 * 8 + Rb));
         } else if (ch->files == 1) {
+            if ((rc = wall_model())) return rc;
             k_sgs_raw<R><<<nblk((long long)g.n2m * g.np), TPB, 0, st>>>(a, l);
             mark(ch, nl, "sgs_raw", N * (6 * 8 + 22 * Rb));
             k_sgs_dyn<R><<<g.n2m, 256, 0, st>>>(a, l);
             mark(ch, nl, "sgs_dyn", N * 23 * Rb);
         }
-        if (ch->files != 0 && ch->wmodel == 1) {
-            const int nb = nblk(g.np);
-            k_wall<R><<<nb, TPB, 0, st>>>(a, l);
-            k_wall_sum<R><<<1, 256, 0, st>>>(a, l, nb);
-            mark(ch, nl, "wall", 32.0 * g.np);
-        } else if (ch->files != 0 && ch->wmodel == 4) {
-            const int nb = nblk(g.np);
-            k_wall_werner<R><<<nb, TPB, 0, st>>>(a, l, ch->wtaue);
-            k_wall_sum<R><<<1, 256, 0, st>>>(a, l, nb);
-            k_wall_werner_avg<R><<<nb, TPB, 0, st>>>(a, l, ch->wtaue);
-            *nl += 2;
-            mark(ch, nl, "wall", 96.0 * g.np);
-        }
+        if (fork) ch->wjoin_pending = 1;
         return 0;
     }
     switch ((g.n1m + 31) / 32) {
@@ -824,6 +1205,10 @@ int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *n
     mark(ch, nl, "les_z1", N * (24 + 7 * Rb));
     k_les_z2<R, ZL><<<nblk(nz), TPB, 0, st>>>(a, l);
     mark(ch, nl, "les_z2", N * (16 + 12 * Rb));
+    if (ch->wjoin_pending) {   // TAUW/TAUB of this step's wall model
+        CK_RC(cudaStreamWaitEvent(st, ch->wjoin, 0));
+        ch->wjoin_pending = 0;
+    }
     switch ((g.n1m + 31) / 32) {
         case 1: launch_les_x<R, 1>(ch, a, l, 1, nl); break;
         case 2: launch_les_x<R, 2>(ch, a, l, 1, nl); break;

@@ -19,15 +19,6 @@
 #include <vector>
 #include "c3d_kern.cuh"
 
-#define CK_RC(call)                                                                     \
-    do {                                                                                \
-        cudaError_t e_ = (call);                                                        \
-        if (e_ != cudaSuccess) {                                                        \
-            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));             \
-            return C3D_ECUDA;                                                           \
-        }                                                                               \
-    } while (0)
-
 namespace c3d {
 
 int launch_ptables(c3d_channel *ch, const double *ak1, const double *ak3, const double *pm, const double *pc,

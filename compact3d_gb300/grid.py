@@ -239,5 +239,5 @@ def make_grid(name: str, precision: int = C3D_FP64, **over) -> tuple[Grid, float
     dt = w.pop("dt")
     g = Grid(n1m=w["n1m"], n2m=w["n2m"], n3m=w["n3m"], alx=w["alx"], aly=w["aly"],
              alz=w["alz"], re=w["re"], cks=w.get("cks", 2.5), wmodel=w.get("wmodel", 0),
-             files=w.get("files", 0), precision=precision)
+             files=w.get("files", 0), precision=precision, y0=w.get("y0", 0.0))
     return g, dt

@@ -64,10 +64,12 @@ extern "C" {
  *   /PARA/  RE                             -> re
  *   /FINOUT/ FILES (SGS model)             -> files  (0 none, 1 SGSDY, 2 SGSCS)
  *   /WALLMODEL/ WMODEL                     -> wmodel (0 none, 1 WALLMODEL_INSTANT,
- *                                             4 WALLMODEL_WERNER; with 1, Y(0) must
- *                                             be 0: Y0 != 0 selects the rough-wall
- *                                             model, which is not built; 4 needs
- *                                             N3 <= N1, see below)
+ *                                             3 MARUSIC1, 4 WALLMODEL_WERNER,
+ *                                             5 PIOMELLI; with 1, Y(0) must be 0:
+ *                                             Y0 != 0 selects the rough-wall model,
+ *                                             which is not built; 4 needs N3 <= N1;
+ *                                             3 and 5 need Y(1:N2) increasing, see
+ *                                             below)
  * The library takes the driver's metric arrays as given; it recomputes only
  * the Poisson metrics of INIWAVE / METRICPOISSON (compact3d.f:9182-9263),
  * which depend on nothing else.
@@ -122,8 +124,7 @@ int c3d_set_device(int device);
  *               upload, step, download in one call.
  *
  * LES (files != 0, compact3d.f:931-937): each step zeroes SGSVIS and runs the SGS
- * model (SGSDY or SGSCS) and, with wmodel = 1 or 4, WALLMODEL_INSTANT or
- * WALLMODEL_WERNER before BCOND; the
+ * model (SGSDY or SGSCS) and, with wmodel != 0, the wall model before BCOND; the
  * SGS fluxes and the wall-stress terms enter RHS1-3.  SGSVIS passed to c3d_upload
  * is not used (the step recomputes it); c3d_download / c3d_getup return it.  With
  * wmodel = 0 the step first evaluates WALLSS on the current field, which is what the
@@ -134,11 +135,21 @@ int c3d_set_device(int device);
  * 4815-4958) sets both walls' stresses from the Werner-Wengle power law and WSM(1)
  * from the bottom wall; like the reference it takes the x neighbour of a wall point
  * with the z index (IPA(K), IMA(K)), which the reference's index arrays allow only for
- * N3 <= N1, so c3d_create refuses wmodel = 4 on other grids.
+ * N3 <= N1, so c3d_create refuses wmodel = 4 on other grids.  MARUSIC1 (wmodel 3,
+ * compact3d.f:4336-4495) and PIOMELLI (wmodel 5, 4960-5110) take u_tau of each wall
+ * from the log law on the plane mean of u at a reference plane (MARUSIC1: the Y(J)
+ * nearest 0.06; PIOMELLI: the first cell) by the reference's bisection, and set both
+ * walls' stresses from the velocity interpolated trilinearly at a point shifted
+ * downstream (MARUSIC1: by DELTAP / tan 16 deg; PIOMELLI: not shifted, its DELTP is
+ * never set); WSM(1) is the bottom wall's u_tau^2.  They search the Y faces for the
+ * interpolation cell, so Y(1:N2) must increase; PIOMELLI's height H(1) climbs by 1e-6
+ * per wall point while it lies below YC(1), as the reference's by-reference INDEX_IJK
+ * does, and c3d_create refuses grids where it starts more than 2e-3 below.
  * c3d_upload_wall / c3d_download_wall  TAUW, TAUB (0:M1,0:M3,2) of /TAUXYZ/ (the
  *               interior I = 1..N1M, K = 1..N3M of both walls; either may be NULL).
- *               The wall model updates the bottom wall (index 1); the top wall keeps
- *               what was uploaded, as in the reference.
+ *               WALLMODEL_INSTANT updates the bottom wall (index 1) and the top
+ *               wall keeps what was uploaded, as in the reference; WERNER, MARUSIC1
+ *               and PIOMELLI update both walls.
  * c3d_set_wsm / c3d_get_wsm  /WSMEM/ WSM(1:3) as the SGS model reads it and the
  *               wall model writes WSM(1).
  */

@@ -180,8 +180,9 @@ class Oracle:
         return X
 
     def wallmodel(self, U):
-        """The grid's wall model (WMODEL 1: WALLMODEL_INSTANT, 4: WALLMODEL_WERNER) on U;
-        returns the status (0, or -4 if an INSTANT point hit the iteration cap)."""
+        """The grid's wall model (WMODEL 1: WALLMODEL_INSTANT, 3: MARUSIC1, 4:
+        WALLMODEL_WERNER, 5: PIOMELLI) on U; returns the status (0, -4 if an INSTANT point
+        hit the iteration cap, -1 if a shifted point found no cell)."""
         return lib().orc_wallmodel(self.h, _p(U))
 
     def set_wall(self, tauw=None, taub=None, ifwall=0):

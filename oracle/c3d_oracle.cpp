@@ -1653,9 +1653,194 @@ int wallmodel_werner(Orc &g, const double *U) {
     return 0;
 }
 
-// The wall model WALL_MODEL dispatches to (compact3d.f:1982-2011) for WMODEL = 1 or 4.
+// MESH02's coordinates (compact3d.f:322-380): faces XG, ZG of the uniform x and z grids,
+// centres XC, YC, ZC; indices as in Fortran.
+struct Mesh02 {
+    std::vector<double> XG, XC, YC, ZG, ZC;
+};
+static Mesh02 mesh02(const Orc &g) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
+    Mesh02 m;
+    m.XG.assign(N1M + 2, 0.0);
+    m.XC.assign(N1M + 2, 0.0);
+    m.ZG.assign(N3M + 2, 0.0);
+    m.ZC.assign(N3M + 2, 0.0);
+    m.YC.assign(N2 + 1, 0.0);
+    for (int I = 1; I <= N1M; I++) m.XG[I] = (double)(I - 1) * g.ALX / (double)N1M;
+    m.XG[N1M + 1] = g.ALX;
+    for (int K = 1; K <= N3M; K++) m.ZG[K] = (double)(K - 1) * g.ALZ / (double)N3M;
+    m.ZG[N3M + 1] = g.ALZ;
+    for (int I = 1; I <= N1M; I++) m.XC[I] = 0.5 * (m.XG[I + 1] + m.XG[I]);
+    m.XC[N1M + 1] = m.XG[N1M + 1];
+    for (int K = 1; K <= N3M; K++) m.ZC[K] = 0.5 * (m.ZG[K + 1] + m.ZG[K]);
+    m.ZC[N3M + 1] = m.ZG[N3M + 1];
+    m.YC[0] = g.Y[0];
+    for (int J = 1; J <= N2M; J++) m.YC[J] = 0.5 * (g.Y[J + 1] + g.Y[J]);
+    m.YC[N2] = g.Y[N2];
+    return m;
+}
+
+// INDEX_IJK (compact3d.f:12763-12807): a point outside the outermost cell centres is moved
+// by ANINT(... +- 0.5)/1E6 (the coordinates are changed in the caller, as the reference's
+// by-reference arguments are), then the first cell whose faces bracket it in each direction.
+static void index_ijk(const Orc &g, const Mesh02 &m, double &XP, double &YP, double &ZP, int &IP, int &JP, int &KP) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    if (XP < m.XC[1]) XP = std::round(XP * 1E06 + 0.5) / 1E06;
+    if (XP > m.XC[N1M]) XP = std::round(XP * 1E06 - 0.5) / 1E06;
+    if (YP < m.YC[1]) YP = std::round(YP * 1E06 + 0.5) / 1E06;
+    if (YP > m.YC[N2M]) YP = std::round(YP * 1E06 - 0.5) / 1E06;
+    if (ZP < m.ZC[1]) ZP = std::round(ZP * 1E06 + 0.5) / 1E06;
+    if (ZP > m.ZC[N3M]) ZP = std::round(ZP * 1E06 - 0.5) / 1E06;
+    IP = JP = KP = -1;
+    for (int I = 1; I <= N1M && IP == -1; I++)
+        if (XP >= m.XG[I] && XP <= m.XG[I + 1]) IP = I;
+    for (int J = 1; J <= N2M && JP == -1; J++)
+        if (YP >= g.Y[J] && YP <= g.Y[J + 1]) JP = J;
+    for (int K = 1; K <= N3M && KP == -1; K++)
+        if (ZP >= m.ZG[K] && ZP <= m.ZG[K + 1]) KP = K;
+}
+
+// INTERPOLAT (compact3d.f:12602-12760): trilinear interpolation of velocity component C
+// (1 u at x faces, 2 v at y faces, 3 w at z faces) at (XP, YP, ZP) in cell (IP, JP, KP).
+static double interpolat(const Orc &g, const Mesh02 &m, double XP, double YP, double ZP, int IP, int JP, int KP,
+                         const double *U, int C) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2, N1 = g.N1, N3 = g.N3;
+    int IUM, IUP, JUM, JUP, KUM, KUP;
+    double XUM, XUP, YUM, YUP, ZUM, ZUP;
+    if (C == 1) {
+        IUM = IP; IUP = g.IPA[IP]; XUM = m.XG[IP]; XUP = m.XG[IUP];
+        if (IP == N1M) XUP = m.XG[N1];
+    } else if (XP >= m.XC[IP]) {
+        IUM = IP; IUP = g.IPA[IP]; XUM = m.XC[IP]; XUP = m.XC[IUP];
+        if (IP == N1M) XUP = m.XC[N1M] + 1. / g.DX1;
+    } else {
+        IUM = g.IMA[IP]; IUP = IP; XUM = m.XC[IUM]; XUP = m.XC[IP];
+        if (IP == 1) XUM = m.XC[1] - 1. / g.DX1;
+    }
+    if (C == 2) {
+        JUM = JP; JUP = g.JPA[JP]; YUM = g.Y[JP]; YUP = g.Y[JUP];
+        if (JP == N2M) YUP = m.YC[N2];
+    } else if (YP >= m.YC[JP]) {
+        JUM = JP; JUP = g.JPA[JP]; YUM = m.YC[JP]; YUP = m.YC[JUP];
+        if (JP == N2M) YUP = m.YC[N2];
+    } else {
+        JUM = g.JMU[JP]; JUP = JP; YUM = m.YC[JUM]; YUP = m.YC[JP];
+        if (JP == 1) YUM = g.Y[1];
+    }
+    if (C == 3) {
+        KUM = KP; KUP = g.KPA[KP]; ZUM = m.ZG[KP]; ZUP = m.ZG[KUP];
+        if (KP == N3M) ZUP = m.ZG[N3];
+    } else if (ZP >= m.ZC[KP]) {
+        KUM = KP; KUP = g.KPA[KP]; ZUM = m.ZC[KP]; ZUP = m.ZC[KUP];
+        if (KP == N3M) ZUP = m.ZC[N3M] + 1. / g.DX3;
+    } else {
+        KUM = g.KMA[KP]; KUP = KP; ZUM = m.ZC[KUM]; ZUP = m.ZC[KP];
+        if (KP == 1) ZUM = m.ZC[1] - 1. / g.DX3;
+    }
+    auto u = [&](int i, int j, int k) { return U[g.iuc(i, j, k, C)]; };
+    const double PHA = u(IUM, JUM, KUM), PHB = u(IUP, JUM, KUM), PHC = u(IUP, JUP, KUM), PHD = u(IUM, JUP, KUM);
+    const double PHE = u(IUM, JUM, KUP), PHF = u(IUP, JUM, KUP), PHG = u(IUP, JUP, KUP), PHH = u(IUM, JUP, KUP);
+    const double PHAB = (PHB - PHA) / (XUP - XUM) * (XP - XUM) + PHA;
+    const double PHCD = (PHC - PHD) / (XUP - XUM) * (XP - XUM) + PHD;
+    const double PHEF = (PHF - PHE) / (XUP - XUM) * (XP - XUM) + PHE;
+    const double PHGH = (PHG - PHH) / (XUP - XUM) * (XP - XUM) + PHH;
+    const double PHABCD = (PHCD - PHAB) / (YUP - YUM) * (YP - YUM) + PHAB;
+    const double PHEFGH = (PHGH - PHEF) / (YUP - YUM) * (YP - YUM) + PHEF;
+    return (PHEFGH - PHABCD) / (ZUP - ZUM) * (ZP - ZUM) + PHABCD;
+}
+
+// The bisection for u_tau of the log law on a plane-mean velocity (compact3d.f:5017-5029,
+// 4390-4402): the lower end of the final bracket.
+static double utau_bisect(double U_ave, double DELTAP, double RE, double U_tau1, double U_tau2) {
+    const double KAPA = 0.41, B = 5.2;
+    while (std::fabs(U_tau2 - U_tau1) > 0.0000001) {
+        double TEMP = 0.5 * U_tau2 + 0.5 * U_tau1;
+        const double FUtau1 = U_ave / U_tau1 - std::log(U_tau1 * DELTAP * RE) / KAPA - B;
+        const double FUtau2 = U_ave / TEMP - std::log(TEMP * DELTAP * RE) / KAPA - B;
+        TEMP = FUtau1 * FUtau2;
+        if (TEMP <= 0.0) U_tau2 = 0.5 * U_tau2 + 0.5 * U_tau1;
+        else U_tau1 = 0.5 * U_tau2 + 0.5 * U_tau1;
+    }
+    return U_tau1;
+}
+
+// The shifted-point models: PIOMELLI (WMODEL 5, compact3d.f:4960-5110) and MARUSIC1
+// (WMODEL 3, 4336-4495).  u_tau of each wall from the log law on a plane-mean u, then per
+// wall point the velocity interpolated at a point shifted downstream by DELTS.  PIOMELLI
+// computes its y+ from DELTP, a variable the routine never sets (F:5035, 5088); it is taken
+// as zero, so its shift DELTS is zero.  MARUSIC1's outer plane ZS is the plane nearest
+// y = 0.06 (the last J found by its loop).
+int wallmodel_shifted(Orc &g, const double *U) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double RE = g.RE, PI = std::acos(-1.0);
+    const bool mar = g.WMODEL == 3;
+    const Mesh02 m = mesh02(g);
+    int ZS = -1;
+    if (mar) {
+        const double ZO = 0.06;
+        for (int J = 1; J <= N2M; J++)
+            if (std::fabs(g.Y[J] - ZO) <= std::fabs(g.Y[J + 1] - ZO) && std::fabs(g.Y[J] - ZO) <= std::fabs(g.Y[J - 1] - ZO))
+                ZS = J;
+        if (ZS < 1) return C3D_EINVAL;
+    }
+    const int jd = mar ? ZS : 1, ju = mar ? N2M - ZS + 1 : N2M;
+    double U1DOWN = 0.0, U1UP = 0.0;
+    for (int K = 1; K <= N3M; K++)
+        for (int I = 1; I <= N1M; I++) {
+            U1DOWN = U1DOWN + U[g.iuc(I, jd, K, 1)];
+            U1UP = U1UP + U[g.iuc(I, ju, K, 1)];
+        }
+    U1DOWN = U1DOWN / (double)(N1M * N3M);
+    U1UP = U1UP / (double)(N1M * N3M);
+    for (int wall = 1; wall <= 2; wall++) {
+        const double U_ave = wall == 1 ? U1DOWN : U1UP;
+        double DELTAP, UTAU2, TAUW1, DELTS, CC = 1.0, YP;
+        if (mar) {
+            DELTAP = m.YC[ZS];
+            UTAU2 = utau_bisect(U_ave, DELTAP, RE, 1.0, 0.000001);
+            TAUW1 = UTAU2 * UTAU2;
+            const double YPLUSML = DELTAP * UTAU2 * RE, YPLUS1 = g.DY[1] / 2.0 * UTAU2 * RE;
+            CC = 1.0 + 0.05 * std::pow(std::log(YPLUS1 / YPLUSML), 2);
+            DELTS = DELTAP / std::tan(16.0 * PI / 180);
+            YP = wall == 1 ? DELTAP : m.YC[N2M - ZS + 1];
+        } else {
+            DELTAP = (wall == 1 ? g.DY[1] : g.DY[N2M]) / 2.0;
+            UTAU2 = utau_bisect(U_ave, DELTAP, RE, 0.000001, 0.2);
+            TAUW1 = UTAU2 * UTAU2;
+            DELTS = 0.0;   // y+ from the unset DELTP
+            YP = wall == 1 ? g.H[1] : m.YC[N2M];
+        }
+        if (wall == 1) {
+            g.TAOW = TAUW1;
+            g.WSM[0] = TAUW1;
+        }
+        for (int I = 1; I <= N1M; I++)
+            for (int K = 1; K <= N3M; K++) {
+                int IP, JP, KP;
+                double XP = m.XG[I] + DELTS;
+                if (XP > g.ALX) XP = XP - g.ALX;
+                double ZP = m.ZC[K];
+                index_ijk(g, m, XP, YP, ZP, IP, JP, KP);
+                if (IP < 0 || JP < 0 || KP < 0) return C3D_EINVAL;
+                const double F = interpolat(g, m, XP, YP, ZP, IP, JP, KP, U, mar ? 1 : 2);
+                g.TAUW[g.itw(I, K, wall)] = mar ? TAUW1 + CC * 0.1 * UTAU2 * (F - U_ave) : TAUW1 + 0.1 * UTAU2 * F;
+                XP = m.XC[I] + DELTS;
+                if (XP > g.ALX) XP = XP - g.ALX;
+                ZP = m.ZG[K];
+                index_ijk(g, m, XP, YP, ZP, IP, JP, KP);
+                if (IP < 0 || JP < 0 || KP < 0) return C3D_EINVAL;
+                const double WF = interpolat(g, m, XP, YP, ZP, IP, JP, KP, U, 3);
+                g.TAUB[g.itw(I, K, wall)] = TAUW1 * WF / U_ave;
+            }
+    }
+    return 0;
+}
+
+// The wall model WALL_MODEL dispatches to (compact3d.f:1982-2011) for WMODEL = 1, 3, 4, 5.
 int wallmodel(Orc &g, const double *U) {
-    return g.WMODEL == 4 ? wallmodel_werner(g, U) : wallmodel_instant(g, U);
+    if (g.WMODEL == 4) return wallmodel_werner(g, U);
+    if (g.WMODEL == 3 || g.WMODEL == 5) return wallmodel_shifted(g, U);
+    return wallmodel_instant(g, U);
 }
 
 // ----------------------------------------------------------------------------------
@@ -2180,7 +2365,7 @@ int orc_getup(void *h, double *U, double *P, double *HH, double *SGSVIS, int NTI
               double *PRESG, double *PRESG3) {
     Orc &g = *(Orc *)h;
     (void)NTIME;
-    if (g.FILES < 0 || g.FILES > 2 || !(g.WMODEL == 0 || g.WMODEL == 1 || g.WMODEL == 4)) return C3D_EINVAL;
+    if (g.FILES < 0 || g.FILES > 2 || g.WMODEL < 0 || g.WMODEL == 2 || g.WMODEL > 5) return C3D_EINVAL;
     if (g.WMODEL == 4 && g.N3M > g.N1M) return C3D_EINVAL;   // WERNER indexes INDX(N1M) with K
     const int N1 = g.N1, N2 = g.N2, N3 = g.N3;
     double *UH = g.UH.data(), *HH2 = g.HH2.data();

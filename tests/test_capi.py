@@ -65,7 +65,7 @@ def test_create_rejects_null_metrics(L):
 
 def test_create_rejects_bad_precision_and_models(L):
     g, _ = make_grid("small32")
-    for field, val in (("precision", 7), ("files", 3), ("re", -1.0), ("wmodel", 2), ("wmodel", 3), ("wmodel", 5)):
+    for field, val in (("precision", 7), ("files", 3), ("re", -1.0), ("wmodel", 2), ("wmodel", 6), ("wmodel", -1)):
         s = g.struct()
         setattr(s, field, val)
         h = ctypes.c_void_p()
@@ -91,3 +91,21 @@ def test_werner_needs_n3_not_above_n1(L):
     s = g.struct()
     h = ctypes.c_void_p()
     assert L.c3d_create(ctypes.byref(s), ctypes.byref(h)) == -1
+
+
+def test_shifted_wall_models_check_the_y_faces(L):
+    """WMODEL 3 / 5 (MARUSIC1 / PIOMELLI) search the Y faces for the interpolation cell,
+    so Y(1:N2) must increase; PIOMELLI's H(1) must lie within 2e-3 of YC(1) (its height
+    climbs by 1e-6 per wall point below YC(1)).  Both are refused before any device work."""
+    for wmodel in (3, 5):
+        g, _ = make_grid("les32cs", wmodel=wmodel)
+        g.arrays["y"][4] = g.arrays["y"][3]
+        s = g.struct()
+        h = ctypes.c_void_p()
+        assert L.c3d_create(ctypes.byref(s), ctypes.byref(h)) == -1
+        assert b"increase" in L.c3d_last_error()
+    g, _ = make_grid("les32cs", wmodel=5, y0=0.01)
+    s = g.struct()
+    h = ctypes.c_void_p()
+    assert L.c3d_create(ctypes.byref(s), ctypes.byref(h)) == -1
+    assert b"H(1)" in L.c3d_last_error()

@@ -69,6 +69,10 @@ def gpu_from(libc3d, orc, g, U, P, HH, precision=C3D_FP64):
     ("les32dy", dict(wmodel=0, cks=2.0)),   # dynamic, no-slip walls, stretched y
     ("les32cs", dict(wmodel=4)),            # Smagorinsky + WALLMODEL_WERNER (both walls)
     ("les32dy", dict(wmodel=4)),            # dynamic + WALLMODEL_WERNER
+    ("les32cs", dict(wmodel=3)),            # Smagorinsky + MARUSIC1, reference plane ZS = 1
+    ("les32dy", dict(wmodel=3, n2m=32)),    # dynamic + MARUSIC1, ZS = 2
+    ("les32cs", dict(wmodel=5)),            # Smagorinsky + PIOMELLI
+    ("les32dy", dict(wmodel=5, y0=1e-5)),   # PIOMELLI with H(1) 5e-6 below YC(1): YP climbs
 ])
 def test_les_one_step_fp64(libc3d, oracle_mod, name, over):
     g, dt, orc, U, P, HH, S, pg, pg3 = warm_start(oracle_mod, name, **over)
@@ -111,8 +115,9 @@ def test_les_ten_steps_fp64(libc3d, oracle_mod):
     assert d["divmax"] < 1e-12
 
 
-def test_les_mixed_against_fp64(libc3d, oracle_mod):
-    g, dt, orc, U, P, HH, S, pg, pg3 = warm_start(oracle_mod, "les32dy")
+@pytest.mark.parametrize("name,over", [("les32dy", {}), ("les32cs", dict(wmodel=3)), ("les32dy", dict(wmodel=5))])
+def test_les_mixed_against_fp64(libc3d, oracle_mod, name, over):
+    g, dt, orc, U, P, HH, S, pg, pg3 = warm_start(oracle_mod, name, **over)
     c64 = gpu_from(libc3d, orc, g, U, P, HH, C3D_FP64)
     cmx = gpu_from(libc3d, orc, g, U, P, HH, C3D_MIXED)
     for c in (c64, cmx):

@@ -289,3 +289,108 @@ def test_les_step_runs_and_conserves(oracle_mod):
         tw, tb, wsm = o.get_wall()
         utau = math.sqrt(wsm[0])
         assert 1500 < utau * g.re < 2600
+
+
+def _loglaw_utau(U_ave, deltap, re):
+    """u_tau with U_ave / u_tau = log(u_tau deltap re) / 0.41 + 5.2 (bisection to 1e-14)."""
+    lo, hi = 1e-6, 1.0
+    f = lambda ut: U_ave / ut - np.log(ut * deltap * re) / 0.41 - 5.2
+    while hi - lo > 1e-14:
+        mid = 0.5 * (lo + hi)
+        if f(lo) * f(mid) <= 0:
+            hi = mid
+        else:
+            lo = mid
+    return lo
+
+
+def _mesh02(g):
+    y = g.arrays["y"]
+    xg = np.arange(g.n1m + 2) * 0.0
+    xg[1:g.n1m + 1] = np.arange(g.n1m) * g.alx / g.n1m
+    xg[g.n1m + 1] = g.alx
+    zg = np.zeros(g.n3m + 2)
+    zg[1:g.n3m + 1] = np.arange(g.n3m) * g.alz / g.n3m
+    zg[g.n3m + 1] = g.alz
+    xc = 0.5 * (xg[1:] + xg[:-1])
+    yc = 0.5 * (y[1:] + y[:-1])
+    return xg, xc, y, yc, zg
+
+
+@pytest.mark.parametrize("wmodel", [3, 5])
+def test_shifted_wall_models_uniform_and_linear_fields(oracle_mod, wmodel):
+    """PIOMELLI (5) and MARUSIC1 (3) on a field with uniform w, v = c y and u = a + b y
+    (fields the trilinear interpolation reproduces exactly): u_tau of each wall from the
+    log law on the plane-mean u of its reference plane, TAUB = u_tau^2 W / <u>, and
+    TAUW = u_tau^2 + 0.1 u_tau v (PIOMELLI, v at y = H(1) and, through JPA(N2M) = N2M, at
+    Y(N2M)) or
+    u_tau^2 + C 0.1 u_tau (u - <u>) = u_tau^2 (MARUSIC1, u uniform on the plane)."""
+    g, _ = _grid("les32cs", wmodel=wmodel)
+    o = oracle_mod.Oracle(g)
+    xg, xc, y, yc, zg = _mesh02(g)
+    a, b, c, W = 0.4, 0.9, 0.02, 0.15
+    U = g.zeros_u()
+    for j in range(0, g.n2m + 2):
+        yy = yc[j] if 1 <= j <= g.n2m else y[0 if j == 0 else g.n2m + 1]   # yc[J] = YC(J)
+        U[:, j, :, 0] = a + b * yy
+        U[:, j, :, 1] = c * y[min(j, g.n2m + 1)]
+        U[:, j, :, 2] = W
+    assert o.wallmodel(U) == 0
+    tw, tb, wsm = o.get_wall()
+    n1, n2, n3 = g.n1m, g.n2m, g.n3m
+    if wmodel == 3:
+        zs = [J for J in range(1, n2 + 1) if abs(y[J] - 0.06) <= abs(y[J + 1] - 0.06) and abs(y[J] - 0.06) <= abs(y[J - 1] - 0.06)][-1]
+        planes, deltap = (zs, n2 - zs + 1), (yc[zs], yc[zs])
+    else:
+        planes, deltap = (1, n2), (g.arrays["dy"][1] / 2, g.arrays["dy"][n2] / 2)
+    for wall in (0, 1):
+        uave = a + b * yc[planes[wall]]
+        ut = _loglaw_utau(uave, deltap[wall], g.re)
+        t = tw[1:n1 + 1, 1:n3 + 1, wall]
+        if wmodel == 3:
+            np.testing.assert_allclose(t, ut ** 2, rtol=2e-5)
+        else:
+            # bottom: v between Y(1) and Y(2) at H(1); top: JPA(N2M) = N2M, so both
+            # v corners are V(N2M) and the interpolant is c Y(N2M), not c YC(N2M)
+            yp = g.arrays["h"][0] if wall == 0 else y[n2]
+            np.testing.assert_allclose(t, ut ** 2 + 0.1 * ut * c * yp, rtol=2e-5)
+        np.testing.assert_allclose(tb[1:n1 + 1, 1:n3 + 1, wall], ut ** 2 * W / uave, rtol=2e-5)
+    assert wsm[0] == pytest.approx(_loglaw_utau(a + b * yc[planes[0]], deltap[0], g.re) ** 2, rel=2e-5)
+
+
+def test_marusic_shift_follows_linear_u(oracle_mod):
+    """MARUSIC1 samples u at XG(I) + DELTAP / tan(16 deg), wrapped into the box: with
+    u = a + b y + e x on the interior x faces the interpolant is a + e XP exactly wherever
+    XP falls between two interior faces, so TAUW = u_tau^2 + CC 0.1 u_tau (a + b YP + e XP
+    - <u>) there, CC = 1 + 0.05 log(DY(1) / (2 DELTAP))^2 (compact3d.f:4405-4440)."""
+    g, _ = _grid("les32cs", wmodel=3)
+    o = oracle_mod.Oracle(g)
+    xg, xc, y, yc, zg = _mesh02(g)
+    a, b, e = 0.4, 0.9, 0.05
+    n1, n2, n3 = g.n1m, g.n2m, g.n3m
+    U = g.zeros_u()
+    for j in range(0, n2 + 2):
+        yy = yc[j] if 1 <= j <= n2 else y[0 if j == 0 else n2 + 1]
+        U[1:n1 + 1, j, :, 0] = (a + b * yy + e * xg[1:n1 + 1])[:, None]
+        U[0, j, :, 0] = U[n1, j, :, 0]
+    assert o.wallmodel(U) == 0
+    tw, _, _ = o.get_wall()
+    zs = [J for J in range(1, n2 + 1) if abs(y[J] - 0.06) <= abs(y[J + 1] - 0.06) and abs(y[J] - 0.06) <= abs(y[J - 1] - 0.06)][-1]
+    deltap = yc[zs]
+    delts = deltap / math.tan(16.0 * math.pi / 180)
+    cc = 1.0 + 0.05 * math.log(g.arrays["dy"][1] / 2.0 / deltap) ** 2
+    checked = 0
+    for wall, plane in ((0, zs), (1, n2 - zs + 1)):
+        uave = a + b * yc[plane] + e * xg[1:n1 + 1].mean()
+        ut = _loglaw_utau(uave, deltap, g.re)
+        for i in range(1, n1 + 1):
+            xp = xg[i] + delts
+            if xp > g.alx:
+                xp -= g.alx
+            if not (xg[1] <= xp <= xg[n1]):
+                continue
+            want = ut ** 2 + cc * 0.1 * ut * (a + b * yc[plane] + e * xp - uave)
+            # the reference's bisection stops at a bracket of 1e-7 in u_tau
+            np.testing.assert_allclose(tw[i, 1:n3 + 1, wall], want, rtol=0, atol=4e-7 * ut)
+            checked += 1
+    assert checked >= n1
