@@ -484,8 +484,8 @@ def error_study(lib, g, dt, U0, P0, HH0, steps: int, floor: bool = True):
 
 def run_next(args, D: Dist, g, dt, U0, P0, HH0):
     """ENERGY's plane statistics and a checkpoint write + read on the main workload (mixed
-    form), and the LES step with the algebraic wall models WERNER, MARUSIC1 and PIOMELLI on
-    les128 (mixed form)."""
+    form), and the LES step with the algebraic wall models WERNER, MARUSIC1 and PIOMELLI and
+    with the scale-dependent SGS model on les128 (mixed form)."""
     import shutil
     import tempfile
     from compact3d_gb300 import lib
@@ -520,9 +520,11 @@ def run_next(args, D: Dist, g, dt, U0, P0, HH0):
     finally:
         shutil.rmtree(d, ignore_errors=True)
     ch.close()
-    for key, wm, label in (("les_werner", 4, "WALLMODEL_WERNER (WMODEL 4)"), ("les_marusic", 3, "MARUSIC1 (WMODEL 3)"),
-                           ("les_piomelli", 5, "PIOMELLI (WMODEL 5)")):
-        gl, dtl = make_grid("les128", wmodel=wm)
+    for key, over, label in (("les_werner", dict(wmodel=4), "SGSCS + WALLMODEL_WERNER (WMODEL 4)"),
+                             ("les_marusic", dict(wmodel=3), "SGSCS + MARUSIC1 (WMODEL 3)"),
+                             ("les_piomelli", dict(wmodel=5), "SGSCS + PIOMELLI (WMODEL 5)"),
+                             ("les_sgssd", dict(files=3), "SGSSD (FILES 3) + WALLMODEL_INSTANT")):
+        gl, dtl = make_grid("les128", **over)
         Ul, Pl, Hl = ic.loglaw(gl, 2000.0, amp=0.05, seed=ic.SEED0 + 3000 + D.rank)
         c = make_channel(lib, gl, "mixed", Ul, Pl, Hl)
         if not args.no_tune:
@@ -542,7 +544,7 @@ def run_next(args, D: Dist, g, dt, U0, P0, HH0):
             n += 1
             msl += c.timer_stop()
         msl = D.max(msl)
-        out[key] = dict(workload=f"les128, SGSCS + {label}, mixed form, L2 flushed per step",
+        out[key] = dict(workload=f"les128, {label}, mixed form, L2 flushed per step",
                         value=D.sum(gl.points) * K / (msl / 1e3), unit=UNIT, ms_per_step=msl / K, steps=K,
                         wsm=float(c.get_wsm()[0]))
         c.close()

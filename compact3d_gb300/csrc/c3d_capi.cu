@@ -198,6 +198,8 @@ void free_channel(c3d_channel *ch) {
     if (ch->xfer) cudaFree(ch->xfer);
     if (ch->wtaue) cudaFree(ch->wtaue);
     if (ch->wshift) cudaFree(ch->wshift);
+    if (ch->sdpart) cudaFree(ch->sdpart);
+    if (ch->sdbeta) cudaFree(ch->sdbeta);
     if (ch->wfork) cudaEventDestroy(ch->wfork);
     if (ch->wjoin) cudaEventDestroy(ch->wjoin);
     if (ch->wside) cudaStreamDestroy(ch->wside);
@@ -332,8 +334,8 @@ int check_grid(const c3d_grid *g) {
         set_error("precision must be C3D_FP64, C3D_MIXED or C3D_MIXED_IR");
         return C3D_EINVAL;
     }
-    if (g->files < 0 || g->files > 2) {
-        set_error("FILES must be 0 (DNS), 1 (SGSDY) or 2 (SGSCS); the scale-dependent model (3) is not built");
+    if (g->files < 0 || g->files > 3) {
+        set_error("FILES must be 0 (DNS), 1 (SGSDY), 2 (SGSCS) or 3 (SGSSD)");
         return C3D_EINVAL;
     }
     if (!(g->wmodel == 0 || g->wmodel == 1 || g->wmodel == 3 || g->wmodel == 4 || g->wmodel == 5)) {
@@ -475,8 +477,14 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
             if (cudaMalloc(&ch->les[q], nf * rs) != cudaSuccess) { set_error("cudaMalloc LES"); return fail(C3D_ENOMEM); }
             cudaMemset(ch->les[q], 0, nf * rs);
         }
-        if (ch->files == 1 && cudaMalloc(&ch->dyn, 21 * (size_t)g.n2m * g.np * rs) != cudaSuccess)
+        if ((ch->files == 1 || ch->files == 3) && cudaMalloc(&ch->dyn, 21 * (size_t)g.n2m * g.np * rs) != cudaSuccess)
             return fail(C3D_ENOMEM);
+        if (ch->files == 3) {   // SGSSD: tiles of 256 points per plane, at most 16
+            ch->sdnt = std::min(16, (g.np + 255) / 256);
+            if (dalloc(&ch->sdpart, (size_t)g.n2m * ch->sdnt * 10) || dalloc(&ch->sdbeta, (size_t)g.n2 + 1))
+                return fail(C3D_ENOMEM);
+            cudaMemset(ch->sdbeta, 0, ((size_t)g.n2 + 1) * 8);
+        }
         const int nbw = (g.np + 127) / 128;   // blocks of k_wall (TPB = 128 threads)
         if (dalloc(&ch->smagc, (size_t)g.n2 + 1) || dalloc(&ch->d23, (size_t)g.n2 + 1) ||
             dalloc(&ch->ycs, (size_t)g.n2 + 1) || dalloc(&ch->wpart, 2 * (size_t)nbw))

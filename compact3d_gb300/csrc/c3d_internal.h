@@ -166,6 +166,9 @@ struct c3d_channel {
     // MARUSIC1 / PIOMELLI: Y(0:N2), YC(0:N2), per-wall constants and YP heights; the
     // reference plane ZS of MARUSIC1 (the Y(J) nearest 0.06) and tan(16 deg)
     double *wshift = nullptr;
+    // SGSSD: per-plane partial sums of k_sgs_sd_sums (N2M x sdnt x 10) and BETA(0:N2)
+    double *sdpart = nullptr, *sdbeta = nullptr;
+    int sdnt = 0;
     // the wall model runs on its own stream beside the SGS model and the RHS passes: forked
     // after the last reader of WSM, joined before the first reader of TAUW/TAUB
     cudaStream_t wside = nullptr;

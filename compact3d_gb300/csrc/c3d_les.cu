@@ -292,6 +292,257 @@ __global__ void __launch_bounds__(256) k_sgs_dyn(StepArgs<R> a, LesArgs<R> l) {
 }
 
 // ---------------------------------------------------------------------------------
+// SGSSD (compact3d.f:1502-1948), the scale-dependent dynamic model, on SGSDY's raw
+// quantities (k_sgs_raw).  k_sgs_sd_sums reads each raw quantity's 5x5 neighbourhood once
+// and forms both test filters from it, FILTER (Simpson (1,4,1)/6 in x then z: 2 DELTA) and
+// FILTER4 ((1,4,2,4,1)/12: 4 DELTA), then per level the five plane sums of the Germano
+// identity, SR1 = DELTA^(2/3) |S~| S~ and COM1 = (DELTA^(2/3) |S| S)~:
+//   L.SR1, L.COM1, COM1.COM1, SR1.SR1, SR1.COM1   (2x weight on the off-diagonal terms)
+// per block in FP64.  The reference's third pass (the coefficient at 2 DELTA with
+// M = 4 BETA DELTA^(2/3) |S~| S~ - COM1, its unclipped BETA) needs no sums of its own: M
+// is linear in BETA, so sum(L.M) = 4 BETA sum(L.SR1) - sum(L.COM1) and sum(M.M) =
+// 16 BETA^2 sum(SR1.SR1) - 8 BETA sum(SR1.COM1) + sum(COM1.COM1) at the FILTER level.
+// k_sgs_sd_coef: per plane COEFFICIENT, DQRRT/CHHQR and SMAGC; k_sgs_apply: nu.
+// ---------------------------------------------------------------------------------
+constexpr int SD_NS = 10;
+
+// 2 a1 b1 + a0 b0 + 2 a2 b2 + a3 b3 + 2 a4 b4 + a5 b5
+template <typename R>
+__device__ __forceinline__ R dot6(const R *a, const R *b) {
+    return (R)2.0 * a[1] * b[1] + a[0] * b[0] + (R)2.0 * a[2] * b[2] + a[3] * b[3] + (R)2.0 * a[4] * b[4] + a[5] * b[5];
+}
+
+// the five sums of one filter level from the filtered S (f[0..5]), COM1 (6..11), UC
+// (12..14, relative to a per-plane velocity) and UC products (15..20)
+template <typename R>
+__device__ __forceinline__ void sd_level(const R *f, R d23, double *acc) {
+    R m[6], sr1[6], L[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) m[c] = f[c];
+    const R fdabs = d23 * sqrt((R)2.0 * sumsq6(m));
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sr1[c] = fdabs * m[c];
+    const R *uc = f + 12, *up = f + 15, *cf = f + 6;
+    L[0] = up[0] - uc[0] * uc[0];
+    L[1] = up[1] - uc[0] * uc[1];
+    L[2] = up[2] - uc[0] * uc[2];
+    L[3] = up[3] - uc[1] * uc[1];
+    L[4] = up[4] - uc[1] * uc[2];
+    L[5] = up[5] - uc[2] * uc[2];
+    acc[0] += (double)dot6(L, sr1);
+    acc[1] += (double)dot6(L, cf);
+    acc[2] += (double)dot6(cf, cf);
+    acc[3] += (double)dot6(sr1, sr1);
+    acc[4] += (double)dot6(sr1, cf);
+}
+
+// grid (tiles, N2M), 256 threads; part[((j - 1) tiles + tile) SD_NS + q]
+template <typename R>
+__global__ void __launch_bounds__(256) k_sgs_sd_sums(StepArgs<R> a, LesArgs<R> l, double *part) {
+    const Geo g = a.g;
+    const int j = 1 + blockIdx.y, nt = gridDim.x, n1 = g.n1m, n3 = g.n3m;
+    const long long fs = (long long)g.n2m * g.np, pb = (long long)(j - 1) * g.np;
+    const R d23 = l.d23r[j];
+    const R four = (R)4.0, two = (R)2.0, six = (R)6.0, twelve = (R)12.0;
+    double acc[SD_NS];
+#pragma unroll
+    for (int q = 0; q < SD_NS; ++q) acc[q] = 0.0;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < g.np; e += nt * blockDim.x) {
+        const int i = e % n1, k = e / n1;
+        int ix[5], kr[5];
+#pragma unroll
+        for (int d = 0; d < 5; ++d) {
+            int ii = i + d - 2, kk = k + d - 2;
+            ii = ii < 0 ? ii + n1 : (ii >= n1 ? ii - n1 : ii);
+            kk = kk < 0 ? kk + n3 : (kk >= n3 ? kk - n3 : kk);
+            ix[d] = ii;
+            kr[d] = kk * n1;
+        }
+        R f3[21], f4[21];
+#pragma unroll
+        for (int c = 0; c < 21; ++c) {
+            const R *f = l.dyn + c * fs + pb;
+            R t3[3], t4[5];
+#pragma unroll
+            for (int r = 0; r < 5; ++r) {
+                const R *row = f + kr[r];
+                const R v0 = row[ix[0]], v1 = row[ix[1]], v2 = row[ix[2]], v3 = row[ix[3]], v4 = row[ix[4]];
+                t4[r] = (v0 + four * v1 + two * v2 + four * v3 + v4) / twelve;
+                if (r >= 1 && r <= 3) t3[r - 1] = (v1 + four * v2 + v3) / six;
+            }
+            f3[c] = (t3[0] + four * t3[1] + t3[2]) / six;
+            f4[c] = (t4[0] + four * t4[1] + two * t4[2] + four * t4[3] + t4[4]) / twelve;
+        }
+        sd_level(f3, d23, acc);
+        sd_level(f4, d23, acc + 5);
+    }
+    __shared__ double red[SD_NS][256];
+#pragma unroll
+    for (int q = 0; q < SD_NS; ++q) red[q][threadIdx.x] = acc[q];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+#pragma unroll
+            for (int q = 0; q < SD_NS; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x < SD_NS) part[((long long)(j - 1) * nt + blockIdx.x) * SD_NS + threadIdx.x] = red[threadIdx.x][0];
+}
+
+// CHHQR (compact3d.f:11571-11676) for the 5x5 companion matrix, every operation rounded as
+// written: eigenvalues of an upper Hessenberg matrix by the Francis double-shift QR with
+// the deflation test |A(L,L-1)| <= EPS (|A(L-1,L-1)| + |A(L,L)|), at most 60 sweeps per
+// deflation (after which the roots not found stay 0).  A is column-major, 1-based.
+#define SD_M(x, y) __dmul_rn(x, y)
+#define SD_A(x, y) __dadd_rn(x, y)
+#define SD_S(x, y) __dsub_rn(x, y)
+__device__ void sd_chhqr5(double *A, double *WR, double EPS) {
+    constexpr int N = 5;
+    auto a = [&](int i, int j) -> double & { return A[(i - 1) + N * (j - 1)]; };
+    int M = N, IT = 0;
+    for (int guard = 0; M > 0 && guard < 1000; ++guard) {
+        int L = M;
+        while (L > 1 && fabs(a(L, L - 1)) > SD_M(EPS, SD_A(fabs(a(L - 1, L - 1)), fabs(a(L, L))))) L = L - 1;
+        if (L == M) {
+            WR[M - 1] = a(M, M);
+            M = M - 1;
+            IT = 0;
+            continue;
+        }
+        if (L == M - 1) {
+            const double B = -SD_A(a(M, M), a(M - 1, M - 1));
+            const double C = SD_S(SD_M(a(M, M), a(M - 1, M - 1)), SD_M(a(M, M - 1), a(M - 1, M)));
+            const double W = SD_S(SD_M(B, B), SD_M(4.0, C));
+            const double Y = sqrt(fabs(W));
+            if (W > 0.0) {
+                const double XY = B < 0.0 ? -1.0 : 1.0;
+                WR[M - 1] = SD_S(-B, SD_M(XY, Y)) / 2.0;
+                WR[M - 2] = C / WR[M - 1];
+            } else {
+                WR[M - 1] = -B / 2.0;
+                WR[M - 2] = WR[M - 1];
+            }
+            M = M - 2;
+            IT = 0;
+            continue;
+        }
+        if (IT >= 60) return;
+        IT = IT + 1;
+        for (int J = L + 2; J <= M; J++) a(J, J - 2) = 0.0;
+        for (int J = L + 3; J <= M; J++) a(J, J - 3) = 0.0;
+        for (int K = L; K <= M - 1; K++) {
+            double P, Q, R;
+            if (K != L) {
+                P = a(K, K - 1);
+                Q = a(K + 1, K - 1);
+                R = K != M - 1 ? a(K + 2, K - 1) : 0.0;
+            } else {
+                const double X = SD_A(a(M, M), a(M - 1, M - 1));
+                const double Y = SD_S(SD_M(a(M - 1, M - 1), a(M, M)), SD_M(a(M - 1, M), a(M, M - 1)));
+                P = SD_A(SD_A(SD_M(a(L, L), SD_S(a(L, L), X)), SD_M(a(L, L + 1), a(L + 1, L))), Y);
+                Q = SD_M(a(L + 1, L), SD_S(SD_A(a(L, L), a(L + 1, L + 1)), X));
+                R = SD_M(a(L + 1, L), a(L + 2, L + 1));
+            }
+            if (SD_A(SD_A(fabs(P), fabs(Q)), fabs(R)) == 0.0) continue;
+            const double XY = P < 0.0 ? -1.0 : 1.0;
+            const double S = SD_M(XY, sqrt(SD_A(SD_A(SD_M(P, P), SD_M(Q, Q)), SD_M(R, R))));
+            if (K != L) a(K, K - 1) = -S;
+            const double E = -Q / S, F = -R / S, X = -P / S;
+            const double PS = SD_A(P, S);
+            const double Y = SD_S(-X, SD_M(F, R) / PS);
+            const double G = SD_M(E, R) / PS;
+            const double Z = SD_S(-X, SD_M(E, Q) / PS);
+            for (int J = K; J <= M; J++) {
+                double p = SD_A(SD_M(X, a(K, J)), SD_M(E, a(K + 1, J)));
+                double q = SD_A(SD_M(E, a(K, J)), SD_M(Y, a(K + 1, J)));
+                double r = SD_A(SD_M(F, a(K, J)), SD_M(G, a(K + 1, J)));
+                if (K != M - 1) {
+                    p = SD_A(p, SD_M(F, a(K + 2, J)));
+                    q = SD_A(q, SD_M(G, a(K + 2, J)));
+                    r = SD_A(r, SD_M(Z, a(K + 2, J)));
+                    a(K + 2, J) = r;
+                }
+                a(K + 1, J) = q;
+                a(K, J) = p;
+            }
+            const int JJ = K + 3 >= M ? M : K + 3;
+            for (int I = L; I <= JJ; I++) {
+                double p = SD_A(SD_M(X, a(I, K)), SD_M(E, a(I, K + 1)));
+                double q = SD_A(SD_M(E, a(I, K)), SD_M(Y, a(I, K + 1)));
+                double r = SD_A(SD_M(F, a(I, K)), SD_M(G, a(I, K + 1)));
+                if (K != M - 1) {
+                    p = SD_A(p, SD_M(F, a(I, K + 2)));
+                    q = SD_A(q, SD_M(G, a(I, K + 2)));
+                    r = SD_A(r, SD_M(Z, a(I, K + 2)));
+                    a(I, K + 2) = r;
+                }
+                a(I, K + 1) = q;
+                a(I, K) = p;
+            }
+        }
+    }
+}
+
+// per plane: the sums, COEFFICIENT (compact3d.f:2079-2095), DQRRT's BETA (11548-11569,
+// EPS 1.0E-5) and SMAGC; one thread per plane
+template <typename R>
+__global__ void k_sgs_sd_coef(StepArgs<R> a, LesArgs<R> l, const double *part, int nt, double *beta) {
+    const Geo g = a.g;
+    const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > g.n2m) return;
+    double s[SD_NS];
+#pragma unroll
+    for (int q = 0; q < SD_NS; ++q) s[q] = 0.0;
+    for (int t = 0; t < nt; ++t)
+#pragma unroll
+        for (int q = 0; q < SD_NS; ++q) s[q] += part[((long long)(j - 1) * nt + t) * SD_NS + q];
+    const double NXZ = 1.0 / (double)(g.n1m * g.n3m);
+    const double A1 = -8.0 * s[0] * NXZ, B1 = -2.0 * s[1] * NXZ, C1 = 4.0 * s[2] * NXZ, D1 = 64.0 * s[3] * NXZ,
+                 E1 = 32.0 * s[4] * NXZ;
+    const double A2 = -32.0 * s[5] * NXZ, B2 = -2.0 * s[6] * NXZ, C2 = 4.0 * s[7] * NXZ, D2 = 1024.0 * s[8] * NXZ,
+                 E2 = 128.0 * s[9] * NXZ;
+    double PA[5];
+    const double AD = SD_M(A1, D2);
+    PA[4] = SD_S(SD_M(B2, C1), SD_M(B1, C2)) / AD;
+    PA[3] = SD_S(SD_M(A1, C2), SD_M(B2, E1)) / AD;
+    PA[2] = SD_S(SD_A(SD_M(B2, D1), SD_M(B1, E2)), SD_M(A2, C1)) / AD;
+    PA[1] = SD_S(SD_M(A2, E1), SD_M(A1, E2)) / AD;
+    PA[0] = -SD_A(SD_M(A2, D1), SD_M(B1, D2)) / AD;
+    double Amat[25], WR[5];
+#pragma unroll
+    for (int q = 0; q < 25; ++q) Amat[q] = 0.0;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) WR[q] = 0.0;
+    for (int J = 1; J <= 5; J++) Amat[5 * (J - 1)] = -PA[J - 1];
+    for (int I = 1; I <= 4; I++) Amat[I + 5 * (I - 1)] = 1.0;
+    sd_chhqr5(Amat, WR, 1.0E-5);
+    double BETA = 0.;
+    for (int J = 0; J < 5; J++)
+        if (WR[J] > BETA && WR[J] < 2.0) BETA = WR[J];
+    beta[j] = BETA;
+    const double num = SD_S(SD_M(SD_M(4.0, BETA), s[0]), s[1]);
+    const double den = SD_A(SD_S(SD_M(SD_M(SD_M(16.0, BETA), BETA), s[3]), SD_M(SD_M(8.0, BETA), s[4])), s[2]);
+    const double sm = -0.5 * (num * NXZ) / (den * NXZ);
+    l.smagc[j] = sm;
+    l.coef[j] = (R)(sm * l.d23[j]);
+}
+#undef SD_M
+#undef SD_A
+#undef SD_S
+
+// nu = max(coef(J) |S|, -1/RE) over the N2M planes (|S| left in nu by k_sgs_raw)
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_sgs_apply(StepArgs<R> a, LesArgs<R> l) {
+    const Geo g = a.g;
+    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (unsigned)g.n2m * (unsigned)g.np) return;
+    const int j = 1 + (int)(tid / (unsigned)g.np);
+    R *nup = l.nu + (long long)g.np + tid;   // fidx(g, 0, j, 0) + e with j >= 1
+    const R t = l.coef[j] * *nup;
+    *nup = t > -l.reninv ? t : -l.reninv;
+}
+
+// ---------------------------------------------------------------------------------
 // WALLMODEL_INSTANT: one thread per bottom-wall point; FP64.  The reference's Newton loop
 // has no cap; here a point that has not converged after l.wall_cap iterations is counted
 // and the step reports C3D_ENOTCONV.
@@ -1186,6 +1437,16 @@ int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *n
             mark(ch, nl, "sgs_raw", N * (6 * 8 + 22 * Rb));
             k_sgs_dyn<R><<<g.n2m, 256, 0, st>>>(a, l);
             mark(ch, nl, "sgs_dyn", N * 23 * Rb);
+        } else if (ch->files == 3) {
+            if ((rc = wall_model())) return rc;
+            k_sgs_raw<R><<<nblk((long long)g.n2m * g.np), TPB, 0, st>>>(a, l);
+            mark(ch, nl, "sgs_raw", N * (6 * 8 + 22 * Rb));
+            k_sgs_sd_sums<R><<<dim3(ch->sdnt, g.n2m), 256, 0, st>>>(a, l, ch->sdpart);
+            mark(ch, nl, "sgs_sd_sums", N * 21 * Rb);
+            k_sgs_sd_coef<R><<<(g.n2m + 31) / 32, 32, 0, st>>>(a, l, ch->sdpart, ch->sdnt, ch->sdbeta);
+            k_sgs_apply<R><<<nblk((long long)g.n2m * g.np), TPB, 0, st>>>(a, l);
+            *nl += 1;
+            mark(ch, nl, "sgs_sd_apply", N * 2 * Rb);
         }
         if (fork) ch->wjoin_pending = 1;
         return 0;

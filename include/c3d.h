@@ -62,7 +62,8 @@ extern "C" {
  *                                             h,hm,hc,hp (n2 values, index J-1)
  *   /MESH4/ DYM,DYC,DYP(1:N2)              -> dym,dyc,dyp (n2 values, index J-1)
  *   /PARA/  RE                             -> re
- *   /FINOUT/ FILES (SGS model)             -> files  (0 none, 1 SGSDY, 2 SGSCS)
+ *   /FINOUT/ FILES (SGS model)             -> files  (0 none, 1 SGSDY, 2 SGSCS,
+ *                                             3 SGSSD)
  *   /WALLMODEL/ WMODEL                     -> wmodel (0 none, 1 WALLMODEL_INSTANT,
  *                                             3 MARUSIC1, 4 WALLMODEL_WERNER,
  *                                             5 PIOMELLI; with 1, Y(0) must be 0:
@@ -124,7 +125,7 @@ int c3d_set_device(int device);
  *               upload, step, download in one call.
  *
  * LES (files != 0, compact3d.f:931-937): each step zeroes SGSVIS and runs the SGS
- * model (SGSDY or SGSCS) and, with wmodel != 0, the wall model before BCOND; the
+ * model (SGSDY, SGSCS or SGSSD) and, with wmodel != 0, the wall model before BCOND; the
  * SGS fluxes and the wall-stress terms enter RHS1-3.  SGSVIS passed to c3d_upload
  * is not used (the step recomputes it); c3d_download / c3d_getup return it.  With
  * wmodel = 0 the step first evaluates WALLSS on the current field, which is what the
@@ -135,7 +136,13 @@ int c3d_set_device(int device);
  * 4815-4958) sets both walls' stresses from the Werner-Wengle power law and WSM(1)
  * from the bottom wall; like the reference it takes the x neighbour of a wall point
  * with the z index (IPA(K), IMA(K)), which the reference's index arrays allow only for
- * N3 <= N1, so c3d_create refuses wmodel = 4 on other grids.  MARUSIC1 (wmodel 3,
+ * N3 <= N1, so c3d_create refuses wmodel = 4 on other grids.  SGSSD (files 3,
+ * compact3d.f:1502-1948) is the scale-dependent dynamic model: per plane the Germano
+ * sums at the test filters 2 DELTA (FILTER) and 4 DELTA (FILTER4) give a quintic
+ * (COEFFICIENT) whose largest real root in (0, 2), by the reference's companion-matrix
+ * QR iteration with its deflation tolerance 1e-5 (DQRRT/CHHQR), is the scale
+ * dependence BETA; the coefficient is the dynamic one at 2 DELTA with BETA in M_ij (the
+ * reference's file BETA.plt is not written).  MARUSIC1 (wmodel 3,
  * compact3d.f:4336-4495) and PIOMELLI (wmodel 5, 4960-5110) take u_tau of each wall
  * from the log law on the plane mean of u at a reference plane (MARUSIC1: the Y(J)
  * nearest 0.06; PIOMELLI: the first cell) by the reference's bisection, and set both

@@ -68,6 +68,10 @@ def lib():
         L.orc_operator.argtypes = [vp, ip, dp, dp]
         L.orc_sgs_rhs.argtypes = [vp, dp, dp, dp]
         L.orc_wallmodel.argtypes = [vp, dp]
+        L.orc_dqrrt.restype = ip
+        L.orc_dqrrt.argtypes = [dp, ip, ctypes.c_double, dp, dp, dp]
+        L.orc_get_beta.argtypes = [vp, dp]
+        L.orc_filter.argtypes = [vp, ip, dp, ip]
         for f in ("orc_ctdma11", "orc_ctdma_recip"):
             getattr(L, f).argtypes = [ip, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp, dp]
         L.orc_tdmap.argtypes = [ip, dp, dp, dp, dp, dp]
@@ -185,6 +189,18 @@ class Oracle:
         hit the iteration cap, -1 if a shifted point found no cell)."""
         return lib().orc_wallmodel(self.h, _p(U))
 
+    def get_beta(self):
+        """SGSSD's scale-dependence BETA(1:N2M) of the last SGS evaluation (unclipped)."""
+        b = np.zeros(self.grid.n2m)
+        lib().orc_get_beta(self.h, _p(b))
+        return b
+
+    def filter(self, F, four=False):
+        """FILTER (or FILTER4) of fields F (n, N3M, N1M) (x fastest); returns a copy."""
+        F = np.ascontiguousarray(F, dtype=np.float64).copy()
+        lib().orc_filter(self.h, int(four), _p(F.reshape(-1)), F.shape[0])
+        return F
+
     def set_wall(self, tauw=None, taub=None, ifwall=0):
         lib().orc_set_wall(self.h, _p(tauw), _p(taub), ifwall)
 
@@ -245,6 +261,16 @@ def dft2d(z, sign=-1):
     n1, n3 = z.shape
     lib().orc_dft2d(n1, n3, z.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), sign)
     return z
+
+
+def dqrrt(pa, eps=1.0e-5):
+    """DQRRT/CHHQR: (BETA, eigenvalues as complex, ok) for x^n + pa[0] x^(n-1) + ... + pa[n-1]."""
+    pa = np.ascontiguousarray(pa, dtype=np.float64)
+    n = len(pa)
+    wr, wi = np.zeros(n), np.zeros(n)
+    beta = (ctypes.c_double * 1)()
+    ok = lib().orc_dqrrt(_p(pa), n, eps, beta, _p(wr), _p(wi))
+    return beta[0], wr + 1j * wi, ok
 
 
 def set_threads(n: int):

@@ -54,6 +54,7 @@ struct Orc {
     double WSM[3] = {0.0, 0.0, 0.0};  // /WSMEM/ WSM(1:3) as the SGS model and wall model see it
     double TAOW = 0.0;                // /WALLTAO/ TAOW
     std::vector<double> SMAGC;        // /SGSMEAN/ SMAGC(1:N2M)
+    std::vector<double> BETA;         // SGSSD's scale-dependence BETA per plane (unclipped)
     std::vector<double> SGS;          // SGSVIS when the caller passes none
     int wall_iter_cap = 10000;        // Newton iterations allowed per wall point
     // work arrays of GETUP / UHCALC / DPCALC
@@ -1522,6 +1523,312 @@ void sgscs(Orc &g, const double *U, double *SGSVIS) {
     }
 }
 
+// FILTER4 (compact3d.f:5481-5545): five-point (1,4,2,4,1)/12 in x, then in z, periodic.
+void filter4(Orc &g, std::vector<double> &F, int N) {
+    const int N1M = g.N1M, N3M = g.N3M;
+    std::vector<double> T((size_t)N1M * N3M);
+    auto wrap = [](int i, int n) { return i < 1 ? i + n : (i > n ? i - n : i); };
+    for (int L = 1; L <= N; L++) {
+        double *f = F.data() + (size_t)N1M * N3M * (L - 1);
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                auto at = [&](int i) { return f[(wrap(i, N1M) - 1) + (size_t)N1M * (K - 1)]; };
+                T[(I - 1) + (size_t)N1M * (K - 1)] = (at(I - 2) + 4.0 * at(I - 1) + 2.0 * at(I) + 4.0 * at(I + 1) + at(I + 2)) / 12.0;
+            }
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                auto at = [&](int k) { return T[(I - 1) + (size_t)N1M * (wrap(k, N3M) - 1)]; };
+                f[(I - 1) + (size_t)N1M * (K - 1)] = (at(K - 2) + 4.0 * at(K - 1) + 2.0 * at(K) + 4.0 * at(K + 1) + at(K + 2)) / 12.0;
+            }
+    }
+}
+
+// CHHQR (compact3d.f:11571-11676): eigenvalues (WR, WI) of the N x N upper Hessenberg
+// matrix A (column-major, A(i,j) = A[(i-1) + N (j-1)], overwritten) by the Francis
+// double-shift QR iteration.  The active block is rows L..M; a subdiagonal entry with
+// |A(L,L-1)| <= EPS (|A(L-1,L-1)| + |A(L,L)|) splits it; a 1x1 block gives a real root, a
+// 2x2 block a pair from its quadratic; otherwise one double-shift sweep of 3x3
+// Householder reflections chases the bulge from L to M.  At most 60 sweeps per
+// deflation; returns 0 on that failure (roots not yet found are left as they were).
+int chhqr(double *A, int N, double *WR, double *WI, double EPS) {
+    auto a = [&](int i, int j) -> double & { return A[(i - 1) + (size_t)N * (j - 1)]; };
+    int M = N, IT = 0;
+    while (M > 0) {
+        int L = M;
+        while (L > 1 && std::fabs(a(L, L - 1)) > EPS * (std::fabs(a(L - 1, L - 1)) + std::fabs(a(L, L)))) L = L - 1;
+        if (L == M) {
+            WR[M - 1] = a(M, M);
+            WI[M - 1] = 0.0;
+            M = M - 1;
+            IT = 0;
+            continue;
+        }
+        if (L == M - 1) {
+            const double B = -(a(M, M) + a(M - 1, M - 1));
+            const double C = a(M, M) * a(M - 1, M - 1) - a(M, M - 1) * a(M - 1, M);
+            const double W = B * B - 4 * C;
+            const double Y = std::sqrt(std::fabs(W));
+            if (W > 0.0) {
+                const double XY = B < 0.0 ? -1.0 : 1.0;
+                WR[M - 1] = (-B - XY * Y) / 2.0;
+                WR[M - 2] = C / WR[M - 1];
+                WI[M - 1] = 0.0;
+                WI[M - 2] = 0.0;
+            } else {
+                WR[M - 1] = -B / 2.0;
+                WR[M - 2] = WR[M - 1];
+                WI[M - 1] = Y / 2.0;
+                WI[M - 2] = -WI[M - 1];
+            }
+            M = M - 2;
+            IT = 0;
+            continue;
+        }
+        if (IT >= 60) return 0;
+        IT = IT + 1;
+        for (int J = L + 2; J <= M; J++) a(J, J - 2) = 0.0;
+        for (int J = L + 3; J <= M; J++) a(J, J - 3) = 0.0;
+        for (int K = L; K <= M - 1; K++) {
+            double P, Q, R;
+            if (K != L) {
+                P = a(K, K - 1);
+                Q = a(K + 1, K - 1);
+                R = K != M - 1 ? a(K + 2, K - 1) : 0.0;
+            } else {   // first column of (H - s1)(H - s2) from the trailing 2x2 block
+                const double X = a(M, M) + a(M - 1, M - 1);
+                const double Y = a(M - 1, M - 1) * a(M, M) - a(M - 1, M) * a(M, M - 1);
+                P = a(L, L) * (a(L, L) - X) + a(L, L + 1) * a(L + 1, L) + Y;
+                Q = a(L + 1, L) * (a(L, L) + a(L + 1, L + 1) - X);
+                R = a(L + 1, L) * a(L + 2, L + 1);
+            }
+            if (std::fabs(P) + std::fabs(Q) + std::fabs(R) == 0.0) continue;
+            const double XY = P < 0.0 ? -1.0 : 1.0;
+            const double S = XY * std::sqrt(P * P + Q * Q + R * R);
+            if (K != L) a(K, K - 1) = -S;
+            const double E = -Q / S, F = -R / S, X = -P / S;
+            const double Y = -X - F * R / (P + S);
+            const double G = E * R / (P + S);
+            const double Z = -X - E * Q / (P + S);
+            for (int J = K; J <= M; J++) {   // rows K..K+2 from the left
+                double p = X * a(K, J) + E * a(K + 1, J);
+                double q = E * a(K, J) + Y * a(K + 1, J);
+                double r = F * a(K, J) + G * a(K + 1, J);
+                if (K != M - 1) {
+                    p = p + F * a(K + 2, J);
+                    q = q + G * a(K + 2, J);
+                    r = r + Z * a(K + 2, J);
+                    a(K + 2, J) = r;
+                }
+                a(K + 1, J) = q;
+                a(K, J) = p;
+            }
+            const int JJ = K + 3 >= M ? M : K + 3;
+            for (int I = L; I <= JJ; I++) {   // columns K..K+2 from the right
+                double p = X * a(I, K) + E * a(I, K + 1);
+                double q = E * a(I, K) + Y * a(I, K + 1);
+                double r = F * a(I, K) + G * a(I, K + 1);
+                if (K != M - 1) {
+                    p = p + F * a(I, K + 2);
+                    q = q + G * a(I, K + 2);
+                    r = r + Z * a(I, K + 2);
+                    a(I, K + 2) = r;
+                }
+                a(I, K + 1) = q;
+                a(I, K) = p;
+            }
+        }
+    }
+    return 1;
+}
+
+// DQRRT (compact3d.f:11548-11569): the roots of x^N + PA(1) x^(N-1) + ... + PA(N) as the
+// eigenvalues of the companion matrix (first row -PA, ones on the subdiagonal); BETA is
+// the largest real part in (0, 2), 0 if there is none (complex roots count by their real
+// part, as in the reference's scan).
+double dqrrt(const double *PA, int N, double EPS) {
+    std::vector<double> B((size_t)N * N, 0.0), WR(N, 0.0), WI(N, 0.0);
+    for (int J = 1; J <= N; J++) B[(size_t)N * (J - 1)] = -PA[J - 1];
+    for (int I = 1; I <= N - 1; I++) B[I + (size_t)N * (I - 1)] = 1.0;
+    chhqr(B.data(), N, WR.data(), WI.data(), EPS);
+    double BETA = 0.;
+    for (int J = 0; J < N; J++)
+        if (WR[J] > BETA && WR[J] < 2.0) BETA = WR[J];
+    return BETA;
+}
+
+// COEFFICIENT (compact3d.f:2079-2095): the quintic of the scale-dependent model,
+// PA(1..5) of x^5 + PA(1) x^4 + ... + PA(5), from the plane sums of the two test filters.
+void coefficient(double A1, double B1, double C1, double D1, double E1, double A2, double B2, double C2,
+                 double D2, double E2, double *PA) {
+    PA[4] = (B2 * C1 - B1 * C2) / (A1 * D2);
+    PA[3] = (A1 * C2 - B2 * E1) / (A1 * D2);
+    PA[2] = (B2 * D1 + B1 * E2 - A2 * C1) / (A1 * D2);
+    PA[1] = (A2 * E1 - A1 * E2) / (A1 * D2);
+    PA[0] = -(A2 * D1 + B1 * D2) / (A1 * D2);
+}
+
+// SGSSD (compact3d.f:1502-1948): the scale-dependent dynamic model.  Per plane, the
+// Germano identity at the test filters 2 DELTA (FILTER) and 4 DELTA (FILTER4) gives the
+// sums A..E of each; the scale-dependence BETA solves the quintic of COEFFICIENT (DQRRT,
+// EPS 1.0E-5); the coefficient is then the dynamic one at 2 DELTA with
+// M_ij = 4 DELTA^(2/3) BETA |S~| S~_ij - (DELTA^(2/3) |S| S_ij)~ (the unclipped BETA; the
+// reference clips only the copy BETAZ it writes to a file every 100 steps).
+void sgssd(Orc &g, const double *U, double *SGSVIS) {
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const size_t NP = (size_t)N1M * N3M;
+    const double NXZ = 1.0 / (double)(N1M * N3M), RENINV = 1. / g.RE;
+    std::vector<double> SR(NP * 6), COM(NP * 6), COM1(NP * 6), SR1(NP * 6), UC(NP * 3);
+    g.BETA.assign((size_t)g.N2 + 1, 0.0);
+    for (int J = 1; J <= N2M; J++) {
+        const double DXYZ = 1.0 / g.DX1 * g.DY[J] / g.DX3;
+        // one test filter (FILTER or FILTER4) of the raw quantities, then its five sums
+        auto level = [&](bool four, double sa, double sd, double se, double &A, double &B, double &C, double &D, double &E) {
+            strain(g, U, SR, J);
+            for (size_t q = 0; q < NP; q++) {
+                double DELTA2 = std::pow(DXYZ, 2. / 3.);
+                double SUMSR = sumsq6(SR[q], SR[q + NP], SR[q + 2 * NP], SR[q + 3 * NP], SR[q + 4 * NP], SR[q + 5 * NP]);
+                double ABSSR = std::sqrt(2. * SUMSR);
+                double DELABS = DELTA2 * ABSSR;
+                for (int c = 0; c < 6; c++) COM1[q + c * NP] = DELABS * SR[q + c * NP];
+            }
+            if (four) {
+                filter4(g, COM1, 6);
+                filter4(g, SR, 6);
+            } else {
+                filter(g, COM1, 6);
+                filter(g, SR, 6);
+            }
+            for (size_t q = 0; q < NP; q++) {
+                double SUMFSR = sumsq6(SR[q], SR[q + NP], SR[q + 2 * NP], SR[q + 3 * NP], SR[q + 4 * NP], SR[q + 5 * NP]);
+                double ABSFSR = std::sqrt(2. * SUMFSR);
+                double FDXYZ = std::pow(DXYZ, 2. / 3.);
+                double FDABS = FDXYZ * ABSFSR;
+                for (int c = 0; c < 6; c++) SR1[q + c * NP] = FDABS * SR[q + c * NP];
+            }
+            const int JP = J + 1;
+            for (int K = 1; K <= N3M; K++) {
+                const int KP = g.KPA[K];
+                for (int I = 1; I <= N1M; I++) {
+                    const int IP = g.IPA[I];
+                    const size_t q = (I - 1) + (size_t)N1M * (K - 1);
+                    double a = (U[g.iuc(I, J, K, 1)] + U[g.iuc(IP, J, K, 1)]) * 0.5;
+                    double b = (U[g.iuc(I, J, K, 2)] + U[g.iuc(I, JP, K, 2)]) * 0.5;
+                    double c = (U[g.iuc(I, J, K, 3)] + U[g.iuc(I, J, KP, 3)]) * 0.5;
+                    UC[q] = a;
+                    UC[q + NP] = b;
+                    UC[q + 2 * NP] = c;
+                    COM[q] = a * a;
+                    COM[q + NP] = a * b;
+                    COM[q + 2 * NP] = a * c;
+                    COM[q + 3 * NP] = b * b;
+                    COM[q + 4 * NP] = b * c;
+                    COM[q + 5 * NP] = c * c;
+                }
+            }
+            if (four) {
+                filter4(g, UC, 3);
+                filter4(g, COM, 6);
+            } else {
+                filter(g, UC, 3);
+                filter(g, COM, 6);
+            }
+            A = 0.0, B = 0.0, C = 0.0, D = 0.0, E = 0.0;
+            for (size_t q = 0; q < NP; q++) {
+                const double u1 = UC[q], u2 = UC[q + NP], u3 = UC[q + 2 * NP];
+                const double X11 = COM[q] - u1 * u1, X12 = COM[q + NP] - u1 * u2, X13 = COM[q + 2 * NP] - u1 * u3;
+                const double X22 = COM[q + 3 * NP] - u2 * u2, X23 = COM[q + 4 * NP] - u2 * u3,
+                             X33 = COM[q + 5 * NP] - u3 * u3;
+                const double *s = &SR1[q], *m = &COM1[q];
+                A = A + 2. * X12 * s[NP] + X11 * s[0] + 2. * X13 * s[2 * NP] + X22 * s[3 * NP] + 2. * X23 * s[4 * NP] + X33 * s[5 * NP];
+                B = B + 2. * X12 * m[NP] + X11 * m[0] + 2. * X13 * m[2 * NP] + X22 * m[3 * NP] + 2. * X23 * m[4 * NP] + X33 * m[5 * NP];
+            }
+            for (size_t q = 0; q < NP; q++) {
+                const double *s = &SR1[q], *m = &COM1[q];
+                C = C + 2. * m[NP] * m[NP] + m[0] * m[0] + 2. * m[2 * NP] * m[2 * NP] + m[3 * NP] * m[3 * NP] +
+                    2. * m[4 * NP] * m[4 * NP] + m[5 * NP] * m[5 * NP];
+                D = D + 2. * s[NP] * s[NP] + s[0] * s[0] + 2. * s[2 * NP] * s[2 * NP] + s[3 * NP] * s[3 * NP] +
+                    2. * s[4 * NP] * s[4 * NP] + s[5 * NP] * s[5 * NP];
+                E = E + 2. * s[NP] * m[NP] + s[0] * m[0] + 2. * s[2 * NP] * m[2 * NP] + s[3 * NP] * m[3 * NP] +
+                    2. * s[4 * NP] * m[4 * NP] + s[5 * NP] * m[5 * NP];
+            }
+            A = sa * A * NXZ;
+            B = -2.0 * B * NXZ;
+            C = 4.0 * C * NXZ;
+            D = sd * D * NXZ;
+            E = se * E * NXZ;
+        };
+        double A1, B1, C1, D1, E1, A2, B2, C2, D2, E2, PA[5];
+        level(false, -8.0, 64.0, 32.0, A1, B1, C1, D1, E1);
+        level(true, -32.0, 1024.0, 128.0, A2, B2, C2, D2, E2);
+        coefficient(A1, B1, C1, D1, E1, A2, B2, C2, D2, E2, PA);
+        const double BETA = dqrrt(PA, 5, 1.0E-5);
+        g.BETA[J] = BETA;
+        // the coefficient at 2 DELTA with the scale-dependent M_ij
+        strain(g, U, SR, J);
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                const size_t q = (I - 1) + (size_t)N1M * (K - 1);
+                double DELTA2 = std::pow(DXYZ, 2. / 3.);
+                double SUMSR = sumsq6(SR[q], SR[q + NP], SR[q + 2 * NP], SR[q + 3 * NP], SR[q + 4 * NP], SR[q + 5 * NP]);
+                double ABSSR = std::sqrt(2. * SUMSR);
+                SGSVIS[g.iu(I, J, K)] = ABSSR;
+                double DELABS = DELTA2 * ABSSR;
+                for (int c = 0; c < 6; c++) COM[q + c * NP] = DELABS * SR[q + c * NP];
+            }
+        filter(g, COM, 6);
+        filter(g, SR, 6);
+        for (size_t q = 0; q < NP; q++) {
+            double SUMFSR = sumsq6(SR[q], SR[q + NP], SR[q + 2 * NP], SR[q + 3 * NP], SR[q + 4 * NP], SR[q + 5 * NP]);
+            double ABSFSR = std::sqrt(2. * SUMFSR);
+            double FDXYZ = 4.0 * std::pow(DXYZ, 2. / 3.) * BETA;
+            double FDABS = FDXYZ * ABSFSR;
+            for (int c = 0; c < 6; c++) SR[q + c * NP] = FDABS * SR[q + c * NP] - COM[q + c * NP];
+        }
+        const int JP = J + 1;
+        for (int K = 1; K <= N3M; K++) {
+            const int KP = g.KPA[K];
+            for (int I = 1; I <= N1M; I++) {
+                const int IP = g.IPA[I];
+                const size_t q = (I - 1) + (size_t)N1M * (K - 1);
+                double a = (U[g.iuc(I, J, K, 1)] + U[g.iuc(IP, J, K, 1)]) * 0.5;
+                double b = (U[g.iuc(I, J, K, 2)] + U[g.iuc(I, JP, K, 2)]) * 0.5;
+                double c = (U[g.iuc(I, J, K, 3)] + U[g.iuc(I, J, KP, 3)]) * 0.5;
+                UC[q] = a;
+                UC[q + NP] = b;
+                UC[q + 2 * NP] = c;
+                COM[q] = a * a;
+                COM[q + NP] = a * b;
+                COM[q + 2 * NP] = a * c;
+                COM[q + 3 * NP] = b * b;
+                COM[q + 4 * NP] = b * c;
+                COM[q + 5 * NP] = c * c;
+            }
+        }
+        filter(g, UC, 3);
+        filter(g, COM, 6);
+        double SUMNUM = 0., SUMDEN = 0.;
+        for (size_t q = 0; q < NP; q++) {
+            const double u1 = UC[q], u2 = UC[q + NP], u3 = UC[q + 2 * NP];
+            double XL11 = COM[q] - u1 * u1, XL12 = COM[q + NP] - u1 * u2, XL13 = COM[q + 2 * NP] - u1 * u3;
+            double XL22 = COM[q + 3 * NP] - u2 * u2, XL23 = COM[q + 4 * NP] - u2 * u3, XL33 = COM[q + 5 * NP] - u3 * u3;
+            const double *m = &SR[q];
+            double SQMM = sumsq6(m[0], m[NP], m[2 * NP], m[3 * NP], m[4 * NP], m[5 * NP]);
+            double SQLM = 2. * XL12 * m[NP] + XL11 * m[0] + 2. * XL13 * m[2 * NP] + XL22 * m[3 * NP] +
+                          2. * XL23 * m[4 * NP] + XL33 * m[5 * NP];
+            SUMDEN = SUMDEN + SQMM;
+            SUMNUM = SUMNUM + SQLM;
+        }
+        SUMNUM = SUMNUM * NXZ;
+        SUMDEN = SUMDEN * NXZ;
+        g.SMAGC[J] = -0.5 * SUMNUM / SUMDEN;
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                double TURBV = g.SMAGC[J] * std::pow(DXYZ, 2. / 3.) * SGSVIS[g.iu(I, J, K)];
+                SGSVIS[g.iu(I, J, K)] = std::max(TURBV, -RENINV) * 1.0;
+            }
+    }
+}
+
 // WALLSS (compact3d.f:11077-11143): plane-mean wall shear into wsm[0..2] (/WSMEM/ WSM),
 // one running sum in K, I order.  The reference adds the top wall's u-shear WST(I,K,1)
 // to all three components (scaled by ALY-1).
@@ -2261,8 +2568,39 @@ void orc_get_wall(void *h, double *tauw, double *taub, double *wsm) {
 void orc_set_wsm(void *h, const double *wsm) { std::memcpy(((Orc *)h)->WSM, wsm, 3 * sizeof(double)); }
 void orc_set_wall_iter_cap(void *h, int cap) { ((Orc *)h)->wall_iter_cap = cap; }
 
-// The SGS model alone (SGSDY for FILES=1, SGSCS for FILES=2) on U, after GETUP's zeroing
+// The SGS model alone (SGSDY for FILES=1, SGSCS for FILES=2, SGSSD for FILES=3) on U, after GETUP's zeroing
 // of SGSVIS; smagc (length N2M, may be null) receives SMAGC(1:N2M).
+// DQRRT's BETA for x^n + pa[0] x^(n-1) + ... + pa[n-1] (n <= 8), EPS as given; wr/wi
+// (may be null) receive CHHQR's eigenvalues and the return value is CHHQR's flag.
+int orc_dqrrt(const double *pa, int n, double eps, double *beta, double *wr, double *wi) {
+    if (n < 1 || n > 8) return -1;
+    std::vector<double> B((size_t)n * n, 0.0), WR(n, 0.0), WI(n, 0.0);
+    for (int J = 1; J <= n; J++) B[(size_t)n * (J - 1)] = -pa[J - 1];
+    for (int I = 1; I <= n - 1; I++) B[I + (size_t)n * (I - 1)] = 1.0;
+    const int ok = chhqr(B.data(), n, WR.data(), WI.data(), eps);
+    for (int J = 0; J < n; J++) {
+        if (wr) wr[J] = WR[J];
+        if (wi) wi[J] = WI[J];
+    }
+    *beta = dqrrt(pa, n, eps);
+    return ok;
+}
+
+// FILTER (four = 0) or FILTER4 (four = 1) in place on n fields of N1M x N3M (x fastest)
+void orc_filter(void *h, int four, double *F, int n) {
+    Orc &g = *(Orc *)h;
+    std::vector<double> v(F, F + (size_t)g.N1M * g.N3M * n);
+    if (four) filter4(g, v, n);
+    else filter(g, v, n);
+    std::copy(v.begin(), v.end(), F);
+}
+
+// SGSSD's BETA(1:N2M) of the last SGS evaluation
+void orc_get_beta(void *h, double *beta) {
+    Orc &g = *(Orc *)h;
+    for (int J = 1; J <= g.N2M; J++) beta[J - 1] = J < (int)g.BETA.size() ? g.BETA[J] : 0.0;
+}
+
 int orc_sgs(void *h, const double *U, double *SGSVIS, double *smagc) {
     Orc &g = *(Orc *)h;
     for (int K = 1; K <= g.N3; K++)
@@ -2270,6 +2608,7 @@ int orc_sgs(void *h, const double *U, double *SGSVIS, double *smagc) {
             for (int I = 1; I <= g.N1; I++) SGSVIS[g.iu(I, J, K)] = 0.0;
     if (g.FILES == 1) sgsdy(g, U, SGSVIS);
     else if (g.FILES == 2) sgscs(g, U, SGSVIS);
+    else if (g.FILES == 3) sgssd(g, U, SGSVIS);
     else return C3D_EINVAL;
     if (smagc)
         for (int J = 1; J <= g.N2M; J++) smagc[J - 1] = g.SMAGC[J];
@@ -2365,7 +2704,7 @@ int orc_getup(void *h, double *U, double *P, double *HH, double *SGSVIS, int NTI
               double *PRESG, double *PRESG3) {
     Orc &g = *(Orc *)h;
     (void)NTIME;
-    if (g.FILES < 0 || g.FILES > 2 || g.WMODEL < 0 || g.WMODEL == 2 || g.WMODEL > 5) return C3D_EINVAL;
+    if (g.FILES < 0 || g.FILES > 3 || g.WMODEL < 0 || g.WMODEL == 2 || g.WMODEL > 5) return C3D_EINVAL;
     if (g.WMODEL == 4 && g.N3M > g.N1M) return C3D_EINVAL;   // WERNER indexes INDX(N1M) with K
     const int N1 = g.N1, N2 = g.N2, N3 = g.N3;
     double *UH = g.UH.data(), *HH2 = g.HH2.data();
@@ -2402,6 +2741,7 @@ int orc_getup(void *h, double *U, double *P, double *HH, double *SGSVIS, int NTI
     }
     if (g.FILES == 1) sgsdy(g, U, SGSVIS);
     if (g.FILES == 2) sgscs(g, U, SGSVIS);
+    if (g.FILES == 3) sgssd(g, U, SGSVIS);
     int status = 0;
     if (g.FILES != 0) {   // WALL_MODEL (compact3d.f:1952-2026)
         if (g.WMODEL == 0) {

@@ -65,7 +65,7 @@ def test_create_rejects_null_metrics(L):
 
 def test_create_rejects_bad_precision_and_models(L):
     g, _ = make_grid("small32")
-    for field, val in (("precision", 7), ("files", 3), ("re", -1.0), ("wmodel", 2), ("wmodel", 6), ("wmodel", -1)):
+    for field, val in (("precision", 7), ("files", 4), ("re", -1.0), ("wmodel", 2), ("wmodel", 6), ("wmodel", -1)):
         s = g.struct()
         setattr(s, field, val)
         h = ctypes.c_void_p()

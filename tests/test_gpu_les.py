@@ -73,6 +73,9 @@ def gpu_from(libc3d, orc, g, U, P, HH, precision=C3D_FP64):
     ("les32dy", dict(wmodel=3, n2m=32)),    # dynamic + MARUSIC1, ZS = 2
     ("les32cs", dict(wmodel=5)),            # Smagorinsky + PIOMELLI
     ("les32dy", dict(wmodel=5, y0=1e-5)),   # PIOMELLI with H(1) 5e-6 below YC(1): YP climbs
+    ("les32dy", dict(files=3)),             # SGSSD (scale-dependent) + WALLMODEL_INSTANT
+    ("les32dy", dict(files=3, wmodel=0, cks=2.0)),   # SGSSD, no-slip walls, stretched y
+    ("les32dy", dict(files=3, wmodel=3)),   # SGSSD + MARUSIC1
 ])
 def test_les_one_step_fp64(libc3d, oracle_mod, name, over):
     g, dt, orc, U, P, HH, S, pg, pg3 = warm_start(oracle_mod, name, **over)
@@ -115,7 +118,8 @@ def test_les_ten_steps_fp64(libc3d, oracle_mod):
     assert d["divmax"] < 1e-12
 
 
-@pytest.mark.parametrize("name,over", [("les32dy", {}), ("les32cs", dict(wmodel=3)), ("les32dy", dict(wmodel=5))])
+@pytest.mark.parametrize("name,over", [("les32dy", {}), ("les32cs", dict(wmodel=3)), ("les32dy", dict(wmodel=5)),
+                                       ("les32dy", dict(files=3))])
 def test_les_mixed_against_fp64(libc3d, oracle_mod, name, over):
     g, dt, orc, U, P, HH, S, pg, pg3 = warm_start(oracle_mod, name, **over)
     c64 = gpu_from(libc3d, orc, g, U, P, HH, C3D_FP64)

@@ -394,3 +394,91 @@ def test_marusic_shift_follows_linear_u(oracle_mod):
             np.testing.assert_allclose(tw[i, 1:n3 + 1, wall], want, rtol=0, atol=4e-7 * ut)
             checked += 1
     assert checked >= n1
+
+
+def test_dqrrt_matches_numpy_roots(oracle_mod):
+    """DQRRT/CHHQR (compact3d.f:11548-11676): with a tight deflation tolerance the
+    companion-matrix eigenvalues are the polynomial's roots; BETA is the largest real part
+    in (0, 2), complex pairs counting by their real part, 0 when there is none.  With the
+    reference's EPS = 1e-5 the deflation is early: a root moves by up to about EPS, and
+    near-double roots by up to about sqrt(EPS)."""
+    rng = np.random.default_rng(5)
+    for _ in range(20):
+        r = rng.uniform(-3.0, 3.0, 5)
+        pa = np.poly(r)[1:]
+        beta, ev, ok = oracle_mod.dqrrt(pa, eps=1e-14)
+        assert ok == 1
+        np.testing.assert_allclose(np.sort(ev.real), np.sort(r), atol=1e-7)
+        inside = [x for x in r if 0.0 < x < 2.0]
+        assert beta == pytest.approx(max(inside) if inside else 0.0, abs=1e-7)
+        beta5, _, _ = oracle_mod.dqrrt(pa)   # near-double roots move by up to sqrt(EPS)
+        assert beta5 == pytest.approx(max(inside) if inside else 0.0, abs=2e-2)
+    r = np.array([0.5 + 0.3j, 0.5 - 0.3j, 1.2, -0.7, 2.5])
+    beta, ev, ok = oracle_mod.dqrrt(np.real(np.poly(r))[1:], eps=1e-14)
+    np.testing.assert_allclose(np.sort_complex(ev), np.sort_complex(r), atol=1e-7)
+    assert beta == pytest.approx(1.2, abs=1e-9)
+    r = np.array([0.6 + 0.3j, 0.6 - 0.3j, 0.2, -0.7, 2.5])
+    beta, _, _ = oracle_mod.dqrrt(np.real(np.poly(r))[1:], eps=1e-14)
+    assert beta == pytest.approx(0.6, abs=1e-9)
+
+
+@pytest.mark.parametrize("four", [False, True])
+def test_filters_on_fourier_modes(oracle_mod, four):
+    """FILTER multiplies a mode cos(a x + b z) by (4 + 2 cos a)(4 + 2 cos b) / 36 and
+    FILTER4 (compact3d.f:5481-5545) by (2 + 8 cos a + 2 cos 2a)(2 + 8 cos b + 2 cos 2b)
+    / 144, a and b the mode's phase steps per cell."""
+    g, _ = _grid("les32dy")
+    o = oracle_mod.Oracle(g)
+    n1, n3 = g.n1m, g.n3m
+    i, k = np.meshgrid(np.arange(n1), np.arange(n3))
+    F = np.stack([np.cos(2 * np.pi * (mx * i / n1 + mz * k / n3)) for mx, mz in ((1, 0), (3, 2), (5, 7))])
+    out = o.filter(F, four)
+    for q, (mx, mz) in enumerate(((1, 0), (3, 2), (5, 7))):
+        a, b = 2 * np.pi * mx / n1, 2 * np.pi * mz / n3
+        if four:
+            gain = (2 + 8 * np.cos(a) + 2 * np.cos(2 * a)) * (2 + 8 * np.cos(b) + 2 * np.cos(2 * b)) / 144
+        else:
+            gain = (4 + 2 * np.cos(a)) * (4 + 2 * np.cos(b)) / 36
+        np.testing.assert_allclose(out[q], gain * F[q], atol=1e-14)
+
+
+def test_sgssd_invariances(oracle_mod):
+    """SGSSD (compact3d.f:1502-1948): the Germano sums are quartic in the velocity, so the
+    quintic and BETA are unchanged when U is scaled, SGSVIS scales with U (where it is
+    not clipped), and a uniform velocity added to the field changes nothing (the filters
+    have unit weight sums)."""
+    g, _ = _grid("les32dy", files=3, wmodel=0, cks=2.0)
+    o = oracle_mod.Oracle(g)
+    U, P, HH = ic.loglaw(g, 2000.0)
+    o.project(U)
+    S0, sm0 = o.sgs(U)
+    b0 = o.get_beta()
+    assert np.all((b0 > 0) & (b0 < 2))
+    S1, sm1 = o.sgs(2.5 * U)
+    np.testing.assert_allclose(o.get_beta(), b0, rtol=1e-9)
+    np.testing.assert_allclose(sm1, sm0, rtol=1e-8)
+    sl = (slice(1, g.n1m + 1), slice(1, g.n2m + 1), slice(1, g.n3m + 1))
+    unclipped = 2.5 * S0[sl] > -1.0 / g.re
+    np.testing.assert_allclose(S1[sl][unclipped], 2.5 * S0[sl][unclipped], rtol=1e-8, atol=1e-20)
+    U2 = U.copy(order="F")
+    U2[..., 0] += 0.3
+    U2[..., 2] -= 0.2
+    S2, sm2 = o.sgs(U2)
+    np.testing.assert_allclose(o.get_beta(), b0, rtol=1e-8)
+    np.testing.assert_allclose(S2[sl], S0[sl], rtol=1e-8, atol=1e-14)
+
+
+def test_sgssd_step_runs_and_conserves(oracle_mod):
+    g, dt = _grid("les32dy", files=3)
+    o = oracle_mod.Oracle(g)
+    U, P, HH = ic.loglaw(g, 2000.0)
+    o.project(U)
+    f0 = o.chkmf(U)[0]
+    S = g.zeros_s()
+    pg = pg3 = 0.0
+    for n in range(1, 4):
+        pg, pg3 = o.getup(U, P, HH, n, dt, pg, pg3, S)
+    assert np.isfinite(U).all() and np.isfinite(S).all()
+    assert o.divcheck(U) < 1e-12
+    assert o.chkmf(U)[0] == pytest.approx(f0, rel=1e-10)
+    assert np.all((o.get_beta() >= 0) & (o.get_beta() < 2))
