@@ -199,6 +199,9 @@ void free_channel(c3d_channel *ch) {
     if (ch->wtaue) cudaFree(ch->wtaue);
     if (ch->wshift) cudaFree(ch->wshift);
     if (ch->sdpart) cudaFree(ch->sdpart);
+    if (ch->sfork) cudaEventDestroy(ch->sfork);
+    if (ch->sjoin) cudaEventDestroy(ch->sjoin);
+    if (ch->sside) cudaStreamDestroy(ch->sside);
     if (ch->sdbeta) cudaFree(ch->sdbeta);
     if (ch->wfork) cudaEventDestroy(ch->wfork);
     if (ch->wjoin) cudaEventDestroy(ch->wjoin);
@@ -479,11 +482,15 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
         }
         if ((ch->files == 1 || ch->files == 3) && cudaMalloc(&ch->dyn, 21 * (size_t)g.n2m * g.np * rs) != cudaSuccess)
             return fail(C3D_ENOMEM);
-        if (ch->files == 3) {   // SGSSD: tiles of 256 points per plane, at most 16
-            ch->sdnt = std::min(16, (g.np + 255) / 256);
+        if (ch->files == 3) {   // SGSSD: per-plane sums of tiles of 32 x 16 points
+            ch->sdnt = ((g.n1m + 31) / 32) * (g.n3m / 16);
             if (dalloc(&ch->sdpart, (size_t)g.n2m * ch->sdnt * 10) || dalloc(&ch->sdbeta, (size_t)g.n2 + 1))
                 return fail(C3D_ENOMEM);
             cudaMemset(ch->sdbeta, 0, ((size_t)g.n2 + 1) * 8);
+            if (cudaStreamCreateWithFlags(&ch->sside, cudaStreamNonBlocking) != cudaSuccess ||
+                cudaEventCreateWithFlags(&ch->sfork, cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&ch->sjoin, cudaEventDisableTiming) != cudaSuccess)
+                return fail(C3D_ECUDA);
         }
         const int nbw = (g.np + 127) / 128;   // blocks of k_wall (TPB = 128 threads)
         if (dalloc(&ch->smagc, (size_t)g.n2 + 1) || dalloc(&ch->d23, (size_t)g.n2 + 1) ||

@@ -169,6 +169,11 @@ struct c3d_channel {
     // SGSSD: per-plane partial sums of k_sgs_sd_sums (N2M x sdnt x 10) and BETA(0:N2)
     double *sdpart = nullptr, *sdbeta = nullptr;
     int sdnt = 0;
+    // SGSSD's per-plane root solve and nu run beside BCOND and the RHS passes, which do
+    // not read nu: forked after the sums, joined before the SGS fluxes
+    cudaStream_t sside = nullptr;
+    cudaEvent_t sfork = nullptr, sjoin = nullptr;
+    int sjoin_pending = 0;
     // the wall model runs on its own stream beside the SGS model and the RHS passes: forked
     // after the last reader of WSM, joined before the first reader of TAUW/TAUB
     cudaStream_t wside = nullptr;

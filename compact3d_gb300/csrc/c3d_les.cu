@@ -336,75 +336,91 @@ __device__ __forceinline__ void sd_level(const R *f, R d23, double *acc) {
     acc[4] += (double)dot6(sr1, cf);
 }
 
-// grid (tiles, N2M), 256 threads; part[((j - 1) tiles + tile) SD_NS + q]
+// One block per tile of SD_TX x SD_TZ points of a plane (grid: x tiles, z tiles, N2M),
+// one thread per point.  Field by field, the tile and a halo of two is staged in shared
+// memory, filtered along x by both stencils, then along z at each point; both levels'
+// sums go to part[((j - 1) tiles + tile) SD_NS + q].
+constexpr int SD_TX = 32, SD_TZ = 16, SD_THREADS = SD_TX * SD_TZ;
 template <typename R>
-__global__ void __launch_bounds__(256) k_sgs_sd_sums(StepArgs<R> a, LesArgs<R> l, double *part) {
+__global__ void __launch_bounds__(SD_THREADS) k_sgs_sd_sums(StepArgs<R> a, LesArgs<R> l, double *part) {
     const Geo g = a.g;
-    const int j = 1 + blockIdx.y, nt = gridDim.x, n1 = g.n1m, n3 = g.n3m;
+    const int n1 = g.n1m, n3 = g.n3m;
+    const int j = 1 + blockIdx.z, i0 = blockIdx.x * SD_TX, k0 = blockIdx.y * SD_TZ;
+    const int tx = threadIdx.x % SD_TX, tz = threadIdx.x / SD_TX;
     const long long fs = (long long)g.n2m * g.np, pb = (long long)(j - 1) * g.np;
-    const R d23 = l.d23r[j];
-    const R four = (R)4.0, two = (R)2.0, six = (R)6.0, twelve = (R)12.0;
+    // the stencils' divisions by 6 and 12 as products with the rounded reciprocals (a
+    // rounding of the last bit; the sums are FP64 and reordered anyway)
+    const R four = (R)4.0, two = (R)2.0, r6 = (R)(1.0 / 6.0), r12 = (R)(1.0 / 12.0);
+    __shared__ R raw[SD_TZ + 4][SD_TX + 4];
+    __shared__ R f3x[SD_TZ + 2][SD_TX], f4x[SD_TZ + 4][SD_TX];
+    R f3[21], f4[21];
+#pragma unroll 1
+    for (int c = 0; c < 21; ++c) {
+        const R *f = l.dyn + c * fs + pb;
+        for (int q = threadIdx.x; q < (SD_TZ + 4) * (SD_TX + 4); q += SD_THREADS) {
+            const int rz = q / (SD_TX + 4), rx = q - rz * (SD_TX + 4);
+            int ii = i0 + rx - 2, kk = k0 + rz - 2;
+            ii = ii < 0 ? ii + n1 : (ii >= n1 ? ii - n1 : ii);
+            kk = kk < 0 ? kk + n3 : (kk >= n3 ? kk - n3 : kk);
+            ii = ii < 0 ? ii + n1 : (ii >= n1 ? ii - n1 : ii);   // tiles wider than N1M
+            raw[rz][rx] = f[(long long)kk * n1 + ii];
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < (SD_TZ + 4) * SD_TX; q += SD_THREADS) {
+            const int rz = q / SD_TX, x = q - rz * SD_TX;
+            const R *r = &raw[rz][x];
+            f4x[rz][x] = (r[0] + four * r[1] + two * r[2] + four * r[3] + r[4]) * r12;
+            if (rz >= 1 && rz <= SD_TZ + 2) f3x[rz - 1][x] = (r[1] + four * r[2] + r[3]) * r6;
+        }
+        __syncthreads();
+        f3[c] = (f3x[tz][tx] + four * f3x[tz + 1][tx] + f3x[tz + 2][tx]) * r6;
+        f4[c] = (f4x[tz][tx] + four * f4x[tz + 1][tx] + two * f4x[tz + 2][tx] + four * f4x[tz + 3][tx] + f4x[tz + 4][tx]) *
+                r12;
+    }
     double acc[SD_NS];
 #pragma unroll
     for (int q = 0; q < SD_NS; ++q) acc[q] = 0.0;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < g.np; e += nt * blockDim.x) {
-        const int i = e % n1, k = e / n1;
-        int ix[5], kr[5];
-#pragma unroll
-        for (int d = 0; d < 5; ++d) {
-            int ii = i + d - 2, kk = k + d - 2;
-            ii = ii < 0 ? ii + n1 : (ii >= n1 ? ii - n1 : ii);
-            kk = kk < 0 ? kk + n3 : (kk >= n3 ? kk - n3 : kk);
-            ix[d] = ii;
-            kr[d] = kk * n1;
-        }
-        R f3[21], f4[21];
-#pragma unroll
-        for (int c = 0; c < 21; ++c) {
-            const R *f = l.dyn + c * fs + pb;
-            R t3[3], t4[5];
-#pragma unroll
-            for (int r = 0; r < 5; ++r) {
-                const R *row = f + kr[r];
-                const R v0 = row[ix[0]], v1 = row[ix[1]], v2 = row[ix[2]], v3 = row[ix[3]], v4 = row[ix[4]];
-                t4[r] = (v0 + four * v1 + two * v2 + four * v3 + v4) / twelve;
-                if (r >= 1 && r <= 3) t3[r - 1] = (v1 + four * v2 + v3) / six;
-            }
-            f3[c] = (t3[0] + four * t3[1] + t3[2]) / six;
-            f4[c] = (t4[0] + four * t4[1] + two * t4[2] + four * t4[3] + t4[4]) / twelve;
-        }
+    if (i0 + tx < n1) {
+        const R d23 = l.d23r[j];
         sd_level(f3, d23, acc);
         sd_level(f4, d23, acc + 5);
     }
-    __shared__ double red[SD_NS][256];
+    // fixed-order reduction: lanes by shuffle, then the block's warps in order
+    __shared__ double red[SD_THREADS / 32][SD_NS];
 #pragma unroll
-    for (int q = 0; q < SD_NS; ++q) red[q][threadIdx.x] = acc[q];
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s)
-#pragma unroll
-            for (int q = 0; q < SD_NS; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + s];
-        __syncthreads();
+    for (int q = 0; q < SD_NS; ++q) {
+        double v = acc[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][q] = v;
     }
-    if (threadIdx.x < SD_NS) part[((long long)(j - 1) * nt + blockIdx.x) * SD_NS + threadIdx.x] = red[threadIdx.x][0];
+    __syncthreads();
+    if (threadIdx.x < SD_NS) {
+        double v = 0.0;
+        for (int w = 0; w < SD_THREADS / 32; ++w) v += red[w][threadIdx.x];
+        const int nt = gridDim.x * gridDim.y, tile = blockIdx.y * gridDim.x + blockIdx.x;
+        part[((long long)(j - 1) * nt + tile) * SD_NS + threadIdx.x] = v;
+    }
 }
 
-// CHHQR (compact3d.f:11571-11676) for the 5x5 companion matrix, every operation rounded as
-// written: eigenvalues of an upper Hessenberg matrix by the Francis double-shift QR with
-// the deflation test |A(L,L-1)| <= EPS (|A(L-1,L-1)| + |A(L,L)|), at most 60 sweeps per
-// deflation (after which the roots not found stay 0).  A is column-major, 1-based.
+// CHHQR (compact3d.f:11571-11676) for the 5x5 companion matrix by one warp, every
+// operation rounded as written: eigenvalues of an upper Hessenberg matrix by the Francis
+// double-shift QR with the deflation test |A(L,L-1)| <= EPS (|A(L-1,L-1)| + |A(L,L)|), at
+// most 60 sweeps per deflation (after which the roots not found stay 0).  A (column-major,
+// 1-based) and WR are in shared memory; every lane forms the reflection's scalars, lane t
+// updates column K + t (rows K..K+2) and then row L + t (columns K..K+2).
 #define SD_M(x, y) __dmul_rn(x, y)
 #define SD_A(x, y) __dadd_rn(x, y)
 #define SD_S(x, y) __dsub_rn(x, y)
-__device__ void sd_chhqr5(double *A, double *WR, double EPS) {
+__device__ void sd_chhqr5_warp(double *A, double *WR, double EPS) {
     constexpr int N = 5;
+    const int lane = threadIdx.x & 31;
     auto a = [&](int i, int j) -> double & { return A[(i - 1) + N * (j - 1)]; };
     int M = N, IT = 0;
     for (int guard = 0; M > 0 && guard < 1000; ++guard) {
         int L = M;
         while (L > 1 && fabs(a(L, L - 1)) > SD_M(EPS, SD_A(fabs(a(L - 1, L - 1)), fabs(a(L, L))))) L = L - 1;
         if (L == M) {
-            WR[M - 1] = a(M, M);
+            if (lane == 0) WR[M - 1] = a(M, M);
             M = M - 1;
             IT = 0;
             continue;
@@ -414,13 +430,15 @@ __device__ void sd_chhqr5(double *A, double *WR, double EPS) {
             const double C = SD_S(SD_M(a(M, M), a(M - 1, M - 1)), SD_M(a(M, M - 1), a(M - 1, M)));
             const double W = SD_S(SD_M(B, B), SD_M(4.0, C));
             const double Y = sqrt(fabs(W));
-            if (W > 0.0) {
-                const double XY = B < 0.0 ? -1.0 : 1.0;
-                WR[M - 1] = SD_S(-B, SD_M(XY, Y)) / 2.0;
-                WR[M - 2] = C / WR[M - 1];
-            } else {
-                WR[M - 1] = -B / 2.0;
-                WR[M - 2] = WR[M - 1];
+            if (lane == 0) {
+                if (W > 0.0) {
+                    const double XY = B < 0.0 ? -1.0 : 1.0;
+                    WR[M - 1] = SD_S(-B, SD_M(XY, Y)) / 2.0;
+                    WR[M - 2] = C / WR[M - 1];
+                } else {
+                    WR[M - 1] = -B / 2.0;
+                    WR[M - 2] = WR[M - 1];
+                }
             }
             M = M - 2;
             IT = 0;
@@ -428,8 +446,12 @@ __device__ void sd_chhqr5(double *A, double *WR, double EPS) {
         }
         if (IT >= 60) return;
         IT = IT + 1;
-        for (int J = L + 2; J <= M; J++) a(J, J - 2) = 0.0;
-        for (int J = L + 3; J <= M; J++) a(J, J - 3) = 0.0;
+        __syncwarp();
+        if (lane == 0) {
+            for (int J = L + 2; J <= M; J++) a(J, J - 2) = 0.0;
+            for (int J = L + 3; J <= M; J++) a(J, J - 3) = 0.0;
+        }
+        __syncwarp();
         for (int K = L; K <= M - 1; K++) {
             double P, Q, R;
             if (K != L) {
@@ -446,13 +468,15 @@ __device__ void sd_chhqr5(double *A, double *WR, double EPS) {
             if (SD_A(SD_A(fabs(P), fabs(Q)), fabs(R)) == 0.0) continue;
             const double XY = P < 0.0 ? -1.0 : 1.0;
             const double S = SD_M(XY, sqrt(SD_A(SD_A(SD_M(P, P), SD_M(Q, Q)), SD_M(R, R))));
-            if (K != L) a(K, K - 1) = -S;
             const double E = -Q / S, F = -R / S, X = -P / S;
             const double PS = SD_A(P, S);
             const double Y = SD_S(-X, SD_M(F, R) / PS);
             const double G = SD_M(E, R) / PS;
             const double Z = SD_S(-X, SD_M(E, Q) / PS);
-            for (int J = K; J <= M; J++) {
+            __syncwarp();
+            if (K != L && lane == 0) a(K, K - 1) = -S;
+            const int J = K + lane;
+            if (J <= M) {
                 double p = SD_A(SD_M(X, a(K, J)), SD_M(E, a(K + 1, J)));
                 double q = SD_A(SD_M(E, a(K, J)), SD_M(Y, a(K + 1, J)));
                 double r = SD_A(SD_M(F, a(K, J)), SD_M(G, a(K + 1, J)));
@@ -465,8 +489,10 @@ __device__ void sd_chhqr5(double *A, double *WR, double EPS) {
                 a(K + 1, J) = q;
                 a(K, J) = p;
             }
+            __syncwarp();
             const int JJ = K + 3 >= M ? M : K + 3;
-            for (int I = L; I <= JJ; I++) {
+            const int I = L + lane;
+            if (I <= JJ) {
                 double p = SD_A(SD_M(X, a(I, K)), SD_M(E, a(I, K + 1)));
                 double q = SD_A(SD_M(E, a(I, K)), SD_M(Y, a(I, K + 1)));
                 double r = SD_A(SD_M(F, a(I, K)), SD_M(G, a(I, K + 1)));
@@ -479,52 +505,56 @@ __device__ void sd_chhqr5(double *A, double *WR, double EPS) {
                 a(I, K + 1) = q;
                 a(I, K) = p;
             }
+            __syncwarp();
         }
     }
 }
 
 // per plane: the sums, COEFFICIENT (compact3d.f:2079-2095), DQRRT's BETA (11548-11569,
-// EPS 1.0E-5) and SMAGC; one thread per plane
+// EPS 1.0E-5) and SMAGC; one warp per plane
 template <typename R>
-__global__ void k_sgs_sd_coef(StepArgs<R> a, LesArgs<R> l, const double *part, int nt, double *beta) {
+__global__ void __launch_bounds__(32) k_sgs_sd_coef(StepArgs<R> a, LesArgs<R> l, const double *part, int nt,
+                                                    double *beta) {
     const Geo g = a.g;
-    const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (j > g.n2m) return;
-    double s[SD_NS];
-#pragma unroll
-    for (int q = 0; q < SD_NS; ++q) s[q] = 0.0;
-    for (int t = 0; t < nt; ++t)
-#pragma unroll
-        for (int q = 0; q < SD_NS; ++q) s[q] += part[((long long)(j - 1) * nt + t) * SD_NS + q];
+    const int j = 1 + blockIdx.x, lane = threadIdx.x;
+    __shared__ double Am[25], WR[5], s[SD_NS];
+    if (lane < SD_NS) {
+        double v = 0.0;
+        for (int t = 0; t < nt; ++t) v += part[((long long)(j - 1) * nt + t) * SD_NS + lane];
+        s[lane] = v;
+    }
+    if (lane < 5) WR[lane] = 0.0;
+    __syncwarp();
     const double NXZ = 1.0 / (double)(g.n1m * g.n3m);
     const double A1 = -8.0 * s[0] * NXZ, B1 = -2.0 * s[1] * NXZ, C1 = 4.0 * s[2] * NXZ, D1 = 64.0 * s[3] * NXZ,
                  E1 = 32.0 * s[4] * NXZ;
     const double A2 = -32.0 * s[5] * NXZ, B2 = -2.0 * s[6] * NXZ, C2 = 4.0 * s[7] * NXZ, D2 = 1024.0 * s[8] * NXZ,
                  E2 = 128.0 * s[9] * NXZ;
-    double PA[5];
     const double AD = SD_M(A1, D2);
+    double PA[5];
     PA[4] = SD_S(SD_M(B2, C1), SD_M(B1, C2)) / AD;
     PA[3] = SD_S(SD_M(A1, C2), SD_M(B2, E1)) / AD;
     PA[2] = SD_S(SD_A(SD_M(B2, D1), SD_M(B1, E2)), SD_M(A2, C1)) / AD;
     PA[1] = SD_S(SD_M(A2, E1), SD_M(A1, E2)) / AD;
     PA[0] = -SD_A(SD_M(A2, D1), SD_M(B1, D2)) / AD;
-    double Amat[25], WR[5];
-#pragma unroll
-    for (int q = 0; q < 25; ++q) Amat[q] = 0.0;
-#pragma unroll
-    for (int q = 0; q < 5; ++q) WR[q] = 0.0;
-    for (int J = 1; J <= 5; J++) Amat[5 * (J - 1)] = -PA[J - 1];
-    for (int I = 1; I <= 4; I++) Amat[I + 5 * (I - 1)] = 1.0;
-    sd_chhqr5(Amat, WR, 1.0E-5);
+    if (lane < 25) {   // the companion matrix: first row -PA, ones below the diagonal
+        const int i = lane % 5, c = lane / 5;
+        Am[lane] = i == 0 ? -PA[c] : (i == c + 1 ? 1.0 : 0.0);
+    }
+    __syncwarp();
+    sd_chhqr5_warp(Am, WR, 1.0E-5);
+    __syncwarp();
     double BETA = 0.;
     for (int J = 0; J < 5; J++)
         if (WR[J] > BETA && WR[J] < 2.0) BETA = WR[J];
-    beta[j] = BETA;
-    const double num = SD_S(SD_M(SD_M(4.0, BETA), s[0]), s[1]);
-    const double den = SD_A(SD_S(SD_M(SD_M(SD_M(16.0, BETA), BETA), s[3]), SD_M(SD_M(8.0, BETA), s[4])), s[2]);
-    const double sm = -0.5 * (num * NXZ) / (den * NXZ);
-    l.smagc[j] = sm;
-    l.coef[j] = (R)(sm * l.d23[j]);
+    if (lane == 0) {
+        beta[j] = BETA;
+        const double num = SD_S(SD_M(SD_M(4.0, BETA), s[0]), s[1]);
+        const double den = SD_A(SD_S(SD_M(SD_M(SD_M(16.0, BETA), BETA), s[3]), SD_M(SD_M(8.0, BETA), s[4])), s[2]);
+        const double sm = -0.5 * (num * NXZ) / (den * NXZ);
+        l.smagc[j] = sm;
+        l.coef[j] = (R)(sm * l.d23[j]);
+    }
 }
 #undef SD_M
 #undef SD_A
@@ -1379,6 +1409,10 @@ int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *n
             CK_RC(cudaStreamWaitEvent(st, ch->wjoin, 0));
             ch->wjoin_pending = 0;
         }
+        if (ch->sjoin_pending) {
+            CK_RC(cudaStreamWaitEvent(st, ch->sjoin, 0));
+            ch->sjoin_pending = 0;
+        }
         if (ch->files != 0 && ch->wmodel == 0) {
             k_les_wallss<R><<<1, 256, 0, st>>>(a);
             mark(ch, nl, "les_wallss", 64.0 * g.np);
@@ -1441,15 +1475,29 @@ int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *n
             if ((rc = wall_model())) return rc;
             k_sgs_raw<R><<<nblk((long long)g.n2m * g.np), TPB, 0, st>>>(a, l);
             mark(ch, nl, "sgs_raw", N * (6 * 8 + 22 * Rb));
-            k_sgs_sd_sums<R><<<dim3(ch->sdnt, g.n2m), 256, 0, st>>>(a, l, ch->sdpart);
+            k_sgs_sd_sums<R><<<dim3((g.n1m + SD_TX - 1) / SD_TX, g.n3m / SD_TZ, g.n2m), SD_THREADS, 0, st>>>(a, l, ch->sdpart);
             mark(ch, nl, "sgs_sd_sums", N * 21 * Rb);
-            k_sgs_sd_coef<R><<<(g.n2m + 31) / 32, 32, 0, st>>>(a, l, ch->sdpart, ch->sdnt, ch->sdbeta);
-            k_sgs_apply<R><<<nblk((long long)g.n2m * g.np), TPB, 0, st>>>(a, l);
+            const bool sfork = ch->sside && !ch->prof_on;
+            const cudaStream_t sst = sfork ? ch->sside : st;
+            if (sfork) {
+                CK_RC(cudaEventRecord(ch->sfork, st));
+                CK_RC(cudaStreamWaitEvent(sst, ch->sfork, 0));
+            }
+            k_sgs_sd_coef<R><<<g.n2m, 32, 0, sst>>>(a, l, ch->sdpart, ch->sdnt, ch->sdbeta);
+            k_sgs_apply<R><<<nblk((long long)g.n2m * g.np), TPB, 0, sst>>>(a, l);
+            if (sfork) {
+                CK_RC(cudaEventRecord(ch->sjoin, sst));
+                ch->sjoin_pending = 1;
+            }
             *nl += 1;
             mark(ch, nl, "sgs_sd_apply", N * 2 * Rb);
         }
         if (fork) ch->wjoin_pending = 1;
         return 0;
+    }
+    if (ch->sjoin_pending) {   // nu of this step's SGSSD
+        CK_RC(cudaStreamWaitEvent(st, ch->sjoin, 0));
+        ch->sjoin_pending = 0;
     }
     switch ((g.n1m + 31) / 32) {
         case 1: launch_les_x<R, 1>(ch, a, l, 0, nl); break;
