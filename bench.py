@@ -502,6 +502,14 @@ def run_next(args, D: Dist, g, dt, U0, P0, HH0):
     alg = 7 * 8.0 * g.points
     out["plane_stats"] = dict(ms_per_call=ms, alg_bytes=alg, gbs=alg / ms / 1e6, values_per_plane=29,
                               note="FP64 arithmetic on the double-float state; host-timed call incl. copy-out")
+    ch.plane_spectra()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        ch.plane_spectra()
+    ms_sp = (time.perf_counter() - t0) / 2 * 1e3
+    out["plane_spectra"] = dict(ms_per_call=ms_sp, tables="XSPCTR, ZSPCTR, RXX, RZZ, RXY (3 components)",
+                                note="FP64 FFTs of every x and z line of the three components, the plane statistics "
+                                     "for VM/VRMS, host-timed call incl. copy-out")
     d = tempfile.mkdtemp(prefix="c3d_ckpt_")
     try:
         path = os.path.join(d, "ckpt.bin")

@@ -198,6 +198,7 @@ void free_channel(c3d_channel *ch) {
     if (ch->xfer) cudaFree(ch->xfer);
     if (ch->wtaue) cudaFree(ch->wtaue);
     if (ch->wshift) cudaFree(ch->wshift);
+    if (ch->specbuf) cudaFree(ch->specbuf);
     if (ch->sdpart) cudaFree(ch->sdpart);
     if (ch->sfork) cudaEventDestroy(ch->sfork);
     if (ch->sjoin) cudaEventDestroy(ch->sjoin);
@@ -1206,6 +1207,61 @@ int c3d_plane_stats(c3d_channel *ch, double *out) {
     int rc = launch_stats(ch, ch->stats, ch->stats + nout);
     if (rc) return rc;
     CK(cudaMemcpyAsync(out, ch->stats, nout * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    return 0;
+}
+
+int c3d_plane_spectra(c3d_channel *ch, const double *vmo, double *xspec, double *zspec, double *rxx, double *rzz,
+                      double *rxy) {
+    if (!ch) { set_error("null argument"); return C3D_EINVAL; }
+    if (!ch->have_state) { set_error("c3d_upload must be called before c3d_plane_spectra"); return C3D_ESTATE; }
+    cudaSetDevice(ch->device);
+    const Geo &g = ch->g;
+    const size_t ns = stats_scratch_doubles(g), nout = (size_t)g.n2m * 29;
+    const size_t nx = 3 * (size_t)g.n2m * g.n1m, nz = 3 * (size_t)g.n2m * g.n3m, nm = 3 * (size_t)g.n2m;
+    if (!ch->stats && dalloc(&ch->stats, ns)) return C3D_ENOMEM;
+    if (!ch->specbuf && dalloc(&ch->specbuf, nm + 3 * nx + 2 * nz)) return C3D_ENOMEM;
+    double *dvmo = ch->specbuf, *dxs = dvmo + nm, *dzs = dxs + nx, *drxx = dzs + nz, *drzz = drxx + nx,
+           *drxy = drzz + nz;
+    int rc = launch_stats(ch, ch->stats, ch->stats + nout);
+    if (rc) return rc;
+    if (vmo) {
+        CK(cudaMemcpyAsync(dvmo, vmo, nm * sizeof(double), cudaMemcpyHostToDevice, ch->stream));
+    } else {   // the instantaneous plane means VM(J, L), columns 0..2 of the statistics table
+        for (int L = 0; L < 3; ++L)
+            CK(cudaMemcpy2DAsync(dvmo + (size_t)L * g.n2m, sizeof(double), ch->stats + L, 29 * sizeof(double),
+                                 sizeof(double), g.n2m, cudaMemcpyDeviceToDevice, ch->stream));
+    }
+    rc = launch_spectra(ch, dvmo, ch->stats, xspec ? dxs : nullptr, zspec ? dzs : nullptr, rxx ? drxx : nullptr,
+                        rzz ? drzz : nullptr, rxy ? drxy : nullptr);
+    if (rc) { set_error("spectra kernels"); return rc; }
+    if (xspec) CK(cudaMemcpyAsync(xspec, dxs, nx * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
+    if (zspec) CK(cudaMemcpyAsync(zspec, dzs, nz * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
+    if (rxx) CK(cudaMemcpyAsync(rxx, drxx, nx * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
+    if (rzz) CK(cudaMemcpyAsync(rzz, drzz, nz * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
+    if (rxy) CK(cudaMemcpyAsync(rxy, drxy, nx * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
+    CK(cudaStreamSynchronize(ch->stream));
+    return 0;
+}
+
+int c3d_plane_quadrants(c3d_channel *ch, const double *vmp, double *out) {
+    if (!ch || !out) { set_error("null argument"); return C3D_EINVAL; }
+    if (!ch->have_state) { set_error("c3d_upload must be called before c3d_plane_quadrants"); return C3D_ESTATE; }
+    cudaSetDevice(ch->device);
+    const Geo &g = ch->g;
+    // the statistics scratch holds the output (8 N2M) and the partial sums (8 SB N2M)
+    if (!ch->stats && dalloc(&ch->stats, stats_scratch_doubles(g))) return C3D_ENOMEM;
+    if (!ch->specbuf && dalloc(&ch->specbuf, 3 * (size_t)g.n2m * (1 + 3 * (size_t)g.n1m + 2 * (size_t)g.n3m)))
+        return C3D_ENOMEM;
+    double *dvmp = nullptr;
+    if (vmp) {
+        dvmp = ch->specbuf;
+        CK(cudaMemcpyAsync(dvmp, vmp, 2 * (size_t)g.n2m * sizeof(double), cudaMemcpyHostToDevice, ch->stream));
+    }
+    double *dout = ch->stats, *part = ch->stats + 8 * (size_t)g.n2m;
+    int rc = launch_quadrants(ch, dvmp, dout, part);
+    if (rc) { set_error("quadrant kernels"); return rc; }
+    CK(cudaMemcpyAsync(out, dout, 8 * (size_t)g.n2m * sizeof(double), cudaMemcpyDeviceToHost, ch->stream));
     CK(cudaStreamSynchronize(ch->stream));
     return 0;
 }

@@ -167,6 +167,7 @@ struct c3d_channel {
     // reference plane ZS of MARUSIC1 (the Y(J) nearest 0.06) and tan(16 deg)
     double *wshift = nullptr;
     // SGSSD: per-plane partial sums of k_sgs_sd_sums (N2M x sdnt x 10) and BETA(0:N2)
+    double *specbuf = nullptr;   // c3d_plane_spectra: means and the five output tables
     double *sdpart = nullptr, *sdbeta = nullptr;
     int sdnt = 0;
     // SGSSD's per-plane root solve and nu run beside BCOND and the RHS passes, which do
@@ -286,6 +287,11 @@ void mark(c3d_channel *ch, int *nl, const char *name, double bytes);
     } while (0)
 // the shifted-point wall models' scratch: its size in doubles and the mesh tables
 size_t wall_shift_doubles(const Geo &g);
+// ENERGY's spectra and correlations (vmo: 3 N2M means; st: the plane statistics table)
+int launch_spectra(c3d_channel *ch, const double *vmo, const double *st, double *xs, double *zs, double *rxx,
+                   double *rzz, double *rxy);
+// ENERGY's quadrant sums into out (8 N2M), part: 8 SB N2M partial sums
+int launch_quadrants(c3d_channel *ch, const double *vmp, double *out, double *part);
 void launch_wall_shift_init(c3d_channel *ch);
 void prof_begin(c3d_channel *ch);
 int prof_collect(c3d_channel *ch);

@@ -173,6 +173,200 @@ int launch_stats_t(c3d_channel *ch, StepArgs<R> &a, double *out, double *part) {
 template int launch_stats_t<double>(c3d_channel *, StepArgs<double> &, double *, double *);
 template int launch_stats_t<float>(c3d_channel *, StepArgs<float> &, double *, double *);
 
+// ---------------------------------------------------------------------------------
+// ENERGY's 1-D spectra and two-point correlations (compact3d.f:10243-10515), FP64.
+// Spectra: one block of SPW warps per (plane, component); warp w transforms the lines
+// w, w + SPW, ... with the channel's Stockham plans and double twiddles: an x line of
+// N1M reals as N1M/2 complex pairs, then the real-input split, giving |X_k|^2 for
+// k <= N1M/2 (the rest mirrored); a z line as N3M complex values with zero imaginary
+// part.  The warps' sums are added in a fixed order.  Correlations: one block per
+// (plane, component); RXX and RXY with a thread per x point summing over K in order,
+// RZZ with a warp per z point.
+// ---------------------------------------------------------------------------------
+constexpr int SPW = 4;
+
+// cell-centre velocity of component L (0..2) at (i, j, k), v between j and jv
+template <typename R>
+__device__ __forceinline__ double vcell(const StepArgs<R> &a, int L, int i, int j, int k, int jv) {
+    const Geo &g = a.g;
+    if (L == 0) return (sv<R>(a.u, g, i, j, k) + sv<R>(a.u, g, i + 1 == g.n1m ? 0 : i + 1, j, k)) * 0.5;
+    if (L == 1) return (sv<R>(a.v, g, i, j, k) + sv<R>(a.v, g, i, jv, k)) * 0.5;
+    return (sv<R>(a.w, g, i, j, k) + sv<R>(a.w, g, i, j, k + 1 == g.n3m ? 0 : k + 1)) * 0.5;
+}
+
+// x spectra: dynamic shared memory SPW x (2 (N1M/2) double2 + (N1M/2 + 1) doubles)
+template <typename R>
+__global__ void __launch_bounds__(32 * SPW) k_spec_x(StepArgs<R> a, const double *vmo, const double2 *twp,
+                                                     double *xs) {
+    const Geo g = a.g;
+    const int j = 1 + blockIdx.x, L = blockIdx.y, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int N = g.n1m, M = N / 2;
+    extern __shared__ double2 smx[];
+    double2 *bufa = smx + (size_t)w * (2 * M), *bufb = bufa + M;
+    double *acc = reinterpret_cast<double *>(smx + (size_t)SPW * 2 * M) + (size_t)w * (M + 1);
+    const double FS = 3.141592653589793 * g.dx1, mean = vmo[L * g.n2m + (j - 1)];
+    for (int q = lane; q <= M; q += 32) acc[q] = 0.0;
+    for (int k = w; k < g.n3m; k += SPW) {
+        for (int q = lane; q < M; q += 32)
+            bufa[q] = make_double2(vcell(a, L, 2 * q, j, k, j + 1) - mean, vcell(a, L, 2 * q + 1, j, k, j + 1) - mean);
+        __syncwarp();
+        double2 *Z = fft_smem<double2, false>(bufa, bufb, a.fx, 0, 1, 0, -1, lane, 32);
+        for (int q = lane; q <= M; q += 32) {
+            const double2 zk = Z[q == M ? 0 : q], zc = Z[q == 0 ? 0 : M - q];
+            const double2 zm = make_double2(zc.x, -zc.y);
+            const double Ex = 0.5 * (zk.x + zm.x), Ey = 0.5 * (zk.y + zm.y);
+            const double Ox = 0.5 * (zk.y - zm.y), Oy = -0.5 * (zk.x - zm.x);
+            const double2 t = twp[q];   // exp(-2 pi i q / N1M)
+            const double Xx = Ex + (t.x * Ox - t.y * Oy), Xy = Ey + (t.x * Oy + t.y * Ox);
+            acc[q] += (Xx * Xx + Xy * Xy) / N / FS;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    double *out = xs + (size_t)N * ((j - 1) + (size_t)g.n2m * L);
+    for (int q = threadIdx.x; q < N; q += blockDim.x) {
+        const int kk = q <= M ? q : N - q;
+        double s = 0.0;
+        for (int ww = 0; ww < SPW; ++ww)
+            s += reinterpret_cast<double *>(smx + (size_t)SPW * 2 * M)[(size_t)ww * (M + 1) + kk];
+        out[q] = s / (double)g.n3m;
+    }
+}
+
+// z spectra: dynamic shared memory SPW x (2 N3M double2 + N3M doubles)
+template <typename R>
+__global__ void __launch_bounds__(32 * SPW) k_spec_z(StepArgs<R> a, const double *vmo, double *zs) {
+    const Geo g = a.g;
+    const int j = 1 + blockIdx.x, L = blockIdx.y, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int N = g.n3m;
+    extern __shared__ double2 smz[];
+    double2 *bufa = smz + (size_t)w * (2 * N), *bufb = bufa + N;
+    double *accs = reinterpret_cast<double *>(smz + (size_t)SPW * 2 * N), *acc = accs + (size_t)w * N;
+    const double FS = 3.141592653589793 * g.dx3, mean = vmo[L * g.n2m + (j - 1)];
+    for (int q = lane; q < N; q += 32) acc[q] = 0.0;
+    for (int i = w; i < g.n1m; i += SPW) {
+        for (int q = lane; q < N; q += 32) bufa[q] = make_double2(vcell(a, L, i, j, q, j + 1) - mean, 0.0);
+        __syncwarp();
+        const double2 *Z = fft_smem<double2, false>(bufa, bufb, a.fz, 0, 1, 0, -1, lane, 32);
+        for (int q = lane; q < N; q += 32) acc[q] += (Z[q].x * Z[q].x + Z[q].y * Z[q].y) / N / FS;
+        __syncwarp();
+    }
+    __syncthreads();
+    double *out = zs + (size_t)N * ((j - 1) + (size_t)g.n2m * L);
+    for (int q = threadIdx.x; q < N; q += blockDim.x) {
+        double s = 0.0;
+        for (int ww = 0; ww < SPW; ++ww) s += accs[(size_t)ww * N + q];
+        out[q] = s / (double)g.n1m;
+    }
+}
+
+// correlations; st = the plane statistics table (VM in columns 0..2, VRMS in 7..9)
+template <typename R>
+__global__ void __launch_bounds__(256) k_corr(StepArgs<R> a, const double *st, double *rxx, double *rzz,
+                                             double *rxy) {
+    const Geo g = a.g;
+    const int j = 1 + blockIdx.x, L = blockIdx.y;
+    const int n1h = g.n1m / 2, n3h = g.n3m / 2;   // N1H - 1, N3H - 1 (0-based)
+    const double vm = st[(size_t)(j - 1) * 29 + L], var = st[(size_t)(j - 1) * 29 + 7 + L] - vm * vm;
+    const double vm1 = st[L], var1 = st[7 + L] - vm1 * vm1;
+    const int jv = j == g.n2m ? g.n2m : j + 1, jv1 = g.n2m == 1 ? 1 : 2;   // JPA(J), JPA(1)
+    auto vp = [&](int i, int k) { return vcell(a, L, i, j, k, jv) - vm; };
+    const size_t o = (size_t)g.n2m * L + (j - 1);
+    for (int i = threadIdx.x; i < g.n1m; i += blockDim.x) {
+        double rx = 0.0, ry = 0.0;
+        for (int k = 0; k < g.n3m; ++k) {
+            const double p = vp(i, k);
+            rx = rx + vp(n1h, k) * p;
+            ry = ry + (vcell(a, L, n1h, 1, k, jv1) - vm1) * p;
+        }
+        if (rxx) rxx[o * g.n1m + i] = rx / (double)g.n3m / var;
+        if (rxy) rxy[o * g.n1m + i] = ry / (double)g.n3m / sqrt(var) / sqrt(var1);
+    }
+    if (!rzz) return;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = w; k < g.n3m; k += blockDim.x / 32) {
+        double r = 0.0;
+        for (int i = lane; i < g.n1m; i += 32) r += vp(i, n3h) * vp(i, k);
+        for (int s = 16; s > 0; s >>= 1) r += __shfl_down_sync(0xffffffffu, r, s);
+        if (lane == 0) rzz[o * g.n3m + k] = r / (double)g.n1m / var;
+    }
+}
+
+// ENERGY's quadrant analysis (compact3d.f:10560-10604): per plane the sums of
+// u'v' = (u - VMP)(v - VMP) over the points of each sign quadrant of (u', v') and the
+// points' counts; cell-centre u and v (V between J and J+1); vmp = VMP(J,1..2) (the
+// reference's VMP is a local never assigned: zero-valued in practice).
+template <typename R>
+__global__ void __launch_bounds__(STB) k_quad(StepArgs<R> a, const double *vmp, double *part) {
+    __shared__ double sh[8 * STB];
+    const Geo &g = a.g;
+    const int j = 1 + blockIdx.y;
+    const int chunk = (g.np + SB - 1) / SB, e0 = blockIdx.x * chunk, e1 = min(g.np, e0 + chunk);
+    const double m1 = vmp ? vmp[j - 1] : 0.0, m2 = vmp ? vmp[g.n2m + j - 1] : 0.0;
+    double acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    for (int e = e0 + threadIdx.x; e < e1; e += STB) {
+        const int i = e % g.n1m, k = e / g.n1m;
+        const double V1P = vcell(a, 0, i, j, k, j + 1) - m1, V2P = vcell(a, 1, i, j, k, j + 1) - m2;
+        const double uv = V1P * V2P;
+        if (V1P > 0.0 && V2P > 0.0) { acc[0] += uv; acc[4] += 1.0; }
+        if (V1P < 0.0 && V2P > 0.0) { acc[1] += uv; acc[5] += 1.0; }
+        if (V1P < 0.0 && V2P < 0.0) { acc[2] += uv; acc[6] += 1.0; }
+        if (V1P > 0.0 && V2P < 0.0) { acc[3] += uv; acc[7] += 1.0; }
+    }
+    block_sums(acc, 8, sh, part + ((size_t)blockIdx.y * SB + blockIdx.x) * 8);
+}
+
+// Q(J,1..4) = -sum / (N1M N3M), QP(J,1..4) = count / (N1M N3M): out[(J-1) 8 + q]
+__global__ void k_quad_fin(Geo g, const double *part, double *out) {
+    const int j = blockIdx.x, q = threadIdx.x;
+    if (q >= 8) return;
+    double s = 0.0;
+    for (int b = 0; b < SB; ++b) s += part[((size_t)j * SB + b) * 8 + q];
+    const double NXZ = 1.0 / (double)(g.n1m * g.n3m);
+    out[(size_t)j * 8 + q] = q < 4 ? -s * NXZ : s * NXZ;
+}
+
+template <typename R>
+int launch_quadrants_t(c3d_channel *ch, StepArgs<R> &a, const double *vmp, double *out, double *part) {
+    const Geo &g = ch->g;
+    k_quad<R><<<dim3(SB, g.n2m), STB, 0, ch->stream>>>(a, vmp, part);
+    k_quad_fin<<<g.n2m, 32, 0, ch->stream>>>(g, part, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : C3D_ECUDA;
+}
+
+template int launch_quadrants_t<double>(c3d_channel *, StepArgs<double> &, const double *, double *, double *);
+template int launch_quadrants_t<float>(c3d_channel *, StepArgs<float> &, const double *, double *, double *);
+
+template <typename R>
+int launch_spectra_t(c3d_channel *ch, StepArgs<R> &a, const double *vmo, const double *st, double *xs, double *zs,
+                     double *rxx, double *rzz, double *rxy) {
+    const Geo &g = ch->g;
+    const dim3 grid(g.n2m, 3);
+    if (xs) {
+        const int M = g.n1m / 2;
+        const size_t sm = (size_t)SPW * (2 * M * sizeof(double2) + (M + 1) * sizeof(double));
+        if (cudaFuncSetAttribute(k_spec_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+            return C3D_ECUDA;
+        const double2 *twp = ch->tw64 + g.n1m / 2 + g.n3m;   // exp(-2 pi i q / N1M), q = 0..N1M/2
+        k_spec_x<R><<<grid, 32 * SPW, sm, ch->stream>>>(a, vmo, twp, xs);
+    }
+    if (zs) {
+        const size_t sm = (size_t)SPW * (2 * g.n3m * sizeof(double2) + g.n3m * sizeof(double));
+        if (cudaFuncSetAttribute(k_spec_z<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+            return C3D_ECUDA;
+        k_spec_z<R><<<grid, 32 * SPW, sm, ch->stream>>>(a, vmo, zs);
+    }
+    if (rxx || rzz || rxy) k_corr<R><<<grid, 256, 0, ch->stream>>>(a, st, rxx, rzz, rxy);
+    return cudaGetLastError() == cudaSuccess ? 0 : C3D_ECUDA;
+}
+
+template int launch_spectra_t<double>(c3d_channel *, StepArgs<double> &, const double *, const double *, double *,
+                                      double *, double *, double *, double *);
+template int launch_spectra_t<float>(c3d_channel *, StepArgs<float> &, const double *, const double *, double *,
+                                     double *, double *, double *, double *);
+
 // Scratch the statistics need on the device: the output table and the partial sums.
 size_t stats_scratch_doubles(const Geo &g) { return (size_t)g.n2m * 29 + (size_t)g.n2m * SB * NS1; }
 

@@ -473,6 +473,32 @@ int launch_stats(c3d_channel *ch, double *out, double *part) {
 }
 
 template <typename R>
+int launch_spectra_t(c3d_channel *ch, StepArgs<R> &a, const double *vmo, const double *st, double *xs, double *zs,
+                     double *rxx, double *rzz, double *rxy);
+
+template <typename R>
+int launch_quadrants_t(c3d_channel *ch, StepArgs<R> &a, const double *vmp, double *out, double *part);
+
+int launch_quadrants(c3d_channel *ch, const double *vmp, double *out, double *part) {
+    if (ch->precision == C3D_MIXED) {
+        StepArgs<float> a = make_args<float>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
+        return launch_quadrants_t<float>(ch, a, vmp, out, part);
+    }
+    StepArgs<double> a = make_args<double>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
+    return launch_quadrants_t<double>(ch, a, vmp, out, part);
+}
+
+int launch_spectra(c3d_channel *ch, const double *vmo, const double *st, double *xs, double *zs, double *rxx,
+                   double *rzz, double *rxy) {
+    if (ch->precision == C3D_MIXED) {
+        StepArgs<float> a = make_args<float>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
+        return launch_spectra_t<float>(ch, a, vmo, st, xs, zs, rxx, rzz, rxy);
+    }
+    StepArgs<double> a = make_args<double>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
+    return launch_spectra_t<double>(ch, a, vmo, st, xs, zs, rxx, rzz, rxy);
+}
+
+template <typename R>
 static int operator_impl(c3d_channel *ch, int op, int *nl) {
     StepArgs<R> a = make_args<R>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
     return launch_op<R>(ch, a, op, (const R *)ch->opbuf[0], (R *)ch->opbuf[1], nl);

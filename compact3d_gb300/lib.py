@@ -55,6 +55,8 @@ SIGNATURES = {
     "c3d_op_apply": (_ip, [_vp, _ip, _ip]),
     "c3d_op_get": (_ip, [_vp, _dp]),
     "c3d_plane_stats": (_ip, [_vp, _dp]),
+    "c3d_plane_spectra": (_ip, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "c3d_plane_quadrants": (_ip, [_vp, _dp, _dp]),
     "c3d_checkpoint_write": (_ip, [_vp, ctypes.c_char_p, _ip, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     "c3d_checkpoint_read": (_ip, [_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), _dp, _dp, _dp]),
     "c3d_step": (_ip, [_vp, _ip, ctypes.c_double, _dp, _dp]),
@@ -215,6 +217,27 @@ class Channel:
         check(load().c3d_plane_stats(self.h, _p(out)), "c3d_plane_stats")
         return out.reshape(self.grid.n2m, 29)
 
+    def plane_spectra(self, vmo=None):
+        """ENERGY's spectra and two-point correlations: dict of Fortran (N, N2M, 3) arrays
+        xspec, zspec, rxx, rzz, rxy; vmo (N2M, 3) is the mean the spectra subtract (None:
+        the instantaneous plane means)."""
+        g = self.grid
+        out = {k: np.zeros((n, g.n2m, 3), order="F") for k, n in
+               (("xspec", g.n1m), ("zspec", g.n3m), ("rxx", g.n1m), ("rzz", g.n3m), ("rxy", g.n1m))}
+        v = None if vmo is None else np.asfortranarray(vmo, dtype=np.float64)
+        check(load().c3d_plane_spectra(self.h, _p(v), *(_p(out[k].reshape(-1, order="F")) for k in
+                                                        ("xspec", "zspec", "rxx", "rzz", "rxy"))),
+              "c3d_plane_spectra")
+        return out
+
+    def plane_quadrants(self, vmp=None):
+        """ENERGY's quadrant analysis: (N2M, 8) array, Q(J,1..4) then QP(J,1..4); vmp
+        (N2M, 2) or None (the reference's never-assigned VMP, zero)."""
+        out = np.zeros(self.grid.n2m * 8)
+        v = None if vmp is None else np.asfortranarray(vmp, dtype=np.float64)
+        check(load().c3d_plane_quadrants(self.h, _p(v), _p(out)), "c3d_plane_quadrants")
+        return out.reshape(self.grid.n2m, 8)
+
     # ---- checkpoint (CWRITE / READUP in a format that round-trips) ----
     def checkpoint_write(self, path, ntime: int, time: float, presg: float, presg3: float):
         check(load().c3d_checkpoint_write(self.h, str(path).encode(), int(ntime), float(time), float(presg),
@@ -365,6 +388,30 @@ class Batch:
         n = (ctypes.c_int * 1)()
         check(load().c3d_batch_last_step_stats(self.h, ms, n), "c3d_batch_last_step_stats")
         return ms[0], n[0]
+
+
+class TimeAverage:
+    """TAVER (compact3d.f:10755-11060): running means of statistics tables over the samples
+    NAVG = 1, 2, ...: the first sample is copied, later ones enter as
+    XO = (XO (NAVG - 1) + X) / NAVG, in that operation order.  Tables are numpy arrays
+    (plane_stats, plane_spectra's tables, plane_quadrants, wall stresses, ...) keyed by
+    name; every sample must carry the same keys."""
+
+    def __init__(self):
+        self.navg = 0
+        self.mean = {}
+
+    def add(self, **tables):
+        self.navg += 1
+        if self.navg == 1:
+            self.mean = {k: np.array(v, dtype=np.float64, copy=True) for k, v in tables.items()}
+        else:
+            if set(tables) != set(self.mean):
+                raise ValueError("TimeAverage: a sample's tables differ from the first sample's")
+            n = float(self.navg)
+            for k, v in tables.items():
+                self.mean[k] = (self.mean[k] * (n - 1.0) + np.asarray(v, dtype=np.float64)) / n
+        return self.mean
 
 
 def host_register(a: np.ndarray):

@@ -250,9 +250,35 @@ int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
  *    20-22 VSKEW(J,1..3), 23-25 VFLAT(J,1..3)  third and fourth central moments
  *    26-28 DUDY, DVDY, DWDY mean wall-normal gradients
  * (raw moments as ENERGY stores them; the time averaging of TAVER and the output of
- * WRITEAVG stay with the driver).  The spectra, correlations, quadrant and budget
- * terms of ENERGY are not computed. */
+ * WRITEAVG stay with the driver).  ENERGY's spectra and two-point correlations are
+ * c3d_plane_spectra's, its quadrant analysis c3d_plane_quadrants' (its budget terms are
+ * commented out in the reference). */
 int c3d_plane_stats(c3d_channel *ch, double *out);
+
+/* c3d_plane_spectra computes ENERGY's 1-D energy spectra and two-point correlations
+ * (compact3d.f:10243-10515) for the current state, in FP64.  vmo (VMO(J,L), 3*N2M
+ * values, J fastest; NULL: the instantaneous plane means VM) is the mean the spectra
+ * subtract; the reference passes TAVER's running average.  Outputs are Fortran arrays,
+ * each may be NULL:
+ *   xspec XSPCTR(1:N1M,1:N2M,3)  sum over the x lines of |DFT(v_L - VMO)|^2 / N1M /
+ *                                (PI DX1), divided by N3M (wavenumber index I-1)
+ *   zspec ZSPCTR(1:N3M,1:N2M,3)  the same along z, / N3M / (PI DX3) / N1M
+ *   rxx   RXX(1:N1M,1:N2M,3)     sum_K VP(N1H,J,K) VP(I,J,K) / N3M / (VRMS - VM^2)
+ *   rzz   RZZ(1:N3M,1:N2M,3)     sum_I VP(I,J,N3H) VP(I,J,K) / N1M / (VRMS - VM^2)
+ *   rxy   RXY(1:N1M,1:N2M,3)     sum_K VP(N1H,1,K) VP(I,J,K) / N3M / the two rms
+ * with VP = v_L - VM(J,L), V between J and JPA(J) (JPA(N2M) = N2M), N1H = N1M/2 + 1,
+ * N3H = N3M/2 + 1. */
+int c3d_plane_spectra(c3d_channel *ch, const double *vmo, double *xspec, double *zspec, double *rxx, double *rzz,
+                      double *rxy);
+
+/* c3d_plane_quadrants: ENERGY's quadrant analysis (compact3d.f:10560-10604) for the
+ * current state, FP64: out[(J-1)*8 + q] = Q(J,1..4) for q = 0..3, the sums of
+ * u'v' over the points of quadrants 1-4 of (u', v') negated and divided by N1M N3M, and
+ * QP(J,1..4) for q = 4..7, the quadrants' point fractions, with u' = u - VMP(J,1),
+ * v' = v - VMP(J,2) of the cell-centre velocities.  vmp (2*N2M, J fastest) may be NULL:
+ * the reference's VMP is a local whose assignments are commented out, zero-valued in
+ * practice, which NULL reproduces. */
+int c3d_plane_quadrants(c3d_channel *ch, const double *vmp, double *out);
 
 /* ---- checkpoint ------------------------------------------------------------
  * The restart pair of the reference, CWRITE / READUP (compact3d.f:741-872), writes a

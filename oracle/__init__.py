@@ -72,6 +72,8 @@ def lib():
         L.orc_dqrrt.argtypes = [dp, ip, ctypes.c_double, dp, dp, dp]
         L.orc_get_beta.argtypes = [vp, dp]
         L.orc_filter.argtypes = [vp, ip, dp, ip]
+        L.orc_plane_spectra.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp]
+        L.orc_plane_quadrants.argtypes = [vp, dp, dp, dp]
         for f in ("orc_ctdma11", "orc_ctdma_recip"):
             getattr(L, f).argtypes = [ip, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp, dp]
         L.orc_tdmap.argtypes = [ip, dp, dp, dp, dp, dp]
@@ -152,6 +154,23 @@ class Oracle:
         out = np.zeros(self.grid.n2m * 29)
         lib().orc_plane_stats(self.h, _p(U), _p(P), _p(out))
         return out.reshape(self.grid.n2m, 29)
+
+    def plane_spectra(self, U, vmo=None):
+        """ENERGY's spectra and correlations: dict of Fortran (N, N2M, 3) arrays xspec,
+        zspec (N1M / N3M wavenumbers), rxx, rzz, rxy; vmo (N2M, 3) or None."""
+        g = self.grid
+        out = {k: np.zeros((n, g.n2m, 3), order="F") for k, n in
+               (("xspec", g.n1m), ("zspec", g.n3m), ("rxx", g.n1m), ("rzz", g.n3m), ("rxy", g.n1m))}
+        v = None if vmo is None else np.asfortranarray(vmo, dtype=np.float64)
+        lib().orc_plane_spectra(self.h, _p(U), _p(v), *(_p(out[k]) for k in ("xspec", "zspec", "rxx", "rzz", "rxy")))
+        return out
+
+    def plane_quadrants(self, U, vmp=None):
+        """ENERGY's quadrant analysis: (N2M, 8), Q(J,1..4) then QP(J,1..4)."""
+        out = np.zeros(self.grid.n2m * 8)
+        v = None if vmp is None else np.asfortranarray(vmp, dtype=np.float64)
+        lib().orc_plane_quadrants(self.h, _p(U), _p(v), _p(out))
+        return out.reshape(self.grid.n2m, 8)
 
     def diagnose(self, U):
         f1, f3 = self.chkmf(U)

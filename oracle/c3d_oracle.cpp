@@ -2907,6 +2907,135 @@ void orc_wallss(void *h, const double *U, double *wsm) { wallss_common(*(Orc *)h
 // (uu, vv, ww, uv, uw, vw), 13 PRMS (pp), 14 PV (pv), 15-17 WRMS (vorticity squares),
 // 18 U2V (uuv), 19 VW2 (vww), 20-22 VSKEW and 23-25 VFLAT (third and fourth central
 // moments), 26-28 DUDY, DVDY, DWDY.  Plane means over K, I in that order, as the loops.
+// ENERGY's 1-D spectra and two-point correlations (compact3d.f:10243-10515).  VM(J,L)
+// and VRMS(J,L) = <v_L v_L> are the plane statistics of the cell-centre velocities
+// (10095-10133, V at (J, J+1)); VMO (3 N2M, J fastest; null: VM) is the mean the spectra
+// subtract.  XSPCTR(I,J,L) = sum_K |DFT_x(v_L - VMO)(I-1)|^2 / N1M / (PI DX1) / N3M over the
+// x lines and ZSPCTR(K,J,L) likewise along z (/ N3M / (PI DX3) / N1M).  The correlations
+// use VP = v_L - VM with V at (J, JPA(J)) (JPA(N2M) = N2M) and the points N1H = N1M/2+1,
+// N3H = N3M/2+1: RXX(I,J,L) = sum_K VP(N1H,J,K) VP(I,J,K) / N3M / (VRMS - VM^2),
+// RZZ(K,J,L) = sum_I VP(I,J,N3H) VP(I,J,K) / N1M / (VRMS - VM^2) and RXY(I,J,L) =
+// sum_K VP(N1H,1,K) VP(I,J,K) / N3M / sqrt(VRMS - VM^2)(J) / sqrt(VRMS - VM^2)(1).
+// Outputs are Fortran (N,N2M,3) arrays; any may be null.
+void orc_plane_spectra(void *h, const double *U, const double *VMO, double *XS, double *ZS, double *RXX,
+                       double *RZZ, double *RXY) {
+    Orc &g = *(Orc *)h;
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double NXZ = 1.0 / (double)(N1M * N3M), PI = std::acos(-1.0);
+    std::vector<double> VM((size_t)(N2M + 1) * 4, 0.0), VRMS((size_t)(N2M + 1) * 4, 0.0);
+    auto vm = [&](int J, int L) -> double & { return VM[(size_t)J * 4 + L]; };
+    auto vr = [&](int J, int L) -> double & { return VRMS[(size_t)J * 4 + L]; };
+    auto vc = [&](int I, int J, int K, int L, int JP) {   // cell-centre velocity
+        if (L == 1) return (U[g.iuc(I, J, K, 1)] + U[g.iuc(g.IPA[I], J, K, 1)]) * 0.5;
+        if (L == 2) return (U[g.iuc(I, J, K, 2)] + U[g.iuc(I, JP, K, 2)]) * 0.5;
+        return (U[g.iuc(I, J, K, 3)] + U[g.iuc(I, J, g.KPA[K], 3)]) * 0.5;
+    };
+    for (int J = 1; J <= N2M; J++) {
+        double s[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++)
+                for (int L = 1; L <= 3; L++) {
+                    const double v = vc(I, J, K, L, J + 1);
+                    s[L] = s[L] + v;
+                    q[L] = q[L] + v * v;
+                }
+        for (int L = 1; L <= 3; L++) {
+            vm(J, L) = s[L] * NXZ;
+            vr(J, L) = q[L] * NXZ;
+        }
+    }
+    auto vmo = [&](int J, int L) { return VMO ? VMO[(size_t)(L - 1) * N2M + (J - 1)] : vm(J, L); };
+    if (XS) {
+        const double FS = PI * g.DX1;
+        std::vector<cplx> c(N1M);
+        for (int L = 1; L <= 3; L++)
+            for (int J = 1; J <= N2M; J++) {
+                std::vector<double> acc(N1M, 0.0);
+                for (int K = 1; K <= N3M; K++) {
+                    for (int I = 1; I <= N1M; I++) c[I - 1] = cplx(vc(I, J, K, L, J + 1) - vmo(J, L), 0.0);
+                    fft1d(N1M, -1, c.data(), 1);
+                    for (int I = 0; I < N1M; I++) acc[I] = acc[I] + std::norm(c[I]) / N1M / FS;
+                }
+                for (int I = 0; I < N1M; I++) XS[I + (size_t)N1M * ((J - 1) + (size_t)N2M * (L - 1))] = acc[I] / (double)N3M;
+            }
+    }
+    if (ZS) {
+        const double FS = PI * g.DX3;
+        std::vector<cplx> c(N3M);
+        for (int L = 1; L <= 3; L++)
+            for (int J = 1; J <= N2M; J++) {
+                std::vector<double> acc(N3M, 0.0);
+                for (int I = 1; I <= N1M; I++) {
+                    for (int K = 1; K <= N3M; K++) c[K - 1] = cplx(vc(I, J, K, L, J + 1) - vmo(J, L), 0.0);
+                    fft1d(N3M, -1, c.data(), 1);
+                    for (int K = 0; K < N3M; K++) acc[K] = acc[K] + std::norm(c[K]) / N3M / FS;
+                }
+                for (int K = 0; K < N3M; K++) ZS[K + (size_t)N3M * ((J - 1) + (size_t)N2M * (L - 1))] = acc[K] / (double)N1M;
+            }
+    }
+    const int N1H = N1M / 2 + 1, N3H = N3M / 2 + 1;
+    auto vp = [&](int I, int J, int K, int L) { return vc(I, J, K, L, g.JPA[J]) - vm(J, L); };
+    for (int L = 1; L <= 3; L++)
+        for (int J = 1; J <= N2M; J++) {
+            const double var = vr(J, L) - vm(J, L) * vm(J, L);
+            if (RXX)
+                for (int I = 1; I <= N1M; I++) {
+                    double r = 0.0;
+                    for (int K = 1; K <= N3M; K++) r = r + vp(N1H, J, K, L) * vp(I, J, K, L);
+                    RXX[(I - 1) + (size_t)N1M * ((J - 1) + (size_t)N2M * (L - 1))] = r / (double)N3M / var;
+                }
+            if (RZZ)
+                for (int K = 1; K <= N3M; K++) {
+                    double r = 0.0;
+                    for (int I = 1; I <= N1M; I++) r = r + vp(I, J, N3H, L) * vp(I, J, K, L);
+                    RZZ[(K - 1) + (size_t)N3M * ((J - 1) + (size_t)N2M * (L - 1))] = r / (double)N1M / var;
+                }
+            if (RXY) {
+                const double var1 = vr(1, L) - vm(1, L) * vm(1, L);
+                for (int I = 1; I <= N1M; I++) {
+                    double r = 0.0;
+                    for (int K = 1; K <= N3M; K++) r = r + vp(N1H, 1, K, L) * vp(I, J, K, L);
+                    RXY[(I - 1) + (size_t)N1M * ((J - 1) + (size_t)N2M * (L - 1))] =
+                        r / (double)N3M / std::sqrt(var) / std::sqrt(var1);
+                }
+            }
+        }
+}
+
+// ENERGY's quadrant analysis (compact3d.f:10560-10604): out[(J-1)*8 + q], Q(J,1..4) =
+// -sum(u'v') / (N1M N3M) per sign quadrant of (u', v'), QP(J,1..4) = point counts /
+// (N1M N3M); u' = u_c - VMP(J,1), v' = v_c - VMP(J,2) (VMP 2 N2M, J fastest; null: 0).
+void orc_plane_quadrants(void *h, const double *U, const double *VMP, double *out) {
+    Orc &g = *(Orc *)h;
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double NXZ = 1.0 / (double)(N1M * N3M);
+    for (int J = 1; J <= N2M; J++) {
+        const int JP = J + 1;
+        const double m1 = VMP ? VMP[J - 1] : 0.0, m2 = VMP ? VMP[N2M + J - 1] : 0.0;
+        double UV[4] = {0, 0, 0, 0}, UVP[4] = {0, 0, 0, 0};
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) {
+                const int IP = g.IPA[I];
+                const double V1 = (U[g.iuc(I, J, K, 1)] + U[g.iuc(IP, J, K, 1)]) * 0.5;
+                const double V2 = (U[g.iuc(I, J, K, 2)] + U[g.iuc(I, JP, K, 2)]) * 0.5;
+                const double V1P = V1 - m1, V2P = V2 - m2;
+                int q = -1;
+                if (V1P > 0.0 && V2P > 0.0) q = 0;
+                if (V1P < 0.0 && V2P > 0.0) q = 1;
+                if (V1P < 0.0 && V2P < 0.0) q = 2;
+                if (V1P > 0.0 && V2P < 0.0) q = 3;
+                if (q >= 0) {
+                    UV[q] = UV[q] + V1P * V2P;
+                    UVP[q] = UVP[q] + 1.0;
+                }
+            }
+        for (int q = 0; q < 4; q++) {
+            out[(size_t)(J - 1) * 8 + q] = -UV[q] * NXZ;
+            out[(size_t)(J - 1) * 8 + 4 + q] = UVP[q] * NXZ;
+        }
+    }
+}
+
 void orc_plane_stats(void *h, const double *U, const double *P, double *out) {
     Orc &g = *(Orc *)h;
     const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;
