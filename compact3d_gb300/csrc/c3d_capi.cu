@@ -1266,6 +1266,43 @@ int c3d_plane_quadrants(c3d_channel *ch, const double *vmp, double *out) {
     return 0;
 }
 
+int c3d_wall_spectrum(c3d_channel *ch, double utau, double *out) {
+    if (!ch || !out) { set_error("null argument"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    const Geo &g = ch->g;
+    const size_t nc = ((size_t)g.n1m / 2 + 1) * g.n3m, np_ = (size_t)g.np;
+    double *buf = nullptr;
+    if (dalloc(&buf, 2 * nc + np_)) return C3D_ENOMEM;
+    double2 *c1 = reinterpret_cast<double2 *>(buf);
+    int rc = launch_wall_spectrum(ch, utau, c1, buf + 2 * nc);
+    if (!rc && cudaMemcpyAsync(out, buf + 2 * nc, np_ * sizeof(double), cudaMemcpyDeviceToHost, ch->stream) != cudaSuccess)
+        rc = C3D_ECUDA;
+    if (!rc && cudaStreamSynchronize(ch->stream) != cudaSuccess) rc = C3D_ECUDA;
+    if (rc) set_error("wall spectrum");
+    cudaFree(buf);
+    return rc;
+}
+
+int c3d_corr3d(c3d_channel *ch, double *out) {
+    if (!ch || !out) { set_error("null argument"); return C3D_EINVAL; }
+    if (!ch->have_state) { set_error("c3d_upload must be called before c3d_corr3d"); return C3D_ESTATE; }
+    cudaSetDevice(ch->device);
+    const Geo &g = ch->g;
+    const size_t n = 3 * (size_t)g.n1m * g.n2m * g.n3m, nout = (size_t)g.n2m * 29;
+    if (!ch->stats && dalloc(&ch->stats, stats_scratch_doubles(g))) return C3D_ENOMEM;
+    int rc = launch_stats(ch, ch->stats, ch->stats + nout);
+    if (rc) return rc;
+    double *buf = nullptr;
+    if (dalloc(&buf, n)) return C3D_ENOMEM;
+    rc = launch_corr3d(ch, ch->stats, buf);
+    if (!rc && cudaMemcpyAsync(out, buf, n * sizeof(double), cudaMemcpyDeviceToHost, ch->stream) != cudaSuccess)
+        rc = C3D_ECUDA;
+    if (!rc && cudaStreamSynchronize(ch->stream) != cudaSuccess) rc = C3D_ECUDA;
+    if (rc) set_error("3-D correlation");
+    cudaFree(buf);
+    return rc;
+}
+
 int c3d_checkpoint_write(c3d_channel *ch, const char *path, int ntime, double time, double presg,
                          double presg3) {
     if (!ch || !path) { set_error("null argument"); return C3D_EINVAL; }

@@ -292,6 +292,10 @@ int launch_spectra(c3d_channel *ch, const double *vmo, const double *st, double 
                    double *rzz, double *rxy);
 // ENERGY's quadrant sums into out (8 N2M), part: 8 SB N2M partial sums
 int launch_quadrants(c3d_channel *ch, const double *vmp, double *out, double *part);
+// ENERGY's 3-D correlation into out (3 N1M N2M N3M) and the wall-stress spectrum
+// (c1: (N1M/2 + 1) N3M complex scratch, out: N1M N3M)
+int launch_corr3d(c3d_channel *ch, const double *st, double *out);
+int launch_wall_spectrum(c3d_channel *ch, double utau, double2 *c1, double *out);
 void launch_wall_shift_init(c3d_channel *ch);
 void prof_begin(c3d_channel *ch);
 int prof_collect(c3d_channel *ch);

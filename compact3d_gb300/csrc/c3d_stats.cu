@@ -339,6 +339,94 @@ int launch_quadrants_t(c3d_channel *ch, StepArgs<R> &a, const double *vmp, doubl
 template int launch_quadrants_t<double>(c3d_channel *, StepArgs<double> &, const double *, double *, double *);
 template int launch_quadrants_t<float>(c3d_channel *, StepArgs<float> &, const double *, double *, double *);
 
+// ENERGY's wall-stress spectrum (compact3d.f:10394-10416): the 2-D DFT of the bottom
+// wall's TAUW - UTAU^2.  k_wspec_x: a warp per z row, the x transform of N1M reals as
+// N1M/2 complex pairs and the real-input split, C1(kx, k) for kx = 0..N1M/2 into c1;
+// k_wspec_z: a warp per kx, the z transform and |C|^2 / N1M / N3M / (PI DX3) / (PI DX1)
+// at (kx, kz) and, by the conjugate symmetry of real data, at (N1M - kx, -kz).
+__global__ void __launch_bounds__(32 * SPW) k_wspec_x(Geo g, FftPlan fx, const double *tauw, double utau,
+                                                      const double2 *twp, double2 *c1) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, M = g.n1m / 2;
+    const int k = blockIdx.x * SPW + w;
+    extern __shared__ double2 smw[];
+    double2 *bufa = smw + (size_t)w * (2 * M), *bufb = bufa + M;
+    if (k >= g.n3m) return;
+    const double t2 = utau * utau;
+    const double *row = tauw + (size_t)k * g.n1m;
+    for (int q = lane; q < M; q += 32) bufa[q] = make_double2(row[2 * q] - t2, row[2 * q + 1] - t2);
+    __syncwarp();
+    const double2 *Z = fft_smem<double2, false>(bufa, bufb, fx, 0, 1, 0, -1, lane, 32);
+    for (int q = lane; q <= M; q += 32) {
+        const double2 zk = Z[q == M ? 0 : q], zc = Z[q == 0 ? 0 : M - q];
+        const double2 zm = make_double2(zc.x, -zc.y);
+        const double Ex = 0.5 * (zk.x + zm.x), Ey = 0.5 * (zk.y + zm.y);
+        const double Ox = 0.5 * (zk.y - zm.y), Oy = -0.5 * (zk.x - zm.x);
+        const double2 t = twp[q];
+        c1[(size_t)q * g.n3m + k] = make_double2(Ex + (t.x * Ox - t.y * Oy), Ey + (t.x * Oy + t.y * Ox));
+    }
+}
+
+__global__ void __launch_bounds__(32 * SPW) k_wspec_z(Geo g, FftPlan fz, const double2 *c1, double *out) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, M = g.n1m / 2, N = g.n3m;
+    const int kx = blockIdx.x * SPW + w;
+    extern __shared__ double2 smw[];
+    double2 *bufa = smw + (size_t)w * (2 * N), *bufb = bufa + N;
+    if (kx > M) return;
+    for (int q = lane; q < N; q += 32) bufa[q] = c1[(size_t)kx * N + q];
+    __syncwarp();
+    const double2 *Z = fft_smem<double2, false>(bufa, bufb, fz, 0, 1, 0, -1, lane, 32);
+    const double s = 1.0 / g.n1m / N / (3.141592653589793 * g.dx3) / (3.141592653589793 * g.dx1);
+    for (int q = lane; q < N; q += 32) {
+        const double p = (Z[q].x * Z[q].x + Z[q].y * Z[q].y);
+        out[(size_t)q * g.n1m + kx] = p * s;
+        if (kx > 0 && kx < M) out[(size_t)((N - q) % N) * g.n1m + (g.n1m - kx)] = p * s;
+    }
+}
+
+// ENERGY's 3-D two-point correlation (compact3d.f:10524-10556), a thread per point:
+// RXYZ(I,J,K,L) = VP(N1H,N2H,N3H,L) VP(I,J,K,L) / rms(J) / rms(N2H), Fortran (N1M,N2M,N3M,3)
+template <typename R>
+__global__ void __launch_bounds__(256) k_corr3d(StepArgs<R> a, const double *st, double *out) {
+    const Geo g = a.g;
+    const long long n = (long long)g.n1m * g.n2m * g.n3m;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * n) return;
+    const int L = (int)(t / n);
+    long long r = t - L * n;
+    const int i = (int)(r % g.n1m);
+    r /= g.n1m;
+    const int j = 1 + (int)(r % g.n2m), k = (int)(r / g.n2m);
+    const int jh = g.aly == 1.0 ? g.n2m / 2 + 1 : g.n2m / 4 + 1, ih = g.n1m / 2, kh = g.n3m / 2;
+    auto vm = [&](int jj) { return st[(size_t)(jj - 1) * 29 + L]; };
+    auto rms = [&](int jj) { return sqrt(st[(size_t)(jj - 1) * 29 + 7 + L] - vm(jj) * vm(jj)); };
+    auto jpa = [&](int jj) { return jj == g.n2m ? g.n2m : jj + 1; };
+    const double ref = vcell(a, L, ih, jh, kh, jpa(jh)) - vm(jh);
+    const double vp = vcell(a, L, i, j, k, jpa(j)) - vm(j);
+    out[t] = ref * vp / rms(j) / rms(jh);
+}
+
+template <typename R>
+int launch_corr3d_t(c3d_channel *ch, StepArgs<R> &a, const double *st, double *out) {
+    const long long n = 3LL * ch->g.n1m * ch->g.n2m * ch->g.n3m;
+    k_corr3d<R><<<(unsigned)((n + 255) / 256), 256, 0, ch->stream>>>(a, st, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : C3D_ECUDA;
+}
+template int launch_corr3d_t<double>(c3d_channel *, StepArgs<double> &, const double *, double *);
+template int launch_corr3d_t<float>(c3d_channel *, StepArgs<float> &, const double *, double *);
+
+int launch_wall_spectrum(c3d_channel *ch, double utau, double2 *c1, double *out) {
+    const Geo &g = ch->g;
+    const int M = g.n1m / 2;
+    const size_t smx = (size_t)SPW * 2 * M * sizeof(double2), smz = (size_t)SPW * 2 * g.n3m * sizeof(double2);
+    if (cudaFuncSetAttribute(k_wspec_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx) != cudaSuccess ||
+        cudaFuncSetAttribute(k_wspec_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz) != cudaSuccess)
+        return C3D_ECUDA;
+    const double2 *twp = ch->tw64 + g.n1m / 2 + g.n3m;
+    k_wspec_x<<<(g.n3m + SPW - 1) / SPW, 32 * SPW, smx, ch->stream>>>(g, ch->fx, ch->tauw, utau, twp, c1);
+    k_wspec_z<<<(M + 1 + SPW - 1) / SPW, 32 * SPW, smz, ch->stream>>>(g, ch->fz, c1, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : C3D_ECUDA;
+}
+
 template <typename R>
 int launch_spectra_t(c3d_channel *ch, StepArgs<R> &a, const double *vmo, const double *st, double *xs, double *zs,
                      double *rxx, double *rzz, double *rxy) {

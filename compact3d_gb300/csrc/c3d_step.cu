@@ -477,6 +477,18 @@ int launch_spectra_t(c3d_channel *ch, StepArgs<R> &a, const double *vmo, const d
                      double *rxx, double *rzz, double *rxy);
 
 template <typename R>
+int launch_corr3d_t(c3d_channel *ch, StepArgs<R> &a, const double *st, double *out);
+
+int launch_corr3d(c3d_channel *ch, const double *st, double *out) {
+    if (ch->precision == C3D_MIXED) {
+        StepArgs<float> a = make_args<float>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
+        return launch_corr3d_t<float>(ch, a, st, out);
+    }
+    StepArgs<double> a = make_args<double>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
+    return launch_corr3d_t<double>(ch, a, st, out);
+}
+
+template <typename R>
 int launch_quadrants_t(c3d_channel *ch, StepArgs<R> &a, const double *vmp, double *out, double *part);
 
 int launch_quadrants(c3d_channel *ch, const double *vmp, double *out, double *part) {

@@ -57,6 +57,8 @@ SIGNATURES = {
     "c3d_plane_stats": (_ip, [_vp, _dp]),
     "c3d_plane_spectra": (_ip, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "c3d_plane_quadrants": (_ip, [_vp, _dp, _dp]),
+    "c3d_wall_spectrum": (_ip, [_vp, ctypes.c_double, _dp]),
+    "c3d_corr3d": (_ip, [_vp, _dp]),
     "c3d_checkpoint_write": (_ip, [_vp, ctypes.c_char_p, _ip, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     "c3d_checkpoint_read": (_ip, [_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), _dp, _dp, _dp]),
     "c3d_step": (_ip, [_vp, _ip, ctypes.c_double, _dp, _dp]),
@@ -237,6 +239,19 @@ class Channel:
         v = None if vmp is None else np.asfortranarray(vmp, dtype=np.float64)
         check(load().c3d_plane_quadrants(self.h, _p(v), _p(out)), "c3d_plane_quadrants")
         return out.reshape(self.grid.n2m, 8)
+
+    def wall_spectrum(self, utau: float):
+        """SPECTAUW(1:N1M, 1:N3M, 1) of the bottom wall's TAUW about utau^2."""
+        out = np.zeros((self.grid.n1m, self.grid.n3m), order="F")
+        check(load().c3d_wall_spectrum(self.h, float(utau), _p(out)), "c3d_wall_spectrum")
+        return out
+
+    def corr3d(self):
+        """RXYZ(1:N1M, 1:N2M, 1:N3M, 3)."""
+        g = self.grid
+        out = np.zeros((g.n1m, g.n2m, g.n3m, 3), order="F")
+        check(load().c3d_corr3d(self.h, _p(out)), "c3d_corr3d")
+        return out
 
     # ---- checkpoint (CWRITE / READUP in a format that round-trips) ----
     def checkpoint_write(self, path, ntime: int, time: float, presg: float, presg3: float):

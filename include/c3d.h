@@ -280,6 +280,16 @@ int c3d_plane_spectra(c3d_channel *ch, const double *vmo, double *xspec, double 
  * practice, which NULL reproduces. */
 int c3d_plane_quadrants(c3d_channel *ch, const double *vmp, double *out);
 
+/* c3d_wall_spectrum: ENERGY's 2-D spectrum of the bottom wall's streamwise stress
+ * (compact3d.f:10394-10416), SPECTAUW(I,K,1) = |DFT2(TAUW(.,.,1) - utau^2)(I-1,K-1)|^2
+ * / N1M / N3M / (PI DX3) / (PI DX1), out Fortran (N1M, N3M), FP64; utau is the friction
+ * velocity the driver holds (the reference's sqrt of the averaged wall stress).
+ * c3d_corr3d: ENERGY's 3-D two-point correlation (10524-10556), out RXYZ(N1M,N2M,N3M,3)
+ * = VP(N1H,N2H,N3H,L) VP(I,J,K,L) / rms(J,L) / rms(N2H,L), VP and rms as for
+ * c3d_plane_spectra, N2H = N2M/2 + 1 with ALY = 1 and N2M/4 + 1 otherwise. */
+int c3d_wall_spectrum(c3d_channel *ch, double utau, double *out);
+int c3d_corr3d(c3d_channel *ch, double *out);
+
 /* ---- checkpoint ------------------------------------------------------------
  * The restart pair of the reference, CWRITE / READUP (compact3d.f:741-872), writes a
  * list-directed text file and reads it back unformatted in another loop order, so the

@@ -74,6 +74,8 @@ def lib():
         L.orc_filter.argtypes = [vp, ip, dp, ip]
         L.orc_plane_spectra.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_plane_quadrants.argtypes = [vp, dp, dp, dp]
+        L.orc_wall_spectrum.argtypes = [vp, ctypes.c_double, dp]
+        L.orc_corr3d.argtypes = [vp, dp, dp]
         for f in ("orc_ctdma11", "orc_ctdma_recip"):
             getattr(L, f).argtypes = [ip, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp, dp]
         L.orc_tdmap.argtypes = [ip, dp, dp, dp, dp, dp]
@@ -171,6 +173,19 @@ class Oracle:
         v = None if vmp is None else np.asfortranarray(vmp, dtype=np.float64)
         lib().orc_plane_quadrants(self.h, _p(U), _p(v), _p(out))
         return out.reshape(self.grid.n2m, 8)
+
+    def wall_spectrum(self, utau):
+        """SPECTAUW(1:N1M, 1:N3M, 1) of the oracle's current bottom-wall TAUW."""
+        out = np.zeros((self.grid.n1m, self.grid.n3m), order="F")
+        lib().orc_wall_spectrum(self.h, float(utau), _p(out.reshape(-1, order="F")))
+        return out
+
+    def corr3d(self, U):
+        """RXYZ(1:N1M, 1:N2M, 1:N3M, 3)."""
+        g = self.grid
+        out = np.zeros((g.n1m, g.n2m, g.n3m, 3), order="F")
+        lib().orc_corr3d(self.h, _p(U), _p(out.reshape(-1, order="F")))
+        return out
 
     def diagnose(self, U):
         f1, f3 = self.chkmf(U)

@@ -3036,6 +3036,63 @@ void orc_plane_quadrants(void *h, const double *U, const double *VMP, double *ou
     }
 }
 
+// ENERGY's wall-stress spectrum (compact3d.f:10394-10416): SPECTAUW(I,K,1) =
+// |DFT2(TAUW(.,.,1) - UTAU^2)(I-1,K-1)|^2 / N1M / N3M / (PI DX3) / (PI DX1), Fortran
+// (N1M, N3M); UTAU as the driver holds it (sqrt of the averaged wall stress).
+void orc_wall_spectrum(void *h, double UTAU, double *out) {
+    Orc &g = *(Orc *)h;
+    const int N1M = g.N1M, N3M = g.N3M;
+    const double PI = std::acos(-1.0), FS = PI * g.DX1, FS1 = PI * g.DX3;
+    std::vector<cplx> c((size_t)N1M * N3M);
+    for (int K = 1; K <= N3M; K++)
+        for (int I = 1; I <= N1M; I++) c[(I - 1) + (size_t)N1M * (K - 1)] = cplx(g.TAUW[g.itw(I, K, 1)] - UTAU * UTAU, 0.0);
+    dft2d(N1M, N3M, c.data(), -1);
+    for (size_t q = 0; q < c.size(); q++) out[q] = std::norm(c[q]) / N1M / N3M / FS1 / FS;
+}
+
+// ENERGY's 3-D two-point correlation (compact3d.f:10524-10556): RXYZ(I,J,K,L) =
+// VP(N1H,N2H,N3H,L) VP(I,J,K,L) / sqrt(VRMS - VM^2)(J) / sqrt(VRMS - VM^2)(N2H), VP as in
+// orc_plane_spectra; N2H = N2M/2 + 1 with ALY = 1, N2M/4 + 1 otherwise.  Fortran
+// (N1M, N2M, N3M, 3).
+void orc_corr3d(void *h, const double *U, double *out) {
+    Orc &g = *(Orc *)h;
+    const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M;
+    const double NXZ = 1.0 / (double)(N1M * N3M);
+    auto vc = [&](int I, int J, int K, int L, int JP) {
+        if (L == 1) return (U[g.iuc(I, J, K, 1)] + U[g.iuc(g.IPA[I], J, K, 1)]) * 0.5;
+        if (L == 2) return (U[g.iuc(I, J, K, 2)] + U[g.iuc(I, JP, K, 2)]) * 0.5;
+        return (U[g.iuc(I, J, K, 3)] + U[g.iuc(I, J, g.KPA[K], 3)]) * 0.5;
+    };
+    std::vector<double> VM((size_t)(N2M + 1) * 4, 0.0), VR((size_t)(N2M + 1) * 4, 0.0);
+    for (int J = 1; J <= N2M; J++) {
+        double s[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++)
+                for (int L = 1; L <= 3; L++) {
+                    const double v = vc(I, J, K, L, J + 1);
+                    s[L] = s[L] + v;
+                    q[L] = q[L] + v * v;
+                }
+        for (int L = 1; L <= 3; L++) {
+            VM[(size_t)J * 4 + L] = s[L] * NXZ;
+            VR[(size_t)J * 4 + L] = q[L] * NXZ;
+        }
+    }
+    const int N1H = N1M / 2 + 1, N3H = N3M / 2 + 1, N2H = g.ALY == 1.0 ? N2M / 2 + 1 : N2M / 4 + 1;
+    auto vp = [&](int I, int J, int K, int L) { return vc(I, J, K, L, g.JPA[J]) - VM[(size_t)J * 4 + L]; };
+    for (int L = 1; L <= 3; L++) {
+        const double ref = vp(N1H, N2H, N3H, L);
+        const double sh = std::sqrt(VR[(size_t)N2H * 4 + L] - VM[(size_t)N2H * 4 + L] * VM[(size_t)N2H * 4 + L]);
+        for (int K = 1; K <= N3M; K++)
+            for (int J = 1; J <= N2M; J++) {
+                const double sj = std::sqrt(VR[(size_t)J * 4 + L] - VM[(size_t)J * 4 + L] * VM[(size_t)J * 4 + L]);
+                for (int I = 1; I <= N1M; I++)
+                    out[(I - 1) + (size_t)N1M * ((J - 1) + (size_t)N2M * ((K - 1) + (size_t)N3M * (L - 1)))] =
+                        ref * vp(I, J, K, L) / sj / sh;
+            }
+    }
+}
+
 void orc_plane_stats(void *h, const double *U, const double *P, double *out) {
     Orc &g = *(Orc *)h;
     const int N1M = g.N1M, N2M = g.N2M, N3M = g.N3M, N2 = g.N2;

@@ -92,3 +92,28 @@ def test_plane_quadrants_match_oracle(libc3d, oracle_mod, prec):
         else:
             assert np.abs(a[:, :4] - b[:, :4]).max() <= 1e-6 * np.abs(b[:, :4]).max()
             assert np.abs(a[:, 4:] - b[:, 4:]).max() <= 1.0 / (g.n1m * g.n3m) + 1e-15
+
+
+@pytest.mark.parametrize("prec", [C3D_FP64, C3D_MIXED])
+def test_wall_spectrum_and_corr3d_match_oracle(libc3d, oracle_mod, prec):
+    """SPECTAUW (c3d_wall_spectrum) and RXYZ (c3d_corr3d) against the oracle: the wall
+    spectrum is FP64 on the FP64 wall stress in both forms (1e-12 relative to its peak);
+    RXYZ 1e-10 (FP64, VRMS - VM^2 cancels) and 1e-6 (mixed) relative L2 per component."""
+    g, dt = make_grid("small32", n1m=64, n2m=32, n3m=48)
+    orc = oracle_mod.Oracle(g)
+    U, P, HH = ic.perturbed_laminar(g, amp=0.3)
+    orc.project(U)
+    ch = libc3d.Channel(g, prec)
+    ch.upload(U, P, HH)
+    rng = np.random.default_rng(4)
+    tw = np.zeros(g.shape_tau(), order="F")
+    tw[1:g.n1m + 1, 1:g.n3m + 1, :] = 2.5e-3 + 1e-4 * rng.standard_normal((g.n1m, g.n3m, 2))
+    tb = np.asfortranarray(0.1 * tw)
+    orc.set_wall(tw, tb, 1)
+    ch.upload_wall(tw, tb)
+    a, b = ch.wall_spectrum(0.05), orc.wall_spectrum(0.05)
+    assert np.abs(a - b).max() < 1e-12 * np.abs(b).max()
+    r, q = ch.corr3d(), orc.corr3d(U)
+    tol = 1e-10 if prec == C3D_FP64 else 1e-6
+    for L in range(3):
+        assert np.linalg.norm(r[..., L] - q[..., L]) < tol * np.linalg.norm(q[..., L]), L

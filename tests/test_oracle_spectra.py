@@ -109,3 +109,28 @@ def test_time_average_follows_taver():
     np.testing.assert_allclose(m, np.mean(xs, axis=0), rtol=1e-13)
     with pytest.raises(ValueError):
         ta.add(other=xs[0])
+
+
+def test_wall_spectrum_and_corr3d_known_answers(oracle_mod):
+    """SPECTAUW of TAUW = UTAU^2 + A cos(2 pi (m i / N1M + n k / N3M)) has its two peaks
+    A^2 N1M N3M / 4 / (PI DX1) / (PI DX3) at (m, n) and (-m, -n); RXYZ of an x mode is
+    2 cos(theta(N1H)) cos(theta(I)) on every plane and z index."""
+    g, _ = make_grid("tiny16")
+    o = oracle_mod.Oracle(g)
+    utau, A, m, n = 0.05, 1e-3, 2, 3
+    i = np.arange(g.n1m)[:, None]
+    k = np.arange(g.n3m)[None, :]
+    tw = np.zeros(g.shape_tau(), order="F")
+    tw[1:g.n1m + 1, 1:g.n3m + 1, 0] = utau ** 2 + A * np.cos(2 * np.pi * (m * i / g.n1m + n * k / g.n3m))
+    o.set_wall(tw, np.zeros(g.shape_tau(), order="F"), 1)
+    s = o.wall_spectrum(utau)
+    want = np.zeros((g.n1m, g.n3m))
+    peak = A ** 2 * g.n1m * g.n3m / 4 / (math.pi * g.arrays["dx1"]) / (math.pi * g.arrays["dx3"])
+    want[m, n] = want[g.n1m - m, g.n3m - n] = peak
+    np.testing.assert_allclose(s, want, atol=1e-12 * peak)
+    U = _mode_field(g, 3, 0, 0.3)
+    r = o.corr3d(U)
+    theta = 2 * np.pi * 3 * (np.arange(g.n1m) + 0.5) / g.n1m + 0.4
+    want3 = 2 * np.cos(theta[g.n1m // 2]) * np.cos(theta)
+    np.testing.assert_allclose(r[:, 4, 7, 0], want3, atol=1e-12)
+    np.testing.assert_allclose(r[:, 0, 2, 0], want3, atol=1e-12)
