@@ -531,7 +531,9 @@ def run_next(args, D: Dist, g, dt, U0, P0, HH0):
     for key, over, label in (("les_werner", dict(wmodel=4), "SGSCS + WALLMODEL_WERNER (WMODEL 4)"),
                              ("les_marusic", dict(wmodel=3), "SGSCS + MARUSIC1 (WMODEL 3)"),
                              ("les_piomelli", dict(wmodel=5), "SGSCS + PIOMELLI (WMODEL 5)"),
-                             ("les_sgssd", dict(files=3), "SGSSD (FILES 3) + WALLMODEL_INSTANT")):
+                             ("les_sgssd", dict(files=3), "SGSSD (FILES 3) + WALLMODEL_INSTANT"),
+                             ("les_iwmles", dict(wmodel=2), "SGSCS + WALLMODEL_IWMLES_SMOOTH (WMODEL 2), "
+                                                            "model updates every fifth step inside the timed steps")):
         gl, dtl = make_grid("les128", **over)
         Ul, Pl, Hl = ic.loglaw(gl, 2000.0, amp=0.05, seed=ic.SEED0 + 3000 + D.rank)
         c = make_channel(lib, gl, "mixed", Ul, Pl, Hl)

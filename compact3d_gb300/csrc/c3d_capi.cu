@@ -199,6 +199,7 @@ void free_channel(c3d_channel *ch) {
     if (ch->wtaue) cudaFree(ch->wtaue);
     if (ch->wshift) cudaFree(ch->wshift);
     if (ch->specbuf) cudaFree(ch->specbuf);
+    if (ch->iwm) cudaFree(ch->iwm);
     if (ch->sdpart) cudaFree(ch->sdpart);
     if (ch->sfork) cudaEventDestroy(ch->sfork);
     if (ch->sjoin) cudaEventDestroy(ch->sjoin);
@@ -342,9 +343,13 @@ int check_grid(const c3d_grid *g) {
         set_error("FILES must be 0 (DNS), 1 (SGSDY), 2 (SGSCS) or 3 (SGSSD)");
         return C3D_EINVAL;
     }
-    if (!(g->wmodel == 0 || g->wmodel == 1 || g->wmodel == 3 || g->wmodel == 4 || g->wmodel == 5)) {
-        set_error("WMODEL must be 0, 1 (WALLMODEL_INSTANT), 3 (MARUSIC1), 4 (WALLMODEL_WERNER) or 5 (PIOMELLI); "
-                  "the other wall models are not built");
+    if (g->wmodel < 0 || g->wmodel > 5) {
+        set_error("WMODEL must be 0, 1 (WALLMODEL_INSTANT), 2 (WALLMODEL_IWMLES_SMOOTH), 3 (MARUSIC1), "
+                  "4 (WALLMODEL_WERNER) or 5 (PIOMELLI)");
+        return C3D_EINVAL;
+    }
+    if (g->wmodel == 2 && g->y[0] != 0.0) {
+        set_error("Y(0) = Y0 != 0 with WMODEL 2 selects WALLMODEL_IWMLES_ROUGH, which is not built");
         return C3D_EINVAL;
     }
     if (g->wmodel == 3 || g->wmodel == 5) {
@@ -503,6 +508,10 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
              cudaEventCreateWithFlags(&ch->wfork, cudaEventDisableTiming) != cudaSuccess ||
              cudaEventCreateWithFlags(&ch->wjoin, cudaEventDisableTiming) != cudaSuccess))
             return fail(C3D_ECUDA);
+        if (gr->wmodel == 2) {
+            if (dalloc(&ch->iwm, c3d::iwm_doubles(g))) return fail(C3D_ENOMEM);
+            ch->iwm_dzp = gr->dy[1] + gr->dy[2] + gr->dy[3] / 2.0;
+        }
         if (gr->wmodel == 3 || gr->wmodel == 5) {
             const size_t ny = (size_t)g.n2 + 1;
             if (dalloc(&ch->wshift, c3d::wall_shift_doubles(g))) return fail(C3D_ENOMEM);
@@ -963,8 +972,8 @@ static int step_common(c3d_channel *ch, double dt, double *presg, double *presg3
 }
 
 int c3d_step(c3d_channel *ch, int ntime, double dt, double *presg, double *presg3) {
-    (void)ntime;
     if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    ch->ntime = ntime;
     if (!presg || !presg3) { set_error("null PRESG/PRESG3"); return C3D_EINVAL; }
     if (!ch->have_state) { set_error("c3d_upload must be called before c3d_step"); return C3D_ESTATE; }
     cudaSetDevice(ch->device);
@@ -972,11 +981,17 @@ int c3d_step(c3d_channel *ch, int ntime, double dt, double *presg, double *presg
 }
 
 int c3d_step_async(c3d_channel *ch, int ntime, double dt) {
-    (void)ntime;
     if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    ch->ntime = ntime;
     if (!ch->have_state) { set_error("c3d_upload must be called before c3d_step_async"); return C3D_ESTATE; }
     cudaSetDevice(ch->device);
     return step_common(ch, dt, nullptr, nullptr, false);
+}
+
+int c3d_set_cflmax(c3d_channel *ch, double cflmax) {
+    if (!ch || !(cflmax > 0) || !isfinite(cflmax)) { set_error("CFLMAX must be positive and finite"); return C3D_EINVAL; }
+    ch->cflmax = cflmax;
+    return 0;
 }
 
 int c3d_set_presg(c3d_channel *ch, double presg, double presg3) {
@@ -1137,7 +1152,7 @@ int c3d_getup(c3d_channel *ch, double *u, double *p, double *hh, double *sgsvis,
         double *sg = ch->files != 0 ? sgsvis : nullptr;
         if (host_pinned(u, 3 * n3 * 8) && host_pinned(p, np_ * 8) && host_pinned(hh, 3 * n3 * 8) &&
             (!sg || host_pinned(sg, n3 * 8)) && !ch->prof_on) {
-            (void)ntime;
+            ch->ntime = ntime;
             if (!(dt > 0) || !isfinite(dt)) { set_error("dt must be positive and finite"); return C3D_EINVAL; }
             return getup_overlapped(ch, u, u, p, p, hh, hh, sg, dt, presg, presg3);
         }
@@ -1689,6 +1704,11 @@ int c3d_batch_create(int nchan, const c3d_grid *grids, c3d_batch **out) {
             return rc;
         }
         b->ch.push_back(c);
+        if (grids[i].files != 0 && grids[i].wmodel == 2) {   // its update schedule follows NTIME
+            set_error("WMODEL 2 (WALLMODEL_IWMLES_SMOOTH) channels step individually, not in a batch graph");
+            batch_free(b);
+            return C3D_EINVAL;
+        }
     }
     b->join.resize(nchan, nullptr);
     bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&

@@ -168,6 +168,12 @@ struct c3d_channel {
     double *wshift = nullptr;
     // SGSSD: per-plane partial sums of k_sgs_sd_sums (N2M x sdnt x 10) and BETA(0:N2)
     double *specbuf = nullptr;   // c3d_plane_spectra: means and the five output tables
+    // WALLMODEL_IWMLES_SMOOTH: per-point state, whether it is set, the accumulated model
+    // step, DY(1) + DY(2) + DY(3)/2, the driver's CFLMAX and the NTIME of the step
+    double *iwm = nullptr;
+    int iwm_ready = 0;
+    double iwm_dt = 0.0, iwm_dzp = 0.0, cflmax = 1.0;
+    int ntime = 1;
     double *sdpart = nullptr, *sdbeta = nullptr;
     int sdnt = 0;
     // SGSSD's per-plane root solve and nu run beside BCOND and the RHS passes, which do
@@ -287,6 +293,10 @@ void mark(c3d_channel *ch, int *nl, const char *name, double bytes);
     } while (0)
 // the shifted-point wall models' scratch: its size in doubles and the mesh tables
 size_t wall_shift_doubles(const Geo &g);
+// WALLMODEL_IWMLES_SMOOTH: the state's size in doubles and one step of the model on st
+size_t iwm_doubles(const Geo &g);
+template <typename R>
+int launch_iwm_t(c3d_channel *ch, StepArgs<R> &a, cudaStream_t st, double *tauw, double *taub);
 // ENERGY's spectra and correlations (vmo: 3 N2M means; st: the plane statistics table)
 int launch_spectra(c3d_channel *ch, const double *vmo, const double *st, double *xs, double *zs, double *rxx,
                    double *rzz, double *rxy);

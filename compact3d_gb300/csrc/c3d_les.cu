@@ -1445,6 +1445,10 @@ int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *n
                 k_wall_werner_avg<R><<<nb, TPB, 0, wst>>>(a, l, ch->wtaue);
                 *nl += 2;
                 mark(ch, nl, "wall", 96.0 * g.np);
+            } else if (ch->files != 0 && ch->wmodel == 2) {
+                int rc2 = launch_iwm_t<R>(ch, a, wst, l.tauw, l.taub);
+                if (rc2) return rc2;
+                mark(ch, nl, "wall", 64.0 * g.np);
             } else if (ch->files != 0 && (ch->wmodel == 3 || ch->wmodel == 5)) {
                 const int nb = nblk(g.np);
                 const int jd = ch->wmodel == 3 ? ch->wzs : 1, ju = ch->wmodel == 3 ? g.n2m - ch->wzs + 1 : g.n2m;

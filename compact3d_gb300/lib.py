@@ -58,6 +58,7 @@ SIGNATURES = {
     "c3d_plane_spectra": (_ip, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "c3d_plane_quadrants": (_ip, [_vp, _dp, _dp]),
     "c3d_wall_spectrum": (_ip, [_vp, ctypes.c_double, _dp]),
+    "c3d_set_cflmax": (_ip, [_vp, ctypes.c_double]),
     "c3d_corr3d": (_ip, [_vp, _dp]),
     "c3d_checkpoint_write": (_ip, [_vp, ctypes.c_char_p, _ip, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     "c3d_checkpoint_read": (_ip, [_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), _dp, _dp, _dp]),
@@ -239,6 +240,9 @@ class Channel:
         v = None if vmp is None else np.asfortranarray(vmp, dtype=np.float64)
         check(load().c3d_plane_quadrants(self.h, _p(v), _p(out)), "c3d_plane_quadrants")
         return out.reshape(self.grid.n2m, 8)
+
+    def set_cflmax(self, cflmax: float):
+        check(load().c3d_set_cflmax(self.h, float(cflmax)), "c3d_set_cflmax")
 
     def wall_spectrum(self, utau: float):
         """SPECTAUW(1:N1M, 1:N3M, 1) of the bottom wall's TAUW about utau^2."""

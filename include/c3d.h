@@ -65,10 +65,11 @@ extern "C" {
  *   /FINOUT/ FILES (SGS model)             -> files  (0 none, 1 SGSDY, 2 SGSCS,
  *                                             3 SGSSD)
  *   /WALLMODEL/ WMODEL                     -> wmodel (0 none, 1 WALLMODEL_INSTANT,
- *                                             3 MARUSIC1, 4 WALLMODEL_WERNER,
- *                                             5 PIOMELLI; with 1, Y(0) must be 0:
- *                                             Y0 != 0 selects the rough-wall model,
- *                                             which is not built; 4 needs N3 <= N1;
+ *                                             2 WALLMODEL_IWMLES_SMOOTH, 3 MARUSIC1,
+ *                                             4 WALLMODEL_WERNER, 5 PIOMELLI; with 1
+ *                                             and 2, Y(0) must be 0: Y0 != 0 selects
+ *                                             the rough-wall models, which are not
+ *                                             built; 4 needs N3 <= N1;
  *                                             3 and 5 need Y(1:N2) increasing, see
  *                                             below)
  * The library takes the driver's metric arrays as given; it recomputes only
@@ -152,6 +153,14 @@ int c3d_set_device(int device);
  * interpolation cell, so Y(1:N2) must increase; PIOMELLI's height H(1) climbs by 1e-6
  * per wall point while it lies below YC(1), as the reference's by-reference INDEX_IJK
  * does, and c3d_create refuses grids where it starts more than 2e-3 below.
+ * WALLMODEL_IWMLES_SMOOTH (wmodel 2, compact3d.f:3386-4279) is the integral wall model
+ * on the bottom wall: its per-point state (filtered velocity and pressure, integrals,
+ * u_tau) is initialised at NTIME = 1 (or at the channel's first step with it) from the
+ * log law on the mean u of plane 3 and CFLMAX (c3d_set_cflmax, default 1), updated every
+ * fifth step (NTIME mod 5 = 0, the NTIME passed to c3d_step) and imposed every step;
+ * the spanwise stress the reference writes to TAUW(I,K,3), beyond TAUW, lands on
+ * TAUB(I,K,1) of /TAUXYZ/, where it is stored; WSM(1) is the plane mean of
+ * |(tauwx, tauwy)|.  Batches refuse it (its schedule follows NTIME).
  * c3d_upload_wall / c3d_download_wall  TAUW, TAUB (0:M1,0:M3,2) of /TAUXYZ/ (the
  *               interior I = 1..N1M, K = 1..N3M of both walls; either may be NULL).
  *               WALLMODEL_INSTANT updates the bottom wall (index 1) and the top
@@ -202,6 +211,9 @@ int c3d_last_step_stats(c3d_channel *ch, double *ms, int *kernel_launches);
  * (c3d_set_presg before the first step, c3d_get_presg to read them, which
  * waits for the queued work). */
 int c3d_step_async(c3d_channel *ch, int ntime, double dt);
+/* CFLMAX of the driver, which WALLMODEL_IWMLES_SMOOTH's initial filter time scale uses
+ * (wm_tR = (CFLMAX ALX / N1M / U) / (DZ / 0.4 / u_tau)); default 1. */
+int c3d_set_cflmax(c3d_channel *ch, double cflmax);
 int c3d_set_presg(c3d_channel *ch, double presg, double presg3);
 int c3d_get_presg(c3d_channel *ch, double *presg, double *presg3);
 /* CUDA-event timer on the channel's stream: start, then stop returns the

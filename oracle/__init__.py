@@ -75,6 +75,9 @@ def lib():
         L.orc_plane_spectra.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_plane_quadrants.argtypes = [vp, dp, dp, dp]
         L.orc_wall_spectrum.argtypes = [vp, ctypes.c_double, dp]
+        L.orc_set_cflmax.argtypes = [vp, ctypes.c_double]
+        L.orc_iwm_slots.restype = ip
+        L.orc_get_iwm.argtypes = [vp, dp]
         L.orc_corr3d.argtypes = [vp, dp, dp]
         for f in ("orc_ctdma11", "orc_ctdma_recip"):
             getattr(L, f).argtypes = [ip, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp, dp]
@@ -186,6 +189,16 @@ class Oracle:
         out = np.zeros((g.n1m, g.n2m, g.n3m, 3), order="F")
         lib().orc_corr3d(self.h, _p(U), _p(out.reshape(-1, order="F")))
         return out
+
+    def set_cflmax(self, cflmax):
+        lib().orc_set_cflmax(self.h, float(cflmax))
+
+    def get_iwm(self):
+        """WALLMODEL_IWMLES_SMOOTH's per-point state, (slots, N3M, N1M)."""
+        g = self.grid
+        out = np.zeros(lib().orc_iwm_slots() * g.n1m * g.n3m)
+        lib().orc_get_iwm(self.h, _p(out))
+        return out.reshape(-1, g.n3m, g.n1m)
 
     def diagnose(self, U):
         f1, f3 = self.chkmf(U)

@@ -55,6 +55,9 @@ struct Orc {
     double TAOW = 0.0;                // /WALLTAO/ TAOW
     std::vector<double> SMAGC;        // /SGSMEAN/ SMAGC(1:N2M)
     std::vector<double> BETA;         // SGSSD's scale-dependence BETA per plane (unclipped)
+    std::vector<double> IWM;          // WALLMODEL_IWMLES_SMOOTH's per-point state (IW_NS x N1M N3M)
+    double WM_DT = 0.0, CFLMAX = 1.0; // its accumulated step and the driver's CFLMAX
+    int iwm_ready = 0;
     std::vector<double> SGS;          // SGSVIS when the caller passes none
     int wall_iter_cap = 10000;        // Newton iterations allowed per wall point
     // work arrays of GETUP / UHCALC / DPCALC
@@ -2143,10 +2146,311 @@ int wallmodel_shifted(Orc &g, const double *U) {
     return 0;
 }
 
-// The wall model WALL_MODEL dispatches to (compact3d.f:1982-2011) for WMODEL = 1, 3, 4, 5.
-int wallmodel(Orc &g, const double *U) {
+// ----------------------------------------------------------------------------------
+// WALLMODEL_IWMLES_SMOOTH (WMODEL 2 with Y0 = 0, compact3d.f:3386-4279), the integral
+// wall model of Yang et al. 2015 on the bottom wall.  Per wall point a state of IWM_NS
+// values (the reference's /IWMLES/ arrays) persists across steps: it is initialised at
+// NTIME = 1 (or at the first call, where the reference would read a zeroed COMMON), the
+// time-filtered velocity and pressure, the integrals and the stresses are recomputed every
+// iwm_ntime_skip = 5 steps (NTIME mod 5 = 0) with the step WM_DT accumulated since, and
+// TAUW is imposed every step.  The reference stores the spanwise stress in TAUW(I,K,3),
+// beyond TAUW's extent (0:M1,0:M3,2); in /TAUXYZ/ that element is TAUB(I,K,1), which is
+// where it is stored here.  WSM(1) = TAOW is the plane mean of sqrt(tauwx^2 + tauwy^2).
+// ----------------------------------------------------------------------------------
+enum {
+    IW_UTX, IW_UTY, IW_TAUWX, IW_TAUWY, IW_FTX, IW_FTY, IW_FTMX, IW_FTMY, IW_FP, IW_INTE, IW_INTEM = IW_INTE + 5,
+    IW_DIFFX = IW_INTEM + 5, IW_DIFFY, IW_LHSX, IW_LHSY, IW_FUS, IW_TR, IW_DZ, IW_AX, IW_AY, IW_CX, IW_CY,
+    IW_UNSX, IW_UNSY, IW_DELI, IW_DELV, IW_DTX, IW_DTY, IW_DBX, IW_DBY, IW_CONVX, IW_CONVY, IW_PRSX, IW_PRSY,
+    IW_NS
+};
+// integral indices iwm_Lu = 1, iwm_Luu = 2, iwm_Lv = 3, iwm_Lvv = 4, iwm_Luv = 5
+enum { IW_LU = 0, IW_LUU = 1, IW_LV = 2, IW_LVV = 3, IW_LUV = 4 };
+
+// the Newton iteration for u_tau on the log law U/u - log(u DZP RE)/KAPA - B (KAPA 0.4,
+// B 5), as in iwm_init_smooth and the equilibrium fallback (compact3d.f:3589-3604, 4079-4091)
+static double iwm_loglaw(double U_ave, double DZP, double RE) {
+    const double KAPA = 0.4, B = 5.0;
+    double U_tau1 = 1.0, U_tau2 = 0.000001, LAMBDA = 1.0;
+    for (int it = 0; it < 100000 && std::fabs(U_tau2 - U_tau1) > 1.0E-6; it++) {
+        U_tau1 = U_tau2;
+        const double FUtau1 = U_ave / U_tau1 - std::log(U_tau1 * DZP * RE) / KAPA - B;
+        const double FUtau2 = -U_ave / std::pow(U_tau1, 2.0) - 1. / KAPA / U_tau1;
+        U_tau2 = U_tau1 - LAMBDA * FUtau1 / FUtau2;
+        const double FUtau3 = U_ave / U_tau2 - std::log(U_tau2 * DZP * RE) / KAPA - B;
+        if (std::fabs(FUtau3) > std::fabs(FUtau1)) LAMBDA = 0.5 * LAMBDA;
+    }
+    return U_tau1;
+}
+
+// iwm_slv_smooth (compact3d.f:3881-3926): the integrated momentum residuals (fx, fy)
+static void iwm_slv(double lhsx, double lhsy, double Ux, double Uy, double Dz, double utx, double uty, double RE,
+                    double &fx, double &fy) {
+    const double vonk = 0.4, reinv = 1.0 / RE;
+    const double us = std::pow(std::pow(utx, 4.0) + std::pow(uty, 4.0), 0.25);
+    const double delv = reinv / us;
+    const double deli = std::min(11.0 * reinv / us, Dz);
+    const double Vel = std::sqrt(std::pow(Ux, 2.0) + std::pow(Uy, 2.0));
+    const double Ax = (Ux / us + Ux / Vel / vonk * std::log(deli / Dz) - deli / delv * utx / us) / (1.0 - deli / Dz);
+    const double Ay = (Uy / us + Uy / Vel / vonk * std::log(deli / Dz) - deli / delv * uty / us) / (1.0 - deli / Dz);
+    const double Cx = Ux / us - Ax, Cy = Uy / us - Ay;
+    const double inteLu = 0.5 * utx * std::pow(deli, 2.0) / delv +
+                          us * Dz * (0.5 * Ax * (1.0 - std::pow(deli, 2.0) / std::pow(Dz, 2.0)) + Cx * (1.0 - deli / Dz) -
+                                     1.0 / vonk * Ux / Vel * (1.0 - deli / Dz + deli / Dz * std::log(deli / Dz)));
+    const double inteLv = 0.5 * uty * std::pow(deli, 2.0) / delv +
+                          us * Dz * (0.5 * Ay * (1.0 - std::pow(deli, 2.0) / std::pow(Dz, 2.0)) + Cy * (1.0 - deli / Dz) -
+                                     1.0 / vonk * Uy / Vel * (1.0 - deli / Dz + deli / Dz * std::log(deli / Dz)));
+    fx = inteLu + lhsx;
+    fy = inteLv + lhsy;
+}
+
+int wallmodel_iwmles(Orc &g, const double *U, const double *P, int NTIME, double DT, double PRESG, double PRESG3) {
+    const int N1M = g.N1M, N3M = g.N3M;
+    const size_t NP = (size_t)N1M * N3M;
+    const double RE = g.RE, reinv = 1.0 / RE, vonk = 0.4;
+    auto st = [&](int I, int K, int q) -> double & { return g.IWM[(size_t)q * NP + (I - 1) + (size_t)N1M * (K - 1)]; };
+    const double Dzp = g.DY[1] + g.DY[2] + g.DY[3] / 2.0;
+    if (NTIME == 1 || !g.iwm_ready) {   // iwm_init_smooth (compact3d.f:3561-3714)
+        g.IWM.assign(NP * IW_NS, 0.0);
+        double uinit = 0.0;
+        for (int K = 1; K <= N3M; K++)
+            for (int I = 1; I <= N1M; I++) uinit = uinit + U[g.iuc(I, 3, K, 1)];
+        uinit = uinit / (double)(N1M * N3M);
+        const double usinit = iwm_loglaw(uinit, Dzp, RE);
+        for (int I = 1; I <= N1M; I++)
+            for (int K = 1; K <= N3M; K++) {
+                st(I, K, IW_UTX) = usinit;
+                st(I, K, IW_TAUWX) = std::pow(usinit, 2.0);
+                st(I, K, IW_FTX) = uinit;
+                st(I, K, IW_FTMX) = uinit;
+                st(I, K, IW_INTE + IW_LU) = uinit * Dzp;
+                st(I, K, IW_INTE + IW_LUU) = std::pow(uinit, 2.0) * Dzp;
+                st(I, K, IW_INTEM + IW_LU) = uinit * Dzp;
+                st(I, K, IW_INTEM + IW_LUU) = std::pow(uinit, 2.0) * Dzp;
+                st(I, K, IW_LHSX) = -uinit * Dzp;
+                st(I, K, IW_LHSY) = -uinit * Dzp;
+                st(I, K, IW_DTX) = usinit / vonk / Dzp;
+                st(I, K, IW_FUS) = usinit;
+                st(I, K, IW_TR) = (g.CFLMAX * g.ALX / N1M / uinit) / (Dzp / vonk / usinit);
+                st(I, K, IW_DZ) = Dzp;
+                st(I, K, IW_DELI) = std::min(11.0 * reinv / usinit, Dzp);
+                st(I, K, IW_DELV) = reinv / usinit;
+            }
+        g.WM_DT = 5 * DT;
+        g.iwm_ready = 1;
+    }
+    // iwm_wallstress_smooth (compact3d.f:3489-3557)
+    if (NTIME % 5 == 1) g.WM_DT = DT;
+    else g.WM_DT = g.WM_DT + DT;
+    const double wm_dt = g.WM_DT;
+    int status = 0;
+    if (NTIME % 5 == 0) {
+        // iwm_calc_lhs_smooth (3718-3877)
+        double p_bar = 0.0;
+        for (int I = 1; I <= N1M; I++)
+            for (int K = 1; K <= N3M; K++) p_bar = p_bar + P[g.ip(I, 1, K)];
+        p_bar = p_bar / (double)N1M / (double)N3M;
+        for (int I = 1; I <= N1M; I++)
+            for (int K = 1; K <= N3M; K++) {
+                st(I, K, IW_FTMX) = st(I, K, IW_FTX);
+                st(I, K, IW_FTMY) = st(I, K, IW_FTY);
+                const double u_inst = U[g.iuc(I, 3, K, 1)], v_inst = U[g.iuc(I, 3, K, 3)];
+                const double p_inst = P[g.ip(I, 1, K)] - p_bar, tR = st(I, K, IW_TR);
+                st(I, K, IW_FTX) = st(I, K, IW_FTX) * (1.0 - tR) + u_inst * tR;
+                st(I, K, IW_FTY) = st(I, K, IW_FTY) * (1.0 - tR) + v_inst * tR;
+                st(I, K, IW_FP) = st(I, K, IW_FP) * (1.0 - tR) + p_inst * tR;
+            }
+        for (int K = 1; K <= N3M; K++) {
+            const int KP = g.KPA[K], KM = g.KMA[K];
+            for (int I = 1; I <= N1M; I++) {
+                const int IP = g.IPA[I], IM = g.IMA[I];
+                st(I, K, IW_UNSX) = (st(I, K, IW_INTE + IW_LU) - st(I, K, IW_INTEM + IW_LU)) / wm_dt;
+                st(I, K, IW_UNSY) = (st(I, K, IW_INTE + IW_LV) - st(I, K, IW_INTEM + IW_LV)) / wm_dt;
+                const double uux = (st(IP, K, IW_INTE + IW_LUU) - st(IM, K, IW_INTE + IW_LUU)) * g.DX1 / 2.0;
+                const double uvy = (st(I, KP, IW_INTE + IW_LUV) - st(I, KM, IW_INTE + IW_LUV)) * g.DX3 / 2.0;
+                const double uvx = (st(IP, K, IW_INTE + IW_LUV) - st(IM, K, IW_INTE + IW_LUV)) * g.DX1 / 2.0;
+                const double vvy = (st(I, KP, IW_INTE + IW_LVV) - st(I, KM, IW_INTE + IW_LVV)) * g.DX3 / 2.0;
+                const double ux = (st(IP, K, IW_INTE + IW_LU) - st(IM, K, IW_INTE + IW_LU)) * g.DX1 / 2.0;
+                const double vy = (st(I, KP, IW_INTE + IW_LV) - st(I, KM, IW_INTE + IW_LV)) * g.DX3 / 2.0;
+                st(I, K, IW_CONVX) = uux + uvy - st(I, K, IW_FTMX) * (ux + vy);
+                st(I, K, IW_CONVY) = uvx + vvy - st(I, K, IW_FTMY) * (ux + vy);
+                const double Dz = st(I, K, IW_DZ);
+                st(I, K, IW_PRSX) = (st(IP, K, IW_FP) - st(IM, K, IW_FP)) * g.DX1 / 2.0 * Dz + PRESG * Dz;
+                st(I, K, IW_PRSY) = (st(I, KP, IW_FP) - st(I, KM, IW_FP)) * g.DX3 / 2.0 * Dz + PRESG3 * Dz;
+                st(I, K, IW_LHSX) = -st(I, K, IW_INTE + IW_LU) +
+                                    wm_dt * (st(I, K, IW_CONVX) + st(I, K, IW_PRSX) - st(I, K, IW_DIFFX));
+                st(I, K, IW_LHSY) = -st(I, K, IW_INTE + IW_LV) +
+                                    wm_dt * (st(I, K, IW_CONVY) + st(I, K, IW_PRSY) - st(I, K, IW_DIFFY));
+            }
+        }
+        // iwm_calc_wallstress_smooth (3930-4279)
+        const double KAPA = 0.4, B = 5.0, deltap = Dzp;
+        const int MaxIter = 1500;
+        const double wm_tol = 0.000001, wm_eps = 0.000000001;
+        (void)KAPA;
+        (void)B;
+        // equilutx/equiluty are locals of the point loop that only the equilibrium fallback
+        // sets: a point whose linear correction |A| > 1 sends it to that branch without a
+        // fallback of its own takes the values of the last point (I outer, K inner) that
+        // had one (zero before the first)
+        double equilutx = 0.0, equiluty = 0.0;
+        for (int I = 1; I <= N1M; I++)
+            for (int K = 1; K <= N3M; K++) {
+                const double lhsx = st(I, K, IW_LHSX), lhsy = st(I, K, IW_LHSY);
+                const double Ux = st(I, K, IW_FTX), Uy = st(I, K, IW_FTY), Dz = st(I, K, IW_DZ);
+                double &utx = st(I, K, IW_UTX), &uty = st(I, K, IW_UTY);
+                double fx, fy, fxp, fyp;
+                iwm_slv(lhsx, lhsy, Ux, Uy, Dz, utx, uty, RE, fx, fy);
+                int iter = 0, equil_flag = 0;
+                while (std::max(std::fabs(fx), std::fabs(fy)) > wm_tol) {
+                    iwm_slv(lhsx, lhsy, Ux, Uy, Dz, utx + wm_eps, uty, RE, fxp, fyp);
+                    const double a11 = (fxp - fx) / wm_eps, a21 = (fyp - fy) / wm_eps;
+                    iwm_slv(lhsx, lhsy, Ux, Uy, Dz, utx, uty + wm_eps, RE, fxp, fyp);
+                    const double a12 = (fxp - fx) / wm_eps, a22 = (fyp - fy) / wm_eps;
+                    const double det = a11 * a22 - a12 * a21;
+                    const double nx = utx - (a22 * fx - a12 * fy) / det;
+                    const double ny = uty - (-a21 * fx + a11 * fy) / det;
+                    utx = nx;
+                    uty = ny;
+                    iwm_slv(lhsx, lhsy, Ux, Uy, Dz, utx, uty, RE, fx, fy);
+                    iter = iter + 1;
+                    if (iter > MaxIter) {
+                        equil_flag = 1;
+                        break;
+                    }
+                }
+                if (utx - 1.0 == utx || uty - 1.0 == uty) equil_flag = 1;
+                if (equil_flag == 1) {
+                    const double U_ave = std::sqrt(std::pow(Ux, 2.) + std::pow(Uy, 2.));
+                    const double U_tau1 = iwm_loglaw(U_ave, deltap, RE);
+                    const double TAUW1 = std::pow(U_tau1, 2);
+                    equilutx = TAUW1 * Ux / U_ave;
+                    equiluty = TAUW1 * Uy / U_ave;
+                    utx = std::sqrt(std::fabs(equilutx));
+                    uty = std::sqrt(std::fabs(equiluty));
+                }
+                const double wmputx = utx, wmputy = uty, wmpDz = Dz;
+                const double utaup = std::pow(std::pow(wmputx, 4.0) + std::pow(wmputy, 4.0), 0.25);
+                const double wmpdelv = reinv / utaup;
+                const double wmpdeli = std::min(11.0 * reinv / utaup, wmpDz);
+                const double wmpUx = Ux, wmpUy = Uy;
+                const double wmpVel = std::sqrt(std::pow(wmpUx, 2.0) + std::pow(wmpUy, 2.0));
+                double wmpAx = 0.0, wmpAy = 0.0, wmpCx = 0.0, wmpCy = 0.0;
+                const double lg = std::log(wmpdeli / wmpDz);
+                if (equil_flag != 1) {
+                    wmpAx = (wmpUx / utaup + wmpUx / wmpVel / vonk * lg - wmpdeli / wmpdelv * wmputx / utaup) /
+                            (1.0 - wmpdeli / wmpDz);
+                    wmpAy = (wmpUy / utaup + wmpUy / wmpVel / vonk * lg - wmpdeli / wmpdelv * wmputy / utaup) /
+                            (1.0 - wmpdeli / wmpDz);
+                    wmpCx = wmpUx / utaup - wmpAx;
+                    wmpCy = wmpUy / utaup - wmpAy;
+                }
+                double px = wmputx, py = wmputy;   // the values the integrals below use
+                if (std::fabs(wmpAx) > 1.0 || std::fabs(wmpAy) > 1.0) {
+                    equil_flag = 1;
+                    utx = std::sqrt(std::fabs(equilutx));
+                    uty = std::sqrt(std::fabs(equiluty));
+                    wmpAx = 0.0;
+                    wmpAy = 0.0;
+                    wmpCx = 0.0;
+                    wmpCy = 0.0;
+                }
+                st(I, K, IW_AX) = wmpAx;
+                st(I, K, IW_AY) = wmpAy;
+                st(I, K, IW_CX) = wmpCx;
+                st(I, K, IW_CY) = wmpCy;
+                for (int q = 0; q < 5; q++) st(I, K, IW_INTEM + q) = st(I, K, IW_INTE + q);
+                st(I, K, IW_INTE + IW_LU) =
+                    0.5 * px * std::pow(wmpdeli, 2.0) / wmpdelv +
+                    utaup * wmpDz *
+                        (0.5 * wmpAx * (1.0 - std::pow(wmpdeli, 2.0) / std::pow(wmpDz, 2.0)) +
+                         wmpCx * (1.0 - wmpdeli / wmpDz) -
+                         1.0 / vonk * wmpUx / wmpVel * (1.0 - wmpdeli / wmpDz + wmpdeli / wmpDz * lg));
+                st(I, K, IW_INTE + IW_LV) =
+                    0.5 * py * std::pow(wmpdeli, 2.0) / wmpdelv +
+                    utaup * wmpDz *
+                        (0.5 * wmpAy * (1.0 - std::pow(wmpdeli, 2.0) / std::pow(wmpDz, 2.0)) +
+                         wmpCy * (1.0 - wmpdeli / wmpDz) -
+                         1.0 / vonk * wmpUy / wmpVel * (1.0 - wmpdeli / wmpDz + wmpdeli / wmpDz * lg));
+                st(I, K, IW_INTE + IW_LUV) =
+                    1.0 / 3.0 * px * py * std::pow(wmpdeli, 3.0) / std::pow(wmpdelv, 2.0) +
+                    std::pow(utaup, 2.0) * wmpDz *
+                        (-1.0 / vonk * (wmpAx * wmpUy / wmpVel + wmpAy * wmpUx / wmpVel) *
+                             (0.25 - 0.25 * std::pow(wmpdeli, 2.0) / std::pow(wmpDz, 2.0) +
+                              0.5 * std::pow(wmpdeli, 2.0) / wmpDz * lg) -
+                         1.0 / vonk * (wmpCx * wmpUy / wmpVel + wmpCy * wmpUx / wmpVel) *
+                             (1.0 - wmpdeli / wmpDz + wmpdeli / wmpDz * lg) -
+                         wmpUx * wmpUy / std::pow(wmpVel, 2.0) / std::pow(vonk, 2.0) *
+                             (wmpdeli / wmpDz - 2.0 + wmpdeli / wmpDz * std::pow(lg - 1.0, 2.0)) +
+                         1.0 / 3.0 * wmpAx * wmpAy * (1.0 - std::pow(wmpdeli, 3.0) / std::pow(wmpDz, 3.0)) +
+                         0.5 * (wmpAx * wmpCy + wmpAy * wmpCx) * (1.0 - std::pow(wmpdeli, 2.0) / std::pow(wmpDz, 2.0)) +
+                         wmpCx * wmpCy * (1.0 - wmpdeli / wmpDz));
+                auto inte_sq = [&](double pu, double A, double C, double Uc) {   // Eq. C20, x or y
+                    return 1.0 / 3.0 * std::pow(pu, 2.0) * std::pow(wmpdeli, 3.0) / std::pow(wmpdelv, 2.0) +
+                           std::pow(utaup, 2.0) * wmpDz *
+                               (-A * Uc / wmpVel / vonk * std::pow(wmpdeli, 2.0) / std::pow(wmpDz, 2.0) * lg +
+                                A * (C - 1.0 / 2.0 / vonk * Uc / wmpVel) * (1.0 - std::pow(wmpdeli, 2.0) / std::pow(wmpDz, 2.0)) +
+                                std::pow(A, 2.0) / 3.0 * (1.0 - std::pow(wmpdeli, 3.0) / std::pow(wmpDz, 3.0)) +
+                                std::pow(C - 1.0 / vonk * Uc / wmpVel, 2.0) -
+                                wmpdeli / wmpDz * std::pow(C - Uc / wmpVel / vonk + Uc / wmpVel / vonk * lg, 2.0) +
+                                1.0 / std::pow(vonk, 2.0) * std::pow(Uc, 2.0) / std::pow(wmpVel, 2.0) * (1.0 - wmpdeli / wmpDz));
+                };
+                st(I, K, IW_INTE + IW_LUU) = inte_sq(px, wmpAx, wmpCx, wmpUx);
+                st(I, K, IW_INTE + IW_LVV) = inte_sq(py, wmpAy, wmpCy, wmpUy);
+                double dTx, dTy;
+                if (wmpdeli < wmpDz) {
+                    dTx = utaup / wmpDz * (wmpAx + 1.0 / vonk * wmpUx / wmpVel);
+                    dTy = utaup / wmpDz * (wmpAy + 1.0 / vonk * wmpUy / wmpVel);
+                } else {
+                    dTx = px / wmpdelv;
+                    dTy = py / wmpdelv;
+                }
+                const double dBx = px / wmpdelv, dBy = py / wmpdelv;
+                st(I, K, IW_DTX) = dTx;
+                st(I, K, IW_DTY) = dTy;
+                st(I, K, IW_DBX) = dBx;
+                st(I, K, IW_DBY) = dBy;
+                const double dVelzT = std::fabs(wmpUx / wmpVel * dTx + wmpUy / wmpVel * dTy);
+                if (wmpdeli < wmpDz) {
+                    st(I, K, IW_DIFFX) = (reinv + std::pow(vonk * wmpDz, 2.0) * dVelzT) * dTx - reinv * dBx;
+                    st(I, K, IW_DIFFY) = (reinv + std::pow(vonk * wmpDz, 2.0) * dVelzT) * dTy - reinv * dBy;
+                } else {
+                    st(I, K, IW_DIFFX) = 0.0;
+                    st(I, K, IW_DIFFY) = 0.0;
+                }
+                if (equil_flag == 1) {
+                    st(I, K, IW_TAUWX) = equilutx;
+                    st(I, K, IW_TAUWY) = equiluty;
+                } else if (wmpdeli < wmpDz) {
+                    st(I, K, IW_TAUWX) = std::pow(px, 2.0);
+                    st(I, K, IW_TAUWY) = std::pow(py, 2.0);
+                } else {
+                    st(I, K, IW_TAUWX) = reinv * wmpUx / wmpDz;
+                    st(I, K, IW_TAUWY) = reinv * wmpUy / wmpDz;
+                }
+                st(I, K, IW_FUS) = st(I, K, IW_FUS) * (1.0 - st(I, K, IW_TR)) + utaup * st(I, K, IW_TR);
+                st(I, K, IW_TR) = wm_dt / (st(I, K, IW_DZ) / st(I, K, IW_FUS) / vonk);
+                if (st(I, K, IW_TR) > 1.0) st(I, K, IW_TR) = 1.0;
+            }
+    }
+    // every step: the stresses and WSM(1) (3541-3556, 3466-3479)
+    double WSM1 = 0.0;
+    for (int K = 1; K <= N3M; K++)
+        for (int I = 1; I <= N1M; I++) {
+            g.TAUW[g.itw(I, K, 1)] = st(I, K, IW_TAUWX);
+            g.TAUB[g.itw(I, K, 1)] = st(I, K, IW_TAUWY);
+            WSM1 = WSM1 + std::sqrt(std::pow(g.TAUW[g.itw(I, K, 1)], 2.) + std::pow(g.TAUB[g.itw(I, K, 1)], 2.));
+        }
+    g.WSM[0] = WSM1 / (double)(N1M * N3M);
+    g.TAOW = g.WSM[0];
+    return status;
+}
+
+// The wall model WALL_MODEL dispatches to (compact3d.f:1982-2011) for WMODEL = 1..5.
+int wallmodel(Orc &g, const double *U, const double *P = nullptr, int NTIME = 1, double DT = 0.0, double PRESG = 0.0,
+              double PRESG3 = 0.0) {
     if (g.WMODEL == 4) return wallmodel_werner(g, U);
     if (g.WMODEL == 3 || g.WMODEL == 5) return wallmodel_shifted(g, U);
+    if (g.WMODEL == 2) return P ? wallmodel_iwmles(g, U, P, NTIME, DT, PRESG, PRESG3) : C3D_EINVAL;
     return wallmodel_instant(g, U);
 }
 
@@ -2595,6 +2899,15 @@ void orc_filter(void *h, int four, double *F, int n) {
     std::copy(v.begin(), v.end(), F);
 }
 
+// WALLMODEL_IWMLES_SMOOTH: the driver's CFLMAX (its initial filter time scale) and the
+// per-point state (IW_NS slots of N1M N3M values, I fastest)
+void orc_set_cflmax(void *h, double cflmax) { ((Orc *)h)->CFLMAX = cflmax; }
+int orc_iwm_slots() { return IW_NS; }
+void orc_get_iwm(void *h, double *out) {
+    Orc &g = *(Orc *)h;
+    std::copy(g.IWM.begin(), g.IWM.end(), out);
+}
+
 // SGSSD's BETA(1:N2M) of the last SGS evaluation
 void orc_get_beta(void *h, double *beta) {
     Orc &g = *(Orc *)h;
@@ -2704,7 +3017,7 @@ int orc_getup(void *h, double *U, double *P, double *HH, double *SGSVIS, int NTI
               double *PRESG, double *PRESG3) {
     Orc &g = *(Orc *)h;
     (void)NTIME;
-    if (g.FILES < 0 || g.FILES > 3 || g.WMODEL < 0 || g.WMODEL == 2 || g.WMODEL > 5) return C3D_EINVAL;
+    if (g.FILES < 0 || g.FILES > 3 || g.WMODEL < 0 || g.WMODEL > 5) return C3D_EINVAL;
     if (g.WMODEL == 4 && g.N3M > g.N1M) return C3D_EINVAL;   // WERNER indexes INDX(N1M) with K
     const int N1 = g.N1, N2 = g.N2, N3 = g.N3;
     double *UH = g.UH.data(), *HH2 = g.HH2.data();
@@ -2748,7 +3061,7 @@ int orc_getup(void *h, double *U, double *P, double *HH, double *SGSVIS, int NTI
             g.IFWALL = 0;
             wallss_common(g, U, g.WSM);
         } else {
-            status = wallmodel(g, U);
+            status = wallmodel(g, U, P, NTIME, DT, *PRESG, *PRESG3);
             g.IFWALL = 1;
         }
     }

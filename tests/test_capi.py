@@ -65,7 +65,7 @@ def test_create_rejects_null_metrics(L):
 
 def test_create_rejects_bad_precision_and_models(L):
     g, _ = make_grid("small32")
-    for field, val in (("precision", 7), ("files", 4), ("re", -1.0), ("wmodel", 2), ("wmodel", 6), ("wmodel", -1)):
+    for field, val in (("precision", 7), ("files", 4), ("re", -1.0), ("wmodel", 6), ("wmodel", -1)):
         s = g.struct()
         setattr(s, field, val)
         h = ctypes.c_void_p()
@@ -109,3 +109,12 @@ def test_shifted_wall_models_check_the_y_faces(L):
     h = ctypes.c_void_p()
     assert L.c3d_create(ctypes.byref(s), ctypes.byref(h)) == -1
     assert b"H(1)" in L.c3d_last_error()
+
+
+def test_iwmles_rough_refused(L):
+    """Y(0) = Y0 != 0 with WMODEL 2 selects WALLMODEL_IWMLES_ROUGH, which is not built."""
+    g, _ = make_grid("les32cs", wmodel=2, y0=0.01)
+    s = g.struct()
+    h = ctypes.c_void_p()
+    assert L.c3d_create(ctypes.byref(s), ctypes.byref(h)) == -1
+    assert b"IWMLES_ROUGH" in L.c3d_last_error()

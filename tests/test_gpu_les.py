@@ -152,3 +152,35 @@ def test_les_wall_model_iteration_cap(libc3d, oracle_mod):
     ch.step(3, dt, pg, pg3)
     Ug, _, _ = ch.download()
     assert np.isfinite(Ug).all()
+
+
+@pytest.mark.parametrize("name,over", [("les32cs", dict(wmodel=2)), ("les32dy", dict(wmodel=2, n2m=64))])
+def test_iwmles_steps_fp64(libc3d, oracle_mod, name, over):
+    """WALLMODEL_IWMLES_SMOOTH (WMODEL 2) from NTIME = 1 on both sides for 12 steps (two
+    model updates): wall stresses and WSM(1) within 1e-8 after every step (the Newton
+    Jacobian differences the residual over 1e-9, which amplifies last-bit differences of
+    pow and log), the field within 1e-9 at the end."""
+    g, dt = make_grid(name, **over)
+    orc = oracle_mod.Oracle(g)
+    orc.set_cflmax(0.5)
+    U, P, HH = ic.loglaw(g, RETAU)
+    orc.project(U)
+    S = g.zeros_s()
+    ch = libc3d.Channel(g, C3D_FP64)
+    ch.upload(U, P, HH)
+    ch.set_cflmax(0.5)
+    pg = pg3 = pgg = pg3g = 0.0
+    isl = (slice(1, g.n1m + 1), slice(1, g.n3m + 1), 0)
+    for n in range(1, 13):
+        pg, pg3 = orc.getup(U, P, HH, n, dt, pg, pg3, S)
+        pgg, pg3g = ch.step(n, dt, pgg, pg3g)
+        tw, tb, wsm = orc.get_wall()
+        twg, tbg = ch.download_wall()
+        scale = max(np.abs(tw[isl]).max(), 1e-300)
+        assert np.abs(twg[isl] - tw[isl]).max() <= 1e-8 * scale, n
+        assert np.abs(tbg[isl] - tb[isl]).max() <= 1e-8 * max(scale, np.abs(tb[isl]).max()), n
+        assert ch.get_wsm()[0] == pytest.approx(wsm[0], rel=1e-8, abs=1e-300), n
+    Ug, Pg, Hg = ch.download()
+    a, b = interior(g, Ug, Pg, Hg), interior(g, U, P, HH)
+    for f in ("u", "v", "w"):
+        assert rel(a[f], b[f]) < 1e-9, (f, rel(a[f], b[f]))

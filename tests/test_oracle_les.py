@@ -482,3 +482,190 @@ def test_sgssd_step_runs_and_conserves(oracle_mod):
     assert o.divcheck(U) < 1e-12
     assert o.chkmf(U)[0] == pytest.approx(f0, rel=1e-10)
     assert np.all((o.get_beta() >= 0) & (o.get_beta() < 2))
+
+
+# --- WALLMODEL_IWMLES_SMOOTH (WMODEL 2): a numpy restatement of one model update ---
+_IW = {n: q for q, n in enumerate(
+    "UTX UTY TAUWX TAUWY FTX FTY FTMX FTMY FP I0 I1 I2 I3 I4 M0 M1 M2 M3 M4 DIFFX DIFFY LHSX LHSY FUS TR DZ "
+    "AX AY CX CY UNSX UNSY DELI DELV DTX DTY DBX DBY CONVX CONVY PRSX PRSY".split())}
+
+
+def _iwm_slv(lhsx, lhsy, Ux, Uy, Dz, utx, uty, re):
+    vonk, reinv = 0.4, 1.0 / re
+    us = (utx ** 4 + uty ** 4) ** 0.25
+    delv, deli = reinv / us, min(11.0 * reinv / us, Dz)
+    Vel = math.sqrt(Ux ** 2 + Uy ** 2)
+    lg = math.log(deli / Dz)
+    Ax = (Ux / us + Ux / Vel / vonk * lg - deli / delv * utx / us) / (1 - deli / Dz)
+    Ay = (Uy / us + Uy / Vel / vonk * lg - deli / delv * uty / us) / (1 - deli / Dz)
+    Cx, Cy = Ux / us - Ax, Uy / us - Ay
+    Lu = 0.5 * utx * deli ** 2 / delv + us * Dz * (0.5 * Ax * (1 - deli ** 2 / Dz ** 2) + Cx * (1 - deli / Dz)
+                                                   - Ux / Vel / vonk * (1 - deli / Dz + deli / Dz * lg))
+    Lv = 0.5 * uty * deli ** 2 / delv + us * Dz * (0.5 * Ay * (1 - deli ** 2 / Dz ** 2) + Cy * (1 - deli / Dz)
+                                                   - Uy / Vel / vonk * (1 - deli / Dz + deli / Dz * lg))
+    return Lu + lhsx, Lv + lhsy
+
+
+def _iwm_loglaw(U_ave, dz, re):
+    u1, u2, lam = 1.0, 1e-6, 1.0
+    while abs(u2 - u1) > 1e-6:
+        u1 = u2
+        f1 = U_ave / u1 - math.log(u1 * dz * re) / 0.4 - 5.0
+        f2 = -U_ave / u1 ** 2 - 1.0 / 0.4 / u1
+        u2 = u1 - lam * f1 / f2
+        if abs(U_ave / u2 - math.log(u2 * dz * re) / 0.4 - 5.0) > abs(f1):
+            lam *= 0.5
+    return u1
+
+
+def _iwm_update(g, st, U, P, wm_dt, presg, presg3):
+    """One update of iwm_calc_lhs_smooth and iwm_calc_wallstress_smooth
+    (compact3d.f:3718-4279); st is (slots, N3M, N1M), modified in place."""
+    n1, n3, re, vonk = g.n1m, g.n3m, g.re, 0.4
+    reinv = 1.0 / re
+    S = {n: st[q] for n, q in _IW.items()}
+    u_inst = U[1:n1 + 1, 3, 1:n3 + 1, 0].T
+    v_inst = U[1:n1 + 1, 3, 1:n3 + 1, 2].T
+    p_inst = P[:n1, 0, :n3].T
+    p_inst = p_inst - p_inst.sum() / n1 / n3
+    S["FTMX"][:] = S["FTX"]
+    S["FTMY"][:] = S["FTY"]
+    tR = S["TR"].copy()
+    S["FTX"][:] = S["FTX"] * (1 - tR) + u_inst * tR
+    S["FTY"][:] = S["FTY"] * (1 - tR) + v_inst * tR
+    S["FP"][:] = S["FP"] * (1 - tR) + p_inst * tR
+    dx1, dx3 = g.arrays["dx1"], g.arrays["dx3"]
+    dxf = lambda a: (np.roll(a, -1, 1) - np.roll(a, 1, 1)) * dx1 / 2.0
+    dzf = lambda a: (np.roll(a, -1, 0) - np.roll(a, 1, 0)) * dx3 / 2.0
+    ux, vy = dxf(S["I0"]), dzf(S["I2"])
+    S["CONVX"][:] = dxf(S["I1"]) + dzf(S["I4"]) - S["FTMX"] * (ux + vy)
+    S["CONVY"][:] = dxf(S["I4"]) + dzf(S["I3"]) - S["FTMY"] * (ux + vy)
+    S["PRSX"][:] = dxf(S["FP"]) * S["DZ"] + presg * S["DZ"]
+    S["PRSY"][:] = dzf(S["FP"]) * S["DZ"] + presg3 * S["DZ"]
+    S["LHSX"][:] = -S["I0"] + wm_dt * (S["CONVX"] + S["PRSX"] - S["DIFFX"])
+    S["LHSY"][:] = -S["I2"] + wm_dt * (S["CONVY"] + S["PRSY"] - S["DIFFY"])
+    deltap = g.arrays["dy"][1] + g.arrays["dy"][2] + g.arrays["dy"][3] / 2.0
+    eqx = eqy = 0.0
+    for i in range(n1):
+        for k in range(n3):
+            lhsx, lhsy, Ux, Uy, Dz = S["LHSX"][k, i], S["LHSY"][k, i], S["FTX"][k, i], S["FTY"][k, i], S["DZ"][k, i]
+            utx, uty = S["UTX"][k, i], S["UTY"][k, i]
+            fx, fy = _iwm_slv(lhsx, lhsy, Ux, Uy, Dz, utx, uty, re)
+            it, eq = 0, 0
+            while max(abs(fx), abs(fy)) > 1e-6:
+                e = 1e-9
+                fxp, fyp = _iwm_slv(lhsx, lhsy, Ux, Uy, Dz, utx + e, uty, re)
+                a11, a21 = (fxp - fx) / e, (fyp - fy) / e
+                fxp, fyp = _iwm_slv(lhsx, lhsy, Ux, Uy, Dz, utx, uty + e, re)
+                a12, a22 = (fxp - fx) / e, (fyp - fy) / e
+                det = a11 * a22 - a12 * a21
+                utx, uty = utx - (a22 * fx - a12 * fy) / det, uty - (-a21 * fx + a11 * fy) / det
+                fx, fy = _iwm_slv(lhsx, lhsy, Ux, Uy, Dz, utx, uty, re)
+                it += 1
+                if it > 1500:
+                    eq = 1
+                    break
+            if utx - 1.0 == utx or uty - 1.0 == uty:
+                eq = 1
+            if eq:
+                U_ave = math.sqrt(Ux ** 2 + Uy ** 2)
+                t1 = _iwm_loglaw(U_ave, deltap, re) ** 2
+                eqx, eqy = t1 * Ux / U_ave, t1 * Uy / U_ave
+                utx, uty = math.sqrt(abs(eqx)), math.sqrt(abs(eqy))
+            px, py = utx, uty
+            ut = (px ** 4 + py ** 4) ** 0.25
+            delv, deli = reinv / ut, min(11 * reinv / ut, Dz)
+            Vel = math.sqrt(Ux ** 2 + Uy ** 2)
+            lg = math.log(deli / Dz)
+            Ax = Ay = Cx = Cy = 0.0
+            if not eq:
+                Ax = (Ux / ut + Ux / Vel / vonk * lg - deli / delv * px / ut) / (1 - deli / Dz)
+                Ay = (Uy / ut + Uy / Vel / vonk * lg - deli / delv * py / ut) / (1 - deli / Dz)
+                Cx, Cy = Ux / ut - Ax, Uy / ut - Ay
+            if abs(Ax) > 1.0 or abs(Ay) > 1.0:
+                eq = 1
+                utx, uty = math.sqrt(abs(eqx)), math.sqrt(abs(eqy))
+                Ax = Ay = Cx = Cy = 0.0
+            S["UTX"][k, i], S["UTY"][k, i] = utx, uty
+            r1, r2, r3 = deli / Dz, deli ** 2 / Dz ** 2, deli ** 3 / Dz ** 3
+            lu = lambda pu, A, C, Uc: 0.5 * pu * deli ** 2 / delv + ut * Dz * (
+                0.5 * A * (1 - r2) + C * (1 - r1) - Uc / Vel / vonk * (1 - r1 + r1 * lg))
+            luu = lambda pu, A, C, Uc: pu ** 2 * deli ** 3 / delv ** 2 / 3 + ut ** 2 * Dz * (
+                -A * Uc / Vel / vonk * r2 * lg + A * (C - Uc / Vel / 2 / vonk) * (1 - r2) + A ** 2 / 3 * (1 - r3)
+                + (C - Uc / Vel / vonk) ** 2 - r1 * (C - Uc / Vel / vonk + Uc / Vel / vonk * lg) ** 2
+                + Uc ** 2 / Vel ** 2 / vonk ** 2 * (1 - r1))
+            S["M0"][k, i], S["M1"][k, i], S["M2"][k, i], S["M3"][k, i], S["M4"][k, i] = (
+                S["I0"][k, i], S["I1"][k, i], S["I2"][k, i], S["I3"][k, i], S["I4"][k, i])
+            S["I0"][k, i] = lu(px, Ax, Cx, Ux)
+            S["I2"][k, i] = lu(py, Ay, Cy, Uy)
+            S["I1"][k, i] = luu(px, Ax, Cx, Ux)
+            S["I3"][k, i] = luu(py, Ay, Cy, Uy)
+            S["I4"][k, i] = px * py * deli ** 3 / delv ** 2 / 3 + ut ** 2 * Dz * (
+                -(Ax * Uy / Vel + Ay * Ux / Vel) / vonk * (0.25 - 0.25 * r2 + 0.5 * deli ** 2 / Dz * lg)
+                - (Cx * Uy / Vel + Cy * Ux / Vel) / vonk * (1 - r1 + r1 * lg)
+                - Ux * Uy / Vel ** 2 / vonk ** 2 * (r1 - 2 + r1 * (lg - 1) ** 2)
+                + Ax * Ay / 3 * (1 - r3) + 0.5 * (Ax * Cy + Ay * Cx) * (1 - r2) + Cx * Cy * (1 - r1))
+            if deli < Dz:
+                dTx, dTy = ut / Dz * (Ax + Ux / Vel / vonk), ut / Dz * (Ay + Uy / Vel / vonk)
+            else:
+                dTx, dTy = px / delv, py / delv
+            dBx, dBy = px / delv, py / delv
+            dV = abs(Ux / Vel * dTx + Uy / Vel * dTy)
+            if deli < Dz:
+                S["DIFFX"][k, i] = (reinv + (vonk * Dz) ** 2 * dV) * dTx - reinv * dBx
+                S["DIFFY"][k, i] = (reinv + (vonk * Dz) ** 2 * dV) * dTy - reinv * dBy
+            else:
+                S["DIFFX"][k, i] = S["DIFFY"][k, i] = 0.0
+            if eq:
+                S["TAUWX"][k, i], S["TAUWY"][k, i] = eqx, eqy
+            elif deli < Dz:
+                S["TAUWX"][k, i], S["TAUWY"][k, i] = px ** 2, py ** 2
+            else:
+                S["TAUWX"][k, i], S["TAUWY"][k, i] = reinv * Ux / Dz, reinv * Uy / Dz
+            S["FUS"][k, i] = S["FUS"][k, i] * (1 - S["TR"][k, i]) + ut * S["TR"][k, i]
+            S["TR"][k, i] = min(wm_dt / (Dz / S["FUS"][k, i] / vonk), 1.0)
+
+
+@pytest.mark.parametrize("n2m", [16, 64])
+def test_iwmles_update_matches_numpy_restatement(oracle_mod, n2m):
+    """WALLMODEL_IWMLES_SMOOTH: the state after the first two model updates (steps 5 and
+    10) against a numpy restatement applied to the state, field and pressure the oracle
+    held before each update; steps 1-4 impose the initial u_tau^2 (from the log law on the
+    plane-mean u of plane 3), the spanwise stress in TAUB, and WSM(1) is the mean stress."""
+    g, dt = _grid("les32cs", wmodel=2, n2m=n2m)
+    o = oracle_mod.Oracle(g)
+    o.set_cflmax(0.5)
+    U, P, HH = ic.loglaw(g, 2000.0)
+    o.project(U)
+    S = g.zeros_s()
+    pg = pg3 = 0.0
+    dzp = g.arrays["dy"][1] + g.arrays["dy"][2] + g.arrays["dy"][3] / 2.0
+    uinit = U[1:g.n1m + 1, 3, 1:g.n3m + 1, 0].mean()
+    us0 = _iwm_loglaw(uinit, dzp, g.re)
+    for n in range(1, 11):
+        if n % 5 == 0:
+            st = o.get_iwm().copy()
+            U0, P0 = U.copy(), P.copy()
+            pgs, pg3s = pg, pg3
+        pg, pg3 = o.getup(U, P, HH, n, dt, pg, pg3, S)
+        tw, tb, wsm = o.get_wall()
+        if n < 5:
+            np.testing.assert_allclose(tw[1:g.n1m + 1, 1:g.n3m + 1, 0], us0 ** 2, rtol=1e-12)
+            assert np.abs(tb[1:g.n1m + 1, 1:g.n3m + 1, 0]).max() == 0.0
+            assert wsm[0] == pytest.approx(us0 ** 2, rel=1e-12)
+        if n % 5 == 0:
+            # the reference's stale fallback leaves u_tau = 0 at points, after which its
+            # formulas divide by zero: the restatement follows them through inf and NaN
+            with np.errstate(divide="ignore", invalid="ignore"):
+                _iwm_update(g, st, U0, P0, 5 * dt, pgs, pg3s)
+            got = o.get_iwm()
+            for name in ("UTX", "UTY", "TAUWX", "TAUWY", "FTX", "FTY", "FP", "I0", "I1", "I2", "I3", "I4", "DIFFX",
+                         "DIFFY", "LHSX", "LHSY", "FUS", "TR"):
+                q = _IW[name]
+                np.testing.assert_allclose(got[q], st[q], rtol=1e-9, atol=1e-13 * max(1.0, np.abs(st[q]).max()),
+                                           err_msg=name)
+            np.testing.assert_allclose(tw[1:g.n1m + 1, 1:g.n3m + 1, 0], got[_IW["TAUWX"]].T, rtol=0, atol=0)
+            np.testing.assert_allclose(tb[1:g.n1m + 1, 1:g.n3m + 1, 0], got[_IW["TAUWY"]].T, rtol=0, atol=0)
+            assert wsm[0] == pytest.approx(np.mean(np.sqrt(got[_IW["TAUWX"]] ** 2 + got[_IW["TAUWY"]] ** 2)),
+                                           rel=1e-12, abs=1e-300)
+    assert np.isfinite(U).all()
