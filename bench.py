@@ -523,6 +523,21 @@ def run_next(args, D: Dist, g, dt, U0, P0, HH0):
     out["plane_spectra"] = dict(ms_per_call=ms_sp, tables="XSPCTR, ZSPCTR, RXX, RZZ, RXY (3 components)",
                                 note="FP64 FFTs of every x and z line of the three components, the plane statistics "
                                      "for VM/VRMS, host-timed call incl. copy-out")
+    # particles: one step of 1M particles in the channel (host arrays in and out)
+    rng = np.random.default_rng(5)
+    npar = 1_000_000
+    Dp = 0.0002 / 0.05
+    par = np.column_stack([rng.uniform(0, g.alx, npar), rng.uniform(0.5 * Dp, 2.0 - 0.5 * Dp, npar),
+                           rng.uniform(0, g.alz, npar), rng.normal(0.5, 0.2, npar), rng.normal(0, 0.05, npar),
+                           rng.normal(0, 0.05, npar)])
+    ch.particles_advance(par, dt)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        ch.particles_advance(par, dt)
+    ms_p = (time.perf_counter() - t0) / 3 * 1e3
+    out["particles"] = dict(particles=npar, ms_per_step=ms_p, particles_per_s=npar / ms_p * 1e3,
+                            note="CALC_UX_4RK + BC_PAR on the device (4 interpolations of u, v, w per particle, FP64), "
+                                 "host arrays copied in and out inside the timing")
     d = tempfile.mkdtemp(prefix="c3d_ckpt_")
     try:
         path = os.path.join(d, "ckpt.bin")

@@ -474,6 +474,20 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
         cudaMemset(*q, 0, nf * rs);
     }
     if (cudaMalloc(&ch->spec, nmodes * g.n2m * 2 * rs) != cudaSuccess) return fail(C3D_ENOMEM);
+    {   // MESH02's Y, YC and face / centre tables (the shifted wall models and the particles)
+        const size_t ny = (size_t)g.n2 + 1;
+        if (dalloc(&ch->wshift, c3d::wall_shift_doubles(g))) return fail(C3D_ENOMEM);
+        std::vector<double> yy(2 * ny, 0.0);
+        for (size_t j = 0; j < ny; ++j) yy[j] = gr->y[j];
+        yy[ny] = gr->y[0];
+        for (int j = 1; j <= g.n2m; ++j) yy[ny + j] = 0.5 * (gr->y[j + 1] + gr->y[j]);
+        yy[ny + g.n2] = gr->y[g.n2];
+        cudaMemcpy(ch->wshift, yy.data(), 2 * ny * 8, cudaMemcpyHostToDevice);
+        c3d::launch_wall_shift_init(ch);
+        ch->y_increasing = 1;
+        for (int j = 1; j <= g.n2m; ++j)
+            if (!(gr->y[j + 1] > gr->y[j])) ch->y_increasing = 0;
+    }
     // wall stresses (any FILES/WMODEL: c3d_upload_wall may set them) and the LES fields
     ch->files = gr->files;
     ch->wmodel = gr->wmodel;
@@ -513,15 +527,6 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
             ch->iwm_dzp = gr->dy[1] + gr->dy[2] + gr->dy[3] / 2.0;
         }
         if (gr->wmodel == 3 || gr->wmodel == 5) {
-            const size_t ny = (size_t)g.n2 + 1;
-            if (dalloc(&ch->wshift, c3d::wall_shift_doubles(g))) return fail(C3D_ENOMEM);
-            std::vector<double> yy(2 * ny, 0.0);
-            for (size_t j = 0; j < ny; ++j) yy[j] = gr->y[j];
-            yy[ny] = gr->y[0];
-            for (int j = 1; j <= g.n2m; ++j) yy[ny + j] = 0.5 * (gr->y[j + 1] + gr->y[j]);
-            yy[ny + g.n2] = gr->y[g.n2];
-            cudaMemcpy(ch->wshift, yy.data(), 2 * ny * 8, cudaMemcpyHostToDevice);
-            c3d::launch_wall_shift_init(ch);
             ch->wzs = marusic_plane(gr->y, g.n2m);
             ch->wtan16 = std::tan(16.0 * std::acos(-1.0) / 180);
         }
@@ -1315,6 +1320,60 @@ int c3d_corr3d(c3d_channel *ch, double *out) {
     if (!rc && cudaStreamSynchronize(ch->stream) != cudaSuccess) rc = C3D_ECUDA;
     if (rc) set_error("3-D correlation");
     cudaFree(buf);
+    return rc;
+}
+
+static int particles_common(c3d_channel *ch, int n, const double *par, double diam, double dens, double hhh) {
+    if (!ch || n < 0 || (n > 0 && !par)) { set_error("null argument"); return C3D_EINVAL; }
+    if (!ch->have_state) { set_error("c3d_upload must be called before the particle calls"); return C3D_ESTATE; }
+    if (!(diam > 0) || !(dens > 0) || !(hhh > 0)) { set_error("DIAM, DENS and HHH must be positive"); return C3D_EINVAL; }
+    if (!ch->y_increasing) { set_error("the particle interpolation searches the Y faces: Y(1:N2) must increase"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    return 0;
+}
+
+int c3d_particles_advance(c3d_channel *ch, int n, double *par, double diam, double dens, double hhh, double dt,
+                          int *impact) {
+    int rc = particles_common(ch, n, par, diam, dens, hhh);
+    if (rc || n == 0) return rc;
+    if (!(dt > 0) || !isfinite(dt)) { set_error("dt must be positive and finite"); return C3D_EINVAL; }
+    double *dp = nullptr;
+    int *di = nullptr;
+    if (dalloc(&dp, 6 * (size_t)n)) return C3D_ENOMEM;
+    if (dalloc(&di, (size_t)n)) { cudaFree(dp); return C3D_ENOMEM; }
+    rc = cudaMemcpyAsync(dp, par, 6 * (size_t)n * 8, cudaMemcpyHostToDevice, ch->stream) == cudaSuccess ? 0 : C3D_ECUDA;
+    if (!rc) rc = launch_particles(ch, dp, n, diam, dens, hhh, dt, di, nullptr, nullptr, nullptr);
+    if (!rc && cudaMemcpyAsync(par, dp, 6 * (size_t)n * 8, cudaMemcpyDeviceToHost, ch->stream) != cudaSuccess) rc = C3D_ECUDA;
+    if (!rc && impact && cudaMemcpyAsync(impact, di, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, ch->stream) != cudaSuccess)
+        rc = C3D_ECUDA;
+    if (!rc && cudaStreamSynchronize(ch->stream) != cudaSuccess) rc = C3D_ECUDA;
+    if (rc) set_error("particle step");
+    cudaFree(dp);
+    cudaFree(di);
+    return rc;
+}
+
+int c3d_particles_source(c3d_channel *ch, int n, const double *par, double diam, double dens, double hhh,
+                         double *ruh1, double *ruh2, double *ruh3) {
+    int rc = particles_common(ch, n, par, diam, dens, hhh);
+    if (rc) return rc;
+    if (!ruh1 || !ruh2 || !ruh3) { set_error("null argument"); return C3D_EINVAL; }
+    const Geo &g = ch->g;
+    const size_t ns = (size_t)(g.n1m + 2) * (g.n2 + 1) * (g.n3m + 2);
+    double *buf = nullptr, *dp = nullptr;
+    if (dalloc(&buf, 3 * ns)) return C3D_ENOMEM;
+    if (n > 0 && dalloc(&dp, 6 * (size_t)n)) { cudaFree(buf); return C3D_ENOMEM; }
+    rc = cudaMemsetAsync(buf, 0, 3 * ns * 8, ch->stream) == cudaSuccess ? 0 : C3D_ECUDA;
+    if (!rc && n > 0)
+        rc = cudaMemcpyAsync(dp, par, 6 * (size_t)n * 8, cudaMemcpyHostToDevice, ch->stream) == cudaSuccess ? 0 : C3D_ECUDA;
+    if (!rc && n > 0) rc = launch_particles(ch, dp, n, diam, dens, hhh, 0.0, nullptr, buf, buf + ns, buf + 2 * ns);
+    double *outs[3] = {ruh1, ruh2, ruh3};
+    for (int q = 0; q < 3 && !rc; ++q)
+        if (cudaMemcpyAsync(outs[q], buf + q * ns, ns * 8, cudaMemcpyDeviceToHost, ch->stream) != cudaSuccess) rc = C3D_ECUDA;
+    if (!rc && cudaStreamSynchronize(ch->stream) != cudaSuccess) rc = C3D_ECUDA;
+    if (rc) set_error("particle source");
+    cudaFree(buf);
+    if (dp) cudaFree(dp);
     return rc;
 }
 

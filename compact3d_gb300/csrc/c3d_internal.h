@@ -187,6 +187,7 @@ struct c3d_channel {
     cudaEvent_t wfork = nullptr, wjoin = nullptr;
     int wjoin_pending = 0;
     int wzs = 0;
+    int y_increasing = 0;      // Y(1:N2) increases (the particle and shifted-model searches)
     double wtan16 = 0.0;
     double *stats = nullptr;  // plane statistics table and partial sums (allocated on first use)
     cudaStream_t cs = nullptr;          // copy stream of the DMA transfers
@@ -306,6 +307,9 @@ int launch_quadrants(c3d_channel *ch, const double *vmp, double *out, double *pa
 // (c1: (N1M/2 + 1) N3M complex scratch, out: N1M N3M)
 int launch_corr3d(c3d_channel *ch, const double *st, double *out);
 int launch_wall_spectrum(c3d_channel *ch, double utau, double2 *c1, double *out);
+// the particle step (r1 == nullptr) or SOURCE_PAR's terms into r1..r3 for n particles
+int launch_particles(c3d_channel *ch, double *par, int n, double diam, double dens, double hhh, double dt, int *impact,
+                     double *r1, double *r2, double *r3);
 void launch_wall_shift_init(c3d_channel *ch);
 void prof_begin(c3d_channel *ch);
 int prof_collect(c3d_channel *ch);

@@ -844,7 +844,7 @@ __device__ double ws_interp(const StepArgs<R> &a, const WsMesh &m, double XP, do
     }
     const typename StepArgs<R>::S *F = C == 1 ? a.u : (C == 2 ? a.v : a.w);
     auto f = [&](int I, int J, int K) {
-        return C == 2 && J == 1 ? m.V1[(K - 1) * n1 + (I - 1)] : ST::dbl(F[fidx(g, I - 1, J, K - 1)]);
+        return C == 2 && J == 1 && m.V1 ? m.V1[(K - 1) * n1 + (I - 1)] : ST::dbl(F[fidx(g, I - 1, J, K - 1)]);
     };
     const double PHA = f(IUM, JUM, KUM), PHB = f(IUP, JUM, KUM), PHC = f(IUP, JUP, KUM), PHD = f(IUM, JUP, KUM);
     const double PHE = f(IUM, JUM, KUP), PHF = f(IUP, JUM, KUP), PHG = f(IUP, JUP, KUP), PHH = f(IUM, JUP, KUP);
@@ -1537,5 +1537,177 @@ int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *n
 
 template int launch_les<double>(c3d_channel *, StepArgs<double> &, LesArgs<double> &, int, int *);
 template int launch_les<float>(c3d_channel *, StepArgs<float> &, LesArgs<float> &, int, int *);
+
+}  // namespace c3d
+
+namespace c3d {
+
+// ---------------------------------------------------------------------------------
+// Lagrangian particles (compact3d.f:11882-12470, 2029-2075), FP64, one thread per
+// particle: CALC_UX_4RK's step with FORCE_PAR's drag and gravity and INDEX_IJK /
+// INTERPOLAT of the three components at every stage, the periodic shifts by DIAM_P and
+// the explicit Euler step from the start when a stage leaves the channel; BC_PAR's
+// periodic shifts and top-wall reflection, a bottom-wall impact flagged (the reference's
+// SPLASH draws from RAN2 seeded by CPU_TIME); SOURCE_PAR's two-way coupling terms,
+// deposited with FP64 atomics.  The reference's time loop has GET_PAR and SOURCE_PAR
+// commented out (compact3d.f:128, 1026); these run when the driver calls them.
+// ---------------------------------------------------------------------------------
+struct ParC {
+    double D, TAU, MASS, HHH;
+};
+
+// INDEX_IJK with its nudges (the coordinates change, as the reference's arguments do)
+__device__ __forceinline__ bool ws_locate(const Geo &g, const WsMesh &m, double &XP, double &YP, double &ZP, int &IP,
+                                          int &JP, int &KP) {
+    if (XP < m.XC[1]) XP = nudge_up(XP);
+    if (XP > m.XC[g.n1m]) XP = nudge_dn(XP);
+    if (YP < m.YC[1]) YP = nudge_up(YP);
+    if (YP > m.YC[g.n2m]) YP = nudge_dn(YP);
+    if (ZP < m.ZC[1]) ZP = nudge_up(ZP);
+    if (ZP > m.ZC[g.n3m]) ZP = nudge_dn(ZP);
+    IP = ws_cell(XP, m.XG, g.n1m, m.rx);
+    JP = ws_ycell(YP, m.Y, g.n2m);
+    KP = ws_cell(ZP, m.ZG, g.n3m, m.rz);
+    return IP >= 0 && JP >= 0 && KP >= 0;
+}
+
+template <typename R>
+__device__ void par_fluid(const StepArgs<R> &a, const WsMesh &m, double XP, double YP, double ZP, double &UF,
+                          double &VF, double &WF) {
+    int IP, JP, KP;
+    if (!ws_locate(a.g, m, XP, YP, ZP, IP, JP, KP)) {
+        UF = VF = WF = __longlong_as_double(0x7ff8000000000000LL);
+        return;
+    }
+    UF = ws_interp(a, m, XP, YP, ZP, IP, JP, KP, 1);
+    VF = ws_interp(a, m, XP, YP, ZP, IP, JP, KP, 2);
+    WF = ws_interp(a, m, XP, YP, ZP, IP, JP, KP, 3);
+}
+
+// FORCE_PAR (compact3d.f:12320-12350): Clift-Gauvin drag and gravity
+__device__ __forceinline__ void force_par(double re, const ParC &c, double UP, double VP, double WP, double UF,
+                                          double VF, double WF, double &QU, double &QV, double &QW) {
+    const double VISCOS = 0.000015;
+    const double REP = sqrt((UF - UP) * (UF - UP) + (VF - VP) * (VF - VP) + (WF - WP) * (WF - WP)) * c.D * re;
+    const double FCOR = 1. + 0.15 * pow(REP, 0.687) + 0.0175 * pow(1. + 42500 * pow(REP, -1.16), -1.0);
+    QU = FCOR * (UF - UP) / c.TAU;
+    const double t = VISCOS * re / c.HHH;
+    QV = FCOR * (VF - VP) / c.TAU + (-9.8 / (t * t));
+    QW = FCOR * (WF - WP) / c.TAU;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_par_advance(StepArgs<R> a, WsMesh m, ParC c, double *par, int n, double dt,
+                                                     int *impact) {
+    const Geo g = a.g;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    double *P = par + 6 * (size_t)q;
+    const double D = c.D, ALX = g.alx, ALY = g.aly, ALZ = g.alz;
+    double QXRK = 0., QYRK = 0., QZRK = 0., QURK = 0., QVRK = 0., QWRK = 0.;
+    double XP = P[0], YP = P[1], ZP = P[2], UP = P[3], VP = P[4], WP = P[5], UF, VF, WF, QU, QV, QW;
+    bool euler = YP < 0.5 * D || YP > ALY - 0.5 * D;
+    const double cs[3] = {0.5, 0.5, 1.0}, wt[4] = {1.0, 2.0, 2.0, 1.0};
+    for (int stg = 0; stg < 4 && !euler; ++stg) {
+        if (XP > (ALX - 0.5 * D)) XP = 1.0 * D + XP - ALX;
+        if (XP < (0.5 * D)) XP = ALX - D + XP;
+        if (ZP > (ALZ - 0.5 * D)) ZP = 1.0 * D + ZP - ALZ;
+        if (ZP < (0.5 * D)) ZP = ALZ - D + ZP;
+        par_fluid(a, m, XP, YP, ZP, UF, VF, WF);
+        force_par(g.re, c, UP, VP, WP, UF, VF, WF, QU, QV, QW);
+        QXRK = QXRK + wt[stg] * UP;
+        QYRK = QYRK + wt[stg] * VP;
+        QZRK = QZRK + wt[stg] * WP;
+        QURK = QURK + wt[stg] * QU;
+        QVRK = QVRK + wt[stg] * QV;
+        QWRK = QWRK + wt[stg] * QW;
+        if (stg == 3) break;
+        XP = P[0] + cs[stg] * dt * UP;
+        YP = P[1] + cs[stg] * dt * VP;
+        ZP = P[2] + cs[stg] * dt * WP;
+        UP = P[3] + cs[stg] * dt * QU;
+        VP = P[4] + cs[stg] * dt * QV;
+        WP = P[5] + cs[stg] * dt * QW;
+        euler = YP < 0.5 * D || YP > ALY - 0.5 * D;
+    }
+    if (!euler) {
+        XP = P[0] + dt * QXRK / 6.;
+        YP = P[1] + dt * QYRK / 6.;
+        ZP = P[2] + dt * QZRK / 6.;
+        UP = P[3] + dt * QURK / 6.;
+        VP = P[4] + dt * QVRK / 6.;
+        WP = P[5] + dt * QWRK / 6.;
+    } else {
+        UP = P[3];
+        VP = P[4];
+        WP = P[5];
+        par_fluid(a, m, P[0], P[1], P[2], UF, VF, WF);
+        force_par(g.re, c, UP, VP, WP, UF, VF, WF, QU, QV, QW);
+        XP = P[0] + dt * UP;
+        YP = P[1] + dt * VP;
+        ZP = P[2] + dt * WP;
+        UP = P[3] + dt * QU;
+        VP = P[4] + dt * QV;
+        WP = P[5] + dt * QW;
+    }
+    if (XP > (ALX - 0.5 * D)) XP = 1.0 * D + XP - ALX;
+    if (XP < (0.5 * D)) XP = ALX - D + XP;
+    if (ZP > (ALZ - 0.5 * D)) ZP = 1.0 * D + ZP - ALZ;
+    if (ZP < (0.5 * D)) ZP = ALZ - D + ZP;
+    if (YP > (ALY - 0.5 * D) && VP >= 0.0) {
+        VP = -VP;
+        YP = 2. * ALY - D - YP;
+    }
+    P[0] = XP, P[1] = YP, P[2] = ZP, P[3] = UP, P[4] = VP, P[5] = WP;
+    if (impact) impact[q] = (YP < (0.5 * D) && VP <= 0.0) ? 1 : 0;
+}
+
+// SOURCE_PAR: ruh[3] are Fortran (0:M1,0:M2,0:M3) arrays; h = H(1..N2) by Fortran J
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_par_source(StepArgs<R> a, WsMesh m, ParC c, const double *par, int n,
+                                                    double *r1, double *r2, double *r3) {
+    const Geo g = a.g;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const double *P = par + 6 * (size_t)q;
+    double XP = P[0], YP = P[1], ZP = P[2], QU, QV, QW;
+    int IP, JP, KP;
+    if (!ws_locate(g, m, XP, YP, ZP, IP, JP, KP)) return;
+    const double UF = ws_interp(a, m, XP, YP, ZP, IP, JP, KP, 1);
+    const double VF = ws_interp(a, m, XP, YP, ZP, IP, JP, KP, 2);
+    const double WF = ws_interp(a, m, XP, YP, ZP, IP, JP, KP, 3);
+    force_par(g.re, c, P[3], P[4], P[5], UF, VF, WF, QU, QV, QW);
+    int IPP = IP, JPP = JP, KPP = KP;
+    if (XP > m.XC[IP]) IPP = IP == g.n1m ? 1 : IP + 1;
+    if (YP > m.YC[JP]) JPP = JP == g.n2m ? g.n2m : JP + 1;
+    if (ZP > m.ZC[KP]) KPP = KP == g.n3m ? 1 : KP + 1;
+    const double QQ = 1000.0, t = g.re * 1.5 / 100000 / c.HHH, G = 9.8 / (t * t);
+    const long long su1 = g.n1m + 2, su2 = (long long)(g.n1m + 2) * (g.n2 + 1);
+    auto iu = [&](int i, int j, int k) { return i + su1 * j + su2 * k; };
+    atomicAdd(r1 + iu(IPP, JP, KP), -(c.MASS * QQ * QU * g.dx1 * g.dx3 / g.h[JP]));
+    atomicAdd(r2 + iu(IP, JPP, KP), -(c.MASS * QQ * (QV + G) * g.dx1 * g.dx3 / g.h[JPP]));
+    atomicAdd(r3 + iu(IP, JP, KPP), -(c.MASS * QQ * QW * g.dx1 * g.dx3 / g.h[JP]));
+}
+
+template <typename R>
+int launch_particles_t(c3d_channel *ch, StepArgs<R> &a, double *par, int n, double diam, double dens, double hhh,
+                       double dt, int *impact, double *r1, double *r2, double *r3) {
+    ParC c;
+    const double PI = 3.141592653;
+    c.D = diam / hhh;
+    c.MASS = dens * PI * (c.D * c.D * c.D) / 6.;
+    c.TAU = dens * (c.D * c.D) / 18. * ch->g.re;
+    c.HHH = hhh;
+    WsMesh m = WsMesh::of(ch->g, ch->wshift);
+    m.V1 = nullptr;
+    const int nb = (n + TPB - 1) / TPB;
+    if (r1) k_par_source<R><<<nb, TPB, 0, ch->stream>>>(a, m, c, par, n, r1, r2, r3);
+    else k_par_advance<R><<<nb, TPB, 0, ch->stream>>>(a, m, c, par, n, dt, impact);
+    return cudaGetLastError() == cudaSuccess ? 0 : C3D_ECUDA;
+}
+template int launch_particles_t<double>(c3d_channel *, StepArgs<double> &, double *, int, double, double, double, double,
+                                        int *, double *, double *, double *);
+template int launch_particles_t<float>(c3d_channel *, StepArgs<float> &, double *, int, double, double, double, double,
+                                       int *, double *, double *, double *);
 
 }  // namespace c3d

@@ -477,6 +477,20 @@ int launch_spectra_t(c3d_channel *ch, StepArgs<R> &a, const double *vmo, const d
                      double *rxx, double *rzz, double *rxy);
 
 template <typename R>
+int launch_particles_t(c3d_channel *ch, StepArgs<R> &a, double *par, int n, double diam, double dens, double hhh,
+                       double dt, int *impact, double *r1, double *r2, double *r3);
+
+int launch_particles(c3d_channel *ch, double *par, int n, double diam, double dens, double hhh, double dt, int *impact,
+                     double *r1, double *r2, double *r3) {
+    if (ch->precision == C3D_MIXED) {
+        StepArgs<float> a = make_args<float>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
+        return launch_particles_t<float>(ch, a, par, n, diam, dens, hhh, dt, impact, r1, r2, r3);
+    }
+    StepArgs<double> a = make_args<double>(ch, ch->dt_cached > 0 ? ch->dt_cached : 1.0);
+    return launch_particles_t<double>(ch, a, par, n, diam, dens, hhh, dt, impact, r1, r2, r3);
+}
+
+template <typename R>
 int launch_corr3d_t(c3d_channel *ch, StepArgs<R> &a, const double *st, double *out);
 
 int launch_corr3d(c3d_channel *ch, const double *st, double *out) {

@@ -59,6 +59,9 @@ SIGNATURES = {
     "c3d_plane_quadrants": (_ip, [_vp, _dp, _dp]),
     "c3d_wall_spectrum": (_ip, [_vp, ctypes.c_double, _dp]),
     "c3d_set_cflmax": (_ip, [_vp, ctypes.c_double]),
+    "c3d_particles_advance": (_ip, [_vp, _ip, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double, ctypes.POINTER(ctypes.c_int)]),
+    "c3d_particles_source": (_ip, [_vp, _ip, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp]),
     "c3d_corr3d": (_ip, [_vp, _dp]),
     "c3d_checkpoint_write": (_ip, [_vp, ctypes.c_char_p, _ip, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     "c3d_checkpoint_read": (_ip, [_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), _dp, _dp, _dp]),
@@ -240,6 +243,22 @@ class Channel:
         v = None if vmp is None else np.asfortranarray(vmp, dtype=np.float64)
         check(load().c3d_plane_quadrants(self.h, _p(v), _p(out)), "c3d_plane_quadrants")
         return out.reshape(self.grid.n2m, 8)
+
+    def particles_advance(self, par, dt, diam=0.0002, dens=2220.0, hhh=0.05):
+        """One particle step on the device: par (N, 6) x, y, z, u, v, w -> (par, impact)."""
+        p = np.ascontiguousarray(par, dtype=np.float64).copy()
+        imp = np.zeros(len(p), dtype=np.int32)
+        check(load().c3d_particles_advance(self.h, len(p), _p(p.reshape(-1)), diam, dens, hhh, dt,
+                                           imp.ctypes.data_as(ctypes.POINTER(ctypes.c_int))), "c3d_particles_advance")
+        return p, imp
+
+    def particles_source(self, par, diam=0.0002, dens=2220.0, hhh=0.05):
+        """SOURCE_PAR's terms for par (N, 6): three Fortran (0:N1,0:N2,0:N3) arrays."""
+        p = np.ascontiguousarray(par, dtype=np.float64)
+        out = [self.grid.zeros_s() for _ in range(3)]
+        check(load().c3d_particles_source(self.h, len(p), _p(p.reshape(-1)), diam, dens, hhh, *(_p(o) for o in out)),
+              "c3d_particles_source")
+        return out
 
     def set_cflmax(self, cflmax: float):
         check(load().c3d_set_cflmax(self.h, float(cflmax)), "c3d_set_cflmax")

@@ -302,6 +302,24 @@ int c3d_plane_quadrants(c3d_channel *ch, const double *vmp, double *out);
 int c3d_wall_spectrum(c3d_channel *ch, double utau, double *out);
 int c3d_corr3d(c3d_channel *ch, double *out);
 
+/* ---- Lagrangian particles ------------------------------------------------------
+ * The particle routines of the reference (compact3d.f:11817-12894) with their calls in
+ * the time loop commented out (GET_PAR at 128, SOURCE_PAR at 1026).  Particles are
+ * par[6*q .. 6*q+5] = x, y, z, u, v, w (the reference's PAR(1:6, q)); diam (m), dens and
+ * hhh (m) give INIT_PAR's DIAM_P = diam / hhh, MASS_P and TAU_P = dens DIAM_P^2 / 18 RE.
+ * c3d_particles_advance: one CALC_UX_4RK step of dt on the device with FORCE_PAR's
+ *   Clift-Gauvin drag and gravity and INDEX_IJK / INTERPOLAT of the current field at every
+ *   stage (the explicit Euler step when a stage leaves the channel), then BC_PAR's
+ *   periodic shifts and top-wall reflection; impact[q] (may be NULL) = 1 for a particle
+ *   that reached the bottom wall moving down, where the reference calls SPLASH (its draws
+ *   come from RAN2 seeded by CPU_TIME and are left to the driver).  par is updated.
+ * c3d_particles_source: SOURCE_PAR's two-way coupling terms for the particles, written to
+ *   ruh1..3 (Fortran (0:N1,0:N2,0:N3) each, zero elsewhere). */
+int c3d_particles_advance(c3d_channel *ch, int n, double *par, double diam, double dens, double hhh, double dt,
+                          int *impact);
+int c3d_particles_source(c3d_channel *ch, int n, const double *par, double diam, double dens, double hhh,
+                         double *ruh1, double *ruh2, double *ruh3);
+
 /* ---- checkpoint ------------------------------------------------------------
  * The restart pair of the reference, CWRITE / READUP (compact3d.f:741-872), writes a
  * list-directed text file and reads it back unformatted in another loop order, so the

@@ -76,6 +76,10 @@ def lib():
         L.orc_plane_quadrants.argtypes = [vp, dp, dp, dp]
         L.orc_wall_spectrum.argtypes = [vp, ctypes.c_double, dp]
         L.orc_set_cflmax.argtypes = [vp, ctypes.c_double]
+        L.orc_particles_advance.argtypes = [vp, dp, ip, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
+        L.orc_particles_source.argtypes = [vp, dp, ip, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                           dp, dp, dp]
         L.orc_iwm_slots.restype = ip
         L.orc_get_iwm.argtypes = [vp, dp]
         L.orc_corr3d.argtypes = [vp, dp, dp]
@@ -199,6 +203,21 @@ class Oracle:
         out = np.zeros(lib().orc_iwm_slots() * g.n1m * g.n3m)
         lib().orc_get_iwm(self.h, _p(out))
         return out.reshape(-1, g.n3m, g.n1m)
+
+    def particles_advance(self, U, par, dt, diam=0.0002, dens=2220.0, hhh=0.05):
+        """One CALC_UX_4RK + BC_PAR step of particles par (N, 6): returns (par, impact)."""
+        p = np.ascontiguousarray(par, dtype=np.float64).copy()
+        imp = np.zeros(len(p), dtype=np.int32)
+        lib().orc_particles_advance(self.h, _p(U), len(p), _p(p.reshape(-1)), diam, dens, hhh, dt,
+                                    imp.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+        return p, imp
+
+    def particles_source(self, U, par, diam=0.0002, dens=2220.0, hhh=0.05):
+        """SOURCE_PAR's terms: (RUH1, RUH2, RUH3), each a Fortran (0:M1,0:M2,0:M3) array."""
+        p = np.ascontiguousarray(par, dtype=np.float64)
+        out = [self.grid.zeros_s() for _ in range(3)]
+        lib().orc_particles_source(self.h, _p(U), len(p), _p(p.reshape(-1)), diam, dens, hhh, *(_p(o) for o in out))
+        return out
 
     def diagnose(self, U):
         f1, f3 = self.chkmf(U)

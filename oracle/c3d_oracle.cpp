@@ -2908,6 +2908,156 @@ void orc_get_iwm(void *h, double *out) {
     std::copy(g.IWM.begin(), g.IWM.end(), out);
 }
 
+// ----------------------------------------------------------------------------------
+// Lagrangian particles (compact3d.f:11817-12894, 2029-2075).  The reference's time loop
+// has the calls commented out (GET_PAR at 128, SOURCE_PAR at 1026); these restate its
+// deterministic part for the tests: CALC_UX_4RK's step (FORCE_PAR's Clift-Gauvin drag
+// and gravity, INDEX_IJK/INTERPOLAT at every stage, the periodic shifts by DIAM_P, the
+// explicit Euler step from the start when a stage leaves the channel), BC_PAR's periodic
+// shifts and top-wall reflection, with a bottom-wall impact flagged (the reference
+// calls SPLASH there, which draws from RAN2 seeded by CPU_TIME), and SOURCE_PAR's
+// two-way coupling terms.  PAR is (6, N): x, y, z, u, v, w.
+// ----------------------------------------------------------------------------------
+struct ParConst {
+    double DIAM_P, TAU_P, MASS_P, HHH;
+};
+static ParConst par_const(const Orc &g, double diam_m, double dens, double hhh) {
+    ParConst c;
+    const double PI = 3.141592653;   // INIT_PAR's PI
+    c.DIAM_P = diam_m / hhh;
+    c.MASS_P = dens * PI * std::pow(c.DIAM_P, 3) / 6.;
+    c.TAU_P = dens * std::pow(c.DIAM_P, 2) / 18. * g.RE;
+    c.HHH = hhh;
+    return c;
+}
+
+// FORCE_PAR (compact3d.f:12320-12350)
+static void force_par(const Orc &g, const ParConst &c, double UP, double VP, double WP, double UF, double VF,
+                      double WF, double &QU, double &QV, double &QW) {
+    const double VISCOS = 0.000015;
+    const double REP = std::sqrt(std::pow(UF - UP, 2) + std::pow(VF - VP, 2) + std::pow(WF - WP, 2)) * c.DIAM_P * g.RE;
+    const double FCOR = 1. + 0.15 * std::pow(REP, 0.687) + 0.0175 * std::pow(1. + 42500 * std::pow(REP, -1.16), -1);
+    QU = FCOR * (UF - UP) / c.TAU_P;
+    QV = -9.8 / std::pow(VISCOS * g.RE / c.HHH, 2);
+    QV = FCOR * (VF - VP) / c.TAU_P + QV;
+    QW = FCOR * (WF - WP) / c.TAU_P;
+}
+
+// the fluid velocity at a particle; a point INDEX_IJK finds no cell for (a particle left
+// below the bottom wall, which the reference hands to SPLASH) gets NaN, where the
+// reference would read outside its arrays
+static void par_fluid(const Orc &g, const Mesh02 &m, const double *U, double XP, double YP, double ZP, double &UF,
+                      double &VF, double &WF) {
+    int IP, JP, KP;
+    index_ijk(g, m, XP, YP, ZP, IP, JP, KP);
+    if (IP < 0 || JP < 0 || KP < 0) {
+        UF = VF = WF = std::nan("");
+        return;
+    }
+    UF = interpolat(g, m, XP, YP, ZP, IP, JP, KP, U, 1);
+    VF = interpolat(g, m, XP, YP, ZP, IP, JP, KP, U, 2);
+    WF = interpolat(g, m, XP, YP, ZP, IP, JP, KP, U, 3);
+}
+
+void orc_particles_advance(void *h, const double *U, int n, double *PAR, double diam_m, double dens, double hhh,
+                           double DT_P, int *impact) {
+    Orc &g = *(Orc *)h;
+    const Mesh02 m = mesh02(g);
+    const ParConst c = par_const(g, diam_m, dens, hhh);
+    const double D = c.DIAM_P, ALX = g.ALX, ALY = g.ALY, ALZ = g.ALZ;
+    auto wrap = [&](double &XP, double &ZP, double one) {
+        if (XP > (ALX - 0.5 * D)) XP = one * D + XP - ALX;
+        if (XP < (0.5 * D)) XP = ALX - D + XP;
+        if (ZP > (ALZ - 0.5 * D)) ZP = one * D + ZP - ALZ;
+        if (ZP < (0.5 * D)) ZP = ALZ - D + ZP;
+    };
+    for (int II = 0; II < n; II++) {
+        double *P = PAR + 6 * (size_t)II;
+        double QXRK = 0., QYRK = 0., QZRK = 0., QURK = 0., QVRK = 0., QWRK = 0.;
+        double XP = P[0], YP = P[1], ZP = P[2], UP = P[3], VP = P[4], WP = P[5], UF, VF, WF, QU, QV, QW;
+        bool euler = YP < 0.5 * D || YP > ALY - 0.5 * D;
+        const double cs[4] = {0.5, 0.5, 1.0, 0.0}, ws[4] = {1.0, 2.0, 2.0, 1.0};
+        for (int stg = 0; stg < 4 && !euler; stg++) {
+            wrap(XP, ZP, 1.0);
+            par_fluid(g, m, U, XP, YP, ZP, UF, VF, WF);
+            force_par(g, c, UP, VP, WP, UF, VF, WF, QU, QV, QW);
+            QXRK = QXRK + ws[stg] * UP;
+            QYRK = QYRK + ws[stg] * VP;
+            QZRK = QZRK + ws[stg] * WP;
+            QURK = QURK + ws[stg] * QU;
+            QVRK = QVRK + ws[stg] * QV;
+            QWRK = QWRK + ws[stg] * QW;
+            if (stg == 3) break;
+            XP = P[0] + cs[stg] * DT_P * UP;
+            YP = P[1] + cs[stg] * DT_P * VP;
+            ZP = P[2] + cs[stg] * DT_P * WP;
+            UP = P[3] + cs[stg] * DT_P * QU;
+            VP = P[4] + cs[stg] * DT_P * QV;
+            WP = P[5] + cs[stg] * DT_P * QW;
+            euler = YP < 0.5 * D || YP > ALY - 0.5 * D;
+        }
+        if (!euler) {
+            XP = P[0] + DT_P * QXRK / 6.;
+            YP = P[1] + DT_P * QYRK / 6.;
+            ZP = P[2] + DT_P * QZRK / 6.;
+            UP = P[3] + DT_P * QURK / 6.;
+            VP = P[4] + DT_P * QVRK / 6.;
+            WP = P[5] + DT_P * QWRK / 6.;
+        } else {   // label 100: explicit Euler from the particle's state
+            UP = P[3];
+            VP = P[4];
+            WP = P[5];
+            par_fluid(g, m, U, P[0], P[1], P[2], UF, VF, WF);
+            force_par(g, c, UP, VP, WP, UF, VF, WF, QU, QV, QW);
+            XP = P[0] + DT_P * UP;
+            YP = P[1] + DT_P * VP;
+            ZP = P[2] + DT_P * WP;
+            UP = P[3] + DT_P * QU;
+            VP = P[4] + DT_P * QV;
+            WP = P[5] + DT_P * QW;
+        }
+        P[0] = XP, P[1] = YP, P[2] = ZP, P[3] = UP, P[4] = VP, P[5] = WP;
+        // BC_PAR (12352-12470)
+        if (P[0] > (ALX - 0.5 * D)) P[0] = 1.0 * D + P[0] - ALX;
+        if (P[0] < (0.5 * D)) P[0] = ALX - D + P[0];
+        if (P[2] > (ALZ - 0.5 * D)) P[2] = 1.0 * D + P[2] - ALZ;
+        if (P[2] < (0.5 * D)) P[2] = ALZ - D + P[2];
+        if (P[1] > (ALY - 0.5 * D) && P[4] >= 0.0) {
+            P[4] = -P[4];
+            P[1] = 2. * ALY - D - P[1];
+        }
+        impact[II] = (P[1] < (0.5 * D) && P[4] <= 0.0) ? 1 : 0;
+    }
+}
+
+// SOURCE_PAR (compact3d.f:2029-2075): the terms the particles add to RUH1..3 (Fortran
+// (0:M1,0:M2,0:M3) each, added to what is passed), QQ = 1000 and gravity G.
+void orc_particles_source(void *h, const double *U, int n, const double *PAR, double diam_m, double dens, double hhh,
+                          double *RUH1, double *RUH2, double *RUH3) {
+    Orc &g = *(Orc *)h;
+    const Mesh02 m = mesh02(g);
+    const ParConst c = par_const(g, diam_m, dens, hhh);
+    const double QQ = 1000.0, G = 9.8 / std::pow(g.RE * 1.5 / 100000 / hhh, 2);
+    for (int II = 0; II < n; II++) {
+        const double *P = PAR + 6 * (size_t)II;
+        double XP = P[0], YP = P[1], ZP = P[2], UF, VF, WF, QU, QV, QW;
+        int IP, JP, KP;
+        index_ijk(g, m, XP, YP, ZP, IP, JP, KP);
+        if (IP < 0 || JP < 0 || KP < 0) continue;   // outside the channel: no cell to deposit in
+        UF = interpolat(g, m, XP, YP, ZP, IP, JP, KP, U, 1);
+        VF = interpolat(g, m, XP, YP, ZP, IP, JP, KP, U, 2);
+        WF = interpolat(g, m, XP, YP, ZP, IP, JP, KP, U, 3);
+        force_par(g, c, P[3], P[4], P[5], UF, VF, WF, QU, QV, QW);
+        int IPP = IP, JPP = JP, KPP = KP;
+        if (XP > m.XC[IP]) IPP = g.IPA[IP];
+        if (YP > m.YC[JP]) JPP = g.JPA[JP];
+        if (ZP > m.ZC[KP]) KPP = g.KPA[KP];
+        RUH1[g.iu(IPP, JP, KP)] -= c.MASS_P * QQ * QU * g.DX1 * g.DX3 / g.H[JP];
+        RUH2[g.iu(IP, JPP, KP)] -= c.MASS_P * QQ * (QV + G) * g.DX1 * g.DX3 / g.H[JPP];
+        RUH3[g.iu(IP, JP, KPP)] -= c.MASS_P * QQ * QW * g.DX1 * g.DX3 / g.H[JP];
+    }
+}
+
 // SGSSD's BETA(1:N2M) of the last SGS evaluation
 void orc_get_beta(void *h, double *beta) {
     Orc &g = *(Orc *)h;
