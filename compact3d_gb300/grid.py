@@ -205,7 +205,8 @@ def re_from_retau(ret: float) -> float:
 
 PI = math.pi
 
-# Channel workloads.  Cells are N1M x N2M x N3M; Re_bulk(2h) = 4/3 RE.
+# Channel workloads.  Cells are N1M x N2M x N3M; Re_bulk(2h) = 4/3 RE (the laminar bulk
+# velocity of the unit-centreline profile is 2/3).
 WORKLOADS = {
     # 64 x 65 x 64 points, 4pi x 2 x 4/3 pi, beta=2.0, Re_bulk=5600 -> RE=4200, dt=0.002
     "channel64": dict(n1m=64, n2m=64, n3m=64, alx=4 * PI, aly=2.0, alz=4 * PI / 3, cks=2.0,
