@@ -77,3 +77,43 @@ def test_batch_dt_change_recaptures(L):
         assert np.array_equal(ch.download()[0], s.download()[0])
         s.close()
     b.close()
+
+
+def test_batch_of_les_channels_matches_single_channels(L):
+    """LES channels in a batch graph, whose wall models and SGSSD root solve run on side
+    streams forked and joined inside each channel's step: bitwise the single steps."""
+    specs = [("les32cs", C3D_FP64, dict(wmodel=3)), ("les32dy", C3D_FP64, dict(files=3)),
+             ("les32cs", C3D_MIXED, dict(wmodel=1)), ("les32dy", C3D_MIXED, dict(wmodel=5))]
+    ens = []
+    for i, (name, prec, over) in enumerate(specs):
+        g, dt = make_grid(name, precision=prec, **over)
+        ens.append((g, dt, ic.loglaw(g, 2000.0, seed=ic.SEED0 + i)))
+    b = L.Batch([g for g, _, _ in ens])
+    singles = []
+    for (g, dt, (U, P, HH)), ch in zip(ens, b.channels):
+        for c in (ch, None):
+            s = c or L.Channel(g)
+            s.upload(U, P, HH)
+            s.project()
+            if c is None:
+                singles.append(s)
+    dts = [dt for _, dt, _ in ens]
+    pb, pb3 = [0.0] * len(ens), [0.0] * len(ens)
+    ps = [(0.0, 0.0) for _ in ens]
+    for n in range(1, 5):
+        pb, pb3 = b.step(n, dts, pb, pb3)
+        ps = [s.step(n, dt, *p) for s, dt, p in zip(singles, dts, ps)]
+    for i, (ch, s) in enumerate(zip(b.channels, singles)):
+        for x, y in zip(ch.download(), s.download()):
+            assert np.array_equal(x, y), i
+        for x, y in zip(ch.download_wall(), s.download_wall()):
+            assert np.array_equal(x, y), i
+    for s in singles:
+        s.close()
+    b.close()
+
+
+def test_batch_refuses_iwmles(L):
+    g, _ = make_grid("les32cs", wmodel=2)
+    with pytest.raises(L.C3DError):
+        L.Batch([g])
