@@ -373,8 +373,9 @@ int check_grid(const c3d_grid *g) {
         set_error("WMODEL 4 (WALLMODEL_WERNER) takes the x neighbour with the z index, so it needs N3-1 <= N1-1");
         return C3D_EINVAL;
     }
-    if (g->wmodel == 1 && g->y[0] != 0.0) {
-        set_error("Y(0) = Y0 != 0 selects WALLMODEL_ROUGH, which is not built");
+    if (g->wmodel == 1 && g->y[0] != 0.0 &&
+        !(g->y[0] > 0 && g->dy[1] + g->dy[2] + g->dy[3] / 2.0 > g->y[0])) {
+        set_error("WALLMODEL_ROUGH (WMODEL 1, Y0 = Y(0) != 0) needs 0 < Y0 < DY(1) + DY(2) + DY(3)/2");
         return C3D_EINVAL;
     }
     return 0;
@@ -525,6 +526,10 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
         if (gr->wmodel == 2) {
             if (dalloc(&ch->iwm, c3d::iwm_doubles(g))) return fail(C3D_ENOMEM);
             ch->iwm_dzp = gr->dy[1] + gr->dy[2] + gr->dy[3] / 2.0;
+        }
+        if (gr->wmodel == 1 && gr->y[0] != 0.0) {   // WALLMODEL_ROUGH's KAPA / log(DELTAP / Y0)
+            ch->wrough = 1;
+            ch->wklog = 0.41 / std::log((gr->dy[1] + gr->dy[2] + gr->dy[3] / 2.0) / gr->y[0]);
         }
         if (gr->wmodel == 3 || gr->wmodel == 5) {
             ch->wzs = marusic_plane(gr->y, g.n2m);
@@ -934,7 +939,7 @@ static int check_wall_flag(c3d_channel *ch, const double *scal_host) {
         set_error("a shared-memory bulk-copy stage did not complete within its wait limit");
         return C3D_ECUDA;
     }
-    if (ch->files != 0 && ch->wmodel == 1 && scal_host[SCAL_WALLERR] != 0.0) {
+    if (ch->files != 0 && ch->wmodel == 1 && !ch->wrough && scal_host[SCAL_WALLERR] != 0.0) {
         set_error("wall model: the Newton iteration for u_tau did not converge within the iteration cap");
         return C3D_ENOTCONV;
     }

@@ -187,6 +187,8 @@ struct c3d_channel {
     cudaEvent_t wfork = nullptr, wjoin = nullptr;
     int wjoin_pending = 0;
     int wzs = 0;
+    int wrough = 0;            // WALLMODEL_ROUGH (WMODEL 1 with Y0 != 0) and its KAPA / log(DELTAP / Y0)
+    double wklog = 0.0;
     int y_increasing = 0;      // Y(1:N2) increases (the particle and shifted-model searches)
     double wtan16 = 0.0;
     double *stats = nullptr;  // plane statistics table and partial sums (allocated on first use)

@@ -627,6 +627,37 @@ __global__ void __launch_bounds__(TPB) k_wall(StepArgs<R> a, LesArgs<R> l) {
     }
 }
 
+// WALLMODEL_ROUGH (WMODEL 1 with Y0 = Y(0) != 0, compact3d.f:2496-2558), FP64: the rough-
+// wall log law TAUW1 = (0.41 U / log(DELTAP / Y0))^2 per bottom-wall point along the
+// velocity of plane 3, with per-block sums of TAUW1 for WSM(1).
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_wall_rough(StepArgs<R> a, LesArgs<R> l, double klog) {
+    typedef St<R> ST;
+    const Geo g = a.g;
+    __shared__ double ssum[TPB];
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double tw1 = 0.0;
+    if (e < g.np) {
+        const int i = e % g.n1m, k = e / g.n1m;
+        const double u3 = ST::dbl(a.u[fidx(g, i, 3, k)]), w3 = ST::dbl(a.w[fidx(g, i, 3, k)]);
+        const double uave = sqrt(__dadd_rn(__dmul_rn(u3, u3), __dmul_rn(w3, w3)));
+        const double t = klog * uave;
+        tw1 = t * t;
+        l.tauw[e] = tw1 * u3 / uave;
+        l.taub[e] = tw1 * w3 / uave;
+    }
+    ssum[threadIdx.x] = tw1;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) ssum[threadIdx.x] += ssum[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        l.wpart[blockIdx.x] = ssum[0];
+        l.wpart[gridDim.x + blockIdx.x] = 0.0;
+    }
+}
+
 // WALLMODEL_WERNER (compact3d.f:4815-4958), FP64: the Werner-Wengle power law at the first
 // cell centre of both walls into tw4 (TAUWE(I,K,1..4), four planes of N1M x N3M), with
 // per-block sums of the bottom u-stress for WSM(1); the reference's x neighbour taken with
@@ -1433,7 +1464,12 @@ int launch_les(c3d_channel *ch, StepArgs<R> &a, LesArgs<R> &l, int stage, int *n
                 CK_RC(cudaEventRecord(ch->wfork, st));
                 CK_RC(cudaStreamWaitEvent(wst, ch->wfork, 0));
             }
-            if (ch->files != 0 && ch->wmodel == 1) {
+            if (ch->files != 0 && ch->wmodel == 1 && ch->wrough) {
+                const int nb = nblk(g.np);
+                k_wall_rough<R><<<nb, TPB, 0, wst>>>(a, l, ch->wklog);
+                k_wall_sum<R><<<1, 256, 0, wst>>>(a, l, nb);
+                mark(ch, nl, "wall", 24.0 * g.np);
+            } else if (ch->files != 0 && ch->wmodel == 1) {
                 const int nb = nblk(g.np);
                 k_wall<R><<<nb, TPB, 0, wst>>>(a, l);
                 k_wall_sum<R><<<1, 256, 0, wst>>>(a, l, nb);

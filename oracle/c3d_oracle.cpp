@@ -1871,6 +1871,27 @@ void wallss_common(Orc &g, const double *U, double *wsm) {
 // the third cell centre by damped Newton iterations; bottom wall only (the top-wall
 // stresses TAUW(.,.,2), TAUB(.,.,2) are left as they are).  The reference iterates
 // without a cap; here the cap `wall_iter_cap` makes a non-converging point an error.
+// WALLMODEL_ROUGH (WMODEL 1 with Y0 = Y(0) != 0, compact3d.f:2496-2558): the rough-wall
+// log law u_tau = KAPA U / log(DELTAP / Y0) on the bottom wall, KAPA = 0.41.
+int wallmodel_rough(Orc &g, const double *U) {
+    const int N1M = g.N1M, N3M = g.N3M;
+    const double KAPA = 0.41, Y0 = g.Y[0];
+    const double DELTAP = g.DY[1] + g.DY[2] + g.DY[3] / 2.0;
+    double WSM1 = 0.0;
+    for (int K = 1; K <= N3M; K++)
+        for (int I = 1; I <= N1M; I++) {
+            const double u = U[g.iuc(I, 3, K, 1)], w = U[g.iuc(I, 3, K, 3)];
+            const double U_ave = std::sqrt(std::pow(u, 2.) + std::pow(w, 2.));
+            const double TAUW1 = std::pow(KAPA / std::log(DELTAP / Y0) * U_ave, 2.0);
+            WSM1 = WSM1 + TAUW1;
+            g.TAUW[g.itw(I, K, 1)] = TAUW1 * u / U_ave;
+            g.TAUB[g.itw(I, K, 1)] = TAUW1 * w / U_ave;
+        }
+    g.WSM[0] = WSM1 / (double)(N1M * N3M);
+    g.TAOW = g.WSM[0];
+    return 0;
+}
+
 int wallmodel_instant(Orc &g, const double *U) {
     const int N1M = g.N1M, N3M = g.N3M;
     const double KAPA = 0.41, B = 5.2;
@@ -2451,6 +2472,7 @@ int wallmodel(Orc &g, const double *U, const double *P = nullptr, int NTIME = 1,
     if (g.WMODEL == 4) return wallmodel_werner(g, U);
     if (g.WMODEL == 3 || g.WMODEL == 5) return wallmodel_shifted(g, U);
     if (g.WMODEL == 2) return P ? wallmodel_iwmles(g, U, P, NTIME, DT, PRESG, PRESG3) : C3D_EINVAL;
+    if (g.Y[0] != 0.0) return wallmodel_rough(g, U);
     return wallmodel_instant(g, U);
 }
 

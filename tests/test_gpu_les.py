@@ -76,6 +76,7 @@ def gpu_from(libc3d, orc, g, U, P, HH, precision=C3D_FP64):
     ("les32dy", dict(files=3)),             # SGSSD (scale-dependent) + WALLMODEL_INSTANT
     ("les32dy", dict(files=3, wmodel=0, cks=2.0)),   # SGSSD, no-slip walls, stretched y
     ("les32dy", dict(files=3, wmodel=3)),   # SGSSD + MARUSIC1
+    ("les32cs", dict(y0=2e-3)),             # Smagorinsky + WALLMODEL_ROUGH (Y0 != 0)
 ])
 def test_les_one_step_fp64(libc3d, oracle_mod, name, over):
     g, dt, orc, U, P, HH, S, pg, pg3 = warm_start(oracle_mod, name, **over)

@@ -669,3 +669,22 @@ def test_iwmles_update_matches_numpy_restatement(oracle_mod, n2m):
             assert wsm[0] == pytest.approx(np.mean(np.sqrt(got[_IW["TAUWX"]] ** 2 + got[_IW["TAUWY"]] ** 2)),
                                            rel=1e-12, abs=1e-300)
     assert np.isfinite(U).all()
+
+
+def test_rough_wall_model_log_law(oracle_mod):
+    """WALLMODEL_ROUGH (WMODEL 1 with Y0 = Y(0) != 0, compact3d.f:2496-2558): TAUW1 =
+    (0.41 |U| / log(DELTAP / Y0))^2 along the velocity of plane 3 per bottom-wall point,
+    WSM(1) its plane mean, DELTAP = DY(1) + DY(2) + DY(3)/2."""
+    g, _ = _grid("les32cs", y0=2e-3)
+    o = oracle_mod.Oracle(g)
+    U, P, HH = ic.loglaw(g, 2000.0)
+    assert o.wallmodel(U) == 0
+    tw, tb, wsm = o.get_wall()
+    dy = g.arrays["dy"]
+    dp = dy[1] + dy[2] + dy[3] / 2.0
+    u, w = U[1:g.n1m + 1, 3, 1:g.n3m + 1, 0], U[1:g.n1m + 1, 3, 1:g.n3m + 1, 2]
+    mag = np.sqrt(u ** 2 + w ** 2)
+    t1 = (0.41 / math.log(dp / 2e-3) * mag) ** 2
+    np.testing.assert_allclose(tw[1:g.n1m + 1, 1:g.n3m + 1, 0], t1 * u / mag, rtol=1e-13)
+    np.testing.assert_allclose(tb[1:g.n1m + 1, 1:g.n3m + 1, 0], t1 * w / mag, rtol=1e-13)
+    assert wsm[0] == pytest.approx(t1.mean(), rel=1e-13)
