@@ -348,8 +348,8 @@ int check_grid(const c3d_grid *g) {
                   "4 (WALLMODEL_WERNER) or 5 (PIOMELLI)");
         return C3D_EINVAL;
     }
-    if (g->wmodel == 2 && g->y[0] != 0.0) {
-        set_error("Y(0) = Y0 != 0 with WMODEL 2 selects WALLMODEL_IWMLES_ROUGH, which is not built");
+    if (g->wmodel == 2 && g->y[0] != 0.0 && !(g->y[0] > 0 && g->dy[1] + g->dy[2] + g->dy[3] / 2.0 > g->y[0])) {
+        set_error("WALLMODEL_IWMLES_ROUGH (WMODEL 2, Y0 = Y(0) != 0) needs 0 < Y0 < DY(1) + DY(2) + DY(3)/2");
         return C3D_EINVAL;
     }
     if (g->wmodel == 3 || g->wmodel == 5) {
@@ -526,6 +526,7 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
         if (gr->wmodel == 2) {
             if (dalloc(&ch->iwm, c3d::iwm_doubles(g))) return fail(C3D_ENOMEM);
             ch->iwm_dzp = gr->dy[1] + gr->dy[2] + gr->dy[3] / 2.0;
+            ch->iwm_y0 = gr->y[0];
         }
         if (gr->wmodel == 1 && gr->y[0] != 0.0) {   // WALLMODEL_ROUGH's KAPA / log(DELTAP / Y0)
             ch->wrough = 1;

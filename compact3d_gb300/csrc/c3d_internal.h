@@ -172,7 +172,7 @@ struct c3d_channel {
     // step, DY(1) + DY(2) + DY(3)/2, the driver's CFLMAX and the NTIME of the step
     double *iwm = nullptr;
     int iwm_ready = 0;
-    double iwm_dt = 0.0, iwm_dzp = 0.0, cflmax = 1.0;
+    double iwm_dt = 0.0, iwm_dzp = 0.0, cflmax = 1.0, iwm_y0 = 0.0;
     int ntime = 1;
     double *sdpart = nullptr, *sdbeta = nullptr;
     int sdnt = 0;

@@ -1,5 +1,7 @@
-// c3d_iwm.cu -- WALLMODEL_IWMLES_SMOOTH (WMODEL 2 with Y0 = 0, compact3d.f:3386-4279), the
-// integral wall model of Yang et al. 2015 on the bottom wall, FP64.
+// c3d_iwm.cu -- WALLMODEL_IWMLES_SMOOTH (WMODEL 2 with Y0 = 0, compact3d.f:3386-4279) and
+// WALLMODEL_IWMLES_ROUGH (Y0 != 0, 2562-3381), the integral wall model of Yang et al. 2015
+// on the bottom wall, FP64.  The rough variant shares the state, schedule, filter and
+// left-hand side and replaces the Newton solve and the profile (k_iwm_rough).
 //
 // Per wall point a state of IW_NS values (the reference's /IWMLES/ arrays, slot-major in
 // ch->iwm) persists across steps.  It is initialised at NTIME = 1, or at the channel's
@@ -35,7 +37,7 @@ enum {
     IW_UTX, IW_UTY, IW_TAUWX, IW_TAUWY, IW_FTX, IW_FTY, IW_FTMX, IW_FTMY, IW_FP, IW_INTE, IW_INTEM = IW_INTE + 5,
     IW_DIFFX = IW_INTEM + 5, IW_DIFFY, IW_LHSX, IW_LHSY, IW_FUS, IW_TR, IW_DZ, IW_AX, IW_AY, IW_CX, IW_CY,
     IW_UNSX, IW_UNSY, IW_DELI, IW_DELV, IW_DTX, IW_DTY, IW_DBX, IW_DBY, IW_CONVX, IW_CONVY, IW_PRSX, IW_PRSY,
-    IW_NS,
+    IW_Z0, IW_NS,
     // device-only: the Newton result before the |A| > 1 reset, the fallback values and flags
     IW_PUTX = IW_NS, IW_PUTY, IW_EQX, IW_EQY, IW_EQ0, IW_STALE, IW_SLOTS
 };
@@ -90,6 +92,8 @@ struct IwmArgs {
     double *scal;
     Geo g;
     double dzp, cflmax, wm_dt;
+    int rough;         // WALLMODEL_IWMLES_ROUGH: Y0 = Y(0) != 0 is the roughness length
+    double y0;
 };
 
 __device__ __forceinline__ double &S(const IwmArgs &w, int q, int e) { return w.st[(size_t)q * w.g.np + e]; }
@@ -133,7 +137,7 @@ __global__ void k_iwm_fin(IwmArgs w, int nb, int mode) {
     const double n = (double)(w.g.n1m * w.g.n3m);
     if (mode == 0) {
         sc[IW_SC_UINIT] = sh[0] / n;
-        sc[IW_SC_USINIT] = iwm_loglaw(sc[IW_SC_UINIT], w.dzp, w.g.re);
+        sc[IW_SC_USINIT] = w.rough ? sc[IW_SC_UINIT] * 0.4 / log(w.dzp / w.y0) : iwm_loglaw(sc[IW_SC_UINIT], w.dzp, w.g.re);
     } else if (mode == 1) {
         sc[IW_SC_PBAR] = sh[0] / (double)w.g.n1m / (double)w.g.n3m;
     } else {
@@ -161,8 +165,114 @@ __global__ void __launch_bounds__(TPB) k_iwm_init(IwmArgs w) {
     S(w, IW_FUS, e) = usinit;
     S(w, IW_TR, e) = (w.cflmax * w.g.alx / w.g.n1m / uinit) / (Dzp / vonk / usinit);
     S(w, IW_DZ, e) = Dzp;
-    S(w, IW_DELI, e) = smin(11.0 * reinv / usinit, Dzp);
-    S(w, IW_DELV, e) = reinv / usinit;
+    if (w.rough) {   // iwm_init_rough (compact3d.f:2736-2857)
+        S(w, IW_DBX, e) = usinit / vonk / w.y0;
+        S(w, IW_Z0, e) = w.y0;
+    } else {
+        S(w, IW_DELI, e) = smin(11.0 * reinv / usinit, Dzp);
+        S(w, IW_DELV, e) = reinv / usinit;
+    }
+}
+
+// iwm_slv_rough (compact3d.f:3031-3052)
+__device__ void iwm_slv_rough(double lhsx, double lhsy, double Ux, double Uy, double Dz, double z0, double utx,
+                              double uty, double &fx, double &fy) {
+    const double vonk = 0.4, lg = log(Dz / z0);
+    const double Ax = (Ux - utx / vonk * lg) / ((1.0 - z0 / Dz));
+    const double Ay = (Uy - uty / vonk * lg) / ((1.0 - z0 / Dz));
+    fx = 1.0 / 2.0 * Dz * Ax * sq(1.0 - z0 / Dz) + 1.0 / vonk * utx * Dz * (z0 / Dz - 1.0 + lg) + lhsx;
+    fy = 1.0 / 2.0 * Dz * Ay * sq(1.0 - z0 / Dz) + 1.0 / vonk * uty * Dz * (z0 / Dz - 1.0 + lg) + lhsy;
+}
+
+// iwm_calc_wallstress_rough (compact3d.f:3055-3334) per point: the Newton solve with the
+// diagonal finite-difference Jacobian, the equilibrium fallback vonk U / log(Dz / z0),
+// the rough-wall integrals, derivatives, diffusion and stresses.  Kept as written: the Lvv
+// integral has -3 z0^2/Dz^2 where Luu has +3, and tauwy is (vonk * iwmpz0)^2 ... with
+// iwmpz0 an undeclared, zero-valued name.
+__global__ void __launch_bounds__(TPB) k_iwm_rough(IwmArgs w) {
+    const Geo g = w.g;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= g.np) return;
+    const double vonk = 0.4, wm_tol = 0.000001, wm_eps = 0.000000001, wm_dt = w.wm_dt;
+    const double lhsx = S(w, IW_LHSX, e), lhsy = S(w, IW_LHSY, e);
+    const double Ux = S(w, IW_FTX, e), Uy = S(w, IW_FTY, e), Dz = S(w, IW_DZ, e), z0 = S(w, IW_Z0, e);
+    double utx = S(w, IW_UTX, e), uty = S(w, IW_UTY, e), fx, fy, fxp, fyp;
+    iwm_slv_rough(lhsx, lhsy, Ux, Uy, Dz, z0, utx, uty, fx, fy);
+    int iter = 0, eq = 0;
+    while (smax(fabs(fx), fabs(fy)) > wm_tol) {
+        iwm_slv_rough(lhsx, lhsy, Ux, Uy, Dz, z0, utx + wm_eps, uty, fxp, fyp);
+        const double a11 = (fxp - fx) / wm_eps, a21 = 0.0;
+        iwm_slv_rough(lhsx, lhsy, Ux, Uy, Dz, z0, utx, uty + wm_eps, fxp, fyp);
+        const double a12 = 0.0, a22 = (fyp - fy) / wm_eps;
+        const double det = __dsub_rn(__dmul_rn(a11, a22), __dmul_rn(a12, a21));
+        const double nx = utx - __dsub_rn(__dmul_rn(a22, fx), __dmul_rn(a12, fy)) / det;
+        const double ny = uty - __dadd_rn(__dmul_rn(-a21, fx), __dmul_rn(a11, fy)) / det;
+        utx = nx;
+        uty = ny;
+        iwm_slv_rough(lhsx, lhsy, Ux, Uy, Dz, z0, utx, uty, fx, fy);
+        iter = iter + 1;
+        if (iter > 1500) {
+            eq = 1;
+            break;
+        }
+    }
+    if (utx - 1.0 == utx || uty - 1.0 == uty) eq = 1;
+    const double lg = log(Dz / z0);
+    if (eq) {
+        utx = vonk * Ux / lg;
+        uty = vonk * Uy / lg;
+    }
+    double Ax = 0.0, Ay = 0.0;
+    if (!eq) {
+        Ax = (Ux - utx / vonk * lg) / ((1.0 - z0 / Dz));
+        Ay = (Uy - uty / vonk * lg) / ((1.0 - z0 / Dz));
+    }
+    S(w, IW_UTX, e) = utx;
+    S(w, IW_UTY, e) = uty;
+    S(w, IW_AX, e) = Ax;
+    S(w, IW_AY, e) = Ay;
+    for (int q = 0; q < 5; ++q) S(w, IW_INTEM + q, e) = S(w, IW_INTE + q, e);
+    const double px = utx, py = uty, r = z0 / Dz;
+    const double P4 = 1.0 - 4.0 * r + 3.0 * sq(z0) / sq(Dz) - 2.0 * lg + 4.0 * r * lg;
+    const double M4 = 1.0 - 4.0 * r - 3.0 * sq(z0) / sq(Dz) - 2.0 * lg + 4.0 * r * lg;
+    const double c3 = (1.0 - r) * (1.0 - r) * (1.0 - r);
+    S(w, IW_INTE + IW_LU, e) = 1.0 / 2.0 * Dz * Ax * sq(1.0 - r) + 1.0 / vonk * px * Dz * (r - 1.0 + lg);
+    S(w, IW_INTE + IW_LV, e) = 1.0 / 2.0 * Dz * Ay * sq(1.0 - r) + 1.0 / vonk * py * Dz * (r - 1.0 + lg);
+    S(w, IW_INTE + IW_LUV, e) = 1.0 / sq(vonk) * px * py * Dz * (1.0 - 2 * r + sq(1.0 - lg)) +
+                                1.0 / 3.0 * Ax * Ay * Dz * c3 - 1.0 / 4.0 / vonk * (Ax * py + Ay * px) * Dz * P4;
+    S(w, IW_INTE + IW_LUU, e) = 1.0 / sq(vonk) * sq(px) * Dz * (sq(lg - 1.0) - 2.0 * r + 1.0) +
+                                1.0 / 3.0 * sq(Ax) * Dz * c3 - 1.0 / 2.0 / vonk * px * Ax * Dz * P4;
+    S(w, IW_INTE + IW_LVV, e) = 1.0 / sq(vonk) * sq(py) * Dz * (sq(lg - 1.0) - 2.0 * r + 1.0) +
+                                1.0 / 3.0 * sq(Ay) * Dz * c3 - 1.0 / 2.0 / vonk * py * Ay * Dz * M4;
+    const double dTx = 1.0 / Dz * (Ax + px / vonk), dTy = 1.0 / Dz * (Ay + py / vonk);
+    const double dBx = 1.0 / Dz * Ax + px / vonk / z0, dBy = 1.0 / Dz * Ay + py / vonk / z0;
+    S(w, IW_DTX, e) = dTx;
+    S(w, IW_DTY, e) = dTy;
+    S(w, IW_DBX, e) = dBx;
+    S(w, IW_DBY, e) = dBy;
+    const double Vel = sqrt(sq(Ux) + sq(Uy));
+    const double dVelzT = fabs(Ux / Vel * dTx + Uy / Vel * dTy), dVelzB = sqrt(sq(dBx) + sq(dBy));
+    S(w, IW_DIFFX, e) = sq(vonk * Dz) * dVelzT * dTx - sq(vonk * z0) * dVelzB * dBx;
+    S(w, IW_DIFFY, e) = sq(vonk * Dz) * dVelzT * dTy - sq(vonk * z0) * dVelzB * dBy;
+    double tx, ty;
+    if (eq) {
+        const double para = sqrt(sq(Ux) + sq(Uy)) * sq(vonk) / sq(lg);
+        tx = para * Ux;
+        ty = para * Uy;
+    } else {
+        const double iwmpz0 = 0.0;
+        tx = sq(vonk * z0) * dVelzB * dBx;
+        ty = sq(vonk * iwmpz0) * dVelzB * dBy;
+    }
+    S(w, IW_TAUWX, e) = tx;
+    S(w, IW_TAUWY, e) = ty;
+    const double utaup = pow(sq(tx) + sq(ty), 0.25);
+    const double tR = S(w, IW_TR, e);
+    const double fus = __dadd_rn(__dmul_rn(S(w, IW_FUS, e), 1.0 - tR), __dmul_rn(utaup, tR));
+    S(w, IW_FUS, e) = fus;
+    double ntR = wm_dt / (Dz / fus / vonk);
+    if (ntR > 1.0) ntR = 1.0;
+    S(w, IW_TR, e) = ntR;
 }
 
 template <typename R>
@@ -412,6 +522,8 @@ int launch_iwm_t(c3d_channel *ch, StepArgs<R> &a, cudaStream_t st, double *tauw,
     w.g = g;
     w.dzp = ch->iwm_dzp;
     w.cflmax = ch->cflmax;
+    w.rough = ch->iwm_y0 != 0.0;
+    w.y0 = ch->iwm_y0;
     const int nb = nblk(g.np);
     const int ntime = ch->ntime;
     if (ntime == 1 || !ch->iwm_ready) {
@@ -429,9 +541,13 @@ int launch_iwm_t(c3d_channel *ch, StepArgs<R> &a, cudaStream_t st, double *tauw,
         k_iwm_fin<<<1, 256, 0, st>>>(w, nb, 1);
         k_iwm_filter<R><<<nb, TPB, 0, st>>>(a, w);
         k_iwm_lhs<<<nb, TPB, 0, st>>>(w);
-        k_iwm_newton<<<nb, TPB, 0, st>>>(w);
-        k_iwm_stale<<<1, 1024, 0, st>>>(w);
-        k_iwm_finish<<<nb, TPB, 0, st>>>(w);
+        if (w.rough) {
+            k_iwm_rough<<<nb, TPB, 0, st>>>(w);
+        } else {
+            k_iwm_newton<<<nb, TPB, 0, st>>>(w);
+            k_iwm_stale<<<1, 1024, 0, st>>>(w);
+            k_iwm_finish<<<nb, TPB, 0, st>>>(w);
+        }
     }
     k_iwm_apply<<<nb, TPB, 0, st>>>(w);
     k_iwm_sum<R><<<nb, TPB, 0, st>>>(a, w, 2);

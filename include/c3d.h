@@ -66,11 +66,11 @@ extern "C" {
  *                                             3 SGSSD)
  *   /WALLMODEL/ WMODEL                     -> wmodel (0 none, 1 WALLMODEL_INSTANT,
  *                                             2 WALLMODEL_IWMLES_SMOOTH, 3 MARUSIC1,
- *                                             4 WALLMODEL_WERNER, 5 PIOMELLI; with 1,
- *                                             Y0 = Y(0) != 0 selects WALLMODEL_ROUGH
- *                                             (0 < Y0 < DY(1)+DY(2)+DY(3)/2); with 2,
- *                                             Y(0) must be 0 (IWMLES_ROUGH is not
- *                                             built); 4 needs N3 <= N1;
+ *                                             4 WALLMODEL_WERNER, 5 PIOMELLI; with 1
+ *                                             and 2, Y0 = Y(0) != 0 selects
+ *                                             WALLMODEL_ROUGH / _IWMLES_ROUGH
+ *                                             (0 < Y0 < DY(1)+DY(2)+DY(3)/2);
+ *                                             4 needs N3 <= N1;
  *                                             3 and 5 need Y(1:N2) increasing, see
  *                                             below)
  * The library takes the driver's metric arrays as given; it recomputes only

@@ -2182,7 +2182,7 @@ enum {
     IW_UTX, IW_UTY, IW_TAUWX, IW_TAUWY, IW_FTX, IW_FTY, IW_FTMX, IW_FTMY, IW_FP, IW_INTE, IW_INTEM = IW_INTE + 5,
     IW_DIFFX = IW_INTEM + 5, IW_DIFFY, IW_LHSX, IW_LHSY, IW_FUS, IW_TR, IW_DZ, IW_AX, IW_AY, IW_CX, IW_CY,
     IW_UNSX, IW_UNSY, IW_DELI, IW_DELV, IW_DTX, IW_DTY, IW_DBX, IW_DBY, IW_CONVX, IW_CONVY, IW_PRSX, IW_PRSY,
-    IW_NS
+    IW_Z0, IW_NS
 };
 // integral indices iwm_Lu = 1, iwm_Luu = 2, iwm_Lv = 3, iwm_Lvv = 4, iwm_Luv = 5
 enum { IW_LU = 0, IW_LUU = 1, IW_LV = 2, IW_LVV = 3, IW_LUV = 4 };
@@ -2224,19 +2224,132 @@ static void iwm_slv(double lhsx, double lhsy, double Ux, double Uy, double Dz, d
     fy = inteLv + lhsy;
 }
 
+// iwm_slv_rough (compact3d.f:3031-3052)
+static void iwm_slv_rough(double lhsx, double lhsy, double Ux, double Uy, double Dz, double z0, double utx, double uty,
+                          double &fx, double &fy) {
+    const double vonk = 0.4;
+    const double Ax = (Ux - utx / vonk * std::log(Dz / z0)) / ((1.0 - z0 / Dz));
+    const double Ay = (Uy - uty / vonk * std::log(Dz / z0)) / ((1.0 - z0 / Dz));
+    const double inteLu = 1.0 / 2.0 * Dz * Ax * std::pow(1.0 - z0 / Dz, 2.0) +
+                          1.0 / vonk * utx * Dz * (z0 / Dz - 1.0 + std::log(Dz / z0));
+    const double inteLv = 1.0 / 2.0 * Dz * Ay * std::pow(1.0 - z0 / Dz, 2.0) +
+                          1.0 / vonk * uty * Dz * (z0 / Dz - 1.0 + std::log(Dz / z0));
+    fx = inteLu + lhsx;
+    fy = inteLv + lhsy;
+}
+
+// iwm_calc_wallstress_rough (compact3d.f:3055-3334): a Newton solve with the diagonal
+// finite-difference Jacobian (a12 = a21 = 0), the equilibrium law vonk U / log(Dz / z0)
+// as fallback, the rough-wall integrals and stresses.  Kept as written: the Lvv integral
+// has -3 z0^2/Dz^2 where Luu has +3, and tauwy is (vonk * iwmpz0)^2 ... with iwmpz0 an
+// undeclared, zero-valued name, so tauwy = 0 (times dVelzB dudzB) off the fallback.
+template <typename ST>
+static void iwm_wallstress_rough(Orc &g, ST &st, double Y0, double wm_dt) {
+    const int N1M = g.N1M, N3M = g.N3M;
+    const double vonk = 0.4, wm_tol = 0.000001, wm_eps = 0.000000001;
+    const int MaxIter = 1500;
+    (void)Y0;
+    for (int I = 1; I <= N1M; I++)
+        for (int K = 1; K <= N3M; K++) {
+            const double lhsx = st(I, K, IW_LHSX), lhsy = st(I, K, IW_LHSY);
+            const double Ux = st(I, K, IW_FTX), Uy = st(I, K, IW_FTY), Dz = st(I, K, IW_DZ), z0 = st(I, K, IW_Z0);
+            double &utx = st(I, K, IW_UTX), &uty = st(I, K, IW_UTY);
+            double fx, fy, fxp, fyp;
+            iwm_slv_rough(lhsx, lhsy, Ux, Uy, Dz, z0, utx, uty, fx, fy);
+            int iter = 0, equil_flag = 0;
+            while (std::max(std::fabs(fx), std::fabs(fy)) > wm_tol) {
+                iwm_slv_rough(lhsx, lhsy, Ux, Uy, Dz, z0, utx + wm_eps, uty, fxp, fyp);
+                const double a11 = (fxp - fx) / wm_eps, a21 = 0.0;
+                iwm_slv_rough(lhsx, lhsy, Ux, Uy, Dz, z0, utx, uty + wm_eps, fxp, fyp);
+                const double a12 = 0.0, a22 = (fyp - fy) / wm_eps;
+                const double det = a11 * a22 - a12 * a21;
+                const double nx = utx - (a22 * fx - a12 * fy) / det;
+                const double ny = uty - (-a21 * fx + a11 * fy) / det;
+                utx = nx;
+                uty = ny;
+                iwm_slv_rough(lhsx, lhsy, Ux, Uy, Dz, z0, utx, uty, fx, fy);
+                iter = iter + 1;
+                if (iter > MaxIter) {
+                    equil_flag = 1;
+                    break;
+                }
+            }
+            if (utx - 1.0 == utx || uty - 1.0 == uty) equil_flag = 1;
+            const double lg = std::log(Dz / z0);
+            const double equilutx = vonk * Ux / lg, equiluty = vonk * Uy / lg;
+            if (equil_flag == 1) {
+                utx = equilutx;
+                uty = equiluty;
+            }
+            double Ax = 0.0, Ay = 0.0;
+            if (equil_flag != 1) {
+                Ax = (Ux - utx / vonk * lg) / ((1.0 - z0 / Dz));
+                Ay = (Uy - uty / vonk * lg) / ((1.0 - z0 / Dz));
+            }
+            st(I, K, IW_AX) = Ax;
+            st(I, K, IW_AY) = Ay;
+            for (int q = 0; q < 5; q++) st(I, K, IW_INTEM + q) = st(I, K, IW_INTE + q);
+            const double px = utx, py = uty, r = z0 / Dz;
+            const double P4 = 1.0 - 4.0 * r + 3.0 * std::pow(z0, 2.0) / std::pow(Dz, 2.0) - 2.0 * lg + 4.0 * r * lg;
+            const double M4 = 1.0 - 4.0 * r - 3.0 * std::pow(z0, 2.0) / std::pow(Dz, 2.0) - 2.0 * lg + 4.0 * r * lg;
+            st(I, K, IW_INTE + IW_LU) = 1.0 / 2.0 * Dz * Ax * std::pow(1.0 - r, 2.0) + 1.0 / vonk * px * Dz * (r - 1.0 + lg);
+            st(I, K, IW_INTE + IW_LV) = 1.0 / 2.0 * Dz * Ay * std::pow(1.0 - r, 2.0) + 1.0 / vonk * py * Dz * (r - 1.0 + lg);
+            st(I, K, IW_INTE + IW_LUV) = 1.0 / std::pow(vonk, 2.0) * px * py * Dz * (1.0 - 2 * r + std::pow(1.0 - lg, 2.0)) +
+                                         1.0 / 3.0 * Ax * Ay * Dz * std::pow(1.0 - r, 3.0) -
+                                         1.0 / 4.0 / vonk * (Ax * py + Ay * px) * Dz * P4;
+            st(I, K, IW_INTE + IW_LUU) = 1.0 / std::pow(vonk, 2.0) * std::pow(px, 2.0) * Dz *
+                                             (std::pow(lg - 1.0, 2.0) - 2.0 * r + 1.0) +
+                                         1.0 / 3.0 * std::pow(Ax, 2.0) * Dz * std::pow(1.0 - r, 3.0) -
+                                         1.0 / 2.0 / vonk * px * Ax * Dz * P4;
+            st(I, K, IW_INTE + IW_LVV) = 1.0 / std::pow(vonk, 2.0) * std::pow(py, 2.0) * Dz *
+                                             (std::pow(lg - 1.0, 2.0) - 2.0 * r + 1.0) +
+                                         1.0 / 3.0 * std::pow(Ay, 2.0) * Dz * std::pow(1.0 - r, 3.0) -
+                                         1.0 / 2.0 / vonk * py * Ay * Dz * M4;
+            const double dTx = 1.0 / Dz * (Ax + px / vonk), dTy = 1.0 / Dz * (Ay + py / vonk);
+            const double dBx = 1.0 / Dz * Ax + px / vonk / z0, dBy = 1.0 / Dz * Ay + py / vonk / z0;
+            st(I, K, IW_DTX) = dTx;
+            st(I, K, IW_DTY) = dTy;
+            st(I, K, IW_DBX) = dBx;
+            st(I, K, IW_DBY) = dBy;
+            const double Vel = std::sqrt(std::pow(Ux, 2.0) + std::pow(Uy, 2.0));
+            const double dVelzT = std::fabs(Ux / Vel * dTx + Uy / Vel * dTy);
+            const double dVelzB = std::sqrt(std::pow(dBx, 2.0) + std::pow(dBy, 2.0));
+            st(I, K, IW_DIFFX) = std::pow(vonk * Dz, 2.0) * dVelzT * dTx - std::pow(vonk * z0, 2.0) * dVelzB * dBx;
+            st(I, K, IW_DIFFY) = std::pow(vonk * Dz, 2.0) * dVelzT * dTy - std::pow(vonk * z0, 2.0) * dVelzB * dBy;
+            if (equil_flag == 1) {
+                const double equilWMpara = std::sqrt(std::pow(Ux, 2.0) + std::pow(Uy, 2.0)) * std::pow(vonk, 2.0) /
+                                           std::pow(lg, 2.0);
+                st(I, K, IW_TAUWX) = equilWMpara * Ux;
+                st(I, K, IW_TAUWY) = equilWMpara * Uy;
+            } else {
+                const double iwmpz0 = 0.0;
+                st(I, K, IW_TAUWX) = std::pow(vonk * z0, 2.0) * dVelzB * dBx;
+                st(I, K, IW_TAUWY) = std::pow(vonk * iwmpz0, 2.0) * dVelzB * dBy;
+            }
+            const double utaup = std::pow(std::pow(st(I, K, IW_TAUWX), 2.0) + std::pow(st(I, K, IW_TAUWY), 2.0), 0.25);
+            st(I, K, IW_FUS) = st(I, K, IW_FUS) * (1.0 - st(I, K, IW_TR)) + utaup * st(I, K, IW_TR);
+            st(I, K, IW_TR) = wm_dt / (st(I, K, IW_DZ) / st(I, K, IW_FUS) / vonk);
+            if (st(I, K, IW_TR) > 1.0) st(I, K, IW_TR) = 1.0;
+        }
+}
+
 int wallmodel_iwmles(Orc &g, const double *U, const double *P, int NTIME, double DT, double PRESG, double PRESG3) {
     const int N1M = g.N1M, N3M = g.N3M;
     const size_t NP = (size_t)N1M * N3M;
     const double RE = g.RE, reinv = 1.0 / RE, vonk = 0.4;
     auto st = [&](int I, int K, int q) -> double & { return g.IWM[(size_t)q * NP + (I - 1) + (size_t)N1M * (K - 1)]; };
     const double Dzp = g.DY[1] + g.DY[2] + g.DY[3] / 2.0;
-    if (NTIME == 1 || !g.iwm_ready) {   // iwm_init_smooth (compact3d.f:3561-3714)
+    // WALLMODEL_IWMLES_ROUGH (Y0 = Y(0) != 0, compact3d.f:2562-3381): the same filter, left-
+    // hand side and schedule with the rough-wall profile (roughness length z0 = Y0)
+    const bool rough = g.Y[0] != 0.0;
+    const double Y0 = g.Y[0];
+    if (NTIME == 1 || !g.iwm_ready) {   // iwm_init_smooth / iwm_init_rough (3561-3714, 2736-2857)
         g.IWM.assign(NP * IW_NS, 0.0);
         double uinit = 0.0;
         for (int K = 1; K <= N3M; K++)
             for (int I = 1; I <= N1M; I++) uinit = uinit + U[g.iuc(I, 3, K, 1)];
         uinit = uinit / (double)(N1M * N3M);
-        const double usinit = iwm_loglaw(uinit, Dzp, RE);
+        const double usinit = rough ? uinit * vonk / std::log(Dzp / Y0) : iwm_loglaw(uinit, Dzp, RE);
         for (int I = 1; I <= N1M; I++)
             for (int K = 1; K <= N3M; K++) {
                 st(I, K, IW_UTX) = usinit;
@@ -2253,8 +2366,13 @@ int wallmodel_iwmles(Orc &g, const double *U, const double *P, int NTIME, double
                 st(I, K, IW_FUS) = usinit;
                 st(I, K, IW_TR) = (g.CFLMAX * g.ALX / N1M / uinit) / (Dzp / vonk / usinit);
                 st(I, K, IW_DZ) = Dzp;
-                st(I, K, IW_DELI) = std::min(11.0 * reinv / usinit, Dzp);
-                st(I, K, IW_DELV) = reinv / usinit;
+                if (rough) {
+                    st(I, K, IW_DBX) = usinit / vonk / Y0;
+                    st(I, K, IW_Z0) = Y0;
+                } else {
+                    st(I, K, IW_DELI) = std::min(11.0 * reinv / usinit, Dzp);
+                    st(I, K, IW_DELV) = reinv / usinit;
+                }
             }
         g.WM_DT = 5 * DT;
         g.iwm_ready = 1;
@@ -2303,6 +2421,7 @@ int wallmodel_iwmles(Orc &g, const double *U, const double *P, int NTIME, double
                                     wm_dt * (st(I, K, IW_CONVY) + st(I, K, IW_PRSY) - st(I, K, IW_DIFFY));
             }
         }
+        if (rough) iwm_wallstress_rough(g, st, Y0, wm_dt);
         // iwm_calc_wallstress_smooth (3930-4279)
         const double KAPA = 0.4, B = 5.0, deltap = Dzp;
         const int MaxIter = 1500;
@@ -2314,7 +2433,7 @@ int wallmodel_iwmles(Orc &g, const double *U, const double *P, int NTIME, double
         // fallback of its own takes the values of the last point (I outer, K inner) that
         // had one (zero before the first)
         double equilutx = 0.0, equiluty = 0.0;
-        for (int I = 1; I <= N1M; I++)
+        for (int I = 1; I <= (rough ? 0 : N1M); I++)
             for (int K = 1; K <= N3M; K++) {
                 const double lhsx = st(I, K, IW_LHSX), lhsy = st(I, K, IW_LHSY);
                 const double Ux = st(I, K, IW_FTX), Uy = st(I, K, IW_FTY), Dz = st(I, K, IW_DZ);

@@ -111,10 +111,12 @@ def test_shifted_wall_models_check_the_y_faces(L):
     assert b"H(1)" in L.c3d_last_error()
 
 
-def test_iwmles_rough_refused(L):
-    """Y(0) = Y0 != 0 with WMODEL 2 selects WALLMODEL_IWMLES_ROUGH, which is not built."""
-    g, _ = make_grid("les32cs", wmodel=2, y0=0.01)
-    s = g.struct()
-    h = ctypes.c_void_p()
-    assert L.c3d_create(ctypes.byref(s), ctypes.byref(h)) == -1
-    assert b"IWMLES_ROUGH" in L.c3d_last_error()
+def test_rough_models_need_y0_below_the_sample_height(L):
+    """Y(0) = Y0 != 0 selects the rough-wall models (WMODEL 1: WALLMODEL_ROUGH, 2:
+    WALLMODEL_IWMLES_ROUGH), whose log(DELTAP / Y0) needs 0 < Y0 < DY(1)+DY(2)+DY(3)/2."""
+    for wmodel, name in ((1, b"WALLMODEL_ROUGH"), (2, b"IWMLES_ROUGH")):
+        g, _ = make_grid("les32cs", wmodel=wmodel, y0=-0.01)
+        s = g.struct()
+        h = ctypes.c_void_p()
+        assert L.c3d_create(ctypes.byref(s), ctypes.byref(h)) == -1
+        assert name in L.c3d_last_error()

@@ -155,12 +155,14 @@ def test_les_wall_model_iteration_cap(libc3d, oracle_mod):
     assert np.isfinite(Ug).all()
 
 
-@pytest.mark.parametrize("name,over", [("les32cs", dict(wmodel=2)), ("les32dy", dict(wmodel=2, n2m=64))])
-def test_iwmles_steps_fp64(libc3d, oracle_mod, name, over):
-    """WALLMODEL_IWMLES_SMOOTH (WMODEL 2) from NTIME = 1 on both sides for 12 steps (two
-    model updates): wall stresses and WSM(1) within 1e-8 after every step (the Newton
-    Jacobian differences the residual over 1e-9, which amplifies last-bit differences of
-    pow and log), the field within 1e-9 at the end."""
+@pytest.mark.parametrize("name,over,tol", [("les32cs", dict(wmodel=2), 1e-8), ("les32dy", dict(wmodel=2, n2m=64), 1e-8),
+                                           ("les32cs", dict(wmodel=2, y0=1e-3), 1e-7)])
+def test_iwmles_steps_fp64(libc3d, oracle_mod, name, over, tol):
+    """WALLMODEL_IWMLES_SMOOTH / _ROUGH (WMODEL 2) from NTIME = 1 on both sides for 12 steps
+    (two model updates): wall stresses and WSM(1) within 1e-8 (rough: 1e-7, its stress is a
+    product of three Newton-derived factors) after every step (the Newton Jacobian
+    differences the residual over 1e-9, which amplifies last-bit differences of pow and
+    log), the field within 1e-9 at the end."""
     g, dt = make_grid(name, **over)
     orc = oracle_mod.Oracle(g)
     orc.set_cflmax(0.5)
@@ -178,9 +180,9 @@ def test_iwmles_steps_fp64(libc3d, oracle_mod, name, over):
         tw, tb, wsm = orc.get_wall()
         twg, tbg = ch.download_wall()
         scale = max(np.abs(tw[isl]).max(), 1e-300)
-        assert np.abs(twg[isl] - tw[isl]).max() <= 1e-8 * scale, n
-        assert np.abs(tbg[isl] - tb[isl]).max() <= 1e-8 * max(scale, np.abs(tb[isl]).max()), n
-        assert ch.get_wsm()[0] == pytest.approx(wsm[0], rel=1e-8, abs=1e-300), n
+        assert np.abs(twg[isl] - tw[isl]).max() <= tol * scale, n
+        assert np.abs(tbg[isl] - tb[isl]).max() <= tol * max(scale, np.abs(tb[isl]).max()), n
+        assert ch.get_wsm()[0] == pytest.approx(wsm[0], rel=tol, abs=1e-300), n
     Ug, Pg, Hg = ch.download()
     a, b = interior(g, Ug, Pg, Hg), interior(g, U, P, HH)
     for f in ("u", "v", "w"):

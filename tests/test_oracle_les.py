@@ -688,3 +688,25 @@ def test_rough_wall_model_log_law(oracle_mod):
     np.testing.assert_allclose(tw[1:g.n1m + 1, 1:g.n3m + 1, 0], t1 * u / mag, rtol=1e-13)
     np.testing.assert_allclose(tb[1:g.n1m + 1, 1:g.n3m + 1, 0], t1 * w / mag, rtol=1e-13)
     assert wsm[0] == pytest.approx(t1.mean(), rel=1e-13)
+
+
+def test_iwmles_rough_initial_stress(oracle_mod):
+    """WALLMODEL_IWMLES_ROUGH (WMODEL 2 with Y0 != 0, compact3d.f:2562-3381): until the first
+    update the imposed stress is u_tau^2 with u_tau = 0.4 <u(3)> / log(Dzp / Y0)
+    (iwm_init_rough), the spanwise stress is 0, and the updates keep the field finite."""
+    g, dt = _grid("les32cs", wmodel=2, y0=1e-3)
+    o = oracle_mod.Oracle(g)
+    o.set_cflmax(0.5)
+    U, P, HH = ic.loglaw(g, 2000.0)
+    o.project(U)
+    dzp = g.arrays["dy"][1] + g.arrays["dy"][2] + g.arrays["dy"][3] / 2.0
+    us0 = U[1:g.n1m + 1, 3, 1:g.n3m + 1, 0].mean() * 0.4 / math.log(dzp / 1e-3)
+    S = g.zeros_s()
+    pg = pg3 = 0.0
+    for n in range(1, 12):
+        pg, pg3 = o.getup(U, P, HH, n, dt, pg, pg3, S)
+        tw, tb, wsm = o.get_wall()
+        if n < 5:
+            np.testing.assert_allclose(tw[1:g.n1m + 1, 1:g.n3m + 1, 0], us0 ** 2, rtol=1e-12)
+            assert np.abs(tb[1:g.n1m + 1, 1:g.n3m + 1, 0]).max() == 0.0
+    assert np.isfinite(U).all() and np.isfinite(tw).all()
