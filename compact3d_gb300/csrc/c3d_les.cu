@@ -9,10 +9,19 @@
 //               velocities and their products
 //   sgs_dyn     SGSDY: FILTER (5190-5228) of those, M_ij, L_ij, the plane sums, SMAGC(J)
 //               and nu, one block per plane
+//   sgs_sd_*    SGSSD (1502-1948): both test filters, the Germano sums, the quintic's
+//               root by CHHQR (11571-11676) and SMAGC; sgs_apply: nu
 //   wall        WALLMODEL_INSTANT (2319-2493): damped Newton for u_tau per wall point
+//   wall_rough  WALLMODEL_ROUGH (2496-2558): the rough-wall log law
+//   wall_werner WALLMODEL_WERNER (4815-4958): the Werner-Wengle power law, both walls
+//   wall_shift* MARUSIC1 (4336-4495) and PIOMELLI (4960-5110): plane-mean log law and
+//               INDEX_IJK / INTERPOLAT (12602-12807) at shifted points
 //   wall_sum    WSM(1) = plane mean of TAUW1; non-converged points -> error flag
 //   les_x1/z1/z2/x2   the SGS fluxes of RHS1/2/3 (6436-6770, 6857-6866, 7088-7393,
 //               7774-8111) and the wall-stress terms (6765-6770, 8095-8101)
+//   par_*       the particle step and SOURCE_PAR (11882-12470, 2029-2075), which share
+//               the MESH02 tables and interpolation of the shifted wall models
+// (WALLMODEL_IWMLES_SMOOTH / _ROUGH are in c3d_iwm.cu.)
 //
 // The reference solves each SGS flux separately (36 compact line solves per step).  The
 // sums of fluxes that share an edge viscosity are linear in it, so the kernels form the
