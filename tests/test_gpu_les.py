@@ -1,8 +1,12 @@
-"""GPU parity of the wall-modelled LES step (FILES != 0) against the FP64 oracle.
+"""GPU parity of the wall-modelled LES step (FILES != 0) against the FP64 oracle: the SGS
+models SGSDY, SGSCS and SGSSD with the wall models INSTANT, ROUGH, IWMLES (smooth and
+rough), MARUSIC1, WERNER and PIOMELLI, and no-slip walls.
 
 Tolerances (relative L2 over the interior unless stated):
   * FP64 form, one step: 1e-10 for U, V, W, HH and SGSVIS, 1e-8 for P, 1e-12 for the
-    wall stresses TAUW/TAUB and WSM(1) (the Newton iteration is the same arithmetic).
+    wall stresses TAUW/TAUB and WSM(1) (the wall models are the same arithmetic).
+  * IWMLES from NTIME = 1 over 12 steps: stresses 1e-8 (rough 1e-7) per step, the field
+    1e-9 (its Newton Jacobian differences the residual over 1e-9 in u_tau).
   * FP64 form, 10 steps: 1e-9 for U, V, W.
   * mixed form against the FP64 GPU form after 20 steps: 1e-4 for U, V, W, 1e-3 for the
     mean wall stress (FP32 line solves and SGS fluxes; FP64 wall model and reductions).
