@@ -94,16 +94,67 @@ class Dist:
 # clocks during the timed region
 # ------------------------------------------------------------------------------------
 class Clocks:
+    """SM clock, power and throttle reasons sampled every 10 ms during the timed region.
+
+    NVML is read through ctypes (libnvidia-ml.so.1, the driver's own library; reading
+    changes no setting).  The device is found by the CUDA device's UUID, so the index
+    mapping of CUDA_VISIBLE_DEVICES does not matter.  Without NVML, ``nvidia-smi -lms``
+    samples instead (200 ms apart)."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # NVML clock-event reason bits
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
 
-    def __init__(self, gpu: int):
+    def __init__(self, gpu: int, interval_s: float = 0.01):
         self.gpu = gpu
+        self.interval = interval_s
         self.proc = None
         self.path = None
+        self.nv = None
+        self.thread = None
+        try:
+            self._nvml_open()
+        except Exception:
+            self.nv = None
+
+    def _nvml_open(self):
+        import ctypes
+        import torch
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit")
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(self.gpu).uuid)
+        h = ctypes.c_void_p()
+        if nv.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(h)) != 0:
+            raise RuntimeError("nvmlDeviceGetHandleByUUID")
+        self.h = h
+        self.nv = nv
+        self.reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))   # NVML_CLOCK_SM = 1
+        self.max_mhz = float(mx.value)
+
+    def _sample_loop(self):
+        import ctypes
+        mhz, mw, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop_flag:
+            ok = self.nv.nvmlDeviceGetClockInfo(self.h, 1, ctypes.byref(mhz)) == 0
+            self.nv.nvmlDeviceGetPowerUsage(self.h, ctypes.byref(mw))
+            self.reasons_fn(self.h, ctypes.byref(rs))
+            if ok:
+                self.rows.append((float(mhz.value), mw.value / 1e3, int(rs.value)))
+            time.sleep(self.interval)
 
     def start(self):
+        if self.nv is not None:
+            import threading
+            self.rows = []
+            self.stop_flag = False
+            self.thread = threading.Thread(target=self._sample_loop, daemon=True)
+            self.thread.start()
+            return
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
@@ -115,6 +166,17 @@ class Clocks:
             self.proc = None
 
     def stop(self) -> dict | None:
+        if self.thread is not None:
+            self.stop_flag = True
+            self.thread.join()
+            self.thread = None
+            rows = self.rows
+            if not rows:
+                return None
+            reasons = sorted({k for r in rows for k, b in self.BITS.items() if r[2] & b})
+            return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": self.max_mhz,
+                    "power_w_max": max(r[1] for r in rows), "reasons": reasons, "samples": len(rows),
+                    "source": f"NVML every {self.interval * 1e3:.0f} ms"}
         if self.proc is None:
             return None
         time.sleep(0.25)
@@ -138,7 +200,7 @@ class Clocks:
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "source": "nvidia-smi every 200 ms"}
 
 
 class L2Flush:
@@ -198,45 +260,47 @@ def traffic_for(workload: str, form: str, kernel: str):
 # ------------------------------------------------------------------------------------
 # CPU reference (oracle restatement of the reference's OpenMP path)
 # ------------------------------------------------------------------------------------
-def cpu_reference(workload: str, steps: int, warmup: int, budget_s: float = 150.0):
-    """Run the FP64 OpenMP oracle on a bounded sample of `workload`: the same x-z plane
-    (line lengths, FFT sizes) with the wall-normal extent reduced so that the run fits the
-    budget.  Returns (rate pt-steps/s, cores, sample description)."""
+def cpu_reference(workload: str, steps: int, warmup: int):
+    """Run the FP64 OpenMP oracle (the restatement of the reference's GETUP and its
+    OpenMP loops) on the whole `workload` grid, on all host cores: `warmup` untimed
+    steps, then exactly `steps` timed steps (host wall clock).  Returns (rate in
+    pt-steps/s, seconds per step, cores, sample description)."""
     import oracle
     oracle.build()
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
-    w = WORKLOADS[workload]
-    n2s = w["n2m"]
-    # per-point cost is nearly independent of N2M; take a slab of at most 32 cells
-    n2s = min(n2s, 32)
-    g, dt = make_grid(workload, n2m=n2s)
+    g, dt = make_grid(workload)
     orc = oracle.Oracle(g, threads=cores)
     U, P, HH = ic.perturbed_laminar(g)
     orc.project(U)
     pg = pg3 = 0.0
     n = 1
-    for _ in range(max(1, min(warmup, 1))):
+    for _ in range(warmup):
         pg, pg3 = orc.getup(U, P, HH, n, dt, pg, pg3)
         n += 1
+    steps = max(1, steps)
     t0 = time.perf_counter()
-    done = 0
-    for _ in range(max(1, steps)):
+    for _ in range(steps):
         pg, pg3 = orc.getup(U, P, HH, n, dt, pg, pg3)
         n += 1
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
     t = time.perf_counter() - t0
-    rate = g.points * done / t
-    sample = (f"{done} full GETUP steps on a {g.n1m}x{g.n2m}x{g.n3m} slab of {workload} "
-              f"(same x-z plane, {g.n2m} of {w['n2m']} wall-normal cells), FP64, {cores} OpenMP threads")
-    return rate, cores, sample
+    rate = g.points * steps / t
+    sample = (f"{steps} timed GETUP steps (after {warmup} untimed) on the whole {workload} grid, "
+              f"{g.n1m}x{g.n2m}x{g.n3m} cells, FP64, {cores} OpenMP threads")
+    return rate, t / steps, cores, sample
 
 
 # ------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------
+def workload_config(args, g, dt, form):
+    """The `config` object both arms print for the workload."""
+    return dict(workload=f"{args.workload}: {g.n1m}x{g.n2m + 1}x{g.n3m} points "
+                         f"(cells {g.n1m}x{g.n2m}x{g.n3m}), RE={g.re}, dt={dt}, "
+                         + (f"y tanh-stretched beta={g.cks}" if g.wmodel == 0 else "uniform y"),
+                form=form, cells=[g.n1m, g.n2m, g.n3m])
+
+
 FORMS = {"mixed": C3D_MIXED, "fp64": C3D_FP64, "mixed_ir": C3D_MIXED_IR}
 
 
@@ -297,14 +361,11 @@ def run_ours(args, D: Dist):
     res = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=D.world, steps=K, warmup=W,
                ms_per_step=ms_max / K, higher_is_better=True, scaling="weak", vs_baseline=None,
                dtype="f64" if args.form == "fp64" else "f32+f64 mixed", data="synthetic")
-    res["config"] = dict(workload=f"{args.workload}: {g.n1m}x{g.n2m + 1}x{g.n3m} points "
-                                  f"(cells {g.n1m}x{g.n2m}x{g.n3m}), RE={g.re}, dt={dt}, "
-                                  + (f"y tanh-stretched beta={g.cks}" if g.wmodel == 0 else "uniform y"),
-                         form=args.form, cells=[g.n1m, g.n2m, g.n3m],
-                         l2_policy=(f"L2 flushed (512 MB written) before every timed step, each step timed alone; "
-                                    f"each FP64 field is {field_bytes / 1e6:.0f} MB" if small else
-                                    f"inputs larger than L2: each FP64 field is {field_bytes / 1e6:.0f} MB"),
-                         parallelism=f"replicas x{D.world}")
+    res["config"] = workload_config(args, g, dt, args.form)
+    res["config"]["l2_policy"] = (f"L2 flushed (512 MB written) before every timed step, each step timed alone; "
+                                  f"each FP64 field is {field_bytes / 1e6:.0f} MB" if small else
+                                  f"inputs larger than L2: each FP64 field is {field_bytes / 1e6:.0f} MB")
+    res["config"]["parallelism"] = f"replicas x{D.world}"
     res["gpu_launches"] = launches_per_step * K
     res["schedule"] = schedule
     if ck:
@@ -327,6 +388,14 @@ def run_ours(args, D: Dist):
                            traffic=traffic_for(args.workload, args.form, dom["name"]),
                            alg_bytes_per_launch=dom["bytes"], avg_launch_ms=avg_ms)
     step_ms = sum(e["ms"] for e in prof) / 2
+    # whole step against the five-pass plane-fused schedule's algorithmic bytes per
+    # grid-point-substep (264 B mixed, 320 B FP64), and the bytes the kernels of this
+    # build are specified to move per point
+    b_alg = 320.0 if args.form == "fp64" else 264.0
+    step_gbs = value / D.world * b_alg / 1e9
+    res["step_roofline"] = dict(bytes_per_point=b_alg, achieved=step_gbs, peak=peak, unit="GB/s",
+                                frac=step_gbs / peak, peak_kind=kind,
+                                kernel_bytes_per_point=sum(e["bytes"] for e in prof) / 2 / pts)
     res["kernels"] = {e["name"]: dict(ms=e["ms"] / e["launches"], share=e["ms"] / (2 * step_ms),
                                       gbs=e["bytes"] / (e["ms"] / e["launches"] / 1e3) / 1e9)
                       for e in prof}
@@ -427,9 +496,45 @@ def run_ours(args, D: Dist):
 
     # ---- CPU baseline (rank 0, N=1 only) ----
     if D.rank == 0 and D.world == 1 and not args.no_cpu:
-        rate, cores, sample = cpu_reference(args.workload, steps=3, warmup=1, budget_s=40.0)
+        rate, _, cores, sample = cpu_reference(args.workload, steps=2, warmup=1)
         res["cpu_baseline"] = dict(value=rate, unit=UNIT, cores=cores, kind="port", sample=sample)
-    return res
+    return with_summary(res)
+
+
+def with_summary(res: dict) -> dict:
+    """Orders the line so that the long per-kernel and per-section tables come first and a
+    compact summary of every form's headline figure comes last (the end of the line is
+    what a truncated log keeps)."""
+    big = ("kernels", "schedule", "operators", "next_rows", "les", "batched", "err_vs_fp64")
+    out = {k: v for k, v in res.items() if k not in big}
+    tail = {k: res[k] for k in big if k in res}
+    summ = dict(mixed=res["value"], ms_per_step=res["ms_per_step"])
+    for k in ("fp64", "mixed_ir"):
+        if k in res:
+            summ[k] = res[k]["value"]
+    b = res.get("batched")
+    if b:
+        summ["batched"] = b["value"]
+        for k in ("mixed_sequential", "fp64_sequential"):
+            if k in b:
+                summ["batched_" + k] = b[k]["value"]
+    e = res.get("err_vs_fp64")
+    if e and "mixed" in e:
+        summ["err_vs_fp64"] = {k: e["mixed"][k] for k in ("u", "v", "w", "p", "divmax", "bulk_rel", "wsm_rel")}
+        summ["err_vs_fp64"]["steps"] = e["steps"]
+    l_ = res.get("les")
+    if l_:
+        summ["les128_ms"] = {f: l_[f]["ms_per_step"] for f in ("mixed", "fp64") if f in l_}
+    for k in ("roofline", "step_roofline"):
+        if k in res:
+            summ[k + "_frac"] = res[k]["frac"]
+    if "e2e" in res:
+        summ["e2e"] = res["e2e"]["value"]
+    if "cpu_baseline" in res:
+        summ["cpu_baseline"] = res["cpu_baseline"]["value"]
+    out.update(tail)
+    out["summary"] = summ
+    return out
 
 
 def flow_stats(U, g):
@@ -760,41 +865,44 @@ def run_batched(args, D: Dist):
                form="mixed, one CUDA graph per ensemble step",
                workload="32 channels: Nx,Nz in {48,64,96,128}, Ny in {33,49,65,97}, "
                         "Re_bulk in [3000,12000], seeded")
-    # the same channels, one after another, plain FP64
-    t_seq = 0.0
-    k_seq = max(2, min(K, args.fp64_steps))
-    for i, g in enumerate(grids):
-        g64, _ = g, dt
-        c = lib.Channel(g64, C3D_FP64)
-        U, P, HH = ics[i]
-        c.upload(U, P, HH)
-        c.project()
-        if not args.no_tune:
-            c.autotune()
-        c.set_presg(0.0, 0.0)
-        for s_ in range(1, 3):
-            c.step_async(s_, dt)
-        c.sync()
-        c.timer_start()
-        for s_ in range(k_seq):
-            c.step_async(3 + s_, dt)
-        t_seq += c.timer_stop()
-        c.close()
-    t_seq = D.max(t_seq)
-    out["fp64_sequential"] = dict(value=tot * k_seq / (t_seq / 1e3), ms_per_step=t_seq / k_seq, steps=k_seq)
+    # the same channels, one after another: plain FP64, and the mixed form without the
+    # graph (so that the batching gain and the precision gain can be told apart)
+    for key, prec, k_seq in (("fp64_sequential", C3D_FP64, max(2, min(K, args.fp64_steps))),
+                             ("mixed_sequential", C3D_MIXED, max(2, min(K, 20)))):
+        t_seq = 0.0
+        for i, g in enumerate(grids):
+            c = lib.Channel(g, prec)
+            U, P, HH = ics[i]
+            c.upload(U, P, HH)
+            c.project()
+            if not args.no_tune:
+                c.autotune()
+            c.set_presg(0.0, 0.0)
+            for s_ in range(1, 3):
+                c.step_async(s_, dt)
+            c.sync()
+            c.timer_start()
+            for s_ in range(k_seq):
+                c.step_async(3 + s_, dt)
+            t_seq += c.timer_stop()
+            c.close()
+        t_seq = D.max(t_seq)
+        out[key] = dict(value=tot * k_seq / (t_seq / 1e3), ms_per_step=t_seq / k_seq, steps=k_seq)
     return out
 
 
 def run_reference(args, D: Dist):
+    """The reference arm: the FP64 OpenMP restatement of the reference step on the host
+    cores, on the same workload grid as the GPU arm, every step a full GETUP."""
     if D.rank != 0:
         return None
-    rate, cores, sample = cpu_reference(args.workload, steps=args.steps, warmup=args.warmup, budget_s=150.0)
+    K, W = args.steps, args.warmup
+    rate, s_per_step, cores, sample = cpu_reference(args.workload, steps=K, warmup=W)
     g, dt = make_grid(args.workload)
-    res = dict(impl="reference", metric=METRIC, value=rate, unit=UNIT, n_gpus=D.world, steps=args.steps,
-               warmup=args.warmup, ms_per_step=g.points / rate * 1e3, higher_is_better=True,
+    res = dict(impl="reference", metric=METRIC, value=rate, unit=UNIT, n_gpus=D.world, steps=K,
+               warmup=W, ms_per_step=s_per_step * 1e3, higher_is_better=True,
                scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
-               config=dict(workload=f"{args.workload}: {g.n1m}x{g.n2m + 1}x{g.n3m} points, RE={g.re}, dt={dt}",
-                           form="fp64-cpu", cells=[g.n1m, g.n2m, g.n3m]))
+               config=workload_config(args, g, dt, "fp64-cpu"))
     res["cpu_baseline"] = dict(value=rate, unit=UNIT, cores=cores, kind="port", sample=sample)
     res["e2e"] = dict(value=rate, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0)
     return res
@@ -803,7 +911,8 @@ def run_reference(args, D: Dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 200 for the GPU arm, 20 for the CPU reference arm)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="channel384", choices=sorted(WORKLOADS))
@@ -824,6 +933,8 @@ def main():
     ap.add_argument("--les-steps", type=int, default=200)
     ap.add_argument("--nchan", type=int, default=32)
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 20 if args.impl == "reference" else 200
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     D = Dist()

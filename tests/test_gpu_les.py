@@ -3,7 +3,7 @@ models SGSDY, SGSCS and SGSSD with the wall models INSTANT, ROUGH, IWMLES (smoot
 rough), MARUSIC1, WERNER and PIOMELLI, and no-slip walls.
 
 Tolerances (relative L2 over the interior unless stated):
-  * FP64 form, one step: 1e-10 for U, V, W, HH and SGSVIS, 1e-8 for P, 1e-12 for the
+  * FP64 form, one step: 1e-10 for U, V, W, HH, P and SGSVIS, 1e-12 for the
     wall stresses TAUW/TAUB and WSM(1) (the wall models are the same arithmetic).
   * IWMLES from NTIME = 1 over 12 steps: stresses 1e-8 (rough 1e-7) per step, the field
     1e-9 (its Newton Jacobian differences the residual over 1e-9 in u_tau).
@@ -92,7 +92,7 @@ def test_les_one_step_fp64(libc3d, oracle_mod, name, over):
     a, b = interior(g, Ug, Pg, Hg), interior(g, U, P, HH)
     for f in ("u", "v", "w", "hh"):
         assert rel(a[f], b[f]) < 1e-10, (f, rel(a[f], b[f]))
-    assert rel(a["p"], b["p"]) < 1e-8, rel(a["p"], b["p"])
+    assert rel(a["p"], b["p"]) < 1e-10, rel(a["p"], b["p"])
     Sg = ch.download_sgsvis()
     sl = (slice(1, g.n1m + 1), slice(0, g.n2m + 2), slice(1, g.n3m + 1))
     assert np.abs(S[sl]).max() > 0
