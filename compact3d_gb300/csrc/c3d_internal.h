@@ -113,6 +113,7 @@ struct Tune {
     int zsplit;   // zA as one kernel (0) or as its three sweeps in three kernels (1)
     int xsplit;   // xA as one kernel (0) or as its u, v, w pieces in three kernels (1)
     int xbulk;    // x passes with rows staged by a bulk-copy ring of this many stages (0: off)
+    int xstage;   // xA's pieces read their rows from global memory (0) or stage them in shared memory by bulk copies (1)
 };
 
 // Arguments of the pressure refinement (mixed form with C3D_MIXED_IR): double-float

@@ -20,6 +20,210 @@ namespace c3d {
 // ---------------------------------------------------------------------------------
 // xA
 // ---------------------------------------------------------------------------------
+// Rows of u, v, w and P at J-1, J, J+1 that the xA pieces read, and their slots in the
+// warp's shared-memory stage when the rows are staged by bulk copies.
+enum XaRow { XA_UM, XA_UC, XA_UP, XA_PM, XA_PC, XA_VM, XA_VC, XA_VP, XA_WM, XA_WC, XA_WP };
+template <int PART>
+__host__ __device__ constexpr int xa_slot(int r) {
+    return PART == 1 ? (r == XA_UM ? 0 : r == XA_UC ? 1 : r == XA_UP ? 2 : 3)
+         : PART == 2 ? (r == XA_VM ? 0 : r == XA_VC ? 1 : r == XA_VP ? 2 : r == XA_PM ? 3 : r == XA_PC ? 4
+                        : r == XA_UM ? 5 : 6)
+                     : (r == XA_WM ? 0 : r == XA_WC ? 1 : 2);
+}
+// The row r of (j, k): in global memory at offsets o (J), om (J-1), op (J+1), or slot
+// xa_slot(r) of the stage st (rows of n points).
+template <bool STG, int PART, typename R>
+__device__ __forceinline__ const typename SType<R>::S *xa_src(const StepArgs<R> &a, int r, long long o, long long om,
+                                                               long long op, const typename SType<R>::S *st, int n) {
+    if constexpr (STG) {
+        return st + (size_t)xa_slot<PART>(r) * n;
+    } else {
+        (void)st; (void)n;
+        switch (r) {
+            case XA_UM: return a.u + om;
+            case XA_UC: return a.u + o;
+            case XA_UP: return a.u + op;
+            case XA_PM: return a.p + om;
+            case XA_PC: return a.p + o;
+            case XA_VM: return a.v + om;
+            case XA_VC: return a.v + o;
+            case XA_VP: return a.v + op;
+            case XA_WM: return a.w + om;
+            case XA_WC: return a.w + o;
+            default: return a.w + op;
+        }
+    }
+}
+
+// Row operand of an x pass: a global row (read through the read-only path) or a row
+// already staged in shared memory by bulk copies.
+template <bool STG, typename T, int C>
+__device__ __forceinline__ void xrow(T (&v)[C], const T *p, T *sb, int lane, int P) {
+    if constexpr (STG) crow_load(v, p, lane, P);
+    else srow_load(v, p, sb, lane, P);
+}
+
+// One row (j, k) of the u (PART 1), v (PART 2, faces J >= 2) or w (PART 3) piece of xA.
+template <typename R, int C, int PART, bool STG>
+__device__ __forceinline__ void xa_piece(const StepArgs<R> &a, int j, long long o, long long om, long long op,
+                                         const typename SType<R>::S *st, typename SType<R>::S *sbS, R *sbR, int lane,
+                                         int P) {
+    typedef typename SType<R>::S S;
+    typedef St<R> ST;
+    const int n = a.g.n1m;
+    const R RE1 = a.re1, f12 = a.f12x, f24 = a.f24x, four = (R)4.0;
+    const R presg = (R)a.scal[SCAL_PRESG];
+    if (PART == 2 && j >= 2) {
+        // The v piece on its own, ordered so that few rows are live at once: the y
+        // stencils of V (HH2 stored), then -dP/dy, then the x terms of V (R2 stored),
+        // then E_xy with u at the y faces.
+        const R DYPj = a.m.dyp[j], DYCj = a.m.dyc[j], DYMj = a.m.dym[j], Z0 = a.m.dyz[j];
+        const R Hj1 = a.m.rh[j];
+        R acc[C];
+        {
+            S vc[C], vm[C], vp[C];
+            xrow<STG>(vc, xa_src<STG, PART>(a, XA_VC, o, om, op, st, n), sbS, lane, P);
+            xrow<STG>(vm, xa_src<STG, PART>(a, XA_VM, o, om, op, st, n), sbS, lane, P);
+            xrow<STG>(vp, xa_src<STG, PART>(a, XA_VP, o, om, op, st, n), sbS, lane, P);
+            R hh[C];
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                acc[t] = RE1 * ST::yvisc(DYPj, DYCj, DYMj, Z0, vp[t], vc[t], vm[t]);
+                hh[t] = Hj1 * Sten<R>::vv(vp[t], vc[t], vm[t]);
+            }
+            srow_store(a.hh[1] + o, hh, sbR, lane, P);
+        }
+        {
+            S pc[C], pm[C];
+            xrow<STG>(pc, xa_src<STG, PART>(a, XA_PC, o, om, op, st, n), sbS, lane, P);
+            xrow<STG>(pm, xa_src<STG, PART>(a, XA_PM, o, om, op, st, n), sbS, lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                R pg = ST::d(pc[t], pm[t]) * Hj1;
+                acc[t] = -pg + acc[t];
+            }
+        }
+        S vc[C];
+        xrow<STG>(vc, xa_src<STG, PART>(a, XA_VC, o, om, op, st, n), sbS, lane, P);
+        R d[C];
+        S pv = sprev(vc[C - 1], lane, P), nx = snext(vc[0], lane, P);
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            S l = (t == 0) ? pv : vc[t - 1], rr = (t == C - 1) ? nx : vc[t + 1];
+            d[t] = f12 * ST::d2(l, vc[t], rr);
+        }
+        xsolve(d, lane, P, a.c10x);
+#pragma unroll
+        for (int t = 0; t < C; ++t) acc[t] = acc[t] + RE1 * d[t];
+        srow_store(a.r[1] + o, acc, sbR, lane, P);
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            S l = (t == 0) ? pv : vc[t - 1];
+            d[t] = four * (ST::hi(l) + ST::hi(vc[t]));
+        }
+        xsolve(d, lane, P, a.c6x);
+        {   // u at the y faces
+            S uc[C], um[C];
+            xrow<STG>(uc, xa_src<STG, PART>(a, XA_UC, o, om, op, st, n), sbS, lane, P);
+            xrow<STG>(um, xa_src<STG, PART>(a, XA_UM, o, om, op, st, n), sbS, lane, P);
+            const R a1 = a.m.hdy[j], a2 = a.m.hdy[j - 1];
+#pragma unroll
+            for (int t = 0; t < C; ++t) d[t] = d[t] * (Hj1 * (a1 * ST::hi(um[t]) + a2 * ST::hi(uc[t])));
+        }
+        srow_store(a.exy + o, d, sbR, lane, P);
+    }
+    if (PART == 1) {
+        // The u piece on its own, ordered so that few rows are live at once: the y
+        // stencil of U, the x terms of U (HH1 stored), then -dP/dx (R1 stored).
+        const R HPj = a.m.hp[j], HCj = a.m.hc[j], HMj = a.m.hm[j], Z0 = a.m.hz[j];
+        R acc[C];
+        {
+            S um[C], up[C], uc0[C];
+            xrow<STG>(uc0, xa_src<STG, PART>(a, XA_UC, o, om, op, st, n), sbS, lane, P);
+            xrow<STG>(um, xa_src<STG, PART>(a, XA_UM, o, om, op, st, n), sbS, lane, P);
+            xrow<STG>(up, xa_src<STG, PART>(a, XA_UP, o, om, op, st, n), sbS, lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) acc[t] = RE1 * ST::yvisc(HPj, HCj, HMj, Z0, up[t], uc0[t], um[t]);
+        }
+        S uc[C];
+        xrow<STG>(uc, xa_src<STG, PART>(a, XA_UC, o, om, op, st, n), sbS, lane, P);
+        R d[C];
+        S pv = sprev(uc[C - 1], lane, P), nx = snext(uc[0], lane, P);
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            S l = (t == 0) ? pv : uc[t - 1], rr = (t == C - 1) ? nx : uc[t + 1];
+            d[t] = f12 * ST::d2(l, uc[t], rr);
+        }
+        xsolve(d, lane, P, a.c10x);
+#pragma unroll
+        for (int t = 0; t < C; ++t) acc[t] = acc[t] + RE1 * d[t];
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            S rr = (t == C - 1) ? nx : uc[t + 1];
+            d[t] = four * (ST::hi(uc[t]) + ST::hi(rr));
+        }
+        xsolve(d, lane, P, a.c6x);
+        R sq[C];
+#pragma unroll
+        for (int t = 0; t < C; ++t) sq[t] = d[t] * d[t];
+        R ps = sprev(sq[C - 1], lane, P);
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            R l = (t == 0) ? ps : sq[t - 1];
+            d[t] = f24 * (sq[t] - l);
+        }
+        xsolve(d, lane, P, a.c22x);
+        srow_store(a.hh[0] + o, d, sbR, lane, P);
+        {
+            S pc[C];
+            xrow<STG>(pc, xa_src<STG, PART>(a, XA_PC, o, om, op, st, n), sbS, lane, P);
+            S pp = sprev(pc[C - 1], lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) {
+                S l = (t == 0) ? pp : pc[t - 1];
+                d[t] = f24 * ST::d(pc[t], l);
+            }
+        }
+        xsolve(d, lane, P, a.c22x);
+#pragma unroll
+        for (int t = 0; t < C; ++t) acc[t] = acc[t] - d[t] - presg;
+        srow_store(a.r[0] + o, acc, sbR, lane, P);
+    }
+    if (PART == 3) {
+        // The w piece on its own: the y stencil first, then the x terms.
+        const R HPj = a.m.hp[j], HCj = a.m.hc[j], HMj = a.m.hm[j], Z0 = a.m.hz[j];
+        R acc[C];
+        {
+            S wm[C], wp[C], wc0[C];
+            xrow<STG>(wc0, xa_src<STG, PART>(a, XA_WC, o, om, op, st, n), sbS, lane, P);
+            xrow<STG>(wm, xa_src<STG, PART>(a, XA_WM, o, om, op, st, n), sbS, lane, P);
+            xrow<STG>(wp, xa_src<STG, PART>(a, XA_WP, o, om, op, st, n), sbS, lane, P);
+#pragma unroll
+            for (int t = 0; t < C; ++t) acc[t] = RE1 * ST::yvisc(HPj, HCj, HMj, Z0, wp[t], wc0[t], wm[t]);
+        }
+        S wc[C];
+        xrow<STG>(wc, xa_src<STG, PART>(a, XA_WC, o, om, op, st, n), sbS, lane, P);
+        R d[C];
+        S pv = sprev(wc[C - 1], lane, P), nx = snext(wc[0], lane, P);
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            S l = (t == 0) ? pv : wc[t - 1], rr = (t == C - 1) ? nx : wc[t + 1];
+            d[t] = f12 * ST::d2(l, wc[t], rr);
+        }
+        xsolve(d, lane, P, a.c10x);
+#pragma unroll
+        for (int t = 0; t < C; ++t) acc[t] = acc[t] + RE1 * d[t];
+        srow_store(a.r[2] + o, acc, sbR, lane, P);
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+            S l = (t == 0) ? pv : wc[t - 1];
+            d[t] = four * (ST::hi(l) + ST::hi(wc[t]));
+        }
+        xsolve(d, lane, P, a.c6x);
+        srow_store(a.ww1 + o, d, sbR, lane, P);
+    }
+}
+
 // PART 0 computes the u, v and w pieces in one kernel; PART 1, 2, 3 compute one of them
 // (the split form has fewer registers per thread; PART 2 reads the two u rows of the
 // y-face interpolant again).
@@ -50,154 +254,8 @@ __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
             if (PART == 0 || PART == 3) { pf_row(a.w + om, rb, lane); pf_row(a.w + o, rb, lane); pf_row(a.w + op, rb, lane); }
         }
         R uy[C];
-        if (PART == 2 && j >= 2) {
-            // The v piece on its own, ordered so that few rows are live at once: the y
-            // stencils of V (HH2 stored), then -dP/dy, then the x terms of V (R2 stored),
-            // then E_xy with u at the y faces.
-            const R DYPj = a.m.dyp[j], DYCj = a.m.dyc[j], DYMj = a.m.dym[j], Z0 = a.m.dyz[j];
-            const R Hj1 = a.m.rh[j];
-            R acc[C];
-            {
-                S vc[C], vm[C], vp[C];
-                srow_load(vc, a.v + o, sbS, lane, P);
-                srow_load(vm, a.v + om, sbS, lane, P);
-                srow_load(vp, a.v + op, sbS, lane, P);
-                R hh[C];
-#pragma unroll
-                for (int t = 0; t < C; ++t) {
-                    acc[t] = RE1 * ST::yvisc(DYPj, DYCj, DYMj, Z0, vp[t], vc[t], vm[t]);
-                    hh[t] = Hj1 * Sten<R>::vv(vp[t], vc[t], vm[t]);
-                }
-                srow_store(a.hh[1] + o, hh, sbR, lane, P);
-            }
-            {
-                S pc[C], pm[C];
-                srow_load(pc, a.p + o, sbS, lane, P);
-                srow_load(pm, a.p + om, sbS, lane, P);
-#pragma unroll
-                for (int t = 0; t < C; ++t) {
-                    R pg = ST::d(pc[t], pm[t]) * Hj1;
-                    acc[t] = -pg + acc[t];
-                }
-            }
-            S vc[C];
-            srow_load(vc, a.v + o, sbS, lane, P);
-            R d[C];
-            S pv = sprev(vc[C - 1], lane, P), nx = snext(vc[0], lane, P);
-#pragma unroll
-            for (int t = 0; t < C; ++t) {
-                S l = (t == 0) ? pv : vc[t - 1], rr = (t == C - 1) ? nx : vc[t + 1];
-                d[t] = f12 * ST::d2(l, vc[t], rr);
-            }
-            xsolve(d, lane, P, a.c10x);
-#pragma unroll
-            for (int t = 0; t < C; ++t) acc[t] = acc[t] + RE1 * d[t];
-            srow_store(a.r[1] + o, acc, sbR, lane, P);
-#pragma unroll
-            for (int t = 0; t < C; ++t) {
-                S l = (t == 0) ? pv : vc[t - 1];
-                d[t] = four * (ST::hi(l) + ST::hi(vc[t]));
-            }
-            xsolve(d, lane, P, a.c6x);
-            {   // u at the y faces
-                S uc[C], um[C];
-                srow_load(uc, a.u + o, sbS, lane, P);
-                srow_load(um, a.u + om, sbS, lane, P);
-                const R a1 = a.m.hdy[j], a2 = a.m.hdy[j - 1];
-#pragma unroll
-                for (int t = 0; t < C; ++t) d[t] = d[t] * (Hj1 * (a1 * ST::hi(um[t]) + a2 * ST::hi(uc[t])));
-            }
-            srow_store(a.exy + o, d, sbR, lane, P);
-        }
-        if (PART == 1) {
-            // The u piece on its own, ordered so that few rows are live at once: the y
-            // stencil of U, the x terms of U (HH1 stored), then -dP/dx (R1 stored).
-            const R HPj = a.m.hp[j], HCj = a.m.hc[j], HMj = a.m.hm[j], Z0 = a.m.hz[j];
-            R acc[C];
-            {
-                S um[C], up[C], uc0[C];
-                srow_load(uc0, a.u + o, sbS, lane, P);
-                srow_load(um, a.u + om, sbS, lane, P);
-                srow_load(up, a.u + op, sbS, lane, P);
-#pragma unroll
-                for (int t = 0; t < C; ++t) acc[t] = RE1 * ST::yvisc(HPj, HCj, HMj, Z0, up[t], uc0[t], um[t]);
-            }
-            S uc[C];
-            srow_load(uc, a.u + o, sbS, lane, P);
-            R d[C];
-            S pv = sprev(uc[C - 1], lane, P), nx = snext(uc[0], lane, P);
-#pragma unroll
-            for (int t = 0; t < C; ++t) {
-                S l = (t == 0) ? pv : uc[t - 1], rr = (t == C - 1) ? nx : uc[t + 1];
-                d[t] = f12 * ST::d2(l, uc[t], rr);
-            }
-            xsolve(d, lane, P, a.c10x);
-#pragma unroll
-            for (int t = 0; t < C; ++t) acc[t] = acc[t] + RE1 * d[t];
-#pragma unroll
-            for (int t = 0; t < C; ++t) {
-                S rr = (t == C - 1) ? nx : uc[t + 1];
-                d[t] = four * (ST::hi(uc[t]) + ST::hi(rr));
-            }
-            xsolve(d, lane, P, a.c6x);
-            R sq[C];
-#pragma unroll
-            for (int t = 0; t < C; ++t) sq[t] = d[t] * d[t];
-            R ps = sprev(sq[C - 1], lane, P);
-#pragma unroll
-            for (int t = 0; t < C; ++t) {
-                R l = (t == 0) ? ps : sq[t - 1];
-                d[t] = f24 * (sq[t] - l);
-            }
-            xsolve(d, lane, P, a.c22x);
-            srow_store(a.hh[0] + o, d, sbR, lane, P);
-            {
-                S pc[C];
-                srow_load(pc, a.p + o, sbS, lane, P);
-                S pp = sprev(pc[C - 1], lane, P);
-#pragma unroll
-                for (int t = 0; t < C; ++t) {
-                    S l = (t == 0) ? pp : pc[t - 1];
-                    d[t] = f24 * ST::d(pc[t], l);
-                }
-            }
-            xsolve(d, lane, P, a.c22x);
-#pragma unroll
-            for (int t = 0; t < C; ++t) acc[t] = acc[t] - d[t] - presg;
-            srow_store(a.r[0] + o, acc, sbR, lane, P);
-        }
-        if (PART == 3) {
-            // The w piece on its own: the y stencil first, then the x terms.
-            const R HPj = a.m.hp[j], HCj = a.m.hc[j], HMj = a.m.hm[j], Z0 = a.m.hz[j];
-            R acc[C];
-            {
-                S wm[C], wp[C], wc0[C];
-                srow_load(wc0, a.w + o, sbS, lane, P);
-                srow_load(wm, a.w + om, sbS, lane, P);
-                srow_load(wp, a.w + op, sbS, lane, P);
-#pragma unroll
-                for (int t = 0; t < C; ++t) acc[t] = RE1 * ST::yvisc(HPj, HCj, HMj, Z0, wp[t], wc0[t], wm[t]);
-            }
-            S wc[C];
-            srow_load(wc, a.w + o, sbS, lane, P);
-            R d[C];
-            S pv = sprev(wc[C - 1], lane, P), nx = snext(wc[0], lane, P);
-#pragma unroll
-            for (int t = 0; t < C; ++t) {
-                S l = (t == 0) ? pv : wc[t - 1], rr = (t == C - 1) ? nx : wc[t + 1];
-                d[t] = f12 * ST::d2(l, wc[t], rr);
-            }
-            xsolve(d, lane, P, a.c10x);
-#pragma unroll
-            for (int t = 0; t < C; ++t) acc[t] = acc[t] + RE1 * d[t];
-            srow_store(a.r[2] + o, acc, sbR, lane, P);
-#pragma unroll
-            for (int t = 0; t < C; ++t) {
-                S l = (t == 0) ? pv : wc[t - 1];
-                d[t] = four * (ST::hi(l) + ST::hi(wc[t]));
-            }
-            xsolve(d, lane, P, a.c6x);
-            srow_store(a.ww1 + o, d, sbR, lane, P);
+        if (PART >= 1) {
+            xa_piece<R, C, PART, false>(a, j, o, om, op, nullptr, sbS, sbR, lane, P);
         }
         // ---- u: R1 = visc_y + visc_x/RE - dP/dx - PRESG ; HH1 = d(uu)/dx ----
         if (PART == 0) {
@@ -322,6 +380,69 @@ __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
     }
 }
 
+// The u, v or w piece of xA with the rows it reads staged in shared memory: lane 0 of
+// each warp issues one bulk copy per row (cp.async.bulk, completion counted on one
+// mbarrier by bytes), so every row of the warp's (j, k) is in flight at once instead of
+// one dependent group after another; the piece then reads the rows from shared memory.
+// One row per warp.  Rows staged: u at J-1, J, J+1 and P at J (PART 1); v at J-1, J, J+1,
+// P at J-1, J and u at J-1, J (PART 2); w at J-1, J, J+1 (PART 3).  A wait that runs out
+// (about a second) sets SCAL_PIPEERR, waits once more for the warp's copies in flight and
+// returns.
+template <int PART> struct XaStage { static constexpr int rows = PART == 1 ? 4 : PART == 2 ? 7 : 3; };
+
+__host__ __device__ inline size_t xa_stage_bytes(int part, int n1m) {
+    return 16 + (size_t)(part == 1 ? 4 : part == 2 ? 7 : 3) * (size_t)n1m * 8;
+}
+
+template <typename R, int C, int PART>
+__global__ void __launch_bounds__(XMAXT) k_xAs(StepArgs<R> a) {
+    typedef typename SType<R>::S S;
+    static_assert(sizeof(S) == 8, "state rows are 8-byte values");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Geo g = a.g;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int P = g.n1m / C;
+    constexpr int NR = XaStage<PART>::rows;
+    unsigned char *wb = smem_raw + wid * xa_stage_bytes(PART, g.n1m);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(wb);
+    S *st = reinterpret_cast<S *>(wb + 16);
+    const int row = blockIdx.x * (int)(blockDim.x >> 5) + wid;
+    if (row >= g.n2m * g.n3m) return;
+    const int j = 1 + row / g.n3m, k = row % g.n3m;
+    if (PART == 2 && j < 2) return;
+    const long long o = fidx(g, 0, j, k), om = fidx(g, 0, j - 1, k), op = fidx(g, 0, j + 1, k);
+    const int n = g.n1m;
+    const uint32_t rb = (uint32_t)n * (uint32_t)sizeof(S);
+    if (lane == 0) {
+        const S *src[NR];
+        if constexpr (PART == 1) {
+            src[xa_slot<1>(XA_UM)] = a.u + om; src[xa_slot<1>(XA_UC)] = a.u + o; src[xa_slot<1>(XA_UP)] = a.u + op;
+            src[xa_slot<1>(XA_PC)] = a.p + o;
+        }
+        if constexpr (PART == 2) {
+            src[xa_slot<2>(XA_VM)] = a.v + om; src[xa_slot<2>(XA_VC)] = a.v + o; src[xa_slot<2>(XA_VP)] = a.v + op;
+            src[xa_slot<2>(XA_PM)] = a.p + om; src[xa_slot<2>(XA_PC)] = a.p + o;
+            src[xa_slot<2>(XA_UM)] = a.u + om; src[xa_slot<2>(XA_UC)] = a.u + o;
+        }
+        if constexpr (PART == 3) {
+            src[xa_slot<3>(XA_WM)] = a.w + om; src[xa_slot<3>(XA_WC)] = a.w + o; src[xa_slot<3>(XA_WP)] = a.w + op;
+        }
+        mbar_init(bar, 1);
+        mbar_init_fence();
+        fence_async_smem();
+        mbar_expect_tx(bar, NR * rb);
+#pragma unroll
+        for (int q = 0; q < NR; ++q) bulk_g2s(st + (size_t)q * n, src[q], rb, bar);
+    }
+    __syncwarp();
+    if (!mbar_wait(bar, 0)) {
+        if (lane == 0) a.scal[SCAL_PIPEERR] = 1.0;
+        mbar_wait(bar, 0);   // the copies in flight target this warp's stage
+        return;
+    }
+    xa_piece<R, C, PART, true>(a, j, o, om, op, st, nullptr, nullptr, lane, P);
+}
+
 // ---------------------------------------------------------------------------------
 // xB: remaining convective terms, AB2, x factor of Crank-Nicolson
 // ---------------------------------------------------------------------------------
@@ -430,14 +551,6 @@ __global__ void __launch_bounds__(XMAXT) k_xB(StepArgs<R> a) {
 // ---------------------------------------------------------------------------------
 // xC: RDP = div(UH)/DT and its real-to-complex FFT along x
 // ---------------------------------------------------------------------------------
-// Row operand of an x pass: a global row (read through the read-only path) or a row
-// already staged in shared memory by the bulk-copy ring.
-template <bool SH, typename T, int C>
-__device__ __forceinline__ void xrow(T (&v)[C], const T *p, T *sb, int lane, int P) {
-    if constexpr (SH) crow_load(v, p, lane, P);
-    else srow_load(v, p, sb, lane, P);
-}
-
 // Shared-memory layout of one xC stage (mixed and FP64 forms alike): the rows
 // U(J), DH1(J), RDPZ(J), V(J), DH2(J), V(J+1), DH2(J+1) of one (J, K).
 template <typename R>
@@ -853,6 +966,22 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
     const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(M + 1) * sizeof(C2)) * xw;
     switch (which) {
         case 0:
+            if (ch->tune.xsplit && ch->tune.xstage && ch->g.n1m % 2 == 0) {
+                // the pieces with their rows staged by bulk copies (rows of 16-byte multiples)
+                const size_t s1 = xa_stage_bytes(1, ch->g.n1m) * xw, s2 = xa_stage_bytes(2, ch->g.n1m) * xw,
+                             s3 = xa_stage_bytes(3, ch->g.n1m) * xw;
+                if (s2 > 227 * 1024) { set_error("xA stage exceeds shared memory"); return C3D_EINVAL; }
+                cudaFuncSetAttribute(k_xAs<R, C, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
+                cudaFuncSetAttribute(k_xAs<R, C, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
+                cudaFuncSetAttribute(k_xAs<R, C, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s3);
+                k_xAs<R, C, 1><<<grid, nt, s1, st>>>(a);
+                mark(ch, nl, "xA_u", N * (16 + 2 * Rb));
+                k_xAs<R, C, 2><<<grid, nt, s2, st>>>(a);
+                mark(ch, nl, "xA_v", N * (24 + 3 * Rb));
+                k_xAs<R, C, 3><<<grid, nt, s3, st>>>(a);
+                mark(ch, nl, "xA_w", N * (8 + 2 * Rb));
+                break;
+            }
             if (ch->tune.xsplit) {   // the u, v and w pieces as three kernels
                 cudaFuncSetAttribute(k_xA<R, C, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
                 cudaFuncSetAttribute(k_xA<R, C, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);

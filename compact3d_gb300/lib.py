@@ -110,6 +110,7 @@ def load(path: str = LIB_PATH):
 
 
 # Operators of c3d_op_apply (include/c3d.h)
+C3D_SCHEDULE_LEN = 13   # ints of a launch schedule (include/c3d.h)
 OPS = {"DX1": 1, "DX2": 2, "IX": 3, "DZ1": 4, "DZ2": 5, "IZ": 6, "DY1": 7, "DY2": 8, "POISSON": 9}
 
 
@@ -196,20 +197,20 @@ class Channel:
     # ---- launch schedule ----
     SCHEDULE_KEYS = ("z_segment_zA", "z_segment_zB", "z_segment_zC", "z_segment_zD", "z_segment_zE",
                      "x_rows_per_block", "fft_z_tile", "fft_x_plan", "fft_z_plan", "z_split_zA",
-                     "x_split_xA", "x_bulk_stages")
+                     "x_split_xA", "x_bulk_stages", "x_stage_xA")
 
     def autotune(self) -> dict:
-        sch = (_ip * 12)()
+        sch = (_ip * C3D_SCHEDULE_LEN)()
         check(load().c3d_autotune(self.h, sch), "c3d_autotune")
         return dict(zip(self.SCHEDULE_KEYS, sch[:]))
 
     def get_schedule(self) -> dict:
-        sch = (_ip * 12)()
+        sch = (_ip * C3D_SCHEDULE_LEN)()
         check(load().c3d_get_schedule(self.h, sch), "c3d_get_schedule")
         return dict(zip(self.SCHEDULE_KEYS, sch[:]))
 
     def set_schedule(self, sched: dict):
-        sch = (_ip * 12)(*[int(sched[k]) for k in self.SCHEDULE_KEYS])
+        sch = (_ip * C3D_SCHEDULE_LEN)(*[int(sched.get(k, 0)) for k in self.SCHEDULE_KEYS])
         check(load().c3d_set_schedule(self.h, sch), "c3d_set_schedule")
 
     # ---- ENERGY's plane statistics ----

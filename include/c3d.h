@@ -348,7 +348,8 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
 
 /* ---- launch schedule -----------------------------------------------------
  * The kernels' launch shapes are chosen per grid shape by an autotuner written for
- * this library (no counterpart in the reference).  A schedule is twelve ints:
+ * this library (no counterpart in the reference).  A schedule is thirteen ints
+ * (C3D_SCHEDULE_LEN):
  *   [0..4] z-line segment length (8, 16, 32) of each z pass: the points each thread
  *       solves sequentially (Thomas-like) before the parallel segments of a z line
  *       meet; or 0: one block per 32 z lines of a plane, each thread one segment of
@@ -368,6 +369,9 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
  *   [11] x passes whose rows each warp reads from global memory (0) or streams into
  *       shared memory through a ring of 2 or 3 bulk-copy stages (persistent warps;
  *       mixed form, N1M a multiple of 4)
+ *   [12] the u, v and w pieces of the explicit x pass (with [10] = 1) read their rows
+ *       from global memory (0), or stage every row of a warp's (J, K) in shared memory
+ *       by one bulk copy per row before computing (1; N1M even)
  * c3d_autotune  times the candidates on a scratch channel of the same grid holding a
  *               copy of this channel's state (so the channel needs its state), keeps
  *               the fastest per kernel group, applies it, and caches it per grid
@@ -375,6 +379,7 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
  *               receives the result.
  * c3d_set_schedule / c3d_get_schedule  set or read a schedule directly.
  * Channels of a batch are tuned before the batch's first step captures its graph. */
+#define C3D_SCHEDULE_LEN 13
 int c3d_autotune(c3d_channel *ch, int *sched);
 int c3d_get_schedule(c3d_channel *ch, int *sched);
 int c3d_set_schedule(c3d_channel *ch, const int *sched);

@@ -26,10 +26,10 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def _sched(zl, xw, tw, fx, fz, split, xsplit, xbulk=0):
+def _sched(zl, xw, tw, fx, fz, split, xsplit, xbulk=0, xstage=0):
     d = {f"z_segment_z{c}": z for c, z in zip("ABCDE", zl)}
     d.update(x_rows_per_block=xw, fft_z_tile=tw, fft_x_plan=fx, fft_z_plan=fz, z_split_zA=split,
-             x_split_xA=xsplit, x_bulk_stages=xbulk)
+             x_split_xA=xsplit, x_bulk_stages=xbulk, x_stage_xA=xstage)
     return d
 
 
@@ -124,6 +124,29 @@ def test_bulk_rows_bit_identical(libc3d, shape, fxp):
         ch.upload(U, P, HH)
         s = ch.get_schedule()
         s.update(x_bulk_stages=xb, fft_x_plan=fxp)
+        ch.set_schedule(s)
+        for m in (1, 2, 3):
+            ch.step(m, dt, 0.0, 0.0)
+        out.append(ch.download())
+        ch.close()
+    for r in out[1:]:
+        for a, b in zip(r, out[0]):
+            assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("n1m,prec", [(32, C3D_MIXED), (96, C3D_MIXED), (384, C3D_MIXED), (64, C3D_FP64),
+                                       (384, C3D_FP64)])
+def test_staged_xA_bit_identical(libc3d, n1m, prec):
+    """xA's pieces with their rows staged in shared memory by bulk copies compute the same
+    step bit for bit as with the rows read from global memory, for 2 and 8 rows per block."""
+    g, dt = make_grid("small32", n1m=n1m, n2m=24, n3m=32)
+    U, P, HH = ic.perturbed_laminar(g)
+    out = []
+    for xs, xw in ((0, 2), (1, 2), (1, 8)):
+        ch = libc3d.Channel(g, prec)
+        ch.upload(U, P, HH)
+        s = ch.get_schedule()
+        s.update(x_split_xA=1, x_stage_xA=xs, x_rows_per_block=xw)
         ch.set_schedule(s)
         for m in (1, 2, 3):
             ch.step(m, dt, 0.0, 0.0)
