@@ -1201,6 +1201,24 @@ int rec_read(FILE *f, void *p, size_t bytes) {
     }
     return 0;
 }
+// Walks the records of an open checkpoint without reading their contents: each record
+// must have the expected length and matching markers before and after it.  The file is
+// left at its start.
+int rec_scan(FILE *f, const std::vector<size_t> &sizes) {
+    int rc = 0;
+    for (size_t q = 0; q < sizes.size() && !rc; ++q) {
+        int32_t m0 = 0, m1 = 0;
+        if (fread(&m0, 4, 1, f) != 1 || (size_t)(uint32_t)m0 != sizes[q]) {
+            set_error("checkpoint record length does not match the channel's grid");
+            rc = C3D_EIO;
+        } else if (fseek(f, (long)sizes[q], SEEK_CUR) != 0 || fread(&m1, 4, 1, f) != 1 || m1 != m0) {
+            set_error("checkpoint read failed (truncated file or bad record marker)");
+            rc = C3D_EIO;
+        }
+    }
+    rewind(f);
+    return rc;
+}
 // A device record through the staging area: packed on the device, copied, written.
 int rec_write_dev(c3d_channel *ch, FILE *f, int what, double *slot, size_t n, std::vector<double> &hb) {
     int rc = launch_ckpt(ch, 0, what, slot);
@@ -1425,6 +1443,19 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
     const size_t nu = 3 * (size_t)g.n1m * (g.n2 + 1) * g.n3m, np_ = (size_t)g.n1m * g.n2m * g.n3m;
     FILE *f = fopen(path, "rb");
     if (!f) { set_error(std::string("cannot open ") + path); return C3D_EIO; }
+    const size_t nt_ = (size_t)(g.n1m + 2) * (g.n3m + 2) * 2;
+    {   // every record present and whole before any of the channel's state is replaced
+        std::vector<size_t> sizes = {12, 16, 4, 8, nu * 8, np_ * 8, 3 * np_ * 8};
+        if (ch->files != 0) sizes.push_back((2 * nt_ + 3) * 8);
+        int32_t d0[3] = {0, 0, 0};
+        if (rec_read(f, d0, sizeof(d0)) == 0 && (d0[0] != g.n1m || d0[1] != g.n2m || d0[2] != g.n3m)) {
+            fclose(f);
+            set_error("checkpoint grid does not match the channel's");
+            return C3D_EINVAL;
+        }
+        rewind(f);
+        if ((rc = rec_scan(f, sizes))) { fclose(f); return rc; }
+    }
     std::vector<double> hb;
     int32_t dims[3] = {0, 0, 0}, nt = 0;
     double pg[2] = {0.0, 0.0}, tm = 0.0;
@@ -1436,13 +1467,17 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
     if (!rc && !(rc = rec_read(f, pg, sizeof(pg))) && !(rc = rec_read(f, &nt, 4)) && !(rc = rec_read(f, &tm, 8)) &&
         !(rc = rec_read_dev(ch, f, 0, x.u(0), nu, hb)) && !(rc = rec_read_dev(ch, f, 1, x.p(), np_, hb)) &&
         !(rc = rec_read_dev(ch, f, 2, x.hh(0), 3 * np_, hb)) && ch->files != 0) {
-        const size_t nt_ = (size_t)(g.n1m + 2) * (g.n3m + 2) * 2;
         std::vector<double> w(2 * nt_ + 3);
         if (!(rc = rec_read(f, w.data(), w.size() * 8)) && !(rc = c3d_upload_wall(ch, w.data(), w.data() + nt_)))
             rc = c3d_set_wsm(ch, w.data() + 2 * nt_);
     }
     fclose(f);
-    if (rc) return rc;
+    if (rc) {
+        // a read that failed after the scan (an I/O error) may have replaced part of the
+        // state: the channel refuses to step until a complete state is uploaded or read
+        ch->have_state = 0;
+        return rc;
+    }
     ch->have_state = 1;
     if (ntime) *ntime = nt;
     if (time) *time = tm;
@@ -1493,6 +1528,13 @@ int c3d_op_get(c3d_channel *ch, double *f) {
     if (rc) return rc;
     CK(cudaGetLastError());
     return 0;
+}
+
+int c3d_pipe_wait_selftest(c3d_channel *ch, double limit_ms) {
+    if (!ch) { set_error("null channel"); return C3D_EINVAL; }
+    if (!(limit_ms > 0) || !(limit_ms <= 1000.0)) { set_error("limit_ms must be in (0, 1000]"); return C3D_EINVAL; }
+    cudaSetDevice(ch->device);
+    return launch_pipe_selftest(ch, limit_ms);
 }
 
 int c3d_sync(c3d_channel *ch) {

@@ -271,6 +271,7 @@ int launch_op(c3d_channel *ch, StepArgs<R> &a, int op, const R *in, R *out, int 
 int launch_refine(c3d_channel *ch, StepArgs<float> &a, RefArgs &r, int *nl);            // c3d_refine.cu
 int launch_project(c3d_channel *ch, int *launches);
 int launch_diag(c3d_channel *ch, int *launches);
+int launch_pipe_selftest(c3d_channel *ch, double limit_ms);
 int launch_poisson_tables(c3d_channel *ch);
 // what: 0 U component, 1 P, 2 HH component, 3 SGSVIS (to host), 4 operand (to device),
 // 5 operator result (to host)

@@ -343,12 +343,13 @@ __device__ __forceinline__ unsigned long long gtimer_ns() {
     asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
     return t;
 }
-// Waits for phase `parity` of barrier b to complete; false after about one second.
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity) {
+// Waits for phase `parity` of barrier b to complete; false after limit_ns (about one
+// second by default).
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, unsigned long long limit_ns = 1000000000ull) {
     if (mbar_try_wait(b, parity)) return true;
     const unsigned long long t0 = gtimer_ns();
     while (!mbar_try_wait(b, parity))
-        if (gtimer_ns() - t0 > 1000000000ull) return false;
+        if (gtimer_ns() - t0 > limit_ns) return false;
     return true;
 }
 

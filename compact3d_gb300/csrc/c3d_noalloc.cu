@@ -138,8 +138,10 @@ extern "C" int c3d_divcheck_noalloc(const c3d_grid *gr, const double *u, double 
     const int n1m = gr->n1 - 1, n2m = gr->n2 - 1, n3m = gr->n3 - 1;
     const int C = (n1m + 31) / 32;
     const bool cok = (C == 1 || C == 2 || C == 3 || C == 4 || C == 6 || C == 8 || C == 12);
-    if (!cok || n1m < 16 || n1m % C != 0 || n1m % 2 != 0 || n3m < 16 || n3m % 16 != 0 || n2m < 4)
-        return na_fail(C3D_EINVAL, "c3d_divcheck_noalloc: unsupported extents (same rules as c3d_create)");
+    if (!cok || n1m < 16 || n1m % C != 0 || n1m % 2 != 0 || n3m < 16 || n3m % 16 != 0 || n2m < 4 || n2m > 4096)
+        return na_fail(C3D_EINVAL, "c3d_divcheck_noalloc: unsupported extents (c3d_create's rules without the "
+                                   "FFT lengths: N1-1 even, >= 16, in 32 lane chunks of 1-12 points; N3-1 a "
+                                   "multiple of 16; N2-1 in [4, 4096])");
     if (!(gr->dx1 > 0) || !(gr->dx3 > 0)) return na_fail(C3D_EINVAL, "c3d_divcheck_noalloc: DX1, DX3 must be positive");
     // working set in doubles
     const size_t se = (size_t)(gr->n1 + 1) * (gr->n2 + 1) * (gr->n3 + 1);

@@ -443,6 +443,25 @@ __global__ void __launch_bounds__(XMAXT) k_xAs(StepArgs<R> a) {
     xa_piece<R, C, PART, true>(a, j, o, om, op, st, nullptr, nullptr, lane, P);
 }
 
+// The bounded stage wait of the staged x passes, run on a barrier that nothing arrives on
+// and no copy targets, so the wait runs out after limit_ns and sets SCAL_PIPEERR exactly
+// as a stalled stage would (c3d_pipe_wait_selftest).
+__global__ void k_pipe_selftest(double *scal, unsigned long long limit_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
+    const bool ok = mbar_wait(&bar, 0, limit_ns);
+    if (!ok && threadIdx.x == 0) scal[SCAL_PIPEERR] = 1.0;
+}
+
+int launch_pipe_selftest(c3d_channel *ch, double limit_ms) {
+    k_pipe_selftest<<<1, 32, 0, ch->stream>>>(ch->scal, (unsigned long long)(limit_ms * 1e6));
+    return cudaGetLastError() == cudaSuccess ? 0 : C3D_ECUDA;
+}
+
 // ---------------------------------------------------------------------------------
 // xB: remaining convective terms, AB2, x factor of Crank-Nicolson
 // ---------------------------------------------------------------------------------

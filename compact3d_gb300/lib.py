@@ -72,6 +72,7 @@ SIGNATURES = {
     "c3d_host_register": (_ip, [_vp, ctypes.c_size_t]),
     "c3d_host_unregister": (_ip, [_vp]),
     "c3d_sync": (_ip, [_vp]),
+    "c3d_pipe_wait_selftest": (_ip, [_vp, ctypes.c_double]),
     "c3d_last_step_stats": (_ip, [_vp, _dp, ctypes.POINTER(_ip)]),
     "c3d_step_async": (_ip, [_vp, _ip, ctypes.c_double]),
     "c3d_set_presg": (_ip, [_vp, ctypes.c_double, ctypes.c_double]),

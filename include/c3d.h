@@ -225,6 +225,13 @@ int c3d_timer_stop(c3d_channel *ch, double *ms);
  * c3d_profile_get returns, for kernel index idx < c3d_profile_count(),
  * its name, accumulated device time, launch count and the algorithmic bytes
  * of one launch (compulsory reads + writes of that kernel). */
+/* Diagnostic with no counterpart in the reference: runs the bounded wait that the
+ * shared-memory staged x passes use for their bulk copies, on a barrier that nothing
+ * arrives on, so that it runs out after limit_ms (0 < limit_ms <= 1000).  It sets the
+ * channel's pipeline-error flag as a stalled stage would: the next c3d_sync (and every
+ * later step of the channel) returns C3D_ECUDA with the stall message.  It shows that a
+ * stalled copy ends in an error code instead of a hung kernel. */
+int c3d_pipe_wait_selftest(c3d_channel *ch, double limit_ms);
 int c3d_profile(c3d_channel *ch, int enable);
 int c3d_profile_count(c3d_channel *ch);
 int c3d_profile_get(c3d_channel *ch, int idx, const char **name, double *ms,
@@ -241,11 +248,15 @@ int c3d_profile_get(c3d_channel *ch, int idx, const char **name, double *ms,
  * static __device__ array of C3D_NOALLOC_MAX_BYTES that every GPU loading the
  * library keeps until exit, so grids whose working set (about 8 bytes x
  * ((N1+1)(N2+1)(N3+1) + 4 (N2+1)(N1-1)(N3-1))) exceeds it return C3D_EINVAL.
- * Only grid->n1..n3, dx1, dx3 and dy are read.  All calls share that scratch:
- * calls that overlap on the GPU race, so serialise them.  The first call on a
- * device looks up the scratch address (cudaGetSymbolAddress); make it before
- * any stream capture starts on that device.  Work runs on the legacy default
- * stream; the call returns when *divmax is ready. */
+ * Only grid->n1..n3, dx1, dx3 and dy are read.  Extents: c3d_create's rules
+ * without its FFT-length ones (DIVCHECK has no FFT): N1-1 even, >= 16 and split
+ * into 32 lane chunks of 1, 2, 3, 4, 6, 8 or 12; N3-1 a multiple of 16; N2-1 in
+ * [4, 4096].  All calls share that scratch: calls that overlap on the GPU race,
+ * so serialise them.  The first call on a device looks up the scratch address
+ * (cudaGetSymbolAddress).  Every call issues its copies and kernels on the legacy
+ * default stream and synchronises it, so no call (the first or any later one) may
+ * run while a stream capture is active on that device; the call returns when
+ * *divmax is ready. */
 #define C3D_NOALLOC_MAX_BYTES (64u * 1024u * 1024u)
 int c3d_divcheck_noalloc(const c3d_grid *grid, const double *u, double *divmax);
 
@@ -339,8 +350,11 @@ int c3d_particles_source(c3d_channel *ch, int n, const double *par, double diam,
  * Records 1 and 7-8 extend CWRITE so that a restart continues the run exactly (the
  * reference restarts with HH = 0).  A record longer than 2^31 - 1 bytes (more than
  * 89 M points per component) is refused with C3D_EINVAL.  c3d_checkpoint_read checks
- * the extents against the channel's grid and leaves the channel's state as read.
- * INTEGRATION.md shows the matching Fortran READ statements. */
+ * the extents against the channel's grid (C3D_EINVAL) and the length and both markers
+ * of every record (C3D_EIO) before it replaces any of the channel's state, then leaves
+ * the state as read; if reading still fails after that check, the channel has no state
+ * (c3d_step returns C3D_ESTATE) until one is uploaded or read.  A Fortran driver reads
+ * the file with one unformatted READ per record, in the order above. */
 int c3d_checkpoint_write(c3d_channel *ch, const char *path, int ntime, double time, double presg,
                          double presg3);
 int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *time, double *presg,

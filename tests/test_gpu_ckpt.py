@@ -97,3 +97,25 @@ def test_checkpoint_errors(libc3d, tmp_path):
     with pytest.raises(libc3d.C3DError) as e:
         ch.checkpoint_read(os.path.join(str(tmp_path), "missing.bin"))
     assert e.value.code == -8
+    # a file cut inside the P record and one with a bad HH record marker: refused before
+    # any of the channel's state is replaced (the state downloads unchanged and steps on)
+    before = ch.download()
+    nu = 3 * g.n1m * (g.n2m + 2) * g.n3m
+    np_ = g.n1m * g.n2m * g.n3m
+    p_start = (12 + 8) + (16 + 8) + (4 + 8) + (8 + 8) + (nu * 8 + 8)
+    raw = path.read_bytes()
+    cut_p = tmp_path / "cut_p.bin"
+    cut_p.write_bytes(raw[:p_start + 4 + np_ * 4])
+    bad_hh = bytearray(raw)
+    hh_start = p_start + np_ * 8 + 8
+    bad_hh[hh_start:hh_start + 4] = (12345).to_bytes(4, "little")
+    bad = tmp_path / "bad_hh.bin"
+    bad.write_bytes(bytes(bad_hh))
+    for f in (cut_p, bad):
+        with pytest.raises(libc3d.C3DError) as e:
+            ch.checkpoint_read(f)
+        assert e.value.code == -8
+        after = ch.download()
+        for x, y in zip(before, after):
+            assert np.array_equal(x, y)
+    ch.step(2, dt, pg, pg3)

@@ -178,3 +178,22 @@ def test_block_z_solve_mixed_close_to_segments(libc3d):
         a = res[1][0][1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c]
         b = res[0][0][1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c]
         assert rel(a, b) < 1e-5, (c, rel(a, b))
+
+
+def test_stalled_stage_wait_becomes_error(libc3d):
+    """The bounded wait of the bulk-copy stages runs out (on a barrier that nothing arrives
+    on, with no copy in flight) and the flag it sets reaches the C-ABI as C3D_ECUDA."""
+    g, dt = make_grid("tiny16")
+    U, P, HH = ic.perturbed_laminar(g)
+    ch = libc3d.Channel(g, C3D_MIXED)
+    ch.upload(U, P, HH)
+    ch.step(1, dt, 0.0, 0.0)
+    L = libc3d.load()
+    assert L.c3d_sync(ch.h) == 0
+    assert L.c3d_pipe_wait_selftest(ch.h, 0.0) == -1          # limit out of range
+    assert L.c3d_pipe_wait_selftest(ch.h, 5.0) == 0           # queued: waits 5 ms, then flags
+    assert L.c3d_sync(ch.h) == -2
+    assert b"bulk-copy stage" in L.c3d_last_error()
+    with pytest.raises(libc3d.C3DError):
+        ch.step(2, dt, 0.0, 0.0)
+    ch.close()

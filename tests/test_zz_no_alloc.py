@@ -6,7 +6,9 @@ start-up).  It works out of a static device array instead of cudaMalloc, so this
 checks that it gives DIVCHECK's max|div u| exactly as c3d_diagnose does on a channel, on
 two calls in a row (a strongly divergent field first, then a projected one, so a running
 maximum left over from the first call would show), and that a grid too large for the
-static array is refused.  This file is collected last on purpose.
+static array is refused, and that repeated calls leave the device's free memory exactly
+where it was (a cudaMalloc inside the call would lower it).  This file is collected last
+on purpose.
 """
 import ctypes
 
@@ -69,3 +71,19 @@ def test_noalloc_rejects_oversize_grid(L):
     rc = L.load().c3d_divcheck_noalloc(ctypes.byref(s), U.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), out)
     assert rc == -1
     assert b"too large" in L.load().c3d_last_error()
+
+
+def test_noalloc_allocates_nothing(L):
+    """After a first call (which looks up the scratch address and loads the kernels),
+    five more calls leave the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    g, _ = make_grid("channel64")
+    U, _, _ = ic.perturbed_laminar(g, seed=7)
+    L.check(L.load().c3d_set_device(0), "c3d_set_device")
+    torch.cuda.mem_get_info(0)
+    first = noalloc_divmax(L, g, U)
+    free0, _ = torch.cuda.mem_get_info(0)
+    for _ in range(5):
+        assert noalloc_divmax(L, g, U) == first
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0, (free0, free1)
