@@ -515,7 +515,7 @@ def with_summary(res: dict) -> dict:
     b = res.get("batched")
     if b:
         summ["batched"] = b["value"]
-        for k in ("mixed_sequential", "fp64_sequential"):
+        for k in ("streams_form", "mixed_sequential", "fp64_sequential"):
             if k in b:
                 summ["batched_" + k] = b[k]["value"]
     e = res.get("err_vs_fp64")
@@ -839,32 +839,40 @@ def run_batched(args, D: Dist):
         ch.upload(U, P, HH)
         ch.project()
         if not args.no_tune:
-            ch.autotune()   # per grid shape, cached; before the first step captures the graph
+            ch.autotune()   # per grid shape, cached (the streams form runs the tuned schedules)
     n = len(grids)
     dts = [dt] * n
-    p, p3 = [0.0] * n, [0.0] * n
-    step = 1
-    for _ in range(max(3, args.warmup)):
-        p, p3 = b.step(step, dts, p, p3)
-        step += 1
     K = args.steps
-    D.barrier()
-    t0 = time.perf_counter()
-    dev_ms = 0.0
-    for _ in range(K):
-        p, p3 = b.step(step, dts, p, p3)
-        step += 1
-        dev_ms += b.last_step_stats()[0]
-    wall = D.max(time.perf_counter() - t0)
-    dev_ms = D.max(dev_ms)
-    launches = b.last_step_stats()[1]
-    b.close()
     tot = D.sum(pts)
+    step = 1
+    timed = {}
+    for form in ("worklist", "streams"):
+        b.set_form(form)
+        p, p3 = [0.0] * n, [0.0] * n
+        for _ in range(max(3, args.warmup)):
+            p, p3 = b.step(step, dts, p, p3)
+            step += 1
+        D.barrier()
+        t0 = time.perf_counter()
+        dev_ms = 0.0
+        for _ in range(K):
+            p, p3 = b.step(step, dts, p, p3)
+            step += 1
+            dev_ms += b.last_step_stats()[0]
+        wall = D.max(time.perf_counter() - t0)
+        dev_ms = D.max(dev_ms)
+        timed[form] = (dev_ms, wall, b.last_step_stats()[1])
+    b.close()
+    dev_ms, wall, launches = timed["worklist"]
     out = dict(value=tot * K / (dev_ms / 1e3), unit=UNIT, channels=n, points=pts, steps=K,
                ms_per_step=dev_ms / K, wall_value=tot * K / wall, kernels_per_step=launches,
-               form="mixed, one CUDA graph per ensemble step",
+               form="mixed, work-list form: one launch per pass and kernel group over all channels, "
+                    "one CUDA graph per ensemble step",
                workload="32 channels: Nx,Nz in {48,64,96,128}, Ny in {33,49,65,97}, "
                         "Re_bulk in [3000,12000], seeded")
+    sm, sw, sl = timed["streams"]
+    out["streams_form"] = dict(value=tot * K / (sm / 1e3), ms_per_step=sm / K, kernels_per_step=sl,
+                               form="each channel's own tuned step on its own stream, one CUDA graph")
     # the same channels, one after another: plain FP64, and the mixed form without the
     # graph (so that the batching gain and the precision gain can be told apart)
     for key, prec, k_seq in (("fp64_sequential", C3D_FP64, max(2, min(K, args.fp64_steps))),

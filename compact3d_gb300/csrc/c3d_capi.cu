@@ -1573,7 +1573,10 @@ bool tune_ok(const c3d_channel *ch, const Tune &t) {
         zl = zl && (t.zl[q] == 0 || t.zl[q] == 8 || t.zl[q] == 16 || (t.zl[q] == 32 && ch->g.n3m % 32 == 0));
     const bool xw = t.xw == 2 || t.xw == 4 || t.xw == 8;
     const bool tw = t.twz == 0 || t.twz == 4 || t.twz == 8 || t.twz == 16;
-    return zl && xw && tw && t.fxp >= 0 && t.fxp <= 3 && t.fzp >= 0 && t.fzp <= 2 && (t.zsplit == 0 || t.zsplit == 1) &&
+    // x plan 3 (register row FFTs) needs every lane of the warp to hold a chunk of an even
+    // length: N1M a multiple of 64
+    const bool fx = t.fxp >= 0 && t.fxp <= 2 ? true : (t.fxp == 3 && ch->g.n1m % 64 == 0);
+    return zl && xw && tw && fx && t.fzp >= 0 && t.fzp <= 2 && (t.zsplit == 0 || t.zsplit == 1) &&
            (t.xsplit == 0 || t.xsplit == 1) && (t.xbulk == 0 || t.xbulk == 2 || t.xbulk == 3) &&
            (t.xstage == 0 || (t.xstage == 1 && ch->g.n1m % 2 == 0));
 }
@@ -1736,6 +1739,13 @@ struct c3d_batch {
     std::vector<double> gdt[2];
     int launches = 0;
     float last_ms = 0.f;
+    int form = C3D_BATCH_WORKLIST;            // requested form (c3d_batch_set_form)
+    int groups = 2;                           // work-list form: channel groups on their own streams
+    // work-list form, per AB2 parity: every channel's StepArgs and the block maps
+    void *dargs[2] = {nullptr, nullptr};
+    size_t nargs[2] = {0, 0};
+    BMap *dmap[2] = {nullptr, nullptr};
+    size_t nmap[2] = {0, 0};
 };
 
 static void batch_free(c3d_batch *b) {
@@ -1749,12 +1759,143 @@ static void batch_free(c3d_batch *b) {
     if (b->hpres) cudaFreeHost(b->hpres);
     if (b->dpres) cudaFree(b->dpres);
     if (b->dscal) cudaFree(b->dscal);
+    for (int p = 0; p < 2; ++p) {
+        if (b->dargs[p]) cudaFree(b->dargs[p]);
+        if (b->dmap[p]) cudaFree(b->dmap[p]);
+    }
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
 
+// The work-list form applies when every channel is DNS (FILES = 0) in the same
+// precision, C3D_FP64 or C3D_MIXED.
+static bool batch_worklist_ok(const c3d_batch *b) {
+    for (auto *c : b->ch)
+        if (c->files != 0 || c->refine || c->precision != b->ch[0]->precision) return false;
+    return true;
+}
+
+static int grow(void **p, size_t *have, size_t need) {
+    if (*have >= need && *p) return 0;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    if (cudaMalloc(p, need) != cudaSuccess) { set_error("batch: cudaMalloc of the work lists"); return C3D_ENOMEM; }
+    *have = need;
+    return 0;
+}
+
+// Work-list form of the ensemble step: each pass of the step is one launch per group of
+// channels whose kernel for that pass is the same template instance with the same block
+// shape; block q of a launch runs block map[q].x of channel map[q].ch.  The channels'
+// StepArgs (for the parity the step writes and its DT) and the maps live on the device.
+static int batch_capture_worklist(c3d_batch *b, const double *dt, int par) {
+    const int n = (int)b->ch.size();
+    const size_t asz = batch_args_size(b->ch[0]);
+    std::vector<unsigned char> args(asz * n);
+    std::vector<std::vector<BKern>> plans(n);
+    for (int i = 0; i < n; ++i) {
+        c3d_channel *c = b->ch[i];
+        c->cur = par;   // GETUP's HH2 <- HH: this step writes buffer par
+        batch_args(c, dt[i], args.data() + (size_t)i * asz);
+        int rc = batch_plan(c, plans[i]);
+        if (rc) return rc;
+        if (plans[i].size() != plans[0].size()) { set_error("batch: channels with different pass lists"); return C3D_EINVAL; }
+    }
+    // channel groups: G sets of channels (largest first, dealt round-robin), each with
+    // its own work list on its own stream, so that the passes of one group overlap those
+    // of another; within a launch the channels with the longest wall-normal lines first
+    const int G = std::max(1, std::min(b->groups, n));
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        const Geo &gx = b->ch[x]->g, &gy = b->ch[y]->g;
+        if (gx.n2m != gy.n2m) return gx.n2m > gy.n2m;
+        return (long long)gx.n1m * gx.n3m > (long long)gy.n1m * gy.n3m;
+    });
+    std::vector<std::vector<int>> members(G);
+    for (int q = 0; q < n; ++q) members[q % G].push_back(order[q]);
+    struct Grp { const void *fn; unsigned block; size_t smem, off, cnt; int sg; };
+    std::vector<Grp> launches;
+    std::vector<BMap> map;
+    for (int sg = 0; sg < G; ++sg)
+        for (size_t p = 0; p < plans[0].size(); ++p) {
+            std::vector<Grp> gs;
+            for (int i : members[sg]) {
+                const BKern &k = plans[i][p];
+                size_t q = 0;
+                while (q < gs.size() && !(gs[q].fn == k.fn && gs[q].block == k.block)) ++q;
+                if (q == gs.size()) gs.push_back({k.fn, k.block, 0, 0, 0, sg});
+                gs[q].smem = std::max(gs[q].smem, k.smem);
+            }
+            for (Grp &gr : gs) {
+                gr.off = map.size();
+                for (int i : members[sg]) {
+                    const BKern &k = plans[i][p];
+                    if (k.fn != gr.fn || k.block != gr.block) continue;
+                    for (unsigned x = 0; x < k.nblocks; ++x) map.push_back(BMap{i, x, 0u, k.nblocks});
+                }
+                gr.cnt = map.size() - gr.off;
+                launches.push_back(gr);
+            }
+        }
+    int rc = grow(&b->dargs[par], &b->nargs[par], args.size());
+    if (!rc) rc = grow((void **)&b->dmap[par], &b->nmap[par], map.size() * sizeof(BMap));
+    if (rc) return rc;
+    CK(cudaMemcpy(b->dargs[par], args.data(), args.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b->dmap[par], map.data(), map.size() * sizeof(BMap), cudaMemcpyHostToDevice));
+    for (const Grp &gr : launches)
+        if (gr.smem > 48 * 1024 &&
+            cudaFuncSetAttribute(gr.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gr.smem) != cudaSuccess) {
+            set_error("batch: shared memory of a work-list kernel");
+            return C3D_ECUDA;
+        }
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
+    cudaMemcpyAsync(b->dpres, b->hpres, 2 * n * sizeof(double), cudaMemcpyHostToDevice, b->stream);
+    k_batch_scatter<<<(n + 127) / 128, 128, 0, b->stream>>>(n, b->dpres, b->dscal);
+    cudaEventRecord(b->fork, b->stream);
+    cudaError_t le = cudaSuccess;
+    for (int sg = 0; sg < G; ++sg) {
+        cudaStream_t s = G == 1 ? b->stream : b->ch[sg]->stream;   // a channel stream, idle meanwhile
+        if (G > 1) cudaStreamWaitEvent(s, b->fork, 0);
+        for (const Grp &gr : launches) {
+            if (gr.sg != sg) continue;
+            void *A = b->dargs[par];
+            BMap *M = b->dmap[par] + gr.off;
+            void *kargs[] = {&A, &M};
+            cudaError_t e = cudaLaunchKernel(gr.fn, dim3((unsigned)gr.cnt), dim3(gr.block), kargs, gr.smem, s);
+            if (e != cudaSuccess && le == cudaSuccess) le = e;
+        }
+        if (G > 1) {
+            cudaEventRecord(b->join[sg], s);
+            cudaStreamWaitEvent(b->stream, b->join[sg], 0);
+        }
+    }
+    k_batch_gather<<<(n + 127) / 128, 128, 0, b->stream>>>(n, b->dpres, b->dscal);
+    cudaMemcpyAsync(b->hpres, b->dpres, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+    if (le != cudaSuccess || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        set_error(std::string("batch work-list capture: ") + cudaGetErrorString(le != cudaSuccess ? le : e));
+        return C3D_ECUDA;
+    }
+    if (b->exec[par]) cudaGraphExecDestroy(b->exec[par]);
+    b->exec[par] = nullptr;
+    e = cudaGraphInstantiate(&b->exec[par], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        set_error(std::string("batch graph instantiate: ") + cudaGetErrorString(e));
+        return C3D_ECUDA;
+    }
+    b->gdt[par].assign(dt, dt + n);
+    b->launches = (int)launches.size() + 2;
+    return 0;
+}
+
 // Captures the ensemble step for the parity the channels move to; leaves ch->cur there.
 static int batch_capture(c3d_batch *b, const double *dt, int par) {
+    if (b->form == C3D_BATCH_WORKLIST && batch_worklist_ok(b)) return batch_capture_worklist(b, dt, par);
     const int n = (int)b->ch.size();
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
@@ -1893,6 +2034,38 @@ int c3d_batch_step(c3d_batch *b, int ntime, const double *dt, double *presg, dou
         presg[i] = b->hpres[2 * i];
         presg3[i] = b->hpres[2 * i + 1];
     }
+    return 0;
+}
+
+int c3d_batch_set_form(c3d_batch *b, int form) {
+    if (!b || (form != C3D_BATCH_STREAMS && form != C3D_BATCH_WORKLIST)) { set_error("bad batch form"); return C3D_EINVAL; }
+    CK(cudaStreamSynchronize(b->stream));
+    if (form != b->form)
+        for (int p = 0; p < 2; ++p) {
+            if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
+            b->exec[p] = nullptr;
+            b->gdt[p].clear();
+        }
+    b->form = form;
+    return 0;
+}
+
+int c3d_batch_set_groups(c3d_batch *b, int groups) {
+    if (!b || groups < 1 || groups > 64) { set_error("groups must be in [1, 64]"); return C3D_EINVAL; }
+    CK(cudaStreamSynchronize(b->stream));
+    if (groups != b->groups)
+        for (int p = 0; p < 2; ++p) {
+            if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
+            b->exec[p] = nullptr;
+            b->gdt[p].clear();
+        }
+    b->groups = groups;
+    return 0;
+}
+
+int c3d_batch_get_form(c3d_batch *b, int *form) {
+    if (!b || !form) { set_error("null argument"); return C3D_EINVAL; }
+    *form = (b->form == C3D_BATCH_WORKLIST && batch_worklist_ok(b)) ? C3D_BATCH_WORKLIST : C3D_BATCH_STREAMS;
     return 0;
 }
 

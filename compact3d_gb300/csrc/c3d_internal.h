@@ -69,7 +69,18 @@ struct StepArgs {
     const float2 *twx32;
     double dt;                          // DT of the step (1 for the projection)
     int bulk;                           // apply the bulk-flow forcing (GETUP) or not (projection)
+    const R *ycnw;                      // the CN wall-normal factors in precision R
 };
+
+// ---- work-list launches of a batch of channels -----------------------------------
+// One launch of a step pass covers every channel of a group (channels whose kernel for
+// that pass is the same template instance with the same block shape): block q of the
+// launch runs block (x, y) of channel ch's own grid, whose x extent is gx.
+struct BMap { int ch; unsigned x, y, gx; };
+// One pass of one channel in the batch form: the batch kernel (its template instance is
+// the group key), the block size, dynamic shared memory and the blocks of the channel's
+// own grid.  Batch kernels take (const StepArgs<R> *args, const BMap *map).
+struct BKern { const void *fn; unsigned block; size_t smem; unsigned nblocks; };
 
 // Blocks of the first level of the bulk-flow reduction; `part` holds 2 N2M N3M per-row
 // partials followed by 2 RB block sums.
@@ -272,6 +283,15 @@ int launch_refine(c3d_channel *ch, StepArgs<float> &a, RefArgs &r, int *nl);    
 int launch_project(c3d_channel *ch, int *launches);
 int launch_diag(c3d_channel *ch, int *launches);
 int launch_pipe_selftest(c3d_channel *ch, double limit_ms);
+// Batch form of the DNS step (FILES = 0; precision C3D_FP64 or C3D_MIXED): the passes of
+// one channel's step in order (batch_plan), and its StepArgs<R> for the step with DT dt
+// written as bytes to dst (batch_args, batch_args_size bytes).
+template <typename R> int xpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);
+template <typename R> int zpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);
+template <typename R> int spec_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);
+int batch_plan(c3d_channel *ch, std::vector<BKern> &out);
+size_t batch_args_size(const c3d_channel *ch);
+void batch_args(c3d_channel *ch, double dt, void *dst);
 int launch_poisson_tables(c3d_channel *ch);
 // what: 0 U component, 1 P, 2 HH component, 3 SGSVIS (to host), 4 operand (to device),
 // 5 operator result (to host)

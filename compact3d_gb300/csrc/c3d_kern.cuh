@@ -655,11 +655,15 @@ __device__ __forceinline__ void atomic_max_nonneg(double *addr, double v) {
 
 inline int nblk(long long n, int b = TPB) { return (int)((n + b - 1) / b); }
 
+// Block coordinates of a kernel body within its channel's own grid: the launch's block
+// index for a single channel, the mapped one when a launch covers a batch of channels.
+struct Blk { unsigned x, y, gx; };
+
 // z-direction thread mapping: thread per (i, segment of L points, plane j >= jlo)
 template <int L>
-__device__ __forceinline__ bool zcoord(const Geo &g, int jlo, int &i, int &j, int &k0) {
+__device__ __forceinline__ bool zcoord(const Blk blk, const Geo &g, int jlo, int &i, int &j, int &k0) {
     // 32-bit index arithmetic: a grid has fewer than 2^32 threads (N / L points)
-    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned tid = blk.x * blockDim.x + threadIdx.x;
     const unsigned nseg = (unsigned)(g.n3m / L), n1 = (unsigned)g.n1m;
     const unsigned tot = (unsigned)(g.n2m - jlo + 1) * nseg * n1;
     if (tid >= tot) return false;
@@ -669,6 +673,11 @@ __device__ __forceinline__ bool zcoord(const Geo &g, int jlo, int &i, int &j, in
     k0 = (int)(rest - jq * nseg) * L;
     j = jlo + (int)jq;
     return true;
+}
+
+template <int L>
+__device__ __forceinline__ bool zcoord(const Geo &g, int jlo, int &i, int &j, int &k0) {
+    return zcoord<L>(Blk{blockIdx.x, blockIdx.y, gridDim.x}, g, jlo, i, j, k0);
 }
 
 constexpr int ZL = 16;   // z segment length

@@ -6,14 +6,14 @@ namespace c3d {
 
 // Complex FFT along kz of a tile of `tw` kx columns of one plane, in shared memory.
 template <typename R>
-__global__ void __launch_bounds__(TPB) k_fftz(StepArgs<R> a, int sign, int tw) {
+__device__ __forceinline__ void b_fftz(const StepArgs<R> &a, int sign, int tw, const Blk blk) {
     typedef typename Cx<R>::T C2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Geo g = a.g;
     const int n = g.n3m;
     C2 *A = reinterpret_cast<C2 *>(smem_raw), *B = A + n * tw;
     const int ntile = (g.n1h + tw - 1) / tw;
-    const int plane = blockIdx.x / ntile, tile = blockIdx.x % ntile;
+    const int plane = blk.x / ntile, tile = blk.x % ntile;
     const int kx0 = tile * tw;
     const int w = min(tw, g.n1h - kx0);
     C2 *S = reinterpret_cast<C2 *>(a.spec) + (long long)plane * n * g.n1h + kx0;
@@ -30,6 +30,10 @@ __global__ void __launch_bounds__(TPB) k_fftz(StepArgs<R> a, int sign, int tw) {
         if (l < w) S[q * g.n1h + l] = Z[e];
     }
 }
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_fftz(StepArgs<R> a, int sign, int tw) {
+    b_fftz<R>(a, sign, tw, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
 
 // Complex FFT along kz, one warp per kx column, for N3M = 32 N1 (four-step form).  The
 // block stages a tile of TWW kx columns of one plane in shared memory (coalesced rows,
@@ -41,7 +45,7 @@ __global__ void __launch_bounds__(TPB) k_fftz(StepArgs<R> a, int sign, int tw) {
 constexpr int TWW = 16;    // kx columns per block
 constexpr int FZW = 8;     // warps per block
 template <typename R, int N1, int SIGN>
-__global__ void __launch_bounds__(FZW * 32) k_fftz4(StepArgs<R> a) {
+__device__ __forceinline__ void b_fftz4(const StepArgs<R> &a, const Blk blk) {
     typedef typename Cx<R>::T C2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2 *T = reinterpret_cast<C2 *>(smem_raw);
@@ -49,7 +53,7 @@ __global__ void __launch_bounds__(FZW * 32) k_fftz4(StepArgs<R> a) {
     constexpr int n = 32 * N1, pitch = TWW + 1;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int ntile = (g.n1h + TWW - 1) / TWW;
-    const int plane = blockIdx.x / ntile, kx0 = (blockIdx.x % ntile) * TWW;
+    const int plane = blk.x / ntile, kx0 = (blk.x % ntile) * TWW;
     const int w = min(TWW, g.n1h - kx0);
     C2 *S = reinterpret_cast<C2 *>(a.spec) + (long long)plane * n * g.n1h + kx0;
     const C2 *tw = twsel<C2>(a.fz);
@@ -103,6 +107,10 @@ __global__ void __launch_bounds__(FZW * 32) k_fftz4(StepArgs<R> a) {
         if (l < w) S[q * g.n1h + l] = T[q * pitch + l];
     }
 }
+template <typename R, int N1, int SIGN>
+__global__ void __launch_bounds__(FZW * 32) k_fftz4(StepArgs<R> a) {
+    b_fftz4<R, N1, SIGN>(a, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
 
 // One Thomas solve per mode (kx, kz) with A_J = PMJ, B_J = PCJ - AK3 - AK1, C_J = PPJ,
 // factors tabulated by k_ptables; the (0,0) mode has row 1 = (0, 1, 0 | 0) and the
@@ -114,10 +122,10 @@ __global__ void __launch_bounds__(FZW * 32) k_fftz4(StepArgs<R> a) {
 // The j loops load UJ planes ahead so that the sequential chain does not wait on memory.
 constexpr int UJ = 8;
 
-__global__ void __launch_bounds__(TPB) k_poisson64(StepArgs<double> a) {
+__device__ __forceinline__ void b_poisson64(const StepArgs<double> &a, const Blk blk) {
     const Geo g = a.g;
     const int nm = g.n1h * g.n3m;
-    const int mode = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mode = blk.x * blockDim.x + threadIdx.x;
     if (mode >= nm) return;
     const int kx = mode % g.n1h, kz = mode / g.n1h;
     const bool selfc = (kx == 0 || kx == g.n1m / 2) && (kz == 0 || kz == g.n3m / 2);
@@ -166,11 +174,14 @@ __global__ void __launch_bounds__(TPB) k_poisson64(StepArgs<double> a) {
             if (jt - u >= 0) S[(jt - u) * s] = q[u];
     }
 }
+__global__ void __launch_bounds__(TPB) k_poisson64(StepArgs<double> a) {
+    b_poisson64(a, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
 
-__global__ void __launch_bounds__(TPB) k_poisson32(StepArgs<float> a) {
+__device__ __forceinline__ void b_poisson32(const StepArgs<float> &a, const Blk blk) {
     const Geo g = a.g;
     const int nm = g.n1h * g.n3m;
-    const int mode = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mode = blk.x * blockDim.x + threadIdx.x;
     if (mode >= nm) return;
     const int kx = mode % g.n1h, kz = mode / g.n1h;
     const bool selfc = (kx == 0 || kx == g.n1m / 2) && (kz == 0 || kz == g.n3m / 2);
@@ -233,6 +244,9 @@ __global__ void __launch_bounds__(TPB) k_poisson32(StepArgs<float> a) {
             q[u] = qn[u]; gm[u] = gmn[u];
         }
     }
+}
+__global__ void __launch_bounds__(TPB) k_poisson32(StepArgs<float> a) {
+    b_poisson32(a, Blk{blockIdx.x, blockIdx.y, gridDim.x});
 }
 
 // Factor tables of TDMAP's recurrence for every mode (FP64; double-float copies when rb32 != 0).
@@ -299,6 +313,71 @@ static bool launch_fftz4(c3d_channel *ch, StepArgs<R> &a) {
     fn<<<grid, blk, sm, ch->stream>>>(a);
     return true;
 }
+
+// ---------------------------------------------------------------------------------
+// Batch form: the z FFTs of the channels with the same N3M in one launch (the four-step
+// warp form when N3M = 32 N1, tiles of 8 kx columns in shared memory otherwise) and the
+// Poisson solves of every channel in one launch.
+// ---------------------------------------------------------------------------------
+constexpr int TW_BATCH = 8;
+
+template <typename R, int N1, int SIGN>
+__global__ void __launch_bounds__(FZW * 32) kb_fftz4(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    b_fftz4<R, N1, SIGN>(A[m.ch], Blk{m.x, m.y, m.gx});
+}
+template <typename R, int SIGN>
+__global__ void __launch_bounds__(TPB) kb_fftz(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    b_fftz<R>(A[m.ch], SIGN, TW_BATCH, Blk{m.x, m.y, m.gx});
+}
+__global__ void __launch_bounds__(TPB) kb_poisson64(const StepArgs<double> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    b_poisson64(A[m.ch], Blk{m.x, m.y, m.gx});
+}
+__global__ void __launch_bounds__(TPB) kb_poisson32(const StepArgs<float> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    b_poisson32(A[m.ch], Blk{m.x, m.y, m.gx});
+}
+
+template <typename R, int SIGN>
+static const void *fftz4_batch_fn(int n1) {
+    switch (n1) {
+        case 2: return (const void *)kb_fftz4<R, 2, SIGN>;
+        case 3: return (const void *)kb_fftz4<R, 3, SIGN>;
+        case 4: return (const void *)kb_fftz4<R, 4, SIGN>;
+        case 6: return (const void *)kb_fftz4<R, 6, SIGN>;
+        case 8: return (const void *)kb_fftz4<R, 8, SIGN>;
+        case 12: return (const void *)kb_fftz4<R, 12, SIGN>;
+        case 16: return (const void *)kb_fftz4<R, 16, SIGN>;
+        default: return nullptr;
+    }
+}
+
+template <typename R>
+int spec_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out) {
+    typedef typename Cx<R>::T C2;
+    const Geo &g = ch->g;
+    if (which == 1) {
+        const void *fn = sizeof(R) == 8 ? (const void *)kb_poisson64 : (const void *)kb_poisson32;
+        out.push_back({fn, TPB, 0, (unsigned)nblk((long long)g.n1h * g.n3m)});
+        return 0;
+    }
+    if (which != 0 && which != 2) return C3D_EINVAL;
+    const void *f4 = nullptr;
+    if (g.n3m % 32 == 0) f4 = which == 0 ? fftz4_batch_fn<R, -1>(g.n3m / 32) : fftz4_batch_fn<R, +1>(g.n3m / 32);
+    const size_t sm4 = (size_t)g.n3m * (TWW + 1) * sizeof(C2);
+    if (f4 && sm4 <= 227 * 1024) {
+        out.push_back({f4, FZW * 32, sm4, (unsigned)(g.n2m * ((g.n1h + TWW - 1) / TWW))});
+        return 0;
+    }
+    const size_t smz = 2 * (size_t)g.n3m * TW_BATCH * sizeof(C2);
+    const void *fn = which == 0 ? (const void *)kb_fftz<R, -1> : (const void *)kb_fftz<R, +1>;
+    out.push_back({fn, TPB, smz, (unsigned)(g.n2m * ((g.n1h + TW_BATCH - 1) / TW_BATCH))});
+    return 0;
+}
+template int spec_bkern<double>(const c3d_channel *, int, std::vector<BKern> &);
+template int spec_bkern<float>(const c3d_channel *, int, std::vector<BKern> &);
 
 template <typename R>
 int launch_spec(c3d_channel *ch, StepArgs<R> &a, int which, int *nl) {

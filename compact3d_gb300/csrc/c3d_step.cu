@@ -16,6 +16,7 @@
 //   reduce  DMPRESG, DMPRESG3 (FP64), PRESG, PRESG3
 //   zE      dDP/dz, u/v/w update, P += DP (UPCALC)
 #include <string.h>
+#include <type_traits>
 #include <vector>
 #include "c3d_kern.cuh"
 
@@ -25,10 +26,10 @@ int launch_ptables(c3d_channel *ch, const double *ak1, const double *ak3, const 
                    const double *pp);
 
 template <typename R>
-__global__ void k_bcond(Geo g, typename SType<R>::S *u, typename SType<R>::S *v, typename SType<R>::S *w) {
+__device__ __forceinline__ void b_bcond(Geo g, typename SType<R>::S *u, typename SType<R>::S *v, typename SType<R>::S *w, const Blk blk) {
     typedef typename SType<R>::S S;
     typedef St<R> ST;
-    int id = blockIdx.x * blockDim.x + threadIdx.x;
+    int id = blk.x * blockDim.x + threadIdx.x;
     if (id >= g.np) return;
     const long long b0 = id, bt = (long long)g.n2 * g.np + id, bm = (long long)g.n2m * g.np + id;
     const S z = S();
@@ -41,15 +42,19 @@ __global__ void k_bcond(Geo g, typename SType<R>::S *u, typename SType<R>::S *v,
     v[bt] = z;
     w[bt] = ST::scale(w[bm], top);
 }
+template <typename R>
+__global__ void k_bcond(Geo g, typename SType<R>::S *u, typename SType<R>::S *v, typename SType<R>::S *w) {
+    b_bcond<R>(g, u, v, w, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
 
 // Wall-normal CN factor (TDMAI, compact3d.f:8630-8659), one thread per (i, k), in place.
 // The factors (A, 1/BET, GAM per J) are in the working precision; the j loops load UY
 // planes ahead so that the sequential chain does not wait on memory.
 constexpr int UY = 32;   // planes per batch (8: 0.273 ms, 16: 0.265, 32: 0.252 on channel384)
 template <typename R>
-__global__ void __launch_bounds__(TPB) k_ycn(StepArgs<R> a, const R *ycn) {
+__device__ __forceinline__ void b_ycn(const StepArgs<R> &a, const R *ycn, const Blk blk) {
     const Geo g = a.g;
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long tid = (long long)blk.x * blockDim.x + threadIdx.x;
     if (tid >= 3LL * g.np) return;
     const int c = (int)(tid / g.np);
     const int col = (int)(tid % g.np);
@@ -92,6 +97,10 @@ __global__ void __launch_bounds__(TPB) k_ycn(StepArgs<R> a, const R *ycn) {
             if (j0 - u >= js) X[(j0 - u) * s] = q[u];
     }
 }
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_ycn(StepArgs<R> a, const R *ycn) {
+    b_ycn<R>(a, ycn, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
 
 // DMPRESG / DMPRESG3 in FP64 with a fixed summation order; PRESG += DMPRESG (UPCALC)
 // UPCALC's forcing (compact3d.f:1052-1238) from the summed CN increments of u and w.
@@ -126,10 +135,10 @@ struct AddDF {
 };
 
 template <typename A>
-__global__ void __launch_bounds__(256) k_reduce1(Geo g, typename A::T *part) {
+__device__ __forceinline__ void b_reduce1(Geo g, typename A::T *part, const Blk blk) {
     typedef typename A::T T;
     const int nrows = g.n2m * g.n3m;
-    const int chunk = (nrows + RB - 1) / RB, r0 = blockIdx.x * chunk, r1 = min(nrows, r0 + chunk);
+    const int chunk = (nrows + RB - 1) / RB, r0 = blk.x * chunk, r1 = min(nrows, r0 + chunk);
     __shared__ T sh1[256], sh3[256];
     T s1 = A::zero(), s3 = A::zero();
     for (int r = r0 + (int)threadIdx.x; r < r1; r += 256) {
@@ -147,13 +156,17 @@ __global__ void __launch_bounds__(256) k_reduce1(Geo g, typename A::T *part) {
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        part[2 * nrows + blockIdx.x] = sh1[0];
-        part[2 * nrows + RB + blockIdx.x] = sh3[0];
+        part[2 * nrows + blk.x] = sh1[0];
+        part[2 * nrows + RB + blk.x] = sh3[0];
     }
+}
+template <typename A>
+__global__ void __launch_bounds__(256) k_reduce1(Geo g, typename A::T *part) {
+    b_reduce1<A>(g, part, Blk{blockIdx.x, blockIdx.y, gridDim.x});
 }
 
 template <typename A>
-__global__ void __launch_bounds__(RB) k_reduce2(Geo g, const typename A::T *part, double *scal, double dt, int bulk) {
+__device__ __forceinline__ void b_reduce2(Geo g, const typename A::T *part, double *scal, double dt, int bulk, const Blk blk) {
     typedef typename A::T T;
     const int nrows = g.n2m * g.n3m;
     __shared__ T sh1[RB], sh3[RB];
@@ -168,6 +181,10 @@ __global__ void __launch_bounds__(RB) k_reduce2(Geo g, const typename A::T *part
         __syncthreads();
     }
     if (threadIdx.x == 0) finish_bulk(g, A::dbl(sh1[0]), A::dbl(sh3[0]), scal, dt, bulk);
+}
+template <typename A>
+__global__ void __launch_bounds__(RB) k_reduce2(Geo g, const typename A::T *part, double *scal, double dt, int bulk) {
+    b_reduce2<A>(g, part, scal, dt, bulk, Blk{blockIdx.x, blockIdx.y, gridDim.x});
 }
 
 // CHKMF (compact3d.f:9463-9503) and WALLSS (11077-11143): one block, FP64, fixed order.
@@ -322,6 +339,7 @@ static StepArgs<R> make_args(c3d_channel *ch, double dt) {
     a.twx32 = ch->tw32 + (ch->g.n1m / 2) + ch->g.n3m;
     a.dt = dt;
     a.bulk = 1;
+    a.ycnw = sizeof(R) == 8 ? (const R *)ch->ycn : (const R *)ch->ycn32;
     a.re1 = (R)(1.0 / ch->g.re);
     a.f12x = (R)(12.0 * ch->g.dx1q);
     a.f24x = (R)(24.0 * ch->g.dx1);
@@ -458,6 +476,78 @@ static int step_impl(c3d_channel *ch, double dt, int *nl) {
     if ((rc = launch_zpass<R>(ch, a, 2, dd0, dd1, dd2, 0, nl))) return rc;    // zC
     if ((rc = pressure_and_update<R>(ch, a, dd0, dd1, dd2, 1, nl))) return rc;
     return refine_pressure<R>(ch, a, 1, nl);
+}
+
+// ---------------------------------------------------------------------------------
+// Batch form of the DNS step (the passes of step_impl without SGS model, in order): the
+// small kernels here, the x, z and spectral passes from their files.
+// ---------------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(TPB) kb_bcond(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    const StepArgs<R> &a = A[m.ch];
+    b_bcond<R>(a.g, a.u, a.v, a.w, Blk{m.x, m.y, m.gx});
+}
+template <typename R>
+__global__ void __launch_bounds__(TPB) kb_ycn(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    const StepArgs<R> &a = A[m.ch];
+    b_ycn<R>(a, a.ycnw, Blk{m.x, m.y, m.gx});
+}
+template <typename R, typename Add>
+__global__ void __launch_bounds__(256) kb_reduce1(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    const StepArgs<R> &a = A[m.ch];
+    b_reduce1<Add>(a.g, reinterpret_cast<typename Add::T *>(a.part), Blk{m.x, m.y, m.gx});
+}
+template <typename R, typename Add>
+__global__ void __launch_bounds__(RB) kb_reduce2(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    const StepArgs<R> &a = A[m.ch];
+    b_reduce2<Add>(a.g, reinterpret_cast<const typename Add::T *>(a.part), a.scal, a.dt, a.bulk, Blk{m.x, m.y, m.gx});
+}
+
+template <typename R>
+static int batch_plan_t(c3d_channel *ch, std::vector<BKern> &out) {
+    typedef typename std::conditional<sizeof(R) == 8, AddF64, AddDF>::type Add;
+    const Geo &g = ch->g;
+    int rc;
+    out.push_back({(const void *)kb_bcond<R>, TPB, 0, (unsigned)nblk(g.np)});
+    if ((rc = xpass_bkern<R>(ch, 0, out))) return rc;      // xA (u, v, w)
+    if ((rc = zpass_bkern<R>(ch, 0, out))) return rc;      // zA (u, w and P, v)
+    if ((rc = zpass_bkern<R>(ch, 1, out))) return rc;      // zB
+    if ((rc = xpass_bkern<R>(ch, 1, out))) return rc;      // xB
+    out.push_back({(const void *)kb_ycn<R>, TPB, 0, (unsigned)nblk(3LL * g.np)});
+    if ((rc = zpass_bkern<R>(ch, 2, out))) return rc;      // zC
+    if ((rc = zpass_bkern<R>(ch, 3, out))) return rc;      // zD
+    if ((rc = xpass_bkern<R>(ch, 2, out))) return rc;      // xC
+    if ((rc = spec_bkern<R>(ch, 0, out))) return rc;       // fftz forward
+    if ((rc = spec_bkern<R>(ch, 1, out))) return rc;       // Poisson
+    if ((rc = spec_bkern<R>(ch, 2, out))) return rc;       // fftz inverse
+    if ((rc = xpass_bkern<R>(ch, 3, out))) return rc;      // xD
+    out.push_back({(const void *)kb_reduce1<R, Add>, 256, 0, (unsigned)RB});
+    out.push_back({(const void *)kb_reduce2<R, Add>, RB, 0, 1u});
+    return zpass_bkern<R>(ch, 4, out);                     // zE
+}
+
+int batch_plan(c3d_channel *ch, std::vector<BKern> &out) {
+    if (ch->files != 0 || ch->refine) { set_error("the batch form runs DNS channels without refinement"); return C3D_EINVAL; }
+    if (ch->precision == C3D_MIXED) return batch_plan_t<float>(ch, out);
+    return batch_plan_t<double>(ch, out);
+}
+
+size_t batch_args_size(const c3d_channel *ch) {
+    return ch->precision == C3D_MIXED ? sizeof(StepArgs<float>) : sizeof(StepArgs<double>);
+}
+
+void batch_args(c3d_channel *ch, double dt, void *dst) {
+    if (ch->precision == C3D_MIXED) {
+        StepArgs<float> a = make_args<float>(ch, dt);
+        memcpy(dst, &a, sizeof(a));
+    } else {
+        StepArgs<double> a = make_args<double>(ch, dt);
+        memcpy(dst, &a, sizeof(a));
+    }
 }
 
 template <typename R>

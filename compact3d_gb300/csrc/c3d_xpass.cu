@@ -228,7 +228,7 @@ __device__ __forceinline__ void xa_piece(const StepArgs<R> &a, int j, long long 
 // (the split form has fewer registers per thread; PART 2 reads the two u rows of the
 // y-face interpolant again).
 template <typename R, int C, int PART>
-__global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
+__device__ __forceinline__ void b_xA(const StepArgs<R> &a, const Blk blk) {
     typedef typename SType<R>::S S;
     typedef St<R> ST;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
     const int nrows = g.n2m * g.n3m;
     const R RE1 = a.re1, f12 = a.f12x, f24 = a.f24x, four = (R)4.0;
     const R presg = (R)a.scal[SCAL_PRESG];
-    for (int row = blockIdx.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += gridDim.x * (int)(blockDim.x >> 5)) {
+    for (int row = blk.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += blk.gx * (int)(blockDim.x >> 5)) {
         const int j = 1 + row / g.n3m, k = row % g.n3m;
         const long long o = fidx(g, 0, j, k), om = fidx(g, 0, j - 1, k), op = fidx(g, 0, j + 1, k);
         {   // every row this warp reads, requested from DRAM at once
@@ -379,6 +379,10 @@ __global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
         }
     }
 }
+template <typename R, int C, int PART>
+__global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
+    b_xA<R, C, PART>(a, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
 
 // The u, v or w piece of xA with the rows it reads staged in shared memory: lane 0 of
 // each warp issues one bulk copy per row (cp.async.bulk, completion counted on one
@@ -484,7 +488,7 @@ __device__ __forceinline__ void ab2_cnx(const StepArgs<R> &a, int c, long long o
 }
 
 template <typename R, int C>
-__global__ void __launch_bounds__(XMAXT) k_xB(StepArgs<R> a) {
+__device__ __forceinline__ void b_xB(const StepArgs<R> &a, const Blk blk) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Geo g = a.g;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -493,7 +497,7 @@ __global__ void __launch_bounds__(XMAXT) k_xB(StepArgs<R> a) {
     const int nrows = g.n2m * g.n3m;
     const R f = a.f24x;
     const R dt = (R)a.dt;
-    for (int row = blockIdx.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += gridDim.x * (int)(blockDim.x >> 5)) {
+    for (int row = blk.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += blk.gx * (int)(blockDim.x >> 5)) {
         const int j = 1 + row / g.n3m, k = row % g.n3m;
         const long long o = fidx(g, 0, j, k), op = fidx(g, 0, j + 1, k);
         {
@@ -565,6 +569,10 @@ __global__ void __launch_bounds__(XMAXT) k_xB(StepArgs<R> a) {
         srow_store(a.hh[2] + o, h3, sb, lane, P);
         ab2_cnx(a, 2, o, h3, sb, lane, P, dt);
     }
+}
+template <typename R, int C>
+__global__ void __launch_bounds__(XMAXT) k_xB(StepArgs<R> a) {
+    b_xB<R, C>(a, Blk{blockIdx.x, blockIdx.y, gridDim.x});
 }
 
 // ---------------------------------------------------------------------------------
@@ -670,7 +678,7 @@ __device__ __forceinline__ void xc_row(const StepArgs<R> &a, int j, int k, const
 // computes the current one.
 // ---------------------------------------------------------------------------------
 template <typename R, int C, int NS, bool X4 = false>
-__global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const R *d1) {
+__device__ __forceinline__ void b_xC(const StepArgs<R> &a, const R *d0, const R *d1, const Blk blk) {
     typedef typename SType<R>::S S;
     typedef typename Cx<R>::T C2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -683,7 +691,7 @@ __global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const 
         const size_t sbytes = stage_bytes(g.n1m, C);
         unsigned char *wb = smem_raw + wid * (sbytes + fbytes);
         C2 *bufa = reinterpret_cast<C2 *>(wb + sbytes);
-        for (int row = blockIdx.x * wpb + wid; row < nrows; row += gridDim.x * wpb) {
+        for (int row = blk.x * wpb + wid; row < nrows; row += blk.gx * wpb) {
             const int j = 1 + row / g.n3m, k = row % g.n3m;
             const long long o = fidx(g, 0, j, k), op = fidx(g, 0, j + 1, k);
             {
@@ -704,7 +712,7 @@ __global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const 
         uint64_t *bar = reinterpret_cast<uint64_t *>(wb);
         unsigned char *stg = wb + 16 * NS;
         C2 *bufa = reinterpret_cast<C2 *>(stg + (size_t)NS * L.bytes);
-        const int nw = gridDim.x * wpb, gw = blockIdx.x * wpb + wid;
+        const int nw = blk.gx * wpb, gw = blk.x * wpb + wid;
         const uint32_t sS = g.n1m * (uint32_t)sizeof(S), sR = g.n1m * (uint32_t)sizeof(R);
         if (lane == 0) {
             for (int s = 0; s < NS; ++s) mbar_init(bar + s, 1);
@@ -745,12 +753,16 @@ __global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const 
         }
     }
 }
+template <typename R, int C, int NS, bool X4 = false>
+__global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const R *d1) {
+    b_xC<R, C, NS, X4>(a, d0, d1, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
 
 // ---------------------------------------------------------------------------------
 // xD: complex-to-real FFT -> DP, compact dDP/dx, bulk-flow partial sums
 // ---------------------------------------------------------------------------------
 template <typename R, int C, bool X4 = false>
-__global__ void __launch_bounds__(XMAXT) k_xD(StepArgs<R> a, const R *d0, const R *d2) {
+__device__ __forceinline__ void b_xD(const StepArgs<R> &a, const R *d0, const R *d2, const Blk blk) {
     typedef typename Cx<R>::T C2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Geo g = a.g;
@@ -767,7 +779,7 @@ __global__ void __launch_bounds__(XMAXT) k_xD(StepArgs<R> a, const R *d0, const 
     if constexpr (sizeof(R) == 8) twx = reinterpret_cast<const C2 *>(a.twx64);
     else twx = reinterpret_cast<const C2 *>(a.twx32);
     const R scale = a.xscale, f24 = a.f24x;
-    for (int row = blockIdx.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += gridDim.x * (int)(blockDim.x >> 5)) {
+    for (int row = blk.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += blk.gx * (int)(blockDim.x >> 5)) {
         const int j = 1 + row / g.n3m, k = row % g.n3m;
         const long long o = fidx(g, 0, j, k);
         const C2 *Sp = reinterpret_cast<const C2 *>(a.spec) + ((long long)(j - 1) * g.n3m + k) * g.n1h;
@@ -861,6 +873,10 @@ __global__ void __launch_bounds__(XMAXT) k_xD(StepArgs<R> a, const R *d0, const 
             }
         }
     }
+}
+template <typename R, int C, bool X4 = false>
+__global__ void __launch_bounds__(XMAXT) k_xD(StepArgs<R> a, const R *d0, const R *d2) {
+    b_xD<R, C, X4>(a, d0, d2, Blk{blockIdx.x, blockIdx.y, gridDim.x});
 }
 
 // ---------------------------------------------------------------------------------
@@ -1026,7 +1042,7 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
             bool done = false;
             if constexpr (sizeof(R) == 4) {
                 constexpr bool X4 = (C % 2 == 0);
-                if (X4 && ch->tune.fxp == 3) {
+                if (X4 && ch->tune.fxp == 3 && ch->g.n1m == 32 * C) {
                     if (ch->tune.xbulk == 2) done = launch_xc_bulk<R, C, 2, X4>(ch, a, xw, p0, p1);
                     else if (ch->tune.xbulk == 3) done = launch_xc_bulk<R, C, 3, X4>(ch, a, xw, p0, p1);
                 } else {
@@ -1034,7 +1050,8 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
                     else if (ch->tune.xbulk == 3) done = launch_xc_bulk<R, C, 3, false>(ch, a, xw, p0, p1);
                 }
             }
-            if (!done && C % 2 == 0 && ch->tune.fxp == 3) {   // register row FFT: no shared memory
+            // register row FFT (all 32 lanes hold a chunk: N1M = 32 C, C even): no shared memory
+            if (!done && C % 2 == 0 && ch->tune.fxp == 3 && ch->g.n1m == 32 * C) {
                 k_xC<R, C, 0, (C % 2 == 0)><<<grid, nt, sb, st>>>(a, p0, p1);
                 done = true;
             }
@@ -1046,7 +1063,7 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
             break;
         }
         case 3:
-            if (C % 2 == 0 && ch->tune.fxp == 3) {
+            if (C % 2 == 0 && ch->tune.fxp == 3 && ch->g.n1m == 32 * C) {
                 k_xD<R, C, (C % 2 == 0)><<<grid, nt, sb, st>>>(a, p0, p1);
             } else {
                 cudaFuncSetAttribute(k_xD<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
@@ -1066,6 +1083,80 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
     }
     return 0;
 }
+
+// ---------------------------------------------------------------------------------
+// Batch form: one launch per pass covers the channels whose x rows split into the same
+// lane chunk C (and, for xC and xD, the same row-FFT form).  Rows per block XW_BATCH; xA
+// as its u, v and w pieces with rows read from global memory.  The work arrays of the
+// pressure passes are the channel's exz / eyz / wsq, as in the step.
+// ---------------------------------------------------------------------------------
+constexpr int XW_BATCH = 2;
+
+template <typename R, int C, int PART>
+__global__ void __launch_bounds__(XMAXT) kb_xA(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    b_xA<R, C, PART>(A[m.ch], Blk{m.x, m.y, m.gx});
+}
+template <typename R, int C>
+__global__ void __launch_bounds__(XMAXT) kb_xB(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    b_xB<R, C>(A[m.ch], Blk{m.x, m.y, m.gx});
+}
+template <typename R, int C, bool X4>
+__global__ void __launch_bounds__(XMAXT) kb_xC(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    const StepArgs<R> &a = A[m.ch];
+    b_xC<R, C, 0, X4>(a, a.exz, a.eyz, Blk{m.x, m.y, m.gx});
+}
+template <typename R, int C, bool X4>
+__global__ void __launch_bounds__(XMAXT) kb_xD(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    const StepArgs<R> &a = A[m.ch];
+    b_xD<R, C, X4>(a, a.exz, a.wsq, Blk{m.x, m.y, m.gx});
+}
+
+template <typename R, int C>
+static int xbk(const c3d_channel *ch, int which, std::vector<BKern> &out) {
+    typedef typename Cx<R>::T C2;
+    const int nrows = ch->g.n2m * ch->g.n3m;
+    const unsigned nb = (unsigned)nblk(nrows, XW_BATCH), nt = XW_BATCH * 32;
+    const size_t sb = stage_bytes(ch->g.n1m, C) * XW_BATCH;
+    const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(ch->g.n1m / 2 + 1) * sizeof(C2)) * XW_BATCH;
+    const bool x4 = (C % 2 == 0) && ch->g.n1m == 32 * C;   // register row FFT (see launch_x_c)
+    switch (which) {
+        case 0:
+            out.push_back({(const void *)kb_xA<R, C, 1>, nt, sb, nb});
+            out.push_back({(const void *)kb_xA<R, C, 2>, nt, sb, nb});
+            out.push_back({(const void *)kb_xA<R, C, 3>, nt, sb, nb});
+            return 0;
+        case 1: out.push_back({(const void *)kb_xB<R, C>, nt, sb, nb}); return 0;
+        case 2:
+            if (x4) out.push_back({(const void *)kb_xC<R, C, (C % 2 == 0)>, nt, sb, nb});
+            else out.push_back({(const void *)kb_xC<R, C, false>, nt, fb, nb});
+            return 0;
+        case 3:
+            if (x4) out.push_back({(const void *)kb_xD<R, C, (C % 2 == 0)>, nt, sb, nb});
+            else out.push_back({(const void *)kb_xD<R, C, false>, nt, fb, nb});
+            return 0;
+        default: return C3D_EINVAL;
+    }
+}
+
+template <typename R>
+int xpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out) {
+    switch ((ch->g.n1m + 31) / 32) {
+        case 1: return xbk<R, 1>(ch, which, out);
+        case 2: return xbk<R, 2>(ch, which, out);
+        case 3: return xbk<R, 3>(ch, which, out);
+        case 4: return xbk<R, 4>(ch, which, out);
+        case 6: return xbk<R, 6>(ch, which, out);
+        case 8: return xbk<R, 8>(ch, which, out);
+        case 12: return xbk<R, 12>(ch, which, out);
+        default: return C3D_EINVAL;
+    }
+}
+template int xpass_bkern<double>(const c3d_channel *, int, std::vector<BKern> &);
+template int xpass_bkern<float>(const c3d_channel *, int, std::vector<BKern> &);
 
 template <typename R>
 int launch_xpass(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl) {

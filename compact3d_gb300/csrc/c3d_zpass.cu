@@ -49,14 +49,14 @@ struct ZRing {
 // (32 consecutive i, plane) with blockDim.y = N3M / L segments and the exact cyclic
 // solve (zblock).
 template <int L, int MODE>
-__device__ __forceinline__ bool zcoords(const Geo &g, int jlo, int &i, int &j, int &k0) {
+__device__ __forceinline__ bool zcoords(const Blk blk, const Geo &g, int jlo, int &i, int &j, int &k0) {
     if constexpr (MODE == 1) {
-        i = (int)blockIdx.x * 32 + (int)threadIdx.x;
-        j = jlo + (int)blockIdx.y;
+        i = (int)blk.x * 32 + (int)threadIdx.x;
+        j = jlo + (int)blk.y;
         k0 = (int)threadIdx.y * L;
         return true;
     } else {
-        return zcoord<L>(g, jlo, i, j, k0);
+        return zcoord<L>(blk, g, jlo, i, j, k0);
     }
 }
 template <typename R, int L, int M, int NR, int MODE, typename F>
@@ -170,12 +170,12 @@ struct WalkGradZ {
 // PART 0 runs the three sweeps in one kernel; PART 1, 2, 3 run only the u, the (w, P) or
 // the v sweep (the split form has fewer registers per thread and moves the same bytes).
 template <typename R, int L, int PART, int MODE>
-__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zA(StepArgs<R> a) {
+__device__ __forceinline__ void b_zA(const StepArgs<R> &a, const Blk blk) {
     typedef typename SType<R>::S S;
     typedef St<R> ST;
     const Geo g = a.g;
     int i, j, k0;
-    if (!zcoords<L, MODE>(g, 1, i, j, k0)) return;
+    if (!zcoords<L, MODE>(blk, g, 1, i, j, k0)) return;
     const int n = g.n3m, s = g.n1m;
     const R RE1 = a.re1;
     const long long o = fidx(g, i, j, 0);
@@ -244,12 +244,16 @@ __global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zA(StepArgs<R> a) {
         }
     }
 }
+template <typename R, int L, int PART, int MODE>
+__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zA(StepArgs<R> a) {
+    b_zA<R, L, PART, MODE>(a, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
 
 template <typename R, int L, int MODE>
-__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zB(StepArgs<R> a) {
+__device__ __forceinline__ void b_zB(const StepArgs<R> &a, const Blk blk) {
     const Geo g = a.g;
     int i, j, k0;
-    if (!zcoords<L, MODE>(g, 1, i, j, k0)) return;
+    if (!zcoords<L, MODE>(blk, g, 1, i, j, k0)) return;
     const int n = g.n3m, s = g.n1m;
     const long long o = fidx(g, i, j, 0);
     if ((g.n1m & 31) == 0) {
@@ -275,14 +279,18 @@ __global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zB(StepArgs<R> a) {
         if (j >= 2) H2[kk] = H2[kk] + out[2][t];   // d(vw)/dz
     }
 }
+template <typename R, int L, int MODE>
+__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zB(StepArgs<R> a) {
+    b_zB<R, L, MODE>(a, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
 
 // z factor of Crank-Nicolson: r[c] -> d[c] for the three components (the v component at
 // J=1 is computed from zeros and never read)
 template <typename R, int L, int MODE>
-__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zC(StepArgs<R> a, R *d0, R *d1, R *d2) {
+__device__ __forceinline__ void b_zC(const StepArgs<R> &a, R *d0, R *d1, R *d2, const Blk blk) {
     const Geo g = a.g;
     int i, j, k0;
-    if (!zcoords<L, MODE>(g, 1, i, j, k0)) return;
+    if (!zcoords<L, MODE>(blk, g, 1, i, j, k0)) return;
     const int n = g.n3m, s = g.n1m;
     const long long o = fidx(g, i, j, 0);
     if ((g.n1m & 31) == 0) {
@@ -307,13 +315,17 @@ __global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zC(StepArgs<R> a, R 
         D2[kk] = out[2][t];
     }
 }
+template <typename R, int L, int MODE>
+__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zC(StepArgs<R> a, R *d0, R *d1, R *d2) {
+    b_zC<R, L, MODE>(a, d0, d1, d2, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
 
 // z part of RHSDP: rdpz = compact d(UH3)/dz / DT with UH3 = W + delta3
 template <typename R, int L, int MODE>
-__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zD(StepArgs<R> a, const R *d2) {
+__device__ __forceinline__ void b_zD(const StepArgs<R> &a, const R *d2, const Blk blk) {
     const Geo g = a.g;
     int i, j, k0;
-    if (!zcoords<L, MODE>(g, 1, i, j, k0)) return;
+    if (!zcoords<L, MODE>(blk, g, 1, i, j, k0)) return;
     const int n = g.n3m, s = g.n1m;
     const long long o = fidx(g, i, j, 0);
     if ((g.n1m & 31) == 0) {
@@ -331,15 +343,19 @@ __global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zD(StepArgs<R> a, co
 #pragma unroll
     for (int t = 0; t < L; ++t) Q[(k0 + t) * s] = out[0][t] * rdt;
 }
+template <typename R, int L, int MODE>
+__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zD(StepArgs<R> a, const R *d2) {
+    b_zD<R, L, MODE>(a, d2, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
 
 // UPCALC along z and the state update
 template <typename R, int L, int MODE>
-__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zE(StepArgs<R> a, const R *d0, const R *d1, const R *d2, int updp) {
+__device__ __forceinline__ void b_zE(const StepArgs<R> &a, const R *d0, const R *d1, const R *d2, int updp, const Blk blk) {
     typedef typename SType<R>::S S;
     typedef St<R> ST;
     const Geo g = a.g;
     int i, j, k0;
-    if (!zcoords<L, MODE>(g, 1, i, j, k0)) return;
+    if (!zcoords<L, MODE>(blk, g, 1, i, j, k0)) return;
     const int n = g.n3m, s = g.n1m;
     const long long o = fidx(g, i, j, 0);
     const R dt = (R)a.dt;
@@ -374,6 +390,10 @@ __global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zE(StepArgs<R> a, co
         if (j >= 2) V[kk] = Sten<R>::upd(V[kk], D1[kk], dt * (DP[kk] - DPm[kk]) * rHj, R(0));
         if (updp) Pp[kk] = ST::add(Pp[kk], DP[kk]);
     }
+}
+template <typename R, int L, int MODE>
+__global__ void __launch_bounds__(MODE == 1 ? 1024 : TPB) k_zE(StepArgs<R> a, const R *d0, const R *d1, const R *d2, int updp) {
+    b_zE<R, L, MODE>(a, d0, d1, d2, updp, Blk{blockIdx.x, blockIdx.y, gridDim.x});
 }
 
 // DIVCHECK z part and max |div| (FP64)
@@ -423,6 +443,60 @@ int zblock_len(int n3m) {
         if (n3m % L == 0 && n3m / L <= 32) return L;
     return 0;
 }
+
+// ---------------------------------------------------------------------------------
+// Batch form: one launch per pass covers every channel (segment form, segments of ZL
+// points, which divides every supported N3M); zA as its three sweeps; the work arrays
+// are the channel's exz / eyz / wsq as in the step, and zE adds DP to P.
+// ---------------------------------------------------------------------------------
+template <typename R, int PART>
+__global__ void __launch_bounds__(TPB) kb_zA(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    b_zA<R, ZL, PART, 0>(A[m.ch], Blk{m.x, m.y, m.gx});
+}
+template <typename R>
+__global__ void __launch_bounds__(TPB) kb_zB(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    b_zB<R, ZL, 0>(A[m.ch], Blk{m.x, m.y, m.gx});
+}
+template <typename R>
+__global__ void __launch_bounds__(TPB) kb_zC(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    const StepArgs<R> &a = A[m.ch];
+    b_zC<R, ZL, 0>(a, a.exz, a.eyz, a.wsq, Blk{m.x, m.y, m.gx});
+}
+template <typename R>
+__global__ void __launch_bounds__(TPB) kb_zD(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    const StepArgs<R> &a = A[m.ch];
+    b_zD<R, ZL, 0>(a, a.wsq, Blk{m.x, m.y, m.gx});
+}
+template <typename R>
+__global__ void __launch_bounds__(TPB) kb_zE(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
+    const BMap m = map[blockIdx.x];
+    const StepArgs<R> &a = A[m.ch];
+    b_zE<R, ZL, 0>(a, a.exz, a.eyz, a.wsq, 1, Blk{m.x, m.y, m.gx});
+}
+
+template <typename R>
+int zpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out) {
+    if (ch->g.n3m % ZL != 0) return C3D_EINVAL;
+    const unsigned nb = (unsigned)nblk((long long)ch->g.n2m * (ch->g.n3m / ZL) * ch->g.n1m);
+    switch (which) {
+        case 0:
+            out.push_back({(const void *)kb_zA<R, 1>, TPB, 0, nb});
+            out.push_back({(const void *)kb_zA<R, 2>, TPB, 0, nb});
+            out.push_back({(const void *)kb_zA<R, 3>, TPB, 0, nb});
+            return 0;
+        case 1: out.push_back({(const void *)kb_zB<R>, TPB, 0, nb}); return 0;
+        case 2: out.push_back({(const void *)kb_zC<R>, TPB, 0, nb}); return 0;
+        case 3: out.push_back({(const void *)kb_zD<R>, TPB, 0, nb}); return 0;
+        case 4: out.push_back({(const void *)kb_zE<R>, TPB, 0, nb}); return 0;
+        default: return C3D_EINVAL;
+    }
+}
+template int zpass_bkern<double>(const c3d_channel *, int, std::vector<BKern> &);
+template int zpass_bkern<float>(const c3d_channel *, int, std::vector<BKern> &);
 
 template <typename R>
 int launch_zpass(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *d1, R *d2, int flag, int *nl) {

@@ -88,6 +88,9 @@ SIGNATURES = {
     "c3d_batch_channel": (_ip, [_vp, _ip, ctypes.POINTER(_vp)]),
     "c3d_batch_step": (_ip, [_vp, _ip, _dp, _dp, _dp]),
     "c3d_batch_sync": (_ip, [_vp]),
+    "c3d_batch_set_form": (_ip, [_vp, _ip]),
+    "c3d_batch_get_form": (_ip, [_vp, ctypes.POINTER(_ip)]),
+    "c3d_batch_set_groups": (_ip, [_vp, _ip]),
     "c3d_batch_last_step_stats": (_ip, [_vp, _dp, ctypes.POINTER(_ip)]),
 }
 
@@ -428,6 +431,22 @@ class Batch:
         n = (ctypes.c_int * 1)()
         check(load().c3d_batch_last_step_stats(self.h, ms, n), "c3d_batch_last_step_stats")
         return ms[0], n[0]
+
+    FORMS = {"streams": 0, "worklist": 1}
+
+    def set_form(self, form: str):
+        """'worklist' (one launch per pass over all channels; DNS channels of one
+        precision) or 'streams' (each channel's step on its own stream)."""
+        check(load().c3d_batch_set_form(self.h, self.FORMS[form]), "c3d_batch_set_form")
+
+    def set_groups(self, groups: int):
+        """Work-list form: the channels in `groups` groups, each on its own stream."""
+        check(load().c3d_batch_set_groups(self.h, int(groups)), "c3d_batch_set_groups")
+
+    def get_form(self) -> str:
+        f = (ctypes.c_int * 1)()
+        check(load().c3d_batch_get_form(self.h, f), "c3d_batch_get_form")
+        return {v: k for k, v in self.FORMS.items()}[f[0]]
 
 
 class TimeAverage:

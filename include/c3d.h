@@ -375,7 +375,8 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
  *       shuffle FFT across the lanes) when N3M is 32 x 2, 3, 4, 6, 8, 12 or 16
  *   [7], [8] radix order of the x and z FFT plans (0: radix 4 first, 1: radix 3
  *       first, 2: radix 2 only, then 3); [7] = 3 runs the row FFTs of the pressure
- *       x passes in registers (four-step form, no shared memory) when N1M / 32 is even
+ *       x passes in registers (four-step form, no shared memory) and is accepted only
+ *       when N1M is a multiple of 64 (N1M / 32 even)
  *   [9] the z pass of the explicit terms as one kernel (0) or as its three sweeps
  *       in three kernels (1)
  *   [10] the x pass of the explicit terms as one kernel (0) or as its u, v and w
@@ -433,17 +434,39 @@ int c3d_op_get(c3d_channel *ch, double *f);
 /* ---- batched ensemble --------------------------------------------------
  * Many independent channels (any mix of grid sizes, RE and precision) that
  * advance together.  c3d_batch_step runs one GETUP on every channel as a single
- * CUDA graph (captured on the first call and whenever a channel's DT changes):
- * the channels' kernels run concurrently on their own streams.  presg/presg3
- * are in-out arrays of nchan values; the call returns when the step is done.
- * Upload each channel's state with c3d_batch_channel + c3d_upload first.
+ * CUDA graph (captured on the first call and whenever a channel's DT changes),
+ * in one of two forms:
+ *   C3D_BATCH_WORKLIST (the default; used when every channel is DNS, FILES = 0,
+ *     in one precision, C3D_FP64 or C3D_MIXED): each pass of the step is one
+ *     kernel launch over the blocks of all channels whose kernel for that pass
+ *     is the same template instance (same x lane chunk N1M/32, same z-FFT
+ *     shape), each block working on the channel a device work list names; a
+ *     step is about 20 launches for the whole ensemble.  The work-list form
+ *     runs a fixed schedule (x rows per block 2, xA and zA in pieces, z
+ *     segments of 16, the four-step z FFT where N3M = 32 N1, else tiles of 8,
+ *     register row FFTs where N1M is a multiple of 64), not the channels' own.
+ *   C3D_BATCH_STREAMS (and any other batch): every channel's step, with its own
+ *     schedule, on its own stream; the channels run concurrently.
+ * presg/presg3 are in-out arrays of nchan values; the call returns when the
+ * step is done.  Upload each channel's state with c3d_batch_channel +
+ * c3d_upload first.  c3d_batch_set_form chooses the form (the graphs are
+ * captured again); c3d_batch_get_form reports the form the next step runs.
+ * c3d_batch_set_groups (work-list form; default 2) splits the channels into
+ * that many groups, largest first and dealt in turn, each with its own work
+ * lists on its own stream, so that the passes of one group run beside those of
+ * another instead of every pass waiting for the whole ensemble.
  */
+#define C3D_BATCH_STREAMS   0
+#define C3D_BATCH_WORKLIST  1
 int c3d_batch_create(int nchan, const c3d_grid *grids, c3d_batch **out);
 int c3d_batch_destroy(c3d_batch *b);
 int c3d_batch_channel(c3d_batch *b, int index, c3d_channel **ch);
 int c3d_batch_step(c3d_batch *b, int ntime, const double *dt,
                    double *presg, double *presg3);
 int c3d_batch_sync(c3d_batch *b);
+int c3d_batch_set_form(c3d_batch *b, int form);
+int c3d_batch_get_form(c3d_batch *b, int *form);
+int c3d_batch_set_groups(c3d_batch *b, int groups);
 /* Device time of the last ensemble step (CUDA events around the graph launch) and the
  * number of kernels one ensemble step runs. */
 int c3d_batch_last_step_stats(c3d_batch *b, double *ms, int *kernel_launches);

@@ -117,3 +117,103 @@ def test_batch_refuses_iwmles(L):
     g, _ = make_grid("les32cs", wmodel=2)
     with pytest.raises(L.C3DError):
         L.Batch([g])
+
+
+def worklist_schedule(ch, g):
+    """The fixed schedule of the work-list form (include/c3d.h) on a single channel."""
+    s = ch.get_schedule()
+    s.update({f"z_segment_z{c}": 16 for c in "ABCDE"})
+    s.update(x_rows_per_block=2, fft_z_tile=0, fft_x_plan=3 if g.n1m % 64 == 0 else 0, fft_z_plan=0,
+             z_split_zA=1, x_split_xA=1, x_bulk_stages=0, x_stage_xA=0)
+    ch.set_schedule(s)
+
+
+def dns_ensemble(prec, seed0=0):
+    """DNS channels of one precision covering the lane chunks and z-FFT forms the
+    work-list form groups by: N1M in {48, 64, 96, 128}, N3M in {48, 64, 96, 128}."""
+    shapes = [(48, 32, 64), (64, 48, 48), (96, 40, 96), (128, 24, 128), (48, 64, 96), (64, 32, 64)]
+    out = []
+    for i, (n1, n2, n3) in enumerate(shapes):
+        g, dt = make_grid("channel64", precision=prec, n1m=n1, n2m=n2, n3m=n3, re=3000.0 + 700.0 * i)
+        out.append((g, dt, ic.perturbed_laminar(g, seed=ic.SEED0 + seed0 + i)))
+    return out
+
+
+@pytest.mark.parametrize("prec", [C3D_MIXED, C3D_FP64])
+def test_worklist_batch_matches_single_channels(L, prec):
+    """One launch per pass over all channels (the work-list form) computes, for every
+    channel, the step of that channel alone under the same schedule.  The batch kernels
+    are other compiled instances of the same kernel bodies, whose multiply-add
+    contractions can differ in the last bit, so after five steps they agree to rounding:
+    FP64 1e-12 relative (P 1e-11), mixed 1e-8 for U, 1e-4 for HH and 1e-3 for P (the
+    mixed pressure amplifies FP32 rounding, as its error against FP64 shows)."""
+    ens = dns_ensemble(prec)
+    b = L.Batch([g for g, _, _ in ens])
+    assert b.get_form() == "worklist"
+    singles = []
+    for (g, dt, (U, P, HH)), ch in zip(ens, b.channels):
+        ch.upload(U, P, HH)
+        ch.project()
+        s = L.Channel(g)
+        s.upload(U, P, HH)
+        s.project()
+        worklist_schedule(s, g)
+        singles.append(s)
+    dts = [dt for _, dt, _ in ens]
+    pb, pb3 = [0.0] * len(ens), [0.0] * len(ens)
+    ps = [(0.0, 0.0) for _ in ens]
+    for n in range(1, 6):
+        pb, pb3 = b.step(n, dts, pb, pb3)
+        ps = [s.step(n, dt, *p) for s, dt, p in zip(singles, dts, ps)]
+    tol = (1e-12, 1e-11, 1e-12) if prec == C3D_FP64 else (1e-8, 1e-3, 1e-4)
+    for i, (ch, s) in enumerate(zip(b.channels, singles)):
+        for f, x, y, t_ in zip("UPH", ch.download(), s.download(), tol):
+            e = float(np.linalg.norm(x - y) / np.linalg.norm(y))
+            assert e < t_, (i, f, e)
+        assert pb[i] == pytest.approx(ps[i][0], rel=1e-9 if prec == C3D_FP64 else 1e-6)
+    ms, nl = b.last_step_stats()
+    assert ms > 0 and nl <= 50          # 20 passes, several groups for the x and FFT passes
+    for s in singles:
+        s.close()
+    b.close()
+
+
+def test_worklist_batch_fp64_matches_oracle(L, oracle_mod):
+    """The work-list form in FP64 against the oracle, two steps per channel, 1e-10."""
+    ens = dns_ensemble(C3D_FP64, seed0=10)[:4]
+    b = L.Batch([g for g, _, _ in ens])
+    orcs = []
+    for (g, dt, (U, P, HH)), ch in zip(ens, b.channels):
+        o = oracle_mod.Oracle(g)
+        o.project(U)
+        ch.upload(U, P, HH)
+        orcs.append((o, U, P, HH))
+    dts = [dt for _, dt, _ in ens]
+    pb, pb3 = [0.0] * len(ens), [0.0] * len(ens)
+    po = [(0.0, 0.0) for _ in ens]
+    for n in (1, 2):
+        pb, pb3 = b.step(n, dts, pb, pb3)
+        po = [o.getup(U, P, HH, n, dt, *p) for (o, U, P, HH), dt, p in zip(orcs, dts, po)]
+    for i, ((g, _, _), ch, (o, U, P, HH)) in enumerate(zip(ens, b.channels, orcs)):
+        Ug, Pg, Hg = ch.download()
+        n1, n2, n3 = g.n1m, g.n2m, g.n3m
+        for c, j0 in ((0, 1), (1, 2), (2, 1)):
+            a = Ug[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c]
+            r = U[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c]
+            assert np.linalg.norm(a - r) / np.linalg.norm(r) < 1e-10, (i, c)
+        assert pb[i] == pytest.approx(po[i][0], rel=1e-9)
+    b.close()
+
+
+def test_mixed_precision_batch_runs_streams_form(L):
+    ens = ensemble()
+    b = L.Batch([g for g, _, _ in ens])
+    assert b.get_form() == "streams"            # FP64 and mixed channels together
+    b.close()
+    ens = dns_ensemble(C3D_MIXED)[:2]
+    b = L.Batch([g for g, _, _ in ens])
+    b.set_form("streams")
+    assert b.get_form() == "streams"
+    b.set_form("worklist")
+    assert b.get_form() == "worklist"
+    b.close()

@@ -43,7 +43,8 @@ SCHEDULES = [
     (_sched((0, 0, 0, 0, 0), 2, 0, 0, 1, 1, 1), 64),
     (_sched((0, 0, 0, 0, 0), 2, 0, 0, 1, 0, 0), 384),
     (_sched((16, 16, 16, 16, 16), 2, 0, 0, 1, 1, 1), 96),
-    (_sched((8, 8, 32, 16, 8), 2, 0, 3, 1, 1, 1), 64),
+    (_sched((8, 8, 32, 16, 8), 2, 0, 2, 1, 1, 1), 64),
+    (_sched((16, 8, 32, 16, 8), 4, 0, 2, 1, 1, 1, 0, 1), 64),
 ]
 
 
@@ -63,6 +64,29 @@ def test_register_row_fft_matches_oracle(libc3d, oracle_mod, n1m):
     orc.getup(U, P, HH, 1, dt, 0.0, 0.0)
     ch.step(1, dt, 0.0, 0.0)
     Ug, Pg, _ = ch.download()
+    n1, n2, n3 = g.n1m, g.n2m, g.n3m
+    for c, j0 in ((0, 1), (1, 2), (2, 1)):
+        e = rel(Ug[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c], U[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c])
+        assert e < 1e-10, (n1m, c, e)
+
+
+@pytest.mark.parametrize("n1m", [48, 96])
+def test_x_plan3_refused_unless_n1m_multiple_of_64(libc3d, oracle_mod, n1m):
+    """The register row FFT needs all 32 lanes to hold an even chunk: for N1M = 48 or 96
+    the schedule is refused, and the tuned step of such a grid matches the oracle."""
+    g, dt = make_grid("small32", n1m=n1m, n2m=16, n3m=32)
+    orc = oracle_mod.Oracle(g)
+    U, P, HH = ic.perturbed_laminar(g)
+    orc.project(U)
+    ch = libc3d.Channel(g, C3D_FP64)
+    ch.upload(U, P, HH)
+    s = ch.get_schedule()
+    with pytest.raises(libc3d.C3DError):
+        ch.set_schedule(dict(s, fft_x_plan=3))
+    assert ch.autotune()["fft_x_plan"] != 3
+    orc.getup(U, P, HH, 1, dt, 0.0, 0.0)
+    ch.step(1, dt, 0.0, 0.0)
+    Ug, _, _ = ch.download()
     n1, n2, n3 = g.n1m, g.n2m, g.n3m
     for c, j0 in ((0, 1), (1, 2), (2, 1)):
         e = rel(Ug[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c], U[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c])
