@@ -125,6 +125,7 @@ struct Tune {
     int xsplit;   // xA as one kernel (0) or as its u, v, w pieces in three kernels (1)
     int xbulk;    // x passes with rows staged by a bulk-copy ring of this many stages (0: off)
     int xstage;   // xA's pieces read their rows from global memory (0) or stage them in shared memory by bulk copies (1)
+    int ycn;      // wall-normal CN factor: one thread per column (0) or shared-memory tiles of 32 or 64 columns
 };
 
 // Arguments of the pressure refinement (mixed form with C3D_MIXED_IR): double-float

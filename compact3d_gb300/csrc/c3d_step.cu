@@ -102,6 +102,138 @@ __global__ void __launch_bounds__(TPB) k_ycn(StepArgs<R> a, const R *ycn) {
     b_ycn<R>(a, ycn, Blk{blockIdx.x, blockIdx.y, gridDim.x});
 }
 
+// The wall-normal CN factor with the columns staged in shared memory: a block owns TX
+// consecutive columns (i, k) of one component over all planes; its first warp fetches each
+// plane's TX-value row segment by a bulk copy (cp.async.bulk) into the block's tile, in
+// YCH chunks of planes each completing on its own mbarrier, so the forward sweep starts on
+// the first chunk while the others arrive; the forward sweep writes the tile in place,
+// the backward sweep reads it and stores each result once.  Every value crosses DRAM once
+// in each direction.  A wait that runs out sets SCAL_PIPEERR and returns after waiting
+// (bounded) for the block's copies in flight.
+constexpr int YCH = 8;
+template <typename R>
+__host__ __device__ inline size_t ycn_tile_bytes(int tx, int n2m) {
+    // barriers, coefficients (rounded up to 16 bytes: the tile's rows are bulk-copy targets), tile
+    return 64 + (((3 * (size_t)n2m * sizeof(R)) + 15) & ~(size_t)15) + (size_t)n2m * tx * sizeof(R);
+}
+
+template <typename R, int TX>
+__device__ __forceinline__ void b_ycnt(const StepArgs<R> &a, const R *ycn, const Blk blk) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Geo g = a.g;
+    const int np = g.np, ntile = (np + TX - 1) / TX;
+    const int c = (int)blk.x / ntile, q = (int)blk.x % ntile;
+    const int col0 = q * TX, ncol = min(TX, np - col0);
+    const int js = (c == 1) ? 2 : 1, nj = g.n2m - js + 1;
+    const int m = g.n2 + 1;
+    const R *A = ycn + (c * 3 + 0) * m, *RBt = ycn + (c * 3 + 1) * m, *GM = ycn + (c * 3 + 2) * m;
+    R *X = a.r[c] + col0;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
+    R *sA = reinterpret_cast<R *>(smem_raw + 64), *sR = sA + nj, *sG = sR + nj;
+    R *T = reinterpret_cast<R *>(smem_raw + 64 + (((3 * (size_t)nj * sizeof(R)) + 15) & ~(size_t)15));
+    const int t = threadIdx.x;
+    const int cpl = (nj + YCH - 1) / YCH;
+    const uint32_t rowb = (uint32_t)ncol * (uint32_t)sizeof(R);
+    if (t == 0) {
+        for (int b = 0; b < YCH; ++b) mbar_init(bar + b, 1);
+        mbar_init_fence();
+        fence_async_smem();
+        for (int b = 0; b < YCH; ++b) {
+            const int p0 = b * cpl, p1 = min(nj, p0 + cpl);
+            if (p1 > p0) mbar_expect_tx(bar + b, (uint32_t)(p1 - p0) * rowb);
+        }
+    }
+    for (int p = t; p < nj; p += blockDim.x) {
+        sA[p] = A[js + p];
+        sR[p] = RBt[js + p];
+        sG[p] = GM[js + p];
+    }
+    __syncthreads();   // barriers set up before any copy can complete; coefficients staged
+    if (t < 32)
+        for (int p = t; p < nj; p += 32) bulk_g2s(T + (size_t)p * TX, X + (long long)(js + p) * np, rowb, bar + p / cpl);
+    if (t >= ncol) return;   // no copy targets this thread's column; the block stays until the others end
+    R xp = R(0);
+    for (int b = 0; b < YCH; ++b) {
+        const int p0 = b * cpl, p1 = min(nj, p0 + cpl);
+        if (p1 <= p0) break;
+        if (!mbar_wait(bar + b, 0)) {
+            a.scal[SCAL_PIPEERR] = 1.0;
+            for (int b2 = b; b2 < YCH; ++b2)
+                if (b2 * cpl < nj) mbar_wait(bar + b2, 0);   // the copies in flight target this tile
+            return;
+        }
+        // eight planes read ahead of the recurrence, so the shared-memory latency is not on
+        // its dependent chain
+        int p = p0;
+        for (; p + 8 <= p1; p += 8) {
+            R v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = T[(size_t)(p + u) * TX + t];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int pp = p + u;
+                xp = (pp == 0) ? v[u] * sR[pp] : (v[u] - sA[pp] * xp) * sR[pp];
+                v[u] = xp;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) T[(size_t)(p + u) * TX + t] = v[u];
+        }
+        for (; p < p1; ++p) {
+            const R v = T[(size_t)p * TX + t];
+            xp = (p == 0) ? v * sR[p] : (v - sA[p] * xp) * sR[p];
+            T[(size_t)p * TX + t] = xp;
+        }
+    }
+    X[(long long)(js + nj - 1) * np + t] = xp;
+    int p = nj - 2;
+    for (; p >= 7; p -= 8) {
+        R v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = T[(size_t)(p - u) * TX + t];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            xp = v[u] - xp * sG[p - u];
+            v[u] = xp;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) X[(long long)(js + p - u) * np + t] = v[u];
+    }
+    for (; p >= 0; --p) {
+        xp = T[(size_t)p * TX + t] - xp * sG[p];
+        X[(long long)(js + p) * np + t] = xp;
+    }
+}
+template <typename R, int TX>
+__global__ void __launch_bounds__(64) k_ycnt(StepArgs<R> a, const R *ycn) {
+    b_ycnt<R, TX>(a, ycn, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+}
+
+// Launches the wall-normal CN factor in the form the schedule names (0: one thread per
+// column with register batches; 32 or 64: the shared-memory tiles of that many columns,
+// when the tile fits).
+template <typename R>
+static void launch_ycn(c3d_channel *ch, StepArgs<R> &a, int *nl) {
+    const R *ycn = sizeof(R) == 8 ? (const R *)ch->ycn : (const R *)ch->ycn32;
+    const int tx = ch->tune.ycn;
+    const size_t sm = ycn_tile_bytes<R>(tx == 0 ? 32 : tx, ch->g.n2m);
+    if ((tx == 32 || tx == 64) && sm <= 227 * 1024) {
+        const int nb = 3 * ((ch->g.np + tx - 1) / tx);
+        // the whole shared-memory carve-out, so that as many tiles as fit are resident
+        if (tx == 32) {
+            cudaFuncSetAttribute(k_ycnt<R, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            cudaFuncSetAttribute(k_ycnt<R, 32>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+            k_ycnt<R, 32><<<nb, 32, sm, ch->stream>>>(a, ycn);
+        } else {
+            cudaFuncSetAttribute(k_ycnt<R, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            cudaFuncSetAttribute(k_ycnt<R, 64>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+            k_ycnt<R, 64><<<nb, 64, sm, ch->stream>>>(a, ycn);
+        }
+    } else {
+        k_ycn<R><<<nblk(3LL * ch->g.np), TPB, 0, ch->stream>>>(a, ycn);
+    }
+    mark(ch, nl, "ycn", (double)ch->g.n1m * ch->g.n2m * ch->g.n3m * 6 * sizeof(R));
+}
+
 // DMPRESG / DMPRESG3 in FP64 with a fixed summation order; PRESG += DMPRESG (UPCALC)
 // UPCALC's forcing (compact3d.f:1052-1238) from the summed CN increments of u and w.
 __device__ __forceinline__ void finish_bulk(Geo g, double t1, double t3, double *scal, double dt, int bulk) {
@@ -469,8 +601,7 @@ static int step_impl(c3d_channel *ch, double dt, int *nl) {
     if (ch->hh_hooks) CK_RC(cudaStreamWaitEvent(ch->stream, ch->hh_in, 0));
     if ((rc = launch_xpass<R>(ch, a, 1, nullptr, nullptr, nl))) return rc;    // xB
     if (ch->hh_hooks) CK_RC(cudaEventRecord(ch->hh_out, ch->stream));
-    k_ycn<R><<<nblk(3LL * ch->g.np), TPB, 0, ch->stream>>>(a, sizeof(R) == 8 ? (const R *)ch->ycn : (const R *)ch->ycn32);
-    mark(ch, nl, "ycn", (double)ch->g.n1m * ch->g.n2m * ch->g.n3m * 6 * sizeof(R));
+    launch_ycn<R>(ch, a, nl);
     // deltas go to exz/eyz/wsq, which the RHS passes no longer need
     R *dd0 = (R *)ch->exz, *dd1 = (R *)ch->eyz, *dd2 = (R *)ch->wsq;
     if ((rc = launch_zpass<R>(ch, a, 2, dd0, dd1, dd2, 0, nl))) return rc;    // zC

@@ -362,7 +362,7 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
 
 /* ---- launch schedule -----------------------------------------------------
  * The kernels' launch shapes are chosen per grid shape by an autotuner written for
- * this library (no counterpart in the reference).  A schedule is thirteen ints
+ * this library (no counterpart in the reference).  A schedule is fourteen ints
  * (C3D_SCHEDULE_LEN):
  *   [0..4] z-line segment length (8, 16, 32) of each z pass: the points each thread
  *       solves sequentially (Thomas-like) before the parallel segments of a z line
@@ -387,6 +387,10 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
  *   [12] the u, v and w pieces of the explicit x pass (with [10] = 1) read their rows
  *       from global memory (0), or stage every row of a warp's (J, K) in shared memory
  *       by one bulk copy per row before computing (1; N1M even)
+ *   [13] the wall-normal Crank-Nicolson factor (TDMAI): one thread per column with
+ *       register batches of planes (0), or blocks of 32 or 64 columns whose planes
+ *       are staged in shared memory by bulk copies so that each value is read and
+ *       written once (falls back to 0 when the tile exceeds shared memory)
  * c3d_autotune  times the candidates on a scratch channel of the same grid holding a
  *               copy of this channel's state (so the channel needs its state), keeps
  *               the fastest per kernel group, applies it, and caches it per grid
@@ -394,7 +398,7 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
  *               receives the result.
  * c3d_set_schedule / c3d_get_schedule  set or read a schedule directly.
  * Channels of a batch are tuned before the batch's first step captures its graph. */
-#define C3D_SCHEDULE_LEN 13
+#define C3D_SCHEDULE_LEN 14
 int c3d_autotune(c3d_channel *ch, int *sched);
 int c3d_get_schedule(c3d_channel *ch, int *sched);
 int c3d_set_schedule(c3d_channel *ch, const int *sched);

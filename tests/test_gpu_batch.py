@@ -172,7 +172,9 @@ def test_worklist_batch_matches_single_channels(L, prec):
             assert e < t_, (i, f, e)
         assert pb[i] == pytest.approx(ps[i][0], rel=1e-9 if prec == C3D_FP64 else 1e-6)
     ms, nl = b.last_step_stats()
-    assert ms > 0 and nl <= 50          # 20 passes, several groups for the x and FFT passes
+    # 20 passes per channel group (two by default), a few kernel groups for the x and FFT
+    # passes: tens of launches against one step's 15-20 per channel in the streams form
+    assert ms > 0 and nl <= 100
     for s in singles:
         s.close()
     b.close()

@@ -26,10 +26,10 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def _sched(zl, xw, tw, fx, fz, split, xsplit, xbulk=0, xstage=0):
+def _sched(zl, xw, tw, fx, fz, split, xsplit, xbulk=0, xstage=0, ycn=0):
     d = {f"z_segment_z{c}": z for c, z in zip("ABCDE", zl)}
     d.update(x_rows_per_block=xw, fft_z_tile=tw, fft_x_plan=fx, fft_z_plan=fz, z_split_zA=split,
-             x_split_xA=xsplit, x_bulk_stages=xbulk, x_stage_xA=xstage)
+             x_split_xA=xsplit, x_bulk_stages=xbulk, x_stage_xA=xstage, ycn_tile=ycn)
     return d
 
 
@@ -45,6 +45,8 @@ SCHEDULES = [
     (_sched((16, 16, 16, 16, 16), 2, 0, 0, 1, 1, 1), 96),
     (_sched((8, 8, 32, 16, 8), 2, 0, 2, 1, 1, 1), 64),
     (_sched((16, 8, 32, 16, 8), 4, 0, 2, 1, 1, 1, 0, 1), 64),
+    (_sched((16, 16, 16, 16, 16), 2, 0, 0, 1, 1, 1, 0, 0, 32), 64),
+    (_sched((16, 16, 16, 16, 16), 2, 0, 0, 1, 1, 1, 0, 0, 64), 96),
 ]
 
 
@@ -221,3 +223,29 @@ def test_stalled_stage_wait_becomes_error(libc3d):
     with pytest.raises(libc3d.C3DError):
         ch.step(2, dt, 0.0, 0.0)
     ch.close()
+
+
+@pytest.mark.parametrize("shape,prec", [((64, 48, 64), C3D_MIXED), ((96, 200, 32), C3D_MIXED), ((48, 24, 48), C3D_FP64),
+                                        ((64, 130, 64), C3D_FP64)])
+def test_ycn_tiles_bit_identical(libc3d, shape, prec):
+    """The wall-normal CN factor with the planes staged in shared memory (tiles of 32 or 64
+    columns, eight chunks of planes) performs the same recurrences as the register form:
+    the step is bit-identical.  N2M = 200 and 130 give chunks of uneven length; 48 x 48
+    columns leave a last tile of 32 columns for the 64-column tiles."""
+    n1m, n2m, n3m = shape
+    g, dt = make_grid("small32", n1m=n1m, n2m=n2m, n3m=n3m)
+    U, P, HH = ic.perturbed_laminar(g)
+    out = []
+    for yt in (0, 32, 64):
+        ch = libc3d.Channel(g, prec)
+        ch.upload(U, P, HH)
+        s = ch.get_schedule()
+        s.update(ycn_tile=yt)
+        ch.set_schedule(s)
+        for m in (1, 2):
+            ch.step(m, dt, 0.0, 0.0)
+        out.append(ch.download())
+        ch.close()
+    for r in out[1:]:
+        for a, b in zip(r, out[0]):
+            assert np.array_equal(a, b)
