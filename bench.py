@@ -520,7 +520,8 @@ def with_summary(res: dict) -> dict:
                 summ["batched_" + k] = b[k]["value"]
     e = res.get("err_vs_fp64")
     if e and "mixed" in e:
-        summ["err_vs_fp64"] = {k: e["mixed"][k] for k in ("u", "v", "w", "p", "divmax", "bulk_rel", "wsm_rel")}
+        summ["err_vs_fp64"] = {k: e["mixed"][k] for k in ("u", "v", "w", "p", "p_mean", "p_fluct", "divmax", "bulk_rel",
+                                                           "wsm_rel")}
         summ["err_vs_fp64"]["steps"] = e["steps"]
     l_ = res.get("les")
     if l_:
@@ -589,6 +590,10 @@ def error_study(lib, g, dt, U0, P0, HH0, steps: int, floor: bool = True):
             v=rl(Um[1:n1 + 1, 2:n2 + 1, 1:n3 + 1, 1], Uf[1:n1 + 1, 2:n2 + 1, 1:n3 + 1, 1]),
             w=rl(Um[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 2], Uf[1:n1 + 1, 1:n2 + 1, 1:n3 + 1, 2]),
             p=rl(Pm[:n1, :n2, :n3], Pf[:n1, :n2, :n3]),
+            # P split into its plane means (the kx = kz = 0 Poisson mode) and the rest
+            p_mean=rl(Pm[:n1, :n2, :n3].mean(axis=(0, 2)), Pf[:n1, :n2, :n3].mean(axis=(0, 2))),
+            p_fluct=rl(Pm[:n1, :n2, :n3] - Pm[:n1, :n2, :n3].mean(axis=(0, 2))[None, :, None],
+                       Pf[:n1, :n2, :n3] - Pf[:n1, :n2, :n3].mean(axis=(0, 2))[None, :, None]),
             divmax=d["divmax"], bulk=d["flow1"] / g.aly, wsm=float(d["wsm"][0]), presg=presg[name][0],
             mean_u=rl(sm["mean_u"], sf["mean_u"]),
             rms=rl(np.concatenate([sm[k] for k in ("urms", "vrms", "wrms", "uv")]),
