@@ -52,17 +52,26 @@ def strip_comment(s: str) -> str:
     return "".join(out)
 
 
-def read_statements(path: str, includes: dict):
+def read_statements(path: str, includes: dict, omp: bool = False):
     """Returns a list of (line number, label, statement text) with continuations joined,
-    comments removed and INCLUDE lines expanded from `includes` (name -> text)."""
+    comments removed and INCLUDE lines expanded from `includes` (name -> text).  With
+    `omp`, OpenMP directive lines (!$OMP, continued by !$OMP&) become statements
+    '$OMP <directive>'."""
     raw = open(path, encoding="latin-1").read().split("\n")
-    return _statements(raw, includes, path)
+    return _statements(raw, includes, path, omp)
 
 
-def _statements(raw, includes, where):
+def _statements(raw, includes, where, omp=False):
     stmts = []
     for n, line in enumerate(raw, 1):
         if not line.strip():
+            continue
+        if omp and line[:5].upper() == "!$OMP":
+            if line[5:6] == "&" and stmts and stmts[-1][2].startswith("$OMP"):
+                ln, lab, txt = stmts[-1]
+                stmts[-1] = (ln, lab, txt + " " + line[6:].strip())
+            else:
+                stmts.append((n, None, "$OMP " + line[5:].strip()))
             continue
         if line[0] in "cC*!":
             continue
@@ -92,7 +101,7 @@ def _statements(raw, includes, where):
             name = m.group(1)
             # an include file outside the source tree (omp_lib.h) declares only the
             # OpenMP runtime's interfaces, which the translation does not use
-            stmts.extend(_statements(includes.get(name, "").split("\n"), includes, name))
+            stmts.extend(_statements(includes.get(name, "").split("\n"), includes, name, omp))
             continue
         lab = label_f.strip()
         stmts.append((n, int(lab) if lab.isdigit() else None, body.strip()))
@@ -309,6 +318,14 @@ def parse_expr(s: str):
 CTYPE = {"R": "double", "I": "int", "I8": "long long", "C": "double _Complex", "L": "int", "F": "float",
          "CH": "char"}
 SIZE = {"R": 8, "I": 4, "I8": 8, "C": 16, "L": 4, "F": 4}
+KEYWORDS = {"DO", "IF", "THEN", "ELSE", "ELSEIF", "ENDIF", "END", "ENDDO", "WHILE", "GO", "GOTO", "TO", "CALL",
+            "RETURN", "CONTINUE", "STOP", "EXIT", "CYCLE"}
+# OpenMP form: local arrays up to this size are automatic (one per call, so per thread
+# inside parallel loops, as a recursive Fortran build has them); larger ones stay static
+OMP_AUTO_BYTES = 8 * 1024 * 1024
+# static arrays larger than this, and every COMMON block, are heap memory set up when the
+# library loads
+HEAP_BYTES = 1024 * 1024
 
 
 def split_top(s: str, sep=","):
@@ -449,13 +466,17 @@ INTRINSIC_REAL1 = {"SQRT": "sqrt", "DSQRT": "sqrt", "EXP": "exp", "DEXP": "exp",
 
 
 class Translator:
-    def __init__(self, prog: Program, params: dict, wanted: set, commons_size: dict):
+    def __init__(self, prog: Program, params: dict, wanted: set, commons_size: dict, omp: bool = False):
+        self.omp = omp
+        self.pending_omp = None
+        self.redmap = {}
         self.prog = prog
         self.params = params
         self.wanted = wanted
         self.csize = commons_size
         self.externals = set()
         self.ext_funcs = {}
+        self.heap = []   # (global name, C type, elements) of the static arrays kept on the heap
 
     # ---- declarations pass ----
     def declare(self, u: Unit):
@@ -635,6 +656,8 @@ class Translator:
         return ta if order.get(ta, 4) >= order.get(tb, 4) else tb
 
     def ref(self, u: Unit, name):
+        if name in self.redmap:
+            return self.redmap[name]
         v = u.vars.get(name)
         if v is not None and v.param is not None:
             val = self.const(u, v.param)
@@ -785,6 +808,23 @@ class Translator:
         for ln, lab, txt in u.exe:
             for m in re.finditer(r"(?i)\bGO\s*TO\s*(\d+)", txt):
                 self.goto_targets.add(int(m.group(1)))
+        if self.omp:
+            # every name the routine uses exists before the first parallel loop is emitted,
+            # so that its firstprivate clause lists the scalars first used inside the loop
+            for ln, lab, txt in u.exe:
+                up = txt.upper().strip()
+                if up.startswith("$OMP") or re.match(r"^(CALL|WRITE|READ|PRINT|FORMAT|OPEN|CLOSE)\b", up):
+                    if not up.startswith("CALL"):
+                        continue
+                try:
+                    toks = tokenize(re.sub(r"^CALL\s+\w+", "", up))
+                except SyntaxError:
+                    continue
+                for i, (k, v) in enumerate(toks):
+                    nxt = toks[i + 1][1] if i + 1 < len(toks) else None
+                    if k == "name" and nxt != "(" and v not in self.params and v not in KEYWORDS:
+                        if v not in u.vars and not (u.kind == "FUNCTION" and v == u.name):
+                            u.var(v)
         body = []
         self.ind = 1
         for ln, lab, txt in u.exe:
@@ -814,14 +854,25 @@ class Translator:
                 out.append(f"  {CTYPE[t]} *v_{nm} = ({CTYPE[t]} *)(f77c_{v.common} + {v.offset});")
             elif v.dims:
                 try:
-                    out.append(f"  static {CTYPE[t]} v_{nm}[{self.nelems(u, v)}];")
+                    ne = self.nelems(u, v)
+                    # OpenMP: per-call (per-thread) arrays, except the channel-sized ones
+                    auto = self.omp and ne * SIZE.get(t, 8) <= OMP_AUTO_BYTES
+                    if not auto and ne * SIZE.get(t, 8) > HEAP_BYTES:
+                        # a channel-sized array: zeroed heap memory allocated when the
+                        # library loads (static data of this size exceeds what the code
+                        # model addresses)
+                        gname = f"f77l_{u.name}_{nm}"
+                        self.heap.append((gname, CTYPE[t], ne))
+                        out.append(f"  {CTYPE[t]} *v_{nm} = {gname};")
+                    else:
+                        out.append(f"  {'' if auto else 'static '}{CTYPE[t]} v_{nm}[{ne}];")
                 except ValueError:
                     # automatic array sized by dummy arguments: a zeroed stack array
                     n = " * ".join(f"(({self.ex(u, parse_expr(hi))[0]}) - ({self.ex(u, parse_expr(lo))[0]}) + 1)"
                                    for lo, hi in v.dims)
                     out.append(f"  {CTYPE[t]} v_{nm}[{n}]; memset(v_{nm}, 0, sizeof(v_{nm}));")
             elif self.used_as_var(u, nm):
-                out.append(f"  static {CTYPE[t]} v_{nm};")
+                out.append(f"  {CTYPE[t]} v_{nm} = 0;" if self.omp else f"  static {CTYPE[t]} v_{nm};")
         out.extend(body)
         if u.kind == "FUNCTION":
             out.append("  return f77_result;")
@@ -849,11 +900,13 @@ class Translator:
         self.simple(u, up, txt, body, lab)
         # close labelled DO loops ending here
         while self.do_stack and self.do_stack[-1][0] is not None and self.do_stack[-1][0] == lab:
-            self.do_stack.pop()
-            self.ind -= 1
-            self.emit(body, "}}")
+            self.close_do(body)
 
     def simple(self, u, up, txt, body, lab):
+        if up.startswith("$OMP"):
+            if self.omp:
+                self.omp_directive(up[4:].strip())
+            return
         if up in ("CONTINUE",):
             return
         if re.match(r"^(OPEN|CLOSE|WRITE|READ|PRINT|FORMAT|REWIND|BACKSPACE|INQUIRE|FLUSH)\b", up) or \
@@ -893,6 +946,12 @@ class Translator:
             vref = self.ref(u, var)[0]
             d = len(self.do_stack)
             ct = CTYPE[vt]
+            if self.pending_omp is not None:
+                if any(u.vars.get(nm) is not None and u.vars[nm].dims for _, nm in self.pending_omp["red"]):
+                    self.pending_omp = None   # an array reduction (WALLSS's WSM): the loop runs on one thread
+                else:
+                    self.parallel_do(u, body, lab_end, vref, ct, s, e, st, d)
+                    return
             self.emit(body, f"{{ {ct} s{d} = {st}; long n{d} = (long)((({e}) - ({s}) + s{d}) / s{d}); "
                             f"for ({vref} = {s}; n{d} > 0; --n{d}, {vref} += s{d}) {{")
             self.do_stack.append((lab_end, "do"))
@@ -901,9 +960,7 @@ class Translator:
         if up in ("ENDDO", "END DO"):
             if not self.do_stack or self.do_stack[-1][0] is not None:
                 raise SyntaxError("ENDDO without DO")
-            self.do_stack.pop()
-            self.ind -= 1
-            self.emit(body, "}}")
+            self.close_do(body)
             return
         m = re.match(r"^IF\s*\((.*)$", up)
         if m:
@@ -962,6 +1019,81 @@ class Translator:
             return
         raise SyntaxError(f"unsupported statement {txt!r}")
 
+    def close_do(self, body):
+        ent = self.do_stack.pop()
+        self.ind -= 1
+        if ent[1] == "omp":
+            self.emit(body, "}")
+            for line in ent[2]:
+                self.emit(body, line)
+            self.emit(body, "}")
+            self.redmap = {}
+        else:
+            self.emit(body, "}}")
+
+    def omp_directive(self, text: str):
+        """!$OMP PARALLEL DO [PRIVATE(list)] [REDUCTION(op:list)]: applies to the next DO."""
+        t = text.upper()
+        if not re.match(r"^PARALLEL\s+DO\b", t):
+            raise SyntaxError(f"unsupported OpenMP directive {text!r}")
+        priv = []
+        for m in re.finditer(r"PRIVATE\s*\(([^)]*)\)", t):
+            priv += [x.strip() for x in m.group(1).split(",") if x.strip()]
+        red = []
+        for m in re.finditer(r"REDUCTION\s*\(\s*([+*]|MAX|MIN)\s*:([^)]*)\)", t):
+            red += [(m.group(1), x.strip()) for x in m.group(2).split(",") if x.strip()]
+        self.pending_omp = dict(private=priv, red=red)
+
+    def parallel_do(self, u, body, lab_end, vref, ct, s, e, st, d):
+        """A Fortran PARALLEL DO as an OpenMP loop over the trip count.  Every local scalar is
+        firstprivate (the loop's own and inner DO variables included, as Fortran makes them
+        private, and temporaries the directive may not list); arrays the directive lists are
+        private; a reduction variable gets a local accumulator folded into it after the loop."""
+        pend, self.pending_omp = self.pending_omp, None
+        redn = {nm for _, nm in pend["red"]}
+        pre, post = [], []
+        for op, nm in pend["red"]:
+            t = u.typeof(nm)
+            c = CTYPE[t]
+            init = {"+": "0", "*": "1", "MAX": "-HUGE_VAL" if t in ("R", "F") else "INT_MIN",
+                    "MIN": "HUGE_VAL" if t in ("R", "F") else "INT_MAX"}[op]
+            orig = self.ref(u, nm)[0]
+            pre.append(f"{c} r_{nm} = {init};")
+            if op in ("+", "*"):
+                post.append(f"{orig} = {orig} {op} r_{nm};")
+            else:
+                f = ("f77_dmax" if op == "MAX" else "f77_dmin") if t in ("R", "F") else ("f77_imax" if op == "MAX" else "f77_imin")
+                post.append(f"{orig} = {f}({orig}, r_{nm});")
+        fp, pv = [], []
+        for nm, v in u.vars.items():
+            if v.param is not None or v.dummy or v.external or v.common or nm in redn:
+                continue
+            if u.kind == "FUNCTION" and nm == u.name:
+                continue
+            t = v.typ or u.typeof(nm)
+            if t == "CH":
+                continue
+            if v.dims:
+                if nm in pend["private"]:
+                    pv.append(f"v_{nm}")
+            else:
+                fp.append(f"v_{nm}")
+        self.emit(body, f"{{ {ct} s{d} = {st}; {ct} b{d} = {s}; long n{d} = (long)((({e}) - (b{d}) + s{d}) / s{d});")
+        for line in pre:
+            self.emit(body, line)
+        clauses = []
+        if fp:
+            clauses.append("firstprivate(" + ", ".join(fp) + ")")
+        if pv:
+            clauses.append("private(" + ", ".join(pv) + ")")
+        for op, nm in pend["red"]:
+            clauses.append(f"reduction({'max' if op == 'MAX' else 'min' if op == 'MIN' else op}:r_{nm})")
+        self.emit(body, "#pragma omp parallel for schedule(static) " + " ".join(clauses))
+        self.emit(body, f"for (long i{d} = 0; i{d} < n{d}; ++i{d}) {{ {vref} = b{d} + ({ct})i{d} * s{d};")
+        self.redmap = {nm: (f"r_{nm}", u.typeof(nm)) for _, nm in pend["red"]}
+        self.do_stack.append((lab_end, "omp", post))
+        self.ind += 1
+
     @staticmethod
     def split_paren(s: str):
         """'(cond) rest' -> ('cond', 'rest')."""
@@ -1006,6 +1138,7 @@ HEADER = r"""/* Generated from the reference's Fortran source by oracle/f77c.py;
 #include <complex.h>
 #include <stdlib.h>
 #include <string.h>
+#include <limits.h>
 static inline int f77_ipow(int a, int b) { int r = 1; if (b < 0) return (a == 1) ? 1 : (a == -1 ? ((b & 1) ? -1 : 1) : 0); while (b--) r *= a; return r; }
 static inline double f77_powi(double x, int n) {
     /* x**n for an integer n: binary powering, as compilers expand integer powers */
@@ -1026,13 +1159,13 @@ static void f77_stop(void) { f77_stop_flag = 1; }
 """
 
 
-def translate(src, out_c, m1, m2, m3, roots, fortran_dir=None):
+def translate(src, out_c, m1, m2, m3, roots, fortran_dir=None, omp=False):
     fortran_dir = fortran_dir or os.path.dirname(src)
     includes = {}
     for name in ("PARAM.H", "COMMON1.FI"):
         includes[name] = open(os.path.join(fortran_dir, name), encoding="latin-1").read()
     includes["PARAM.H"] = f"      PARAMETER (M1={m1},M2={m2},M3={m3})\n"
-    prog = Program(read_statements(src, includes))
+    prog = Program(read_statements(src, includes, omp))
     # routines reachable from the roots through CALL statements and function references
     wanted, stack = set(), list(roots)
     while stack:
@@ -1047,7 +1180,7 @@ def translate(src, out_c, m1, m2, m3, roots, fortran_dir=None):
                 if fu.kind == "FUNCTION" and re.search(r"(?i)\b" + fname + r"\s*\(", txt):
                     stack.append(fname)
     csize = {}
-    tr = Translator(prog, {}, wanted, csize)
+    tr = Translator(prog, {}, wanted, csize, omp)
     sigs, bodies = [], []
     for n in sorted(wanted):
         s, b = tr.unit_c(prog.units[n])
@@ -1055,11 +1188,20 @@ def translate(src, out_c, m1, m2, m3, roots, fortran_dir=None):
         bodies.append(b)
     lines = [HEADER]
     for blk, sz in sorted(csize.items()):
-        lines.append(f"unsigned char f77c_{blk}[{(sz + 15) // 16 * 16}] __attribute__((aligned(16)));")
+        lines.append(f"unsigned char *f77c_{blk};   /* COMMON /{blk}/, {sz} bytes */")
     for x in sorted(tr.externals):
         lines.append(f"void f77_{x}();")
     for x, t in sorted(tr.ext_funcs.items()):
         lines.append(f"{CTYPE[t]} f77_{x}();")
+    for gname, ct, ne in tr.heap:
+        lines.append(f"static {ct} *{gname};")
+    # COMMON blocks and the large static arrays: zeroed memory, allocated once at load time
+    lines.append("__attribute__((constructor)) static void f77_load(void) {")
+    for blk, sz in sorted(csize.items()):
+        lines.append(f"  f77c_{blk} = (unsigned char *)calloc({(sz + 15) // 16 * 16}, 1);")
+    for gname, ct, ne in tr.heap:
+        lines.append(f"  {gname} = ({ct} *)calloc({ne}, sizeof({ct}));")
+    lines.append("}")
     lines.extend(sigs)
     lines.extend(bodies)
     open(out_c, "w").write("\n".join(lines) + "\n")

@@ -32,34 +32,39 @@ CT = {"R": ctypes.c_double, "I": ctypes.c_int, "I8": ctypes.c_longlong, "L": cty
 NP = {"R": np.float64, "I": np.int32, "I8": np.int64, "L": np.int32, "F": np.float32, "C": np.complex128}
 
 
-def _paths(m1, m2, m3):
-    base = os.path.join(OUT, f"ref_{m1}_{m2}_{m3}")
+def _paths(m1, m2, m3, omp=False):
+    base = os.path.join(OUT, f"ref{'_omp' if omp else ''}_{m1}_{m2}_{m3}")
     return base + ".c", base + ".json", base + ".so"
 
 
-def available(m1: int = 17, m2: int = 17, m3: int = 17) -> bool:
-    c, j, _ = _paths(m1, m2, m3)
+def available(m1: int = 17, m2: int = 17, m3: int = 17, omp: bool = False) -> bool:
+    c, j, _ = _paths(m1, m2, m3, omp)
     return os.path.exists(SOURCE) or (os.path.exists(c) and os.path.exists(j))
 
 
-def build(m1: int, m2: int, m3: int) -> str:
+def build(m1: int, m2: int, m3: int, omp: bool = False) -> str:
     """Translate (when the reference source is here) and compile the library for
-    PARAMETER (M1=m1, M2=m2, M3=m3)."""
+    PARAMETER (M1=m1, M2=m2, M3=m3).  With `omp` the reference's !$OMP PARALLEL DO
+    directives become OpenMP loops (locals per call, as a recursive build has them) and
+    the library is compiled with -fopenmp: the reference's own OpenMP CPU path, for
+    timing; without, one thread, locals kept between calls (the tests' form)."""
     from . import f77c
     os.makedirs(OUT, exist_ok=True)
-    c, j, so = _paths(m1, m2, m3)
+    c, j, so = _paths(m1, m2, m3, omp)
     shim = os.path.join(HERE, "fftw_shim.c")
     if os.path.exists(SOURCE):
         deps = [SOURCE, os.path.join(HERE, "f77c.py")]
         if not os.path.exists(c) or any(os.path.getmtime(d) > os.path.getmtime(c) for d in deps):
-            f77c.translate(SOURCE, c + ".tmp.c", m1, m2, m3, ROOTS)
+            f77c.translate(SOURCE, c + ".tmp.c", m1, m2, m3, ROOTS, omp=omp)
             os.replace(c + ".tmp.c", c)
             os.replace(c + ".tmp.json", j)
     if not os.path.exists(c):
         raise FileNotFoundError(f"no reference source ({SOURCE}) and no earlier translation ({c})")
     if not os.path.exists(so) or any(os.path.getmtime(d) > os.path.getmtime(so) for d in (c, shim)):
-        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=gnu11",
-                               "-w", "-o", so + ".tmp", c, shim, "-lm"])
+        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=gnu11", "-w"]
+        if omp:
+            cmd.append("-fopenmp")
+        subprocess.check_call(cmd + ["-o", so + ".tmp", c, shim, "-lm"])
         os.replace(so + ".tmp", so)
     return so
 
@@ -69,13 +74,18 @@ def build(m1: int, m2: int, m3: int) -> str:
 TEST_EXTENTS = [(17, 17, 17), (33, 25, 49), (33, 17, 33)]
 
 
+# PARAMETER extents of the benchmark's reference arm (channel384), built with OpenMP
+ARM_EXTENTS = [(385, 257, 385)]
+
+
 def build_for_tests():
-    """Builds the libraries of TEST_EXTENTS (in parallel) where the reference source or an
-    earlier translation is present; returns the paths built."""
+    """Builds the libraries of TEST_EXTENTS and, with OpenMP, of ARM_EXTENTS (in parallel)
+    where the reference source or an earlier translation is present; returns the paths."""
     import concurrent.futures as cf
-    todo = [m for m in TEST_EXTENTS if available(*m)]
+    todo = [(m, False) for m in TEST_EXTENTS if available(*m)]
+    todo += [(m, True) for m in ARM_EXTENTS if available(*m, omp=True)]
     with cf.ThreadPoolExecutor(max_workers=max(1, len(todo))) as ex:
-        return list(ex.map(lambda m: build(*m), todo))
+        return list(ex.map(lambda t: build(*t[0], omp=t[1]), todo))
 
 
 def _dp(a):
@@ -89,12 +99,28 @@ class RefChannel:
     library are given), so grids with any stretching can be compared; ``reference_mesh``
     runs the reference's own MESH instead (CKS = 2.5 as compact3d.f hard-codes it)."""
 
-    def __init__(self, grid, reference_mesh: bool = False):
+    def __init__(self, grid, reference_mesh: bool = False, omp: bool = False):
         self.g = g = grid
         self.m = (g.n1, g.n2, g.n3)
-        so = build(*self.m)
+        self.omp = omp
+        self._runner = None
+        if omp:
+            # the OpenMP build keeps its per-call arrays on the stack, as a recursive Fortran
+            # build does: its calls run on a thread with a 1 GiB stack, its worker threads get
+            # OMP_STACKSIZE (effective when the OpenMP runtime has not started yet)
+            os.environ.setdefault("OMP_STACKSIZE", "64M")
+            import concurrent.futures as cf
+            import threading
+            old = threading.stack_size()
+            threading.stack_size(1 << 30)
+            try:
+                self._runner = cf.ThreadPoolExecutor(max_workers=1)
+                self._runner.submit(lambda: None).result()
+            finally:
+                threading.stack_size(old)
+        so = build(*self.m, omp=omp)
         self.lib = ctypes.CDLL(so)
-        self.layout = json.load(open(_paths(*self.m)[1]))["layout"]
+        self.layout = json.load(open(_paths(*self.m, omp)[1]))["layout"]
         self.set("DIM", N1=g.n1, N2=g.n2, N3=g.n3, N1M=g.n1m, N2M=g.n2m, N3M=g.n3m)
         self.set("SIZE", ALX=g.alx, ALY=2.0 if g.aly > 1.5 else 1.0, ALZ=g.alz)
         self.set("PARA", RE=g.re)
@@ -131,7 +157,7 @@ class RefChannel:
     def view(self, block, name):
         """A numpy view of a COMMON variable (Fortran order, its declared bounds)."""
         v = self._var(block, name)
-        base = ctypes.addressof(ctypes.c_ubyte.in_dll(self.lib, f"f77c_{block}"))
+        base = ctypes.c_void_p.in_dll(self.lib, f"f77c_{block}").value   # the block's memory
         shape = tuple(hi - lo + 1 for lo, hi in v["dims"]) or (1,)
         n = int(np.prod(shape))
         dt = np.dtype(NP[v["type"]])
@@ -162,9 +188,15 @@ class RefChannel:
             # MAIN calls WALLSS before GETUP when there is no wall model (compact3d.f:125):
             # the SGS models' van Driest damping reads its WSM
             t = ctypes.c_double(0.0)
-            self.lib.f77_WALLSS(_dp(U), _dp(P), ctypes.byref(t))
-        self.lib.f77_GETUP(_dp(U), _dp(P), _dp(HH), _dp(self._ss), ctypes.byref(nt), ctypes.byref(pg),
-                           ctypes.byref(pg3), _dp(S))
+            if self._runner is not None:
+                self._runner.submit(self.lib.f77_WALLSS, _dp(U), _dp(P), ctypes.byref(t)).result()
+            else:
+                self.lib.f77_WALLSS(_dp(U), _dp(P), ctypes.byref(t))
+        args = (_dp(U), _dp(P), _dp(HH), _dp(self._ss), ctypes.byref(nt), ctypes.byref(pg), ctypes.byref(pg3), _dp(S))
+        if self._runner is not None:
+            self._runner.submit(self.lib.f77_GETUP, *args).result()
+        else:
+            self.lib.f77_GETUP(*args)
         return pg.value, pg3.value
 
     def divcheck(self, U):

@@ -178,3 +178,25 @@ def test_golden_fixtures_match_oracle(oracle_mod):
             assert rel(tw, d["TAUW"]) < 1e-12 and rel(tb, d["TAUB"]) < 1e-12
             sl = (slice(1, g.n1m + 1), slice(None), slice(1, g.n3m + 1))
             assert rel(S[sl], d["SGSVIS"][sl]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["tiny16", "small32"])
+def test_openmp_translation_matches_serial(name):
+    """The reference with its !$OMP PARALLEL DO loops kept (the form the benchmark's
+    reference arm times) computes the serial translation's steps to rounding: five steps,
+    1e-13 for u, v, w, HH, 1e-10 for P (only the order of the OpenMP reductions differs)."""
+    g, dt = make_grid(name)
+    A = ref.RefChannel(g)
+    B = ref.RefChannel(g, omp=True)
+    U, P, HH = ic.perturbed_laminar(g)
+    X = [x.copy(order="F") for x in (U, P, HH)]
+    Y = [x.copy(order="F") for x in (U, P, HH)]
+    pa = pa3 = pb = pb3 = 0.0
+    for n in range(1, 6):
+        pa, pa3 = A.getup(*X, n, dt, pa, pa3)
+        pb, pb3 = B.getup(*Y, n, dt, pb, pb3)
+    a, b = interior(g, *X), interior(g, *Y)
+    for f in ("u", "v", "w", "hh"):
+        assert rel(b[f], a[f]) < 1e-13, (f, rel(b[f], a[f]))
+    assert rel(b["p"], a["p"]) < 1e-10
+    assert pb == pytest.approx(pa, rel=1e-8)
