@@ -469,9 +469,11 @@ def run_ours(args, D: Dist):
     # ---- end to end through the host-array drop-in (c3d_getup) ----
     if not args.no_e2e:
         from compact3d_gb300 import lib as L
-        U, P, HH = U0.copy(order="F"), P0.copy(order="F"), HH0.copy(order="F")
-        for a in (U, P, HH):
-            L.host_register(a)
+        # the driver's arrays in page-locked memory from c3d_host_alloc (an array pinned
+        # after the fact keeps whatever physical pages it has; after another process has
+        # used and freed tens of GB of host memory those transfer far below the link rate)
+        U, P, HH = (L.host_array(a.shape) for a in (U0, P0, HH0))
+        U[...], P[...], HH[...] = U0, P0, HH0
         ce = lib.Channel(g, FORMS[args.form])
         ce.upload(U, P, HH)
         ce.project()
@@ -481,13 +483,20 @@ def run_ours(args, D: Dist):
         for _ in range(min(W, 2)):
             pg, pg3 = ce.getup(U, P, HH, m, dt, pg, pg3)
             m += 1
+        # The host memory behind the link is shared with the machine's other tenants: a
+        # window of getups now and then runs at half the link rate although the pages and
+        # the path are unchanged, so the figure is the median of several timed windows and
+        # every window is listed.
         ke = max(2, min(K, args.e2e_steps))
-        D.barrier()
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            pg, pg3 = ce.getup(U, P, HH, m, dt, pg, pg3)
-            m += 1
-        te = D.max(time.perf_counter() - t0)
+        wins = []
+        for _ in range(max(1, args.e2e_windows)):
+            D.barrier()
+            t0 = time.perf_counter()
+            for _ in range(ke):
+                pg, pg3 = ce.getup(U, P, HH, m, dt, pg, pg3)
+                m += 1
+            wins.append(D.max(time.perf_counter() - t0))
+        te = statistics.median(wins)
         bytes_io = U.nbytes + P.nbytes + HH.nbytes
         link = host_link_gbs(D.local)
         # Floor of a getup: every input byte must cross the link before the step can finish
@@ -499,12 +508,13 @@ def run_ours(args, D: Dist):
                           d2h_bytes_per_step=bytes_io, steps=ke, ms_per_step=e2e_ms,
                           link_gbs={k: round(v, 1) for k, v in link.items()},
                           floor_ms=floor_ms, frac_of_floor=floor_ms / e2e_ms,
-                          path="c3d_getup: pinned Fortran-layout host arrays by DMA through a device "
+                          windows_ms_per_step=[round(w / ke * 1e3, 2) for w in wins],
+                          path="c3d_getup: Fortran-layout host arrays in page-locked memory (c3d_host_alloc) by DMA through a device "
                                "staging area on a copy stream, U/P then HH in, HH out from the end of xB "
                                "while the step runs, U/P out after it")
-        for a in (U, P, HH):
-            L.host_unregister(a)
         ce.close()
+        for a in (U, P, HH):
+            L.host_free(a)
     ch.close()
 
     # ---- batched ensemble (configs with many independent channels) ----
@@ -962,6 +972,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=5)
     ap.add_argument("--err-steps", type=int, default=20)
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-windows", type=int, default=7, help="timed windows of --e2e-steps getups (median reported)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

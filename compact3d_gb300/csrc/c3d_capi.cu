@@ -871,6 +871,24 @@ int c3d_host_unregister(void *ptr) {
     return 0;
 }
 
+int c3d_host_alloc(size_t bytes, void **ptr) {
+    if (!ptr || !bytes) { set_error("null pointer or zero size"); return C3D_EINVAL; }
+    *ptr = nullptr;
+    if (cudaHostAlloc(ptr, bytes, cudaHostAllocMapped) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        set_error("cudaHostAlloc failed");
+        return C3D_ENOMEM;
+    }
+    return 0;
+}
+
+int c3d_host_free(void *ptr) {
+    if (!ptr) { set_error("null pointer"); return C3D_EINVAL; }
+    CK(cudaFreeHost(ptr));
+    return 0;
+}
+
 // TAUW/TAUB(0:M1,0:M3,2): interior I = 1..N1M, K = 1..N3M of both walls move.
 static int wall_copy(c3d_channel *ch, double *host, double *dev, bool up) {
     const Geo &g = ch->g;

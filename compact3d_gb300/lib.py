@@ -71,6 +71,8 @@ SIGNATURES = {
     "c3d_project": (_ip, [_vp]),
     "c3d_host_register": (_ip, [_vp, ctypes.c_size_t]),
     "c3d_host_unregister": (_ip, [_vp]),
+    "c3d_host_alloc": (_ip, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
+    "c3d_host_free": (_ip, [_vp]),
     "c3d_sync": (_ip, [_vp]),
     "c3d_pipe_wait_selftest": (_ip, [_vp, ctypes.c_double]),
     "c3d_last_step_stats": (_ip, [_vp, _dp, ctypes.POINTER(_ip)]),
@@ -473,6 +475,26 @@ class TimeAverage:
         return self.mean
 
 
+_host_arrays = {}
+
+
+def host_array(shape, dtype=np.float64) -> np.ndarray:
+    """A Fortran-order array in page-locked host memory from c3d_host_alloc (transfers at
+    the host link's rate); release it with host_free."""
+    n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+    p = _vp()
+    check(load().c3d_host_alloc(n, ctypes.byref(p)), "c3d_host_alloc")
+    buf = (ctypes.c_char * n).from_address(p.value)
+    a = np.ndarray(shape, dtype=dtype, buffer=buf, order="F")
+    _host_arrays[a.ctypes.data] = p.value
+    return a
+
+
+def host_free(a: np.ndarray):
+    p = _host_arrays.pop(a.ctypes.data)
+    check(load().c3d_host_free(p), "c3d_host_free")
+
+
 def host_register(a: np.ndarray):
     check(load().c3d_host_register(a.ctypes.data, a.nbytes), "c3d_host_register")
 
@@ -481,5 +503,5 @@ def host_unregister(a: np.ndarray):
     check(load().c3d_host_unregister(a.ctypes.data), "c3d_host_unregister")
 
 
-__all__ = ["Channel", "Batch", "load", "C3DError", "host_register", "host_unregister", "C3D_FP64",
+__all__ = ["Channel", "Batch", "load", "C3DError", "host_register", "host_unregister", "host_array", "host_free", "C3D_FP64",
            "C3D_MIXED", "SIGNATURES"]

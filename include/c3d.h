@@ -201,6 +201,14 @@ int c3d_project(c3d_channel *ch);
  * one-field staging buffer, one field at a time. */
 int c3d_host_register(void *ptr, size_t bytes);
 int c3d_host_unregister(void *ptr);
+/* Allocates `bytes` of page-locked host memory (cudaHostAlloc, mapped) for a driver's
+ * field arrays, and frees it.  Arrays allocated here move at the host link's rate
+ * whatever the state of the host's memory; an existing array that c3d_host_register
+ * pins keeps the physical pages it happens to have, and on a host whose free memory is
+ * fragmented (for example after another process used and released tens of GB) its
+ * transfers measured four times slower.  No counterpart in the reference. */
+int c3d_host_alloc(size_t bytes, void **ptr);
+int c3d_host_free(void *ptr);
 /* Blocks until all work queued on the channel's stream has finished. */
 int c3d_sync(c3d_channel *ch);
 /* Device time of the last c3d_step in milliseconds (CUDA events on the
