@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libc3d.so")
-SOURCES = ["c3d_capi.cu", "c3d_step.cu", "c3d_xpass.cu", "c3d_zpass.cu", "c3d_spec.cu", "c3d_noalloc.cu", "c3d_les.cu", "c3d_ops.cu", "c3d_refine.cu", "c3d_ckpt.cu", "c3d_stats.cu", "c3d_iwm.cu"]
+SOURCES = ["c3d_capi.cu", "c3d_step.cu", "c3d_xpass.cu", "c3d_xbatch.cu", "c3d_zpass.cu", "c3d_spec.cu", "c3d_noalloc.cu", "c3d_les.cu", "c3d_ops.cu", "c3d_refine.cu", "c3d_ckpt.cu", "c3d_stats.cu", "c3d_iwm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

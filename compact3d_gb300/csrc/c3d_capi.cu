@@ -641,7 +641,7 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
     rc = launch_poisson_tables(ch);
     if (rc) return fail(rc);
     // FFT plans and twiddles: [x: N1M/2][z: N3M][x post-processing: N1M/2+1]
-    ch->tune = Tune{{16, 16, 16, 16, 16}, 4, 8, 0, 0, 0, 0, 0, 0, 0};
+    ch->tune = Tune{{16, 16, 16, 16, 16}, 4, 8, 0, 0, 0, 0, 0, 0, 0, 0};
     ch->fx = make_plan(g.n1m / 2, 0);
     ch->fz = make_plan(g.n3m, 0);
     if (ch->fx.nst < 0 || ch->fz.nst < 0) { set_error("FFT plan index arithmetic"); return fail(C3D_EINVAL); }
@@ -1596,7 +1596,8 @@ bool tune_ok(const c3d_channel *ch, const Tune &t) {
     const bool fx = t.fxp >= 0 && t.fxp <= 2 ? true : (t.fxp == 3 && ch->g.n1m % 64 == 0);
     return zl && xw && tw && fx && t.fzp >= 0 && t.fzp <= 2 && (t.zsplit == 0 || t.zsplit == 1) &&
            (t.xsplit == 0 || t.xsplit == 1) && (t.xbulk == 0 || t.xbulk == 2 || t.xbulk == 3) &&
-           (t.xstage == 0 || (t.xstage == 1 && ch->g.n1m % 2 == 0)) && (t.ycn == 0 || t.ycn == 32 || t.ycn == 64);
+           (t.xstage == 0 || (t.xstage == 1 && ch->g.n1m % 2 == 0)) && (t.ycn == 0 || t.ycn == 32 || t.ycn == 64) &&
+           (t.xlanes == 0 || t.xlanes == x_segment_lanes(ch->g.n1m, ch->g.n3m));
 }
 
 // Sets the schedule; the FFT plans get the new radix order and keep their twiddle tables.
@@ -1640,13 +1641,14 @@ int c3d_get_schedule(c3d_channel *ch, int *sched) {
     sched[11] = t.xbulk;
     sched[12] = t.xstage;
     sched[13] = t.ycn;
+    sched[14] = t.xlanes;
     return 0;
 }
 
 int c3d_set_schedule(c3d_channel *ch, const int *sched) {
     if (!ch || !sched) { set_error("null argument"); return C3D_EINVAL; }
     Tune t{{sched[0], sched[1], sched[2], sched[3], sched[4]}, sched[5], sched[6], sched[7], sched[8], sched[9],
-           sched[10], sched[11], sched[12], sched[13]};
+           sched[10], sched[11], sched[12], sched[13], sched[14]};
     if (!tune_ok(ch, t)) { set_error("invalid schedule"); return C3D_EINVAL; }
     apply_tune(ch, t);
     return 0;
@@ -1684,10 +1686,11 @@ int c3d_autotune(c3d_channel *ch, int *sched) {
     const double dt = ch->dt_cached > 0 ? ch->dt_cached : 1e-3;
     // knob q: 0-4 the segment length of zA..zE, 5 x rows per block, 6 z-FFT tile, 7/8 plans,
     // 9 zA split, 10 xA split, 11 bulk-copy stages of the x passes, 12 xA rows staged by bulk copies,
-    // 13 form of the wall-normal CN factor
+    // 13 form of the wall-normal CN factor, 14 lanes per row of xA and xB
     struct Group { int knob; std::vector<int> cand; std::vector<std::string> kernels; };
     const Group groups[] = {
-        {9, {0, 1}, {"zA"}}, {10, {0, 1}, {"xA"}}, {12, {0, 1}, {"xA"}}, {13, {0, 32, 64}, {"ycn"}},
+        {9, {0, 1}, {"zA"}}, {10, {0, 1}, {"xA"}}, {12, {0, 1}, {"xA"}}, {14, {0, 8, 16}, {"xA", "xB"}},
+        {13, {0, 32, 64}, {"ycn"}},
         {0, {0, 8, 16, 32}, {"zA"}}, {1, {0, 8, 16, 32}, {"zB"}}, {2, {0, 8, 16, 32}, {"zC"}},
         {3, {0, 8, 16, 32}, {"zD"}}, {4, {0, 8, 16, 32}, {"zE"}},
         {5, {2, 4, 8}, {"xA", "xB", "xC", "xD"}},
@@ -1697,7 +1700,8 @@ int c3d_autotune(c3d_channel *ch, int *sched) {
         {11, {0, 2, 3}, {"xC"}},
     };
     auto knob = [](Tune &t, int q) -> int & {
-        return q < 5 ? t.zl[q] : q == 5 ? t.xw : q == 6 ? t.twz : q == 7 ? t.fxp : q == 8 ? t.fzp : q == 9 ? t.zsplit : q == 10 ? t.xsplit : q == 11 ? t.xbulk : q == 12 ? t.xstage : t.ycn;
+        return q < 5 ? t.zl[q] : q == 5 ? t.xw : q == 6 ? t.twz : q == 7 ? t.fxp : q == 8 ? t.fzp : q == 9 ? t.zsplit
+             : q == 10 ? t.xsplit : q == 11 ? t.xbulk : q == 12 ? t.xstage : q == 13 ? t.ycn : t.xlanes;
     };
     Tune best = ch->tune;
     for (const Group &gp : groups) {

@@ -108,23 +108,30 @@ __device__ __forceinline__ dfl &operator+=(dfl &a, dfl b) { return a = a + b; }
 __device__ __forceinline__ dfl &operator*=(dfl &a, dfl b) { return a = a * b; }
 
 // Warp shuffles for every value type of the line solvers.
-__device__ __forceinline__ double shfl_up(double v, int d) { return __shfl_up_sync(FULL, v, d); }
-__device__ __forceinline__ float shfl_up(float v, int d) { return __shfl_up_sync(FULL, v, d); }
-__device__ __forceinline__ dfl shfl_up(dfl v, int d) {
-    return dfl(__shfl_up_sync(FULL, v.h, d), __shfl_up_sync(FULL, v.l, d));
+// Shuffles within segments of w lanes (w = 32: the whole warp); lane indexes and
+// offsets are relative to the segment.
+__device__ __forceinline__ double shfl_up(double v, int d, int w = 32) { return __shfl_up_sync(FULL, v, d, w); }
+__device__ __forceinline__ float shfl_up(float v, int d, int w = 32) { return __shfl_up_sync(FULL, v, d, w); }
+__device__ __forceinline__ dfl shfl_up(dfl v, int d, int w = 32) {
+    return dfl(__shfl_up_sync(FULL, v.h, d, w), __shfl_up_sync(FULL, v.l, d, w));
 }
-__device__ __forceinline__ double shfl_down(double v, int d) { return __shfl_down_sync(FULL, v, d); }
-__device__ __forceinline__ float shfl_down(float v, int d) { return __shfl_down_sync(FULL, v, d); }
-__device__ __forceinline__ dfl shfl_down(dfl v, int d) {
-    return dfl(__shfl_down_sync(FULL, v.h, d), __shfl_down_sync(FULL, v.l, d));
+__device__ __forceinline__ double shfl_down(double v, int d, int w = 32) { return __shfl_down_sync(FULL, v, d, w); }
+__device__ __forceinline__ float shfl_down(float v, int d, int w = 32) { return __shfl_down_sync(FULL, v, d, w); }
+__device__ __forceinline__ dfl shfl_down(dfl v, int d, int w = 32) {
+    return dfl(__shfl_down_sync(FULL, v.h, d, w), __shfl_down_sync(FULL, v.l, d, w));
 }
-__device__ __forceinline__ double shfl_idx(double v, int s) { return __shfl_sync(FULL, v, s); }
-__device__ __forceinline__ float shfl_idx(float v, int s) { return __shfl_sync(FULL, v, s); }
-__device__ __forceinline__ dfl shfl_idx(dfl v, int s) { return dfl(__shfl_sync(FULL, v.h, s), __shfl_sync(FULL, v.l, s)); }
+__device__ __forceinline__ double shfl_idx(double v, int s, int w = 32) { return __shfl_sync(FULL, v, s, w); }
+__device__ __forceinline__ float shfl_idx(float v, int s, int w = 32) { return __shfl_sync(FULL, v, s, w); }
+__device__ __forceinline__ dfl shfl_idx(dfl v, int s, int w = 32) {
+    return dfl(__shfl_sync(FULL, v.h, s, w), __shfl_sync(FULL, v.l, s, w));
+}
 
-// Cyclic solve on the warp's row held as lane chunks x[0..C); in place, returns s*B(F(x)).
-template <typename R, int C>
+// Cyclic solve on a row held as lane chunks x[0..C) by a segment of W lanes (lane =
+// the lane within the segment; W = 32: one row per warp, W < 32: 32/W rows per warp,
+// every segment of the warp calling together); in place, returns s*B(F(x)).
+template <int W = 32, typename R, int C>
 __device__ __forceinline__ void xsolve(R (&x)[C], int lane, int P, const Cyc<R> &c) {
+    static_assert(W == 4 || W == 8 || W == 16 || W == 32, "row segments of 4, 8, 16 or 32 lanes");
     const bool act = lane < P;
     const R r = c.r;
     R y = R(0), m = R(1);
@@ -136,17 +143,17 @@ __device__ __forceinline__ void xsolve(R (&x)[C], int lane, int P, const Cyc<R> 
     R e = act ? y : R(0);
     if (!act) m = R(1);
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        R ep = shfl_up(e, off), mp = shfl_up(m, off);
+    for (int off = 1; off < W; off <<= 1) {
+        R ep = shfl_up(e, off, W), mp = shfl_up(m, off, W);
         if (lane >= off) {
             e = e + m * ep;
             m = m * mp;
         }
     }
     {
-        R et = shfl_idx(e, 31), mt = shfl_idx(m, 31);
+        R et = shfl_idx(e, W - 1, W), mt = shfl_idx(m, W - 1, W);
         R y0 = et / (R(1) - mt);
-        R ex = shfl_up(e, 1), mx = shfl_up(m, 1);
+        R ex = shfl_up(e, 1, W), mx = shfl_up(m, 1, W);
         y = (lane == 0) ? y0 : ex + mx * y0;
     }
 #pragma unroll
@@ -164,18 +171,18 @@ __device__ __forceinline__ void xsolve(R (&x)[C], int lane, int P, const Cyc<R> 
     e = act ? z : R(0);
     if (!act) m = R(1);
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        R en = shfl_down(e, off), mn = shfl_down(m, off);
-        if (lane + off < 32) {
+    for (int off = 1; off < W; off <<= 1) {
+        R en = shfl_down(e, off, W), mn = shfl_down(m, off, W);
+        if (lane + off < W) {
             e = e + m * en;
             m = m * mn;
         }
     }
     {
-        R e0 = shfl_idx(e, 0), m0 = shfl_idx(m, 0);
+        R e0 = shfl_idx(e, 0, W), m0 = shfl_idx(m, 0, W);
         R z0 = e0 / (R(1) - m0);
-        R en1 = shfl_down(e, 1), mn1 = shfl_down(m, 1);
-        z = (lane == 31) ? z0 : en1 + mn1 * z0;
+        R en1 = shfl_down(e, 1, W), mn1 = shfl_down(m, 1, W);
+        z = (lane == W - 1) ? z0 : en1 + mn1 * z0;
     }
     const R s = c.s;
 #pragma unroll

@@ -126,6 +126,7 @@ struct Tune {
     int xbulk;    // x passes with rows staged by a bulk-copy ring of this many stages (0: off)
     int xstage;   // xA's pieces read their rows from global memory (0) or stage them in shared memory by bulk copies (1)
     int ycn;      // wall-normal CN factor: one thread per column (0) or shared-memory tiles of 32 or 64 columns
+    int xlanes;   // xA's pieces (read from global memory) and xB with a row per segment of this many lanes (0: a warp)
 };
 
 // Arguments of the pressure refinement (mixed form with C3D_MIXED_IR): double-float
@@ -288,6 +289,8 @@ int launch_pipe_selftest(c3d_channel *ch, double limit_ms);
 // one channel's step in order (batch_plan), and its StepArgs<R> for the step with DT dt
 // written as bytes to dst (batch_args, batch_args_size bytes).
 template <typename R> int xpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);
+// Lanes per row segment of the batch xA and xB for a channel of N1M x N3M (0: one row per warp).
+int x_segment_lanes(int n1m, int n3m);
 template <typename R> int zpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);
 template <typename R> int spec_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);
 int batch_plan(c3d_channel *ch, std::vector<BKern> &out);

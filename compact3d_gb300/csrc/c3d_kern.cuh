@@ -101,17 +101,19 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
     return df_norm(s, e);
 }
 
-// Warp shuffles for every state/working type
-__device__ __forceinline__ double shfl_any(double v, int src) { return __shfl_sync(FULL, v, src); }
-__device__ __forceinline__ float shfl_any(float v, int src) { return __shfl_sync(FULL, v, src); }
-__device__ __forceinline__ dfl shfl_any(dfl v, int src) { return shfl_idx(v, src); }
-__device__ __forceinline__ float2 shfl_any(float2 v, int src) {
-    return make_float2(__shfl_sync(FULL, v.x, src), __shfl_sync(FULL, v.y, src));
+// Warp shuffles for every state/working type, within segments of w lanes
+__device__ __forceinline__ double shfl_any(double v, int src, int w = 32) { return __shfl_sync(FULL, v, src, w); }
+__device__ __forceinline__ float shfl_any(float v, int src, int w = 32) { return __shfl_sync(FULL, v, src, w); }
+__device__ __forceinline__ dfl shfl_any(dfl v, int src, int w = 32) { return shfl_idx(v, src, w); }
+__device__ __forceinline__ float2 shfl_any(float2 v, int src, int w = 32) {
+    return make_float2(__shfl_sync(FULL, v.x, src, w), __shfl_sync(FULL, v.y, src, w));
 }
-template <typename T>
-__device__ __forceinline__ T sprev(T last, int lane, int P) { return shfl_any(last, (lane == 0) ? P - 1 : lane - 1); }
-template <typename T>
-__device__ __forceinline__ T snext(T first, int lane, int P) { return shfl_any(first, (lane + 1 >= P) ? 0 : lane + 1); }
+// The last value of the previous lane's chunk and the first of the next one, cyclic over
+// the P active lanes of a row segment of W lanes.
+template <int W = 32, typename T>
+__device__ __forceinline__ T sprev(T last, int lane, int P) { return shfl_any(last, (lane == 0) ? P - 1 : lane - 1, W); }
+template <int W = 32, typename T>
+__device__ __forceinline__ T snext(T first, int lane, int P) { return shfl_any(first, (lane + 1 >= P) ? 0 : lane + 1, W); }
 
 // Stencils shared by both forms, written once per representation.
 template <typename R> struct Sten;
@@ -628,10 +630,11 @@ __device__ __forceinline__ C2 *fft_smem(C2 *a, C2 *b, const FftPlan &pl, int lsh
 // L2 prefetch of one address (fire and forget)
 __device__ __forceinline__ void pf_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-// The warp prefetches `bytes` contiguous bytes starting at p into L2 (128-byte lines).
-__device__ __forceinline__ void pf_row(const void *p, int bytes, int lane) {
+// The w lanes of a row segment (lane = the lane within it) prefetch `bytes` contiguous
+// bytes starting at p into L2 (128-byte lines).
+__device__ __forceinline__ void pf_row(const void *p, int bytes, int lane, int w = 32) {
     const char *c = (const char *)p;
-    for (int off = lane * 128; off < bytes; off += 32 * 128) pf_l2(c + off);
+    for (int off = lane * 128; off < bytes; off += w * 128) pf_l2(c + off);
 }
 
 // The warp prefetches into L2 the window of positions [k0-m, k0+len+m) of the columns it

@@ -370,7 +370,7 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
 
 /* ---- launch schedule -----------------------------------------------------
  * The kernels' launch shapes are chosen per grid shape by an autotuner written for
- * this library (no counterpart in the reference).  A schedule is fourteen ints
+ * this library (no counterpart in the reference).  A schedule is fifteen ints
  * (C3D_SCHEDULE_LEN):
  *   [0..4] z-line segment length (8, 16, 32) of each z pass: the points each thread
  *       solves sequentially (Thomas-like) before the parallel segments of a z line
@@ -399,6 +399,11 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
  *       register batches of planes (0), or blocks of 32 or 64 columns whose planes
  *       are staged in shared memory by bulk copies so that each value is read and
  *       written once (falls back to 0 when the tile exceeds shared memory)
+ *   [14] lanes per row of the explicit x pieces read from global memory and of the
+ *       x pass of the remaining terms: 0 (a warp per row), or the row segment of
+ *       short rows, accepted only at N1M = 48, 64, 96 (8 lanes) or 128 (16 lanes)
+ *       with N3M a multiple of 32 / lanes, so that each lane holds 6 to 12 points
+ *       and the cross-lane scans of the line solves take 3 or 4 steps instead of 5
  * c3d_autotune  times the candidates on a scratch channel of the same grid holding a
  *               copy of this channel's state (so the channel needs its state), keeps
  *               the fastest per kernel group, applies it, and caches it per grid
@@ -406,7 +411,7 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
  *               receives the result.
  * c3d_set_schedule / c3d_get_schedule  set or read a schedule directly.
  * Channels of a batch are tuned before the batch's first step captures its graph. */
-#define C3D_SCHEDULE_LEN 14
+#define C3D_SCHEDULE_LEN 15
 int c3d_autotune(c3d_channel *ch, int *sched);
 int c3d_get_schedule(c3d_channel *ch, int *sched);
 int c3d_set_schedule(c3d_channel *ch, const int *sched);

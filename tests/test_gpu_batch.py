@@ -119,12 +119,19 @@ def test_batch_refuses_iwmles(L):
         L.Batch([g])
 
 
+def row_lanes(g):
+    """Lanes per row of the work-list form's xA pieces and xB: 8 for rows of 48, 64 or
+    96 points, 16 for 128 (when N3M is a multiple of 32 / lanes), else a warp (0)."""
+    w = {48: 8, 64: 8, 96: 8, 128: 16}.get(g.n1m, 0)
+    return w if w and g.n3m % (32 // w) == 0 else 0
+
+
 def worklist_schedule(ch, g):
     """The fixed schedule of the work-list form (include/c3d.h) on a single channel."""
     s = ch.get_schedule()
     s.update({f"z_segment_z{c}": 16 for c in "ABCDE"})
     s.update(x_rows_per_block=2, fft_z_tile=0, fft_x_plan=3 if g.n1m % 64 == 0 else 0, fft_z_plan=0,
-             z_split_zA=1, x_split_xA=1, x_bulk_stages=0, x_stage_xA=0)
+             z_split_zA=1, x_split_xA=1, x_bulk_stages=0, x_stage_xA=0, x_row_lanes=row_lanes(g))
     ch.set_schedule(s)
 
 

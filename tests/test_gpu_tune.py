@@ -26,10 +26,10 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def _sched(zl, xw, tw, fx, fz, split, xsplit, xbulk=0, xstage=0, ycn=0):
+def _sched(zl, xw, tw, fx, fz, split, xsplit, xbulk=0, xstage=0, ycn=0, xlanes=0):
     d = {f"z_segment_z{c}": z for c, z in zip("ABCDE", zl)}
     d.update(x_rows_per_block=xw, fft_z_tile=tw, fft_x_plan=fx, fft_z_plan=fz, z_split_zA=split,
-             x_split_xA=xsplit, x_bulk_stages=xbulk, x_stage_xA=xstage, ycn_tile=ycn)
+             x_split_xA=xsplit, x_bulk_stages=xbulk, x_stage_xA=xstage, ycn_tile=ycn, x_row_lanes=xlanes)
     return d
 
 
@@ -93,6 +93,47 @@ def test_x_plan3_refused_unless_n1m_multiple_of_64(libc3d, oracle_mod, n1m):
     for c, j0 in ((0, 1), (1, 2), (2, 1)):
         e = rel(Ug[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c], U[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c])
         assert e < 1e-10, (n1m, c, e)
+
+
+@pytest.mark.parametrize("n1m,lanes", [(48, 8), (64, 8), (96, 8), (128, 16)])
+def test_row_segments_match_oracle(libc3d, oracle_mod, n1m, lanes):
+    """xA's pieces and xB with a row per segment of 8 or 16 lanes (4 or 2 rows per warp,
+    6 to 12 points per lane): one FP64 step within 1e-10 of the oracle; the mixed form
+    within FP32 rounding of its whole-warp step; other lane counts are refused."""
+    g, dt = make_grid("small32", n1m=n1m, n2m=16, n3m=32)
+    orc = oracle_mod.Oracle(g)
+    U, P, HH = ic.perturbed_laminar(g)
+    orc.project(U)
+    ch = libc3d.Channel(g, C3D_FP64)
+    ch.upload(U, P, HH)
+    s = ch.get_schedule()
+    s.update(x_split_xA=1, x_stage_xA=0, x_row_lanes=lanes)
+    ch.set_schedule(s)
+    assert ch.get_schedule()["x_row_lanes"] == lanes
+    with pytest.raises(libc3d.C3DError):
+        ch.set_schedule(dict(s, x_row_lanes=24 - lanes))
+    U0, P0, H0 = U.copy(order="F"), P.copy(order="F"), HH.copy(order="F")
+    orc.getup(U, P, HH, 1, dt, 0.0, 0.0)
+    ch.step(1, dt, 0.0, 0.0)
+    Ug, _, Hg = ch.download()
+    n1, n2, n3 = g.n1m, g.n2m, g.n3m
+    for c, j0 in ((0, 1), (1, 2), (2, 1)):
+        e = rel(Ug[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c], U[1:n1 + 1, j0:n2 + 1, 1:n3 + 1, c])
+        assert e < 1e-10, (n1m, c, e)
+    assert rel(Hg[1:n1 + 1, 1:n2 + 1, 1:n3 + 1], HH[1:n1 + 1, 1:n2 + 1, 1:n3 + 1]) < 1e-10
+    ch.close()
+    out = []
+    for w in (0, lanes):
+        m = libc3d.Channel(g, C3D_MIXED)
+        m.upload(U0, P0, H0)
+        m.set_schedule(dict(m.get_schedule(), x_split_xA=1, x_stage_xA=0, x_row_lanes=w))
+        pg = pg3 = 0.0
+        for n in (1, 2, 3):
+            pg, pg3 = m.step(n, dt, pg, pg3)
+        out.append(m.download())
+        m.close()
+    assert rel(out[1][0], out[0][0]) < 1e-8
+    assert rel(out[1][2], out[0][2]) < 1e-4
 
 
 @pytest.mark.parametrize("sched,n3m", SCHEDULES)
