@@ -1689,7 +1689,7 @@ int c3d_autotune(c3d_channel *ch, int *sched) {
     // 13 form of the wall-normal CN factor, 14 lanes per row of xA and xB
     struct Group { int knob; std::vector<int> cand; std::vector<std::string> kernels; };
     const Group groups[] = {
-        {9, {0, 1}, {"zA"}}, {10, {0, 1}, {"xA"}}, {12, {0, 1}, {"xA"}}, {14, {0, 8, 16}, {"xA", "xB"}},
+        {9, {0, 1}, {"zA"}}, {10, {0, 1}, {"xA"}}, {12, {0, 1}, {"xA"}}, {14, {0, 8, 16}, {"xA", "xB", "xC", "xD"}},
         {13, {0, 32, 64}, {"ycn"}},
         {0, {0, 8, 16, 32}, {"zA"}}, {1, {0, 8, 16, 32}, {"zB"}}, {2, {0, 8, 16, 32}, {"zC"}},
         {3, {0, 8, 16, 32}, {"zD"}}, {4, {0, 8, 16, 32}, {"zE"}},

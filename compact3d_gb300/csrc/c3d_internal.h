@@ -126,7 +126,7 @@ struct Tune {
     int xbulk;    // x passes with rows staged by a bulk-copy ring of this many stages (0: off)
     int xstage;   // xA's pieces read their rows from global memory (0) or stage them in shared memory by bulk copies (1)
     int ycn;      // wall-normal CN factor: one thread per column (0) or shared-memory tiles of 32 or 64 columns
-    int xlanes;   // xA's pieces (read from global memory) and xB with a row per segment of this many lanes (0: a warp)
+    int xlanes;   // x passes (xA pieces from global memory, xB, xC/xD with the shared-memory FFT) with a row per segment of this many lanes (0: a warp)
 };
 
 // Arguments of the pressure refinement (mixed form with C3D_MIXED_IR): double-float

@@ -565,13 +565,14 @@ __device__ __forceinline__ void xrow_c2r(R (&d)[C], const typename Cx<R>::T *__r
 }
 
 // One radix-P Stockham stage: a -> b over 2^lsh interleaved sequences of length n
-// (element q of sequence l at q*es + l*ls).  BLOCK = false is one warp on one
-// sequence (lsh = 0, es = 1, ls = 0, 32 threads), so its index arithmetic folds.
-template <int P, int SIGN, bool BLOCK, typename C2>
+// (element q of sequence l at q*es + l*ls).  BLOCK = false is one segment of W lanes on
+// one sequence (lsh = 0, es = 1, ls = 0, W threads; W < 32: the segments of a warp run
+// their own sequences in step), so its index arithmetic folds.
+template <int P, int SIGN, bool BLOCK, typename C2, int W = 32>
 __device__ __forceinline__ void fft_stage(const C2 *__restrict__ a, C2 *__restrict__ b, const C2 *__restrict__ tw,
                                           int n, int Ns, unsigned mg, int tstep, int lsh, int es, int ls, int tid,
                                           int nthr) {
-    if constexpr (!BLOCK) { lsh = 0; es = 1; ls = 0; nthr = 32; }
+    if constexpr (!BLOCK) { lsh = 0; es = 1; ls = 0; nthr = W; }
     const int np = n / P, lmask = (1 << lsh) - 1;
     for (int idx = tid; idx < (np << lsh); idx += nthr) {
         const int l = idx & lmask, jj = idx >> lsh;
@@ -596,7 +597,7 @@ __device__ __forceinline__ void fft_stage(const C2 *__restrict__ a, C2 *__restri
     }
 }
 
-template <typename C2, bool BLOCK, int SIGN>
+template <typename C2, bool BLOCK, int SIGN, int W = 32>
 __device__ __forceinline__ C2 *fft_run(C2 *a, C2 *b, const FftPlan &pl, int lsh, int es, int ls, int tid, int nthr) {
     const int n = pl.n;
     const C2 *tw = twsel<C2>(pl);
@@ -605,9 +606,9 @@ __device__ __forceinline__ C2 *fft_run(C2 *a, C2 *b, const FftPlan &pl, int lsh,
         const int p = pl.rad[s];
         const int tstep = n / (Ns * p);
         const unsigned mg = pl.dmag[s];
-        if (p == 4) fft_stage<4, SIGN, BLOCK>(a, b, tw, n, Ns, mg, tstep, lsh, es, ls, tid, nthr);
-        else if (p == 2) fft_stage<2, SIGN, BLOCK>(a, b, tw, n, Ns, mg, tstep, lsh, es, ls, tid, nthr);
-        else fft_stage<3, SIGN, BLOCK>(a, b, tw, n, Ns, mg, tstep, lsh, es, ls, tid, nthr);
+        if (p == 4) fft_stage<4, SIGN, BLOCK, C2, W>(a, b, tw, n, Ns, mg, tstep, lsh, es, ls, tid, nthr);
+        else if (p == 2) fft_stage<2, SIGN, BLOCK, C2, W>(a, b, tw, n, Ns, mg, tstep, lsh, es, ls, tid, nthr);
+        else fft_stage<3, SIGN, BLOCK, C2, W>(a, b, tw, n, Ns, mg, tstep, lsh, es, ls, tid, nthr);
         if (BLOCK) __syncthreads(); else __syncwarp();
         C2 *t = a;
         a = b;
@@ -618,13 +619,13 @@ __device__ __forceinline__ C2 *fft_run(C2 *a, C2 *b, const FftPlan &pl, int lsh,
 }
 
 // Stockham FFT of 2^lsh sequences of length pl.n at buf[q*es + l*ls]; threads tid..nthr
-// of the warp (BLOCK=false: one sequence, lsh = 0, es = 1, ls = 0) or block (BLOCK=true)
-// cooperate.  Returns the result buffer.
-template <typename C2, bool BLOCK>
+// of a segment of W lanes (BLOCK=false: one sequence, lsh = 0, es = 1, ls = 0) or of the
+// block (BLOCK=true) cooperate.  Returns the result buffer.
+template <typename C2, bool BLOCK, int W = 32>
 __device__ __forceinline__ C2 *fft_smem(C2 *a, C2 *b, const FftPlan &pl, int lsh, int es, int ls, int sign, int tid,
                                         int nthr) {
-    if (sign < 0) return fft_run<C2, BLOCK, -1>(a, b, pl, lsh, es, ls, tid, nthr);
-    return fft_run<C2, BLOCK, +1>(a, b, pl, lsh, es, ls, tid, nthr);
+    if (sign < 0) return fft_run<C2, BLOCK, -1, W>(a, b, pl, lsh, es, ls, tid, nthr);
+    return fft_run<C2, BLOCK, +1, W>(a, b, pl, lsh, es, ls, tid, nthr);
 }
 
 // L2 prefetch of one address (fire and forget)

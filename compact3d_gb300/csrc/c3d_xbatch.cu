@@ -22,17 +22,17 @@ __global__ void __launch_bounds__(XMAXT) kb_xB(const StepArgs<R> *__restrict__ A
     const BMap m = map[blockIdx.x];
     b_xB<R, C, W>(A[m.ch], Blk{m.x, m.y, m.gx});
 }
-template <typename R, int C, bool X4>
+template <typename R, int C, bool X4, int W = 32>
 __global__ void __launch_bounds__(XMAXT) kb_xC(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
     const BMap m = map[blockIdx.x];
     const StepArgs<R> &a = A[m.ch];
-    b_xC<R, C, 0, X4>(a, a.exz, a.eyz, Blk{m.x, m.y, m.gx});
+    b_xC<R, C, 0, X4, W>(a, a.exz, a.eyz, Blk{m.x, m.y, m.gx});
 }
-template <typename R, int C, bool X4>
+template <typename R, int C, bool X4, int W = 32>
 __global__ void __launch_bounds__(XMAXT) kb_xD(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
     const BMap m = map[blockIdx.x];
     const StepArgs<R> &a = A[m.ch];
-    b_xD<R, C, X4>(a, a.exz, a.wsq, Blk{m.x, m.y, m.gx});
+    b_xD<R, C, X4, W>(a, a.exz, a.wsq, Blk{m.x, m.y, m.gx});
 }
 
 template <typename R, int C>
@@ -62,22 +62,30 @@ static int xbk(const c3d_channel *ch, int which, std::vector<BKern> &out) {
     }
 }
 
-// xA and xB of a short row in a segment of W lanes, 32/W rows per warp: chunks of C =
-// N1M/W points instead of N1M/32, so the two cross-lane scans of every line solve take
-// log2(W) steps and are shared by more points (rows of 48-128 points leave 2-4 points per
-// lane of a whole warp).  The rows of a warp share J when N3M is a multiple of 32/W.
+// xA and xB (and xC, xD with the shared-memory row FFT) of a short row in a segment of W
+// lanes, 32/W rows per warp: chunks of C = N1M/W points instead of N1M/32, so the two
+// cross-lane scans of every line solve take log2(W) steps and are shared by more points
+// (rows of 48-128 points leave 2-4 points per lane of a whole warp), and a 24- or
+// 48-point FFT keeps most of its W lanes busy.  The rows of a warp share J when N3M is a
+// multiple of 32/W.
 template <typename R, int C, int W>
 static int xbk_seg(const c3d_channel *ch, int which, std::vector<BKern> &out) {
+    typedef typename Cx<R>::T C2;
     const int nrows = ch->g.n2m * ch->g.n3m, rpb = XW_BATCH * 32 / W;
     const unsigned nb = (unsigned)nblk(nrows, rpb), nt = XW_BATCH * 32;
-    if (which == 0) {
-        out.push_back({(const void *)kb_xA<R, C, 1, W>, nt, 0, nb});
-        out.push_back({(const void *)kb_xA<R, C, 2, W>, nt, 0, nb});
-        out.push_back({(const void *)kb_xA<R, C, 3, W>, nt, 0, nb});
-        return 0;
+    // xC and xD: a stage and the two FFT buffers per row segment
+    const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(ch->g.n1m / 2 + 1) * sizeof(C2)) * rpb;
+    switch (which) {
+        case 0:
+            out.push_back({(const void *)kb_xA<R, C, 1, W>, nt, 0, nb});
+            out.push_back({(const void *)kb_xA<R, C, 2, W>, nt, 0, nb});
+            out.push_back({(const void *)kb_xA<R, C, 3, W>, nt, 0, nb});
+            return 0;
+        case 1: out.push_back({(const void *)kb_xB<R, C, W>, nt, 0, nb}); return 0;
+        case 2: out.push_back({(const void *)kb_xC<R, C, false, W>, nt, fb, nb}); return 0;
+        case 3: out.push_back({(const void *)kb_xD<R, C, false, W>, nt, fb, nb}); return 0;
+        default: return C3D_EINVAL;
     }
-    out.push_back({(const void *)kb_xB<R, C, W>, nt, 0, nb});
-    return 0;
 }
 
 // The row segment of xA and xB for N1M (lanes W, chunk C = N1M/W), or 0 for a whole warp.
@@ -88,7 +96,8 @@ int x_segment_lanes(int n1m, int n3m) {
 
 template <typename R>
 int xpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out) {
-    if ((which == 0 || which == 1) && x_segment_lanes(ch->g.n1m, ch->g.n3m)) {
+    // xC and xD keep the warp's register row FFT where N1M is a multiple of 64
+    if (x_segment_lanes(ch->g.n1m, ch->g.n3m) && (which <= 1 || ch->g.n1m % 64 != 0)) {
         switch (ch->g.n1m) {
             case 48: return xbk_seg<R, 6, 8>(ch, which, out);
             case 64: return xbk_seg<R, 8, 8>(ch, which, out);

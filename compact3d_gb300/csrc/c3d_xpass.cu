@@ -169,16 +169,32 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
 }
 
 
-// xA's pieces (unless staged) and xB with a row per segment of W lanes (schedule knob
-// x_row_lanes); false when the schedule runs them on whole warps.
+// xA's pieces (unless staged), xB, and xC and xD (with the shared-memory row FFT and no
+// bulk-copy ring) with a row per segment of W lanes (schedule knob x_row_lanes); false
+// when the schedule runs the pass on whole warps.
 template <typename R, int C, int W>
-static bool launch_x_seg(c3d_channel *ch, StepArgs<R> &a, int which, int *nl) {
+static bool launch_x_seg(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl) {
+    typedef typename Cx<R>::T C2;
     const Tune &t = ch->tune;
     if (which == 0 && (!t.xsplit || t.xstage)) return false;
+    if ((which == 2 || which == 3) && (t.fxp == 3 || t.xbulk)) return false;
     const int nrows = ch->g.n2m * ch->g.n3m, rpb = t.xw * 32 / W;
     const int grid = nblk(nrows, rpb), nt = t.xw * 32;
     const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
+    const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(ch->g.n1m / 2 + 1) * sizeof(C2)) * rpb;
     cudaStream_t st = ch->stream;
+    if (which == 2) {
+        cudaFuncSetAttribute(k_xC<R, C, 0, false, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
+        k_xC<R, C, 0, false, W><<<grid, nt, fb, st>>>(a, p0, p1);
+        mark(ch, nl, "xC", N * (16 + 4 * Rb));
+        return true;
+    }
+    if (which == 3) {
+        cudaFuncSetAttribute(k_xD<R, C, false, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
+        k_xD<R, C, false, W><<<grid, nt, fb, st>>>(a, p0, p1);
+        mark(ch, nl, "xD", N * 5 * Rb);
+        return true;
+    }
     if (which == 0) {
         k_xA<R, C, 1, W><<<grid, nt, 0, st>>>(a);
         mark(ch, nl, "xA_u", N * (16 + 2 * Rb));
@@ -195,13 +211,13 @@ static bool launch_x_seg(c3d_channel *ch, StepArgs<R> &a, int which, int *nl) {
 
 template <typename R>
 int launch_xpass(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl) {
-    if ((which == 0 || which == 1) && ch->tune.xlanes) {
+    if (which >= 0 && which <= 3 && ch->tune.xlanes) {
         bool done = false;
         switch (ch->g.n1m) {   // the shapes x_segment_lanes accepts
-            case 48: done = launch_x_seg<R, 6, 8>(ch, a, which, nl); break;
-            case 64: done = launch_x_seg<R, 8, 8>(ch, a, which, nl); break;
-            case 96: done = launch_x_seg<R, 12, 8>(ch, a, which, nl); break;
-            case 128: done = launch_x_seg<R, 8, 16>(ch, a, which, nl); break;
+            case 48: done = launch_x_seg<R, 6, 8>(ch, a, which, p0, p1, nl); break;
+            case 64: done = launch_x_seg<R, 8, 8>(ch, a, which, p0, p1, nl); break;
+            case 96: done = launch_x_seg<R, 12, 8>(ch, a, which, p0, p1, nl); break;
+            case 128: done = launch_x_seg<R, 8, 16>(ch, a, which, p0, p1, nl); break;
             default: break;
         }
         if (done) return 0;

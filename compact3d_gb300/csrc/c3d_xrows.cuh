@@ -573,7 +573,7 @@ struct XcStage {
 
 // One row of xC: the x part of div(UH)/DT from U + DH1 (compact (1,22,1) derivative),
 // the y part from V + DH2 on planes J and J+1, plus RDPZ; then the real-to-complex FFT.
-template <bool SH, typename R, int C, bool X4 = false>
+template <bool SH, typename R, int C, bool X4 = false, int W = 32>
 __device__ __forceinline__ void xc_row(const StepArgs<R> &a, int j, int k, const typename SType<R>::S *u,
                                        const R *d0, const typename SType<R>::S *vc, const R *dc,
                                        const typename SType<R>::S *vp, const R *dp, const R *zr,
@@ -581,6 +581,7 @@ __device__ __forceinline__ void xc_row(const StepArgs<R> &a, int j, int k, const
                                        int lane) {
     typedef typename SType<R>::S S;
     typedef typename Cx<R>::T C2;
+    static_assert(W == 32 || !X4, "the register row FFT spans a warp");
     const Geo &g = a.g;
     const int P = g.n1m / C, M = g.n1m / 2;
     S *sbS = reinterpret_cast<S *>(sbuf);
@@ -593,15 +594,15 @@ __device__ __forceinline__ void xc_row(const StepArgs<R> &a, int j, int k, const
         R dd[C];
         xrow<SH>(uc, u, sbS, lane, P);
         xrow<SH>(dd, d0, sbR, lane, P);
-        S nu = snext(uc[0], lane, P);
-        R nd = snext(dd[0], lane, P);
+        S nu = snext<W>(uc[0], lane, P);
+        R nd = snext<W>(dd[0], lane, P);
 #pragma unroll
         for (int t = 0; t < C; ++t) {
             S ru = (t == C - 1) ? nu : uc[t + 1];
             R rd = (t == C - 1) ? nd : dd[t + 1];
             d[t] = f24 * Sten<R>::dd(ru, rd, uc[t], dd[t]);
         }
-        xsolve(d, lane, P, a.c22x);
+        xsolve<W>(d, lane, P, a.c22x);
     }
     {
         const bool up = (j + 1 <= g.n2m), lo = (j >= 2);
@@ -638,8 +639,8 @@ __device__ __forceinline__ void xc_row(const StepArgs<R> &a, int j, int k, const
         for (int t = 0; t < C; ++t) rbuf[lane * C + t] = d[t];
     }
     __syncwarp();
-    C2 *Z = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, -1, lane, 32);
-    for (int kx = lane; kx <= M; kx += 32) {
+    C2 *Z = fft_smem<C2, false, W>(bufa, bufb, a.fx, 0, 1, 0, -1, lane, W);
+    for (int kx = lane; kx <= M; kx += W) {
         C2 zk = Z[kx == M ? 0 : kx], zm = cconj(Z[kx == 0 ? 0 : M - kx]);
         C2 E, O;
         E.x = (R)0.5 * (zk.x + zm.x);
@@ -658,13 +659,14 @@ __device__ __forceinline__ void xc_row(const StepArgs<R> &a, int j, int k, const
 // an NS-stage bulk-copy ring that fetches the rows of its next NS-1 (J, K) while it
 // computes the current one.
 // ---------------------------------------------------------------------------------
-template <typename R, int C, int NS, bool X4 = false>
+template <typename R, int C, int NS, bool X4 = false, int W = 32>
 __device__ __forceinline__ void b_xC(const StepArgs<R> &a, const R *d0, const R *d1, const Blk blk) {
     typedef typename SType<R>::S S;
     typedef typename Cx<R>::T C2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Geo g = a.g;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, wpb = (int)(blockDim.x >> 5);
+    static_assert(W == 32 || NS == 0, "the bulk-copy ring is per warp");
+    const int lane = threadIdx.x & (W - 1), wid = threadIdx.x / W, wpb = (int)blockDim.x / W;
     const int M = g.n1m / 2;
     const int nrows = g.n2m * g.n3m;
     const size_t fbytes = 2 * (size_t)(M + 1) * sizeof(C2);
@@ -677,11 +679,11 @@ __device__ __forceinline__ void b_xC(const StepArgs<R> &a, const R *d0, const R 
             const long long o = fidx(g, 0, j, k), op = fidx(g, 0, j + 1, k);
             {
                 const int rs_ = g.n1m * (int)sizeof(S), rr_ = g.n1m * (int)sizeof(R);
-                pf_row(a.u + o, rs_, lane); pf_row(d0 + o, rr_, lane); pf_row(a.rdpz + o, rr_, lane);
-                if (j >= 2) { pf_row(a.v + o, rs_, lane); pf_row(d1 + o, rr_, lane); }
-                if (j + 1 <= g.n2m) { pf_row(a.v + op, rs_, lane); pf_row(d1 + op, rr_, lane); }
+                pf_row(a.u + o, rs_, lane, W); pf_row(d0 + o, rr_, lane, W); pf_row(a.rdpz + o, rr_, lane, W);
+                if (j >= 2) { pf_row(a.v + o, rs_, lane, W); pf_row(d1 + o, rr_, lane, W); }
+                if (j + 1 <= g.n2m) { pf_row(a.v + op, rs_, lane, W); pf_row(d1 + op, rr_, lane, W); }
             }
-            xc_row<false, R, C, X4>(a, j, k, a.u + o, d0 + o, a.v + o, d1 + o, a.v + op, d1 + op, a.rdpz + o, wb,
+            xc_row<false, R, C, X4, W>(a, j, k, a.u + o, d0 + o, a.v + o, d1 + o, a.v + op, d1 + op, a.rdpz + o, wb,
                                     bufa, bufa + (M + 1), lane);
         }
     } else {
@@ -734,20 +736,21 @@ __device__ __forceinline__ void b_xC(const StepArgs<R> &a, const R *d0, const R 
         }
     }
 }
-template <typename R, int C, int NS, bool X4 = false>
+template <typename R, int C, int NS, bool X4 = false, int W = 32>
 __global__ void __launch_bounds__(XMAXT) k_xC(StepArgs<R> a, const R *d0, const R *d1) {
-    b_xC<R, C, NS, X4>(a, d0, d1, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+    b_xC<R, C, NS, X4, W>(a, d0, d1, Blk{blockIdx.x, blockIdx.y, gridDim.x});
 }
 
 // ---------------------------------------------------------------------------------
 // xD: complex-to-real FFT -> DP, compact dDP/dx, bulk-flow partial sums
 // ---------------------------------------------------------------------------------
-template <typename R, int C, bool X4 = false>
+template <typename R, int C, bool X4 = false, int W = 32>
 __device__ __forceinline__ void b_xD(const StepArgs<R> &a, const R *d0, const R *d2, const Blk blk) {
     typedef typename Cx<R>::T C2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Geo g = a.g;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    static_assert(W == 32 || !X4, "the register row FFT spans a warp");
+    const int lane = threadIdx.x & (W - 1), wid = threadIdx.x / W, rpb = (int)blockDim.x / W;
     const int P = g.n1m / C;
     const int M = g.n1m / 2;
     const size_t sbytes = stage_bytes(g.n1m, C), fbytes = 2 * (size_t)(M + 1) * sizeof(C2);
@@ -760,13 +763,13 @@ __device__ __forceinline__ void b_xD(const StepArgs<R> &a, const R *d0, const R 
     if constexpr (sizeof(R) == 8) twx = reinterpret_cast<const C2 *>(a.twx64);
     else twx = reinterpret_cast<const C2 *>(a.twx32);
     const R scale = a.xscale, f24 = a.f24x;
-    for (int row = blk.x * (int)(blockDim.x >> 5) + wid; row < nrows; row += blk.gx * (int)(blockDim.x >> 5)) {
+    for (int row = blk.x * rpb + wid; row < nrows; row += blk.gx * rpb) {
         const int j = 1 + row / g.n3m, k = row % g.n3m;
         const long long o = fidx(g, 0, j, k);
         const C2 *Sp = reinterpret_cast<const C2 *>(a.spec) + ((long long)(j - 1) * g.n3m + k) * g.n1h;
         {
             const int rr_ = g.n1m * (int)sizeof(R);
-            pf_row(d0 + o, rr_, lane); pf_row(d2 + o, rr_, lane);
+            pf_row(d0 + o, rr_, lane, W); pf_row(d2 + o, rr_, lane, W);
         }
         R dpv[C];
         if constexpr (X4) {   // four-step row FFT in registers
@@ -774,9 +777,9 @@ __device__ __forceinline__ void b_xD(const StepArgs<R> &a, const R *d0, const R 
 #pragma unroll
             for (int t = 0; t < C; ++t) dpv[t] *= scale;
         } else {
-            for (int kx = lane; kx <= M; kx += 32) bufb[kx] = Sp[kx];
+            for (int kx = lane; kx <= M; kx += W) bufb[kx] = Sp[kx];
             __syncwarp();
-            for (int kx = lane; kx < M; kx += 32) {
+            for (int kx = lane; kx < M; kx += W) {
                 C2 xk = bufb[kx], xm = cconj(bufb[M - kx]);
                 C2 E = cadd(xk, xm);
                 C2 O = cmul(csub(xk, xm), cconj(twx[kx]));
@@ -786,7 +789,7 @@ __device__ __forceinline__ void b_xD(const StepArgs<R> &a, const R *d0, const R 
                 bufa[kx] = Z;
             }
             __syncwarp();
-            C2 *Zr = fft_smem<C2, false>(bufa, bufb, a.fx, 0, 1, 0, +1, lane, 32);
+            C2 *Zr = fft_smem<C2, false, W>(bufa, bufb, a.fx, 0, 1, 0, +1, lane, W);
             const R *rz = reinterpret_cast<const R *>(Zr);
             if (lane < P) {
 #pragma unroll
@@ -799,13 +802,13 @@ __device__ __forceinline__ void b_xD(const StepArgs<R> &a, const R *d0, const R 
         }
         srow_store(a.dp + o, dpv, sbR, lane, P);
         R d[C];
-        R pv = sprev(dpv[C - 1], lane, P);
+        R pv = sprev<W>(dpv[C - 1], lane, P);
 #pragma unroll
         for (int t = 0; t < C; ++t) {
             R l = (t == 0) ? pv : dpv[t - 1];
             d[t] = f24 * (dpv[t] - l);
         }
-        xsolve(d, lane, P, a.c22x);
+        xsolve<W>(d, lane, P, a.c22x);
         srow_store(a.g1 + o, d, sbR, lane, P);
         // bulk-flow partial sums: sum_i delta * DY(J)/DX3/DX1 for u and w
         R q1[C], q3[C];
@@ -820,9 +823,9 @@ __device__ __forceinline__ void b_xD(const StepArgs<R> &a, const R *d0, const R 
             }
             double s1 = (double)l1, s3 = (double)l3;
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                s1 += __shfl_down_sync(FULL, s1, off);
-                s3 += __shfl_down_sync(FULL, s3, off);
+            for (int off = W / 2; off > 0; off >>= 1) {
+                s1 += __shfl_down_sync(FULL, s1, off, W);
+                s3 += __shfl_down_sync(FULL, s3, off, W);
             }
             if (lane == 0) {
                 const double wgt = g.dy[j] / g.dx3 / g.dx1;
@@ -840,9 +843,9 @@ __device__ __forceinline__ void b_xD(const StepArgs<R> &a, const R *d0, const R 
                 s3 = St<float>::add(s3, q3[t]);
             }
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                float2 o1 = make_float2(__shfl_down_sync(FULL, s1.x, off), __shfl_down_sync(FULL, s1.y, off));
-                float2 o3 = make_float2(__shfl_down_sync(FULL, s3.x, off), __shfl_down_sync(FULL, s3.y, off));
+            for (int off = W / 2; off > 0; off >>= 1) {
+                float2 o1 = make_float2(__shfl_down_sync(FULL, s1.x, off, W), __shfl_down_sync(FULL, s1.y, off, W));
+                float2 o3 = make_float2(__shfl_down_sync(FULL, s3.x, off, W), __shfl_down_sync(FULL, s3.y, off, W));
                 s1 = df_add(s1, o1);
                 s3 = df_add(s3, o3);
             }
@@ -855,9 +858,9 @@ __device__ __forceinline__ void b_xD(const StepArgs<R> &a, const R *d0, const R 
         }
     }
 }
-template <typename R, int C, bool X4 = false>
+template <typename R, int C, bool X4 = false, int W = 32>
 __global__ void __launch_bounds__(XMAXT) k_xD(StepArgs<R> a, const R *d0, const R *d2) {
-    b_xD<R, C, X4>(a, d0, d2, Blk{blockIdx.x, blockIdx.y, gridDim.x});
+    b_xD<R, C, X4, W>(a, d0, d2, Blk{blockIdx.x, blockIdx.y, gridDim.x});
 }
 
 // ---------------------------------------------------------------------------------

@@ -399,11 +399,13 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
  *       register batches of planes (0), or blocks of 32 or 64 columns whose planes
  *       are staged in shared memory by bulk copies so that each value is read and
  *       written once (falls back to 0 when the tile exceeds shared memory)
- *   [14] lanes per row of the explicit x pieces read from global memory and of the
- *       x pass of the remaining terms: 0 (a warp per row), or the row segment of
- *       short rows, accepted only at N1M = 48, 64, 96 (8 lanes) or 128 (16 lanes)
- *       with N3M a multiple of 32 / lanes, so that each lane holds 6 to 12 points
- *       and the cross-lane scans of the line solves take 3 or 4 steps instead of 5
+ *   [14] lanes per row of the explicit x pieces read from global memory, of the
+ *       x pass of the remaining terms, and of the pressure x passes with the
+ *       shared-memory row FFT ([7] != 3) and no bulk-copy ring ([11] = 0): 0 (a warp
+ *       per row), or the row segment of short rows, accepted only at N1M = 48, 64,
+ *       96 (8 lanes) or 128 (16 lanes) with N3M a multiple of 32 / lanes, so that each
+ *       lane holds 6 to 12 points and the cross-lane scans of the line solves take 3
+ *       or 4 steps instead of 5
  * c3d_autotune  times the candidates on a scratch channel of the same grid holding a
  *               copy of this channel's state (so the channel needs its state), keeps
  *               the fastest per kernel group, applies it, and caches it per grid
