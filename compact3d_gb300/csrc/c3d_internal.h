@@ -291,9 +291,9 @@ int launch_pipe_selftest(c3d_channel *ch, double limit_ms);
 template <typename R> int xpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);
 // Lanes per row segment of the batch xA and xB for a channel of N1M x N3M (0: one row per warp).
 int x_segment_lanes(int n1m, int n3m);
-template <typename R> int zpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);
+template <typename R> int zpass_bkern(const c3d_channel *ch, int which, int seg, std::vector<BKern> &out);
 template <typename R> int spec_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);
-int batch_plan(c3d_channel *ch, std::vector<BKern> &out);
+int batch_plan(c3d_channel *ch, const int *zseg, std::vector<BKern> &out);
 size_t batch_args_size(const c3d_channel *ch);
 void batch_args(c3d_channel *ch, double dt, void *dst);
 int launch_poisson_tables(c3d_channel *ch);

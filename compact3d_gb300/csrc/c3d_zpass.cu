@@ -449,54 +449,65 @@ int zblock_len(int n3m) {
 // points, which divides every supported N3M); zA as its three sweeps; the work arrays
 // are the channel's exz / eyz / wsq as in the step, and zE adds DP to P.
 // ---------------------------------------------------------------------------------
-template <typename R, int PART>
+template <typename R, int PART, int L>
 __global__ void __launch_bounds__(TPB) kb_zA(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
     const BMap m = map[blockIdx.x];
-    b_zA<R, ZL, PART, 0>(A[m.ch], Blk{m.x, m.y, m.gx});
+    b_zA<R, L, PART, 0>(A[m.ch], Blk{m.x, m.y, m.gx});
 }
-template <typename R>
+template <typename R, int L>
 __global__ void __launch_bounds__(TPB) kb_zB(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
     const BMap m = map[blockIdx.x];
-    b_zB<R, ZL, 0>(A[m.ch], Blk{m.x, m.y, m.gx});
+    b_zB<R, L, 0>(A[m.ch], Blk{m.x, m.y, m.gx});
 }
-template <typename R>
+template <typename R, int L>
 __global__ void __launch_bounds__(TPB) kb_zC(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
     const BMap m = map[blockIdx.x];
     const StepArgs<R> &a = A[m.ch];
-    b_zC<R, ZL, 0>(a, a.exz, a.eyz, a.wsq, Blk{m.x, m.y, m.gx});
+    b_zC<R, L, 0>(a, a.exz, a.eyz, a.wsq, Blk{m.x, m.y, m.gx});
 }
-template <typename R>
+template <typename R, int L>
 __global__ void __launch_bounds__(TPB) kb_zD(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
     const BMap m = map[blockIdx.x];
     const StepArgs<R> &a = A[m.ch];
-    b_zD<R, ZL, 0>(a, a.wsq, Blk{m.x, m.y, m.gx});
+    b_zD<R, L, 0>(a, a.wsq, Blk{m.x, m.y, m.gx});
 }
-template <typename R>
+template <typename R, int L>
 __global__ void __launch_bounds__(TPB) kb_zE(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
     const BMap m = map[blockIdx.x];
     const StepArgs<R> &a = A[m.ch];
-    b_zE<R, ZL, 0>(a, a.exz, a.eyz, a.wsq, 1, Blk{m.x, m.y, m.gx});
+    b_zE<R, L, 0>(a, a.exz, a.eyz, a.wsq, 1, Blk{m.x, m.y, m.gx});
 }
 
-template <typename R>
-int zpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out) {
-    if (ch->g.n3m % ZL != 0) return C3D_EINVAL;
-    const unsigned nb = (unsigned)nblk((long long)ch->g.n2m * (ch->g.n3m / ZL) * ch->g.n1m);
+template <typename R, int L>
+static int zbk(const c3d_channel *ch, int which, std::vector<BKern> &out) {
+    const unsigned nb = (unsigned)nblk((long long)ch->g.n2m * (ch->g.n3m / L) * ch->g.n1m);
     switch (which) {
         case 0:
-            out.push_back({(const void *)kb_zA<R, 1>, TPB, 0, nb});
-            out.push_back({(const void *)kb_zA<R, 2>, TPB, 0, nb});
-            out.push_back({(const void *)kb_zA<R, 3>, TPB, 0, nb});
+            out.push_back({(const void *)kb_zA<R, 1, L>, TPB, 0, nb});
+            out.push_back({(const void *)kb_zA<R, 2, L>, TPB, 0, nb});
+            out.push_back({(const void *)kb_zA<R, 3, L>, TPB, 0, nb});
             return 0;
-        case 1: out.push_back({(const void *)kb_zB<R>, TPB, 0, nb}); return 0;
-        case 2: out.push_back({(const void *)kb_zC<R>, TPB, 0, nb}); return 0;
-        case 3: out.push_back({(const void *)kb_zD<R>, TPB, 0, nb}); return 0;
-        case 4: out.push_back({(const void *)kb_zE<R>, TPB, 0, nb}); return 0;
+        case 1: out.push_back({(const void *)kb_zB<R, L>, TPB, 0, nb}); return 0;
+        case 2: out.push_back({(const void *)kb_zC<R, L>, TPB, 0, nb}); return 0;
+        case 3: out.push_back({(const void *)kb_zD<R, L>, TPB, 0, nb}); return 0;
+        case 4: out.push_back({(const void *)kb_zE<R, L>, TPB, 0, nb}); return 0;
         default: return C3D_EINVAL;
     }
 }
-template int zpass_bkern<double>(const c3d_channel *, int, std::vector<BKern> &);
-template int zpass_bkern<float>(const c3d_channel *, int, std::vector<BKern> &);
+
+// z pass `which` of a batch channel in segments of L points (8, 16 or 32; 16 where N3M
+// is not a multiple of L).
+template <typename R>
+int zpass_bkern(const c3d_channel *ch, int which, int L, std::vector<BKern> &out) {
+    if (ch->g.n3m % ZL != 0) return C3D_EINVAL;
+    if (L != 8 && L != 32) L = 16;
+    if (ch->g.n3m % L != 0) L = 16;
+    if (L == 8) return zbk<R, 8>(ch, which, out);
+    if (L == 32) return zbk<R, 32>(ch, which, out);
+    return zbk<R, 16>(ch, which, out);
+}
+template int zpass_bkern<double>(const c3d_channel *, int, int, std::vector<BKern> &);
+template int zpass_bkern<float>(const c3d_channel *, int, int, std::vector<BKern> &);
 
 template <typename R>
 int launch_zpass(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *d1, R *d2, int flag, int *nl) {

@@ -93,6 +93,7 @@ SIGNATURES = {
     "c3d_batch_set_form": (_ip, [_vp, _ip]),
     "c3d_batch_get_form": (_ip, [_vp, ctypes.POINTER(_ip)]),
     "c3d_batch_set_groups": (_ip, [_vp, _ip]),
+    "c3d_batch_set_z_segments": (_ip, [_vp, _vp]),
     "c3d_batch_last_step_stats": (_ip, [_vp, _dp, ctypes.POINTER(_ip)]),
 }
 
@@ -444,6 +445,11 @@ class Batch:
     def set_groups(self, groups: int):
         """Work-list form: the channels in `groups` groups, each on its own stream."""
         check(load().c3d_batch_set_groups(self.h, int(groups)), "c3d_batch_set_groups")
+
+    def set_z_segments(self, seg):
+        """Work-list form: segment length (8, 16 or 32) of the z passes zA..zE."""
+        a = (ctypes.c_int * 5)(*[int(x) for x in seg])
+        check(load().c3d_batch_set_z_segments(self.h, a), "c3d_batch_set_z_segments")
 
     def get_form(self) -> str:
         f = (ctypes.c_int * 1)()

@@ -462,8 +462,11 @@ int c3d_op_get(c3d_channel *ch, double *f);
  *     shape), each block working on the channel a device work list names; a
  *     step is about 20 launches for the whole ensemble.  The work-list form
  *     runs a fixed schedule (x rows per block 2, xA and zA in pieces, z
- *     segments of 16, the four-step z FFT where N3M = 32 N1, else tiles of 8,
- *     register row FFTs where N1M is a multiple of 64), not the channels' own.
+ *     segments of 8, 8, 16, 16, 8 points for zA..zE unless
+ *     c3d_batch_set_z_segments says otherwise, the
+ *     four-step z FFT where N3M = 32 N1, else tiles of 8, register row FFTs
+ *     where N1M is a multiple of 64, rows of 48-128 points in segments of 8 or
+ *     16 lanes as schedule knob [14] describes), not the channels' own.
  *   C3D_BATCH_STREAMS (and any other batch): every channel's step, with its own
  *     schedule, on its own stream; the channels run concurrently.
  * presg/presg3 are in-out arrays of nchan values; the call returns when the
@@ -474,6 +477,9 @@ int c3d_op_get(c3d_channel *ch, double *f);
  * that many groups, largest first and dealt in turn, each with its own work
  * lists on its own stream, so that the passes of one group run beside those of
  * another instead of every pass waiting for the whole ensemble.
+ * c3d_batch_set_z_segments (work-list form) sets the segment length of the z
+ * passes zA, zB, zC, zD, zE (seg[0..4], each 8, 16 or 32; a channel whose N3M is
+ * not a multiple of it runs 16).
  */
 #define C3D_BATCH_STREAMS   0
 #define C3D_BATCH_WORKLIST  1
@@ -486,6 +492,7 @@ int c3d_batch_sync(c3d_batch *b);
 int c3d_batch_set_form(c3d_batch *b, int form);
 int c3d_batch_get_form(c3d_batch *b, int *form);
 int c3d_batch_set_groups(c3d_batch *b, int groups);
+int c3d_batch_set_z_segments(c3d_batch *b, const int *seg);
 /* Device time of the last ensemble step (CUDA events around the graph launch) and the
  * number of kernels one ensemble step runs. */
 int c3d_batch_last_step_stats(c3d_batch *b, double *ms, int *kernel_launches);
