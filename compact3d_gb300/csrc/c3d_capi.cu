@@ -1765,7 +1765,7 @@ struct c3d_batch {
     float last_ms = 0.f;
     int form = C3D_BATCH_WORKLIST;            // requested form (c3d_batch_set_form)
     int groups = 2;                           // work-list form: channel groups on their own streams
-    int zseg[5] = {8, 8, 16, 16, 8};          // work-list form: z segment length of zA..zE
+    BatchSched sched{{8, 8, 16, 16, 8}, 2};  // work-list form: z segments of zA..zE, warps per x block
     // work-list form, per AB2 parity: every channel's StepArgs and the block maps
     void *dargs[2] = {nullptr, nullptr};
     size_t nargs[2] = {0, 0};
@@ -1823,7 +1823,7 @@ static int batch_capture_worklist(c3d_batch *b, const double *dt, int par) {
         c3d_channel *c = b->ch[i];
         c->cur = par;   // GETUP's HH2 <- HH: this step writes buffer par
         batch_args(c, dt[i], args.data() + (size_t)i * asz);
-        int rc = batch_plan(c, b->zseg, plans[i]);
+        int rc = batch_plan(c, b->sched, plans[i]);
         if (rc) return rc;
         if (plans[i].size() != plans[0].size()) { set_error("batch: channels with different pass lists"); return C3D_EINVAL; }
     }
@@ -2098,7 +2098,19 @@ int c3d_batch_set_z_segments(c3d_batch *b, const int *seg) {
         b->exec[p] = nullptr;
         b->gdt[p].clear();
     }
-    for (int q = 0; q < 5; ++q) b->zseg[q] = seg[q];
+    for (int q = 0; q < 5; ++q) b->sched.zseg[q] = seg[q];
+    return 0;
+}
+
+int c3d_batch_set_x_warps(c3d_batch *b, int warps) {
+    if (!b || (warps != 2 && warps != 4 && warps != 8)) { set_error("x warps per block must be 2, 4 or 8"); return C3D_EINVAL; }
+    CK(cudaStreamSynchronize(b->stream));
+    for (int p = 0; p < 2; ++p) {
+        if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
+        b->exec[p] = nullptr;
+        b->gdt[p].clear();
+    }
+    b->sched.xw = warps;
     return 0;
 }
 

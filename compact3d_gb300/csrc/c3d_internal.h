@@ -288,12 +288,18 @@ int launch_pipe_selftest(c3d_channel *ch, double limit_ms);
 // Batch form of the DNS step (FILES = 0; precision C3D_FP64 or C3D_MIXED): the passes of
 // one channel's step in order (batch_plan), and its StepArgs<R> for the step with DT dt
 // written as bytes to dst (batch_args, batch_args_size bytes).
-template <typename R> int xpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);
+template <typename R> int xpass_bkern(const c3d_channel *ch, int which, int xw, std::vector<BKern> &out);
 // Lanes per row segment of the batch xA and xB for a channel of N1M x N3M (0: one row per warp).
 int x_segment_lanes(int n1m, int n3m);
 template <typename R> int zpass_bkern(const c3d_channel *ch, int which, int seg, std::vector<BKern> &out);
 template <typename R> int spec_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);
-int batch_plan(c3d_channel *ch, const int *zseg, std::vector<BKern> &out);
+// Schedule of the work-list form: segment length of the z passes zA..zE and warps per
+// block of the x passes.
+struct BatchSched {
+    int zseg[5];
+    int xw;
+};
+int batch_plan(c3d_channel *ch, const BatchSched &s, std::vector<BKern> &out);
 size_t batch_args_size(const c3d_channel *ch);
 void batch_args(c3d_channel *ch, double dt, void *dst);
 int launch_poisson_tables(c3d_channel *ch);

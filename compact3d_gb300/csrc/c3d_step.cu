@@ -639,32 +639,33 @@ __global__ void __launch_bounds__(RB) kb_reduce2(const StepArgs<R> *__restrict__
 }
 
 template <typename R>
-static int batch_plan_t(c3d_channel *ch, const int *zs, std::vector<BKern> &out) {
+static int batch_plan_t(c3d_channel *ch, const BatchSched &bs, std::vector<BKern> &out) {
+    const int *zs = bs.zseg;
     typedef typename std::conditional<sizeof(R) == 8, AddF64, AddDF>::type Add;
     const Geo &g = ch->g;
     int rc;
     out.push_back({(const void *)kb_bcond<R>, TPB, 0, (unsigned)nblk(g.np)});
-    if ((rc = xpass_bkern<R>(ch, 0, out))) return rc;      // xA (u, v, w)
+    if ((rc = xpass_bkern<R>(ch, 0, bs.xw, out))) return rc;      // xA (u, v, w)
     if ((rc = zpass_bkern<R>(ch, 0, zs[0], out))) return rc;      // zA (u, w and P, v)
     if ((rc = zpass_bkern<R>(ch, 1, zs[1], out))) return rc;      // zB
-    if ((rc = xpass_bkern<R>(ch, 1, out))) return rc;      // xB
+    if ((rc = xpass_bkern<R>(ch, 1, bs.xw, out))) return rc;      // xB
     out.push_back({(const void *)kb_ycn<R>, TPB, 0, (unsigned)nblk(3LL * g.np)});
     if ((rc = zpass_bkern<R>(ch, 2, zs[2], out))) return rc;      // zC
     if ((rc = zpass_bkern<R>(ch, 3, zs[3], out))) return rc;      // zD
-    if ((rc = xpass_bkern<R>(ch, 2, out))) return rc;      // xC
+    if ((rc = xpass_bkern<R>(ch, 2, bs.xw, out))) return rc;      // xC
     if ((rc = spec_bkern<R>(ch, 0, out))) return rc;       // fftz forward
     if ((rc = spec_bkern<R>(ch, 1, out))) return rc;       // Poisson
     if ((rc = spec_bkern<R>(ch, 2, out))) return rc;       // fftz inverse
-    if ((rc = xpass_bkern<R>(ch, 3, out))) return rc;      // xD
+    if ((rc = xpass_bkern<R>(ch, 3, bs.xw, out))) return rc;      // xD
     out.push_back({(const void *)kb_reduce1<R, Add>, 256, 0, (unsigned)RB});
     out.push_back({(const void *)kb_reduce2<R, Add>, RB, 0, 1u});
     return zpass_bkern<R>(ch, 4, zs[4], out);              // zE
 }
 
-int batch_plan(c3d_channel *ch, const int *zseg, std::vector<BKern> &out) {
+int batch_plan(c3d_channel *ch, const BatchSched &s, std::vector<BKern> &out) {
     if (ch->files != 0 || ch->refine) { set_error("the batch form runs DNS channels without refinement"); return C3D_EINVAL; }
-    if (ch->precision == C3D_MIXED) return batch_plan_t<float>(ch, zseg, out);
-    return batch_plan_t<double>(ch, zseg, out);
+    if (ch->precision == C3D_MIXED) return batch_plan_t<float>(ch, s, out);
+    return batch_plan_t<double>(ch, s, out);
 }
 
 size_t batch_args_size(const c3d_channel *ch) {

@@ -6,11 +6,10 @@
 namespace c3d {
 // ---------------------------------------------------------------------------------
 // Batch form: one launch per pass covers the channels whose x rows split into the same
-// lane chunk C (and, for xC and xD, the same row-FFT form).  Rows per block XW_BATCH; xA
+// lane chunk C (and, for xC and xD, the same row-FFT form).  xw warps per block; xA
 // as its u, v and w pieces with rows read from global memory.  The work arrays of the
 // pressure passes are the channel's exz / eyz / wsq, as in the step.
 // ---------------------------------------------------------------------------------
-constexpr int XW_BATCH = 2;
 
 template <typename R, int C, int PART, int W = 32>
 __global__ void __launch_bounds__(XMAXT) kb_xA(const StepArgs<R> *__restrict__ A, const BMap *__restrict__ map) {
@@ -36,12 +35,12 @@ __global__ void __launch_bounds__(XMAXT) kb_xD(const StepArgs<R> *__restrict__ A
 }
 
 template <typename R, int C>
-static int xbk(const c3d_channel *ch, int which, std::vector<BKern> &out) {
+static int xbk(const c3d_channel *ch, int which, int xw, std::vector<BKern> &out) {
     typedef typename Cx<R>::T C2;
     const int nrows = ch->g.n2m * ch->g.n3m;
-    const unsigned nb = (unsigned)nblk(nrows, XW_BATCH), nt = XW_BATCH * 32;
-    const size_t sb = stage_bytes(ch->g.n1m, C) * XW_BATCH;
-    const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(ch->g.n1m / 2 + 1) * sizeof(C2)) * XW_BATCH;
+    const unsigned nb = (unsigned)nblk(nrows, xw), nt = xw * 32;
+    const size_t sb = stage_bytes(ch->g.n1m, C) * xw;
+    const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(ch->g.n1m / 2 + 1) * sizeof(C2)) * xw;
     const bool x4 = (C % 2 == 0) && ch->g.n1m == 32 * C;   // register row FFT (see launch_x_c)
     switch (which) {
         case 0:
@@ -69,10 +68,10 @@ static int xbk(const c3d_channel *ch, int which, std::vector<BKern> &out) {
 // 48-point FFT keeps most of its W lanes busy.  The rows of a warp share J when N3M is a
 // multiple of 32/W.
 template <typename R, int C, int W>
-static int xbk_seg(const c3d_channel *ch, int which, std::vector<BKern> &out) {
+static int xbk_seg(const c3d_channel *ch, int which, int xw, std::vector<BKern> &out) {
     typedef typename Cx<R>::T C2;
-    const int nrows = ch->g.n2m * ch->g.n3m, rpb = XW_BATCH * 32 / W;
-    const unsigned nb = (unsigned)nblk(nrows, rpb), nt = XW_BATCH * 32;
+    const int nrows = ch->g.n2m * ch->g.n3m, rpb = xw * 32 / W;
+    const unsigned nb = (unsigned)nblk(nrows, rpb), nt = xw * 32;
     // xC and xD: a stage and the two FFT buffers per row segment
     const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(ch->g.n1m / 2 + 1) * sizeof(C2)) * rpb;
     switch (which) {
@@ -95,29 +94,29 @@ int x_segment_lanes(int n1m, int n3m) {
 }
 
 template <typename R>
-int xpass_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out) {
+int xpass_bkern(const c3d_channel *ch, int which, int xw, std::vector<BKern> &out) {
     // xC and xD keep the warp's register row FFT where N1M is a multiple of 64
     if (x_segment_lanes(ch->g.n1m, ch->g.n3m) && (which <= 1 || ch->g.n1m % 64 != 0)) {
         switch (ch->g.n1m) {
-            case 48: return xbk_seg<R, 6, 8>(ch, which, out);
-            case 64: return xbk_seg<R, 8, 8>(ch, which, out);
-            case 96: return xbk_seg<R, 12, 8>(ch, which, out);
-            case 128: return xbk_seg<R, 8, 16>(ch, which, out);
+            case 48: return xbk_seg<R, 6, 8>(ch, which, xw, out);
+            case 64: return xbk_seg<R, 8, 8>(ch, which, xw, out);
+            case 96: return xbk_seg<R, 12, 8>(ch, which, xw, out);
+            case 128: return xbk_seg<R, 8, 16>(ch, which, xw, out);
             default: break;
         }
     }
     switch ((ch->g.n1m + 31) / 32) {
-        case 1: return xbk<R, 1>(ch, which, out);
-        case 2: return xbk<R, 2>(ch, which, out);
-        case 3: return xbk<R, 3>(ch, which, out);
-        case 4: return xbk<R, 4>(ch, which, out);
-        case 6: return xbk<R, 6>(ch, which, out);
-        case 8: return xbk<R, 8>(ch, which, out);
-        case 12: return xbk<R, 12>(ch, which, out);
+        case 1: return xbk<R, 1>(ch, which, xw, out);
+        case 2: return xbk<R, 2>(ch, which, xw, out);
+        case 3: return xbk<R, 3>(ch, which, xw, out);
+        case 4: return xbk<R, 4>(ch, which, xw, out);
+        case 6: return xbk<R, 6>(ch, which, xw, out);
+        case 8: return xbk<R, 8>(ch, which, xw, out);
+        case 12: return xbk<R, 12>(ch, which, xw, out);
         default: return C3D_EINVAL;
     }
 }
-template int xpass_bkern<double>(const c3d_channel *, int, std::vector<BKern> &);
-template int xpass_bkern<float>(const c3d_channel *, int, std::vector<BKern> &);
+template int xpass_bkern<double>(const c3d_channel *, int, int, std::vector<BKern> &);
+template int xpass_bkern<float>(const c3d_channel *, int, int, std::vector<BKern> &);
 
 }  // namespace c3d

@@ -94,6 +94,7 @@ SIGNATURES = {
     "c3d_batch_get_form": (_ip, [_vp, ctypes.POINTER(_ip)]),
     "c3d_batch_set_groups": (_ip, [_vp, _ip]),
     "c3d_batch_set_z_segments": (_ip, [_vp, _vp]),
+    "c3d_batch_set_x_warps": (_ip, [_vp, _ip]),
     "c3d_batch_last_step_stats": (_ip, [_vp, _dp, ctypes.POINTER(_ip)]),
 }
 
@@ -450,6 +451,10 @@ class Batch:
         """Work-list form: segment length (8, 16 or 32) of the z passes zA..zE."""
         a = (ctypes.c_int * 5)(*[int(x) for x in seg])
         check(load().c3d_batch_set_z_segments(self.h, a), "c3d_batch_set_z_segments")
+
+    def set_x_warps(self, warps: int):
+        """Work-list form: warps per block of the x passes (2, 4 or 8)."""
+        check(load().c3d_batch_set_x_warps(self.h, int(warps)), "c3d_batch_set_x_warps")
 
     def get_form(self) -> str:
         f = (ctypes.c_int * 1)()

@@ -479,7 +479,8 @@ int c3d_op_get(c3d_channel *ch, double *f);
  * another instead of every pass waiting for the whole ensemble.
  * c3d_batch_set_z_segments (work-list form) sets the segment length of the z
  * passes zA, zB, zC, zD, zE (seg[0..4], each 8, 16 or 32; a channel whose N3M is
- * not a multiple of it runs 16).
+ * not a multiple of it runs 16).  c3d_batch_set_x_warps (work-list form) sets
+ * the warps per block of the x passes (2, 4 or 8; default 2).
  */
 #define C3D_BATCH_STREAMS   0
 #define C3D_BATCH_WORKLIST  1
@@ -493,6 +494,7 @@ int c3d_batch_set_form(c3d_batch *b, int form);
 int c3d_batch_get_form(c3d_batch *b, int *form);
 int c3d_batch_set_groups(c3d_batch *b, int groups);
 int c3d_batch_set_z_segments(c3d_batch *b, const int *seg);
+int c3d_batch_set_x_warps(c3d_batch *b, int warps);
 /* Device time of the last ensemble step (CUDA events around the graph launch) and the
  * number of kernels one ensemble step runs. */
 int c3d_batch_last_step_stats(c3d_batch *b, double *ms, int *kernel_launches);

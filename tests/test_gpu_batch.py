@@ -129,11 +129,11 @@ def row_lanes(g):
 WORKLIST_Z = (8, 8, 16, 16, 8)   # default z segment lengths of zA..zE in the work-list form
 
 
-def worklist_schedule(ch, g, zseg=WORKLIST_Z):
+def worklist_schedule(ch, g, zseg=WORKLIST_Z, xw=2):
     """The fixed schedule of the work-list form (include/c3d.h) on a single channel."""
     s = ch.get_schedule()
     s.update({f"z_segment_z{c}": (L if g.n3m % L == 0 else 16) for c, L in zip("ABCDE", zseg)})
-    s.update(x_rows_per_block=2, fft_z_tile=0, fft_x_plan=3 if g.n1m % 64 == 0 else 0, fft_z_plan=0,
+    s.update(x_rows_per_block=xw, fft_z_tile=0, fft_x_plan=3 if g.n1m % 64 == 0 else 0, fft_z_plan=0,
              z_split_zA=1, x_split_xA=1, x_bulk_stages=0, x_stage_xA=0, x_row_lanes=row_lanes(g))
     ch.set_schedule(s)
 
@@ -149,9 +149,9 @@ def dns_ensemble(prec, seed0=0):
     return out
 
 
-@pytest.mark.parametrize("prec,zseg", [(C3D_MIXED, WORKLIST_Z), (C3D_FP64, WORKLIST_Z),
-                                       (C3D_FP64, (32, 16, 8, 32, 16))])
-def test_worklist_batch_matches_single_channels(L, prec, zseg):
+@pytest.mark.parametrize("prec,zseg,xw", [(C3D_MIXED, WORKLIST_Z, 2), (C3D_FP64, WORKLIST_Z, 2),
+                                          (C3D_FP64, (32, 16, 8, 32, 16), 8)])
+def test_worklist_batch_matches_single_channels(L, prec, zseg, xw):
     """One launch per pass over all channels (the work-list form) computes, for every
     channel, the step of that channel alone under the same schedule.  The batch kernels
     are other compiled instances of the same kernel bodies, whose multiply-add
@@ -163,6 +163,8 @@ def test_worklist_batch_matches_single_channels(L, prec, zseg):
     assert b.get_form() == "worklist"
     if zseg != WORKLIST_Z:   # segment lengths a channel cannot take (32 on N3M = 48) run 16
         b.set_z_segments(zseg)
+    if xw != 2:
+        b.set_x_warps(xw)
     singles = []
     for (g, dt, (U, P, HH)), ch in zip(ens, b.channels):
         ch.upload(U, P, HH)
@@ -170,7 +172,7 @@ def test_worklist_batch_matches_single_channels(L, prec, zseg):
         s = L.Channel(g)
         s.upload(U, P, HH)
         s.project()
-        worklist_schedule(s, g, zseg)
+        worklist_schedule(s, g, zseg, xw)
         singles.append(s)
     dts = [dt for _, dt, _ in ens]
     pb, pb3 = [0.0] * len(ens), [0.0] * len(ens)
@@ -233,4 +235,6 @@ def test_mixed_precision_batch_runs_streams_form(L):
     assert b.get_form() == "worklist"
     with pytest.raises(L.C3DError):
         b.set_z_segments([12, 16, 16, 16, 16])
+    with pytest.raises(L.C3DError):
+        b.set_x_warps(3)
     b.close()
