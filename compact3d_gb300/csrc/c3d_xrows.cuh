@@ -378,8 +378,11 @@ __device__ __forceinline__ void b_xA(const StepArgs<R> &a, const Blk blk) {
         }
     }
 }
+// At least 3 blocks of XMAXT threads per SM: at most 80 registers, so more rows are in
+// flight (the pieces are latency-bound; measured on 384-point rows: 0.742 -> 0.705 ms for
+// the three pieces, with a few dozen bytes of spills).
 template <typename R, int C, int PART, int W = 32>
-__global__ void __launch_bounds__(XMAXT) k_xA(StepArgs<R> a) {
+__global__ void __launch_bounds__(XMAXT, 3) k_xA(StepArgs<R> a) {
     b_xA<R, C, PART, W>(a, Blk{blockIdx.x, blockIdx.y, gridDim.x});
 }
 

@@ -197,6 +197,9 @@ __device__ __forceinline__ void b_zA(const StepArgs<R> &a, const Blk blk) {
         if ((PART == 0 || PART == 3) && j >= 2) {
             pf_cols(a.v + o0, sb * sizeof(S), ss, k0, zmargin<MODE>(M6), L, n, lane);
             pf_cols(a.r[1] + o0, sb * sizeof(R), sr, k0, 0, L, n, lane);
+            // w at the y face: planes J and J-1 of the segment, read after the solve
+            if (PART == 3) pf_cols(a.w + o0, sb * sizeof(S), ss, k0, 0, L, n, lane);
+            pf_cols(a.w + fidx(g, i - lane, j - 1, 0), sb * sizeof(S), ss, k0, 0, L, n, lane);
         }
     }
     if (PART == 0 || PART == 1) {   // u: R1 += (1/RE) d2u/dz2 ; E_xz = UU3 * WW1
