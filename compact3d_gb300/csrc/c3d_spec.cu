@@ -77,7 +77,6 @@ __device__ __forceinline__ void b_fftz4(const StepArgs<R> &a, const Blk blk) {
         ts[st] = twd((lane & (h - 1)) * (n / (2 * h)));
     }
     __syncthreads();
-    const int rl = __brev((unsigned)lane) >> 27;   // bitrev5(lane)
     for (int c = wid; c < w; c += FZW) {
         C2 x[N1];
 #pragma unroll
@@ -98,13 +97,18 @@ __device__ __forceinline__ void b_fftz4(const StepArgs<R> &a, const Blk blk) {
             }
         }
         __syncwarp();
+        // x[k] is frequency k + N1 * bitrev5(lane); it goes to tile row lane + 32 k, so that
+        // the 16 lanes of a half-warp write 16 distinct bank pairs (row k + N1 bitrev5(lane)
+        // would put them on 4), and the copy-out below reads each frequency's row.
 #pragma unroll
-        for (int k = 0; k < N1; ++k) T[(k + N1 * rl) * pitch + c] = x[k];
+        for (int k = 0; k < N1; ++k) T[(lane + 32 * k) * pitch + c] = x[k];
     }
     __syncthreads();
     for (int e = threadIdx.x; e < n * TWW; e += FZW * 32) {
         const int q = e >> 4, l = e & (TWW - 1);
-        if (l < w) S[q * g.n1h + l] = T[q * pitch + l];
+        const int lq = q / N1, kq = q - lq * N1;
+        const int row = (int)(__brev((unsigned)lq) >> 27) + 32 * kq;
+        if (l < w) S[q * g.n1h + l] = T[row * pitch + l];
     }
 }
 template <typename R, int N1, int SIGN>
