@@ -126,12 +126,94 @@ __device__ __forceinline__ dfl shfl_idx(dfl v, int s, int w = 32) {
     return dfl(__shfl_sync(FULL, v.h, s, w), __shfl_sync(FULL, v.l, s, w));
 }
 
+// 1 - x rounds to 1 (so that y / (1 - x) is y exactly) for |x| below half an ulp of 1.
+__device__ __forceinline__ bool below_half_ulp(float x) { return fabsf(x) < 0x1p-25f; }
+__device__ __forceinline__ bool below_half_ulp(double x) { return fabs(x) < 0x1p-54; }
+template <typename R>
+__device__ __forceinline__ bool below_half_ulp(R) { return false; }
+
+// xsolve for a row whose every lane holds a chunk (P = W): every lane's chunk multiplier is
+// r^C, so the scans combine with the constant powers r^(C 2^b) (one shuffle and one
+// multiply-add per level), the chunk sweeps carry no multiplier, and the cyclic closure
+// y / (1 - r^(C W)) needs no division once r^(C W) is below half an ulp.  The powers are
+// formed with the same products, in the same order, as the general form forms its
+// multipliers at each level.
+template <int W, typename R, int C>
+__device__ __forceinline__ void xsolve_full(R (&x)[C], int lane, const Cyc<R> &c) {
+    constexpr int LW = W == 32 ? 5 : W == 16 ? 4 : W == 8 ? 3 : 2;
+    const R r = c.r;
+    R pw[LW + 1];
+    {
+        R m = R(1);
+#pragma unroll
+        for (int t = 0; t < C; ++t) m *= r;
+        pw[0] = m;
+#pragma unroll
+        for (int b = 0; b < LW; ++b) pw[b + 1] = pw[b] * pw[b];
+    }
+    R ml = R(1), mr = R(1);   // r^(C lane) and r^(C (W - 1 - lane))
+#pragma unroll
+    for (int b = 0; b < LW; ++b) {
+        if ((lane >> b) & 1) ml = ml * pw[b];
+        if (((W - 1 - lane) >> b) & 1) mr = mr * pw[b];
+    }
+    const bool exact1 = below_half_ulp(pw[LW]);
+    R y = R(0);
+#pragma unroll
+    for (int t = 0; t < C; ++t) y = x[t] + r * y;
+    R e = y;
+#pragma unroll
+    for (int b = 0; b < LW; ++b) {
+        const int off = 1 << b;
+        const R ep = shfl_up(e, off, W);
+        if (lane >= off) e = e + pw[b] * ep;
+    }
+    {
+        const R et = shfl_idx(e, W - 1, W);
+        const R y0 = exact1 ? et : et / (R(1) - pw[LW]);
+        const R ex = shfl_up(e, 1, W);
+        y = (lane == 0) ? y0 : ex + ml * y0;
+    }
+#pragma unroll
+    for (int t = 0; t < C; ++t) {
+        y = x[t] + r * y;
+        x[t] = y;
+    }
+    R z = R(0);
+#pragma unroll
+    for (int t = C - 1; t >= 0; --t) z = x[t] + r * z;
+    e = z;
+#pragma unroll
+    for (int b = 0; b < LW; ++b) {
+        const int off = 1 << b;
+        const R en = shfl_down(e, off, W);
+        if (lane + off < W) e = e + pw[b] * en;
+    }
+    {
+        const R e0 = shfl_idx(e, 0, W);
+        const R z0 = exact1 ? e0 : e0 / (R(1) - pw[LW]);
+        const R en1 = shfl_down(e, 1, W);
+        z = (lane == W - 1) ? z0 : en1 + mr * z0;
+    }
+    const R s = c.s;
+#pragma unroll
+    for (int t = C - 1; t >= 0; --t) {
+        z = x[t] + r * z;
+        x[t] = s * z;
+    }
+}
+
 // Cyclic solve on a row held as lane chunks x[0..C) by a segment of W lanes (lane =
 // the lane within the segment; W = 32: one row per warp, W < 32: 32/W rows per warp,
-// every segment of the warp calling together); in place, returns s*B(F(x)).
+// every segment of the warp calling together); in place, returns s*B(F(x)).  P = W takes
+// the constant-multiplier form above; P < W (idle lanes) the general one.
 template <int W = 32, typename R, int C>
 __device__ __forceinline__ void xsolve(R (&x)[C], int lane, int P, const Cyc<R> &c) {
     static_assert(W == 4 || W == 8 || W == 16 || W == 32, "row segments of 4, 8, 16 or 32 lanes");
+    if (P == W) {
+        xsolve_full<W>(x, lane, c);
+        return;
+    }
     const bool act = lane < P;
     const R r = c.r;
     R y = R(0), m = R(1);
