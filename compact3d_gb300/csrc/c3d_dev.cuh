@@ -13,8 +13,9 @@
 //   tridiag(a, b, a) = (-a/r) (1 - r S)(1 - r S^-1)      (S = cyclic shift)
 // so x = s * B(F(d)) with s = -r/a, F: y_i = d_i + r y_{i-1} and B: z_i = y_i + r z_{i+1},
 // both cyclic.  The kernels evaluate these two first-order recurrences:
-//   * along x (contiguous rows): one warp per row, every lane owns C consecutive points,
-//     and the cyclic carries between lanes come from warp-shuffle scans of affine maps;
+//   * along x (contiguous rows): one warp per row (or, for rows of 48-128 points, a
+//     segment of 8 or 16 lanes per row), every lane owns C consecutive points, and the
+//     cyclic carries between lanes come from shuffle scans of affine maps;
 //   * along z (strided columns): one thread per (column, segment of L points); the cyclic
 //     start values come from a warm-up of M points, M chosen so |r|^M is below the
 //     working precision's rounding unit.
@@ -52,7 +53,8 @@ __host__ __device__ inline long long fidx(const Geo &g, int i, int j, int k) {
 }
 
 // ---------------------------------------------------------------------------------
-// x direction: warp per row, lane chunks of C points, P = N1M / C active lanes.
+// x direction: warp per row, lane chunks of C points, P = N1M / C active lanes (the
+// lane_* helpers; the kernels' segmented forms use sprev/snext/xsolve with a width).
 // ---------------------------------------------------------------------------------
 template <typename T>
 __device__ __forceinline__ T lane_prev(T last, int lane, int P) {
