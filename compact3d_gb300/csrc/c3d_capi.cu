@@ -21,6 +21,22 @@ static thread_local std::string g_last_error;
 static thread_local int g_device = -1;
 void set_error(const std::string &msg) { g_last_error = msg; }
 
+bool par_on(const c3d_channel *ch) { return ch->tune.conc && !ch->prof_on; }
+
+int par_fork(c3d_channel *ch) {
+    CK_RC(cudaEventRecord(ch->pev[0], ch->stream));
+    for (int q = 0; q < 2; ++q) CK_RC(cudaStreamWaitEvent(ch->par[q], ch->pev[0], 0));
+    return 0;
+}
+
+int par_join(c3d_channel *ch) {
+    for (int q = 0; q < 2; ++q) {
+        CK_RC(cudaEventRecord(ch->pev[1 + q], ch->par[q]));
+        CK_RC(cudaStreamWaitEvent(ch->stream, ch->pev[1 + q], 0));
+    }
+    return 0;
+}
+
 void mark(c3d_channel *ch, int *nl, const char *name, double bytes) {
     (*nl)++;
     if (!ch->prof_on) return;
@@ -191,6 +207,10 @@ void free_channel(c3d_channel *ch) {
     if (ch->tm0) cudaEventDestroy(ch->tm0);
     if (ch->tm1) cudaEventDestroy(ch->tm1);
     if (ch->stream) cudaStreamDestroy(ch->stream);
+    for (cudaStream_t q : ch->par)
+        if (q) cudaStreamDestroy(q);
+    for (cudaEvent_t e : ch->pev)
+        if (e) cudaEventDestroy(e);
     if (ch->side) cudaStreamDestroy(ch->side);
     if (ch->cs) cudaStreamDestroy(ch->cs);
     for (cudaEvent_t e : ch->xev)
@@ -445,6 +465,10 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
         return code;
     };
     if (cudaStreamCreateWithFlags(&ch->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(C3D_ECUDA);
+    for (int q = 0; q < 2; ++q)
+        if (cudaStreamCreateWithFlags(&ch->par[q], cudaStreamNonBlocking) != cudaSuccess) return fail(C3D_ECUDA);
+    for (int q = 0; q < 3; ++q)
+        if (cudaEventCreateWithFlags(&ch->pev[q], cudaEventDisableTiming) != cudaSuccess) return fail(C3D_ECUDA);
     if (cudaEventCreate(&ch->ev0) != cudaSuccess || cudaEventCreate(&ch->ev1) != cudaSuccess ||
         cudaEventCreate(&ch->tm0) != cudaSuccess || cudaEventCreate(&ch->tm1) != cudaSuccess)
         return fail(C3D_ECUDA);
@@ -641,7 +665,7 @@ int c3d_create(const c3d_grid *gr, c3d_channel **out) {
     rc = launch_poisson_tables(ch);
     if (rc) return fail(rc);
     // FFT plans and twiddles: [x: N1M/2][z: N3M][x post-processing: N1M/2+1]
-    ch->tune = Tune{{16, 16, 16, 16, 16}, 4, 8, 0, 0, 0, 0, 0, 0, 0, 0};
+    ch->tune = Tune{{16, 16, 16, 16, 16}, 4, 8, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     ch->fx = make_plan(g.n1m / 2, 0);
     ch->fz = make_plan(g.n3m, 0);
     if (ch->fx.nst < 0 || ch->fz.nst < 0) { set_error("FFT plan index arithmetic"); return fail(C3D_EINVAL); }
@@ -1597,7 +1621,7 @@ bool tune_ok(const c3d_channel *ch, const Tune &t) {
     return zl && xw && tw && fx && t.fzp >= 0 && t.fzp <= 2 && (t.zsplit == 0 || t.zsplit == 1) &&
            (t.xsplit == 0 || t.xsplit == 1) && (t.xbulk == 0 || t.xbulk == 2 || t.xbulk == 3) &&
            (t.xstage == 0 || (t.xstage == 1 && ch->g.n1m % 2 == 0)) && (t.ycn == 0 || t.ycn == 32 || t.ycn == 64) &&
-           (t.xlanes == 0 || t.xlanes == x_segment_lanes(ch->g.n1m, ch->g.n3m));
+           (t.xlanes == 0 || t.xlanes == x_segment_lanes(ch->g.n1m, ch->g.n3m)) && (t.conc == 0 || t.conc == 1);
 }
 
 // Sets the schedule; the FFT plans get the new radix order and keep their twiddle tables.
@@ -1642,13 +1666,14 @@ int c3d_get_schedule(c3d_channel *ch, int *sched) {
     sched[12] = t.xstage;
     sched[13] = t.ycn;
     sched[14] = t.xlanes;
+    sched[15] = t.conc;
     return 0;
 }
 
 int c3d_set_schedule(c3d_channel *ch, const int *sched) {
     if (!ch || !sched) { set_error("null argument"); return C3D_EINVAL; }
     Tune t{{sched[0], sched[1], sched[2], sched[3], sched[4]}, sched[5], sched[6], sched[7], sched[8], sched[9],
-           sched[10], sched[11], sched[12], sched[13], sched[14]};
+           sched[10], sched[11], sched[12], sched[13], sched[14], sched[15]};
     if (!tune_ok(ch, t)) { set_error("invalid schedule"); return C3D_EINVAL; }
     apply_tune(ch, t);
     return 0;
@@ -1701,7 +1726,8 @@ int c3d_autotune(c3d_channel *ch, int *sched) {
     };
     auto knob = [](Tune &t, int q) -> int & {
         return q < 5 ? t.zl[q] : q == 5 ? t.xw : q == 6 ? t.twz : q == 7 ? t.fxp : q == 8 ? t.fzp : q == 9 ? t.zsplit
-             : q == 10 ? t.xsplit : q == 11 ? t.xbulk : q == 12 ? t.xstage : q == 13 ? t.ycn : t.xlanes;
+             : q == 10 ? t.xsplit : q == 11 ? t.xbulk : q == 12 ? t.xstage : q == 13 ? t.ycn : q == 14 ? t.xlanes
+             : t.conc;
     };
     Tune best = ch->tune;
     for (const Group &gp : groups) {
@@ -1717,6 +1743,29 @@ int c3d_autotune(c3d_channel *ch, int *sched) {
             if (cost < bcost) { bcost = cost; bval = v; }
         }
         knob(best, gp.knob) = bval;
+    }
+    // knob 15 by whole-step time: the per-kernel profile runs the pieces one after another,
+    // so the concurrent form is judged on five unprofiled steps (twice each, the minimum)
+    if (best.xsplit || best.zsplit) {
+        float bms[2] = {1e30f, 1e30f};
+        for (int rep = 0; rep < 2; ++rep)
+            for (int v = 0; v < 2; ++v) {
+                Tune t = best;
+                t.conc = v;
+                apply_tune(sc, t);
+                rc = step_common(sc, dt, nullptr, nullptr, true);
+                if (rc && rc != C3D_ENOTCONV) { c3d_destroy(sc); return rc; }
+                rc = 0;
+                CK(cudaEventRecord(sc->tm0, sc->stream));
+                for (int q = 0; q < 5 && !rc; ++q) rc = step_common(sc, dt, nullptr, nullptr, false);
+                if (rc) { c3d_destroy(sc); return rc; }
+                CK(cudaEventRecord(sc->tm1, sc->stream));
+                CK(cudaEventSynchronize(sc->tm1));
+                float ms = 0.f;
+                CK(cudaEventElapsedTime(&ms, sc->tm0, sc->tm1));
+                bms[v] = std::min(bms[v], ms);
+            }
+        best.conc = bms[1] < bms[0] ? 1 : 0;
     }
     c3d_destroy(sc);
     apply_tune(ch, best);

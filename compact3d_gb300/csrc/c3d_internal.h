@@ -127,6 +127,7 @@ struct Tune {
     int xstage;   // xA's pieces read their rows from global memory (0) or stage them in shared memory by bulk copies (1)
     int ycn;      // wall-normal CN factor: one thread per column (0) or shared-memory tiles of 32 or 64 columns
     int xlanes;   // x passes (xA pieces from global memory, xB, xC/xD with the shared-memory FFT) with a row per segment of this many lanes (0: a warp)
+    int conc;     // xA's pieces, then zA's pieces, on three streams at once (1) or one after another (0)
 };
 
 // Arguments of the pressure refinement (mixed form with C3D_MIXED_IR): double-float
@@ -175,6 +176,10 @@ struct c3d_channel {
     cudaStream_t side = nullptr;
     cudaEvent_t hh_in = nullptr, hh_out = nullptr;
     bool hh_hooks = false;
+    // concurrent pieces (schedule knob 15): two more streams for the u and v pieces of xA
+    // and zA, a fork event and their two join events
+    cudaStream_t par[2] = {nullptr, nullptr};
+    cudaEvent_t pev[3] = {nullptr, nullptr, nullptr};
     double *xfer = nullptr;   // DMA staging area of pinned host arrays (one slot per field)
     double *wtaue = nullptr;  // WALLMODEL_WERNER: TAUWE(I,K,1..4) at the cell centres (4 x N1M N3M)
     // MARUSIC1 / PIOMELLI: Y(0:N2), YC(0:N2), per-wall constants and YP heights; the
@@ -317,6 +322,13 @@ int launch_repack(c3d_channel *ch, int dir, int what, int comp, double *fort = n
 void set_error(const std::string &msg);
 // Records a kernel-boundary mark for the profiler and counts the launch.
 void mark(c3d_channel *ch, int *nl, const char *name, double bytes);
+// The three pieces of xA or zA as concurrent branches: par_fork makes the two extra streams
+// wait for the work so far on the channel's stream, par_join makes the channel's stream
+// wait for both.  par_on says whether the pieces run concurrently (knob 15, not while the
+// per-kernel profile is on, whose events are recorded on the channel's stream).
+bool par_on(const c3d_channel *ch);
+int par_fork(c3d_channel *ch);
+int par_join(c3d_channel *ch);
 // returns C3D_ECUDA with the failing call named when a CUDA runtime call fails
 #define CK_RC(call)                                                                     \
     do {                                                                                \

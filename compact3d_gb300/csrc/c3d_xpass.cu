@@ -75,6 +75,7 @@ static bool launch_xc_bulk(c3d_channel *ch, StepArgs<R> &a, int xw, const R *p0,
 template <typename R, int C>
 static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl) {
     typedef typename Cx<R>::T C2;
+    int rc = 0;
     const int nrows = ch->g.n2m * ch->g.n3m;
     const int xw = (which == 4) ? TPB / 32 : ch->tune.xw;   // rows (warps) per block
     const int grid = nblk(nrows, xw), nt = xw * 32;
@@ -93,24 +94,30 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
                 cudaFuncSetAttribute(k_xAs<R, C, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
                 cudaFuncSetAttribute(k_xAs<R, C, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
                 cudaFuncSetAttribute(k_xAs<R, C, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s3);
-                k_xAs<R, C, 1><<<grid, nt, s1, st>>>(a);
+                const bool cc = par_on(ch);   // the pieces as concurrent branches (knob 15)
+                if (cc && (rc = par_fork(ch))) return rc;
+                k_xAs<R, C, 1><<<grid, nt, s1, cc ? ch->par[0] : st>>>(a);
                 mark(ch, nl, "xA_u", N * (16 + 2 * Rb));
-                k_xAs<R, C, 2><<<grid, nt, s2, st>>>(a);
+                k_xAs<R, C, 2><<<grid, nt, s2, cc ? ch->par[1] : st>>>(a);
                 mark(ch, nl, "xA_v", N * (24 + 3 * Rb));
                 k_xAs<R, C, 3><<<grid, nt, s3, st>>>(a);
                 mark(ch, nl, "xA_w", N * (8 + 2 * Rb));
+                if (cc && (rc = par_join(ch))) return rc;
                 break;
             }
             if (ch->tune.xsplit) {   // the u, v and w pieces as three kernels
                 cudaFuncSetAttribute(k_xA<R, C, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
                 cudaFuncSetAttribute(k_xA<R, C, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
                 cudaFuncSetAttribute(k_xA<R, C, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
-                k_xA<R, C, 1><<<grid, nt, sb, st>>>(a);
+                const bool cc = par_on(ch);
+                if (cc && (rc = par_fork(ch))) return rc;
+                k_xA<R, C, 1><<<grid, nt, sb, cc ? ch->par[0] : st>>>(a);
                 mark(ch, nl, "xA_u", N * (16 + 2 * Rb));   // u, P; R1, HH1
-                k_xA<R, C, 2><<<grid, nt, sb, st>>>(a);
+                k_xA<R, C, 2><<<grid, nt, sb, cc ? ch->par[1] : st>>>(a);
                 mark(ch, nl, "xA_v", N * (24 + 3 * Rb));   // v, P, u; R2, HH2, E_xy
                 k_xA<R, C, 3><<<grid, nt, sb, st>>>(a);
                 mark(ch, nl, "xA_w", N * (8 + 2 * Rb));    // w; R3, WW1
+                if (cc && (rc = par_join(ch))) return rc;
                 break;
             }
             cudaFuncSetAttribute(k_xA<R, C, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb);
@@ -170,14 +177,14 @@ static int launch_x_c(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, c
 
 
 // xA's pieces (unless staged), xB, and xC and xD (with the shared-memory row FFT and no
-// bulk-copy ring) with a row per segment of W lanes (schedule knob x_row_lanes); false
-// when the schedule runs the pass on whole warps.
+// bulk-copy ring) with a row per segment of W lanes (schedule knob x_row_lanes).  Returns
+// 0 when launched, 1 when the schedule runs the pass on whole warps, or an error code.
 template <typename R, int C, int W>
-static bool launch_x_seg(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl) {
+static int launch_x_seg(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl) {
     typedef typename Cx<R>::T C2;
     const Tune &t = ch->tune;
-    if (which == 0 && (!t.xsplit || t.xstage)) return false;
-    if ((which == 2 || which == 3) && (t.fxp == 3 || t.xbulk)) return false;
+    if (which == 0 && (!t.xsplit || t.xstage)) return 1;
+    if ((which == 2 || which == 3) && (t.fxp == 3 || t.xbulk)) return 1;
     const int nrows = ch->g.n2m * ch->g.n3m, rpb = t.xw * 32 / W;
     const int grid = nblk(nrows, rpb), nt = t.xw * 32;
     const double N = (double)ch->g.n1m * ch->g.n2m * ch->g.n3m, Rb = sizeof(R);
@@ -187,40 +194,44 @@ static bool launch_x_seg(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0
         cudaFuncSetAttribute(k_xC<R, C, 0, false, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
         k_xC<R, C, 0, false, W><<<grid, nt, fb, st>>>(a, p0, p1);
         mark(ch, nl, "xC", N * (16 + 4 * Rb));
-        return true;
+        return 0;
     }
     if (which == 3) {
         cudaFuncSetAttribute(k_xD<R, C, false, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb);
         k_xD<R, C, false, W><<<grid, nt, fb, st>>>(a, p0, p1);
         mark(ch, nl, "xD", N * 5 * Rb);
-        return true;
+        return 0;
     }
     if (which == 0) {
-        k_xA<R, C, 1, W><<<grid, nt, 0, st>>>(a);
+        const bool cc = par_on(ch);   // the pieces as concurrent branches (knob 15)
+        int rc;
+        if (cc && (rc = par_fork(ch))) return rc;
+        k_xA<R, C, 1, W><<<grid, nt, 0, cc ? ch->par[0] : st>>>(a);
         mark(ch, nl, "xA_u", N * (16 + 2 * Rb));
-        k_xA<R, C, 2, W><<<grid, nt, 0, st>>>(a);
+        k_xA<R, C, 2, W><<<grid, nt, 0, cc ? ch->par[1] : st>>>(a);
         mark(ch, nl, "xA_v", N * (24 + 3 * Rb));
         k_xA<R, C, 3, W><<<grid, nt, 0, st>>>(a);
         mark(ch, nl, "xA_w", N * (8 + 2 * Rb));
+        if (cc && (rc = par_join(ch))) return rc;
     } else {
         k_xB<R, C, W><<<grid, nt, 0, st>>>(a);
         mark(ch, nl, "xB", N * 18 * Rb);
     }
-    return true;
+    return 0;
 }
 
 template <typename R>
 int launch_xpass(c3d_channel *ch, StepArgs<R> &a, int which, const R *p0, const R *p1, int *nl) {
     if (which >= 0 && which <= 3 && ch->tune.xlanes) {
-        bool done = false;
+        int r = 1;
         switch (ch->g.n1m) {   // the shapes x_segment_lanes accepts
-            case 48: done = launch_x_seg<R, 6, 8>(ch, a, which, p0, p1, nl); break;
-            case 64: done = launch_x_seg<R, 8, 8>(ch, a, which, p0, p1, nl); break;
-            case 96: done = launch_x_seg<R, 12, 8>(ch, a, which, p0, p1, nl); break;
-            case 128: done = launch_x_seg<R, 8, 16>(ch, a, which, p0, p1, nl); break;
+            case 48: r = launch_x_seg<R, 6, 8>(ch, a, which, p0, p1, nl); break;
+            case 64: r = launch_x_seg<R, 8, 8>(ch, a, which, p0, p1, nl); break;
+            case 96: r = launch_x_seg<R, 12, 8>(ch, a, which, p0, p1, nl); break;
+            case 128: r = launch_x_seg<R, 8, 16>(ch, a, which, p0, p1, nl); break;
             default: break;
         }
-        if (done) return 0;
+        if (r <= 0) return r;
     }
     switch ((ch->g.n1m + 31) / 32) {
         case 1: return launch_x_c<R, 1>(ch, a, which, p0, p1, nl);

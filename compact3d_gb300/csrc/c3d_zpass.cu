@@ -543,12 +543,18 @@ static int launch_zpass_l(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *
     switch (which) {
         case 0:
             if (ch->tune.zsplit) {   // u, (w, P), v sweeps as three kernels
-                k_zA<R, L, 1, MODE><<<nb, TB, zsm, st>>>(a);
+                // as concurrent branches with knob 15: each writes its own R component and
+                // product, and they share only inputs that none of them writes
+                const bool cc = par_on(ch);
+                int rc;
+                if (cc && (rc = par_fork(ch))) return rc;
+                k_zA<R, L, 1, MODE><<<nb, TB, zsm, cc ? ch->par[0] : st>>>(a);
                 mark(ch, nl, "zA_u", N * (8 + 4 * Rb));    // u; WW1, R1 -> R1, E_xz
-                k_zA<R, L, 2, MODE><<<nb, TB, zsm, st>>>(a);
+                k_zA<R, L, 2, MODE><<<nb, TB, zsm, cc ? ch->par[1] : st>>>(a);
                 mark(ch, nl, "zA_wp", N * (16 + 3 * Rb));  // w, P; R3 -> R3, WW3^2
                 k_zA<R, L, 3, MODE><<<nb, TB, zsm, st>>>(a);
                 mark(ch, nl, "zA_v", N * (16 + 3 * Rb));   // v, w; R2 -> R2, E_yz
+                if (cc && (rc = par_join(ch))) return rc;
             } else {
                 k_zA<R, L, 0, MODE><<<nb, TB, zsm, st>>>(a);
                 mark(ch, nl, "zA", N * (32 + 10 * Rb));

@@ -118,7 +118,7 @@ def load(path: str = LIB_PATH):
 
 
 # Operators of c3d_op_apply (include/c3d.h)
-C3D_SCHEDULE_LEN = 15   # ints of a launch schedule (include/c3d.h)
+C3D_SCHEDULE_LEN = 16   # ints of a launch schedule (include/c3d.h)
 OPS = {"DX1": 1, "DX2": 2, "IX": 3, "DZ1": 4, "DZ2": 5, "IZ": 6, "DY1": 7, "DY2": 8, "POISSON": 9}
 
 
@@ -205,7 +205,7 @@ class Channel:
     # ---- launch schedule ----
     SCHEDULE_KEYS = ("z_segment_zA", "z_segment_zB", "z_segment_zC", "z_segment_zD", "z_segment_zE",
                      "x_rows_per_block", "fft_z_tile", "fft_x_plan", "fft_z_plan", "z_split_zA",
-                     "x_split_xA", "x_bulk_stages", "x_stage_xA", "ycn_tile", "x_row_lanes")
+                     "x_split_xA", "x_bulk_stages", "x_stage_xA", "ycn_tile", "x_row_lanes", "concurrent_pieces")
 
     def autotune(self) -> dict:
         sch = (_ip * C3D_SCHEDULE_LEN)()

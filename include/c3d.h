@@ -370,7 +370,7 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
 
 /* ---- launch schedule -----------------------------------------------------
  * The kernels' launch shapes are chosen per grid shape by an autotuner written for
- * this library (no counterpart in the reference).  A schedule is fifteen ints
+ * this library (no counterpart in the reference).  A schedule is sixteen ints
  * (C3D_SCHEDULE_LEN):
  *   [0..4] z-line segment length (8, 16, 32) of each z pass: the points each thread
  *       solves sequentially (Thomas-like) before the parallel segments of a z line
@@ -406,6 +406,11 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
  *       96 (8 lanes) or 128 (16 lanes) with N3M a multiple of 32 / lanes, so that each
  *       lane holds 6 to 12 points and the cross-lane scans of the line solves take 3
  *       or 4 steps instead of 5
+ *   [15] the u, v and w pieces of the explicit x pass ([10] = 1), then those of the
+ *       explicit z pass ([9] = 1), as three concurrent branches on three streams (1)
+ *       or one after another (0); they write disjoint fields.  The per-kernel profile
+ *       (c3d_profile) runs them one after another; c3d_autotune judges this knob by
+ *       the time of whole unprofiled steps
  * c3d_autotune  times the candidates on a scratch channel of the same grid holding a
  *               copy of this channel's state (so the channel needs its state), keeps
  *               the fastest per kernel group, applies it, and caches it per grid
@@ -413,7 +418,7 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
  *               receives the result.
  * c3d_set_schedule / c3d_get_schedule  set or read a schedule directly.
  * Channels of a batch are tuned before the batch's first step captures its graph. */
-#define C3D_SCHEDULE_LEN 15
+#define C3D_SCHEDULE_LEN 16
 int c3d_autotune(c3d_channel *ch, int *sched);
 int c3d_get_schedule(c3d_channel *ch, int *sched);
 int c3d_set_schedule(c3d_channel *ch, const int *sched);

@@ -113,6 +113,36 @@ def test_batch_of_les_channels_matches_single_channels(L):
     b.close()
 
 
+def test_streams_form_with_concurrent_pieces(L):
+    """Channels whose explicit pieces run as concurrent branches (schedule knob 15) inside
+    the streams form's graph: the forks onto each channel's extra streams are captured with
+    its step, and the results are bitwise those of single channels that run the pieces one
+    after another."""
+    ens = dns_ensemble(C3D_MIXED)[:3]
+    b = L.Batch([g for g, _, _ in ens])
+    b.set_form("streams")
+    singles = []
+    for (g, dt, (U, P, HH)), ch in zip(ens, b.channels):
+        ch.upload(U, P, HH)
+        ch.set_schedule(dict(ch.get_schedule(), x_split_xA=1, z_split_zA=1, concurrent_pieces=1))
+        s = L.Channel(g)
+        s.upload(U, P, HH)
+        s.set_schedule(dict(s.get_schedule(), x_split_xA=1, z_split_zA=1, concurrent_pieces=0))
+        singles.append(s)
+    dts = [dt for _, dt, _ in ens]
+    pb, pb3 = [0.0] * len(ens), [0.0] * len(ens)
+    ps = [(0.0, 0.0) for _ in ens]
+    for n in range(1, 4):
+        pb, pb3 = b.step(n, dts, pb, pb3)
+        ps = [s.step(n, dt, *p) for s, dt, p in zip(singles, dts, ps)]
+    for i, (ch, s) in enumerate(zip(b.channels, singles)):
+        for x, y in zip(ch.download(), s.download()):
+            assert np.array_equal(x, y), i
+    for s in singles:
+        s.close()
+    b.close()
+
+
 def test_batch_refuses_iwmles(L):
     g, _ = make_grid("les32cs", wmodel=2)
     with pytest.raises(L.C3DError):

@@ -26,10 +26,11 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def _sched(zl, xw, tw, fx, fz, split, xsplit, xbulk=0, xstage=0, ycn=0, xlanes=0):
+def _sched(zl, xw, tw, fx, fz, split, xsplit, xbulk=0, xstage=0, ycn=0, xlanes=0, conc=0):
     d = {f"z_segment_z{c}": z for c, z in zip("ABCDE", zl)}
     d.update(x_rows_per_block=xw, fft_z_tile=tw, fft_x_plan=fx, fft_z_plan=fz, z_split_zA=split,
-             x_split_xA=xsplit, x_bulk_stages=xbulk, x_stage_xA=xstage, ycn_tile=ycn, x_row_lanes=xlanes)
+             x_split_xA=xsplit, x_bulk_stages=xbulk, x_stage_xA=xstage, ycn_tile=ycn, x_row_lanes=xlanes,
+             concurrent_pieces=conc)
     return d
 
 
@@ -134,6 +135,28 @@ def test_row_segments_match_oracle(libc3d, oracle_mod, n1m, lanes):
         m.close()
     assert rel(out[1][0], out[0][0]) < 1e-8
     assert rel(out[1][2], out[0][2]) < 1e-4
+
+
+@pytest.mark.parametrize("prec,xstage", [(C3D_MIXED, 0), (C3D_MIXED, 1), (C3D_FP64, 0)])
+def test_concurrent_pieces_bit_identical(libc3d, prec, xstage):
+    """The explicit pieces as concurrent branches (knob 15) run the same kernels on the same
+    data in another order of launch; they write disjoint fields, so the step is
+    bit-identical to the pieces one after another."""
+    g, dt = make_grid("small32", n1m=64, n2m=24, n3m=64)
+    U, P, HH = ic.perturbed_laminar(g)
+    out = []
+    for conc in (0, 1):
+        ch = libc3d.Channel(g, prec)
+        ch.upload(U, P, HH)
+        ch.set_schedule(dict(ch.get_schedule(), x_split_xA=1, z_split_zA=1, x_stage_xA=xstage,
+                             concurrent_pieces=conc))
+        pg = pg3 = 0.0
+        for m in (1, 2, 3):
+            pg, pg3 = ch.step(m, dt, pg, pg3)
+        out.append(ch.download() + (pg,))
+        ch.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("sched,n3m", SCHEDULES)
