@@ -1814,7 +1814,7 @@ struct c3d_batch {
     float last_ms = 0.f;
     int form = C3D_BATCH_WORKLIST;            // requested form (c3d_batch_set_form)
     int groups = 2;                           // work-list form: channel groups on their own streams
-    BatchSched sched{{8, 8, 16, 16, 8}, 2};  // work-list form: z segments of zA..zE, warps per x block
+    BatchSched sched{{8, 8, 16, 16, 8}, 2, 0};   // work-list form: z segments of zA..zE, warps per x block, concurrent pieces
     // work-list form, per AB2 parity: every channel's StepArgs and the block maps
     void *dargs[2] = {nullptr, nullptr};
     size_t nargs[2] = {0, 0};
@@ -1889,7 +1889,7 @@ static int batch_capture_worklist(c3d_batch *b, const double *dt, int par) {
     });
     std::vector<std::vector<int>> members(G);
     for (int q = 0; q < n; ++q) members[q % G].push_back(order[q]);
-    struct Grp { const void *fn; unsigned block; size_t smem, off, cnt; int sg; };
+    struct Grp { const void *fn; unsigned block; size_t smem, off, cnt; int sg, run, piece; };
     std::vector<Grp> launches;
     std::vector<BMap> map;
     for (int sg = 0; sg < G; ++sg)
@@ -1899,7 +1899,7 @@ static int batch_capture_worklist(c3d_batch *b, const double *dt, int par) {
                 const BKern &k = plans[i][p];
                 size_t q = 0;
                 while (q < gs.size() && !(gs[q].fn == k.fn && gs[q].block == k.block)) ++q;
-                if (q == gs.size()) gs.push_back({k.fn, k.block, 0, 0, 0, sg});
+                if (q == gs.size()) gs.push_back({k.fn, k.block, 0, 0, 0, sg, b->sched.conc ? k.run : 0, k.piece});
                 gs[q].smem = std::max(gs[q].smem, k.smem);
             }
             for (Grp &gr : gs) {
@@ -1932,15 +1932,33 @@ static int batch_capture_worklist(c3d_batch *b, const double *dt, int par) {
     cudaError_t le = cudaSuccess;
     for (int sg = 0; sg < G; ++sg) {
         cudaStream_t s = G == 1 ? b->stream : b->ch[sg]->stream;   // a channel stream, idle meanwhile
+        c3d_channel *own = b->ch[sg];   // its two extra streams carry pieces 0 and 1 of a run
         if (G > 1) cudaStreamWaitEvent(s, b->fork, 0);
+        int run = 0;
+        auto join = [&]() {
+            for (int q = 0; q < 2; ++q) {
+                cudaEventRecord(own->pev[1 + q], own->par[q]);
+                cudaStreamWaitEvent(s, own->pev[1 + q], 0);
+            }
+        };
         for (const Grp &gr : launches) {
             if (gr.sg != sg) continue;
+            if (gr.run != run) {   // a run of independent pieces ends or begins
+                if (run) join();
+                run = gr.run;
+                if (run) {
+                    cudaEventRecord(own->pev[0], s);
+                    for (int q = 0; q < 2; ++q) cudaStreamWaitEvent(own->par[q], own->pev[0], 0);
+                }
+            }
+            cudaStream_t ls = (run && gr.piece < 2) ? own->par[gr.piece] : s;
             void *A = b->dargs[par];
             BMap *M = b->dmap[par] + gr.off;
             void *kargs[] = {&A, &M};
-            cudaError_t e = cudaLaunchKernel(gr.fn, dim3((unsigned)gr.cnt), dim3(gr.block), kargs, gr.smem, s);
+            cudaError_t e = cudaLaunchKernel(gr.fn, dim3((unsigned)gr.cnt), dim3(gr.block), kargs, gr.smem, ls);
             if (e != cudaSuccess && le == cudaSuccess) le = e;
         }
+        if (run) join();
         if (G > 1) {
             cudaEventRecord(b->join[sg], s);
             cudaStreamWaitEvent(b->stream, b->join[sg], 0);
@@ -2148,6 +2166,18 @@ int c3d_batch_set_z_segments(c3d_batch *b, const int *seg) {
         b->gdt[p].clear();
     }
     for (int q = 0; q < 5; ++q) b->sched.zseg[q] = seg[q];
+    return 0;
+}
+
+int c3d_batch_set_concurrent(c3d_batch *b, int on) {
+    if (!b || (on != 0 && on != 1)) { set_error("concurrent must be 0 or 1"); return C3D_EINVAL; }
+    CK(cudaStreamSynchronize(b->stream));
+    for (int p = 0; p < 2; ++p) {
+        if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
+        b->exec[p] = nullptr;
+        b->gdt[p].clear();
+    }
+    b->sched.conc = on;
     return 0;
 }
 

@@ -80,7 +80,15 @@ struct BMap { int ch; unsigned x, y, gx; };
 // One pass of one channel in the batch form: the batch kernel (its template instance is
 // the group key), the block size, dynamic shared memory and the blocks of the channel's
 // own grid.  Batch kernels take (const StepArgs<R> *args, const BMap *map).
-struct BKern { const void *fn; unsigned block; size_t smem; unsigned nblocks; };
+// run > 0: the pass is piece `piece` (0-2) of a run of three independent passes that the
+// work-list capture may launch as concurrent branches (run 1: xA's pieces, run 2: zA's).
+struct BKern {
+    const void *fn;
+    unsigned block;
+    size_t smem;
+    unsigned nblocks;
+    int run = 0, piece = 0;
+};
 
 // Blocks of the first level of the bulk-flow reduction; `part` holds 2 N2M N3M per-row
 // partials followed by 2 RB block sums.
@@ -303,6 +311,7 @@ template <typename R> int spec_bkern(const c3d_channel *ch, int which, std::vect
 struct BatchSched {
     int zseg[5];
     int xw;
+    int conc;   // the pieces of xA and of zA as concurrent branches of each group (1) or not (0)
 };
 int batch_plan(c3d_channel *ch, const BatchSched &s, std::vector<BKern> &out);
 size_t batch_args_size(const c3d_channel *ch);

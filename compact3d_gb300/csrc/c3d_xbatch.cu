@@ -44,9 +44,9 @@ static int xbk(const c3d_channel *ch, int which, int xw, std::vector<BKern> &out
     const bool x4 = (C % 2 == 0) && ch->g.n1m == 32 * C;   // register row FFT (see launch_x_c)
     switch (which) {
         case 0:
-            out.push_back({(const void *)kb_xA<R, C, 1>, nt, sb, nb});
-            out.push_back({(const void *)kb_xA<R, C, 2>, nt, sb, nb});
-            out.push_back({(const void *)kb_xA<R, C, 3>, nt, sb, nb});
+            out.push_back({(const void *)kb_xA<R, C, 1>, nt, sb, nb, 1, 0});
+            out.push_back({(const void *)kb_xA<R, C, 2>, nt, sb, nb, 1, 1});
+            out.push_back({(const void *)kb_xA<R, C, 3>, nt, sb, nb, 1, 2});
             return 0;
         case 1: out.push_back({(const void *)kb_xB<R, C>, nt, sb, nb}); return 0;
         case 2:
@@ -76,9 +76,9 @@ static int xbk_seg(const c3d_channel *ch, int which, int xw, std::vector<BKern> 
     const size_t fb = (stage_bytes(ch->g.n1m, C) + 2 * (size_t)(ch->g.n1m / 2 + 1) * sizeof(C2)) * rpb;
     switch (which) {
         case 0:
-            out.push_back({(const void *)kb_xA<R, C, 1, W>, nt, 0, nb});
-            out.push_back({(const void *)kb_xA<R, C, 2, W>, nt, 0, nb});
-            out.push_back({(const void *)kb_xA<R, C, 3, W>, nt, 0, nb});
+            out.push_back({(const void *)kb_xA<R, C, 1, W>, nt, 0, nb, 1, 0});
+            out.push_back({(const void *)kb_xA<R, C, 2, W>, nt, 0, nb, 1, 1});
+            out.push_back({(const void *)kb_xA<R, C, 3, W>, nt, 0, nb, 1, 2});
             return 0;
         case 1: out.push_back({(const void *)kb_xB<R, C, W>, nt, 0, nb}); return 0;
         case 2: out.push_back({(const void *)kb_xC<R, C, false, W>, nt, fb, nb}); return 0;

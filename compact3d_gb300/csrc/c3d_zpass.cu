@@ -486,9 +486,9 @@ static int zbk(const c3d_channel *ch, int which, std::vector<BKern> &out) {
     const unsigned nb = (unsigned)nblk((long long)ch->g.n2m * (ch->g.n3m / L) * ch->g.n1m);
     switch (which) {
         case 0:
-            out.push_back({(const void *)kb_zA<R, 1, L>, TPB, 0, nb});
-            out.push_back({(const void *)kb_zA<R, 2, L>, TPB, 0, nb});
-            out.push_back({(const void *)kb_zA<R, 3, L>, TPB, 0, nb});
+            out.push_back({(const void *)kb_zA<R, 1, L>, TPB, 0, nb, 2, 0});
+            out.push_back({(const void *)kb_zA<R, 2, L>, TPB, 0, nb, 2, 1});
+            out.push_back({(const void *)kb_zA<R, 3, L>, TPB, 0, nb, 2, 2});
             return 0;
         case 1: out.push_back({(const void *)kb_zB<R, L>, TPB, 0, nb}); return 0;
         case 2: out.push_back({(const void *)kb_zC<R, L>, TPB, 0, nb}); return 0;

@@ -95,6 +95,7 @@ SIGNATURES = {
     "c3d_batch_set_groups": (_ip, [_vp, _ip]),
     "c3d_batch_set_z_segments": (_ip, [_vp, _vp]),
     "c3d_batch_set_x_warps": (_ip, [_vp, _ip]),
+    "c3d_batch_set_concurrent": (_ip, [_vp, _ip]),
     "c3d_batch_last_step_stats": (_ip, [_vp, _dp, ctypes.POINTER(_ip)]),
 }
 
@@ -455,6 +456,10 @@ class Batch:
     def set_x_warps(self, warps: int):
         """Work-list form: warps per block of the x passes (2, 4 or 8)."""
         check(load().c3d_batch_set_x_warps(self.h, int(warps)), "c3d_batch_set_x_warps")
+
+    def set_concurrent(self, on: int):
+        """Work-list form: the pieces of the explicit passes as concurrent branches."""
+        check(load().c3d_batch_set_concurrent(self.h, int(on)), "c3d_batch_set_concurrent")
 
     def get_form(self) -> str:
         f = (ctypes.c_int * 1)()

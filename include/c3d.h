@@ -485,7 +485,12 @@ int c3d_op_get(c3d_channel *ch, double *f);
  * c3d_batch_set_z_segments (work-list form) sets the segment length of the z
  * passes zA, zB, zC, zD, zE (seg[0..4], each 8, 16 or 32; a channel whose N3M is
  * not a multiple of it runs 16).  c3d_batch_set_x_warps (work-list form) sets
- * the warps per block of the x passes (2, 4 or 8; default 2).
+ * the warps per block of the x passes (2, 4 or 8; default 2).  c3d_batch_set_concurrent
+ * (work-list form; default 0) runs the three pieces of the explicit x pass, and then
+ * those of the explicit z pass, of each channel group as concurrent branches (1) or one
+ * after another (0); the pieces write disjoint fields, so the results do not change.
+ * Concurrent pieces pay with one channel group and cost with two (the default), where
+ * the groups already overlap.
  */
 #define C3D_BATCH_STREAMS   0
 #define C3D_BATCH_WORKLIST  1
@@ -500,6 +505,7 @@ int c3d_batch_get_form(c3d_batch *b, int *form);
 int c3d_batch_set_groups(c3d_batch *b, int groups);
 int c3d_batch_set_z_segments(c3d_batch *b, const int *seg);
 int c3d_batch_set_x_warps(c3d_batch *b, int warps);
+int c3d_batch_set_concurrent(c3d_batch *b, int on);
 /* Device time of the last ensemble step (CUDA events around the graph launch) and the
  * number of kernels one ensemble step runs. */
 int c3d_batch_last_step_stats(c3d_batch *b, double *ms, int *kernel_launches);

@@ -113,6 +113,31 @@ def test_batch_of_les_channels_matches_single_channels(L):
     b.close()
 
 
+@pytest.mark.parametrize("groups", [1, 2])
+def test_worklist_concurrent_pieces_bit_identical(L, groups):
+    """The work-list form with the pieces of xA and zA as concurrent branches of each group
+    against the same form with the pieces one after another (the default): the same
+    kernels on the same data, disjoint outputs, so every channel's state is bitwise equal."""
+    ens = dns_ensemble(C3D_MIXED)
+    res = []
+    for conc in (0, 1):
+        b = L.Batch([g for g, _, _ in ens])
+        for (g, dt, (U, P, HH)), ch in zip(ens, b.channels):
+            ch.upload(U, P, HH)
+        b.set_groups(groups)
+        b.set_concurrent(conc)
+        dts = [dt for _, dt, _ in ens]
+        p, p3 = [0.0] * len(ens), [0.0] * len(ens)
+        for n in range(1, 4):
+            p, p3 = b.step(n, dts, p, p3)
+        res.append([ch.download() for ch in b.channels] + [p])
+        b.close()
+    for x, y in zip(res[0][:-1], res[1][:-1]):
+        for a, c in zip(x, y):
+            assert np.array_equal(a, c)
+    assert res[0][-1] == res[1][-1]
+
+
 def test_streams_form_with_concurrent_pieces(L):
     """Channels whose explicit pieces run as concurrent branches (schedule knob 15) inside
     the streams form's graph: the forks onto each channel's extra streams are captured with
@@ -267,4 +292,6 @@ def test_mixed_precision_batch_runs_streams_form(L):
         b.set_z_segments([12, 16, 16, 16, 16])
     with pytest.raises(L.C3DError):
         b.set_x_warps(3)
+    with pytest.raises(L.C3DError):
+        b.set_concurrent(2)
     b.close()
