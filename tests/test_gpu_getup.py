@@ -99,3 +99,33 @@ def test_getup_host_alloc_arrays(libc3d):
     ref.close()
     for a in (U, P, HH):
         libc3d.host_free(a)
+
+
+def test_getup_concurrent_pieces(libc3d):
+    """c3d_getup on page-locked arrays with the explicit pieces as concurrent branches
+    (knob 15): the upload of HH_old on the side stream, the pieces on the two extra
+    streams and the download of the new HH after xB keep their order, so the host arrays
+    equal the device-resident step with the pieces one after another, bit for bit (FP64)."""
+    g, dt = make_grid("small32", C3D_FP64, n1m=64, n2m=32, n3m=64)
+    U0, P0, HH0 = ic.perturbed_laminar(g)
+    U, P, HH = (libc3d.host_array(a.shape) for a in (U0, P0, HH0))
+    U[...], P[...], HH[...] = U0, P0, HH0
+    ch = libc3d.Channel(g, C3D_FP64)
+    ch.set_schedule(dict(ch.get_schedule(), x_split_xA=1, z_split_zA=1, concurrent_pieces=1))
+    pg = pg3 = 0.0
+    for m in (1, 2, 3):
+        pg, pg3 = ch.getup(U, P, HH, m, dt, pg, pg3)
+    ch.close()
+    ref = libc3d.Channel(g, C3D_FP64)
+    ref.set_schedule(dict(ref.get_schedule(), x_split_xA=1, z_split_zA=1, concurrent_pieces=0))
+    ref.upload(U0, P0, HH0)
+    qg = qg3 = 0.0
+    for m in (1, 2, 3):
+        qg, qg3 = ref.step(m, dt, qg, qg3)
+    for x, y in zip((U, P, HH), ref.download()):
+        assert np.array_equal(x, y)
+    assert pg == qg and pg3 == qg3
+    ref.close()
+    for a in (U, P, HH):
+        libc3d.host_free(a)
+
