@@ -812,10 +812,18 @@ __device__ __forceinline__ void b_xD(const StepArgs<R> &a, const R *d0, const R 
             d[t] = f24 * (dpv[t] - l);
         }
         xsolve<W>(d, lane, P, a.c22x);
-        srow_store(a.g1 + o, d, sbR, lane, P);
-        // bulk-flow partial sums: sum_i delta * DY(J)/DX3/DX1 for u and w
+        // bulk-flow partial sums below: sum_i delta * DY(J)/DX3/DX1 for u and w
         R q1[C], q3[C];
         srow_load(q1, d0 + o, sbR, lane, P);
+        if constexpr (sizeof(R) == 4) {
+            // mixed form: the u update's increment delta1 - DT dDP/dx, formed here in the
+            // order UPCALC's update forms it in FP32 (zE then adds it, less dm, to U and
+            // reads neither delta1 nor dDP/dx)
+            const R dt = (R)a.dt;
+#pragma unroll
+            for (int t = 0; t < C; ++t) d[t] = q1[t] - dt * d[t];
+        }
+        srow_store(a.g1 + o, d, sbR, lane, P);
         srow_load(q3, d2 + o, sbR, lane, P);
         if constexpr (sizeof(R) == 8) {
             R l1 = R(0), l3 = R(0);

@@ -372,7 +372,7 @@ __device__ __forceinline__ void b_zE(const StepArgs<R> &a, const R *d0, const R 
         pf_cols(a.v + o0, sb * sizeof(S), 32 * (int)sizeof(S), k0, 0, L, n, lane);
         pf_cols(a.w + o0, sb * sizeof(S), 32 * (int)sizeof(S), k0, 0, L, n, lane);
         pf_cols(a.p + o0, sb * sizeof(S), 32 * (int)sizeof(S), k0, 0, L, n, lane);
-        pf_cols(d0 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
+        if (sizeof(R) == 8) pf_cols(d0 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
         pf_cols(d1 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
         pf_cols(d2 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
         pf_cols(a.g1 + o0, sb * sizeof(R), 32 * (int)sizeof(R), k0, 0, L, n, lane);
@@ -389,7 +389,8 @@ __device__ __forceinline__ void b_zE(const StepArgs<R> &a, const R *d0, const R 
     for (int t = 0; t < L; ++t) {
         const int kk = (k0 + t) * s;
         W[kk] = Sten<R>::upd(W[kk], D2[kk], dt * out[0][t], dtdm3);
-        U[kk] = Sten<R>::upd(U[kk], D0[kk], dt * G1[kk], dtdm);
+        if constexpr (sizeof(R) == 4) U[kk] = ST::add(U[kk], G1[kk] - dtdm);   // G1: delta1 - DT dDP/dx (xD)
+        else U[kk] = Sten<R>::upd(U[kk], D0[kk], dt * G1[kk], dtdm);
         if (j >= 2) V[kk] = Sten<R>::upd(V[kk], D1[kk], dt * (DP[kk] - DPm[kk]) * rHj, R(0));
         if (updp) Pp[kk] = ST::add(Pp[kk], DP[kk]);
     }
@@ -563,7 +564,10 @@ static int launch_zpass_l(c3d_channel *ch, StepArgs<R> &a, int which, R *d0, R *
         case 1: k_zB<R, L, MODE><<<nb, TB, zsm, st>>>(a); mark(ch, nl, "zB", N * 8 * Rb); break;
         case 2: k_zC<R, L, MODE><<<nb, TB, zsm, st>>>(a, d0, d1, d2); mark(ch, nl, "zC", N * 6 * Rb); break;
         case 3: k_zD<R, L, MODE><<<nb, TB, zsm, st>>>(a, d2); mark(ch, nl, "zD", N * (8 + 2 * Rb)); break;
-        case 4: k_zE<R, L, MODE><<<nb, TB, zsm, st>>>(a, d0, d1, d2, flag); mark(ch, nl, "zE", N * (64 + 5 * Rb)); break;
+        case 4:   // the mixed form reads delta1 - DT dDP/dx from one field (xD), FP64 both
+            k_zE<R, L, MODE><<<nb, TB, zsm, st>>>(a, d0, d1, d2, flag);
+            mark(ch, nl, "zE", N * (64 + (sizeof(R) == 4 ? 4 : 5) * Rb));
+            break;
         case 5: {
             if (MODE == 1) return C3D_EINVAL;   // the diagnostics run the segment form only
             const double b = 22.0, r = -2.0 / (b + sqrt(b * b - 4.0));
