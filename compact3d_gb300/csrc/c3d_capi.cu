@@ -1711,7 +1711,7 @@ int c3d_autotune(c3d_channel *ch, int *sched) {
     const double dt = ch->dt_cached > 0 ? ch->dt_cached : 1e-3;
     // knob q: 0-4 the segment length of zA..zE, 5 x rows per block, 6 z-FFT tile, 7/8 plans,
     // 9 zA split, 10 xA split, 11 bulk-copy stages of the x passes, 12 xA rows staged by bulk copies,
-    // 13 form of the wall-normal CN factor, 14 lanes per row of xA and xB
+    // 13 form of the wall-normal CN factor, 14 lanes per row of the x passes (15, concurrent pieces, below)
     struct Group { int knob; std::vector<int> cand; std::vector<std::string> kernels; };
     const Group groups[] = {
         {9, {0, 1}, {"zA"}}, {10, {0, 1}, {"xA"}}, {12, {0, 1}, {"xA"}}, {14, {0, 8, 16}, {"xA", "xB", "xC", "xD"}},
@@ -2129,28 +2129,34 @@ int c3d_batch_step(c3d_batch *b, int ntime, const double *dt, double *presg, dou
     return 0;
 }
 
+}  // extern "C"
+
+// A change of the ensemble's form or schedule: wait for the running step and drop the
+// captured graphs, so that the next c3d_batch_step captures them again.
+static int batch_recapture(c3d_batch *b) {
+    CK(cudaStreamSynchronize(b->stream));
+    for (int p = 0; p < 2; ++p) {
+        if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
+        b->exec[p] = nullptr;
+        b->gdt[p].clear();
+    }
+    return 0;
+}
+
+extern "C" {
+
 int c3d_batch_set_form(c3d_batch *b, int form) {
     if (!b || (form != C3D_BATCH_STREAMS && form != C3D_BATCH_WORKLIST)) { set_error("bad batch form"); return C3D_EINVAL; }
-    CK(cudaStreamSynchronize(b->stream));
     if (form != b->form)
-        for (int p = 0; p < 2; ++p) {
-            if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
-            b->exec[p] = nullptr;
-            b->gdt[p].clear();
-        }
+        if (int rc = batch_recapture(b)) return rc;
     b->form = form;
     return 0;
 }
 
 int c3d_batch_set_groups(c3d_batch *b, int groups) {
     if (!b || groups < 1 || groups > 64) { set_error("groups must be in [1, 64]"); return C3D_EINVAL; }
-    CK(cudaStreamSynchronize(b->stream));
     if (groups != b->groups)
-        for (int p = 0; p < 2; ++p) {
-            if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
-            b->exec[p] = nullptr;
-            b->gdt[p].clear();
-        }
+        if (int rc = batch_recapture(b)) return rc;
     b->groups = groups;
     return 0;
 }
@@ -2159,36 +2165,21 @@ int c3d_batch_set_z_segments(c3d_batch *b, const int *seg) {
     if (!b || !seg) { set_error("null argument"); return C3D_EINVAL; }
     for (int q = 0; q < 5; ++q)
         if (seg[q] != 8 && seg[q] != 16 && seg[q] != 32) { set_error("z segment lengths must be 8, 16 or 32"); return C3D_EINVAL; }
-    CK(cudaStreamSynchronize(b->stream));
-    for (int p = 0; p < 2; ++p) {
-        if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
-        b->exec[p] = nullptr;
-        b->gdt[p].clear();
-    }
+    if (int rc = batch_recapture(b)) return rc;
     for (int q = 0; q < 5; ++q) b->sched.zseg[q] = seg[q];
     return 0;
 }
 
 int c3d_batch_set_concurrent(c3d_batch *b, int on) {
     if (!b || (on != 0 && on != 1)) { set_error("concurrent must be 0 or 1"); return C3D_EINVAL; }
-    CK(cudaStreamSynchronize(b->stream));
-    for (int p = 0; p < 2; ++p) {
-        if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
-        b->exec[p] = nullptr;
-        b->gdt[p].clear();
-    }
+    if (int rc = batch_recapture(b)) return rc;
     b->sched.conc = on;
     return 0;
 }
 
 int c3d_batch_set_x_warps(c3d_batch *b, int warps) {
     if (!b || (warps != 2 && warps != 4 && warps != 8)) { set_error("x warps per block must be 2, 4 or 8"); return C3D_EINVAL; }
-    CK(cudaStreamSynchronize(b->stream));
-    for (int p = 0; p < 2; ++p) {
-        if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
-        b->exec[p] = nullptr;
-        b->gdt[p].clear();
-    }
+    if (int rc = batch_recapture(b)) return rc;
     b->sched.xw = warps;
     return 0;
 }
