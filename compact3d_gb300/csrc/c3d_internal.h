@@ -302,7 +302,7 @@ int launch_pipe_selftest(c3d_channel *ch, double limit_ms);
 // one channel's step in order (batch_plan), and its StepArgs<R> for the step with DT dt
 // written as bytes to dst (batch_args, batch_args_size bytes).
 template <typename R> int xpass_bkern(const c3d_channel *ch, int which, int xw, std::vector<BKern> &out);
-// Lanes per row segment of the batch xA and xB for a channel of N1M x N3M (0: one row per warp).
+// Lanes per row segment of the x passes for a channel of N1M x N3M (0: one row per warp).
 int x_segment_lanes(int n1m, int n3m);
 template <typename R> int zpass_bkern(const c3d_channel *ch, int which, int seg, std::vector<BKern> &out);
 template <typename R> int spec_bkern(const c3d_channel *ch, int which, std::vector<BKern> &out);

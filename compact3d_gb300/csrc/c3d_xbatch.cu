@@ -87,7 +87,7 @@ static int xbk_seg(const c3d_channel *ch, int which, int xw, std::vector<BKern> 
     }
 }
 
-// The row segment of xA and xB for N1M (lanes W, chunk C = N1M/W), or 0 for a whole warp.
+// The row segment of the x passes for N1M (lanes W, chunk C = N1M/W), or 0 for a whole warp.
 int x_segment_lanes(int n1m, int n3m) {
     const int w = (n1m == 48 || n1m == 64 || n1m == 96) ? 8 : (n1m == 128) ? 16 : 32;
     return (w < 32 && n3m % (32 / w) == 0) ? w : 0;
