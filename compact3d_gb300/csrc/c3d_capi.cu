@@ -1745,7 +1745,7 @@ int c3d_autotune(c3d_channel *ch, int *sched) {
         knob(best, gp.knob) = bval;
     }
     // knob 15 by whole-step time: the per-kernel profile runs the pieces one after another,
-    // so the concurrent form is judged on five unprofiled steps (twice each, the minimum)
+    // so the concurrent form is chosen on five unprofiled steps (twice each, the minimum)
     if (best.xsplit || best.zsplit) {
         float bms[2] = {1e30f, 1e30f};
         for (int rep = 0; rep < 2; ++rep)

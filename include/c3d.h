@@ -409,7 +409,7 @@ int c3d_checkpoint_read(c3d_channel *ch, const char *path, int *ntime, double *t
  *   [15] the u, v and w pieces of the explicit x pass ([10] = 1), then those of the
  *       explicit z pass ([9] = 1), as three concurrent branches on three streams (1)
  *       or one after another (0); they write disjoint fields.  The per-kernel profile
- *       (c3d_profile) runs them one after another; c3d_autotune judges this knob by
+ *       (c3d_profile) runs them one after another; c3d_autotune sets this knob by
  *       the time of whole unprofiled steps
  * c3d_autotune  times the candidates on a scratch channel of the same grid holding a
  *               copy of this channel's state (so the channel needs its state), keeps
