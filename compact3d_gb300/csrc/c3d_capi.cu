@@ -1637,20 +1637,28 @@ void apply_tune(c3d_channel *ch, const Tune &t) {
     ch->fz = fz;
 }
 
+// Time of the kernels `names` over five profiled steps under schedule t, the smaller of
+// two such runs (a single run of a few milliseconds moves by a few percent between
+// candidates that differ by less).
 int time_schedule(c3d_channel *sc, const Tune &t, double dt, const std::vector<std::string> &names, double *cost) {
     apply_tune(sc, t);
     int rc = step_common(sc, dt, nullptr, nullptr, true);
     if (rc && rc != C3D_ENOTCONV) return rc;
-    c3d_profile(sc, 1);
-    for (int q = 0; q < 5 && !rc; ++q) rc = step_common(sc, dt, nullptr, nullptr, false);
-    if (rc) return rc;
-    CK(cudaStreamSynchronize(sc->stream));
-    double c = 0.0;
-    for (size_t q = 0; q < sc->prof_name.size(); ++q)
-        for (const std::string &n : names)   // a name covers its split pieces (zA -> zA_u, ...)
-            if (sc->prof_name[q] == n || sc->prof_name[q].rfind(n + "_", 0) == 0) c += sc->prof_ms[q];
-    c3d_profile(sc, 0);
-    *cost = c;
+    double best = 1e300;
+    for (int rep = 0; rep < 2; ++rep) {
+        rc = 0;
+        c3d_profile(sc, 1);
+        for (int q = 0; q < 5 && !rc; ++q) rc = step_common(sc, dt, nullptr, nullptr, false);
+        if (rc) { c3d_profile(sc, 0); return rc; }
+        CK(cudaStreamSynchronize(sc->stream));
+        double c = 0.0;
+        for (size_t q = 0; q < sc->prof_name.size(); ++q)
+            for (const std::string &n : names)   // a name covers its split pieces (zA -> zA_u, ...)
+                if (sc->prof_name[q] == n || sc->prof_name[q].rfind(n + "_", 0) == 0) c += sc->prof_ms[q];
+        c3d_profile(sc, 0);
+        best = std::min(best, c);
+    }
+    *cost = best;
     return 0;
 }
 }  // namespace
