@@ -32,6 +32,15 @@ def test_every_declared_symbol_is_exported(L):
     assert set(names) == set(lib.SIGNATURES), "Python signatures out of sync with c3d.h"
 
 
+def test_schedule_length_agrees():
+    """C3D_SCHEDULE_LEN in the header, the binding's constant and its knob names agree, so
+    that a schedule dictionary maps onto the ints the library reads."""
+    src = open(os.path.join(ROOT, "include", "c3d.h")).read()
+    n = int(re.search(r"#define\s+C3D_SCHEDULE_LEN\s+(\d+)", src).group(1))
+    assert n == lib.C3D_SCHEDULE_LEN == len(lib.Channel.SCHEDULE_KEYS)
+    assert len(set(lib.Channel.SCHEDULE_KEYS)) == n
+
+
 def test_error_strings(L):
     for code in (0, -1, -2, -3, -4, -5, -6, -7, -8, -99):
         assert L.c3d_error_string(code)
