@@ -2,9 +2,10 @@
 
 The kernels factor the constant-coefficient cyclic operator tridiag(a, b, a) as
 (-a/r)(1 - rS)(1 - rS^-1) and evaluate two first-order recurrences.  These numpy models
-follow the device code step by step (lane chunks with affine warp scans along x; segments
-with a warm-up of M points along z) and are compared with the oracle's bordered-LU solver
-(CTDMA11, compact3d.f:8952-8998).
+follow the device code step by step (lane chunks with affine warp scans along x, the
+general form and the constant-multiplier form of row segments of 8, 16 or 32 lanes;
+segments with a warm-up of M points along z) and are compared with the oracle's
+bordered-LU solver (CTDMA11, compact3d.f:8952-8998).
 """
 import math
 
@@ -78,6 +79,60 @@ def xsolve_model(d, a, b):
     return out
 
 
+def xsolve_full_model(d, a, b, W):
+    """A row held by a segment of W lanes with every lane holding a chunk of C = n/W points
+    (the device's xsolve_full): the scans combine with the constant multipliers
+    r^(C 2^b), lane l closes with r^(C l) (forward) and r^(C (W-1-l)) (backward), formed
+    from the bits of l, and the cyclic closure divides by 1 - r^(C W) only when that
+    power is not below half an ulp."""
+    n = len(d)
+    assert n % W == 0
+    C = n // W
+    lw = W.bit_length() - 1
+    r, s, _ = coeffs(a, b)
+    pw = [1.0]
+    for _ in range(C):
+        pw[0] *= r
+    for q in range(lw):
+        pw.append(pw[q] * pw[q])
+    ml = [math.prod(pw[q] for q in range(lw) if (l >> q) & 1) for l in range(W)]
+    mr = [math.prod(pw[q] for q in range(lw) if ((W - 1 - l) >> q) & 1) for l in range(W)]
+    exact1 = abs(pw[lw]) < 2.0 ** -54
+    x = [list(d[l * C:(l + 1) * C]) for l in range(W)]
+    e = []
+    for l in range(W):
+        y = 0.0
+        for t in range(C):
+            y = x[l][t] + r * y
+        e.append(y)
+    for q in range(lw):
+        off = 1 << q
+        e = [e[l] + pw[q] * e[l - off] if l >= off else e[l] for l in range(W)]
+    y0 = e[W - 1] if exact1 else e[W - 1] / (1.0 - pw[lw])
+    for l in range(W):
+        y = y0 if l == 0 else e[l - 1] + ml[l] * y0
+        for t in range(C):
+            y = x[l][t] + r * y
+            x[l][t] = y
+    e = []
+    for l in range(W):
+        z = 0.0
+        for t in reversed(range(C)):
+            z = x[l][t] + r * z
+        e.append(z)
+    for q in range(lw):
+        off = 1 << q
+        e = [e[l] + pw[q] * e[l + off] if l + off < W else e[l] for l in range(W)]
+    z0 = e[0] if exact1 else e[0] / (1.0 - pw[lw])
+    out = np.zeros(n)
+    for l in range(W):
+        z = z0 if l == W - 1 else e[l + 1] + mr[l] * z0
+        for t in reversed(range(C)):
+            z = x[l][t] + r * z
+            out[l * C + t] = s * z
+    return out
+
+
 def zseg_model(d, a, b, L=16):
     n = len(d)
     r, s, M = coeffs(a, b)
@@ -108,6 +163,17 @@ def test_warp_scan_solver(oracle_mod, n, ab):
     d = np.random.default_rng(n).normal(size=n)
     ref = oracle_mod.ctdma11(d, ab[0], ab[1], ab[0])
     assert np.abs(xsolve_model(d, *ab) - ref).max() < 4e-15 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("n,W", [(16, 8), (48, 8), (64, 8), (96, 8), (128, 16), (64, 32), (384, 32)])
+@pytest.mark.parametrize("ab", [(1.0, 6.0), (1.0, 10.0), (1.0, 22.0), (0.9985, 10.003)])
+def test_constant_multiplier_segment_solver(oracle_mod, n, ab, W):
+    """The row-segment line solve with constant scan multipliers, for the row lengths and
+    segment widths the kernels use (and a 16-point row, where r^(C W) is not negligible
+    and the closure divides)."""
+    d = np.random.default_rng(n + W).normal(size=n)
+    ref = oracle_mod.ctdma11(d, ab[0], ab[1], ab[0])
+    assert np.abs(xsolve_full_model(d, *ab, W) - ref).max() < 4e-15 * np.abs(ref).max()
 
 
 @pytest.mark.parametrize("n", [16, 48, 64, 384])
