@@ -99,7 +99,7 @@ __device__ __forceinline__ void b_fftz4(const StepArgs<R> &a, const Blk blk) {
         __syncwarp();
         // x[k] is frequency k + N1 * bitrev5(lane); it goes to tile row lane + 32 k, so that
         // the 16 lanes of a half-warp write 16 distinct bank pairs (row k + N1 bitrev5(lane)
-        // would put them on 4), and the copy-out below reads each frequency's row.
+        // puts them on 2 when N1 = 12), and the copy-out below reads each frequency's row.
 #pragma unroll
         for (int k = 0; k < N1; ++k) T[(lane + 32 * k) * pitch + c] = x[k];
     }
